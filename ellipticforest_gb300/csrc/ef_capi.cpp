@@ -1,0 +1,383 @@
+// C ABI of the GB300 HPS solver (include/ellipticforest_gb300.h).
+//
+// Thin layer over efgb::Mesh and efgb::Hps: argument checks, exception-to-status conversion and
+// host<->device copies.  No computation happens on the host here; every numerical step runs in
+// the CUDA kernels of this library.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ellipticforest_gb300.h"
+#include "ef_hps.hpp"
+#include "ef_kernels.cuh"
+#include "ef_mesh.hpp"
+
+struct ef_mesh {
+    efgb::Mesh mesh;
+};
+
+struct ef_hps {
+    std::unique_ptr<efgb::Hps> hps;
+    bool cache_operators = false;
+    bool homogeneous_rhs = false;
+    bool upward_done = false;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc& e) {
+        return fail(EF_ERR_NOMEM, std::string("allocation failed: ") + e.what());
+    } catch (const std::invalid_argument& e) {
+        return fail(EF_ERR_INVALID, e.what());
+    } catch (const std::runtime_error& e) {
+        const std::string m = e.what();
+        if (m.find("out of memory") != std::string::npos) return fail(EF_ERR_NOMEM, m);
+        return fail(EF_ERR_CUDA, m);
+    } catch (...) {
+        return fail(EF_ERR_INVALID, "unknown exception");
+    }
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return EF_OK;
+    if (e == cudaErrorMemoryAllocation)
+        return fail(EF_ERR_NOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+    return fail(EF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool finite_box(double a, double b) { return a == a && b == b && b > a; }
+
+// One-patch run of a leaf kernel (FiniteVolumeSolver entry points).
+int run_single_patch(int solver_type, int n, double xl, double xu, double yl, double yu,
+                     double lambda, int mode, const double* g_host, const double* f_host,
+                     double* out_host, size_t out_count) {
+    if (solver_type != EF_SOLVER_FISHPACK90)
+        return fail(EF_ERR_UNSUPPORTED,
+                    "single-patch entry points implement the FISHPACK90 (constant coefficient) solver");
+    if (n < 2 || n > 64) return fail(EF_ERR_INVALID, "n must be in [2, 64]");
+    if (!finite_box(xl, xu) || !finite_box(yl, yu)) return fail(EF_ERR_INVALID, "bad patch box");
+    if (!out_host) return fail(EF_ERR_INVALID, "null output");
+    const int nn = n * n;
+    const double dx = (xu - xl) / n, dy = (yu - yl) / n;
+    std::vector<double> V(nn), Dinv(nn);
+    efgb::leaf_tables(n, dx, dy, lambda, V.data(), Dinv.data());
+    const int nitems = (mode == efgb::LEAF_DTN_COLUMN) ? 4 * n : 1;
+    const size_t bytes = sizeof(double) * (2 * nn + 4 * n + nn + out_count) + sizeof(efgb::LeafType) +
+                         sizeof(efgb::LeafItem) * nitems + 1024;
+    char* buf = nullptr;
+    int st = cuda_status(cudaMalloc(&buf, bytes), "cudaMalloc");
+    if (st) return st;
+    double* dV = reinterpret_cast<double*>(buf);
+    double* dD = dV + nn;
+    double* dg = dD + nn;
+    double* df = dg + 4 * n;
+    double* dout = df + nn;
+    auto* dty = reinterpret_cast<efgb::LeafType*>(
+        (reinterpret_cast<uintptr_t>(dout + out_count) + 255) & ~uintptr_t(255));
+    auto* ditems = reinterpret_cast<efgb::LeafItem*>(
+        (reinterpret_cast<uintptr_t>(dty + 1) + 255) & ~uintptr_t(255));
+    if (reinterpret_cast<char*>(ditems + nitems) > buf + bytes + 1024) {
+        cudaFree(buf);
+        return fail(EF_ERR_INVALID, "internal layout error");
+    }
+    efgb::LeafType ty{n, dx, dy, dV, dD};
+    std::vector<efgb::LeafItem> items(nitems);
+    for (int k = 0; k < nitems; ++k)
+        items[k] = efgb::LeafItem{0, k, f_host ? df : nullptr, g_host ? dg : nullptr, dout};
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemcpy(dV, V.data(), nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dD, Dinv.data(), nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && g_host) e = cudaMemcpy(dg, g_host, 4 * n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && f_host) e = cudaMemcpy(df, f_host, nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dty, &ty, sizeof(ty), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(ditems, items.data(), nitems * sizeof(efgb::LeafItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        efgb::leaf_eigen(0, mode, dty, ditems, nitems, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out_host, dout, out_count * 8, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    return cuda_status(e, "single patch");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ef_last_error(void) { return g_last_error.c_str(); }
+
+int ef_version(void) { return 1; }
+
+int ef_mesh_create_refined(double xl, double xu, double yl, double yu, int nx, int ny, int min_level,
+                           int max_level, ef_refine_fn fn, void* ctx, ef_mesh** out) {
+    if (!out || !fn) return fail(EF_ERR_INVALID, "null argument");
+    if (!finite_box(xl, xu) || !finite_box(yl, yu)) return fail(EF_ERR_INVALID, "bad domain box");
+    return guarded([&] {
+        auto m = std::make_unique<ef_mesh>();
+        m->mesh = efgb::Mesh::refine_by_function(
+            xl, xu, yl, yu, nx, ny, min_level, max_level,
+            [fn, ctx](double x, double y) { return fn(x, y, ctx) != 0; });
+        *out = m.release();
+        return EF_OK;
+    });
+}
+
+int ef_mesh_create_uniform(double xl, double xu, double yl, double yu, int nx, int ny, int level,
+                           ef_mesh** out) {
+    if (!out) return fail(EF_ERR_INVALID, "null argument");
+    if (!finite_box(xl, xu) || !finite_box(yl, yu)) return fail(EF_ERR_INVALID, "bad domain box");
+    if (nx <= 0 || ny <= 0) return fail(EF_ERR_INVALID, "bad patch size");
+    return guarded([&] {
+        auto m = std::make_unique<ef_mesh>();
+        m->mesh = efgb::Mesh::uniform(xl, xu, yl, yu, nx, ny, level);
+        *out = m.release();
+        return EF_OK;
+    });
+}
+
+int ef_mesh_num_leaves(const ef_mesh* mesh, int* out) {
+    if (!mesh || !out) return fail(EF_ERR_INVALID, "null argument");
+    *out = int(mesh->mesh.leaves.size());
+    return EF_OK;
+}
+
+int ef_mesh_num_nodes(const ef_mesh* mesh, int* out) {
+    if (!mesh || !out) return fail(EF_ERR_INVALID, "null argument");
+    *out = int(mesh->mesh.nodes.size());
+    return EF_OK;
+}
+
+int ef_mesh_leaf(const ef_mesh* mesh, int k, int* level, long long* ix, long long* iy, double box[4]) {
+    if (!mesh) return fail(EF_ERR_INVALID, "null mesh");
+    if (k < 0 || k >= int(mesh->mesh.leaves.size())) return fail(EF_ERR_INVALID, "leaf index out of range");
+    const efgb::MeshNode& nd = mesh->mesh.nodes[mesh->mesh.leaves[k]];
+    if (level) *level = nd.level;
+    if (ix) *ix = nd.ix;
+    if (iy) *iy = nd.iy;
+    if (box) { box[0] = nd.xl; box[1] = nd.xu; box[2] = nd.yl; box[3] = nd.yu; }
+    return EF_OK;
+}
+
+int ef_mesh_destroy(ef_mesh* mesh) {
+    delete mesh;
+    return EF_OK;
+}
+
+int ef_hps_create(const ef_mesh* mesh, int solver_type, double lambda, ef_hps** out) {
+    if (!mesh || !out) return fail(EF_ERR_INVALID, "null argument");
+    if (solver_type != EF_SOLVER_FISHPACK90)
+        return fail(EF_ERR_UNSUPPORTED, "solver type not available: use EF_SOLVER_FISHPACK90");
+    return guarded([&] {
+        auto h = std::make_unique<ef_hps>();
+        h->hps = std::make_unique<efgb::Hps>(mesh->mesh, solver_type, lambda, false);
+        *out = h.release();
+        return EF_OK;
+    });
+}
+
+int ef_hps_set_option(ef_hps* h, const char* key, int value) {
+    if (!h || !key) return fail(EF_ERR_INVALID, "null argument");
+    const std::string k(key);
+    if (k == "cache-operators") {
+        h->cache_operators = value != 0;
+    } else if (k == "homogeneous-rhs") {
+        h->homogeneous_rhs = value != 0;
+        h->hps->set_homogeneous_rhs(value != 0);
+    } else {
+        return fail(EF_ERR_INVALID, "unknown option key: " + k);
+    }
+    return EF_OK;
+}
+
+int ef_hps_set_stream(ef_hps* h, void* stream) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    h->hps->set_stream(reinterpret_cast<cudaStream_t>(stream));
+    return EF_OK;
+}
+
+int ef_hps_info(const ef_hps* h, int* nleaves, int* n, int* M, long long* bytes) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (nleaves) *nleaves = h->hps->num_leaves();
+    if (n) *n = h->hps->leaf_n();
+    if (M) *M = h->hps->root_M();
+    if (bytes) *bytes = (long long)h->hps->device_bytes();
+    return EF_OK;
+}
+
+int ef_hps_setup(ef_hps* h) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    return EF_OK;
+}
+
+int ef_hps_build(ef_hps* h) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    return guarded([&] {
+        h->hps->build();
+        if (h->hps->singular_count() > 0)
+            return fail(EF_ERR_SINGULAR, std::to_string(h->hps->singular_count()) +
+                                             " interface matrices had a zero pivot (dgesv INFO != 0)");
+        return EF_OK;
+    });
+}
+
+int ef_hps_upwards(ef_hps* h, const double* f_host) {
+    if (!h || !f_host) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "upwards stage before build stage");
+    return guarded([&] {
+        efgb::Hps& H = *h->hps;
+        const size_t cnt = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();
+        int st = cuda_status(cudaMemcpyAsync(H.leaf_f(), f_host, cnt * 8, cudaMemcpyHostToDevice,
+                                             H.stream()), "copy f");
+        if (st) return st;
+        H.upwards();
+        st = cuda_status(cudaGetLastError(), "upwards launch");
+        if (st) return st;
+        st = cuda_status(cudaStreamSynchronize(H.stream()), "upwards");
+        if (st) return st;
+        h->upward_done = true;
+        return EF_OK;
+    });
+}
+
+int ef_hps_solve(ef_hps* h, const double* a, const double* b, const double* r) {
+    if (!h || !a || !b || !r) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "solve stage before build stage");
+    return guarded([&] {
+        efgb::Hps& H = *h->hps;
+        const size_t m = 4 * size_t(H.root_M());
+        bool general = false;
+        for (size_t i = 0; i < m; ++i)
+            if (b[i] != 0.0) { general = true; break; }
+        cudaStream_t s = H.stream();
+        int st = cuda_status(cudaMemcpyAsync(H.bc_a(), a, m * 8, cudaMemcpyHostToDevice, s), "copy a");
+        if (!st) st = cuda_status(cudaMemcpyAsync(H.bc_b(), b, m * 8, cudaMemcpyHostToDevice, s), "copy b");
+        if (!st) st = cuda_status(cudaMemcpyAsync(H.bc_r(), r, m * 8, cudaMemcpyHostToDevice, s), "copy r");
+        if (st) return st;
+        H.set_bc_general(general);
+        H.root_from_bc();
+        H.downwards();
+        st = cuda_status(cudaGetLastError(), "solve launch");
+        if (st) return st;
+        return cuda_status(cudaStreamSynchronize(s), "solve");
+    });
+}
+
+int ef_hps_solve_root_dirichlet(ef_hps* h, const double* g) {
+    if (!h || !g) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "solve stage before build stage");
+    return guarded([&] {
+        efgb::Hps& H = *h->hps;
+        const size_t m = 4 * size_t(H.root_M());
+        int st = cuda_status(cudaMemcpyAsync(H.root_g(), g, m * 8, cudaMemcpyHostToDevice, H.stream()),
+                             "copy root g");
+        if (st) return st;
+        H.downwards();
+        st = cuda_status(cudaGetLastError(), "solve launch");
+        if (st) return st;
+        return cuda_status(cudaStreamSynchronize(H.stream()), "solve");
+    });
+}
+
+int ef_hps_get_leaf_u(ef_hps* h, double* u) {
+    if (!h || !u) return fail(EF_ERR_INVALID, "null argument");
+    efgb::Hps& H = *h->hps;
+    const size_t cnt = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();
+    int st = cuda_status(cudaMemcpyAsync(u, H.leaf_u(), cnt * 8, cudaMemcpyDeviceToHost, H.stream()), "copy u");
+    if (st) return st;
+    return cuda_status(cudaStreamSynchronize(H.stream()), "copy u");
+}
+
+int ef_hps_get_root_T(ef_hps* h, double* T) {
+    if (!h || !T) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "root T before build stage");
+    efgb::Hps& H = *h->hps;
+    const size_t m = 4 * size_t(H.root_M());
+    int st = cuda_status(cudaMemcpyAsync(T, H.root_T(), m * m * 8, cudaMemcpyDeviceToHost, H.stream()), "copy T");
+    if (st) return st;
+    return cuda_status(cudaStreamSynchronize(H.stream()), "copy T");
+}
+
+int ef_hps_get_root_h(ef_hps* h, double* out) {
+    if (!h || !out) return fail(EF_ERR_INVALID, "null argument");
+    efgb::Hps& H = *h->hps;
+    const size_t m = 4 * size_t(H.root_M());
+    int st = cuda_status(cudaMemcpyAsync(out, H.root_h(), m * 8, cudaMemcpyDeviceToHost, H.stream()), "copy h");
+    if (st) return st;
+    return cuda_status(cudaStreamSynchronize(H.stream()), "copy h");
+}
+
+int ef_hps_destroy(ef_hps* h) {
+    delete h;
+    return EF_OK;
+}
+
+int ef_hps_device_buffers(ef_hps* h, double** f, double** u, double** a, double** b, double** r) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    efgb::Hps& H = *h->hps;
+    if (f) *f = H.leaf_f();
+    if (u) *u = H.leaf_u();
+    if (a) *a = H.bc_a();
+    if (b) *b = H.bc_b();
+    if (r) *r = H.bc_r();
+    return EF_OK;
+}
+
+int ef_hps_solve_device_async(ef_hps* h, int b_is_zero) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "solve before build stage");
+    return guarded([&] {
+        h->hps->set_bc_general(b_is_zero == 0);
+        h->hps->solve_async();
+        return cuda_status(cudaGetLastError(), "solve launch");
+    });
+}
+
+int ef_hps_synchronize(ef_hps* h) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    return cuda_status(cudaStreamSynchronize(h->hps->stream()), "synchronize");
+}
+
+int ef_fv_build_d2n(int solver_type, int n, double xl, double xu, double yl, double yu, double lambda,
+                    double* T) {
+    return guarded([&] {
+        return run_single_patch(solver_type, n, xl, xu, yl, yu, lambda, efgb::LEAF_DTN_COLUMN, nullptr,
+                                nullptr, T, size_t(16) * n * n);
+    });
+}
+
+int ef_fv_solve(int solver_type, int n, double xl, double xu, double yl, double yu, double lambda,
+                const double* g, const double* f, double* u) {
+    if (!g) return fail(EF_ERR_INVALID, "null Dirichlet data");
+    return guarded([&] {
+        return run_single_patch(solver_type, n, xl, xu, yl, yu, lambda, efgb::LEAF_SOLVE, g, f, u,
+                                size_t(n) * n);
+    });
+}
+
+int ef_fv_map_d2n(int solver_type, int n, double xl, double xu, double yl, double yu, double lambda,
+                  const double* g, const double* f, double* h) {
+    if (!g) return fail(EF_ERR_INVALID, "null Dirichlet data");
+    return guarded([&] {
+        return run_single_patch(solver_type, n, xl, xu, yl, yu, lambda, efgb::LEAF_MAPD2N, g, f, h,
+                                size_t(4) * n);
+    });
+}
+
+}  // extern "C"

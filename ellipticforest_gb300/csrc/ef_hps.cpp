@@ -1,0 +1,516 @@
+// GB300 HPS solver: plan, device arena and the level-by-level stage drivers.
+//
+// Stage order follows src/HPSAlgorithm.hpp: buildStage (:120-161, leaf DtN + post-order merges),
+// upwardsStage (:178-272, leaf particular Neumann data + upwards4to1), solveStage (:343-445, root
+// Dirichlet data, pre-order split1to4, leafSolve).  Each tree level is processed as a whole; the
+// merges of one level are independent, so the result equals the reference's post-order traversal.
+#include "ef_hps.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+
+namespace efgb {
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
+
+int ilog2_exact(int v) {
+    int k = 0;
+    while ((1 << k) < v) ++k;
+    if ((1 << k) != v) throw std::invalid_argument("patch size ratio is not a power of two");
+    return k;
+}
+
+// Carves the device arena.  Run once dry to measure, once to assign.
+struct Carver {
+    char* base = nullptr;
+    size_t off = 0;
+    template <class T>
+    T* get(size_t count) {
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += align_up(std::max<size_t>(count, 1) * sizeof(T));
+        return p;
+    }
+};
+
+}  // namespace
+
+void leaf_tables(int n, double dx, double dy, double lambda, double* V, double* Dinv) {
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < n; ++k) {
+            const double c = (k == n - 1) ? std::sqrt(1.0 / n) : std::sqrt(2.0 / n);
+            V[i * n + k] = c * std::sin(M_PI * (k + 1) * (i + 0.5) / n);
+        }
+    for (int k = 0; k < n; ++k)
+        for (int l = 0; l < n; ++l) {
+            const double sx = std::sin(M_PI * (k + 1) / (2.0 * n));
+            const double sy = std::sin(M_PI * (l + 1) / (2.0 * n));
+            const double mux = -(4.0 / (dx * dx)) * sx * sx;
+            const double muy = -(4.0 / (dy * dy)) * sy * sy;
+            Dinv[k * n + l] = 1.0 / (mux + muy + lambda);
+        }
+}
+
+void Hps::check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+
+Hps::Hps(const Mesh& mesh, int solver_type, double lambda, bool cache_operators)
+    : mesh_(mesh), solver_type_(solver_type), lambda_(lambda), cache_ops_(cache_operators) {
+    if (mesh.nx != mesh.ny) throw std::invalid_argument("patches must be square (nx == ny)");
+    if (mesh.nx < 2 || mesh.nx > 64) throw std::invalid_argument("leaf patch size must be in [2, 64]");
+    if (solver_type != SOLVER_FISHPACK90 && solver_type != SOLVER_FIVE_POINT)
+        throw std::invalid_argument("unknown solver type");
+    n_ = mesh.nx;
+    plan();
+    allocate();
+    upload_tables();
+}
+
+Hps::~Hps() {
+    if (arena_) cudaFree(arena_);
+    if (d_rootA_) cudaFree(d_rootA_);
+}
+
+void Hps::plan() {
+    const int N = int(mesh_.nodes.size());
+    nodes_.assign(N, NodeDev());
+    for (int id = N - 1; id >= 0; --id) {  // reverse pre-order: children first
+        const MeshNode& mn = mesh_.nodes[id];
+        NodeDev& nd = nodes_[id];
+        if (mn.leaf()) {
+            nd.nx = n_;
+        } else {
+            int mn_side = 1 << 30;
+            for (int c = 0; c < 4; ++c) mn_side = std::min(mn_side, nodes_[mn.child[c]].nx);
+            for (int c = 0; c < 4; ++c) {
+                NodeDev& ch = nodes_[mn.child[c]];
+                ch.ncoarsen = ilog2_exact(ch.nx / mn_side);
+                if (ch.ncoarsen > 0 && (ch.nx >> (ch.ncoarsen - 1)) < 8)
+                    throw std::invalid_argument("coarsening needs patches of at least 4 cells");
+            }
+            nd.s = mn_side;
+            nd.nx = 2 * mn_side;  // mergePatch_ (HPSAlgorithm.hpp:1004-1009)
+        }
+        nd.size = nd.nx;
+    }
+    for (int id = 0; id < N; ++id) nodes_[id].size = nodes_[id].nx >> nodes_[id].ncoarsen;
+
+    // leaf types keyed by the exact grid spacing (FISHPACK90: lambda is global)
+    std::map<std::pair<uint64_t, uint64_t>, int> key2type;
+    for (int l : mesh_.leaves) {
+        const MeshNode& mn = mesh_.nodes[l];
+        const double dx = (mn.xu - mn.xl) / n_, dy = (mn.yu - mn.yl) / n_;
+        uint64_t kx, ky;
+        std::memcpy(&kx, &dx, 8);
+        std::memcpy(&ky, &dy, 8);
+        auto it = key2type.find({kx, ky});
+        int t;
+        if (it == key2type.end()) {
+            t = int(types_.size());
+            types_.push_back(LeafTypeHost{n_, dx, dy, nullptr});
+            key2type[{kx, ky}] = t;
+        } else {
+            t = it->second;
+        }
+        nodes_[l].leaf_type = t;
+    }
+    (void)cache_ops_;
+
+    // groups per (level, s), deepest level first
+    std::map<std::pair<int, int>, int> gidx;
+    for (int id = 0; id < N; ++id) {
+        const MeshNode& mn = mesh_.nodes[id];
+        if (mn.leaf()) continue;
+        auto key = std::make_pair(-mn.level, nodes_[id].s);
+        if (!gidx.count(key)) gidx[key] = 0;
+    }
+    int gi = 0;
+    for (auto& kv : gidx) kv.second = gi++;
+    groups_.assign(gidx.size(), Group());
+    for (auto& kv : gidx) {
+        groups_[kv.second].level = -kv.first.first;
+        groups_[kv.second].s = kv.first.second;
+    }
+    for (int id = 0; id < N; ++id) {
+        const MeshNode& mn = mesh_.nodes[id];
+        if (mn.leaf()) continue;
+        groups_[gidx[{-mn.level, nodes_[id].s}]].nodes.push_back(id);
+    }
+}
+
+void Hps::allocate() {
+    const int N = int(nodes_.size());
+    const int L = int(mesh_.leaves.size());
+    const int nn = n_ * n_;
+    const int M = nodes_[0].nx;
+
+    // resample steps: (level, step, nf) -> list of node ids
+    std::map<std::tuple<int, int, int>, std::vector<int>> tmap, gmap;
+    for (int id = 0; id < N; ++id) {
+        const NodeDev& nd = nodes_[id];
+        for (int t = 0; t < nd.ncoarsen; ++t) {
+            tmap[{mesh_.nodes[id].level, t, nd.nx >> t}].push_back(id);
+            const int cf = nd.ncoarsen - (t + 1);
+            gmap[{mesh_.nodes[id].level, t, nd.nx >> cf}].push_back(id);
+        }
+    }
+
+    auto layout = [&](Carver& cv) {
+        for (auto& ty : types_) ty.T = cv.get<double>(size_t(16) * nn);
+        d_V_ = cv.get<double>(size_t(types_.size()) * nn);
+        d_Dinv_ = cv.get<double>(size_t(types_.size()) * nn);
+        for (int id = 0; id < N; ++id) {
+            NodeDev& nd = nodes_[id];
+            const MeshNode& mn = mesh_.nodes[id];
+            nd.Tsteps.clear(); nd.hsteps.clear(); nd.gsteps.clear();
+            if (mn.leaf()) {
+                nd.T = types_[nd.leaf_type].T;
+                nd.h = cv.get<double>(4 * n_);
+                nd.g = cv.get<double>(4 * n_);
+            } else {
+                const size_t s = nd.s;
+                nd.T = cv.get<double>(64 * s * s);
+                nd.X = cv.get<double>(16 * s * s);
+                nd.RHS = cv.get<double>(48 * s * s);
+                nd.H = cv.get<double>(32 * s * s);
+                nd.piv = cv.get<int>(4 * s);
+                nd.perm = cv.get<int>(4 * s);
+                nd.h = cv.get<double>(8 * s);
+                nd.w = cv.get<double>(4 * s);
+                nd.g = cv.get<double>(4 * size_t(nd.size));
+            }
+            for (int t = 0; t < nd.ncoarsen; ++t) {
+                const size_t nc = size_t(nd.nx >> t) / 2;
+                nd.Tsteps.push_back(cv.get<double>(16 * nc * nc));
+                nd.hsteps.push_back(cv.get<double>(4 * nc));
+                const int cf = nd.ncoarsen - (t + 1);
+                nd.gsteps.push_back(cv.get<double>(4 * size_t(nd.nx >> cf)));
+            }
+            nd.Tc = nd.ncoarsen ? nd.Tsteps.back() : nd.T;
+            nd.hc = nd.ncoarsen ? nd.hsteps.back() : nd.h;
+            nd.gf = nd.ncoarsen ? nd.gsteps.back() : nd.g;
+        }
+        d_f_ = cv.get<double>(size_t(L) * nn);
+        d_u_ = cv.get<double>(size_t(L) * nn);
+        d_bca_ = cv.get<double>(4 * size_t(M));
+        d_bcb_ = cv.get<double>(4 * size_t(M));
+        d_bcr_ = cv.get<double>(4 * size_t(M));
+        d_types_ = cv.get<LeafType>(types_.size());
+        nitems_dtn_ = int(types_.size()) * 4 * n_;
+        d_items_dtn_ = cv.get<LeafItem>(nitems_dtn_);
+        d_items_neu_ = cv.get<LeafItem>(L);
+        d_items_solve_ = cv.get<LeafItem>(L);
+        for (auto& g : groups_) {
+            const int cnt = int(g.nodes.size());
+            const int per4 = (4 * g.s + 31) / 32, per8 = (8 * g.s + 31) / 32;
+            g.nwork4 = cnt * per4;
+            g.nwork8 = cnt * per8;
+            g.d_items = cv.get<MergeItem>(cnt);
+            g.d_work4 = cv.get<RowWork>(g.nwork4);
+            g.d_work8 = cv.get<RowWork>(g.nwork8);
+            g.d_X = cv.get<double*>(cnt);
+            g.d_RHS = cv.get<double*>(cnt);
+            g.d_H = cv.get<double*>(cnt);
+            g.d_T = cv.get<double*>(cnt);
+            g.d_piv = cv.get<int*>(cnt);
+            g.d_perm = cv.get<int*>(cnt);
+            g.d_info = cv.get<int>(cnt);
+        }
+        tsteps_.clear(); hsteps_.clear(); gsteps_.clear();
+        for (auto& kv : tmap) {
+            ResampleStep r;
+            r.level = std::get<0>(kv.first);
+            r.nf = std::get<2>(kv.first);
+            r.count = int(kv.second.size());
+            r.d_in = cv.get<const double*>(r.count);
+            r.d_out = cv.get<double*>(r.count);
+            tsteps_.push_back(r);
+            ResampleStep h = r;
+            h.d_in = cv.get<const double*>(r.count);
+            h.d_out = cv.get<double*>(r.count);
+            hsteps_.push_back(h);
+        }
+        for (auto& kv : gmap) {
+            ResampleStep r;
+            r.level = std::get<0>(kv.first);
+            r.nf = std::get<2>(kv.first);
+            r.count = int(kv.second.size());
+            r.d_in = cv.get<const double*>(r.count);
+            r.d_out = cv.get<double*>(r.count);
+            gsteps_.push_back(r);
+        }
+    };
+    Carver dry;
+    layout(dry);
+    arena_bytes_ = dry.off;
+    check(cudaMalloc(&arena_, arena_bytes_), "cudaMalloc(arena)");
+    Carver real;
+    real.base = arena_;
+    layout(real);
+
+    // remember which nodes each resample step covers (same iteration order as the layout)
+    step_nodes_t_.clear();
+    step_nodes_g_.clear();
+    for (auto& kv : tmap) step_nodes_t_.push_back(kv.second);
+    for (auto& kv : gmap) step_nodes_g_.push_back(kv.second);
+    step_index_t_.clear();
+    step_index_g_.clear();
+    for (auto& kv : tmap) step_index_t_.push_back(std::get<1>(kv.first));
+    for (auto& kv : gmap) step_index_g_.push_back(std::get<1>(kv.first));
+}
+
+void Hps::upload_tables() {
+    const int L = int(mesh_.leaves.size());
+    const int nn = n_ * n_;
+    // zero the whole arena once (h of the root must read as 0 before any upward pass)
+    check(cudaMemsetAsync(arena_, 0, arena_bytes_, st_), "memset(arena)");
+
+    // leaf types: sine basis and inverse eigenvalue table
+    std::vector<LeafType> hty(types_.size());
+    std::vector<double> V(nn), Dinv(nn);
+    for (size_t t = 0; t < types_.size(); ++t) {
+        leaf_tables(n_, types_[t].dx, types_[t].dy, lambda_, V.data(), Dinv.data());
+        check(cudaMemcpy(d_V_ + t * nn, V.data(), nn * 8, cudaMemcpyHostToDevice), "upload V");
+        check(cudaMemcpy(d_Dinv_ + t * nn, Dinv.data(), nn * 8, cudaMemcpyHostToDevice), "upload Dinv");
+        hty[t] = LeafType{n_, types_[t].dx, types_[t].dy, d_V_ + t * nn, d_Dinv_ + t * nn};
+    }
+    check(cudaMemcpy(d_types_, hty.data(), hty.size() * sizeof(LeafType), cudaMemcpyHostToDevice),
+          "upload types");
+
+    std::vector<LeafItem> items;
+    for (size_t t = 0; t < types_.size(); ++t)
+        for (int u = 0; u < 4 * n_; ++u) items.push_back(LeafItem{int(t), u, nullptr, nullptr, types_[t].T});
+    check(cudaMemcpy(d_items_dtn_, items.data(), items.size() * sizeof(LeafItem), cudaMemcpyHostToDevice),
+          "upload dtn items");
+    items.clear();
+    for (int k = 0; k < L; ++k) {
+        const NodeDev& nd = nodes_[mesh_.leaves[k]];
+        items.push_back(LeafItem{nd.leaf_type, 0, d_f_ + size_t(k) * nn, nullptr, nd.h});
+    }
+    check(cudaMemcpy(d_items_neu_, items.data(), items.size() * sizeof(LeafItem), cudaMemcpyHostToDevice),
+          "upload neumann items");
+    items.clear();
+    for (int k = 0; k < L; ++k) {
+        const NodeDev& nd = nodes_[mesh_.leaves[k]];
+        items.push_back(LeafItem{nd.leaf_type, 0, d_f_ + size_t(k) * nn, nd.g, d_u_ + size_t(k) * nn});
+    }
+    check(cudaMemcpy(d_items_solve_, items.data(), items.size() * sizeof(LeafItem), cudaMemcpyHostToDevice),
+          "upload solve items");
+
+    for (auto& g : groups_) {
+        const int cnt = int(g.nodes.size());
+        std::vector<MergeItem> mi(cnt);
+        std::vector<RowWork> w4, w8;
+        std::vector<double*> X(cnt), R(cnt), H(cnt), T(cnt);
+        std::vector<int*> P(cnt), Q(cnt);
+        for (int i = 0; i < cnt; ++i) {
+            const int id = g.nodes[i];
+            const NodeDev& nd = nodes_[id];
+            const MeshNode& mn = mesh_.nodes[id];
+            MergeItem& m = mi[i];
+            for (int c = 0; c < 4; ++c) {
+                const NodeDev& ch = nodes_[mn.child[c]];
+                m.Tc[c] = ch.Tc;
+                m.hc[c] = ch.hc;
+                m.gc[c] = ch.g;
+            }
+            m.X = nd.X; m.piv = nd.piv; m.perm = nd.perm; m.RHS = nd.RHS; m.H = nd.H; m.T = nd.T;
+            m.h = nd.h; m.w = nd.w; m.gf = nd.gf;
+            X[i] = nd.X; R[i] = nd.RHS; H[i] = nd.H; T[i] = nd.T; P[i] = nd.piv; Q[i] = nd.perm;
+            for (int r = 0; r < 4 * g.s; r += 32) w4.push_back(RowWork{i, r});
+            for (int r = 0; r < 8 * g.s; r += 32) w8.push_back(RowWork{i, r});
+        }
+        check(cudaMemcpy(g.d_items, mi.data(), cnt * sizeof(MergeItem), cudaMemcpyHostToDevice), "items");
+        check(cudaMemcpy(g.d_work4, w4.data(), w4.size() * sizeof(RowWork), cudaMemcpyHostToDevice), "w4");
+        check(cudaMemcpy(g.d_work8, w8.data(), w8.size() * sizeof(RowWork), cudaMemcpyHostToDevice), "w8");
+        check(cudaMemcpy(g.d_X, X.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "X");
+        check(cudaMemcpy(g.d_RHS, R.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "RHS");
+        check(cudaMemcpy(g.d_H, H.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "H");
+        check(cudaMemcpy(g.d_T, T.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "T");
+        check(cudaMemcpy(g.d_piv, P.data(), cnt * sizeof(int*), cudaMemcpyHostToDevice), "piv");
+        check(cudaMemcpy(g.d_perm, Q.data(), cnt * sizeof(int*), cudaMemcpyHostToDevice), "perm");
+    }
+    for (size_t k = 0; k < tsteps_.size(); ++k) {
+        const int t = step_index_t_[k];
+        std::vector<const double*> in, hin;
+        std::vector<double*> out, hout;
+        for (int id : step_nodes_t_[k]) {
+            const NodeDev& nd = nodes_[id];
+            in.push_back(t == 0 ? nd.T : nd.Tsteps[t - 1]);
+            out.push_back(nd.Tsteps[t]);
+            hin.push_back(t == 0 ? nd.h : nd.hsteps[t - 1]);
+            hout.push_back(nd.hsteps[t]);
+        }
+        const size_t c = in.size();
+        check(cudaMemcpy(tsteps_[k].d_in, in.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "tin");
+        check(cudaMemcpy(tsteps_[k].d_out, out.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "tout");
+        check(cudaMemcpy(hsteps_[k].d_in, hin.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "hin");
+        check(cudaMemcpy(hsteps_[k].d_out, hout.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "hout");
+    }
+    for (size_t k = 0; k < gsteps_.size(); ++k) {
+        const int t = step_index_g_[k];
+        std::vector<const double*> in;
+        std::vector<double*> out;
+        for (int id : step_nodes_g_[k]) {
+            const NodeDev& nd = nodes_[id];
+            in.push_back(t == 0 ? nd.g : nd.gsteps[t - 1]);
+            out.push_back(nd.gsteps[t]);
+        }
+        const size_t c = in.size();
+        check(cudaMemcpy(gsteps_[k].d_in, in.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "gin");
+        check(cudaMemcpy(gsteps_[k].d_out, out.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "gout");
+    }
+    check(cudaStreamSynchronize(st_), "upload sync");
+}
+
+void Hps::build_leaf_types() {
+    leaf_eigen(st_, LEAF_DTN_COLUMN, d_types_, d_items_dtn_, nitems_dtn_, n_);
+}
+
+void Hps::build() {
+    build_leaf_types();
+    const int maxL = mesh_.max_level;
+    for (int lvl = maxL - 1; lvl >= 0; --lvl) {
+        for (size_t k = 0; k < tsteps_.size(); ++k)
+            if (tsteps_[k].level == lvl + 1)
+                coarsen_T(st_, tsteps_[k].d_in, tsteps_[k].d_out, tsteps_[k].count, tsteps_[k].nf);
+        for (auto& g : groups_) {
+            if (g.level != lvl) continue;
+            const int cnt = int(g.nodes.size()), s = g.s, m = 4 * s;
+            merge_gather_xht(st_, g.d_items, cnt, s);
+            check(cudaMemsetAsync(g.d_info, 0, cnt * sizeof(int), st_), "memset info");
+            dgetrf_batched(st_, m, g.d_X, m, g.d_piv, g.d_info, cnt);
+            piv_to_perm(st_, m, g.d_piv, g.d_perm, cnt);
+            merge_gather_rhs(st_, g.d_items, cnt, s);
+            dlu_solve_permuted(st_, m, 3 * m, (const double* const*)g.d_X, m, g.d_RHS, 3 * m, cnt);
+            // T = T_LHS + H S  (HPSAlgorithm.hpp:940-968), S = first 8s columns of RHS
+            GemmArgs ga{(const double* const*)g.d_H, 0, m, (const double* const*)g.d_RHS, 0, 3 * m,
+                        g.d_T, 0, 2 * m};
+            dgemm_batched(st_, 2 * m, 2 * m, m, 1.0, ga, 1.0, cnt);
+        }
+    }
+    check(cudaGetLastError(), "build launch");
+    check(cudaStreamSynchronize(st_), "build sync");
+    singular_ = 0;
+    for (auto& g : groups_) {
+        std::vector<int> info(g.nodes.size());
+        check(cudaMemcpy(info.data(), g.d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "info");
+        for (int v : info) singular_ += (v != 0);
+    }
+    built_ = true;
+}
+
+void Hps::upwards() {
+    leaf_eigen(st_, LEAF_NEUMANN, d_types_, d_items_neu_, num_leaves(), n_);
+    if (homogeneous_) return;
+    const int maxL = mesh_.max_level;
+    for (int lvl = maxL - 1; lvl >= 0; --lvl) {
+        for (size_t k = 0; k < hsteps_.size(); ++k)
+            if (hsteps_[k].level == lvl + 1)
+                coarsen_vec(st_, hsteps_[k].d_in, hsteps_[k].d_out, hsteps_[k].count, hsteps_[k].nf);
+        for (auto& g : groups_) {
+            if (g.level != lvl) continue;
+            upward_w(st_, g.d_items, g.d_work4, g.nwork4, g.s);
+            upward_h(st_, g.d_items, g.d_work8, g.nwork8, g.s);
+        }
+    }
+}
+
+void Hps::root_from_bc() {
+    const int m = 4 * nodes_[0].nx;
+    // The caller tells whether b is identically zero through bc_general_.
+    if (!bc_general_) {
+        root_diag(st_, m, d_bca_, d_bcb_, d_bcr_, nodes_[0].h, nodes_[0].g);
+        return;
+    }
+    if (!d_rootA_) {
+        const size_t bytes = align_up(size_t(m) * m * 8) + align_up(size_t(m) * 8) + 2 * align_up(size_t(m) * 4) +
+                             align_up(sizeof(int)) + 4 * align_up(sizeof(void*));
+        check(cudaMalloc(&d_rootA_, bytes), "cudaMalloc(root)");
+        Carver cv;
+        cv.base = reinterpret_cast<char*>(d_rootA_);
+        cv.get<double>(size_t(m) * m);
+        d_rootrhs_ = cv.get<double>(m);
+        d_rootpiv_ = cv.get<int>(m);
+        d_rootperm_ = cv.get<int>(m);
+        d_rootinfo_ = cv.get<int>(1);
+        d_rootA_arr_ = cv.get<double*>(1);
+        d_rootrhs_arr_ = cv.get<double*>(1);
+        d_rootpiv_arr_ = cv.get<int*>(1);
+        d_rootperm_arr_ = cv.get<int*>(1);
+        check(cudaMemcpy(d_rootA_arr_, &d_rootA_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
+        check(cudaMemcpy(d_rootrhs_arr_, &d_rootrhs_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
+        check(cudaMemcpy(d_rootpiv_arr_, &d_rootpiv_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
+        check(cudaMemcpy(d_rootperm_arr_, &d_rootperm_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
+    }
+    // g = (diag(a) + diag(b) T)^{-1} (r - diag(b) h)   (HPSAlgorithm.hpp:402-420)
+    root_assemble(st_, m, d_bca_, d_bcb_, nodes_[0].T, d_rootA_);
+    check(cudaMemsetAsync(d_rootinfo_, 0, sizeof(int), st_), "memset root info");
+    dgetrf_batched(st_, m, d_rootA_arr_, m, d_rootpiv_arr_, d_rootinfo_, 1);
+    piv_to_perm(st_, m, d_rootpiv_arr_, d_rootperm_arr_, 1);
+    root_rhs(st_, m, d_bcb_, d_bcr_, nodes_[0].h, d_rootperm_, d_rootrhs_);
+    dlu_solve_permuted(st_, m, 1, (const double* const*)d_rootA_arr_, m, d_rootrhs_arr_, 1, 1);
+    check(cudaMemcpyAsync(nodes_[0].g, d_rootrhs_, m * sizeof(double), cudaMemcpyDeviceToDevice, st_),
+          "root g");
+}
+
+void Hps::downwards() {
+    const int maxL = mesh_.max_level;
+    for (int lvl = 0; lvl < maxL; ++lvl) {
+        for (size_t k = 0; k < gsteps_.size(); ++k)
+            if (gsteps_[k].level == lvl)
+                uncoarsen_vec(st_, gsteps_[k].d_in, gsteps_[k].d_out, gsteps_[k].count, gsteps_[k].nf);
+        for (auto& g : groups_) {
+            if (g.level != lvl) continue;
+            downward(st_, g.d_items, g.d_work4, g.nwork4, g.s, homogeneous_ ? 0 : 1);
+        }
+    }
+    if (homogeneous_) fill_zero(st_, d_f_, (long long)num_leaves() * n_ * n_);
+    leaf_eigen(st_, LEAF_SOLVE, d_types_, d_items_solve_, num_leaves(), n_);
+}
+
+void Hps::solve_async() {
+    upwards();
+    root_from_bc();
+    downwards();
+}
+
+double Hps::build_flops() const {
+    double f = 0;
+    for (const auto& g : groups_) {
+        const double m = 4.0 * g.s, cnt = double(g.nodes.size());
+        f += cnt * (2.0 / 3.0 * m * m * m + 2.0 * m * m * (3 * m) + 2.0 * (2 * m) * (2 * m) * m);
+    }
+    return f;
+}
+
+double Hps::solve_bytes() const {
+    double b = 0;
+    for (const auto& g : groups_) {
+        const double s = g.s, cnt = double(g.nodes.size());
+        // X^{-1} (16 s^2) + nonzero half of H (16 s^2) + S (32 s^2)
+        b += cnt * 8.0 * (16 * s * s + 16 * s * s + 32 * s * s);
+    }
+    b += double(num_leaves()) * n_ * n_ * 8.0 * 3;  // f read twice, u written
+    return b;
+}
+
+double Hps::solve_flops() const {
+    double f = 0;
+    for (const auto& g : groups_) {
+        const double s = g.s, cnt = double(g.nodes.size());
+        f += cnt * 2.0 * (16 * s * s + 16 * s * s + 32 * s * s);
+    }
+    f += double(num_leaves()) * (8.0 * n_ * n_ * n_ + 6.0 * n_ * n_ * n_);
+    return f;
+}
+
+}  // namespace efgb

@@ -1,0 +1,160 @@
+// GB300 HPS solver: plan + device storage + stage drivers (plain FP64 form).
+//
+// Replaces HPSAlgorithm<FiniteVolumeGrid, FiniteVolumeSolver, FiniteVolumePatch, double>
+// (src/HPSAlgorithm.hpp) on one GPU.  Instead of one callback per node in a p4est traversal, every
+// stage runs level by level: all merges (or splits) of one tree level with the same child size are
+// one grouped launch sequence.  Operators live in device memory owned by the Hps object.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ef_kernels.cuh"
+#include "ef_mesh.hpp"
+
+namespace efgb {
+
+enum SolverType : int { SOLVER_FIVE_POINT = 0, SOLVER_FISHPACK90 = 1 };
+
+// Orthonormal sine basis V (n x n, V[i][k]) of the 1-D Dirichlet-ghost operator and the inverse
+// 2-D eigenvalue table Dinv[k][l] = 1 / (mu_x[k] + mu_y[l] + lambda) of one patch geometry.
+void leaf_tables(int n, double dx, double dy, double lambda, double* V, double* Dinv);
+
+struct NodeDev {
+    int nx = 0;        // grid cells per side of the node's patch (leaves: n, internal: 2s)
+    int size = 0;      // nx >> ncoarsen (PatchBase::size(), Patch.hpp:99-101)
+    int ncoarsen = 0;  // n_coarsens set when the parent merges (HPSAlgorithm.hpp:707-741)
+    int s = 0;         // internal: coarsened child side
+    int leaf_type = -1;
+    double *T = nullptr, *Tc = nullptr;
+    double *X = nullptr, *RHS = nullptr, *H = nullptr;
+    int *piv = nullptr, *perm = nullptr;
+    double *h = nullptr, *hc = nullptr, *g = nullptr, *gf = nullptr, *w = nullptr;
+    std::vector<double*> Tsteps, hsteps, gsteps;  // intermediate (un)coarsening buffers
+};
+
+struct Group {
+    int level = 0, s = 0;
+    std::vector<int> nodes;
+    MergeItem* d_items = nullptr;
+    RowWork *d_work4 = nullptr, *d_work8 = nullptr;
+    int nwork4 = 0, nwork8 = 0;
+    double** d_X = nullptr;
+    double** d_RHS = nullptr;
+    double** d_H = nullptr;
+    double** d_T = nullptr;
+    int** d_piv = nullptr;
+    int** d_perm = nullptr;
+    int* d_info = nullptr;
+};
+
+struct ResampleStep {  // one batched (un)coarsening step: `count` items of fine size nf
+    int level = 0;     // tree level of the nodes
+    int nf = 0;
+    int count = 0;
+    const double** d_in = nullptr;
+    double** d_out = nullptr;
+};
+
+struct LeafTypeHost {
+    int n;
+    double dx, dy;
+    double* T = nullptr;
+};
+
+class Hps {
+public:
+    Hps(const Mesh& mesh, int solver_type, double lambda, bool cache_operators);
+    ~Hps();
+    Hps(const Hps&) = delete;
+    Hps& operator=(const Hps&) = delete;
+
+    void set_stream(cudaStream_t st) { st_ = st; }
+    cudaStream_t stream() const { return st_; }
+    void set_homogeneous_rhs(bool v) { homogeneous_ = v; }
+    // true when the boundary coefficient b of a*u + b*du/dn = r is not identically zero
+    void set_bc_general(bool v) { bc_general_ = v; }
+    bool homogeneous_rhs() const { return homogeneous_; }
+
+    // Stages (synchronous to the host at their end unless noted).
+    void build();                                  // HPSAlgorithm::buildStage
+    void upwards();                                // HPSAlgorithm::upwardsStage on leaf_f()
+    void root_from_bc();                           // root g from bc_a/b/r (HPSAlgorithm.hpp:402-420)
+    void downwards();                              // split1to4 + leafSolve for every node
+    void solve_async();                            // upwards + root + downwards, no host sync
+
+    // Device buffers (resident, owned by this object).
+    double* leaf_f() const { return d_f_; }        // nleaves * n * n, leaf order, j + i*n
+    double* leaf_u() const { return d_u_; }
+    double* bc_a() const { return d_bca_; }        // 4M each, WESN, root face centres
+    double* bc_b() const { return d_bcb_; }
+    double* bc_r() const { return d_bcr_; }
+    double* root_g() const { return nodes_[0].g; }
+    double* root_h() const { return nodes_[0].h; }
+    double* root_T() const { return nodes_[0].T; }
+
+    int num_leaves() const { return int(mesh_.leaves.size()); }
+    int leaf_n() const { return n_; }
+    int root_M() const { return nodes_[0].nx; }
+    int num_nodes() const { return int(nodes_.size()); }
+    const NodeDev& node(int i) const { return nodes_[i]; }
+    const Mesh& mesh() const { return mesh_; }
+    bool built() const { return built_; }
+    int singular_count() const { return singular_; }
+    size_t device_bytes() const { return arena_bytes_; }
+
+    // Counters for the roofline: flops of the build by kernel family (FP64).
+    double build_flops() const;
+    double solve_bytes() const;
+    double solve_flops() const;
+    int kernel_launches_per_solve() const { return launches_per_solve_; }
+
+private:
+    void plan();
+    void allocate();
+    void upload_tables();
+    void build_leaf_types();
+    void check(cudaError_t e, const char* what);
+
+    Mesh mesh_;
+    int solver_type_;
+    double lambda_;
+    bool cache_ops_;
+    bool homogeneous_ = false;
+    bool bc_general_ = false;
+    int n_ = 0;
+    cudaStream_t st_ = 0;
+
+    std::vector<NodeDev> nodes_;
+    std::vector<Group> groups_;                 // ordered deepest level first
+    std::vector<ResampleStep> tsteps_, hsteps_, gsteps_;
+    std::vector<std::vector<int>> step_nodes_t_, step_nodes_g_;
+    std::vector<int> step_index_t_, step_index_g_;
+    double *d_V_ = nullptr, *d_Dinv_ = nullptr;
+    std::vector<LeafTypeHost> types_;
+    LeafType* d_types_ = nullptr;
+    LeafItem *d_items_dtn_ = nullptr, *d_items_neu_ = nullptr, *d_items_solve_ = nullptr;
+    int nitems_dtn_ = 0;
+
+    double *d_f_ = nullptr, *d_u_ = nullptr;
+    double *d_bca_ = nullptr, *d_bcb_ = nullptr, *d_bcr_ = nullptr;
+    // general (b != 0) root solve
+    double *d_rootA_ = nullptr, *d_rootrhs_ = nullptr;
+    int *d_rootpiv_ = nullptr, *d_rootperm_ = nullptr, *d_rootinfo_ = nullptr;
+    double** d_rootA_arr_ = nullptr;
+    double** d_rootrhs_arr_ = nullptr;
+    int** d_rootpiv_arr_ = nullptr;
+    int** d_rootperm_arr_ = nullptr;
+
+    char* arena_ = nullptr;
+    size_t arena_bytes_ = 0, arena_used_ = 0;
+
+    bool built_ = false;
+    int singular_ = 0;
+    int launches_per_solve_ = 0;
+};
+
+}  // namespace efgb

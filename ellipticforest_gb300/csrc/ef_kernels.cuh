@@ -1,0 +1,133 @@
+// Device kernels of the GB300 HPS solver (FP64 plain form) and their host launch wrappers.
+//
+// Conventions (shared with the reference, src/HPSAlgorithm.hpp and FiniteVolumeSolver.cpp):
+//   * every matrix is row-major with an explicit leading dimension;
+//   * boundary vectors are WESN-stacked, each side `n` long (W,E run along y; S,N along x);
+//   * a patch's cell (i, j) (x-index i, y-index j) is stored at j + i*n;
+//   * children of a node are 0=alpha (SW), 1=beta (SE), 2=gamma (NW), 3=omega (NE).
+//
+// The merge of four children with (coarsened) side s uses the interface order of
+// HPSAlgorithm.hpp:870-895: I0 = alpha|gamma, I1 = beta|omega, I2 = alpha|beta, I3 = gamma|omega.
+// Each interface has a "lower" child (alpha, beta, alpha, gamma) and an "upper" child (gamma,
+// omega, beta, omega); with sigma(lower) = -1, sigma(upper) = +1 the reference's blocks are
+//   X(I,I')  = -sum_c sigma(I,c) Tc[q(c,I)][q(c,I')]
+//   S_RHS(I,p) = sigma(I,c(p)) Tc(p)[q(c,I)][q(p)]          (c(p) adjacent to I)
+//   H(p,I)   = Tc(p)[q(p)][q(c(p),I)]                        (c(p) adjacent to I)
+//   T_LHS(p,p') = Tc[q(p)][q(p')]                             (c(p) == c(p'))
+// where p runs over the parent's exterior points already in WESN order, i.e. the permutation
+// pi_WESN = {0,4,2,6,1,3,5,7} of HPSAlgorithm.hpp:979-993 is applied while gathering.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace efgb {
+
+// ------------------------------------------------------------------------------------------------
+// Batched FP64 dense linear algebra (pointer arrays, uniform shapes and offsets per launch)
+// ------------------------------------------------------------------------------------------------
+struct GemmArgs {
+    const double* const* A; long long offA; int lda;
+    const double* const* B; long long offB; int ldb;
+    double* const* C; long long offC; int ldc;
+};
+
+// C = alpha*A*B + beta*C for each batch item (row-major).
+void dgemm_batched(cudaStream_t st, int M, int N, int K, double alpha, const GemmArgs& a,
+                   double beta, int batch);
+
+// In-place LU with partial pivoting of the square n x n matrices A[b] (row-major, lda).
+// piv[b][j] is the 0-based row swapped with row j (LAPACK dgetrf semantics, 0-based);
+// info[b] = first zero pivot (1-based) or 0.  A, piv: device arrays of device pointers.
+void dgetrf_batched(cudaStream_t st, int n, double* const* A, int lda, int* const* piv, int* info,
+                    int batch);
+
+// perm[b][i] = original row that ends at position i after applying piv[b][0..n).
+void piv_to_perm(cudaStream_t st, int n, int* const* piv, int* const* perm, int batch);
+
+// B[b] <- U^{-1} L^{-1} B[b]  (B already row-permuted), n x nrhs, ldb.
+void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* LU, int lda,
+                        double* const* B, int ldb, int batch);
+
+// ------------------------------------------------------------------------------------------------
+// Leaf patch kernels (constant-coefficient Helmholtz u_xx + u_yy + lambda u = f, Dirichlet data on
+// cell faces with ghost u = 2g - u; the discrete system of FiniteVolumeSolver.cpp:27-290)
+// ------------------------------------------------------------------------------------------------
+struct LeafType {
+    int n;
+    double dx, dy;
+    const double* V;     // n x n orthonormal sine basis, V[i][k]
+    const double* Dinv;  // n x n, 1 / (mu_x[k] + mu_y[l] + lambda)
+};
+
+enum LeafMode : int {
+    LEAF_DTN_COLUMN = 0,  // g = e_unit, f = 0, write column `unit` of T (4n x 4n, row-major)
+    LEAF_NEUMANN = 1,     // g = 0, f given, write h (4n)
+    LEAF_SOLVE = 2,       // f (nullable = 0) and g given, write u (n*n)
+    LEAF_MAPD2N = 3,      // f (nullable = 0) and g given, write h (4n)
+};
+
+struct LeafItem {
+    int type;
+    int unit;
+    const double* f;
+    const double* g;
+    double* out;
+};
+
+void leaf_eigen(cudaStream_t st, int mode, const LeafType* types_dev, const LeafItem* items_dev,
+                int nitems, int nmax);
+
+// ------------------------------------------------------------------------------------------------
+// Merge / upward / downward kernels
+// ------------------------------------------------------------------------------------------------
+struct MergeItem {
+    const double* Tc[4];  // children's (coarsened) T, 4s x 4s
+    double* X;            // 4s x 4s (LU in place)
+    int* piv;             // 4s
+    int* perm;            // 4s
+    double* RHS;          // 4s x 12s  = [S (WESN columns) | X^{-1}]
+    double* H;            // 8s x 4s, rows in WESN order
+    double* T;            // 8s x 8s, WESN
+    const double* hc[4];  // children's (coarsened) h, 4s
+    double* h;            // own h, 8s
+    double* w;            // 4s
+    const double* gf;     // own full-size g, 8s
+    double* gc[4];        // children's g (at coarsened size), 4s
+};
+
+// X, H and T (= T_LHS) from the children (build, step 1).
+void merge_gather_xht(cudaStream_t st, const MergeItem* items, int nitems, int s);
+// RHS = P [S_RHS | I] with the row permutation of the LU of X (build, step 3).
+void merge_gather_rhs(cudaStream_t st, const MergeItem* items, int nitems, int s);
+
+// Per-side coarsening of T (4nf x 4nf -> 4nc x 4nc): L21 T L12  (SpecialMatrices.hpp:93-173).
+void coarsen_T(cudaStream_t st, const double* const* Tin, double* const* Tout, int nitems, int nf);
+// Per-side fine-to-coarse averaging of h (4nf -> 4nc).
+void coarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf);
+// Per-side coarse-to-fine interpolation of g (4nc -> 4nf).
+void uncoarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf);
+
+struct RowWork {
+    int item;
+    int row0;
+};
+// w = X^{-1} hdiff, hdiff gathered from the children (upward, step 1).
+void upward_w(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s);
+// h = H w + h_ext (upward, step 2).
+void upward_h(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s);
+// u_Gamma = S gf (+ w) and scatter of the children's Dirichlet data (downward).
+void downward(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s,
+              int add_w);
+
+// Root Dirichlet data.  diag: g = (r - b.h) / a.  general: A = diag(a) + diag(b) T; rhs = r - b.h
+void root_diag(cudaStream_t st, int m, const double* a, const double* b, const double* r,
+               const double* h, double* g);
+void root_assemble(cudaStream_t st, int m, const double* a, const double* b, const double* T,
+                   double* A);
+void root_rhs(cudaStream_t st, int m, const double* b, const double* r, const double* h,
+              const int* perm, double* rhs);
+
+void fill_zero(cudaStream_t st, double* p, long long n);
+
+}  // namespace efgb

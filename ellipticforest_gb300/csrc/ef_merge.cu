@@ -1,0 +1,379 @@
+// Merge (build), upward and downward kernels of the HPS tree, grouped per tree level.
+//
+// Index maps (see ef_kernels.cuh): interfaces I0..I3 = alpha|gamma, beta|omega, alpha|beta,
+// gamma|omega (HPSAlgorithm.hpp:752-788); the lower child of I sees it on its N (I0, I1) or E
+// (I2, I3) side, the upper child on its S or W side.  Parent exterior points are WESN with
+// W = [alpha_W; gamma_W], E = [beta_E; omega_E], S = [alpha_S; beta_S], N = [gamma_N; omega_N]
+// (the pi_WESN = {0,4,2,6,1,3,5,7} reorder of HPSAlgorithm.hpp:979-993).
+#include "ef_kernels.cuh"
+
+namespace efgb {
+
+namespace {
+
+__device__ __forceinline__ int lower_child(int I) { return (I == 1) ? 1 : (I == 3 ? 2 : 0); }
+__device__ __forceinline__ int upper_child(int I) { return (I == 0) ? 2 : (I == 2 ? 1 : 3); }
+__device__ __forceinline__ int q_lower(int I, int o, int s) { return (I < 2 ? 3 * s : s) + o; }
+__device__ __forceinline__ int q_upper(int I, int o, int s) { return (I < 2 ? 2 * s : 0) + o; }
+
+// parent exterior index p in [0, 8s) -> (child, child side index)
+__device__ __forceinline__ void ext_map(int p, int s, int& c, int& q) {
+    const int side = p / (2 * s);
+    const int r = p - side * 2 * s;
+    const int hlf = r >= s ? 1 : 0;
+    const int o = r - hlf * s;
+    // W: alpha, gamma; E: beta, omega; S: alpha, beta; N: gamma, omega
+    c = side < 2 ? side + 2 * hlf : (side == 2 ? 0 : 2) + hlf;
+    q = side * s + o;
+}
+
+// child-side index of interface point (I, o) on child c, or -1 if c is not adjacent to I.
+__device__ __forceinline__ int iface_q(int c, int I, int o, int s, double& sigma) {
+    if (c == lower_child(I)) { sigma = -1.0; return q_lower(I, o, s); }
+    if (c == upper_child(I)) { sigma = 1.0; return q_upper(I, o, s); }
+    return -1;
+}
+
+// the two interfaces adjacent to child c
+__device__ __forceinline__ void child_ifaces(int c, int& Ia, int& Ib) {
+    // alpha: I0, I2; beta: I1, I2; gamma: I0, I3; omega: I1, I3
+    Ia = (c == 0 || c == 2) ? 0 : 1;
+    Ib = (c < 2) ? 2 : 3;
+}
+
+__global__ void k_gather_xht(const MergeItem* __restrict__ items, int s) {
+    const MergeItem& it = items[blockIdx.y];
+    const long long m4 = 4LL * s, m8 = 8LL * s;
+    const long long nX = m4 * m4, nH = m8 * m4, nT = m8 * m8;
+    const long long tot = nX + nH + nT;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        if (e < nX) {
+            const int r = int(e / m4), cc = int(e - (e / m4) * m4);
+            const int I = r / s, o = r - I * s, J = cc / s, oj = cc - J * s;
+            double v = 0.0;
+            // X(I,J) = -sum_c sigma(I,c) Tc[q(c,I)][q(c,J)]
+            const int cl = lower_child(I), cu = upper_child(I);
+            double sj;
+            int qj = iface_q(cl, J, oj, s, sj);
+            if (qj >= 0) v += it.Tc[cl][(long long)q_lower(I, o, s) * m4 + qj];
+            qj = iface_q(cu, J, oj, s, sj);
+            if (qj >= 0) v -= it.Tc[cu][(long long)q_upper(I, o, s) * m4 + qj];
+            it.X[e] = v;
+        } else if (e < nX + nH) {
+            const long long f = e - nX;
+            const int p = int(f / m4), col = int(f - (f / m4) * m4);
+            const int I = col / s, o = col - I * s;
+            int c, q;
+            ext_map(p, s, c, q);
+            double sg;
+            const int qi = iface_q(c, I, o, s, sg);
+            it.H[f] = (qi >= 0) ? it.Tc[c][(long long)q * m4 + qi] : 0.0;
+        } else {
+            const long long f = e - nX - nH;
+            const int p = int(f / m8), pp = int(f - (f / m8) * m8);
+            int c, q, c2, q2;
+            ext_map(p, s, c, q);
+            ext_map(pp, s, c2, q2);
+            it.T[f] = (c == c2) ? it.Tc[c][(long long)q * m4 + q2] : 0.0;
+        }
+    }
+}
+
+__global__ void k_gather_rhs(const MergeItem* __restrict__ items, int s) {
+    const MergeItem& it = items[blockIdx.y];
+    const long long m4 = 4LL * s, m12 = 12LL * s;
+    const long long tot = m4 * m12;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int r = int(e / m12), col = int(e - (e / m12) * m12);
+        const int src = it.perm[r];
+        double v;
+        if (col < 8 * s) {
+            const int I = src / s, o = src - I * s;
+            int c, q;
+            ext_map(col, s, c, q);
+            double sg;
+            const int qi = iface_q(c, I, o, s, sg);
+            v = (qi >= 0) ? sg * it.Tc[c][(long long)qi * m4 + q] : 0.0;
+        } else {
+            v = (col - 8 * s == src) ? 1.0 : 0.0;
+        }
+        it.RHS[e] = v;
+    }
+}
+
+// L12 column j (coarse index) of InterpolationMatrixCoarse2Fine(nf): fine rows and weights.
+__device__ __forceinline__ int l12_col(int j, int nf, int* rows, double* w) {
+    const int nc = nf / 2;
+    int k = 0;
+    if (j <= 2) {
+        rows[k] = 0;
+        w[k++] = (j == 0) ? 1.40625 : (j == 1 ? -0.5625 : 0.15625);
+    }
+    if (j >= 1) { rows[k] = 2 * j - 1; w[k++] = 0.25; rows[k] = 2 * j; w[k++] = 0.75; }
+    if (j <= nc - 2) { rows[k] = 2 * j + 1; w[k++] = 0.75; rows[k] = 2 * j + 2; w[k++] = 0.25; }
+    if (j >= nc - 3) {
+        rows[k] = nf - 1;
+        w[k++] = (j == nc - 3) ? 0.15625 : (j == nc - 2 ? -0.5625 : 1.40625);
+    }
+    return k;
+}
+
+__global__ void k_coarsen_T(const double* const* Tin, double* const* Tout, int nf) {
+    const double* __restrict__ A = Tin[blockIdx.y];
+    double* __restrict__ B = Tout[blockIdx.y];
+    const int nc = nf / 2, mf = 4 * nf, mc = 4 * nc;
+    const long long tot = (long long)mc * mc;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int R = int(e / mc), C = int(e - (e / mc) * mc);
+        const int a = R / nc, i = R - a * nc, b = C / nc, j = C - b * nc;
+        int rows[6];
+        double w[6];
+        const int k = l12_col(j, nf, rows, w);
+        double acc = 0.0;
+        for (int rr = 0; rr < 2; ++rr) {
+            const double* row = A + (long long)(a * nf + 2 * i + rr) * mf + b * nf;
+            double t = 0.0;
+            for (int q = 0; q < k; ++q) t = fma(row[rows[q]], w[q], t);
+            acc = fma(0.5, t, acc);
+        }
+        B[e] = acc;
+    }
+}
+
+__global__ void k_coarsen_vec(const double* const* vin, double* const* vout, int nf) {
+    const double* __restrict__ a = vin[blockIdx.y];
+    double* __restrict__ b = vout[blockIdx.y];
+    const int nc = nf / 2;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 4 * nc; e += gridDim.x * blockDim.x) {
+        const int side = e / nc, i = e - side * nc;
+        b[e] = 0.5 * a[side * nf + 2 * i] + 0.5 * a[side * nf + 2 * i + 1];
+    }
+}
+
+__global__ void k_uncoarsen_vec(const double* const* vin, double* const* vout, int nf) {
+    const double* __restrict__ a = vin[blockIdx.y];
+    double* __restrict__ b = vout[blockIdx.y];
+    const int nc = nf / 2;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 4 * nf; e += gridDim.x * blockDim.x) {
+        const int side = e / nf, c = e - side * nf;
+        const double* y = a + side * nc;
+        double v;
+        if (c == 0) v = 1.40625 * y[0] + (-0.5625) * y[1] + 0.15625 * y[2];
+        else if (c == nf - 1) v = 0.15625 * y[nc - 3] + (-0.5625) * y[nc - 2] + 1.40625 * y[nc - 1];
+        else if (c & 1) { const int jp = (c - 1) / 2; v = 0.75 * y[jp] + 0.25 * y[jp + 1]; }
+        else { const int jp = (c - 2) / 2; v = 0.25 * y[jp] + 0.75 * y[jp + 1]; }
+        b[e] = v;
+    }
+}
+
+constexpr int ROWS_PER_CTA = 32;  // 8 warps x 4 rows
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_upward_w(const MergeItem* __restrict__ items,
+                                                  const RowWork* __restrict__ work, int s) {
+    const RowWork wk = work[blockIdx.x];
+    const MergeItem& it = items[wk.item];
+    extern __shared__ double hd[];
+    const int m4 = 4 * s, m12 = 12 * s;
+    for (int r = threadIdx.x; r < m4; r += blockDim.x) {
+        const int I = r / s, o = r - I * s;
+        // hDiff = h_upper - h_lower (HPSAlgorithm.hpp:1061-1081)
+        hd[r] = it.hc[upper_child(I)][q_upper(I, o, s)] - it.hc[lower_child(I)][q_lower(I, o, s)];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = 0; k < ROWS_PER_CTA / 8; ++k) {
+        const int r = wk.row0 + wid * (ROWS_PER_CTA / 8) + k;
+        if (r >= m4) break;
+        const double* row = it.RHS + (long long)r * m12 + 8 * s;  // X^{-1} block
+        double acc = 0.0;
+        for (int c = lane; c < m4; c += 32) acc = fma(row[c], hd[c], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) it.w[r] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_upward_h(const MergeItem* __restrict__ items,
+                                                  const RowWork* __restrict__ work, int s) {
+    const RowWork wk = work[blockIdx.x];
+    const MergeItem& it = items[wk.item];
+    extern __shared__ double wv[];
+    const int m4 = 4 * s, m8 = 8 * s;
+    for (int r = threadIdx.x; r < m4; r += blockDim.x) wv[r] = it.w[r];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = 0; k < ROWS_PER_CTA / 8; ++k) {
+        const int p = wk.row0 + wid * (ROWS_PER_CTA / 8) + k;
+        if (p >= m8) break;
+        int c, q;
+        ext_map(p, s, c, q);
+        int Ia, Ib;
+        child_ifaces(c, Ia, Ib);
+        const double* row = it.H + (long long)p * m4;
+        double acc = 0.0;
+        for (int o = lane; o < s; o += 32) {
+            acc = fma(row[Ia * s + o], wv[Ia * s + o], acc);
+            acc = fma(row[Ib * s + o], wv[Ib * s + o], acc);
+        }
+        acc = warp_sum(acc);
+        // h_tau = H w + h_update (HPSAlgorithm.hpp:1098-1117), already in WESN order
+        if (lane == 0) it.h[p] = acc + it.hc[c][q];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_downward(const MergeItem* __restrict__ items,
+                                                  const RowWork* __restrict__ work, int s,
+                                                  int add_w) {
+    const RowWork wk = work[blockIdx.x];
+    const MergeItem& it = items[wk.item];
+    extern __shared__ double gs[];
+    const int m4 = 4 * s, m8 = 8 * s, m12 = 12 * s;
+    for (int p = threadIdx.x; p < m8; p += blockDim.x) {
+        const double v = it.gf[p];
+        gs[p] = v;
+        if (wk.row0 == 0) {
+            // exterior Dirichlet data of the children (HPSAlgorithm.hpp:1214-1227)
+            int c, q;
+            ext_map(p, s, c, q);
+            it.gc[c][q] = v;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = 0; k < ROWS_PER_CTA / 8; ++k) {
+        const int r = wk.row0 + wid * (ROWS_PER_CTA / 8) + k;
+        if (r >= m4) break;
+        const double* row = it.RHS + (long long)r * m12;  // S block
+        double acc = 0.0;
+        for (int c = lane; c < m8; c += 32) acc = fma(row[c], gs[c], acc);
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            // u_Gamma = S g + w (HPSAlgorithm.hpp:1197-1204)
+            const double u = add_w ? acc + it.w[r] : acc;
+            const int I = r / s, o = r - I * s;
+            it.gc[lower_child(I)][q_lower(I, o, s)] = u;
+            it.gc[upper_child(I)][q_upper(I, o, s)] = u;
+        }
+    }
+}
+
+__global__ void k_root_diag(int m, const double* a, const double* b, const double* r,
+                            const double* h, double* g) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double bh = (h != nullptr) ? b[i] * h[i] : 0.0;
+        g[i] = (r[i] - bh) / a[i];
+    }
+}
+
+__global__ void k_root_assemble(int m, const double* a, const double* b, const double* T, double* A) {
+    const long long tot = (long long)m * m;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = int(e / m), j = int(e - (e / m) * m);
+        const double v = b[i] * T[e];
+        A[e] = (i == j) ? a[i] + v : v;
+    }
+}
+
+__global__ void k_root_rhs(int m, const double* b, const double* r, const double* h, const int* perm,
+                           double* rhs) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const int k = perm[i];
+        const double bh = (h != nullptr) ? b[k] * h[k] : 0.0;
+        rhs[i] = r[k] - bh;
+    }
+}
+
+__global__ void k_fill_zero(double* p, long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x)
+        p[e] = 0.0;
+}
+
+inline int grid_for(long long tot, int per_item_items) {
+    long long b = (tot + 255) / 256;
+    if (b > 4096) b = 4096;
+    if (b < 1) b = 1;
+    (void)per_item_items;
+    return int(b);
+}
+
+void set_smem(const void* fn, size_t bytes) {
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+}
+
+}  // namespace
+
+void merge_gather_xht(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+    const long long tot = 16LL * s * s + 32LL * s * s + 64LL * s * s;
+    dim3 g(grid_for(tot, nitems), nitems);
+    k_gather_xht<<<g, 256, 0, st>>>(items, s);
+}
+
+void merge_gather_rhs(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+    const long long tot = 48LL * s * s;
+    dim3 g(grid_for(tot, nitems), nitems);
+    k_gather_rhs<<<g, 256, 0, st>>>(items, s);
+}
+
+void coarsen_T(cudaStream_t st, const double* const* Tin, double* const* Tout, int nitems, int nf) {
+    const long long tot = 4LL * nf * 4LL * nf / 4;
+    dim3 g(grid_for(tot, nitems), nitems);
+    k_coarsen_T<<<g, 256, 0, st>>>(Tin, Tout, nf);
+}
+
+void coarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf) {
+    dim3 g((2 * nf + 255) / 256, nitems);
+    k_coarsen_vec<<<g, 256, 0, st>>>(vin, vout, nf);
+}
+
+void uncoarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf) {
+    dim3 g((4 * nf + 255) / 256, nitems);
+    k_uncoarsen_vec<<<g, 256, 0, st>>>(vin, vout, nf);
+}
+
+void upward_w(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s) {
+    const size_t smem = size_t(4) * s * sizeof(double);
+    set_smem((const void*)k_upward_w, smem);
+    k_upward_w<<<nwork, 256, smem, st>>>(items, work, s);
+}
+
+void upward_h(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s) {
+    const size_t smem = size_t(4) * s * sizeof(double);
+    set_smem((const void*)k_upward_h, smem);
+    k_upward_h<<<nwork, 256, smem, st>>>(items, work, s);
+}
+
+void downward(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s, int add_w) {
+    const size_t smem = size_t(8) * s * sizeof(double);
+    set_smem((const void*)k_downward, smem);
+    k_downward<<<nwork, 256, smem, st>>>(items, work, s, add_w);
+}
+
+void root_diag(cudaStream_t st, int m, const double* a, const double* b, const double* r,
+               const double* h, double* g) {
+    k_root_diag<<<(m + 255) / 256, 256, 0, st>>>(m, a, b, r, h, g);
+}
+
+void root_assemble(cudaStream_t st, int m, const double* a, const double* b, const double* T, double* A) {
+    k_root_assemble<<<grid_for((long long)m * m, 1), 256, 0, st>>>(m, a, b, T, A);
+}
+
+void root_rhs(cudaStream_t st, int m, const double* b, const double* r, const double* h,
+              const int* perm, double* rhs) {
+    k_root_rhs<<<(m + 255) / 256, 256, 0, st>>>(m, b, r, h, perm, rhs);
+}
+
+void fill_zero(cudaStream_t st, double* p, long long n) {
+    if (n > 0) k_fill_zero<<<grid_for(n, 1), 256, 0, st>>>(p, n);
+}
+
+}  // namespace efgb

@@ -1,0 +1,385 @@
+"""Python mirror of EllipticForest's HPS path, running on the GB300 CUDA library.
+
+Same class and method names as the reference's C++ API (``src/HPSAlgorithm.hpp``,
+``src/Mesh.hpp``, ``src/Patches/FiniteVolume/*``) so that drivers and tests read like the
+reference's own.  Every numerical step goes through the C ABI of ``libellipticforest_gb300.so``;
+this module only samples the user's callbacks at the reference's sampling points and moves arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr
+
+FivePointStencil = "FivePointStencil"
+FISHPACK90 = "FISHPACK90"
+XDIM, YDIM = 0, 1
+
+
+def _solver_code(solver_type: str) -> int:
+    if solver_type == FISHPACK90:
+        return _lib.EF_SOLVER_FISHPACK90
+    if solver_type == FivePointStencil:
+        return _lib.EF_SOLVER_FIVE_POINT
+    raise ValueError(f"unknown solver type {solver_type!r}")
+
+
+class FiniteVolumeGrid:
+    """FiniteVolumeGrid (FiniteVolumeGrid.cpp:9-36)."""
+
+    def __init__(self, nx: int, x_lower: float, x_upper: float, ny: int, y_lower: float, y_upper: float):
+        self._nx, self._ny = int(nx), int(ny)
+        self._xl, self._xu = float(x_lower), float(x_upper)
+        self._yl, self._yu = float(y_lower), float(y_upper)
+        self._dx = (self._xu - self._xl) / self._nx
+        self._dy = (self._yu - self._yl) / self._ny
+
+    def nx(self): return self._nx
+    def ny(self): return self._ny
+    def xLower(self): return self._xl
+    def xUpper(self): return self._xu
+    def yLower(self): return self._yl
+    def yUpper(self): return self._yu
+    def dx(self): return self._dx
+    def dy(self): return self._dy
+
+    def point(self, dim: int, index):
+        if dim == XDIM:
+            return (self._xl + self._dx / 2) + np.asarray(index) * self._dx
+        if dim == YDIM:
+            return (self._yl + self._dy / 2) + np.asarray(index) * self._dy
+        raise ValueError("Invalid `dim` argument.")
+
+    def __call__(self, dim, index):
+        return self.point(dim, index)
+
+
+class FiniteVolumeSolver:
+    """FiniteVolumeSolver (FiniteVolumeSolver.hpp:53-162) on the GPU.
+
+    ``solver_type = FISHPACK90`` solves u_xx + u_yy + lambda u = f with
+    ``lambda = lambda_function(0, 0)`` (FiniteVolumeSolver.cpp:253); alpha and beta are not used,
+    exactly as in the reference's FISHPACK90 branch.
+    """
+
+    def __init__(self, alpha_function=None, beta_function=None, lambda_function=None, rhs_function=None):
+        self.solver_type = FISHPACK90
+        self.alpha_function = alpha_function or (lambda x, y: 1.0)
+        self.beta_function = beta_function or (lambda x, y: 1.0)
+        self.lambda_function = lambda_function or (lambda x, y: 0.0)
+        self.rhs_function = rhs_function
+
+    def name(self):
+        return "FiniteVolumeSolver"
+
+    def _lam(self) -> float:
+        return float(self.lambda_function(0, 0))
+
+    def _args(self, grid: FiniteVolumeGrid):
+        if grid.nx() != grid.ny():
+            raise ValueError("square patches only (nx == ny)")
+        return (_solver_code(self.solver_type), grid.nx(), grid.xLower(), grid.xUpper(),
+                grid.yLower(), grid.yUpper(), self._lam())
+
+    def buildD2N(self, grid: FiniteVolumeGrid) -> np.ndarray:
+        n = grid.nx()
+        T = np.empty((4 * n, 4 * n))
+        check(_lib.load().ef_fv_build_d2n(*self._args(grid), dptr(T)))
+        return T
+
+    def solve(self, grid: FiniteVolumeGrid, dirichlet_data, rhs_data) -> np.ndarray:
+        n = grid.nx()
+        g = np.ascontiguousarray(dirichlet_data, dtype=np.float64)
+        f = np.ascontiguousarray(rhs_data, dtype=np.float64)
+        if g.size != 4 * n or f.size != n * n:
+            raise ValueError("size mismatch")
+        u = np.empty(n * n)
+        check(_lib.load().ef_fv_solve(*self._args(grid), dptr(g), dptr(f), dptr(u)))
+        return u
+
+    def mapD2N(self, grid: FiniteVolumeGrid, dirichlet_data, rhs_data) -> np.ndarray:
+        n = grid.nx()
+        g = np.ascontiguousarray(dirichlet_data, dtype=np.float64)
+        f = np.ascontiguousarray(rhs_data, dtype=np.float64)
+        if g.size != 4 * n or f.size != n * n:
+            raise ValueError("size mismatch")
+        h = np.empty(4 * n)
+        check(_lib.load().ef_fv_map_d2n(*self._args(grid), dptr(g), dptr(f), dptr(h)))
+        return h
+
+    def particularNeumannData(self, grid: FiniteVolumeGrid, rhs_data) -> np.ndarray:
+        return self.mapD2N(grid, np.zeros(2 * grid.nx() + 2 * grid.ny()), rhs_data)
+
+
+class FiniteVolumePatch:
+    """FiniteVolumePatch (FiniteVolumePatch.hpp:19-73); leaf data are views of the solver's arrays."""
+
+    def __init__(self, grid: Optional[FiniteVolumeGrid] = None):
+        self._grid = grid
+        self.n_coarsens = 0
+        self.u = np.zeros(0)
+        self.f = np.zeros(0)
+        self.g = np.zeros(0)
+        self.h = np.zeros(0)
+
+    def name(self): return "FiniteVolumePatch"
+    def grid(self) -> FiniteVolumeGrid: return self._grid
+    def vectorU(self): return self.u
+    def vectorF(self): return self.f
+    def vectorG(self): return self.g
+    def vectorH(self): return self.h
+
+    def size(self) -> int:
+        return int(self._grid.nx() / 2 ** self.n_coarsens)
+
+
+class FiniteVolumeNodeFactory:
+    """FiniteVolumeNodeFactory: the child geometry is computed inside the library
+    (midpoint halving, FiniteVolumeNodeFactory.cpp:15-66)."""
+
+
+class Mesh:
+    """Mesh<FiniteVolumePatch> (Mesh.hpp) backed by the library's flat quadtree."""
+
+    def __init__(self):
+        self._h = None
+        self.root_patch: Optional[FiniteVolumePatch] = None
+        self.patches: list = []
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib._LIB is not None:
+            _lib._LIB.ef_mesh_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def refineByFunction(self, fn: Callable[[float, float], bool], threshold: float, min_level: int,
+                         max_level: int, root_patch: FiniteVolumePatch,
+                         node_factory: Optional[FiniteVolumeNodeFactory] = None) -> "Mesh":
+        lib = _lib.load()
+        g = root_patch.grid()
+
+        def tramp(x, y, _ctx):
+            return 1 if fn(x, y) else 0
+        cb = _lib.REFINE_FN(tramp)
+        h = C.c_void_p()
+        check(lib.ef_mesh_create_refined(g.xLower(), g.xUpper(), g.yLower(), g.yUpper(), g.nx(), g.ny(),
+                                         int(min_level), int(max_level), cb, None, C.byref(h)))
+        self._adopt(h, root_patch)
+        return self
+
+    def uniform(self, level: int, root_patch: FiniteVolumePatch) -> "Mesh":
+        lib = _lib.load()
+        g = root_patch.grid()
+        h = C.c_void_p()
+        check(lib.ef_mesh_create_uniform(g.xLower(), g.xUpper(), g.yLower(), g.yUpper(), g.nx(), g.ny(),
+                                         int(level), C.byref(h)))
+        self._adopt(h, root_patch)
+        return self
+
+    def _adopt(self, h, root_patch):
+        if self._h is not None:
+            _lib.load().ef_mesh_destroy(self._h)
+        self._h = h
+        self.root_patch = root_patch
+        n = root_patch.grid().nx()
+        self.patches = []
+        for k in range(self.num_leaves()):
+            lvl, _, _, box = self.leaf(k)
+            self.patches.append(FiniteVolumePatch(FiniteVolumeGrid(n, box[0], box[1], n, box[2], box[3])))
+
+    def num_leaves(self) -> int:
+        v = C.c_int()
+        check(_lib.load().ef_mesh_num_leaves(self._h, C.byref(v)))
+        return v.value
+
+    def num_nodes(self) -> int:
+        v = C.c_int()
+        check(_lib.load().ef_mesh_num_nodes(self._h, C.byref(v)))
+        return v.value
+
+    def leaf(self, k: int):
+        lvl = C.c_int()
+        ix = C.c_longlong()
+        iy = C.c_longlong()
+        box = np.zeros(4)
+        check(_lib.load().ef_mesh_leaf(self._h, k, C.byref(lvl), C.byref(ix), C.byref(iy), dptr(box)))
+        return lvl.value, ix.value, iy.value, box
+
+    def leaf_quads(self):
+        return [self.leaf(k)[:3] for k in range(self.num_leaves())]
+
+    def iteratePatches(self, fn):
+        for p in self.patches:
+            fn(p)
+
+    def cell_centres(self):
+        """Leaf cell centres (x, y) in leaf order, cell j + i*n (HPSAlgorithm.hpp:241-249)."""
+        n = self.root_patch.grid().nx()
+        xs, ys = [], []
+        for p in self.patches:
+            g = p.grid()
+            X, Y = np.meshgrid(g.point(0, np.arange(n)), g.point(1, np.arange(n)), indexing="ij")
+            xs.append(X.ravel())
+            ys.append(Y.ravel())
+        return np.concatenate(xs), np.concatenate(ys)
+
+
+class HPSAlgorithm:
+    """HPSAlgorithm<FiniteVolumeGrid, FiniteVolumeSolver, FiniteVolumePatch, double> on one GPU."""
+
+    def __init__(self, mesh: Mesh, patch_solver: FiniteVolumeSolver, options: Optional[dict] = None):
+        self.mesh = mesh
+        self.patch_solver = patch_solver
+        self.options = {"cache-operators": False, "homogeneous-rhs": False}
+        if options:
+            self.options.update(options)
+        lib = _lib.load()
+        h = C.c_void_p()
+        check(lib.ef_hps_create(mesh.handle, _solver_code(patch_solver.solver_type),
+                                float(patch_solver.lambda_function(0, 0)), C.byref(h)))
+        self._h = h
+        nl, n, M, nb = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        check(lib.ef_hps_info(h, C.byref(nl), C.byref(n), C.byref(M), C.byref(nb)))
+        self.num_leaves, self.n, self.M, self.device_bytes = nl.value, n.value, M.value, nb.value
+        self._apply_options()
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib._LIB is not None:
+            _lib._LIB.ef_hps_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _apply_options(self):
+        lib = _lib.load()
+        for k in ("cache-operators", "homogeneous-rhs"):
+            v = self.options[k]
+            if not isinstance(v, bool):
+                raise TypeError(f"option {k!r} must be a bool")  # std::get<bool> in the reference
+            check(lib.ef_hps_set_option(self._h, k.encode(), int(v)))
+
+    def set_stream(self, cuda_stream_ptr: int):
+        check(_lib.load().ef_hps_set_stream(self._h, C.c_void_p(cuda_stream_ptr)))
+
+    # -- stages --------------------------------------------------------------------------------
+    def setupStage(self):
+        check(_lib.load().ef_hps_setup(self._h))
+
+    def buildStage(self):
+        self._apply_options()
+        check(_lib.load().ef_hps_build(self._h))
+
+    def upwardsStage(self, rhs, vectorized: bool = True, patch_callback: bool = False):
+        """``rhs`` is f(x, y) (sampled at leaf cell centres, HPSAlgorithm.hpp:241-249) or, with
+        ``patch_callback=True``, a function that sets ``patch.f`` on each leaf patch."""
+        self._apply_options()
+        n = self.n
+        if patch_callback:
+            for p in self.mesh.patches:
+                rhs(p)
+            f = np.concatenate([np.asarray(p.f, dtype=np.float64).ravel() for p in self.mesh.patches])
+        else:
+            X, Y = self.mesh.cell_centres()
+            if vectorized:
+                f = np.asarray(rhs(X, Y), dtype=np.float64)
+            else:
+                f = np.array([rhs(x, y) for x, y in zip(X, Y)], dtype=np.float64)
+            for k, p in enumerate(self.mesh.patches):
+                p.f = f[k * n * n:(k + 1) * n * n]
+        self.upwards_array(f)
+
+    def upwards_array(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        if f.size != self.num_leaves * self.n * self.n:
+            raise ValueError("f has the wrong size")
+        check(_lib.load().ef_hps_upwards(self._h, dptr(f)))
+
+    def boundary_points(self):
+        """Root face centres per side (HPSAlgorithm.hpp:375-400): lists of (x, y) arrays, WESN."""
+        g = self.mesh.root_patch.grid()
+        M = self.M
+        dx = (g.xUpper() - g.xLower()) / M
+        dy = (g.yUpper() - g.yLower()) / M
+        xc = (g.xLower() + dx / 2) + np.arange(M) * dx
+        yc = (g.yLower() + dy / 2) + np.arange(M) * dy
+        return [(np.full(M, g.xLower()), yc), (np.full(M, g.xUpper()), yc),
+                (xc, np.full(M, g.yLower())), (xc, np.full(M, g.yUpper()))]
+
+    def solveStage(self, bc, vectorized: bool = True, patch_callback: bool = False):
+        """``bc(side, x, y) -> (r, a, b)`` for a u + b du/dn = r on the root faces, or with
+        ``patch_callback=True`` a function given the root patch that sets ``root.g``."""
+        self._apply_options()
+        lib = _lib.load()
+        if patch_callback:
+            root = FiniteVolumePatch(FiniteVolumeGrid(self.M, *self._root_box()))
+            bc(root)
+            g = np.ascontiguousarray(root.g, dtype=np.float64)
+            if g.size != 4 * self.M:
+                raise ValueError("root g has the wrong size")
+            check(lib.ef_hps_solve_root_dirichlet(self._h, dptr(g)))
+        else:
+            r, a, b = [], [], []
+            for side, (x, y) in enumerate(self.boundary_points()):
+                if vectorized:
+                    rv, av, bv = bc(side, x, y)
+                    rv = np.broadcast_to(np.asarray(rv, dtype=np.float64), x.shape)
+                    av = np.broadcast_to(np.asarray(av, dtype=np.float64), x.shape)
+                    bv = np.broadcast_to(np.asarray(bv, dtype=np.float64), x.shape)
+                else:
+                    vals = [bc(side, xi, yi) for xi, yi in zip(x, y)]
+                    rv, av, bv = (np.array([v[k] for v in vals]) for k in range(3))
+                r.append(rv); a.append(av); b.append(bv)
+            self.solve_arrays(np.concatenate(a), np.concatenate(b), np.concatenate(r))
+        u = self.leaf_solution()
+        n2 = self.n * self.n
+        for k, p in enumerate(self.mesh.patches):
+            p.u = u[k * n2:(k + 1) * n2]
+
+    def solve_arrays(self, a, b, r):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        if not (a.size == b.size == r.size == 4 * self.M):
+            raise ValueError("boundary data must have 4*M entries")
+        check(_lib.load().ef_hps_solve(self._h, dptr(a), dptr(b), dptr(r)))
+
+    def _root_box(self):
+        g = self.mesh.root_patch.grid()
+        return g.xLower(), g.xUpper(), self.M, g.yLower(), g.yUpper()
+
+    # -- results ---------------------------------------------------------------------------------
+    def leaf_solution(self) -> np.ndarray:
+        u = np.empty(self.num_leaves * self.n * self.n)
+        check(_lib.load().ef_hps_get_leaf_u(self._h, dptr(u)))
+        return u
+
+    def root_T(self) -> np.ndarray:
+        m = 4 * self.M
+        T = np.empty((m, m))
+        check(_lib.load().ef_hps_get_root_T(self._h, dptr(T)))
+        return T
+
+    def root_h(self) -> np.ndarray:
+        h = np.empty(4 * self.M)
+        check(_lib.load().ef_hps_get_root_h(self._h, dptr(h)))
+        return h
+
+    def device_buffers(self):
+        ptrs = [C.c_void_p() for _ in range(5)]
+        check(_lib.load().ef_hps_device_buffers(self._h, *[C.byref(p) for p in ptrs]))
+        return [p.value for p in ptrs]  # f, u, a, b, r
+
+    def solve_device_async(self, b_is_zero: bool = True):
+        check(_lib.load().ef_hps_solve_device_async(self._h, int(bool(b_is_zero))))
+
+    def synchronize(self):
+        check(_lib.load().ef_hps_synchronize(self._h))

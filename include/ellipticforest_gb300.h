@@ -1,0 +1,122 @@
+/* C ABI of the GB300-native HPS solver (drop-in for EllipticForest's HPS path).
+ *
+ * Every entry point returns EF_OK (0) on success or a negative EF_ERR_* code; ef_last_error()
+ * gives the message of the last failure on the calling thread.  Plain pointers and sizes only.
+ *
+ * Data conventions (the reference's, src/HPSAlgorithm.hpp and
+ * src/Patches/FiniteVolume/FiniteVolumeSolver.cpp):
+ *   - leaves are numbered in pre-order (z-order: child 0 = SW, 1 = SE, 2 = NW, 3 = NE), the order
+ *     in which Quadtree::traversePreOrder visits them;
+ *   - a leaf's cell (i, j) (x-index i, y-index j) is stored at j + i*n (FiniteVolumeSolver.cpp:17);
+ *   - boundary data are WESN-stacked, each side M long (W and E along y, S and N along x).
+ *
+ * One ef_hps handle may be used by one host thread at a time.  Calls are synchronous to the host
+ * unless their name ends in _async.
+ */
+#ifndef ELLIPTICFOREST_GB300_H_
+#define ELLIPTICFOREST_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EF_OK 0
+#define EF_ERR_INVALID (-1)     /* bad argument or size mismatch                       */
+#define EF_ERR_CUDA (-2)        /* CUDA runtime error (message in ef_last_error)       */
+#define EF_ERR_NOMEM (-3)       /* device or host allocation failed                     */
+#define EF_ERR_SINGULAR (-4)    /* an LU factorisation met a zero pivot                 */
+#define EF_ERR_STATE (-5)       /* call out of order (e.g. solve before build)          */
+#define EF_ERR_UNSUPPORTED (-6) /* option or solver type not available in this build    */
+
+#define EF_SOLVER_FIVE_POINT 0  /* FiniteVolumeSolverType::FivePointStencil */
+#define EF_SOLVER_FISHPACK90 1  /* FiniteVolumeSolverType::FISHPACK90       */
+
+typedef struct ef_mesh ef_mesh;
+typedef struct ef_hps ef_hps;
+
+/* Refinement predicate of Mesh::refineByFunction: non-zero means "refine". */
+typedef int (*ef_refine_fn)(double x, double y, void* ctx);
+
+const char* ef_last_error(void);
+int ef_version(void);
+
+/* ---- Mesh ----------------------------------------------------------------------------------- */
+
+/* Mesh::refineByFunction (src/Mesh.hpp:111-180): uniform refinement to min_level, recursive
+ * refinement of every patch with a cell centre where fn is true (up to max_level), then 2:1
+ * corner balance.  nx, ny: cells per leaf patch side. */
+int ef_mesh_create_refined(double x_lower, double x_upper, double y_lower, double y_upper, int nx,
+                           int ny, int min_level, int max_level, ef_refine_fn fn, void* ctx,
+                           ef_mesh** out);
+/* Uniform quadtree of the given level (p4est_new_ext with fill_uniform, src/Mesh.hpp:131). */
+int ef_mesh_create_uniform(double x_lower, double x_upper, double y_lower, double y_upper, int nx,
+                           int ny, int level, ef_mesh** out);
+int ef_mesh_num_leaves(const ef_mesh* mesh, int* out);
+int ef_mesh_num_nodes(const ef_mesh* mesh, int* out);
+/* Leaf k: level, integer coordinates at that level and its box [xl, xu] x [yl, yu]
+ * (the node geometry of FiniteVolumeNodeFactory::createChildNode, NodeFactory.cpp:15-66). */
+int ef_mesh_leaf(const ef_mesh* mesh, int k, int* level, long long* ix, long long* iy,
+                 double box[4]);
+int ef_mesh_destroy(ef_mesh* mesh);
+
+/* ---- HPS solver (HPSAlgorithm<FiniteVolumeGrid, FiniteVolumeSolver, FiniteVolumePatch, double>)
+ * -------------------------------------------------------------------------------------------- */
+
+/* Creates the solver for `mesh` (copied) and allocates its device storage.
+ * solver_type EF_SOLVER_FISHPACK90: u_xx + u_yy + lambda u = f (FiniteVolumeSolver.cpp:224-290,
+ * lambda = lambda_function(0,0)). */
+int ef_hps_create(const ef_mesh* mesh, int solver_type, double lambda, ef_hps** out);
+/* Option keys of the reference: "cache-operators", "homogeneous-rhs" (HPSAlgorithm.hpp:134,532). */
+int ef_hps_set_option(ef_hps* hps, const char* key, int value);
+/* Use an external CUDA stream (cudaStream_t) for all work of this handle; NULL = default stream. */
+int ef_hps_set_stream(ef_hps* hps, void* cuda_stream);
+int ef_hps_info(const ef_hps* hps, int* num_leaves, int* leaf_n, int* root_M, long long* device_bytes);
+
+/* HPSAlgorithm::setupStage (HPSAlgorithm.hpp:91-106): nothing to do; validates the handle. */
+int ef_hps_setup(ef_hps* hps);
+/* HPSAlgorithm::buildStage (HPSAlgorithm.hpp:120-161): leaf DtN maps and all 4-to-1 merges. */
+int ef_hps_build(ef_hps* hps);
+/* HPSAlgorithm::upwardsStage (HPSAlgorithm.hpp:225-272) with the load f sampled at leaf cell
+ * centres, host array of num_leaves * n * n doubles. */
+int ef_hps_upwards(ef_hps* hps, const double* f_host);
+/* HPSAlgorithm::solveStage (HPSAlgorithm.hpp:343-445): a, b, r are the boundary condition
+ * a u + b du/dn = r sampled at the root face centres, host arrays of 4*M doubles (WESN). */
+int ef_hps_solve(ef_hps* hps, const double* a_host, const double* b_host, const double* r_host);
+/* HPSAlgorithm::solveStage(patch callback) (HPSAlgorithm.hpp:291-324): the root Dirichlet data
+ * g (4*M doubles, host) is given directly. */
+int ef_hps_solve_root_dirichlet(ef_hps* hps, const double* g_host);
+/* Leaf solutions u (num_leaves * n * n doubles) to host memory (patch.vectorU() of every leaf). */
+int ef_hps_get_leaf_u(ef_hps* hps, double* u_host);
+/* Root Dirichlet-to-Neumann matrix T (4M x 4M, row-major) and particular Neumann data h (4M). */
+int ef_hps_get_root_T(ef_hps* hps, double* T_host);
+int ef_hps_get_root_h(ef_hps* hps, double* h_host);
+int ef_hps_destroy(ef_hps* hps);
+
+/* Device-resident forms (no host copies; pointers stay valid for the handle's lifetime). */
+int ef_hps_device_buffers(ef_hps* hps, double** f_dev, double** u_dev, double** a_dev,
+                          double** b_dev, double** r_dev);
+/* upwards + root Dirichlet data + downwards + leaf solves on the resident buffers, without a host
+ * synchronisation.  b_is_zero != 0 asserts b == 0 everywhere (Dirichlet root data g = r / a). */
+int ef_hps_solve_device_async(ef_hps* hps, int b_is_zero);
+int ef_hps_synchronize(ef_hps* hps);
+
+/* ---- Single patch (FiniteVolumeSolver::buildD2N / solve / mapD2N) --------------------------- */
+
+/* FiniteVolumeSolver::buildD2N (FiniteVolumeSolver.cpp:355-455) for an n x n patch on
+ * [xl,xu] x [yl,yu]; T_host receives 4n x 4n doubles (row-major, WESN). */
+int ef_fv_build_d2n(int solver_type, int n, double x_lower, double x_upper, double y_lower,
+                    double y_upper, double lambda, double* T_host);
+/* FiniteVolumeSolver::solve (FiniteVolumeSolver.cpp:27-290): g (4n, WESN), f (n*n), u (n*n). */
+int ef_fv_solve(int solver_type, int n, double x_lower, double x_upper, double y_lower,
+                double y_upper, double lambda, const double* g_host, const double* f_host,
+                double* u_host);
+/* FiniteVolumeSolver::mapD2N (FiniteVolumeSolver.cpp:296-353): h (4n). */
+int ef_fv_map_d2n(int solver_type, int n, double x_lower, double x_upper, double y_lower,
+                  double y_upper, double lambda, const double* g_host, const double* f_host,
+                  double* h_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ELLIPTICFOREST_GB300_H_ */
