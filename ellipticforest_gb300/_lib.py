@@ -57,8 +57,15 @@ SIGNATURES = {
     "ef_hps_destroy": (C.c_int, [_vp]),
     "ef_hps_device_buffers": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
                                         C.POINTER(_vp), C.POINTER(_vp)]),
+    "ef_hps_load_device_async": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ef_hps_solve_device_async": (C.c_int, [_vp, C.c_int]),
     "ef_hps_synchronize": (C.c_int, [_vp]),
+    "ef_kernel_launches": (C.c_int, [C.POINTER(C.c_longlong)]),
+    "ef_hps_profile_enable": (C.c_int, [_vp, C.c_int]),
+    "ef_hps_profile_count": (C.c_int, [_vp, C.POINTER(C.c_int)]),
+    "ef_hps_profile_entry": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int, _dp, C.POINTER(C.c_longlong),
+                                       C.POINTER(C.c_longlong), _dp, _dp]),
+    "ef_hps_profile_reset": (C.c_int, [_vp]),
     "ef_fv_build_d2n": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                   C.c_double, _dp]),
     "ef_fv_solve": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,

@@ -339,6 +339,21 @@ int ef_hps_device_buffers(ef_hps* h, double** f, double** u, double** a, double*
     return EF_OK;
 }
 
+int ef_hps_load_device_async(ef_hps* h, const double* f, const double* a, const double* b,
+                             const double* r) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    efgb::Hps& H = *h->hps;
+    cudaStream_t s = H.stream();
+    const size_t nf = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();
+    const size_t m = 4 * size_t(H.root_M());
+    int st = EF_OK;
+    if (f) st = cuda_status(cudaMemcpyAsync(H.leaf_f(), f, nf * 8, cudaMemcpyDeviceToDevice, s), "load f");
+    if (!st && a) st = cuda_status(cudaMemcpyAsync(H.bc_a(), a, m * 8, cudaMemcpyDeviceToDevice, s), "load a");
+    if (!st && b) st = cuda_status(cudaMemcpyAsync(H.bc_b(), b, m * 8, cudaMemcpyDeviceToDevice, s), "load b");
+    if (!st && r) st = cuda_status(cudaMemcpyAsync(H.bc_r(), r, m * 8, cudaMemcpyDeviceToDevice, s), "load r");
+    return st;
+}
+
 int ef_hps_solve_device_async(ef_hps* h, int b_is_zero) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "solve before build stage");
@@ -352,6 +367,54 @@ int ef_hps_solve_device_async(ef_hps* h, int b_is_zero) {
 int ef_hps_synchronize(ef_hps* h) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     return cuda_status(cudaStreamSynchronize(h->hps->stream()), "synchronize");
+}
+
+int ef_kernel_launches(long long* count) {
+    if (!count) return fail(EF_ERR_INVALID, "null argument");
+    *count = efgb::g_kernel_launches.load();
+    return EF_OK;
+}
+
+int ef_hps_profile_enable(ef_hps* h, int on) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    h->hps->set_profiling(on != 0);
+    return EF_OK;
+}
+
+int ef_hps_profile_count(ef_hps* h, int* count) {
+    if (!h || !count) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        *count = int(h->hps->profile_read().size());
+        return EF_OK;
+    });
+}
+
+int ef_hps_profile_entry(ef_hps* h, int i, char* name, int name_len, double* ms, long long* launches,
+                         long long* calls, double* bytes, double* flops) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    return guarded([&] {
+        const auto& st = h->hps->profile_read();
+        if (i < 0 || i >= int(st.size())) return fail(EF_ERR_INVALID, "profile index out of range");
+        const auto& e = st[i];
+        if (name && name_len > 0) {
+            std::strncpy(name, e.name.c_str(), size_t(name_len) - 1);
+            name[name_len - 1] = 0;
+        }
+        if (ms) *ms = e.ms;
+        if (launches) *launches = e.launches;
+        if (calls) *calls = e.calls;
+        if (bytes) *bytes = e.bytes;
+        if (flops) *flops = e.flops;
+        return EF_OK;
+    });
+}
+
+int ef_hps_profile_reset(ef_hps* h) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    return guarded([&] {
+        h->hps->profile_reset();
+        return EF_OK;
+    });
 }
 
 int ef_fv_build_d2n(int solver_type, int n, double xl, double xu, double yl, double yu, double lambda,

@@ -75,8 +75,67 @@ Hps::Hps(const Mesh& mesh, int solver_type, double lambda, bool cache_operators)
 }
 
 Hps::~Hps() {
+    for (auto& m : marks_) { ev_free_.push_back(m.a); ev_free_.push_back(m.b); }
+    for (cudaEvent_t e : ev_free_) cudaEventDestroy(e);
     if (arena_) cudaFree(arena_);
     if (d_rootA_) cudaFree(d_rootA_);
+}
+
+cudaEvent_t Hps::ev_get() {
+    if (!ev_free_.empty()) {
+        cudaEvent_t e = ev_free_.back();
+        ev_free_.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    check(cudaEventCreate(&e), "cudaEventCreate");
+    return e;
+}
+
+void Hps::pb(const char* name) {
+    if (!prof_) return;
+    int idx = -1;
+    for (size_t i = 0; i < stats_.size(); ++i)
+        if (stats_[i].name == name) { idx = int(i); break; }
+    if (idx < 0) {
+        idx = int(stats_.size());
+        stats_.push_back(ProfStat{name});
+    }
+    open_stat_ = idx;
+    open_ev_ = ev_get();
+    open_launch0_ = g_kernel_launches.load();
+    check(cudaEventRecord(open_ev_, st_), "cudaEventRecord");
+}
+
+void Hps::pe(double bytes, double flops) {
+    if (!prof_ || open_stat_ < 0) return;
+    cudaEvent_t b = ev_get();
+    check(cudaEventRecord(b, st_), "cudaEventRecord");
+    marks_.push_back(Mark{open_stat_, open_ev_, b, g_kernel_launches.load() - open_launch0_, bytes, flops});
+    open_stat_ = -1;
+}
+
+const std::vector<Hps::ProfStat>& Hps::profile_read() {
+    check(cudaStreamSynchronize(st_), "profile sync");
+    for (auto& m : marks_) {
+        float ms = 0;
+        check(cudaEventElapsedTime(&ms, m.a, m.b), "cudaEventElapsedTime");
+        ProfStat& ps = stats_[m.stat];
+        ps.ms += ms;
+        ps.launches += m.launches;
+        ps.calls += 1;
+        ps.bytes += m.bytes;
+        ps.flops += m.flops;
+        ev_free_.push_back(m.a);
+        ev_free_.push_back(m.b);
+    }
+    marks_.clear();
+    return stats_;
+}
+
+void Hps::profile_reset() {
+    profile_read();
+    stats_.clear();
 }
 
 void Hps::plan() {
@@ -185,6 +244,7 @@ void Hps::allocate() {
                 nd.perm = cv.get<int>(4 * s);
                 nd.h = cv.get<double>(8 * s);
                 nd.w = cv.get<double>(4 * s);
+                nd.hd = cv.get<double>(4 * s);
                 nd.g = cv.get<double>(4 * size_t(nd.size));
             }
             for (int t = 0; t < nd.ncoarsen; ++t) {
@@ -210,12 +270,7 @@ void Hps::allocate() {
         d_items_solve_ = cv.get<LeafItem>(L);
         for (auto& g : groups_) {
             const int cnt = int(g.nodes.size());
-            const int per4 = (4 * g.s + 31) / 32, per8 = (8 * g.s + 31) / 32;
-            g.nwork4 = cnt * per4;
-            g.nwork8 = cnt * per8;
             g.d_items = cv.get<MergeItem>(cnt);
-            g.d_work4 = cv.get<RowWork>(g.nwork4);
-            g.d_work8 = cv.get<RowWork>(g.nwork8);
             g.d_X = cv.get<double*>(cnt);
             g.d_RHS = cv.get<double*>(cnt);
             g.d_H = cv.get<double*>(cnt);
@@ -308,7 +363,6 @@ void Hps::upload_tables() {
     for (auto& g : groups_) {
         const int cnt = int(g.nodes.size());
         std::vector<MergeItem> mi(cnt);
-        std::vector<RowWork> w4, w8;
         std::vector<double*> X(cnt), R(cnt), H(cnt), T(cnt);
         std::vector<int*> P(cnt), Q(cnt);
         for (int i = 0; i < cnt; ++i) {
@@ -323,14 +377,10 @@ void Hps::upload_tables() {
                 m.gc[c] = ch.g;
             }
             m.X = nd.X; m.piv = nd.piv; m.perm = nd.perm; m.RHS = nd.RHS; m.H = nd.H; m.T = nd.T;
-            m.h = nd.h; m.w = nd.w; m.gf = nd.gf;
+            m.h = nd.h; m.w = nd.w; m.gf = nd.gf; m.hd = nd.hd;
             X[i] = nd.X; R[i] = nd.RHS; H[i] = nd.H; T[i] = nd.T; P[i] = nd.piv; Q[i] = nd.perm;
-            for (int r = 0; r < 4 * g.s; r += 32) w4.push_back(RowWork{i, r});
-            for (int r = 0; r < 8 * g.s; r += 32) w8.push_back(RowWork{i, r});
         }
         check(cudaMemcpy(g.d_items, mi.data(), cnt * sizeof(MergeItem), cudaMemcpyHostToDevice), "items");
-        check(cudaMemcpy(g.d_work4, w4.data(), w4.size() * sizeof(RowWork), cudaMemcpyHostToDevice), "w4");
-        check(cudaMemcpy(g.d_work8, w8.data(), w8.size() * sizeof(RowWork), cudaMemcpyHostToDevice), "w8");
         check(cudaMemcpy(g.d_X, X.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "X");
         check(cudaMemcpy(g.d_RHS, R.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "RHS");
         check(cudaMemcpy(g.d_H, H.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "H");
@@ -372,7 +422,10 @@ void Hps::upload_tables() {
 }
 
 void Hps::build_leaf_types() {
+    pb("leaf_dtn");
     leaf_eigen(st_, LEAF_DTN_COLUMN, d_types_, d_items_dtn_, nitems_dtn_, n_);
+    const double n = n_;
+    pe(double(types_.size()) * 16 * n * n * 8, double(nitems_dtn_) * (6 * n * n * n + 8 * n * n));
 }
 
 void Hps::build() {
@@ -380,21 +433,36 @@ void Hps::build() {
     const int maxL = mesh_.max_level;
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         for (size_t k = 0; k < tsteps_.size(); ++k)
-            if (tsteps_[k].level == lvl + 1)
+            if (tsteps_[k].level == lvl + 1) {
+                const double nf = tsteps_[k].nf, cnt = tsteps_[k].count;
+                pb("coarsen_T");
                 coarsen_T(st_, tsteps_[k].d_in, tsteps_[k].d_out, tsteps_[k].count, tsteps_[k].nf);
+                pe(cnt * 8 * (16 * nf * nf + 4 * nf * nf), cnt * 4 * nf * nf * 10);
+            }
         for (auto& g : groups_) {
             if (g.level != lvl) continue;
             const int cnt = int(g.nodes.size()), s = g.s, m = 4 * s;
+            const double c = cnt, dm = m;
+            pb("gather_xht");
             merge_gather_xht(st_, g.d_items, cnt, s);
+            pe(c * 8 * (dm * dm + 2 * dm * dm + 4 * dm * dm) * 1.5, 0);
             check(cudaMemsetAsync(g.d_info, 0, cnt * sizeof(int), st_), "memset info");
+            pb("getrf");
             dgetrf_batched(st_, m, g.d_X, m, g.d_piv, g.d_info, cnt);
             piv_to_perm(st_, m, g.d_piv, g.d_perm, cnt);
+            pe(c * 8 * 2 * dm * dm, c * 2.0 / 3.0 * dm * dm * dm);
+            pb("gather_rhs");
             merge_gather_rhs(st_, g.d_items, cnt, s);
+            pe(c * 8 * (3 * dm * dm + dm * dm), 0);
+            pb("lu_solve");
             dlu_solve_permuted(st_, m, 3 * m, (const double* const*)g.d_X, m, g.d_RHS, 3 * m, cnt);
+            pe(c * 8 * (dm * dm + 2 * 3 * dm * dm), c * 2.0 * dm * dm * 3 * dm);
             // T = T_LHS + H S  (HPSAlgorithm.hpp:940-968), S = first 8s columns of RHS
+            pb("gemm_T");
             GemmArgs ga{(const double* const*)g.d_H, 0, m, (const double* const*)g.d_RHS, 0, 3 * m,
                         g.d_T, 0, 2 * m};
             dgemm_batched(st_, 2 * m, 2 * m, m, 1.0, ga, 1.0, cnt);
+            pe(c * 8 * (2 * dm * dm + 2 * dm * dm + 2 * 4 * dm * dm), c * 2.0 * (2 * dm) * (2 * dm) * dm);
         }
     }
     check(cudaGetLastError(), "build launch");
@@ -409,17 +477,29 @@ void Hps::build() {
 }
 
 void Hps::upwards() {
+    const double L = num_leaves(), n = n_;
+    pb("leaf_neumann");
     leaf_eigen(st_, LEAF_NEUMANN, d_types_, d_items_neu_, num_leaves(), n_);
+    pe(L * 8 * (n * n + 4 * n), L * (6 * n * n * n + 8 * n * n));
     if (homogeneous_) return;
     const int maxL = mesh_.max_level;
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         for (size_t k = 0; k < hsteps_.size(); ++k)
-            if (hsteps_[k].level == lvl + 1)
+            if (hsteps_[k].level == lvl + 1) {
+                pb("coarsen_h");
                 coarsen_vec(st_, hsteps_[k].d_in, hsteps_[k].d_out, hsteps_[k].count, hsteps_[k].nf);
+                pe(double(hsteps_[k].count) * 8 * 6 * hsteps_[k].nf, double(hsteps_[k].count) * 4 * hsteps_[k].nf);
+            }
         for (auto& g : groups_) {
             if (g.level != lvl) continue;
-            upward_w(st_, g.d_items, g.d_work4, g.nwork4, g.s);
-            upward_h(st_, g.d_items, g.d_work8, g.nwork8, g.s);
+            const double c = double(g.nodes.size()), s = g.s;
+            pb("upward_w");
+            upward_hdiff(st_, g.d_items, int(c), g.s);
+            upward_w(st_, g.d_items, int(c), g.s);
+            pe(c * 8 * (16 * s * s + 8 * s + 4 * s), c * 2 * 16 * s * s);
+            pb("upward_h");
+            upward_h(st_, g.d_items, int(c), g.s);
+            pe(c * 8 * (16 * s * s + 4 * s + 8 * s + 8 * s), c * 2 * 16 * s * s);
         }
     }
 }
@@ -428,9 +508,12 @@ void Hps::root_from_bc() {
     const int m = 4 * nodes_[0].nx;
     // The caller tells whether b is identically zero through bc_general_.
     if (!bc_general_) {
+        pb("root_diag");
         root_diag(st_, m, d_bca_, d_bcb_, d_bcr_, nodes_[0].h, nodes_[0].g);
+        pe(8.0 * 5 * m, 3.0 * m);
         return;
     }
+    pb("root_general");
     if (!d_rootA_) {
         const size_t bytes = align_up(size_t(m) * m * 8) + align_up(size_t(m) * 8) + 2 * align_up(size_t(m) * 4) +
                              align_up(sizeof(int)) + 4 * align_up(sizeof(void*));
@@ -460,21 +543,31 @@ void Hps::root_from_bc() {
     dlu_solve_permuted(st_, m, 1, (const double* const*)d_rootA_arr_, m, d_rootrhs_arr_, 1, 1);
     check(cudaMemcpyAsync(nodes_[0].g, d_rootrhs_, m * sizeof(double), cudaMemcpyDeviceToDevice, st_),
           "root g");
+    pe(8.0 * 3 * double(m) * m, 2.0 / 3.0 * double(m) * m * m + 2.0 * double(m) * m);
 }
 
 void Hps::downwards() {
     const int maxL = mesh_.max_level;
     for (int lvl = 0; lvl < maxL; ++lvl) {
         for (size_t k = 0; k < gsteps_.size(); ++k)
-            if (gsteps_[k].level == lvl)
+            if (gsteps_[k].level == lvl) {
+                pb("uncoarsen_g");
                 uncoarsen_vec(st_, gsteps_[k].d_in, gsteps_[k].d_out, gsteps_[k].count, gsteps_[k].nf);
+                pe(double(gsteps_[k].count) * 8 * 6 * gsteps_[k].nf, double(gsteps_[k].count) * 8 * gsteps_[k].nf);
+            }
         for (auto& g : groups_) {
             if (g.level != lvl) continue;
-            downward(st_, g.d_items, g.d_work4, g.nwork4, g.s, homogeneous_ ? 0 : 1);
+            const double c = double(g.nodes.size()), s = g.s;
+            pb("downward");
+            downward(st_, g.d_items, int(c), g.s, homogeneous_ ? 0 : 1);
+            pe(c * 8 * (32 * s * s + 8 * s + 4 * s + 16 * s), c * 2 * 32 * s * s);
         }
     }
     if (homogeneous_) fill_zero(st_, d_f_, (long long)num_leaves() * n_ * n_);
+    const double L = num_leaves(), n = n_;
+    pb("leaf_solve");
     leaf_eigen(st_, LEAF_SOLVE, d_types_, d_items_solve_, num_leaves(), n_);
+    pe(L * 8 * (2 * n * n + 4 * n), L * 8 * n * n * n);
 }
 
 void Hps::solve_async() {

@@ -32,7 +32,7 @@ struct NodeDev {
     double *T = nullptr, *Tc = nullptr;
     double *X = nullptr, *RHS = nullptr, *H = nullptr;
     int *piv = nullptr, *perm = nullptr;
-    double *h = nullptr, *hc = nullptr, *g = nullptr, *gf = nullptr, *w = nullptr;
+    double *h = nullptr, *hc = nullptr, *g = nullptr, *gf = nullptr, *w = nullptr, *hd = nullptr;
     std::vector<double*> Tsteps, hsteps, gsteps;  // intermediate (un)coarsening buffers
 };
 
@@ -40,8 +40,6 @@ struct Group {
     int level = 0, s = 0;
     std::vector<int> nodes;
     MergeItem* d_items = nullptr;
-    RowWork *d_work4 = nullptr, *d_work8 = nullptr;
-    int nwork4 = 0, nwork8 = 0;
     double** d_X = nullptr;
     double** d_RHS = nullptr;
     double** d_H = nullptr;
@@ -110,7 +108,18 @@ public:
     double build_flops() const;
     double solve_bytes() const;
     double solve_flops() const;
-    int kernel_launches_per_solve() const { return launches_per_solve_; }
+
+    // Section profiler: CUDA events on this handle's stream around every kernel family, with the
+    // algorithmic bytes and flops each section moves/performs.
+    struct ProfStat {
+        std::string name;
+        double ms = 0;
+        long long launches = 0, calls = 0;
+        double bytes = 0, flops = 0;
+    };
+    void set_profiling(bool on) { prof_ = on; }
+    const std::vector<ProfStat>& profile_read();  // synchronises the stream
+    void profile_reset();
 
 private:
     void plan();
@@ -154,7 +163,23 @@ private:
 
     bool built_ = false;
     int singular_ = 0;
-    int launches_per_solve_ = 0;
+
+    struct Mark {
+        int stat;
+        cudaEvent_t a, b;
+        long long launches;
+        double bytes, flops;
+    };
+    bool prof_ = false;
+    std::vector<ProfStat> stats_;
+    std::vector<Mark> marks_;
+    std::vector<cudaEvent_t> ev_free_;
+    int open_stat_ = -1;
+    cudaEvent_t open_ev_ = nullptr;
+    long long open_launch0_ = 0;
+    cudaEvent_t ev_get();
+    void pb(const char* name);                 // begin section
+    void pe(double bytes, double flops);       // end section
 };
 
 }  // namespace efgb

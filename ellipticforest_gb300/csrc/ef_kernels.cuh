@@ -19,9 +19,14 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <cstdint>
 
 namespace efgb {
+
+// Number of kernels this library has launched (all handles, all streams).
+extern std::atomic<long long> g_kernel_launches;
 
 // ------------------------------------------------------------------------------------------------
 // Batched FP64 dense linear algebra (pointer arrays, uniform shapes and offsets per launch)
@@ -91,6 +96,7 @@ struct MergeItem {
     double* T;            // 8s x 8s, WESN
     const double* hc[4];  // children's (coarsened) h, 4s
     double* h;            // own h, 8s
+    double* hd;           // 4s, interface differences of the children's h
     double* w;            // 4s
     const double* gf;     // own full-size g, 8s
     double* gc[4];        // children's g (at coarsened size), 4s
@@ -108,17 +114,14 @@ void coarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout,
 // Per-side coarse-to-fine interpolation of g (4nc -> 4nf).
 void uncoarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf);
 
-struct RowWork {
-    int item;
-    int row0;
-};
-// w = X^{-1} hdiff, hdiff gathered from the children (upward, step 1).
-void upward_w(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s);
-// h = H w + h_ext (upward, step 2).
-void upward_h(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s);
+// hdiff = h_upper - h_lower gathered from the children (upward, step 1).
+void upward_hdiff(cudaStream_t st, const MergeItem* items, int nitems, int s);
+// w = X^{-1} hdiff (upward, step 2): one warp per row, streamed double2 loads.
+void upward_w(cudaStream_t st, const MergeItem* items, int nitems, int s);
+// h = H w + h_ext (upward, step 3).
+void upward_h(cudaStream_t st, const MergeItem* items, int nitems, int s);
 // u_Gamma = S gf (+ w) and scatter of the children's Dirichlet data (downward).
-void downward(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s,
-              int add_w);
+void downward(cudaStream_t st, const MergeItem* items, int nitems, int s, int add_w);
 
 // Root Dirichlet data.  diag: g = (r - b.h) / a.  general: A = diag(a) + diag(b) T; rhs = r - b.h
 void root_diag(cudaStream_t st, int m, const double* a, const double* b, const double* r,

@@ -119,6 +119,7 @@ void launch_leaf(cudaStream_t st, const LeafType* types, const LeafItem* items, 
         configured = true;
     }
     k_leaf_eigen<MODE><<<nitems, 256, smem, st>>>(types, items);
+    ++g_kernel_launches;
 }
 
 }  // namespace

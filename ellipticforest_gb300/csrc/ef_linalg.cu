@@ -10,6 +10,8 @@
 
 namespace efgb {
 
+std::atomic<long long> g_kernel_launches{0};
+
 namespace {
 
 constexpr int TM = 64, TN = 64, TK = 16;
@@ -240,6 +242,7 @@ void dgemm_batched(cudaStream_t st, int M, int N, int K, double alpha, const Gem
         const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
         dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nb);
         k_dgemm<<<grid, 256, 0, st>>>(M, N, K, alpha, a, beta, b0);
+        ++g_kernel_launches;
     }
 }
 
@@ -249,9 +252,11 @@ void dgetrf_batched(cudaStream_t st, int n, double* const* A, int lda, int* cons
         const int jb = (n - k < NB) ? n - k : NB;
         const int threads = (n - k >= 512) ? 1024 : 256;
         k_getf2_panel<<<batch, threads, 0, st>>>(n, k, jb, A, lda, piv, info);
+        ++g_kernel_launches;
         if (n - jb > 0) {
             dim3 g((n - jb + 255) / 256, batch);
             k_laswp_outside<<<g, 256, 0, st>>>(n, k, jb, A, lda, piv);
+            ++g_kernel_launches;
         }
         const int rest = n - k - jb;
         if (rest > 0) {
@@ -270,6 +275,7 @@ void dgetrf_batched(cudaStream_t st, int n, double* const* A, int lda, int* cons
 
 void piv_to_perm(cudaStream_t st, int n, int* const* piv, int* const* perm, int batch) {
     k_piv_to_perm<<<batch, 256, n * sizeof(int), st>>>(n, piv, perm);
+    ++g_kernel_launches;
 }
 
 void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* LU, int lda,
@@ -279,6 +285,7 @@ void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* L
         const int jb = (n - k < NB) ? n - k : NB;
         dim3 g((nrhs + 255) / 256, batch);
         k_trsm_block<true><<<g, 256, 0, st>>>(k, jb, LU, lda, B, ldb, k, 0, nrhs);
+        ++g_kernel_launches;
         const int rest = n - k - jb;
         if (rest > 0) {
             GemmArgs ga{LU, (long long)(k + jb) * lda + k, lda,
@@ -293,6 +300,7 @@ void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* L
         const int jb = (n - k < NB) ? n - k : NB;
         dim3 g((nrhs + 255) / 256, batch);
         k_trsm_block<false><<<g, 256, 0, st>>>(k, jb, LU, lda, B, ldb, k, 0, nrhs);
+        ++g_kernel_launches;
         if (k > 0) {
             GemmArgs ga{LU, (long long)k, lda,
                         (const double* const*)B, (long long)k * ldb, ldb,

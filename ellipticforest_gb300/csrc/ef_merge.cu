@@ -169,7 +169,7 @@ __global__ void k_uncoarsen_vec(const double* const* vin, double* const* vout, i
     }
 }
 
-constexpr int ROWS_PER_CTA = 32;  // 8 warps x 4 rows
+constexpr int WARPS_PER_CTA = 8;  // one matrix row per warp
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -177,91 +177,112 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_upward_w(const MergeItem* __restrict__ items,
-                                                  const RowWork* __restrict__ work, int s) {
-    const RowWork wk = work[blockIdx.x];
-    const MergeItem& it = items[wk.item];
-    extern __shared__ double hd[];
-    const int m4 = 4 * s, m12 = 12 * s;
-    for (int r = threadIdx.x; r < m4; r += blockDim.x) {
-        const int I = r / s, o = r - I * s;
-        // hDiff = h_upper - h_lower (HPSAlgorithm.hpp:1061-1081)
-        hd[r] = it.hc[upper_child(I)][q_upper(I, o, s)] - it.hc[lower_child(I)][q_lower(I, o, s)];
+// Warp dot product of a streamed matrix row segment with a vector read through L1.
+// VEC: both pointers 16-byte aligned and len even -> double2 loads, four independent chains.
+template <bool VEC>
+__device__ __forceinline__ double warp_dot(const double* __restrict__ row, const double* __restrict__ x,
+                                           int len, int lane) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (VEC) {
+        const double2* r2 = reinterpret_cast<const double2*>(row);
+        const double2* x2 = reinterpret_cast<const double2*>(x);
+        const int n2 = len >> 1;
+        int i = lane;
+        for (; i + 96 < n2; i += 128) {
+            const double2 m0 = __ldcs(r2 + i), m1 = __ldcs(r2 + i + 32);
+            const double2 m2 = __ldcs(r2 + i + 64), m3 = __ldcs(r2 + i + 96);
+            const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + 32);
+            const double2 v2 = __ldg(x2 + i + 64), v3 = __ldg(x2 + i + 96);
+            a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
+            a1 = fma(m1.x, v1.x, a1); a1 = fma(m1.y, v1.y, a1);
+            a2 = fma(m2.x, v2.x, a2); a2 = fma(m2.y, v2.y, a2);
+            a3 = fma(m3.x, v3.x, a3); a3 = fma(m3.y, v3.y, a3);
+        }
+        for (; i < n2; i += 32) {
+            const double2 m0 = __ldcs(r2 + i), v0 = __ldg(x2 + i);
+            a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
+        }
+    } else {
+        int i = lane;
+        for (; i + 96 < len; i += 128) {
+            a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
+            a1 = fma(__ldcs(row + i + 32), __ldg(x + i + 32), a1);
+            a2 = fma(__ldcs(row + i + 64), __ldg(x + i + 64), a2);
+            a3 = fma(__ldcs(row + i + 96), __ldg(x + i + 96), a3);
+        }
+        for (; i < len; i += 32) a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = 0; k < ROWS_PER_CTA / 8; ++k) {
-        const int r = wk.row0 + wid * (ROWS_PER_CTA / 8) + k;
-        if (r >= m4) break;
-        const double* row = it.RHS + (long long)r * m12 + 8 * s;  // X^{-1} block
-        double acc = 0.0;
-        for (int c = lane; c < m4; c += 32) acc = fma(row[c], hd[c], acc);
-        acc = warp_sum(acc);
-        if (lane == 0) it.w[r] = acc;
-    }
+    return warp_sum((a0 + a1) + (a2 + a3));
 }
 
-__global__ void __launch_bounds__(256) k_upward_h(const MergeItem* __restrict__ items,
-                                                  const RowWork* __restrict__ work, int s) {
-    const RowWork wk = work[blockIdx.x];
-    const MergeItem& it = items[wk.item];
-    extern __shared__ double wv[];
+// hDiff = h_upper - h_lower per interface point (HPSAlgorithm.hpp:1061-1081)
+__global__ void k_hdiff(const MergeItem* __restrict__ items, int s) {
+    const long long m4 = 4LL * s;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (e >= m4) return;
+    const MergeItem& it = items[b];
+    const int r = int(e), I = r / s, o = r - I * s;
+    it.hd[r] = it.hc[upper_child(I)][q_upper(I, o, s)] - it.hc[lower_child(I)][q_lower(I, o, s)];
+}
+
+// w = X^{-1} hDiff (the X^{-1} block of RHS, columns [8s, 12s))
+template <bool VEC>
+__global__ void __launch_bounds__(256) k_gemv_w(const MergeItem* __restrict__ items, int s, long long nrows) {
+    const int lane = threadIdx.x & 31;
+    const long long g = blockIdx.x * (long long)WARPS_PER_CTA + (threadIdx.x >> 5);
+    if (g >= nrows) return;
+    const int m4 = 4 * s;
+    const int item = int(g / m4), r = int(g - (long long)item * m4);
+    const MergeItem& it = items[item];
+    const double acc = warp_dot<VEC>(it.RHS + (long long)r * (12LL * s) + 8 * s, it.hd, m4, lane);
+    if (lane == 0) it.w[r] = acc;
+}
+
+// h = H w + h_update (HPSAlgorithm.hpp:1098-1117); only the two interface blocks adjacent to the
+// row's child are non-zero; rows are already in WESN order
+template <bool VEC>
+__global__ void __launch_bounds__(256) k_gemv_h(const MergeItem* __restrict__ items, int s, long long nrows) {
+    const int lane = threadIdx.x & 31;
+    const long long g = blockIdx.x * (long long)WARPS_PER_CTA + (threadIdx.x >> 5);
+    if (g >= nrows) return;
+    const int m8 = 8 * s;
+    const int item = int(g / m8), p = int(g - (long long)item * m8);
+    const MergeItem& it = items[item];
+    int c, q, Ia, Ib;
+    ext_map(p, s, c, q);
+    child_ifaces(c, Ia, Ib);
+    const double* row = it.H + (long long)p * (4LL * s);
+    const double acc = warp_dot<VEC>(row + Ia * s, it.w + Ia * s, s, lane) +
+                       warp_dot<VEC>(row + Ib * s, it.w + Ib * s, s, lane);
+    if (lane == 0) it.h[p] = acc + it.hc[c][q];
+}
+
+// u_Gamma = S g + w (HPSAlgorithm.hpp:1197-1204) scattered to the children's interface data; the
+// first CTAs also copy the exterior data of the children (HPSAlgorithm.hpp:1214-1227)
+template <bool VEC>
+__global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__ items, int s,
+                                                   long long nrows, int nitems, int add_w) {
     const int m4 = 4 * s, m8 = 8 * s;
-    for (int r = threadIdx.x; r < m4; r += blockDim.x) wv[r] = it.w[r];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = 0; k < ROWS_PER_CTA / 8; ++k) {
-        const int p = wk.row0 + wid * (ROWS_PER_CTA / 8) + k;
-        if (p >= m8) break;
+    const long long ext = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (ext < (long long)nitems * m8) {
+        const int item = int(ext / m8), p = int(ext - (long long)item * m8);
+        const MergeItem& it = items[item];
         int c, q;
         ext_map(p, s, c, q);
-        int Ia, Ib;
-        child_ifaces(c, Ia, Ib);
-        const double* row = it.H + (long long)p * m4;
-        double acc = 0.0;
-        for (int o = lane; o < s; o += 32) {
-            acc = fma(row[Ia * s + o], wv[Ia * s + o], acc);
-            acc = fma(row[Ib * s + o], wv[Ib * s + o], acc);
-        }
-        acc = warp_sum(acc);
-        // h_tau = H w + h_update (HPSAlgorithm.hpp:1098-1117), already in WESN order
-        if (lane == 0) it.h[p] = acc + it.hc[c][q];
+        it.gc[c][q] = it.gf[p];
     }
-}
-
-__global__ void __launch_bounds__(256) k_downward(const MergeItem* __restrict__ items,
-                                                  const RowWork* __restrict__ work, int s,
-                                                  int add_w) {
-    const RowWork wk = work[blockIdx.x];
-    const MergeItem& it = items[wk.item];
-    extern __shared__ double gs[];
-    const int m4 = 4 * s, m8 = 8 * s, m12 = 12 * s;
-    for (int p = threadIdx.x; p < m8; p += blockDim.x) {
-        const double v = it.gf[p];
-        gs[p] = v;
-        if (wk.row0 == 0) {
-            // exterior Dirichlet data of the children (HPSAlgorithm.hpp:1214-1227)
-            int c, q;
-            ext_map(p, s, c, q);
-            it.gc[c][q] = v;
-        }
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = 0; k < ROWS_PER_CTA / 8; ++k) {
-        const int r = wk.row0 + wid * (ROWS_PER_CTA / 8) + k;
-        if (r >= m4) break;
-        const double* row = it.RHS + (long long)r * m12;  // S block
-        double acc = 0.0;
-        for (int c = lane; c < m8; c += 32) acc = fma(row[c], gs[c], acc);
-        acc = warp_sum(acc);
-        if (lane == 0) {
-            // u_Gamma = S g + w (HPSAlgorithm.hpp:1197-1204)
-            const double u = add_w ? acc + it.w[r] : acc;
-            const int I = r / s, o = r - I * s;
-            it.gc[lower_child(I)][q_lower(I, o, s)] = u;
-            it.gc[upper_child(I)][q_upper(I, o, s)] = u;
-        }
+    const int lane = threadIdx.x & 31;
+    const long long g = blockIdx.x * (long long)WARPS_PER_CTA + (threadIdx.x >> 5);
+    if (g >= nrows) return;
+    const int item = int(g / m4), r = int(g - (long long)item * m4);
+    const MergeItem& it = items[item];
+    const double acc = warp_dot<VEC>(it.RHS + (long long)r * (12LL * s), it.gf, m8, lane);
+    if (lane == 0) {
+        const double u = add_w ? acc + it.w[r] : acc;
+        const int I = r / s, o = r - I * s;
+        it.gc[lower_child(I)][q_lower(I, o, s)] = u;
+        it.gc[upper_child(I)][q_upper(I, o, s)] = u;
     }
 }
 
@@ -306,74 +327,96 @@ inline int grid_for(long long tot, int per_item_items) {
     return int(b);
 }
 
-void set_smem(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
-}
-
 }  // namespace
 
 void merge_gather_xht(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     const long long tot = 16LL * s * s + 32LL * s * s + 64LL * s * s;
     dim3 g(grid_for(tot, nitems), nitems);
     k_gather_xht<<<g, 256, 0, st>>>(items, s);
+    ++g_kernel_launches;
 }
 
 void merge_gather_rhs(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     const long long tot = 48LL * s * s;
     dim3 g(grid_for(tot, nitems), nitems);
     k_gather_rhs<<<g, 256, 0, st>>>(items, s);
+    ++g_kernel_launches;
 }
 
 void coarsen_T(cudaStream_t st, const double* const* Tin, double* const* Tout, int nitems, int nf) {
     const long long tot = 4LL * nf * 4LL * nf / 4;
     dim3 g(grid_for(tot, nitems), nitems);
     k_coarsen_T<<<g, 256, 0, st>>>(Tin, Tout, nf);
+    ++g_kernel_launches;
 }
 
 void coarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf) {
     dim3 g((2 * nf + 255) / 256, nitems);
     k_coarsen_vec<<<g, 256, 0, st>>>(vin, vout, nf);
+    ++g_kernel_launches;
 }
 
 void uncoarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf) {
     dim3 g((4 * nf + 255) / 256, nitems);
     k_uncoarsen_vec<<<g, 256, 0, st>>>(vin, vout, nf);
+    ++g_kernel_launches;
 }
 
-void upward_w(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s) {
-    const size_t smem = size_t(4) * s * sizeof(double);
-    set_smem((const void*)k_upward_w, smem);
-    k_upward_w<<<nwork, 256, smem, st>>>(items, work, s);
+void upward_hdiff(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+    dim3 g((4 * s + 255) / 256, nitems);
+    k_hdiff<<<g, 256, 0, st>>>(items, s);
+    ++g_kernel_launches;
 }
 
-void upward_h(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s) {
-    const size_t smem = size_t(4) * s * sizeof(double);
-    set_smem((const void*)k_upward_h, smem);
-    k_upward_h<<<nwork, 256, smem, st>>>(items, work, s);
+void upward_w(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+    const long long rows = (long long)nitems * 4 * s;
+    const unsigned blocks = unsigned((rows + WARPS_PER_CTA - 1) / WARPS_PER_CTA);
+    if (s % 2 == 0) k_gemv_w<true><<<blocks, 256, 0, st>>>(items, s, rows);
+    else k_gemv_w<false><<<blocks, 256, 0, st>>>(items, s, rows);
+    ++g_kernel_launches;
 }
 
-void downward(cudaStream_t st, const MergeItem* items, const RowWork* work, int nwork, int s, int add_w) {
-    const size_t smem = size_t(8) * s * sizeof(double);
-    set_smem((const void*)k_downward, smem);
-    k_downward<<<nwork, 256, smem, st>>>(items, work, s, add_w);
+void upward_h(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+    const long long rows = (long long)nitems * 8 * s;
+    const unsigned blocks = unsigned((rows + WARPS_PER_CTA - 1) / WARPS_PER_CTA);
+    if (s % 2 == 0) k_gemv_h<true><<<blocks, 256, 0, st>>>(items, s, rows);
+    else k_gemv_h<false><<<blocks, 256, 0, st>>>(items, s, rows);
+    ++g_kernel_launches;
+}
+
+void downward(cudaStream_t st, const MergeItem* items, int nitems, int s, int add_w) {
+    const long long rows = (long long)nitems * 4 * s;
+    // enough CTAs for the rows (one per warp) and for the exterior copy (one element per thread)
+    long long blocks = (rows + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const long long eblocks = ((long long)nitems * 8 * s + 255) / 256;
+    if (eblocks > blocks) blocks = eblocks;
+    if (s % 2 == 0) k_gemv_down<true><<<unsigned(blocks), 256, 0, st>>>(items, s, rows, nitems, add_w);
+    else k_gemv_down<false><<<unsigned(blocks), 256, 0, st>>>(items, s, rows, nitems, add_w);
+    ++g_kernel_launches;
 }
 
 void root_diag(cudaStream_t st, int m, const double* a, const double* b, const double* r,
                const double* h, double* g) {
     k_root_diag<<<(m + 255) / 256, 256, 0, st>>>(m, a, b, r, h, g);
+    ++g_kernel_launches;
 }
 
 void root_assemble(cudaStream_t st, int m, const double* a, const double* b, const double* T, double* A) {
     k_root_assemble<<<grid_for((long long)m * m, 1), 256, 0, st>>>(m, a, b, T, A);
+    ++g_kernel_launches;
 }
 
 void root_rhs(cudaStream_t st, int m, const double* b, const double* r, const double* h,
               const int* perm, double* rhs) {
     k_root_rhs<<<(m + 255) / 256, 256, 0, st>>>(m, b, r, h, perm, rhs);
+    ++g_kernel_launches;
 }
 
 void fill_zero(cudaStream_t st, double* p, long long n) {
-    if (n > 0) k_fill_zero<<<grid_for(n, 1), 256, 0, st>>>(p, n);
+    if (n > 0) {
+        k_fill_zero<<<grid_for(n, 1), 256, 0, st>>>(p, n);
+        ++g_kernel_launches;
+    }
 }
 
 }  // namespace efgb

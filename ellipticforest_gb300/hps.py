@@ -231,6 +231,12 @@ class Mesh:
         return np.concatenate(xs), np.concatenate(ys)
 
 
+def kernel_launches() -> int:
+    v = C.c_longlong()
+    check(_lib.load().ef_kernel_launches(C.byref(v)))
+    return v.value
+
+
 class HPSAlgorithm:
     """HPSAlgorithm<FiniteVolumeGrid, FiniteVolumeSolver, FiniteVolumePatch, double> on one GPU."""
 
@@ -377,6 +383,33 @@ class HPSAlgorithm:
         ptrs = [C.c_void_p() for _ in range(5)]
         check(_lib.load().ef_hps_device_buffers(self._h, *[C.byref(p) for p in ptrs]))
         return [p.value for p in ptrs]  # f, u, a, b, r
+
+    def profile_enable(self, on: bool = True):
+        check(_lib.load().ef_hps_profile_enable(self._h, int(on)))
+
+    def profile_reset(self):
+        check(_lib.load().ef_hps_profile_reset(self._h))
+
+    def profile(self) -> dict:
+        """{section: {ms, launches, calls, bytes, flops}} accumulated since the last reset."""
+        lib = _lib.load()
+        n = C.c_int()
+        check(lib.ef_hps_profile_count(self._h, C.byref(n)))
+        out = {}
+        for i in range(n.value):
+            name = C.create_string_buffer(64)
+            ms, by, fl = C.c_double(), C.c_double(), C.c_double()
+            la, ca = C.c_longlong(), C.c_longlong()
+            check(lib.ef_hps_profile_entry(self._h, i, name, 64, C.byref(ms), C.byref(la), C.byref(ca),
+                                           C.byref(by), C.byref(fl)))
+            out[name.value.decode()] = {"ms": ms.value, "launches": la.value, "calls": ca.value,
+                                        "bytes": by.value, "flops": fl.value}
+        return out
+
+    def load_device_async(self, f_ptr=None, a_ptr=None, b_ptr=None, r_ptr=None):
+        """Device-to-device copy of new inputs (raw device pointers) into the resident buffers."""
+        v = lambda p: C.c_void_p(p) if p else None
+        check(_lib.load().ef_hps_load_device_async(self._h, v(f_ptr), v(a_ptr), v(b_ptr), v(r_ptr)))
 
     def solve_device_async(self, b_is_zero: bool = True):
         check(_lib.load().ef_hps_solve_device_async(self._h, int(bool(b_is_zero))))

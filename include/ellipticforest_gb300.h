@@ -95,10 +95,27 @@ int ef_hps_destroy(ef_hps* hps);
 /* Device-resident forms (no host copies; pointers stay valid for the handle's lifetime). */
 int ef_hps_device_buffers(ef_hps* hps, double** f_dev, double** u_dev, double** a_dev,
                           double** b_dev, double** r_dev);
+/* Device-to-device copy of new inputs into the resident buffers on the handle's stream; any
+ * pointer may be NULL (that input is kept).  f: num_leaves*n*n, a/b/r: 4*M doubles. */
+int ef_hps_load_device_async(ef_hps* hps, const double* f_dev, const double* a_dev,
+                             const double* b_dev, const double* r_dev);
 /* upwards + root Dirichlet data + downwards + leaf solves on the resident buffers, without a host
  * synchronisation.  b_is_zero != 0 asserts b == 0 everywhere (Dirichlet root data g = r / a). */
 int ef_hps_solve_device_async(ef_hps* hps, int b_is_zero);
 int ef_hps_synchronize(ef_hps* hps);
+
+/* ---- Instrumentation (the reference's stage timers, EllipticForestApp.hpp:39-137) ------------ */
+
+/* Kernels launched by this library so far (all handles). */
+int ef_kernel_launches(long long* count);
+/* Per-section CUDA-event timing on the handle's stream (off by default).  A section is one kernel
+ * family of one stage step, e.g. "downward" or "leaf_solve"; bytes and flops are the section's
+ * algorithmic traffic and FP64 operations. */
+int ef_hps_profile_enable(ef_hps* hps, int on);
+int ef_hps_profile_count(ef_hps* hps, int* count);
+int ef_hps_profile_entry(ef_hps* hps, int i, char* name, int name_len, double* ms,
+                         long long* launches, long long* calls, double* bytes, double* flops);
+int ef_hps_profile_reset(ef_hps* hps);
 
 /* ---- Single patch (FiniteVolumeSolver::buildD2N / solve / mapD2N) --------------------------- */
 

@@ -13,7 +13,8 @@ It restates, in numpy (FP64), the reference's algorithm step for step:
   boundary rows ``cC -= c_side`` and ``f += -2 c_side g``), the FISHPACK90 branch ``:224-290``
   (same discrete system with alpha = beta = 1 and ``lambda = lambda_function(0,0)``; the FISHPACK90
   ``hstcrt_`` dependency is not vendored in the reference, so its cyclic-reduction solver is
-  replaced by a dense LU of the identical 5-point system), ``mapD2N`` ``:296-353``, ``buildD2N``
+  replaced by the LAPACK dgesv inverse of the identical 5-point system), ``mapD2N`` ``:296-353``,
+  ``buildD2N``
   ``:355-455`` (the ``#else`` branch: 4n unit Dirichlet solves) and ``particularNeumannData``
   ``:457-462``.
 * Interpolation operators -- ``src/SpecialMatrices.hpp:93-173``.
@@ -239,10 +240,11 @@ def boundary_rhs(grid: FiniteVolumeGrid, g: np.ndarray, cW, cE, cS, cN) -> np.nd
 class FiniteVolumeSolver:
     """Restatement of FiniteVolumeSolver (FiniteVolumeSolver.hpp:53-162).
 
-    The dense 5-point matrix for a grid is LU-factored once and kept (keyed by the grid and the
-    solver type); each call then does the triangular solves.  The reference refactors for every
-    call (PETSc ``MatLUFactor`` per solve, or one ``hstcrt_`` per solve); the solution of the same
-    linear system is the same up to roundoff.
+    The dense 5-point matrix for a grid is inverted once with LAPACK dgesv (numpy) and kept (keyed
+    by the grid and the solver type); each call applies the inverse.  The reference refactors for
+    every call (PETSc ``MatLUFactor`` per solve, or one ``hstcrt_`` per solve); the solution of the
+    same linear system is the same up to roundoff.  Every LAPACK/BLAS call of the oracle goes
+    through numpy's library, so the CPU timings see one BLAS thread pool as the reference does.
     """
 
     def __init__(self, alpha_function=None, beta_function=None, lambda_function=None, rhs_function=None,
@@ -276,18 +278,18 @@ class FiniteVolumeSolver:
         else:
             A, cW, cE, cS, cN = five_point_matrix(grid, self.alpha_function, self.beta_function,
                                                   self.lambda_function)
-        lu = sla.lu_factor(A, check_finite=False)
-        entry = (lu, cW, cE, cS, cN)
+        Ainv = np.linalg.solve(A, np.eye(A.shape[0]))
+        entry = (Ainv, cW, cE, cS, cN)
         self._factor_cache[key] = entry
         return entry
 
     def solve(self, grid: FiniteVolumeGrid, dirichlet_data, rhs_data) -> np.ndarray:
         """FiniteVolumeSolver.cpp:27-290: u = A^{-1} (f + f_boundary(g)); several columns allowed."""
-        lu, cW, cE, cS, cN = self._operator(grid)
+        Ainv, cW, cE, cS, cN = self._operator(grid)
         f = np.asarray(rhs_data, dtype=np.float64)
         g = np.asarray(dirichlet_data, dtype=np.float64)
         rhs = f + boundary_rhs(grid, g, cW, cE, cS, cN)
-        return sla.lu_solve(lu, rhs, check_finite=False)
+        return Ainv @ rhs
 
     def mapD2N(self, grid: FiniteVolumeGrid, dirichlet_data, rhs_data) -> np.ndarray:
         """FiniteVolumeSolver.cpp:296-353: h_W = (2/dx)(u_W - g_W), h_E = -(2/dx)(u_E - g_E), ..."""
@@ -701,6 +703,26 @@ class HPSAlgorithm:
             return 1
 
         self.mesh.quadtree.split(leaf, family)
+
+    def upwards_with_data(self, f_all: np.ndarray):
+        """upwardsStage with the load already sampled: f_all holds every leaf's f in pre-order leaf
+        order (the values the rhs callback of HPSAlgorithm.hpp:241-249 would produce)."""
+        leaves = self.mesh.quadtree.leaves()
+        nn = f_all.size // len(leaves)
+        data = {id(nd.data): f_all[k * nn:(k + 1) * nn] for k, nd in enumerate(leaves)}
+
+        @patch_callback
+        def setf(patch):
+            patch.f = data[id(patch)]
+        self.upwardsStage(setf)
+
+    def solve_with_data(self, a, b, r):
+        """solveStage with the boundary condition already sampled at the root face centres
+        (HPSAlgorithm.hpp:375-400): a, b, r are 4M WESN vectors."""
+        @patch_callback
+        def setg(rp):
+            rp.g = self.root_dirichlet(rp, np.asarray(a, float), np.asarray(b, float), np.asarray(r, float))
+        self.solveStage(setg)
 
     def root_dirichlet(self, root: FiniteVolumePatch, a, b, r):
         """HPSAlgorithm.hpp:402-420: g = (diag(a) + diag(b) T)^{-1} (r - diag(b) h)."""
