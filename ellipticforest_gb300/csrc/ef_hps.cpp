@@ -239,7 +239,7 @@ void Hps::allocate() {
                 nd.T = cv.get<double>(64 * s * s);
                 nd.X = cv.get<double>(16 * s * s);
                 nd.RHS = cv.get<double>(48 * s * s);
-                nd.H = cv.get<double>(32 * s * s);
+                nd.H = cv.get<double>(16 * s * s);
                 nd.piv = cv.get<int>(4 * s);
                 nd.perm = cv.get<int>(4 * s);
                 nd.h = cv.get<double>(8 * s);
@@ -278,6 +278,10 @@ void Hps::allocate() {
             g.d_piv = cv.get<int*>(cnt);
             g.d_perm = cv.get<int*>(cnt);
             g.d_info = cv.get<int>(cnt);
+            g.d_gA = cv.get<const double*>(8 * cnt);
+            g.d_gB = cv.get<const double*>(8 * cnt);
+            g.d_gB2 = cv.get<const double*>(8 * cnt);
+            g.d_gC = cv.get<double*>(8 * cnt);
         }
         tsteps_.clear(); hsteps_.clear(); gsteps_.clear();
         for (auto& kv : tmap) {
@@ -387,6 +391,30 @@ void Hps::upload_tables() {
         check(cudaMemcpy(g.d_T, T.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "T");
         check(cudaMemcpy(g.d_piv, P.data(), cnt * sizeof(int*), cudaMemcpyHostToDevice), "piv");
         check(cudaMemcpy(g.d_perm, Q.data(), cnt * sizeof(int*), cudaMemcpyHostToDevice), "perm");
+        // split GEMM tables: row block b of the parent's WESN exterior belongs to child c(b)
+        // (W: alpha, gamma; E: beta, omega; S: alpha, beta; N: gamma, omega), whose interfaces are
+        // alpha: I0, I2; beta: I1, I2; gamma: I0, I3; omega: I1, I3.
+        {
+            static const int cb[8] = {0, 2, 1, 3, 0, 1, 2, 3};
+            static const int ia[4] = {0, 1, 0, 1}, ib[4] = {2, 2, 3, 3};
+            const size_t sz = size_t(g.s);
+            std::vector<const double*> gA(8 * cnt), gB(8 * cnt), gB2(8 * cnt);
+            std::vector<double*> gC(8 * cnt);
+            for (int i = 0; i < cnt; ++i) {
+                const NodeDev& nd = nodes_[g.nodes[i]];
+                for (int b = 0; b < 8; ++b) {
+                    const int c = cb[b];
+                    gA[8 * i + b] = nd.H + size_t(b) * sz * 2 * sz;
+                    gB[8 * i + b] = nd.RHS + size_t(ia[c]) * sz * 12 * sz;
+                    gB2[8 * i + b] = nd.RHS + size_t(ib[c]) * sz * 12 * sz;
+                    gC[8 * i + b] = nd.T + size_t(b) * sz * 8 * sz;
+                }
+            }
+            check(cudaMemcpy(g.d_gA, gA.data(), gA.size() * sizeof(void*), cudaMemcpyHostToDevice), "gA");
+            check(cudaMemcpy(g.d_gB, gB.data(), gB.size() * sizeof(void*), cudaMemcpyHostToDevice), "gB");
+            check(cudaMemcpy(g.d_gB2, gB2.data(), gB2.size() * sizeof(void*), cudaMemcpyHostToDevice), "gB2");
+            check(cudaMemcpy(g.d_gC, gC.data(), gC.size() * sizeof(void*), cudaMemcpyHostToDevice), "gC");
+        }
     }
     for (size_t k = 0; k < tsteps_.size(); ++k) {
         const int t = step_index_t_[k];
@@ -457,12 +485,12 @@ void Hps::build() {
             pb("lu_solve");
             dlu_solve_permuted(st_, m, 3 * m, (const double* const*)g.d_X, m, g.d_RHS, 3 * m, cnt);
             pe(c * 8 * (dm * dm + 2 * 3 * dm * dm), c * 2.0 * dm * dm * 3 * dm);
-            // T = T_LHS + H S  (HPSAlgorithm.hpp:940-968), S = first 8s columns of RHS
+            // T = T_LHS + H S  (HPSAlgorithm.hpp:940-968), S = first 8s columns of RHS; H's zero
+            // blocks are skipped: each s-row block of T takes K = 2s (its child's two interfaces)
             pb("gemm_T");
-            GemmArgs ga{(const double* const*)g.d_H, 0, m, (const double* const*)g.d_RHS, 0, 3 * m,
-                        g.d_T, 0, 2 * m};
-            dgemm_batched(st_, 2 * m, 2 * m, m, 1.0, ga, 1.0, cnt);
-            pe(c * 8 * (2 * dm * dm + 2 * dm * dm + 2 * 4 * dm * dm), c * 2.0 * (2 * dm) * (2 * dm) * dm);
+            GemmArgs ga{g.d_gA, 0, 2 * s, g.d_gB, 0, 3 * m, g.d_gC, 0, 2 * m, g.d_gB2, 0, s};
+            dgemm_batched(st_, s, 2 * m, 2 * s, 1.0, ga, 1.0, 8 * cnt);
+            pe(c * 8 * (dm * dm / 2 + dm * 2 * dm + 2 * 4 * dm * dm), c * 2.0 * (2 * dm) * (2 * dm) * (dm / 2));
         }
     }
     check(cudaGetLastError(), "build launch");
@@ -499,7 +527,7 @@ void Hps::upwards() {
             pe(c * 8 * (16 * s * s + 8 * s + 4 * s), c * 2 * 16 * s * s);
             pb("upward_h");
             upward_h(st_, g.d_items, int(c), g.s);
-            pe(c * 8 * (16 * s * s + 4 * s + 8 * s + 8 * s), c * 2 * 16 * s * s);
+            pe(c * 8 * (16 * s * s + 4 * s + 8 * s + 8 * s), c * 2 * 16 * s * s);  // compact H
         }
     }
 }
@@ -580,7 +608,7 @@ double Hps::build_flops() const {
     double f = 0;
     for (const auto& g : groups_) {
         const double m = 4.0 * g.s, cnt = double(g.nodes.size());
-        f += cnt * (2.0 / 3.0 * m * m * m + 2.0 * m * m * (3 * m) + 2.0 * (2 * m) * (2 * m) * m);
+        f += cnt * (2.0 / 3.0 * m * m * m + 2.0 * m * m * (3 * m) + 2.0 * (2 * m) * (2 * m) * (m / 2));
     }
     return f;
 }
@@ -589,7 +617,7 @@ double Hps::solve_bytes() const {
     double b = 0;
     for (const auto& g : groups_) {
         const double s = g.s, cnt = double(g.nodes.size());
-        // X^{-1} (16 s^2) + nonzero half of H (16 s^2) + S (32 s^2)
+        // X^{-1} (16 s^2) + compact H (16 s^2) + S (32 s^2)
         b += cnt * 8.0 * (16 * s * s + 16 * s * s + 32 * s * s);
     }
     b += double(num_leaves()) * n_ * n_ * 8.0 * 3;  // f read twice, u written

@@ -47,6 +47,12 @@ struct Group {
     int** d_piv = nullptr;
     int** d_perm = nullptr;
     int* d_info = nullptr;
+    // T += H S as 8 row blocks per node: block b (s rows, child c(b)) multiplies its compact H rows
+    // with the S rows of the two interfaces adjacent to c(b)
+    const double** d_gA = nullptr;
+    const double** d_gB = nullptr;
+    const double** d_gB2 = nullptr;
+    double** d_gC = nullptr;
 };
 
 struct ResampleStep {  // one batched (un)coarsening step: `count` items of fine size nf

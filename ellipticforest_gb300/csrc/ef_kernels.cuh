@@ -35,6 +35,10 @@ struct GemmArgs {
     const double* const* A; long long offA; int lda;
     const double* const* B; long long offB; int ldb;
     double* const* C; long long offC; int ldc;
+    // optional: rows k >= kb of B come from B2 (row k - kb, same ldb)
+    const double* const* B2 = nullptr;
+    long long offB2 = 0;
+    int kb = 1 << 30;
 };
 
 // C = alpha*A*B + beta*C for each batch item (row-major).
@@ -92,7 +96,7 @@ struct MergeItem {
     int* piv;             // 4s
     int* perm;            // 4s
     double* RHS;          // 4s x 12s  = [S (WESN columns) | X^{-1}]
-    double* H;            // 8s x 4s, rows in WESN order
+    double* H;            // 8s x 2s compact: row p holds the two interface blocks adjacent to c(p)
     double* T;            // 8s x 8s, WESN
     const double* hc[4];  // children's (coarsened) h, 4s
     double* h;            // own h, 8s

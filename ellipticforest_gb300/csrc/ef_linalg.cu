@@ -22,6 +22,8 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
     const int b = b0 + blockIdx.z;
     const double* __restrict__ A = a.A[b] + a.offA;
     const double* __restrict__ B = a.B[b] + a.offB;
+    const double* __restrict__ B2 = a.B2 ? a.B2[b] + a.offB2 : B;
+    const int kb = a.B2 ? a.kb : (1 << 30);
     double* C = a.C[b] + a.offC;
     const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
     __shared__ double As[TK][TM + 1];
@@ -46,7 +48,9 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             const int e = tid + 256 * r;
             const int kk = e >> 6, col = e & 63;
             const int gk = k0 + kk, gn = n0 + col;
-            Bs[kk][col] = (gk < K && gn < N) ? B[(long long)gk * a.ldb + gn] : 0.0;
+            Bs[kk][col] = (gk < K && gn < N)
+                              ? (gk < kb ? B[(long long)gk * a.ldb + gn] : B2[(long long)(gk - kb) * a.ldb + gn])
+                              : 0.0;
         }
         __syncthreads();
 #pragma unroll

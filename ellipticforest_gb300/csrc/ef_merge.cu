@@ -43,8 +43,8 @@ __device__ __forceinline__ void child_ifaces(int c, int& Ia, int& Ib) {
 
 __global__ void k_gather_xht(const MergeItem* __restrict__ items, int s) {
     const MergeItem& it = items[blockIdx.y];
-    const long long m4 = 4LL * s, m8 = 8LL * s;
-    const long long nX = m4 * m4, nH = m8 * m4, nT = m8 * m8;
+    const long long m2 = 2LL * s, m4 = 4LL * s, m8 = 8LL * s;
+    const long long nX = m4 * m4, nH = m8 * m2, nT = m8 * m8;
     const long long tot = nX + nH + nT;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
          e += (long long)gridDim.x * blockDim.x) {
@@ -61,14 +61,16 @@ __global__ void k_gather_xht(const MergeItem* __restrict__ items, int s) {
             if (qj >= 0) v -= it.Tc[cu][(long long)q_upper(I, o, s) * m4 + qj];
             it.X[e] = v;
         } else if (e < nX + nH) {
+            // compact H: columns [0,s) <-> interface Ia(c(p)), [s,2s) <-> Ib(c(p))
             const long long f = e - nX;
-            const int p = int(f / m4), col = int(f - (f / m4) * m4);
-            const int I = col / s, o = col - I * s;
-            int c, q;
+            const int p = int(f / m2), col = int(f - (f / m2) * m2);
+            const int seg = col >= s ? 1 : 0, o = col - seg * s;
+            int c, q, Ia, Ib;
             ext_map(p, s, c, q);
+            child_ifaces(c, Ia, Ib);
             double sg;
-            const int qi = iface_q(c, I, o, s, sg);
-            it.H[f] = (qi >= 0) ? it.Tc[c][(long long)q * m4 + qi] : 0.0;
+            const int qi = iface_q(c, seg ? Ib : Ia, o, s, sg);
+            it.H[f] = it.Tc[c][(long long)q * m4 + qi];
         } else {
             const long long f = e - nX - nH;
             const int p = int(f / m8), pp = int(f - (f / m8) * m8);
@@ -169,50 +171,49 @@ __global__ void k_uncoarsen_vec(const double* const* vin, double* const* vout, i
     }
 }
 
-constexpr int WARPS_PER_CTA = 8;  // one matrix row per warp
-
-__device__ __forceinline__ double warp_sum(double v) {
+// Group dot products: LPR consecutive lanes (LPR in {4, 8, 16, 32}) share one matrix row; the
+// row is streamed with evict-first loads, the vector is read through L1.
+template <int LPR>
+__device__ __forceinline__ double group_sum(double v) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    for (int off = LPR / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     return v;
 }
 
-// Warp dot product of a streamed matrix row segment with a vector read through L1.
-// VEC: both pointers 16-byte aligned and len even -> double2 loads, four independent chains.
-template <bool VEC>
-__device__ __forceinline__ double warp_dot(const double* __restrict__ row, const double* __restrict__ x,
-                                           int len, int lane) {
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+// accumulate row[0:len) . x[0:len) over the lanes of one group (sl = lane within the group).
+// VEC: row and x 16-byte aligned and len even -> double2 loads.
+template <bool VEC, int LPR>
+__device__ __forceinline__ void group_dot_acc(const double* __restrict__ row, const double* __restrict__ x,
+                                              int len, int sl, double& a0, double& a1, double& a2, double& a3) {
     if (VEC) {
         const double2* r2 = reinterpret_cast<const double2*>(row);
         const double2* x2 = reinterpret_cast<const double2*>(x);
         const int n2 = len >> 1;
-        int i = lane;
-        for (; i + 96 < n2; i += 128) {
-            const double2 m0 = __ldcs(r2 + i), m1 = __ldcs(r2 + i + 32);
-            const double2 m2 = __ldcs(r2 + i + 64), m3 = __ldcs(r2 + i + 96);
-            const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + 32);
-            const double2 v2 = __ldg(x2 + i + 64), v3 = __ldg(x2 + i + 96);
+        int i = sl;
+        for (; i + 3 * LPR < n2; i += 4 * LPR) {
+            const double2 m0 = __ldcs(r2 + i), m1 = __ldcs(r2 + i + LPR);
+            const double2 m2 = __ldcs(r2 + i + 2 * LPR), m3 = __ldcs(r2 + i + 3 * LPR);
+            const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + LPR);
+            const double2 v2 = __ldg(x2 + i + 2 * LPR), v3 = __ldg(x2 + i + 3 * LPR);
             a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
             a1 = fma(m1.x, v1.x, a1); a1 = fma(m1.y, v1.y, a1);
             a2 = fma(m2.x, v2.x, a2); a2 = fma(m2.y, v2.y, a2);
             a3 = fma(m3.x, v3.x, a3); a3 = fma(m3.y, v3.y, a3);
         }
-        for (; i < n2; i += 32) {
+        for (; i < n2; i += LPR) {
             const double2 m0 = __ldcs(r2 + i), v0 = __ldg(x2 + i);
             a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
         }
     } else {
-        int i = lane;
-        for (; i + 96 < len; i += 128) {
+        int i = sl;
+        for (; i + 3 * LPR < len; i += 4 * LPR) {
             a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
-            a1 = fma(__ldcs(row + i + 32), __ldg(x + i + 32), a1);
-            a2 = fma(__ldcs(row + i + 64), __ldg(x + i + 64), a2);
-            a3 = fma(__ldcs(row + i + 96), __ldg(x + i + 96), a3);
+            a1 = fma(__ldcs(row + i + LPR), __ldg(x + i + LPR), a1);
+            a2 = fma(__ldcs(row + i + 2 * LPR), __ldg(x + i + 2 * LPR), a2);
+            a3 = fma(__ldcs(row + i + 3 * LPR), __ldg(x + i + 3 * LPR), a3);
         }
-        for (; i < len; i += 32) a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
+        for (; i < len; i += LPR) a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
     }
-    return warp_sum((a0 + a1) + (a2 + a3));
 }
 
 // hDiff = h_upper - h_lower per interface point (HPSAlgorithm.hpp:1061-1081)
@@ -226,41 +227,52 @@ __global__ void k_hdiff(const MergeItem* __restrict__ items, int s) {
     it.hd[r] = it.hc[upper_child(I)][q_upper(I, o, s)] - it.hc[lower_child(I)][q_lower(I, o, s)];
 }
 
-// w = X^{-1} hDiff (the X^{-1} block of RHS, columns [8s, 12s))
-template <bool VEC>
-__global__ void __launch_bounds__(256) k_gemv_w(const MergeItem* __restrict__ items, int s, long long nrows) {
-    const int lane = threadIdx.x & 31;
-    const long long g = blockIdx.x * (long long)WARPS_PER_CTA + (threadIdx.x >> 5);
-    if (g >= nrows) return;
-    const int m4 = 4 * s;
-    const int item = int(g / m4), r = int(g - (long long)item * m4);
-    const MergeItem& it = items[item];
-    const double acc = warp_dot<VEC>(it.RHS + (long long)r * (12LL * s) + 8 * s, it.hd, m4, lane);
-    if (lane == 0) it.w[r] = acc;
+// Row index handled by this thread's lane group; groups never leave early (full-warp shuffles).
+template <int LPR>
+__device__ __forceinline__ long long group_row() {
+    return blockIdx.x * (long long)(256 / LPR) + threadIdx.x / LPR;
 }
 
-// h = H w + h_update (HPSAlgorithm.hpp:1098-1117); only the two interface blocks adjacent to the
-// row's child are non-zero; rows are already in WESN order
-template <bool VEC>
+// w = X^{-1} hDiff (the X^{-1} block of RHS, columns [8s, 12s))
+template <bool VEC, int LPR>
+__global__ void __launch_bounds__(256) k_gemv_w(const MergeItem* __restrict__ items, int s, long long nrows) {
+    const int sl = threadIdx.x & (LPR - 1);
+    const long long g = group_row<LPR>();
+    const bool ok = g < nrows;
+    const int m4 = 4 * s;
+    const int item = ok ? int(g / m4) : 0, r = ok ? int(g - (long long)item * m4) : 0;
+    const MergeItem& it = items[item];
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (ok) group_dot_acc<VEC, LPR>(it.RHS + (long long)r * (12LL * s) + 8 * s, it.hd, m4, sl, a0, a1, a2, a3);
+    const double acc = group_sum<LPR>((a0 + a1) + (a2 + a3));
+    if (ok && sl == 0) it.w[r] = acc;
+}
+
+// h = H w + h_update (HPSAlgorithm.hpp:1098-1117), compact H rows already in WESN order
+template <bool VEC, int LPR>
 __global__ void __launch_bounds__(256) k_gemv_h(const MergeItem* __restrict__ items, int s, long long nrows) {
-    const int lane = threadIdx.x & 31;
-    const long long g = blockIdx.x * (long long)WARPS_PER_CTA + (threadIdx.x >> 5);
-    if (g >= nrows) return;
+    const int sl = threadIdx.x & (LPR - 1);
+    const long long g = group_row<LPR>();
+    const bool ok = g < nrows;
     const int m8 = 8 * s;
-    const int item = int(g / m8), p = int(g - (long long)item * m8);
+    const int item = ok ? int(g / m8) : 0, p = ok ? int(g - (long long)item * m8) : 0;
     const MergeItem& it = items[item];
     int c, q, Ia, Ib;
     ext_map(p, s, c, q);
     child_ifaces(c, Ia, Ib);
-    const double* row = it.H + (long long)p * (4LL * s);
-    const double acc = warp_dot<VEC>(row + Ia * s, it.w + Ia * s, s, lane) +
-                       warp_dot<VEC>(row + Ib * s, it.w + Ib * s, s, lane);
-    if (lane == 0) it.h[p] = acc + it.hc[c][q];
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (ok) {
+        const double* row = it.H + (long long)p * (2LL * s);
+        group_dot_acc<VEC, LPR>(row, it.w + Ia * s, s, sl, a0, a1, a2, a3);
+        group_dot_acc<VEC, LPR>(row + s, it.w + Ib * s, s, sl, a0, a1, a2, a3);
+    }
+    const double acc = group_sum<LPR>((a0 + a1) + (a2 + a3));
+    if (ok && sl == 0) it.h[p] = acc + it.hc[c][q];
 }
 
 // u_Gamma = S g + w (HPSAlgorithm.hpp:1197-1204) scattered to the children's interface data; the
-// first CTAs also copy the exterior data of the children (HPSAlgorithm.hpp:1214-1227)
-template <bool VEC>
+// leading threads also copy the exterior data of the children (HPSAlgorithm.hpp:1214-1227)
+template <bool VEC, int LPR>
 __global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__ items, int s,
                                                    long long nrows, int nitems, int add_w) {
     const int m4 = 4 * s, m8 = 8 * s;
@@ -272,19 +284,38 @@ __global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__
         ext_map(p, s, c, q);
         it.gc[c][q] = it.gf[p];
     }
-    const int lane = threadIdx.x & 31;
-    const long long g = blockIdx.x * (long long)WARPS_PER_CTA + (threadIdx.x >> 5);
-    if (g >= nrows) return;
-    const int item = int(g / m4), r = int(g - (long long)item * m4);
+    const int sl = threadIdx.x & (LPR - 1);
+    const long long g = group_row<LPR>();
+    const bool ok = g < nrows;
+    const int item = ok ? int(g / m4) : 0, r = ok ? int(g - (long long)item * m4) : 0;
     const MergeItem& it = items[item];
-    const double acc = warp_dot<VEC>(it.RHS + (long long)r * (12LL * s), it.gf, m8, lane);
-    if (lane == 0) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (ok) group_dot_acc<VEC, LPR>(it.RHS + (long long)r * (12LL * s), it.gf, m8, sl, a0, a1, a2, a3);
+    const double acc = group_sum<LPR>((a0 + a1) + (a2 + a3));
+    if (ok && sl == 0) {
         const double u = add_w ? acc + it.w[r] : acc;
         const int I = r / s, o = r - I * s;
         it.gc[lower_child(I)][q_lower(I, o, s)] = u;
         it.gc[upper_child(I)][q_upper(I, o, s)] = u;
     }
 }
+
+// lanes per row for a row (segment) of `len` doubles
+inline int pick_lpr(int len, bool vec) {
+    const int units = vec ? len / 2 : len;
+    if (units >= 64) return 32;
+    if (units >= 32) return 16;
+    if (units >= 16) return 8;
+    return 4;
+}
+
+#define EF_LPR_DISPATCH(KERNEL, VEC, LPR, GRID, ...)                                     \
+    do {                                                                                 \
+        if (LPR == 32) KERNEL<VEC, 32><<<GRID, 256, 0, st>>>(__VA_ARGS__);               \
+        else if (LPR == 16) KERNEL<VEC, 16><<<GRID, 256, 0, st>>>(__VA_ARGS__);          \
+        else if (LPR == 8) KERNEL<VEC, 8><<<GRID, 256, 0, st>>>(__VA_ARGS__);            \
+        else KERNEL<VEC, 4><<<GRID, 256, 0, st>>>(__VA_ARGS__);                          \
+    } while (0)
 
 __global__ void k_root_diag(int m, const double* a, const double* b, const double* r,
                             const double* h, double* g) {
@@ -370,28 +401,35 @@ void upward_hdiff(cudaStream_t st, const MergeItem* items, int nitems, int s) {
 
 void upward_w(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     const long long rows = (long long)nitems * 4 * s;
-    const unsigned blocks = unsigned((rows + WARPS_PER_CTA - 1) / WARPS_PER_CTA);
-    if (s % 2 == 0) k_gemv_w<true><<<blocks, 256, 0, st>>>(items, s, rows);
-    else k_gemv_w<false><<<blocks, 256, 0, st>>>(items, s, rows);
+    const bool vec = (s % 2 == 0);
+    const int lpr = pick_lpr(4 * s, vec);
+    const unsigned blocks = unsigned((rows * lpr + 255) / 256);
+    if (vec) EF_LPR_DISPATCH(k_gemv_w, true, lpr, blocks, items, s, rows);
+    else EF_LPR_DISPATCH(k_gemv_w, false, lpr, blocks, items, s, rows);
     ++g_kernel_launches;
 }
 
 void upward_h(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     const long long rows = (long long)nitems * 8 * s;
-    const unsigned blocks = unsigned((rows + WARPS_PER_CTA - 1) / WARPS_PER_CTA);
-    if (s % 2 == 0) k_gemv_h<true><<<blocks, 256, 0, st>>>(items, s, rows);
-    else k_gemv_h<false><<<blocks, 256, 0, st>>>(items, s, rows);
+    const bool vec = (s % 2 == 0);
+    const int lpr = pick_lpr(s, vec);
+    const unsigned blocks = unsigned((rows * lpr + 255) / 256);
+    if (vec) EF_LPR_DISPATCH(k_gemv_h, true, lpr, blocks, items, s, rows);
+    else EF_LPR_DISPATCH(k_gemv_h, false, lpr, blocks, items, s, rows);
     ++g_kernel_launches;
 }
 
 void downward(cudaStream_t st, const MergeItem* items, int nitems, int s, int add_w) {
     const long long rows = (long long)nitems * 4 * s;
-    // enough CTAs for the rows (one per warp) and for the exterior copy (one element per thread)
-    long long blocks = (rows + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const bool vec = (s % 2 == 0);
+    const int lpr = pick_lpr(8 * s, vec);
+    // enough CTAs for the rows and for the exterior copy (one element per thread)
+    long long blocks = (rows * lpr + 255) / 256;
     const long long eblocks = ((long long)nitems * 8 * s + 255) / 256;
     if (eblocks > blocks) blocks = eblocks;
-    if (s % 2 == 0) k_gemv_down<true><<<unsigned(blocks), 256, 0, st>>>(items, s, rows, nitems, add_w);
-    else k_gemv_down<false><<<unsigned(blocks), 256, 0, st>>>(items, s, rows, nitems, add_w);
+    const unsigned nb = unsigned(blocks);
+    if (vec) EF_LPR_DISPATCH(k_gemv_down, true, lpr, nb, items, s, rows, nitems, add_w);
+    else EF_LPR_DISPATCH(k_gemv_down, false, lpr, nb, items, s, rows, nitems, add_w);
     ++g_kernel_launches;
 }
 
