@@ -72,6 +72,8 @@ SIGNATURES = {
                               _dp, _dp, _dp]),
     "ef_fv_map_d2n": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, _dp, _dp, _dp]),
+    "ef_fv_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, _vp, _vp, _vp, _vp]),
 }
 
 _LIB = None

@@ -119,6 +119,11 @@ int run_single_patch(int solver_type, int n, double xl, double xu, double yl, do
 
 }  // namespace
 
+namespace efgb {
+// lets the other translation units of the C ABI report a message through ef_last_error()
+void set_last_error_message(const std::string& msg) { g_last_error = msg; }
+}  // namespace efgb
+
 extern "C" {
 
 const char* ef_last_error(void) { return g_last_error.c_str(); }
