@@ -242,6 +242,12 @@ def measure_fp64_peak(torch):
     return 2 * 4096 ** 3 / best / 1e12
 
 
+# DRAM bytes per launch / algorithmic bytes per launch of the solve kernels, from one ncu capture
+# of the same kernels on the uniform L6 tree (profiles/k_gemv_down_uniform_L6.md); L7 launches
+# stream 4x the bytes of L6 launches with the same access pattern.
+TRAFFIC_RATIO = {"downward": 1.005}
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -405,7 +411,10 @@ def run_gb300(args):
                     "d2h_bytes_per_step": int(8 * dofs)},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / hbm_peak,
+                         "traffic": (TRAFFIC_RATIO[dom_name] * d["bytes"] / max(d["launches"], 1)
+                                     if dom_name in TRAFFIC_RATIO else None),
+                         "algorithmic_bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "share_of_solve": d["ms"] / tot_ms},
             "fp64": {"solve_tflops": fp64_solve, "build_tflops": build_flops / build_s / 1e12,
