@@ -276,7 +276,7 @@ def run_gb300(args):
     level, n = args.level, args.n
     root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, DOM[0], DOM[1], n, DOM[2], DOM[3]))
     mesh = ef.Mesh().uniform(level, root)
-    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver())
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
     hps.set_stream(stream.cuda_stream)
     hps.setupStage()
 

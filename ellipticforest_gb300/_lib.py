@@ -42,6 +42,7 @@ SIGNATURES = {
                                C.POINTER(C.c_longlong), _dp]),
     "ef_mesh_destroy": (C.c_int, [_vp]),
     "ef_hps_create": (C.c_int, [_vp, C.c_int, C.c_double, C.POINTER(_vp)]),
+    "ef_hps_set_coefficients": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ef_hps_set_option": (C.c_int, [_vp, C.c_char_p, C.c_int]),
     "ef_hps_set_stream": (C.c_int, [_vp, _vp]),
     "ef_hps_info": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -72,6 +73,11 @@ SIGNATURES = {
                               _dp, _dp, _dp]),
     "ef_fv_map_d2n": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, _dp, _dp, _dp]),
+    "ef_fv5_build_d2n": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp]),
+    "ef_fv5_solve": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp,
+                               _dp]),
+    "ef_fv5_map_d2n": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp,
+                                 _dp, _dp]),
     "ef_fv_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                       C.c_double, _vp, _vp, _vp, _vp]),
 }

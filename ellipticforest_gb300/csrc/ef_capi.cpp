@@ -117,6 +117,58 @@ int run_single_patch(int solver_type, int n, double xl, double xu, double yl, do
     return cuda_status(e, "single patch");
 }
 
+// One-patch run of the variable-coefficient (FivePointStencil) leaf kernels.
+int run_single_patch_fp(int n, double xl, double xu, double yl, double yu, const double* alpha,
+                        const double* beta, const double* lambda, int mode, const double* g_host,
+                        const double* f_host, double* out_host, size_t out_count) {
+    if (n < 2 || n > 64) return fail(EF_ERR_INVALID, "n must be in [2, 64]");
+    if (!finite_box(xl, xu) || !finite_box(yl, yu)) return fail(EF_ERR_INVALID, "bad patch box");
+    if (!alpha || !beta || !lambda || !out_host) return fail(EF_ERR_INVALID, "null argument");
+    const size_t nn = size_t(n) * n;
+    const int nitems = (mode == efgb::LEAF_DTN_COLUMN) ? 4 * n : 1;
+    // doubles: coefficients 6nn, band nn(2n+1), bcoef 4n, g 4n, f nn, out; then structs
+    const size_t ndbl = 6 * nn + nn * (2 * n + 1) + 4 * n + 4 * n + nn + out_count;
+    const size_t bytes = ndbl * 8 + 256 + sizeof(efgb::FpLeaf) + 256 + sizeof(efgb::LeafItem) * nitems + 256;
+    char* buf = nullptr;
+    int st = cuda_status(cudaMalloc(&buf, bytes), "cudaMalloc");
+    if (st) return st;
+    double* coef = reinterpret_cast<double*>(buf);
+    double* band = coef + 6 * nn;
+    double* bcoef = band + nn * (2 * n + 1);
+    double* dg = bcoef + 4 * n;
+    double* df = dg + 4 * n;
+    double* dout = df + nn;
+    auto* dinfo = reinterpret_cast<int*>((reinterpret_cast<uintptr_t>(dout + out_count) + 255) & ~uintptr_t(255));
+    auto* dleaf = reinterpret_cast<efgb::FpLeaf*>((reinterpret_cast<uintptr_t>(dinfo + 1) + 255) & ~uintptr_t(255));
+    auto* ditems = reinterpret_cast<efgb::LeafItem*>((reinterpret_cast<uintptr_t>(dleaf + 1) + 255) & ~uintptr_t(255));
+    const double dx = (xu - xl) / n, dy = (yu - yl) / n;
+    efgb::FpLeaf lf{n, dx, dy, coef, coef + nn, coef + 5 * nn, band, bcoef, dinfo};
+    std::vector<efgb::LeafItem> items(nitems);
+    for (int k = 0; k < nitems; ++k)
+        items[k] = efgb::LeafItem{0, k, f_host ? df : nullptr, g_host ? dg : nullptr, dout};
+    cudaError_t e = cudaMemcpy(coef, alpha, nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(coef + nn, beta, 4 * nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(coef + 5 * nn, lambda, nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && g_host) e = cudaMemcpy(dg, g_host, 4 * n * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && f_host) e = cudaMemcpy(df, f_host, nn * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(dinfo, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(dleaf, &lf, sizeof(lf), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ditems, items.data(), nitems * sizeof(efgb::LeafItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        efgb::fp_factor(0, dleaf, 1, n);
+        efgb::fp_solve(0, mode, dleaf, ditems, nitems, n);
+        e = cudaGetLastError();
+    }
+    int info = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(out_host, dout, out_count * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    st = cuda_status(e, "single patch (five-point)");
+    if (st) return st;
+    if (info) return fail(EF_ERR_SINGULAR, "five-point operator has a zero pivot at row " + std::to_string(info - 1));
+    return EF_OK;
+}
+
 }  // namespace
 
 namespace efgb {
@@ -187,12 +239,20 @@ int ef_mesh_destroy(ef_mesh* mesh) {
 
 int ef_hps_create(const ef_mesh* mesh, int solver_type, double lambda, ef_hps** out) {
     if (!mesh || !out) return fail(EF_ERR_INVALID, "null argument");
-    if (solver_type != EF_SOLVER_FISHPACK90)
-        return fail(EF_ERR_UNSUPPORTED, "solver type not available: use EF_SOLVER_FISHPACK90");
+    if (solver_type != EF_SOLVER_FISHPACK90 && solver_type != EF_SOLVER_FIVE_POINT)
+        return fail(EF_ERR_INVALID, "unknown solver type");
     return guarded([&] {
         auto h = std::make_unique<ef_hps>();
         h->hps = std::make_unique<efgb::Hps>(mesh->mesh, solver_type, lambda, false);
         *out = h.release();
+        return EF_OK;
+    });
+}
+
+int ef_hps_set_coefficients(ef_hps* h, const double* alpha, const double* beta, const double* lambda) {
+    if (!h || !alpha || !beta || !lambda) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        h->hps->set_coefficients(alpha, beta, lambda);
         return EF_OK;
     });
 }
@@ -445,6 +505,32 @@ int ef_fv_map_d2n(int solver_type, int n, double xl, double xu, double yl, doubl
     return guarded([&] {
         return run_single_patch(solver_type, n, xl, xu, yl, yu, lambda, efgb::LEAF_MAPD2N, g, f, h,
                                 size_t(4) * n);
+    });
+}
+
+int ef_fv5_build_d2n(int n, double xl, double xu, double yl, double yu, const double* alpha,
+                     const double* beta, const double* lambda, double* T) {
+    return guarded([&] {
+        return run_single_patch_fp(n, xl, xu, yl, yu, alpha, beta, lambda, efgb::LEAF_DTN_COLUMN, nullptr,
+                                   nullptr, T, size_t(16) * n * n);
+    });
+}
+
+int ef_fv5_solve(int n, double xl, double xu, double yl, double yu, const double* alpha, const double* beta,
+                 const double* lambda, const double* g, const double* f, double* u) {
+    if (!g) return fail(EF_ERR_INVALID, "null Dirichlet data");
+    return guarded([&] {
+        return run_single_patch_fp(n, xl, xu, yl, yu, alpha, beta, lambda, efgb::LEAF_SOLVE, g, f, u,
+                                   size_t(n) * n);
+    });
+}
+
+int ef_fv5_map_d2n(int n, double xl, double xu, double yl, double yu, const double* alpha,
+                   const double* beta, const double* lambda, const double* g, const double* f, double* h) {
+    if (!g) return fail(EF_ERR_INVALID, "null Dirichlet data");
+    return guarded([&] {
+        return run_single_patch_fp(n, xl, xu, yl, yu, alpha, beta, lambda, efgb::LEAF_MAPD2N, g, f, h,
+                                   size_t(4) * n);
     });
 }
 

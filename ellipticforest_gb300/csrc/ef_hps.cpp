@@ -172,7 +172,11 @@ void Hps::plan() {
         std::memcpy(&ky, &dy, 8);
         auto it = key2type.find({kx, ky});
         int t;
-        if (it == key2type.end()) {
+        if (solver_type_ == SOLVER_FIVE_POINT) {
+            // variable coefficients: every leaf has its own operator
+            t = int(types_.size());
+            types_.push_back(LeafTypeHost{n_, dx, dy, nullptr});
+        } else if (it == key2type.end()) {
             t = int(types_.size());
             types_.push_back(LeafTypeHost{n_, dx, dy, nullptr});
             key2type[{kx, ky}] = t;
@@ -222,10 +226,24 @@ void Hps::allocate() {
         }
     }
 
+    const bool fp = solver_type_ == SOLVER_FIVE_POINT;
     auto layout = [&](Carver& cv) {
         for (auto& ty : types_) ty.T = cv.get<double>(size_t(16) * nn);
-        d_V_ = cv.get<double>(size_t(types_.size()) * nn);
-        d_Dinv_ = cv.get<double>(size_t(types_.size()) * nn);
+        if (fp) {
+            // per leaf: coefficients [alpha | beta W,E,S,N | lambda], band LU, boundary coefficients
+            d_coef_ = cv.get<double>(size_t(L) * 6 * nn);
+            fp_band_.assign(L, nullptr);
+            fp_bcoef_.assign(L, nullptr);
+            for (int k = 0; k < L; ++k) {
+                fp_band_[k] = cv.get<double>(size_t(nn) * (2 * n_ + 1));
+                fp_bcoef_[k] = cv.get<double>(4 * size_t(n_));
+            }
+            d_fpinfo_ = cv.get<int>(L);
+            d_fp_ = cv.get<FpLeaf>(L);
+        } else {
+            d_V_ = cv.get<double>(size_t(types_.size()) * nn);
+            d_Dinv_ = cv.get<double>(size_t(types_.size()) * nn);
+        }
         for (int id = 0; id < N; ++id) {
             NodeDev& nd = nodes_[id];
             const MeshNode& mn = mesh_.nodes[id];
@@ -332,17 +350,28 @@ void Hps::upload_tables() {
     // zero the whole arena once (h of the root must read as 0 before any upward pass)
     check(cudaMemsetAsync(arena_, 0, arena_bytes_, st_), "memset(arena)");
 
-    // leaf types: sine basis and inverse eigenvalue table
-    std::vector<LeafType> hty(types_.size());
-    std::vector<double> V(nn), Dinv(nn);
-    for (size_t t = 0; t < types_.size(); ++t) {
-        leaf_tables(n_, types_[t].dx, types_[t].dy, lambda_, V.data(), Dinv.data());
-        check(cudaMemcpy(d_V_ + t * nn, V.data(), nn * 8, cudaMemcpyHostToDevice), "upload V");
-        check(cudaMemcpy(d_Dinv_ + t * nn, Dinv.data(), nn * 8, cudaMemcpyHostToDevice), "upload Dinv");
-        hty[t] = LeafType{n_, types_[t].dx, types_[t].dy, d_V_ + t * nn, d_Dinv_ + t * nn};
+    if (solver_type_ == SOLVER_FIVE_POINT) {
+        // one variable-coefficient operator per leaf (type index == leaf index)
+        std::vector<FpLeaf> fl(L);
+        for (int k = 0; k < L; ++k) {
+            const double* c = d_coef_ + size_t(k) * 6 * nn;
+            fl[k] = FpLeaf{n_, types_[k].dx, types_[k].dy, c, c + nn, c + 5 * nn, fp_band_[k], fp_bcoef_[k],
+                           d_fpinfo_ + k};
+        }
+        check(cudaMemcpy(d_fp_, fl.data(), fl.size() * sizeof(FpLeaf), cudaMemcpyHostToDevice), "upload fp leaves");
+    } else {
+        // leaf types: sine basis and inverse eigenvalue table
+        std::vector<LeafType> hty(types_.size());
+        std::vector<double> V(nn), Dinv(nn);
+        for (size_t t = 0; t < types_.size(); ++t) {
+            leaf_tables(n_, types_[t].dx, types_[t].dy, lambda_, V.data(), Dinv.data());
+            check(cudaMemcpy(d_V_ + t * nn, V.data(), nn * 8, cudaMemcpyHostToDevice), "upload V");
+            check(cudaMemcpy(d_Dinv_ + t * nn, Dinv.data(), nn * 8, cudaMemcpyHostToDevice), "upload Dinv");
+            hty[t] = LeafType{n_, types_[t].dx, types_[t].dy, d_V_ + t * nn, d_Dinv_ + t * nn};
+        }
+        check(cudaMemcpy(d_types_, hty.data(), hty.size() * sizeof(LeafType), cudaMemcpyHostToDevice),
+              "upload types");
     }
-    check(cudaMemcpy(d_types_, hty.data(), hty.size() * sizeof(LeafType), cudaMemcpyHostToDevice),
-          "upload types");
 
     std::vector<LeafItem> items;
     for (size_t t = 0; t < types_.size(); ++t)
@@ -449,10 +478,39 @@ void Hps::upload_tables() {
     check(cudaStreamSynchronize(st_), "upload sync");
 }
 
+void Hps::leaf_run(int mode, const LeafItem* items, int nitems) {
+    if (solver_type_ == SOLVER_FIVE_POINT) fp_solve(st_, mode, d_fp_, items, nitems, n_);
+    else leaf_eigen(st_, mode, d_types_, items, nitems, n_);
+}
+
+void Hps::set_coefficients(const double* alpha, const double* beta, const double* lambda) {
+    if (solver_type_ != SOLVER_FIVE_POINT)
+        throw std::invalid_argument("leaf coefficients apply to the FivePointStencil solver only");
+    const size_t nn = size_t(n_) * n_;
+    const int L = num_leaves();
+    for (int k = 0; k < L; ++k) {
+        double* c = d_coef_ + size_t(k) * 6 * nn;
+        check(cudaMemcpyAsync(c, alpha + k * nn, nn * 8, cudaMemcpyHostToDevice, st_), "coef alpha");
+        check(cudaMemcpyAsync(c + nn, beta + k * 4 * nn, 4 * nn * 8, cudaMemcpyHostToDevice, st_), "coef beta");
+        check(cudaMemcpyAsync(c + 5 * nn, lambda + k * nn, nn * 8, cudaMemcpyHostToDevice, st_), "coef lambda");
+    }
+    check(cudaStreamSynchronize(st_), "coef sync");
+    coef_set_ = true;
+    built_ = false;
+}
+
 void Hps::build_leaf_types() {
-    pb("leaf_dtn");
-    leaf_eigen(st_, LEAF_DTN_COLUMN, d_types_, d_items_dtn_, nitems_dtn_, n_);
     const double n = n_;
+    if (solver_type_ == SOLVER_FIVE_POINT) {
+        if (!coef_set_) throw std::invalid_argument("FivePointStencil: leaf coefficients were not set");
+        const double L = num_leaves(), N = n * n;
+        check(cudaMemsetAsync(d_fpinfo_, 0, num_leaves() * sizeof(int), st_), "memset fp info");
+        pb("leaf_factor");
+        fp_factor(st_, d_fp_, num_leaves(), n_);
+        pe(L * 8 * (6 * N + N * (2 * n + 1)), L * 2.0 * N * n * n);
+    }
+    pb("leaf_dtn");
+    leaf_run(LEAF_DTN_COLUMN, d_items_dtn_, nitems_dtn_);
     pe(double(types_.size()) * 16 * n * n * 8, double(nitems_dtn_) * (6 * n * n * n + 8 * n * n));
 }
 
@@ -501,13 +559,18 @@ void Hps::build() {
         check(cudaMemcpy(info.data(), g.d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "info");
         for (int v : info) singular_ += (v != 0);
     }
+    if (solver_type_ == SOLVER_FIVE_POINT) {
+        std::vector<int> info(num_leaves());
+        check(cudaMemcpy(info.data(), d_fpinfo_, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "fp info");
+        for (int v : info) singular_ += (v != 0);
+    }
     built_ = true;
 }
 
 void Hps::upwards() {
     const double L = num_leaves(), n = n_;
     pb("leaf_neumann");
-    leaf_eigen(st_, LEAF_NEUMANN, d_types_, d_items_neu_, num_leaves(), n_);
+    leaf_run(LEAF_NEUMANN, d_items_neu_, num_leaves());
     pe(L * 8 * (n * n + 4 * n), L * (6 * n * n * n + 8 * n * n));
     if (homogeneous_) return;
     const int maxL = mesh_.max_level;
@@ -594,7 +657,7 @@ void Hps::downwards() {
     if (homogeneous_) fill_zero(st_, d_f_, (long long)num_leaves() * n_ * n_);
     const double L = num_leaves(), n = n_;
     pb("leaf_solve");
-    leaf_eigen(st_, LEAF_SOLVE, d_types_, d_items_solve_, num_leaves(), n_);
+    leaf_run(LEAF_SOLVE, d_items_solve_, num_leaves());
     pe(L * 8 * (2 * n * n + 4 * n), L * 8 * n * n * n);
 }
 

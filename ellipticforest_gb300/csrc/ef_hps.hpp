@@ -77,6 +77,10 @@ public:
     Hps& operator=(const Hps&) = delete;
 
     void set_stream(cudaStream_t st) { st_ = st; }
+    // FivePointStencil: per-leaf coefficients sampled at the reference's points (host arrays in leaf
+    // order: alpha n*n, beta 4*n*n (W, E, S, N face of every cell), lambda n*n per leaf)
+    void set_coefficients(const double* alpha, const double* beta, const double* lambda);
+    int solver_type() const { return solver_type_; }
     cudaStream_t stream() const { return st_; }
     void set_homogeneous_rhs(bool v) { homogeneous_ = v; }
     // true when the boundary coefficient b of a*u + b*du/dn = r is not identically zero
@@ -132,6 +136,7 @@ private:
     void allocate();
     void upload_tables();
     void build_leaf_types();
+    void leaf_run(int mode, const LeafItem* items, int nitems);
     void check(cudaError_t e, const char* what);
 
     Mesh mesh_;
@@ -149,6 +154,12 @@ private:
     std::vector<std::vector<int>> step_nodes_t_, step_nodes_g_;
     std::vector<int> step_index_t_, step_index_g_;
     double *d_V_ = nullptr, *d_Dinv_ = nullptr;
+    // FivePointStencil leaves
+    double* d_coef_ = nullptr;
+    FpLeaf* d_fp_ = nullptr;
+    int* d_fpinfo_ = nullptr;
+    std::vector<double*> fp_band_, fp_bcoef_;
+    bool coef_set_ = false;
     std::vector<LeafTypeHost> types_;
     LeafType* d_types_ = nullptr;
     LeafItem *d_items_dtn_ = nullptr, *d_items_neu_ = nullptr, *d_items_solve_ = nullptr;

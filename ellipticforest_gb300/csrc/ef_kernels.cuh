@@ -87,6 +87,23 @@ struct LeafItem {
 void leaf_eigen(cudaStream_t st, int mode, const LeafType* types_dev, const LeafItem* items_dev,
                 int nitems, int nmax);
 
+// Variable-coefficient leaf (FivePointStencil): coefficients sampled per cell, banded LU of the
+// 5-point operator (bandwidth n, no pivoting), triangular solves one warp per (leaf, RHS).
+struct FpLeaf {
+    int n;
+    double dx, dy;
+    const double* alpha;   // n*n, alpha(x_i, y_j)
+    const double* beta;    // 4*n*n: beta at the W, E, S, N face of every cell
+    const double* lambda;  // n*n
+    double* band;          // n*n rows x (2n+1): row r holds columns r-n .. r+n (L multipliers | U)
+    double* bcoef;         // 4n boundary coupling coefficients c_side (WESN)
+    int* info;             // first zero pivot (1-based) or 0
+};
+void fp_factor(cudaStream_t st, const FpLeaf* leaves, int nleaves, int nmax);
+// items[k].type indexes `leaves`; modes as for leaf_eigen
+void fp_solve(cudaStream_t st, int mode, const FpLeaf* leaves, const LeafItem* items, int nitems,
+              int nmax);
+
 // ------------------------------------------------------------------------------------------------
 // Merge / upward / downward kernels
 // ------------------------------------------------------------------------------------------------

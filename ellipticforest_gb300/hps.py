@@ -58,16 +58,40 @@ class FiniteVolumeGrid:
         return self.point(dim, index)
 
 
+def _sample(fn, X, Y):
+    v = np.asarray(fn(X, Y), dtype=np.float64)
+    return np.ascontiguousarray(np.broadcast_to(v, X.shape), dtype=np.float64)
+
+
+def sample_coefficients(solver, grid):
+    """alpha, beta (W, E, S, N faces of every cell) and lambda of one patch, sampled at the points
+    of FiniteVolumeSolver.cpp:66-79 with the same arithmetic (x_i -/+ dx/2.0, y_j -/+ dy/2.0).
+    The coefficient functions are called with numpy arrays."""
+    n = grid.nx()
+    dx, dy = grid.dx(), grid.dy()
+    X, Y = np.meshgrid(grid.point(0, np.arange(n)), grid.point(1, np.arange(n)), indexing="ij")
+    alpha = _sample(solver.alpha_function, X, Y).ravel()
+    beta = np.concatenate([_sample(solver.beta_function, X - dx / 2.0, Y).ravel(),
+                           _sample(solver.beta_function, X + dx / 2.0, Y).ravel(),
+                           _sample(solver.beta_function, X, Y - dy / 2.0).ravel(),
+                           _sample(solver.beta_function, X, Y + dy / 2.0).ravel()])
+    lam = _sample(solver.lambda_function, X, Y).ravel()
+    return alpha, beta, lam
+
+
 class FiniteVolumeSolver:
     """FiniteVolumeSolver (FiniteVolumeSolver.hpp:53-162) on the GPU.
 
     ``solver_type = FISHPACK90`` solves u_xx + u_yy + lambda u = f with
     ``lambda = lambda_function(0, 0)`` (FiniteVolumeSolver.cpp:253); alpha and beta are not used,
-    exactly as in the reference's FISHPACK90 branch.
+    exactly as in the reference's FISHPACK90 branch.  ``solver_type = FivePointStencil`` solves
+    alpha div(beta grad u) + lambda u = f with the coefficient functions sampled per cell
+    (FiniteVolumeSolver.cpp:27-223); they are called with numpy arrays.
     """
 
-    def __init__(self, alpha_function=None, beta_function=None, lambda_function=None, rhs_function=None):
-        self.solver_type = FISHPACK90
+    def __init__(self, alpha_function=None, beta_function=None, lambda_function=None, rhs_function=None,
+                 solver_type: str = FivePointStencil):
+        self.solver_type = solver_type  # the reference's default is FivePointStencil
         self.alpha_function = alpha_function or (lambda x, y: 1.0)
         self.beta_function = beta_function or (lambda x, y: 1.0)
         self.lambda_function = lambda_function or (lambda x, y: 0.0)
@@ -85,10 +109,20 @@ class FiniteVolumeSolver:
         return (_solver_code(self.solver_type), grid.nx(), grid.xLower(), grid.xUpper(),
                 grid.yLower(), grid.yUpper(), self._lam())
 
+    def _fp_args(self, grid: FiniteVolumeGrid):
+        if grid.nx() != grid.ny():
+            raise ValueError("square patches only (nx == ny)")
+        a, b, l = sample_coefficients(self, grid)
+        self._keep = (a, b, l)
+        return (grid.nx(), grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), dptr(a), dptr(b), dptr(l))
+
     def buildD2N(self, grid: FiniteVolumeGrid) -> np.ndarray:
         n = grid.nx()
         T = np.empty((4 * n, 4 * n))
-        check(_lib.load().ef_fv_build_d2n(*self._args(grid), dptr(T)))
+        if self.solver_type == FivePointStencil:
+            check(_lib.load().ef_fv5_build_d2n(*self._fp_args(grid), dptr(T)))
+        else:
+            check(_lib.load().ef_fv_build_d2n(*self._args(grid), dptr(T)))
         return T
 
     def solve(self, grid: FiniteVolumeGrid, dirichlet_data, rhs_data) -> np.ndarray:
@@ -98,7 +132,10 @@ class FiniteVolumeSolver:
         if g.size != 4 * n or f.size != n * n:
             raise ValueError("size mismatch")
         u = np.empty(n * n)
-        check(_lib.load().ef_fv_solve(*self._args(grid), dptr(g), dptr(f), dptr(u)))
+        if self.solver_type == FivePointStencil:
+            check(_lib.load().ef_fv5_solve(*self._fp_args(grid), dptr(g), dptr(f), dptr(u)))
+        else:
+            check(_lib.load().ef_fv_solve(*self._args(grid), dptr(g), dptr(f), dptr(u)))
         return u
 
     def mapD2N(self, grid: FiniteVolumeGrid, dirichlet_data, rhs_data) -> np.ndarray:
@@ -108,7 +145,10 @@ class FiniteVolumeSolver:
         if g.size != 4 * n or f.size != n * n:
             raise ValueError("size mismatch")
         h = np.empty(4 * n)
-        check(_lib.load().ef_fv_map_d2n(*self._args(grid), dptr(g), dptr(f), dptr(h)))
+        if self.solver_type == FivePointStencil:
+            check(_lib.load().ef_fv5_map_d2n(*self._fp_args(grid), dptr(g), dptr(f), dptr(h)))
+        else:
+            check(_lib.load().ef_fv_map_d2n(*self._args(grid), dptr(g), dptr(f), dptr(h)))
         return h
 
     def particularNeumannData(self, grid: FiniteVolumeGrid, rhs_data) -> np.ndarray:
@@ -255,6 +295,16 @@ class HPSAlgorithm:
         check(lib.ef_hps_info(h, C.byref(nl), C.byref(n), C.byref(M), C.byref(nb)))
         self.num_leaves, self.n, self.M, self.device_bytes = nl.value, n.value, M.value, nb.value
         self._apply_options()
+        if patch_solver.solver_type == FivePointStencil:
+            self._set_coefficients()
+
+    def _set_coefficients(self):
+        """Samples alpha, beta, lambda on every leaf (FiniteVolumeSolver.cpp:66-79) into the library."""
+        parts = [sample_coefficients(self.patch_solver, p.grid()) for p in self.mesh.patches]
+        a = np.ascontiguousarray(np.concatenate([p[0] for p in parts]))
+        b = np.ascontiguousarray(np.concatenate([p[1] for p in parts]))
+        l = np.ascontiguousarray(np.concatenate([p[2] for p in parts]))
+        check(_lib.load().ef_hps_set_coefficients(self._h, dptr(a), dptr(b), dptr(l)))
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and _lib._LIB is not None:

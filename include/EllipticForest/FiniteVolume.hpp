@@ -103,30 +103,71 @@ public:
     }
     double efLambda() const { return lambda_function ? lambda_function(0, 0) : 0.0; }
 
+    // FivePointStencil coefficients of one patch sampled at the points of FiniteVolumeSolver.cpp:66-79:
+    // alpha(x_i, y_j); beta at x_i -/+ dx/2.0 and y_j -/+ dy/2.0 (all W, then E, S, N); lambda(x_i, y_j)
+    void sampleCoefficients(FiniteVolumeGrid& grid, double* alpha, double* beta, double* lambda) const {
+        const std::size_t nx = grid.nx(), ny = grid.ny(), N = nx * ny;
+        const double dx = grid.dx(), dy = grid.dy();
+        for (std::size_t i = 0; i < nx; ++i)
+            for (std::size_t j = 0; j < ny; ++j) {
+                const double xi = grid(0, i), yj = grid(1, j);
+                const std::size_t c = j + i * ny;
+                alpha[c] = alpha_function(xi, yj);
+                beta[c] = beta_function(xi - dx / 2.0, yj);
+                beta[N + c] = beta_function(xi + dx / 2.0, yj);
+                beta[2 * N + c] = beta_function(xi, yj - dy / 2.0);
+                beta[3 * N + c] = beta_function(xi, yj + dy / 2.0);
+                lambda[c] = lambda_function(xi, yj);
+            }
+    }
+
     Vector<double> solve(FiniteVolumeGrid& grid, Vector<double>& dirichlet_data, Vector<double>& rhs_data) {
         const int n = int(grid.nx());
         checkSizes(grid, dirichlet_data, rhs_data);
         Vector<double> u(std::size_t(n) * n);
-        efCheck(ef_fv_solve(efType(), n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), efLambda(),
-                            dirichlet_data.dataPointer(), rhs_data.dataPointer(), u.dataPointer()),
-                "FiniteVolumeSolver::solve");
+        if (solver_type == FiniteVolumeSolverType::FivePointStencil) {
+            Coef c(grid, *this);
+            efCheck(ef_fv5_solve(n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), c.a.data(),
+                                 c.b.data(), c.l.data(), dirichlet_data.dataPointer(), rhs_data.dataPointer(),
+                                 u.dataPointer()),
+                    "FiniteVolumeSolver::solve");
+        } else {
+            efCheck(ef_fv_solve(efType(), n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), efLambda(),
+                                dirichlet_data.dataPointer(), rhs_data.dataPointer(), u.dataPointer()),
+                    "FiniteVolumeSolver::solve");
+        }
         return u;
     }
     Vector<double> mapD2N(FiniteVolumeGrid& grid, Vector<double>& dirichlet_data, Vector<double>& rhs_data) {
         const int n = int(grid.nx());
         checkSizes(grid, dirichlet_data, rhs_data);
         Vector<double> h(4 * std::size_t(n));
-        efCheck(ef_fv_map_d2n(efType(), n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), efLambda(),
-                              dirichlet_data.dataPointer(), rhs_data.dataPointer(), h.dataPointer()),
-                "FiniteVolumeSolver::mapD2N");
+        if (solver_type == FiniteVolumeSolverType::FivePointStencil) {
+            Coef c(grid, *this);
+            efCheck(ef_fv5_map_d2n(n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), c.a.data(),
+                                   c.b.data(), c.l.data(), dirichlet_data.dataPointer(), rhs_data.dataPointer(),
+                                   h.dataPointer()),
+                    "FiniteVolumeSolver::mapD2N");
+        } else {
+            efCheck(ef_fv_map_d2n(efType(), n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(),
+                                  efLambda(), dirichlet_data.dataPointer(), rhs_data.dataPointer(), h.dataPointer()),
+                    "FiniteVolumeSolver::mapD2N");
+        }
         return h;
     }
     Matrix<double> buildD2N(FiniteVolumeGrid& grid) {
         const int n = int(grid.nx());
         Matrix<double> T(4 * std::size_t(n), 4 * std::size_t(n));
-        efCheck(ef_fv_build_d2n(efType(), n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), efLambda(),
-                                T.dataPointer()),
-                "FiniteVolumeSolver::buildD2N");
+        if (solver_type == FiniteVolumeSolverType::FivePointStencil) {
+            Coef c(grid, *this);
+            efCheck(ef_fv5_build_d2n(n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(), c.a.data(),
+                                     c.b.data(), c.l.data(), T.dataPointer()),
+                    "FiniteVolumeSolver::buildD2N");
+        } else {
+            efCheck(ef_fv_build_d2n(efType(), n, grid.xLower(), grid.xUpper(), grid.yLower(), grid.yUpper(),
+                                    efLambda(), T.dataPointer()),
+                    "FiniteVolumeSolver::buildD2N");
+        }
         return T;
     }
     Vector<double> particularNeumannData(FiniteVolumeGrid& grid, Vector<double>& rhs_data) {
@@ -135,6 +176,13 @@ public:
     }
 
 private:
+    struct Coef {
+        std::vector<double> a, b, l;
+        Coef(FiniteVolumeGrid& g, const FiniteVolumeSolver& s)
+            : a(g.nx() * g.ny()), b(4 * g.nx() * g.ny()), l(g.nx() * g.ny()) {
+            s.sampleCoefficients(g, a.data(), b.data(), l.data());
+        }
+    };
     static void checkSizes(FiniteVolumeGrid& grid, Vector<double>& g, Vector<double>& f) {
         if (grid.nx() != grid.ny()) throw std::invalid_argument("[FiniteVolumeSolver] square patches only");
         if (g.size() != 4 * grid.nx() || f.size() != grid.nx() * grid.ny())

@@ -171,6 +171,18 @@ private:
                 "HPSAlgorithm: create");
         long long bytes = 0;
         efCheck(ef_hps_info(h_, &num_leaves_, &n_, &M_, &bytes), "HPSAlgorithm: info");
+        if (patch_solver.solver_type == FiniteVolumeSolverType::FivePointStencil) {
+            // variable coefficients sampled on every leaf (FiniteVolumeSolver.cpp:66-79)
+            const std::size_t nn = std::size_t(n_) * n_;
+            std::vector<double> a(num_leaves_ * nn), b(4 * num_leaves_ * nn), l(num_leaves_ * nn);
+            std::size_t k = 0;
+            for (auto* leaf : mesh.leaves()) {
+                patch_solver.sampleCoefficients(leaf->data.grid(), a.data() + k * nn, b.data() + 4 * k * nn,
+                                                l.data() + k * nn);
+                ++k;
+            }
+            efCheck(ef_hps_set_coefficients(h_, a.data(), b.data(), l.data()), "HPSAlgorithm: coefficients");
+        }
     }
     void requireBuilt() {
         if (!h_ || !isBuilt) throw std::logic_error("[HPSAlgorithm] build stage must run first");

@@ -66,6 +66,12 @@ int ef_mesh_destroy(ef_mesh* mesh);
  * solver_type EF_SOLVER_FISHPACK90: u_xx + u_yy + lambda u = f (FiniteVolumeSolver.cpp:224-290,
  * lambda = lambda_function(0,0)). */
 int ef_hps_create(const ef_mesh* mesh, int solver_type, double lambda, ef_hps** out);
+/* FivePointStencil coefficients (required before ef_hps_build for EF_SOLVER_FIVE_POINT), sampled
+ * per leaf cell at the reference's points (FiniteVolumeSolver.cpp:66-79), host arrays in leaf
+ * order: alpha(x_i, y_j) (n*n per leaf), beta at the cell's W, E, S, N faces (x_i -/+ dx/2, y_j),
+ * (x_i, y_j -/+ dy/2) (4*n*n per leaf: all W values, then E, S, N), lambda(x_i, y_j) (n*n). */
+int ef_hps_set_coefficients(ef_hps* hps, const double* alpha, const double* beta,
+                            const double* lambda);
 /* Option keys of the reference: "cache-operators", "homogeneous-rhs" (HPSAlgorithm.hpp:134,532). */
 int ef_hps_set_option(ef_hps* hps, const char* key, int value);
 /* Use an external CUDA stream (cudaStream_t) for all work of this handle; NULL = default stream. */
@@ -131,6 +137,18 @@ int ef_fv_solve(int solver_type, int n, double x_lower, double x_upper, double y
 int ef_fv_map_d2n(int solver_type, int n, double x_lower, double x_upper, double y_lower,
                   double y_upper, double lambda, const double* g_host, const double* f_host,
                   double* h_host);
+
+/* FiniteVolumeSolver with solver_type FivePointStencil (FiniteVolumeSolver.cpp:27-223): the same
+ * three operations for one patch whose coefficients are sampled as for ef_hps_set_coefficients
+ * (alpha n*n, beta 4*n*n, lambda n*n). */
+int ef_fv5_build_d2n(int n, double x_lower, double x_upper, double y_lower, double y_upper,
+                     const double* alpha, const double* beta, const double* lambda, double* T_host);
+int ef_fv5_solve(int n, double x_lower, double x_upper, double y_lower, double y_upper,
+                 const double* alpha, const double* beta, const double* lambda, const double* g_host,
+                 const double* f_host, double* u_host);
+int ef_fv5_map_d2n(int n, double x_lower, double x_upper, double y_lower, double y_upper,
+                   const double* alpha, const double* beta, const double* lambda,
+                   const double* g_host, const double* f_host, double* h_host);
 
 /* ---- Single patch without allocation -------------------------------------------------------- */
 

@@ -41,7 +41,7 @@ def ef(lib):
                                        (32, (-1, 1, -1, 1), -3.0)])
 def test_build_d2n_matches_oracle(ef, n, box, lam):
     gg = ef.FiniteVolumeGrid(n, box[0], box[1], n, box[2], box[3])
-    s = ef.FiniteVolumeSolver(lambda_function=lambda x, y: lam)
+    s = ef.FiniteVolumeSolver(lambda_function=lambda x, y: lam, solver_type=ef.FISHPACK90)
     T = s.buildD2N(gg)
     og = O.FiniteVolumeGrid(n, box[0], box[1], n, box[2], box[3])
     To = O.FiniteVolumeSolver(solver_type=O.FISHPACK90, lambda_function=lambda x, y: lam).buildD2N(og)
@@ -54,7 +54,7 @@ def test_patch_solve_and_map_d2n_match_oracle(ef, n):
     g, f = rng.standard_normal(4 * n), rng.standard_normal(n * n)
     gg = ef.FiniteVolumeGrid(n, -1, 2, n, 0, 3)
     og = O.FiniteVolumeGrid(n, -1, 2, n, 0, 3)
-    s = ef.FiniteVolumeSolver()
+    s = ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90)
     so = O.FiniteVolumeSolver(solver_type=O.FISHPACK90)
     assert rel(s.solve(gg, g, f), so.solve(og, g, f)) <= REL
     assert rel(s.mapD2N(gg, g, f), so.mapD2N(og, g, f)) <= REL
@@ -70,7 +70,7 @@ def test_patch_solver_readme_error_table(ef, n):
     g = np.concatenate([u_exact(-1, y), u_exact(1, y), u_exact(x, -1), u_exact(x, 1)])
     X, Y = np.meshgrid(x, y, indexing="ij")
     ue = u_exact(X, Y).ravel()
-    u = ef.FiniteVolumeSolver().solve(gg, g, -ue)
+    u = ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90).solve(gg, g, -ue)
     err = np.abs(u - ue).max()
     assert abs(err - ref) <= 1e-8 * ref
 
@@ -84,7 +84,7 @@ def run_gpu(ef, mesh_kind, n, dom, f, bc, options=None, lam=0.0, patch_g=None):
         mesh = ef.Mesh().uniform(mesh_kind[1], root)
     else:
         mesh = ef.Mesh().refineByFunction(mesh_kind[1], 0.0, mesh_kind[2], mesh_kind[3], root)
-    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(lambda_function=lambda x, y: lam), options)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(lambda_function=lambda x, y: lam, solver_type=ef.FISHPACK90), options)
     hps.setupStage()
     hps.buildStage()
     hps.upwardsStage(f)
@@ -263,7 +263,7 @@ def test_repeated_solves_on_one_build(ef):
     dom = (-1.0, 1.0, -1.0, 1.0)
     root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(8, *dom[:2], 8, *dom[2:]))
     mesh = ef.Mesh().uniform(3, root)
-    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver())
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
     hps.buildStage()
     for seed in (11, 12):
         f, bc = _random_problem(seed)
@@ -302,7 +302,7 @@ def test_linearity_large(ef):
     dom = (-1.0, 1.0, -1.0, 1.0)
     root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, *dom[:2], 16, *dom[2:]))
     mesh = ef.Mesh().uniform(5, root)
-    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver())
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
     hps.buildStage()
     f1, b1 = _random_problem(21)
     f2, b2 = _random_problem(22)
