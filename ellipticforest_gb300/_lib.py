@@ -61,6 +61,11 @@ SIGNATURES = {
     "ef_hps_load_device_async": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ef_hps_solve_device_async": (C.c_int, [_vp, C.c_int]),
     "ef_hps_synchronize": (C.c_int, [_vp]),
+    "ef_hps_mixed_init": (C.c_int, [_vp, C.c_int]),
+    "ef_hps_mixed_buffers": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
+    "ef_hps_mixed_solve_async": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "ef_hps_mixed_solve": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, _dp]),
+    "ef_hps_mixed_residuals": (C.c_int, [_vp, C.c_int, _dp]),
     "ef_kernel_launches": (C.c_int, [C.POINTER(C.c_longlong)]),
     "ef_hps_profile_enable": (C.c_int, [_vp, C.c_int]),
     "ef_hps_profile_count": (C.c_int, [_vp, C.POINTER(C.c_int)]),

@@ -23,6 +23,7 @@ struct ef_mesh {
 
 struct ef_hps {
     std::unique_ptr<efgb::Hps> hps;
+    std::unique_ptr<efgb::MixedSolver> mixed;
     bool cache_operators = false;
     bool homogeneous_rhs = false;
     bool upward_done = false;
@@ -294,6 +295,7 @@ int ef_hps_setup(ef_hps* h) {
 int ef_hps_build(ef_hps* h) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     return guarded([&] {
+        h->mixed.reset();  // FP32 operator copies belong to the previous build
         h->hps->build();
         if (h->hps->singular_count() > 0)
             return fail(EF_ERR_SINGULAR, std::to_string(h->hps->singular_count()) +
@@ -432,6 +434,69 @@ int ef_hps_solve_device_async(ef_hps* h, int b_is_zero) {
 int ef_hps_synchronize(ef_hps* h) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     return cuda_status(cudaStreamSynchronize(h->hps->stream()), "synchronize");
+}
+
+int ef_hps_mixed_init(ef_hps* h, int bmax) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "mixed solver before build stage");
+    return guarded([&] {
+        h->mixed.reset();
+        h->mixed = std::make_unique<efgb::MixedSolver>(*h->hps, bmax);
+        return EF_OK;
+    });
+}
+
+int ef_hps_mixed_buffers(ef_hps* h, double** f, double** a, double** r, double** u) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    if (f) *f = h->mixed->f();
+    if (a) *a = h->mixed->a();
+    if (r) *r = h->mixed->r();
+    if (u) *u = h->mixed->u();
+    return EF_OK;
+}
+
+int ef_hps_mixed_solve_async(ef_hps* h, int batch, int sweeps) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    return guarded([&] {
+        h->mixed->solve(batch, sweeps);
+        return cuda_status(cudaGetLastError(), "mixed solve launch");
+    });
+}
+
+int ef_hps_mixed_solve(ef_hps* h, int batch, int sweeps, const double* f, const double* a, const double* r,
+                       double* u) {
+    if (!h || !f || !a || !r || !u) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    if (batch < 1 || batch > h->mixed->bmax()) return fail(EF_ERR_INVALID, "batch size out of range");
+    return guarded([&] {
+        efgb::Hps& H = *h->hps;
+        efgb::MixedSolver& X = *h->mixed;
+        cudaStream_t s = H.stream();
+        const size_t cells = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n() * batch;
+        const size_t m = 4 * size_t(H.root_M()) * batch;
+        int st = cuda_status(cudaMemcpyAsync(X.f(), f, cells * 8, cudaMemcpyHostToDevice, s), "copy f");
+        if (!st) st = cuda_status(cudaMemcpyAsync(X.a(), a, m * 8, cudaMemcpyHostToDevice, s), "copy a");
+        if (!st) st = cuda_status(cudaMemcpyAsync(X.r(), r, m * 8, cudaMemcpyHostToDevice, s), "copy r");
+        if (st) return st;
+        X.solve(batch, sweeps);
+        st = cuda_status(cudaGetLastError(), "mixed solve launch");
+        if (!st) st = cuda_status(cudaMemcpyAsync(u, X.u(), cells * 8, cudaMemcpyDeviceToHost, s), "copy u");
+        if (st) return st;
+        return cuda_status(cudaStreamSynchronize(s), "mixed solve");
+    });
+}
+
+int ef_hps_mixed_residuals(ef_hps* h, int passes, double* out) {
+    if (!h || !out) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    if (passes < 1 || passes > efgb::MixedSolver::kMaxPasses) return fail(EF_ERR_INVALID, "passes out of range");
+    efgb::MixedSolver& X = *h->mixed;
+    int st = cuda_status(cudaStreamSynchronize(h->hps->stream()), "mixed residuals");
+    if (st) return st;
+    return cuda_status(cudaMemcpy(out, X.residual_max(), size_t(passes) * X.bmax() * 8, cudaMemcpyDeviceToHost),
+                       "copy residuals");
 }
 
 int ef_kernel_launches(long long* count) {

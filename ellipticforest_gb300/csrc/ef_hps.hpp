@@ -69,8 +69,11 @@ struct LeafTypeHost {
     double* T = nullptr;
 };
 
+class MixedSolver;
+
 class Hps {
 public:
+    friend class MixedSolver;
     Hps(const Mesh& mesh, int solver_type, double lambda, bool cache_operators);
     ~Hps();
     Hps(const Hps&) = delete;
@@ -197,6 +200,70 @@ private:
     cudaEvent_t ev_get();
     void pb(const char* name);                 // begin section
     void pe(double bytes, double flops);       // end section
+};
+
+// Mixed-precision many-RHS solver on a built FP64 Hps (FISHPACK90 leaves, Dirichlet root data):
+// FP32 copies of S, X^{-1}, H and the leaf tables; FP64 residual (5-point leaf residual + interface
+// flux mismatches) and FP32 correction passes, see ef_mixed.cu.
+class MixedSolver {
+public:
+    MixedSolver(Hps& hps, int bmax);
+    ~MixedSolver();
+    MixedSolver(const MixedSolver&) = delete;
+    MixedSolver& operator=(const MixedSolver&) = delete;
+
+    int bmax() const { return bmax_; }
+    // Resident inputs: f [B][L][n*n], a and r [B][4M] (b == 0 assumed); output u [B][L][n*n].
+    double* f() const { return f_; }
+    double* a() const { return a_; }
+    double* r() const { return r_; }
+    double* u() const { return u64_; }
+    // max |leaf residual| per request before each pass: [passes][bmax]
+    double* residual_max() const { return rmax_; }
+    size_t device_bytes() const { return bytes_; }
+    // 1 + sweeps FP32 passes on B <= bmax requests; asynchronous on the Hps stream.
+    void solve(int B, int sweeps);
+    static constexpr int kMaxPasses = 8;
+
+private:
+    struct MNode {
+        float *S = nullptr, *Xi = nullptr, *H32 = nullptr;
+        float *h32 = nullptr, *hd32 = nullptr, *w32 = nullptr, *m32 = nullptr, *g32 = nullptr;
+        double *uG = nullptr, *g64 = nullptr, *h64 = nullptr;
+        std::vector<float*> hs32, gs32;
+        std::vector<double*> hs64, gs64;
+        float *hc32 = nullptr, *gf32 = nullptr;
+        double *hc64 = nullptr, *gf64 = nullptr;
+    };
+    struct MGroup {
+        int level = 0, s = 0, cnt = 0;
+        MixItem* d_items = nullptr;
+        MixConv* d_conv = nullptr;
+    };
+    struct MStep {
+        int level = 0, nf = 0, count = 0;
+        void** in32 = nullptr;
+        void** out32 = nullptr;
+        void** in64 = nullptr;
+        void** out64 = nullptr;
+    };
+    void residual(int B, double* rmax);
+    void pass(int B);
+
+    Hps& H_;
+    int bmax_;
+    char* arena_ = nullptr;
+    size_t bytes_ = 0;
+    std::vector<MNode> mn_;
+    std::vector<MGroup> groups_;
+    std::vector<MStep> hsteps_, gsteps_;
+    LeafType32* d_types32_ = nullptr;
+    MixLeaf* d_leaves_ = nullptr;
+    float* q32_ = nullptr;
+    double *u64_ = nullptr, *f_ = nullptr, *a_ = nullptr, *r_ = nullptr, *rmax_ = nullptr;
+    char* uG_begin_ = nullptr;
+    size_t uG_bytes_ = 0;
+    float* tables_ = nullptr;
 };
 
 }  // namespace efgb

@@ -105,6 +105,64 @@ void fp_solve(cudaStream_t st, int mode, const FpLeaf* leaves, const LeafItem* i
               int nmax);
 
 // ------------------------------------------------------------------------------------------------
+// Mixed-precision many-RHS passes (ef_mixed.cu).  Node vectors are [len][B], leaf cells [B][L][n*n].
+// ------------------------------------------------------------------------------------------------
+struct LeafType32 {
+    int n;
+    float dx, dy;
+    const float* V;
+    const float* Dinv;
+};
+
+struct MixLeaf {
+    int type;
+    float* g32;   // [4n][B] Dirichlet data of the FP32 pass
+    float* h32;   // [4n][B] particular flux of the FP32 pass
+    double* g64;  // [4n][B] exact Dirichlet data of the state
+    double* h64;  // [4n][B] edge flux of the state
+};
+
+struct MixItem {
+    const float* S;       // 4s x 8s
+    const float* Xi;      // 4s x 4s
+    const float* H;       // 8s x 2s (compact)
+    const float* hc[4];   // children's coarsened particular flux [4s][B]
+    float* h;             // [8s][B]
+    float* hd;            // [4s][B]
+    float* w;             // [4s][B]
+    const float* m;       // [4s][B] interface flux mismatch of the state
+    const float* gf;      // [8s][B] own full-size Dirichlet data of the pass
+    float* gc[4];         // children's Dirichlet data of the pass [4s][B]
+    double* uG;           // [4s][B] interface values of the state
+    const double* gf64;   // [8s][B] own full-size exact Dirichlet data
+    double* gc64[4];      // children's exact Dirichlet data [4s][B]
+    const double* hc64[4];// children's coarsened edge flux [4s][B]
+    double* h64;          // [8s][B] own edge flux
+    float* mout;          // = m, written by the residual
+};
+
+struct MixConv {  // FP64 operators -> FP32 copies
+    const double* RHS;
+    const double* H;
+    float* S;
+    float* Xi;
+    float* H32;
+};
+
+void mx_convert(cudaStream_t st, const MixConv* items, int nitems, int s);
+void mx_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+void mx_down(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
+void mx_uncoarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
+void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
+               const float* q, double* u64);
+void mx_leaf_residual(cudaStream_t st, const LeafType* types, const MixLeaf* leaves, int L, int B, double lambda,
+                      const double* f, const double* u64, float* q, double* rmax);
+void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g);
+
+// ------------------------------------------------------------------------------------------------
 // Merge / upward / downward kernels
 // ------------------------------------------------------------------------------------------------
 struct MergeItem {

@@ -434,6 +434,38 @@ class HPSAlgorithm:
         check(_lib.load().ef_hps_device_buffers(self._h, *[C.byref(p) for p in ptrs]))
         return [p.value for p in ptrs]  # f, u, a, b, r
 
+    # -- mixed precision, many right-hand sides (no counterpart in the reference) ----------------
+    def mixed_init(self, bmax: int):
+        """FP32 operator copies for batches of up to bmax requests (after buildStage)."""
+        check(_lib.load().ef_hps_mixed_init(self._h, int(bmax)))
+        self.mixed_bmax = int(bmax)
+
+    def mixed_solve(self, f, a, r, sweeps: int = 1) -> np.ndarray:
+        """Solve a block of requests: f [B, leaves*n*n], a and r [B, 4M] (a u = r on the root
+        faces).  Returns u [B, leaves*n*n] refined to the FP64 HPS solution."""
+        f = np.ascontiguousarray(np.atleast_2d(f), dtype=np.float64)
+        a = np.ascontiguousarray(np.atleast_2d(a), dtype=np.float64)
+        r = np.ascontiguousarray(np.atleast_2d(r), dtype=np.float64)
+        B = f.shape[0]
+        if f.shape[1] != self.num_leaves * self.n * self.n or a.shape != (B, 4 * self.M) or r.shape != (B, 4 * self.M):
+            raise ValueError("mixed_solve: bad shapes")
+        u = np.empty_like(f)
+        check(_lib.load().ef_hps_mixed_solve(self._h, B, int(sweeps), dptr(f), dptr(a), dptr(r), dptr(u)))
+        return u
+
+    def mixed_residuals(self, passes: int) -> np.ndarray:
+        out = np.empty((passes, self.mixed_bmax))
+        check(_lib.load().ef_hps_mixed_residuals(self._h, int(passes), dptr(out)))
+        return out
+
+    def mixed_buffers(self):
+        ptrs = [C.c_void_p() for _ in range(4)]
+        check(_lib.load().ef_hps_mixed_buffers(self._h, *[C.byref(p) for p in ptrs]))
+        return [p.value for p in ptrs]  # f, a, r, u
+
+    def mixed_solve_async(self, batch: int, sweeps: int = 1):
+        check(_lib.load().ef_hps_mixed_solve_async(self._h, int(batch), int(sweeps)))
+
     def profile_enable(self, on: bool = True):
         check(_lib.load().ef_hps_profile_enable(self._h, int(on)))
 

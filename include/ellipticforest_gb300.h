@@ -110,6 +110,23 @@ int ef_hps_load_device_async(ef_hps* hps, const double* f_dev, const double* a_d
 int ef_hps_solve_device_async(ef_hps* hps, int b_is_zero);
 int ef_hps_synchronize(ef_hps* hps);
 
+/* ---- Mixed precision, many right-hand sides (no counterpart in the reference) ---------------
+ * After ef_hps_build: FP32 copies of the merge operators and leaf tables; each solve runs FP32
+ * HPS passes on a block of up to bmax requests and refines them against an FP64 residual (the
+ * 5-point residual of every leaf cell plus the flux mismatch at every merge interface), so the
+ * result converges to the FP64 HPS solution.  FISHPACK90 leaves and Dirichlet root data
+ * (b == 0) only. */
+int ef_hps_mixed_init(ef_hps* hps, int bmax);
+/* Resident buffers: f [B][num_leaves*n*n], a and r [B][4M] (root data, a u = r), u [B][...]. */
+int ef_hps_mixed_buffers(ef_hps* hps, double** f_dev, double** a_dev, double** r_dev, double** u_dev);
+/* 1 + sweeps passes on the first `batch` requests of the resident buffers, no host sync. */
+int ef_hps_mixed_solve_async(ef_hps* hps, int batch, int sweeps);
+/* Host convenience form: copies the inputs in, solves, copies u out (synchronous). */
+int ef_hps_mixed_solve(ef_hps* hps, int batch, int sweeps, const double* f_host, const double* a_host,
+                       const double* r_host, double* u_host);
+/* max |leaf residual| per request before each pass: passes x bmax doubles (synchronous). */
+int ef_hps_mixed_residuals(ef_hps* hps, int passes, double* out_host);
+
 /* ---- Instrumentation (the reference's stage timers, EllipticForestApp.hpp:39-137) ------------ */
 
 /* Kernels launched by this library so far (all handles). */

@@ -1,0 +1,85 @@
+"""Mixed-precision many-RHS form: FP32 HPS passes refined against the FP64 residual must reach the
+FP64 HPS solution to <= 1e-10 relative, on uniform and adaptive trees, and a request's result must
+not depend on the other requests of its block."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ef(lib):
+    import ellipticforest_gb300
+    return ellipticforest_gb300
+
+
+def requests(hps, mesh, B, seed):
+    rng = np.random.default_rng(seed)
+    X, Y = mesh.cell_centres()
+    pts = hps.boundary_points()
+    F, A, R = [], [], []
+    for _ in range(B):
+        amp, cx, cy, wd = rng.uniform(-1, 1, 8), rng.uniform(-1, 1, 8), rng.uniform(-1, 1, 8), rng.uniform(0.05, 0.3, 8)
+        f = sum(amp[k] * np.exp(-((X - cx[k]) ** 2 + (Y - cy[k]) ** 2) / wd[k] ** 2) for k in range(8))
+        co = rng.standard_normal((4, 6))
+        r = np.concatenate([sum(co[s, m] * np.sin((m + 1) * np.pi * ((y if s < 2 else x) + 1) / 2) for m in range(6))
+                            for s, (x, y) in enumerate(pts)])
+        F.append(f); A.append(np.ones_like(r)); R.append(r)
+    return np.array(F), np.array(A), np.array(R)
+
+
+def fp64_solutions(hps, F, A, R):
+    out = []
+    for f, a, r in zip(F, A, R):
+        hps.upwards_array(f)
+        hps.solve_arrays(a, np.zeros_like(a), r)
+        out.append(hps.leaf_solution())
+    return np.array(out)
+
+
+def make(ef, kind, n, dom):
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, dom[0], dom[1], n, dom[2], dom[3]))
+    if kind[0] == "uniform":
+        mesh = ef.Mesh().uniform(kind[1], root)
+    else:
+        mesh = ef.Mesh().refineByFunction(kind[1], 0.0, kind[2], kind[3], root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hps.buildStage()
+    return mesh, hps
+
+
+@pytest.mark.parametrize("kind,n", [(("uniform", 4), 16), (("uniform", 5), 8)])
+def test_mixed_reaches_fp64_solution_uniform(ef, kind, n):
+    mesh, hps = make(ef, kind, n, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, 3, 11)
+    ref = fp64_solutions(hps, F, A, R)
+    hps.mixed_init(4)
+    u = hps.mixed_solve(F, A, R, sweeps=2)
+    for k in range(3):
+        err = np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= TOL, (k, err)
+    res = hps.mixed_residuals(3)
+    assert np.all(res[2, :3] < res[0, :3] * 1e-8)
+
+
+def test_mixed_reaches_fp64_solution_adaptive(ef):
+    fn = lambda x, y: y > 0.45 and x > 0.45
+    mesh, hps = make(ef, ("adaptive", fn, 0, 5), 8, (0.0, 1.0, 0.0, 1.0))
+    F, A, R = requests(hps, mesh, 2, 5)
+    ref = fp64_solutions(hps, F, A, R)
+    hps.mixed_init(2)
+    u = hps.mixed_solve(F, A, R, sweeps=2)
+    for k in range(2):
+        assert np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max() <= TOL
+
+
+def test_mixed_result_same_alone_and_in_a_block(ef):
+    mesh, hps = make(ef, ("uniform", 3), 16, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, 11, 23)
+    hps.mixed_init(11)
+    block = hps.mixed_solve(F, A, R, sweeps=1)
+    for k in (0, 5, 10):
+        alone = hps.mixed_solve(F[k:k + 1], A[k:k + 1], R[k:k + 1], sweeps=1)
+        assert np.array_equal(alone[0], block[k])
