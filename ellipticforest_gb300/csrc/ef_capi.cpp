@@ -484,7 +484,9 @@ int ef_hps_mixed_solve(ef_hps* h, int batch, int sweeps, const double* f, const 
         st = cuda_status(cudaGetLastError(), "mixed solve launch");
         if (!st) st = cuda_status(cudaMemcpyAsync(u, X.u(), cells * 8, cudaMemcpyDeviceToHost, s), "copy u");
         if (st) return st;
-        return cuda_status(cudaStreamSynchronize(s), "mixed solve");
+        st = cuda_status(cudaStreamSynchronize(s), "mixed solve");
+        if (!st && X.take_error()) return fail(EF_ERR_CUDA, "mixed solve: an operator tile copy did not complete");
+        return st;
     });
 }
 
@@ -495,6 +497,7 @@ int ef_hps_mixed_residuals(ef_hps* h, int passes, double* out) {
     efgb::MixedSolver& X = *h->mixed;
     int st = cuda_status(cudaStreamSynchronize(h->hps->stream()), "mixed residuals");
     if (st) return st;
+    if (X.take_error()) return fail(EF_ERR_CUDA, "mixed solve: an operator tile copy did not complete");
     return cuda_status(cudaMemcpy(out, X.residual_max(), size_t(passes) * X.bmax() * 8, cudaMemcpyDeviceToHost),
                        "copy residuals");
 }

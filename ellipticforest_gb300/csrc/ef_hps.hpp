@@ -223,6 +223,8 @@ public:
     size_t device_bytes() const { return bytes_; }
     // 1 + sweeps FP32 passes on B <= bmax requests; asynchronous on the Hps stream.
     void solve(int B, int sweeps);
+    // synchronises the stream; 1 when a kernel gave up waiting on a TMA copy since the last call
+    int take_error();
     static constexpr int kMaxPasses = 8;
 
 private:
@@ -239,6 +241,8 @@ private:
         int level = 0, s = 0, cnt = 0;
         MixItem* d_items = nullptr;
         MixConv* d_conv = nullptr;
+        float *S32 = nullptr, *Xi32 = nullptr, *H32 = nullptr;
+        CUtensorMap tmS{}, tmXi{}, tmH{};
     };
     struct MStep {
         int level = 0, nf = 0, count = 0;
@@ -247,8 +251,8 @@ private:
         void** in64 = nullptr;
         void** out64 = nullptr;
     };
-    void residual(int B, double* rmax);
-    void pass(int B);
+    void residual(int B, double* rmax, bool zero_state);
+    void pass(int B, bool first);
 
     Hps& H_;
     int bmax_;
@@ -261,6 +265,9 @@ private:
     MixLeaf* d_leaves_ = nullptr;
     float* q32_ = nullptr;
     double *u64_ = nullptr, *f_ = nullptr, *a_ = nullptr, *r_ = nullptr, *rmax_ = nullptr;
+    int* d_err_ = nullptr;
+    float* rleaf_ = nullptr;
+    MixCoef* d_coef_ = nullptr;
     char* uG_begin_ = nullptr;
     size_t uG_bytes_ = 0;
     float* tables_ = nullptr;

@@ -18,6 +18,7 @@
 // pi_WESN = {0,4,2,6,1,3,5,7} of HPSAlgorithm.hpp:979-993 is applied while gathering.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -149,17 +150,38 @@ struct MixConv {  // FP64 operators -> FP32 copies
     float* H32;
 };
 
+// Rows per tile of the FP32 node GEMMs (kind 0: X^{-1} and S, 4s rows per node; kind 1: compact H,
+// whose tiles stay inside one run of s rows): the largest of 64, 32, 16, 8, 4 dividing the run.
+inline int mx_tile_rows(int kind, int s) {
+    const int run = kind == 1 ? s : 4 * s;
+    for (int rt = 64; rt >= 4; rt /= 2)
+        if (run % rt == 0) return rt;
+    return 0;
+}
+
 void mx_convert(cudaStream_t st, const MixConv* items, int nitems, int s);
-void mx_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
-void mx_down(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+// hd = hc_upper - hc_lower - m (the correction's interface jump)
+void mx_hdiff(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+// FP32 node GEMM of one group: kind 0  w = X^{-1} hd;  kind 1  h = H w + hc;  kind 2  u = S gf + w
+// (scattered to the children and added to u_Gamma).  The group's operators are contiguous row-major
+// matrices read through the TMA tensor map tm (32 columns x mx_tile_rows rows per box, 128-byte
+// swizzle); err is set when a TMA wait times out.
+void mx_gemm(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
+             int* err);
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
 void mx_uncoarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
-               const float* q, double* u64);
-void mx_leaf_residual(cudaStream_t st, const LeafType* types, const MixLeaf* leaves, int L, int B, double lambda,
-                      const double* f, const double* u64, float* q, double* rmax);
+               const float* q, double* u64, int accumulate);
+// FP64 stencil constants of a leaf type: cx = 1/dx^2, cy = 1/dy^2, cc = lambda - 2cx - 2cy, 2/dx, 2/dy
+struct MixCoef {
+    double cx, cy, cc, dtn_x, dtn_y;
+};
+// FP64 residual of every leaf (n % 4 == 0); zero_state when u is identically zero; rleaf [B][L]
+// scratch for the per-request maximum rmax (may be null)
+void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leaves, int L, int B, int n,
+                      int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g);
 
 // ------------------------------------------------------------------------------------------------

@@ -16,7 +16,11 @@
 // The first pass starts from a zero state (the residual is then f plus the boundary terms), so
 // every pass is the same correction pass.  Node vectors are [len][B] (batch index fastest); leaf
 // cell arrays are [B][leaves][n*n].
+#include <cooperative_groups.h>
+
 #include "ef_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace efgb {
 
@@ -38,6 +42,30 @@ __device__ __forceinline__ void mx_child_ifaces(int c, int& Ia, int& Ib) {
     Ib = (c < 2) ? 2 : 3;
 }
 
+// float <-> double by integer bit manipulation.  GB300's FP64 pipe, which also converts between the
+// two widths, runs at a small fraction of its FP32 and integer rates; these stay off it.  Values
+// below the smallest normal number of the target type become signed zeros; d2f_bits rounds toward
+// zero.
+__device__ __forceinline__ double f2d_bits(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long e64 = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(sign | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+__device__ __forceinline__ float d2f_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = int((b >> 52) & 0x7ffull);
+    const unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+    const int e32 = e - 896;
+    if (e32 <= 0) return __uint_as_float(sign);
+    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
+}
+
 // ---- FP32 pass, upward ---------------------------------------------------------------------------
 // hd = hc_upper - hc_lower - m  (the correction's interface jump)
 __global__ void k_mx_hdiff(const MixItem* __restrict__ items, int s, int B) {
@@ -51,118 +79,243 @@ __global__ void k_mx_hdiff(const MixItem* __restrict__ items, int s, int B) {
     }
 }
 
-template <int LPR>
-__device__ __forceinline__ float group_sumf(float v) {
-#pragma unroll
-    for (int off = LPR / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
+// ---- FP32 node GEMMs: Y[rows][B] = A[rows][K] X[K][B] over all nodes of one group -----------------
+//
+// The operators of a group are stored back to back (one row-major matrix of cnt * rows_item rows)
+// and streamed by TMA in tiles of RT rows x 32 columns with the 128-byte swizzle; the request block
+// X (batch index fastest) is staged by cp.async.  Every thread owns 4 rows x 4 requests and reads
+// both operands as float4 from shared memory.  Top levels, whose few long rows would leave most SMs
+// idle, split K over the CTAs of a thread-block cluster and add the partial tiles through
+// distributed shared memory in rank order (deterministic).
+//   W    : w  = X^{-1} hd          rows 4s, K 4s
+//   H    : h  = H [w_Ia; w_Ib] + hc rows 8s, K 2s (compact H; a tile never spans two children)
+//   DOWN : u  = S gf + w           rows 4s, K 8s; u goes to both children and into u_Gamma (FP64)
+constexpr int kKC = 32;      // K columns per stage (128 bytes of FP32: one swizzle row)
+constexpr int kRT = 64;      // rows per tile (at most)
+constexpr int kStages = 3;
 
-// acc[k] += sum_c row[c] * x[c*B + b0 + k], k < BB, over the lanes of one group
-template <int LPR, int BB>
-__device__ __forceinline__ void mx_dot(const float* __restrict__ row, const float* __restrict__ x, int len,
-                                       int B, int b0, int nb, int sl, float* acc) {
-    for (int c = sl; c < len; c += LPR) {
-        const float a = __ldcs(row + c);
-        const float* xc = x + (long long)c * B + b0;
-#pragma unroll
-        for (int k = 0; k < BB; ++k)
-            if (k < nb) acc[k] = fmaf(a, __ldg(xc + k), acc[k]);
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, int nbytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+__device__ __forceinline__ long long global_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// bounded wait on an mbarrier phase: false after about a second without completion
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    long long t0 = 0;
+    for (unsigned it = 0;; ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (it == 0) t0 = global_ns();
+        else if ((it & 63) == 0 && global_ns() - t0 > 1000000000LL) return false;
     }
 }
-
-template <int LPR>
-__device__ __forceinline__ long long mx_group_row() {
-    return blockIdx.x * (long long)(256 / LPR) + threadIdx.x / LPR;
+// one TMA tile (32 columns x rows) of A into shared memory, completing on `bar`
+__device__ __forceinline__ void tma_load_tile(const CUtensorMap* tm, unsigned long long* bar, float* dst, int x,
+                                              int y, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
 }
 
-// w = X^{-1} hd
-template <int LPR, int BB>
-__global__ void __launch_bounds__(256) k_mx_gemv_w(const MixItem* __restrict__ items, int s, long long nrows, int B) {
-    const int sl = threadIdx.x & (LPR - 1);
-    const long long g = mx_group_row<LPR>();
-    const bool ok = g < nrows;
-    const int m4 = 4 * s;
-    const int item = ok ? int(g / m4) : 0, r = ok ? int(g - (long long)item * m4) : 0;
-    const MixItem& it = items[item];
-    const int b0 = blockIdx.y * BB, nb = min(BB, B - b0);
-    float acc[BB];
-#pragma unroll
-    for (int k = 0; k < BB; ++k) acc[k] = 0.f;
-    if (ok) mx_dot<LPR, BB>(it.Xi + (long long)r * m4, it.hd, m4, B, b0, nb, sl, acc);
-#pragma unroll
-    for (int k = 0; k < BB; ++k) acc[k] = group_sumf<LPR>(acc[k]);
-    if (ok && sl == 0)
-        for (int k = 0; k < nb; ++k) it.w[(long long)r * B + b0 + k] = acc[k];
+enum : int { MX_W = 0, MX_H = 1, MX_DOWN = 2 };
+
+template <int KIND>
+__host__ __device__ __forceinline__ void mx_shape(int s, int& rows_item, int& K) {
+    if (KIND == MX_W) { rows_item = 4 * s; K = 4 * s; }
+    else if (KIND == MX_H) { rows_item = 8 * s; K = 2 * s; }
+    else { rows_item = 4 * s; K = 8 * s; }
 }
 
-// h = H w + h_ext  (compact H rows, WESN order)
-template <int LPR, int BB>
-__global__ void __launch_bounds__(256) k_mx_gemv_h(const MixItem* __restrict__ items, int s, long long nrows, int B) {
-    const int sl = threadIdx.x & (LPR - 1);
-    const long long g = mx_group_row<LPR>();
-    const bool ok = g < nrows;
-    const int m8 = 8 * s;
-    const int item = ok ? int(g / m8) : 0, p = ok ? int(g - (long long)item * m8) : 0;
+template <int BN, int KIND>
+__global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                 const MixItem* __restrict__ items, int s, int B, int rt,
+                                                 int ksplit, int* __restrict__ err) {
+    constexpr int TXN = BN / 4;
+    __shared__ __align__(1024) float As[kStages][kRT * kKC];
+    __shared__ __align__(16) float Xs[kStages][kKC * BN];
+    __shared__ __align__(8) unsigned long long full[kStages];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tx = tid % TXN, ty = tid / TXN;
+    const int rq = rt / 4;  // thread rows: ty + i*rq, i < 4
+    int rows_item, K;
+    mx_shape<KIND>(s, rows_item, K);
+    const int tpi = rows_item / rt;
+    const int tile = blockIdx.x / ksplit, kp = blockIdx.x - tile * ksplit;
+    const int item = tile / tpi, tl = tile - item * tpi, row0 = tl * rt;
     const MixItem& it = items[item];
-    int c, q, Ia, Ib;
-    mx_ext_map(p, s, c, q);
-    mx_child_ifaces(c, Ia, Ib);
-    const int b0 = blockIdx.y * BB, nb = min(BB, B - b0);
-    float acc[BB];
-#pragma unroll
-    for (int k = 0; k < BB; ++k) acc[k] = 0.f;
-    if (ok) {
-        const float* row = it.H + (long long)p * (2LL * s);
-        mx_dot<LPR, BB>(row, it.w + (long long)Ia * s * B, s, B, b0, nb, sl, acc);
-        mx_dot<LPR, BB>(row + s, it.w + (long long)Ib * s * B, s, B, b0, nb, sl, acc);
+    const int b0 = blockIdx.y * BN;
+    const float* X1;
+    const float* X2;
+    int kb;
+    int hc_c = 0;
+    if (KIND == MX_W) { X1 = it.hd; X2 = X1; kb = K; }
+    else if (KIND == MX_DOWN) { X1 = it.gf; X2 = X1; kb = K; }
+    else {
+        int q, Ia, Ib;
+        mx_ext_map(row0, s, hc_c, q);
+        mx_child_ifaces(hc_c, Ia, Ib);
+        X1 = it.w + (long long)Ia * s * B;
+        X2 = it.w + (long long)(Ib - 1) * s * B;  // row k >= s of [w_Ia; w_Ib] is w_Ib[k - s]
+        kb = s;
     }
-#pragma unroll
-    for (int k = 0; k < BB; ++k) acc[k] = group_sumf<LPR>(acc[k]);
-    if (ok && sl == 0)
-        for (int k = 0; k < nb; ++k)
-            it.h[(long long)p * B + b0 + k] = acc[k] + it.hc[c][(long long)q * B + b0 + k];
-}
+    const int nkc = (K + kKC - 1) / kKC;
+    const int cpp = (nkc + ksplit - 1) / ksplit;
+    const int c0 = min(nkc, kp * cpp), c1 = min(nkc, c0 + cpp);
+    const int yrow = item * rows_item + row0;
+    const unsigned tile_bytes = unsigned(rt) * kKC * sizeof(float);
 
-// u = S gf + w, scattered to the children's g and added to the FP64 interface state
-template <int LPR, int BB>
-__global__ void __launch_bounds__(256) k_mx_gemv_down(const MixItem* __restrict__ items, int s, long long nrows,
-                                                      int nitems, int B) {
-    const int m4 = 4 * s, m8 = 8 * s;
-    if (blockIdx.y == 0) {
-        const long long tot = (long long)nitems * m8 * B;
-        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
-             e += (long long)gridDim.x * blockDim.x) {
-            const int item = int(e / ((long long)m8 * B));
-            const int rem = int(e - (long long)item * m8 * B);
-            const int p = rem / B, b = rem - (rem / B) * B;
-            const MixItem& it = items[item];
-            int c, q;
-            mx_ext_map(p, s, c, q);
-            it.gc[c][q * B + b] = it.gf[rem];
+    if (tid == 0) {
+        for (int st = 0; st < kStages; ++st) mbar_init(&full[st], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    auto issue = [&](int c, int st) {
+        if (tid == 0) tma_load_tile(&tmA, &full[st], As[st], c * kKC, yrow, tile_bytes);
+        const int k0 = c * kKC;
+        for (int e = tid; e < kKC * BN; e += nt) {
+            const int k = e / BN, col = e - (e / BN) * BN;
+            const int gk = k0 + k, gb = b0 + col;
+            const bool ok = gk < K && gb < B;
+            const float* src = ok ? ((gk < kb ? X1 : X2) + (long long)gk * B + gb) : X1;
+            cp_async4(&Xs[st][e], src, ok ? 4 : 0);
+        }
+    };
+
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+
+    int issued = 0;
+    for (int p = 0; p < kStages - 1; ++p) {
+        if (c0 + p < c1) { issue(c0 + p, p); ++issued; }
+        cp_async_commit();
+    }
+    bool failed = false;
+    for (int c = c0; c < c1; ++c) {
+        const int u = c - c0, st = u % kStages;
+        cp_async_wait<kStages - 2>();
+        const bool ok = mbar_wait(&full[st], unsigned(u / kStages) & 1u);
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        if (c + kStages - 1 < c1) { issue(c + kStages - 1, (u + kStages - 1) % kStages); ++issued; }
+        cp_async_commit();
+        const float* as = As[st];
+        const float* xs = Xs[st];
+#pragma unroll
+        for (int k4 = 0; k4 < kKC / 4; ++k4) {
+            float4 a[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = ty + i * rq;
+                a[i] = *reinterpret_cast<const float4*>(as + r * kKC + 4 * (k4 ^ (r & 7)));
+            }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                const float4 x = *reinterpret_cast<const float4*>(xs + (4 * k4 + kk) * BN + 4 * tx);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float av = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
+                    acc[i][0] = fmaf(av, x.x, acc[i][0]);
+                    acc[i][1] = fmaf(av, x.y, acc[i][1]);
+                    acc[i][2] = fmaf(av, x.z, acc[i][2]);
+                    acc[i][3] = fmaf(av, x.w, acc[i][3]);
+                }
+            }
         }
     }
-    const int sl = threadIdx.x & (LPR - 1);
-    const long long g = mx_group_row<LPR>();
-    const bool ok = g < nrows;
-    const int item = ok ? int(g / m4) : 0, r = ok ? int(g - (long long)item * m4) : 0;
-    const MixItem& it = items[item];
-    const int b0 = blockIdx.y * BB, nb = min(BB, B - b0);
-    float acc[BB];
+    cp_async_wait<0>();
+    if (failed) {
+        // let the tiles still in flight land before this CTA's shared memory goes away
+        const int u_end = issued;
+        for (int u = 0; u < u_end; ++u) (void)mbar_wait(&full[u % kStages], unsigned(u / kStages) & 1u);
+        if (tid == 0) atomicExch(err, 1);
+    }
+    __syncthreads();
+
+    if (ksplit > 1) {
+        // partial tiles -> rank 0 of the cluster through distributed shared memory
+        cg::cluster_group cluster = cg::this_cluster();
+        float* red = &As[0][0];
 #pragma unroll
-    for (int k = 0; k < BB; ++k) acc[k] = 0.f;
-    if (ok) mx_dot<LPR, BB>(it.S + (long long)r * m8, it.gf, m8, B, b0, nb, sl, acc);
+        for (int i = 0; i < 4; ++i)
+            *reinterpret_cast<float4*>(red + (ty + i * rq) * BN + 4 * tx) =
+                make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+        cluster.sync();
+        const bool lead = cluster.block_rank() == 0;
+        if (lead) {
+            for (int rk = 1; rk < ksplit; ++rk) {
+                const float* rr = cluster.map_shared_rank(red, rk);
 #pragma unroll
-    for (int k = 0; k < BB; ++k) acc[k] = group_sumf<LPR>(acc[k]);
-    if (ok && sl == 0) {
-        const int I = r / s, o = r - I * s;
-        float* gl = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B;
-        float* gu = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B;
-        for (int k = 0; k < nb; ++k) {
-            const float u = acc[k] + it.w[(long long)r * B + b0 + k];
-            gl[b0 + k] = u;
-            gu[b0 + k] = u;
-            it.uG[(long long)r * B + b0 + k] += double(u);
+                for (int i = 0; i < 4; ++i) {
+                    const float4 v = *reinterpret_cast<const float4*>(rr + (ty + i * rq) * BN + 4 * tx);
+                    acc[i][0] += v.x; acc[i][1] += v.y; acc[i][2] += v.z; acc[i][3] += v.w;
+                }
+            }
+        }
+        cluster.sync();
+        if (!lead) return;
+    }
+    if (failed) return;
+
+    // epilogue
+    if (KIND == MX_DOWN && blockIdx.y == 0) {
+        // exterior points of the parent go to the children unchanged; each tile copies its share
+        const int tot = 8 * s * B, per = (tot + tpi - 1) / tpi;
+        const int e0 = tl * per, e1 = min(tot, e0 + per);
+        for (int e = e0 + tid; e < e1; e += nt) {
+            const int p = e / B, bb = e - (e / B) * B;
+            int c, q;
+            mx_ext_map(p, s, c, q);
+            it.gc[c][(long long)q * B + bb] = it.gf[e];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = row0 + ty + i * rq;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int b = b0 + 4 * tx + j;
+            if (b >= B) continue;
+            const long long rb = (long long)r * B + b;
+            if (KIND == MX_W) {
+                it.w[rb] = acc[i][j];
+            } else if (KIND == MX_H) {
+                int c, q;
+                mx_ext_map(r, s, c, q);
+                it.h[rb] = acc[i][j] + it.hc[c][(long long)q * B + b];
+            } else {
+                const int I = r / s, o = r - (r / s) * s;
+                const float uu = acc[i][j] + it.w[rb];
+                it.gc[mx_lower_child(I)][(long long)mx_q_lower(I, o, s) * B + b] = uu;
+                it.gc[mx_upper_child(I)][(long long)mx_q_upper(I, o, s) * B + b] = uu;
+                it.uG[rb] += f2d_bits(uu);
+            }
         }
     }
 }
@@ -205,7 +358,7 @@ __global__ void k_mx_flux_up(const MixItem* __restrict__ items, int s, int B) {
             const int I = r / s, o = r - I * s;
             const double ml = it.hc64[mx_lower_child(I)][mx_q_lower(I, o, s) * B + b];
             const double mu = it.hc64[mx_upper_child(I)][mx_q_upper(I, o, s) * B + b];
-            it.mout[f] = float(ml - mu);
+            it.mout[f] = d2f_bits(ml - mu);
         }
     }
 }
@@ -242,70 +395,142 @@ __global__ void k_mx_uncoarsen(const T* const* vin, T* const* vout, int nf, int 
 }
 
 // ---- leaves --------------------------------------------------------------------------------------
-// FP32 eigenbasis leaf pass for (leaf, b): NEUMANN writes h32 = DtN(0, q); SOLVE adds the solution
-// of (g32, q) to the FP64 state u64.
+// FP32 eigenbasis leaf pass over the items (leaf, b), b fastest.  One item is an n x n patch handled
+// by (n/4)^2 threads that each own a 4 x 4 block of every product
+//   WT = (V^T F)^T,  G = Dinv o (V^T F V),  U1T = (V G)^T,  u = V G V^T
+// with float4 operand reads from shared memory (V depends on n only, so one copy serves all types).
+// NEUMANN writes h32 = DtN(0, q); SOLVE adds the solution of (g32, q) to the FP64 state u64 (or
+// stores it there when accumulate is 0).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict__ types,
-                                                   const MixLeaf* __restrict__ leaves, int L, int B,
-                                                   const float* __restrict__ q, double* __restrict__ u64) {
-    const int leaf = blockIdx.x, b = blockIdx.y;
+                                                   const MixLeaf* __restrict__ leaves, int L, int B, int n,
+                                                   int ipc, const float* __restrict__ q, double* __restrict__ u64,
+                                                   int accumulate) {
+    extern __shared__ __align__(16) float smf[];
+    const int nn = n * n, nb = n / 4, tpi = nb * nb;
+    const int istride = 2 * nn + 16;
+    float* VS = smf;
+    float* VT = smf + nn;
+    const int tid = threadIdx.x;
+    const int slot = tid / tpi, lt = tid - slot * tpi;
+    const int item = blockIdx.x * ipc + slot;
+    const bool act = slot < ipc && (long long)item < (long long)L * B;
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
     const MixLeaf lf = leaves[leaf];
     const LeafType32 ty = types[lf.type];
-    const int n = ty.n, nn = n * n;
-    extern __shared__ float smf[];
-    float* V = smf;
-    float* F = smf + nn;
-    float* W = smf + 2 * nn;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    const float cx = 1.0f / (ty.dx * ty.dx), cy = 1.0f / (ty.dy * ty.dy);
-    const float* qq = q + ((long long)b * L + leaf) * nn;
-    for (int e = tid; e < nn; e += nt) {
-        V[e] = ty.V[e];
-        const int i = e / n, j = e - (e / n) * n;
-        float v = qq[e];
-        if (MODE == LEAF_SOLVE && (i == 0 || i == n - 1 || j == 0 || j == n - 1)) {
-            float acc = 0.f;
-            if (i == 0) acc += cx * lf.g32[(0 * n + j) * B + b];
-            else if (i == n - 1) acc += cx * lf.g32[(1 * n + j) * B + b];
-            if (j == 0) acc += cy * lf.g32[(2 * n + i) * B + b];
-            else if (j == n - 1) acc += cy * lf.g32[(3 * n + i) * B + b];
-            v += -2.0f * acc;
+    {
+        const float* V0 = types[0].V;
+        for (int e = tid; e < nn; e += blockDim.x) {
+            const float v = V0[e];
+            VS[e] = v;
+            VT[(e % n) * n + e / n] = v;
         }
-        F[e] = v;
+    }
+    float* F = smf + 2 * nn + slot * istride;
+    float* W = F + nn;
+    const int bi = lt / nb, bj = lt - (lt / nb) * nb;
+    if (act) {
+        const float* qq = q + ((long long)b * L + leaf) * nn;
+        const float cx = 1.0f / (ty.dx * ty.dx), cy = 1.0f / (ty.dy * ty.dy);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = 4 * bi + i;
+            float4 v = *reinterpret_cast<const float4*>(qq + r * n + 4 * bj);
+            if (MODE == LEAF_SOLVE) {
+                float t[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = 4 * bj + j;
+                    float acc = 0.f;
+                    if (r == 0) acc += cx * lf.g32[(long long)(0 * n + c) * B + b];
+                    else if (r == n - 1) acc += cx * lf.g32[(long long)(1 * n + c) * B + b];
+                    if (c == 0) acc += cy * lf.g32[(long long)(2 * n + r) * B + b];
+                    else if (c == n - 1) acc += cy * lf.g32[(long long)(3 * n + r) * B + b];
+                    t[j] += -2.0f * acc;
+                }
+                v = make_float4(t[0], t[1], t[2], t[3]);
+            }
+            *reinterpret_cast<float4*>(F + r * n + 4 * bj) = v;
+        }
     }
     __syncthreads();
-    for (int e = tid; e < nn; e += nt) {
-        const int k = e / n, j = e - (e / n) * n;
-        float acc = 0.f;
-        for (int i = 0; i < n; ++i) acc = fmaf(V[i * n + k], F[i * n + j], acc);
-        W[e] = acc;
+    float acc[4][4];
+    auto zero = [&]() {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    };
+    // acc[a][c] += P[t][4pa + a] * Q[t][4pc + c] over t < n (both row-major n x n in shared memory)
+    auto outer = [&](const float* P, int pa, const float* Q, int pc) {
+        for (int t = 0; t < n; ++t) {
+            const float4 x = *reinterpret_cast<const float4*>(P + t * n + 4 * pa);
+            const float4 y = *reinterpret_cast<const float4*>(Q + t * n + 4 * pc);
+            const float xa[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                acc[a][0] = fmaf(xa[a], y.x, acc[a][0]);
+                acc[a][1] = fmaf(xa[a], y.y, acc[a][1]);
+                acc[a][2] = fmaf(xa[a], y.z, acc[a][2]);
+                acc[a][3] = fmaf(xa[a], y.w, acc[a][3]);
+            }
+        }
+    };
+    // (1) WT[j][k] = sum_i V[i][k] F[i][j]
+    if (act) {
+        zero();
+        outer(VS, bi, F, bj);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            *reinterpret_cast<float4*>(W + (4 * bj + j) * n + 4 * bi) =
+                make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
     }
     __syncthreads();
-    for (int e = tid; e < nn; e += nt) {
-        const int k = e / n, l = e - (e / n) * n;
-        float acc = 0.f;
-        for (int j = 0; j < n; ++j) acc = fmaf(W[k * n + j], V[j * n + l], acc);
-        F[e] = acc * ty.Dinv[e];
+    // (2) G[k][l] = Dinv[k][l] sum_j WT[j][k] V[j][l]  -> F
+    if (act) {
+        zero();
+        outer(W, bi, VS, bj);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float4 d = *reinterpret_cast<const float4*>(ty.Dinv + (4 * bi + k) * n + 4 * bj);
+            *reinterpret_cast<float4*>(F + (4 * bi + k) * n + 4 * bj) =
+                make_float4(acc[k][0] * d.x, acc[k][1] * d.y, acc[k][2] * d.z, acc[k][3] * d.w);
+        }
     }
     __syncthreads();
-    for (int e = tid; e < nn; e += nt) {
-        const int i = e / n, l = e - (e / n) * n;
-        float acc = 0.f;
-        for (int k = 0; k < n; ++k) acc = fmaf(V[i * n + k], F[k * n + l], acc);
-        W[e] = acc;
+    // (3) U1T[l][i] = sum_k VT[k][i] G[k][l]  -> W
+    if (act) {
+        zero();
+        outer(VT, bi, F, bj);
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            *reinterpret_cast<float4*>(W + (4 * bj + l) * n + 4 * bi) =
+                make_float4(acc[0][l], acc[1][l], acc[2][l], acc[3][l]);
     }
     __syncthreads();
+    if (!act) return;
     if (MODE == LEAF_SOLVE) {
+        // (4) u[i][j] = sum_l U1T[l][i] VT[l][j]
+        zero();
+        outer(W, bi, VT, bj);
         double* uu = u64 + ((long long)b * L + leaf) * nn;
-        for (int e = tid; e < nn; e += nt) {
-            const int i = e / n, j = e - (e / n) * n;
-            float acc = 0.f;
-            for (int l = 0; l < n; ++l) acc = fmaf(W[i * n + l], V[j * n + l], acc);
-            uu[e] += double(acc);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            double2* row = reinterpret_cast<double2*>(uu + (4 * bi + i) * n + 4 * bj);
+            double2 v0 = make_double2(f2d_bits(acc[i][0]), f2d_bits(acc[i][1]));
+            double2 v1 = make_double2(f2d_bits(acc[i][2]), f2d_bits(acc[i][3]));
+            if (accumulate) {
+                const double2 o0 = row[0], o1 = row[1];
+                v0.x += o0.x; v0.y += o0.y;
+                v1.x += o1.x; v1.y += o1.y;
+            }
+            row[0] = v0;
+            row[1] = v1;
         }
     } else {
         const float dtn_x = 2.0f / ty.dx, dtn_y = 2.0f / ty.dy;
-        for (int r = tid; r < 4 * n; r += nt) {
+        for (int r = lt; r < 4 * n; r += tpi) {
             const int side = r / n, pos = r - (r / n) * n;
             int i, j;
             if (side == 0) { i = 0; j = pos; }
@@ -313,63 +538,140 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
             else if (side == 2) { i = pos; j = 0; }
             else { i = pos; j = n - 1; }
             float u = 0.f;
-            for (int l = 0; l < n; ++l) u = fmaf(W[i * n + l], V[j * n + l], u);
+            for (int l = 0; l < n; ++l) u = fmaf(W[l * n + i], VT[l * n + j], u);
             const float sg = (side == 0 || side == 2) ? 1.0f : -1.0f;
-            lf.h32[r * B + b] = sg * (side < 2 ? dtn_x : dtn_y) * u;
+            lf.h32[(long long)r * B + b] = sg * (side < 2 ? dtn_x : dtn_y) * u;
         }
     }
 }
 
-// FP64 leaf residual r = f + f_b(g) - A u (stored as the next pass's FP32 load) and the leaf's edge
-// fluxes h = +-(2/d)(u_edge - g) (FP64), for the constant-coefficient operator of FISHPACK90.
-__global__ void __launch_bounds__(256) k_mx_leaf_residual(const LeafType* __restrict__ types,
-                                                          const MixLeaf* __restrict__ leaves, int L, int B,
-                                                          double lambda, const double* __restrict__ f,
+// FP64 leaf residual r = f - (cx (u_W + u_E) + cy (u_S + u_N) + cc u_C) (stored as the next pass's
+// FP32 load), where a neighbour across the patch edge is the ghost value 2g - u_C of the Dirichlet
+// face data (the discrete operator of FiniteVolumeSolver.cpp:27-223), and the leaf's edge fluxes
+// h = +-(2/d)(u_edge - g) (FP64).  GB300's FP64 pipe is narrow, so the kernel runs in two phases
+// that keep its FP64 instruction stream free of predicated-off work: every cell with the interior
+// formula (missing neighbours read as 0), then the 4n-4 boundary cells again with their ghosts.
+// Items (leaf, b) with b fastest; each thread owns 4 consecutive cells of one row.  zero_state: u is
+// identically zero (the first residual).  The largest |r| (as FP32) of every item goes to
+// rleaf[b][leaf] (reduced per request by k_mx_rmax).
+__global__ void __launch_bounds__(256) k_mx_leaf_residual(const MixCoef* __restrict__ coefs,
+                                                          const MixLeaf* __restrict__ leaves, int L, int B, int n,
+                                                          int ipc, int zero_state, const double* __restrict__ f,
                                                           const double* __restrict__ u64, float* __restrict__ q,
-                                                          double* __restrict__ rmax) {
-    const int leaf = blockIdx.x, b = blockIdx.y;
+                                                          float* __restrict__ rleaf) {
+    __shared__ unsigned smax[256];
+    const int nn = n * n, tpi = nn / 4;
+    const int tpe = tpi < 256 ? tpi : 256;
+    const int slot = threadIdx.x / tpe, lt = threadIdx.x - slot * tpe;
+    const int item0 = blockIdx.x * ipc;
+    const int item = item0 + slot;
+    const bool act = slot < ipc && (long long)item < (long long)L * B;
+    if (threadIdx.x < ipc) smax[threadIdx.x] = 0u;
+    __syncthreads();
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
     const MixLeaf lf = leaves[leaf];
-    const LeafType ty = types[lf.type];
-    const int n = ty.n, nn = n * n;
-    const double cx = 1.0 / (ty.dx * ty.dx), cy = 1.0 / (ty.dy * ty.dy);
-    const double cc = -(2.0 * cx + 2.0 * cy) + lambda;
+    const MixCoef cf = coefs[lf.type];
+    const double cx = cf.cx, cy = cf.cy, cc = cf.cc;
     const long long base = ((long long)b * L + leaf) * nn;
     const double* uu = u64 + base;
     const double* ff = f + base;
-    double mx = 0.0;
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-        const int i = e / n, j = e - (e / n) * n;
-        double d = cc, au = 0.0, fb = 0.0;
-        if (i > 0) au = fma(cx, uu[e - n], au); else { d -= cx; fb = fma(cx, lf.g64[(0 * n + j) * B + b], fb); }
-        if (i < n - 1) au = fma(cx, uu[e + n], au); else { d -= cx; fb = fma(cx, lf.g64[(1 * n + j) * B + b], fb); }
-        if (j > 0) au = fma(cy, uu[e - 1], au); else { d -= cy; fb = fma(cy, lf.g64[(2 * n + i) * B + b], fb); }
-        if (j < n - 1) au = fma(cy, uu[e + 1], au); else { d -= cy; fb = fma(cy, lf.g64[(3 * n + i) * B + b], fb); }
-        au = fma(d, uu[e], au);
-        const double r = ff[e] - 2.0 * fb - au;
-        q[base + e] = float(r);
-        mx = fmax(mx, fabs(r));
+    float mx = 0.f;
+    if (act) {
+        for (int e4 = lt; e4 < tpi; e4 += tpe) {
+            const int e = 4 * e4, i = e / n, j0 = e - (e / n) * n;
+            const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
+            const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
+            const double fv[4] = {f01.x, f01.y, f23.x, f23.y};
+            float rr[4];
+            if (zero_state) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) rr[t] = d2f_bits(fv[t]);
+            } else {
+                double c[4], up[4] = {0.0, 0.0, 0.0, 0.0}, dn[4] = {0.0, 0.0, 0.0, 0.0};
+                const double2 c01 = *reinterpret_cast<const double2*>(uu + e);
+                const double2 c23 = *reinterpret_cast<const double2*>(uu + e + 2);
+                c[0] = c01.x; c[1] = c01.y; c[2] = c23.x; c[3] = c23.y;
+                if (i > 0) {
+                    const double2 a = *reinterpret_cast<const double2*>(uu + e - n);
+                    const double2 bq = *reinterpret_cast<const double2*>(uu + e - n + 2);
+                    up[0] = a.x; up[1] = a.y; up[2] = bq.x; up[3] = bq.y;
+                }
+                if (i < n - 1) {
+                    const double2 a = *reinterpret_cast<const double2*>(uu + e + n);
+                    const double2 bq = *reinterpret_cast<const double2*>(uu + e + n + 2);
+                    dn[0] = a.x; dn[1] = a.y; dn[2] = bq.x; dn[3] = bq.y;
+                }
+                const double left = j0 > 0 ? uu[e - 1] : 0.0;
+                const double right = j0 + 4 < n ? uu[e + 4] : 0.0;
+                const double ym[4] = {left, c[0], c[1], c[2]};
+                const double yp[4] = {c[1], c[2], c[3], right};
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    rr[t] = d2f_bits(fv[t] - fma(cc, c[t], fma(cy, ym[t] + yp[t], cx * (up[t] + dn[t]))));
+            }
+            const bool edge_row = i == 0 || i == n - 1;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int j = j0 + t;
+                const bool interior = !edge_row && j > 0 && j < n - 1;
+                mx = fmaxf(mx, interior ? fabsf(rr[t]) : 0.f);
+            }
+            *reinterpret_cast<float4*>(q + base + e) = make_float4(rr[0], rr[1], rr[2], rr[3]);
+        }
     }
-    if (rmax) {
-        for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-        if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(rmax + b),
-                                               __double_as_longlong(mx));
+    __syncthreads();  // the boundary phase rewrites cells stored by other threads of the block
+    if (act) {
+        const double* gW = lf.g64 + b;
+        const double* gE = lf.g64 + (long long)n * B + b;
+        const double* gS = lf.g64 + 2LL * n * B + b;
+        const double* gN = lf.g64 + 3LL * n * B + b;
+        for (int k = lt; k < 4 * n - 4; k += tpe) {
+            int i, j;
+            if (k < n) { i = 0; j = k; }
+            else if (k < 2 * n) { i = n - 1; j = k - n; }
+            else { const int m = k - 2 * n; i = 1 + (m >> 1); j = (m & 1) ? n - 1 : 0; }
+            const int e = i * n + j;
+            const double uc = zero_state ? 0.0 : uu[e];
+            const double xm = i > 0 ? (zero_state ? 0.0 : uu[e - n]) : fma(2.0, gW[(long long)j * B], -uc);
+            const double xp = i < n - 1 ? (zero_state ? 0.0 : uu[e + n]) : fma(2.0, gE[(long long)j * B], -uc);
+            const double ym = j > 0 ? (zero_state ? 0.0 : uu[e - 1]) : fma(2.0, gS[(long long)i * B], -uc);
+            const double yp = j < n - 1 ? (zero_state ? 0.0 : uu[e + 1]) : fma(2.0, gN[(long long)i * B], -uc);
+            const float r = d2f_bits(ff[e] - fma(cc, uc, fma(cy, ym + yp, cx * (xm + xp))));
+            q[base + e] = r;
+            mx = fmaxf(mx, fabsf(r));
+        }
+        atomicMax(&smax[slot], __float_as_uint(mx));
+        for (int r = lt; r < 4 * n; r += tpe) {
+            const int side = r / n, pos = r - (r / n) * n;
+            int cell;
+            if (side == 0) cell = pos;
+            else if (side == 1) cell = (n - 1) * n + pos;
+            else if (side == 2) cell = pos * n;
+            else cell = pos * n + n - 1;
+            const double gv = lf.g64[(long long)r * B + b];
+            const double ue = zero_state ? 0.0 : uu[cell];
+            const double dtn = side < 2 ? cf.dtn_x : cf.dtn_y;
+            lf.h64[(long long)r * B + b] = (side == 0 || side == 2) ? dtn * (ue - gv) : (-dtn) * (ue - gv);
+        }
     }
-    const double dtn_x = 2.0 / ty.dx, dtn_y = 2.0 / ty.dy;
-    for (int r = threadIdx.x; r < 4 * n; r += blockDim.x) {
-        const int side = r / n, pos = r - (r / n) * n;
-        int cell;
-        if (side == 0) cell = pos;
-        else if (side == 1) cell = (n - 1) * n + pos;
-        else if (side == 2) cell = pos * n;
-        else cell = pos * n + n - 1;
-        const double gv = lf.g64[r * B + b];
-        double h;
-        if (side == 0) h = dtn_x * (uu[cell] - gv);
-        else if (side == 1) h = (-dtn_x) * (uu[cell] - gv);
-        else if (side == 2) h = dtn_y * (uu[cell] - gv);
-        else h = (-dtn_y) * (uu[cell] - gv);
-        lf.h64[r * B + b] = h;
+    __syncthreads();
+    if (rleaf && act && lt == 0) rleaf[(long long)b * L + leaf] = __uint_as_float(smax[slot]);
+}
+
+// rmax[b] = max over leaves of rleaf[b][leaf]
+__global__ void __launch_bounds__(256) k_mx_rmax(const float* __restrict__ rleaf, int L, double* __restrict__ rmax) {
+    __shared__ float red[256];
+    const float* p = rleaf + (long long)blockIdx.x * L;
+    float m = 0.f;
+    for (int l = threadIdx.x; l < L; l += blockDim.x) m = fmaxf(m, p[l]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
     }
+    if (threadIdx.x == 0) rmax[blockIdx.x] = double(red[0]);
 }
 
 // FP32 copies of S (RHS columns [0,8s)), X^{-1} (RHS columns [8s,12s)) and the compact H
@@ -400,59 +702,57 @@ __global__ void k_mx_root(int m, int B, const double* a, const double* r, double
     }
 }
 
-inline int mx_pick_lpr(int len) {
-    if (len >= 256) return 32;
-    if (len >= 64) return 16;
-    if (len >= 16) return 8;
-    return 4;
-}
-
 inline unsigned mx_grid(long long tot) {
     long long b = (tot + 255) / 256;
     if (b > 8192) b = 8192;
     return unsigned(b < 1 ? 1 : b);
 }
 
-constexpr int kBB = 8;  // requests accumulated per pass over a matrix row
-
-#define EF_MX_DISPATCH(KERNEL, LPR, GRID, ...)                                        \
-    do {                                                                              \
-        if (LPR == 32) KERNEL<32, kBB><<<GRID, 256, 0, st>>>(__VA_ARGS__);            \
-        else if (LPR == 16) KERNEL<16, kBB><<<GRID, 256, 0, st>>>(__VA_ARGS__);       \
-        else if (LPR == 8) KERNEL<8, kBB><<<GRID, 256, 0, st>>>(__VA_ARGS__);         \
-        else KERNEL<4, kBB><<<GRID, 256, 0, st>>>(__VA_ARGS__);                       \
-    } while (0)
+template <int KIND>
+void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B, int* err) {
+    int rows_item, K;
+    mx_shape<KIND>(s, rows_item, K);
+    const int rt = mx_tile_rows(KIND == MX_H ? 1 : 0, s);
+    const int tiles = nitems * (rows_item / rt);
+    const int BN = B <= 8 ? 8 : (B <= 16 ? 16 : 32);
+    const int chunks = (B + BN - 1) / BN;
+    const int nkc = (K + kKC - 1) / kKC;
+    int ksplit = 1;
+    // Split K only while fewer than ~4 CTAs per SM are in flight, and keep at least 8 chunks per
+    // CTA (the TMA pipeline and the cluster reduction cost a few microseconds per CTA).  Chosen from
+    // the tile count alone so that every request's sums are grouped the same way whatever the batch.
+    while (ksplit < 8 && (long long)tiles * ksplit < 608 && nkc >= 16 * ksplit) ksplit *= 2;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(tiles * ksplit), unsigned(chunks));
+    cfg.blockDim = dim3(unsigned((rt / 4) * (BN / 4)));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(ksplit);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = ksplit > 1 ? 1 : 0;
+    if (BN == 8) cudaLaunchKernelEx(&cfg, k_mx_gemm<8, KIND>, tm, items, s, B, rt, ksplit, err);
+    else if (BN == 16) cudaLaunchKernelEx(&cfg, k_mx_gemm<16, KIND>, tm, items, s, B, rt, ksplit, err);
+    else cudaLaunchKernelEx(&cfg, k_mx_gemm<32, KIND>, tm, items, s, B, rt, ksplit, err);
+    ++g_kernel_launches;
+}
 
 }  // namespace
 
-void mx_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
+void mx_hdiff(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
     dim3 g1(mx_grid(4LL * s * B), nitems);
     k_mx_hdiff<<<g1, 256, 0, st>>>(items, s, B);
-    const int chunks = (B + kBB - 1) / kBB;
-    {
-        const long long rows = (long long)nitems * 4 * s;
-        const int lpr = mx_pick_lpr(4 * s);
-        dim3 g((unsigned)((rows * lpr + 255) / 256), chunks);
-        EF_MX_DISPATCH(k_mx_gemv_w, lpr, g, items, s, rows, B);
-    }
-    {
-        const long long rows = (long long)nitems * 8 * s;
-        const int lpr = mx_pick_lpr(s);
-        dim3 g((unsigned)((rows * lpr + 255) / 256), chunks);
-        EF_MX_DISPATCH(k_mx_gemv_h, lpr, g, items, s, rows, B);
-    }
-    g_kernel_launches += 3;
+    ++g_kernel_launches;
 }
 
-void mx_down(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
-    const int chunks = (B + kBB - 1) / kBB;
-    const long long rows = (long long)nitems * 4 * s;
-    const int lpr = mx_pick_lpr(8 * s);
-    long long blocks = (rows * lpr + 255) / 256;
-    if (blocks < 1) blocks = 1;
-    dim3 g((unsigned)blocks, chunks);
-    EF_MX_DISPATCH(k_mx_gemv_down, lpr, g, items, s, rows, nitems, B);
-    ++g_kernel_launches;
+void mx_gemm(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
+             int* err) {
+    if (kind == 0) mx_gemm<MX_W>(st, tm, items, nitems, s, B, err);
+    else if (kind == 1) mx_gemm<MX_H>(st, tm, items, nitems, s, B, err);
+    else mx_gemm<MX_DOWN>(st, tm, items, nitems, s, B, err);
 }
 
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
@@ -488,25 +788,35 @@ void mx_convert(cudaStream_t st, const MixConv* items, int nitems, int s) {
 }
 
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
-               const float* q, double* u64) {
-    const size_t smem = size_t(3) * n * n * sizeof(float);
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_mx_leaf32<LEAF_NEUMANN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_mx_leaf32<LEAF_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        configured = true;
+               const float* q, double* u64, int accumulate) {
+    const int nb = n / 4, tpi = nb * nb, ipc = tpi >= 256 ? 1 : 256 / tpi;
+    const size_t smem = (size_t(2) * n * n + size_t(ipc) * (2 * n * n + 16)) * sizeof(float);
+    static size_t configured = 48 * 1024;
+    if (smem > configured) {
+        cudaFuncSetAttribute(k_mx_leaf32<LEAF_NEUMANN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaFuncSetAttribute(k_mx_leaf32<LEAF_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        configured = smem;
     }
-    dim3 g(L, B);
-    if (mode == LEAF_NEUMANN) k_mx_leaf32<LEAF_NEUMANN><<<g, 256, smem, st>>>(types, leaves, L, B, q, u64);
-    else k_mx_leaf32<LEAF_SOLVE><<<g, 256, smem, st>>>(types, leaves, L, B, q, u64);
+    const long long items = (long long)L * B;
+    const unsigned grid = unsigned((items + ipc - 1) / ipc);
+    const unsigned threads = unsigned(ipc * tpi);
+    if (mode == LEAF_NEUMANN) k_mx_leaf32<LEAF_NEUMANN><<<grid, threads, smem, st>>>(types, leaves, L, B, n, ipc, q, u64, 0);
+    else k_mx_leaf32<LEAF_SOLVE><<<grid, threads, smem, st>>>(types, leaves, L, B, n, ipc, q, u64, accumulate);
     ++g_kernel_launches;
 }
 
-void mx_leaf_residual(cudaStream_t st, const LeafType* types, const MixLeaf* leaves, int L, int B, double lambda,
-                      const double* f, const double* u64, float* q, double* rmax) {
-    dim3 g(L, B);
-    k_mx_leaf_residual<<<g, 256, 0, st>>>(types, leaves, L, B, lambda, f, u64, q, rmax);
+void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leaves, int L, int B, int n,
+                      int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax) {
+    const int tpi = n * n / 4, tpe = tpi < 256 ? tpi : 256, ipc = 256 / tpe;
+    const long long items = (long long)L * B;
+    const unsigned grid = unsigned((items + ipc - 1) / ipc);
+    k_mx_leaf_residual<<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q,
+                                                             rmax ? rleaf : nullptr);
     ++g_kernel_launches;
+    if (rmax) {
+        k_mx_rmax<<<B, 256, 0, st>>>(rleaf, L, rmax);
+        ++g_kernel_launches;
+    }
 }
 
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g) {

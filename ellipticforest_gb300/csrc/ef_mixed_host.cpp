@@ -4,6 +4,8 @@
 #include <stdexcept>
 #include <string>
 
+#include <cudaTypedefs.h>
+
 #include "ef_hps.hpp"
 
 namespace efgb {
@@ -25,6 +27,34 @@ void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        ck(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
+           "driver entry point cuTensorMapEncodeTiled");
+        if (q != cudaDriverEntryPointSuccess || !p) throw std::runtime_error("cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// row-major FP32 matrix [rows][cols] read in boxes of 32 columns x box_rows rows, 128-byte swizzle
+CUtensorMap make_map(float* base, long long rows, int cols, int box_rows) {
+    CUtensorMap tm;
+    const cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+    const cuuint64_t strides[1] = {cuuint64_t(cols) * sizeof(float)};
+    const cuuint32_t box[2] = {32u, cuuint32_t(box_rows)};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = encode_tiled()(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+    return tm;
+}
+
 }  // namespace
 
 MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
@@ -33,6 +63,10 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
         throw std::invalid_argument("mixed solver: FISHPACK90 (constant coefficient) leaves only");
     if (bmax < 1 || bmax > 1024) throw std::invalid_argument("mixed solver: bmax must be in [1, 1024]");
     const int N = hps.num_nodes(), L = hps.num_leaves(), n = hps.leaf_n();
+    if ((long long)L * bmax >= (1LL << 31) || 12LL * hps.node(0).nx * bmax >= (1LL << 31))
+        throw std::invalid_argument("mixed solver: leaves x bmax too large for 32-bit item indices");
+    if (n % 4 != 0 || n > 64)
+        throw std::invalid_argument("mixed solver: the leaf size must be a multiple of 4 and at most 64");
     const size_t nn = size_t(n) * n, B = size_t(bmax);
     const int M = hps.root_M();
     const Mesh& mesh = hps.mesh();
@@ -55,9 +89,6 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
                 m.h64 = cv.get<double>(4 * size_t(n) * B);
             } else {
                 const size_t s = nd.s;
-                m.S = cv.get<float>(32 * s * s);
-                m.Xi = cv.get<float>(16 * s * s);
-                m.H32 = cv.get<float>(16 * s * s);
                 m.h32 = cv.get<float>(8 * s * B);
                 m.hd32 = cv.get<float>(4 * s * B);
                 m.w32 = cv.get<float>(4 * s * B);
@@ -86,6 +117,9 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
         a_ = cv.get<double>(B * 4 * M);
         r_ = cv.get<double>(B * 4 * M);
         rmax_ = cv.get<double>(B * kMaxPasses);
+        d_err_ = cv.get<int>(1);
+        rleaf_ = cv.get<float>(B * L);
+        d_coef_ = cv.get<MixCoef>(hps.types_.size());
         d_types32_ = cv.get<LeafType32>(hps.types_.size());
         d_leaves_ = cv.get<MixLeaf>(L);
         groups_.assign(hps.groups_.size(), MGroup());
@@ -96,6 +130,20 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
             groups_[gi].cnt = int(g.nodes.size());
             groups_[gi].d_items = cv.get<MixItem>(g.nodes.size());
             groups_[gi].d_conv = cv.get<MixConv>(g.nodes.size());
+            // FP32 operators of the group back to back: one row-major matrix per kind
+            const size_t s = g.s, cnt = g.nodes.size();
+            float* S = cv.get<float>(cnt * 32 * s * s);
+            float* Xi = cv.get<float>(cnt * 16 * s * s);
+            float* H32 = cv.get<float>(cnt * 16 * s * s);
+            groups_[gi].S32 = S;
+            groups_[gi].Xi32 = Xi;
+            groups_[gi].H32 = H32;
+            for (size_t i = 0; i < cnt; ++i) {
+                MNode& m = mn_[g.nodes[i]];
+                m.S = S ? S + i * 32 * s * s : nullptr;
+                m.Xi = Xi ? Xi + i * 16 * s * s : nullptr;
+                m.H32 = H32 ? H32 + i * 16 * s * s : nullptr;
+            }
         }
         hsteps_.assign(hps.step_nodes_t_.size(), MStep());
         for (size_t k = 0; k < hsteps_.size(); ++k) {
@@ -147,6 +195,13 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
                                 tab + 2 * nn * t + nn};
         }
         ck(cudaMemcpy(d_types32_, t32.data(), t32.size() * sizeof(LeafType32), cudaMemcpyHostToDevice), "types32");
+        std::vector<MixCoef> co(hps.types_.size());
+        for (size_t t = 0; t < co.size(); ++t) {
+            const double dx = hps.types_[t].dx, dy = hps.types_[t].dy;
+            const double cx = 1.0 / (dx * dx), cy = 1.0 / (dy * dy);
+            co[t] = MixCoef{cx, cy, -(2.0 * cx + 2.0 * cy) + hps.lambda_, 2.0 / dx, 2.0 / dy};
+        }
+        ck(cudaMemcpy(d_coef_, co.data(), co.size() * sizeof(MixCoef), cudaMemcpyHostToDevice), "mixed coefs");
     }
     std::vector<MixLeaf> leaves(L);
     for (int k = 0; k < L; ++k) {
@@ -205,8 +260,16 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
     };
     fill_steps(hsteps_, hps.step_nodes_t_, hps.step_index_t_, true);
     fill_steps(gsteps_, hps.step_nodes_g_, hps.step_index_g_, false);
-    // FP32 operator copies
-    for (auto& g : groups_) mx_convert(st, g.d_conv, g.cnt, g.s);
+    // FP32 operator copies and the TMA descriptors that stream them
+    for (auto& g : groups_) {
+        mx_convert(st, g.d_conv, g.cnt, g.s);
+        const long long cnt = g.cnt, s = g.s;
+        if (mx_tile_rows(0, g.s) == 0 || mx_tile_rows(1, g.s) == 0)
+            throw std::invalid_argument("mixed solver: interface size not a multiple of 4");
+        g.tmS = make_map(g.S32, cnt * 4 * s, int(8 * s), mx_tile_rows(0, g.s));
+        g.tmXi = make_map(g.Xi32, cnt * 4 * s, int(4 * s), mx_tile_rows(0, g.s));
+        g.tmH = make_map(g.H32, cnt * 8 * s, int(2 * s), mx_tile_rows(1, g.s));
+    }
     ck(cudaGetLastError(), "mixed convert");
     ck(cudaStreamSynchronize(st), "mixed setup");
 }
@@ -216,47 +279,79 @@ MixedSolver::~MixedSolver() {
     if (tables_) cudaFree(tables_);
 }
 
-void MixedSolver::residual(int B, double* rmax) {
+void MixedSolver::residual(int B, double* rmax, bool zero_state) {
     Hps& h = H_;
     cudaStream_t st = h.stream();
     const int maxL = h.mesh().max_level;
+    const double L = h.num_leaves(), nn = double(h.leaf_n()) * h.leaf_n();
     // exact Dirichlet data of every node from the root data and the interface state
+    h.pb("mx_interface");
     for (int lvl = 0; lvl < maxL; ++lvl) {
         for (auto& s : gsteps_)
             if (s.level == lvl) mx_uncoarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
         for (auto& g : groups_)
             if (g.level == lvl) mx_scatter64(st, g.d_items, g.cnt, g.s, B);
     }
-    mx_leaf_residual(st, h.d_types_, d_leaves_, h.num_leaves(), B, h.lambda_, f_, u64_, q32_, rmax);
+    h.pe(0, 0);
+    h.pb("mx_leaf_residual");
+    mx_leaf_residual(st, d_coef_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
+                     rleaf_, rmax);
+    h.pe(L * B * nn * 20.0, L * B * nn * 12.0);
+    h.pb("mx_interface");
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         for (auto& s : hsteps_)
             if (s.level == lvl + 1) mx_coarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
         for (auto& g : groups_)
             if (g.level == lvl) mx_flux_up(st, g.d_items, g.cnt, g.s, B);
     }
+    h.pe(0, 0);
 }
 
-void MixedSolver::pass(int B) {
+void MixedSolver::pass(int B, bool first) {
     Hps& h = H_;
     cudaStream_t st = h.stream();
     const int maxL = h.mesh().max_level;
     const int L = h.num_leaves(), n = h.leaf_n();
-    mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr);
+    const double items = double(L) * B, nn = double(n) * n;
+    h.pb("mx_leaf_neumann");
+    mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr, 0);
+    h.pe(items * (nn * 4 + 4 * n * 4), items * 2.0 * (3 * nn * n + 4 * nn));
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
+        h.pb("mx_interface");
         for (auto& s : hsteps_)
             if (s.level == lvl + 1) mx_coarsen(st, false, s.in32, s.out32, s.count, s.nf, B);
         for (auto& g : groups_)
-            if (g.level == lvl) mx_up(st, g.d_items, g.cnt, g.s, B);
+            if (g.level == lvl) mx_hdiff(st, g.d_items, g.cnt, g.s, B);
+        h.pe(0, 0);
+        for (auto& g : groups_) {
+            if (g.level != lvl) continue;
+            const double c = g.cnt, s2 = double(g.s) * g.s;
+            h.pb("mx_gemm_w");
+            mx_gemm(st, 0, g.tmXi, g.d_items, g.cnt, g.s, B, d_err_);
+            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B);
+            h.pb("mx_gemm_h");
+            mx_gemm(st, 1, g.tmH, g.d_items, g.cnt, g.s, B, d_err_);
+            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B);
+        }
     }
     // homogeneous root data for the correction
     ck(cudaMemsetAsync(mn_[0].g32, 0, sizeof(float) * 4 * size_t(h.root_M()) * B, st), "root g32");
     for (int lvl = 0; lvl < maxL; ++lvl) {
+        h.pb("mx_interface");
         for (auto& s : gsteps_)
             if (s.level == lvl) mx_uncoarsen(st, false, s.in32, s.out32, s.count, s.nf, B);
-        for (auto& g : groups_)
-            if (g.level == lvl) mx_down(st, g.d_items, g.cnt, g.s, B);
+        h.pe(0, 0);
+        for (auto& g : groups_) {
+            if (g.level != lvl) continue;
+            const double c = g.cnt, s2 = double(g.s) * g.s;
+            h.pb("mx_gemm_down");
+            mx_gemm(st, 2, g.tmS, g.d_items, g.cnt, g.s, B, d_err_);
+            h.pe(c * 32 * s2 * 4, c * 2.0 * 32 * s2 * B);
+        }
     }
-    mx_leaf32(st, LEAF_SOLVE, d_types32_, d_leaves_, L, B, n, q32_, u64_);
+    h.pb("mx_leaf_solve");
+    mx_leaf32(st, LEAF_SOLVE, d_types32_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
+    h.pe(items * nn * (4 + 16), items * 2.0 * 4 * nn * n);
 }
 
 void MixedSolver::solve(int B, int sweeps) {
@@ -265,14 +360,21 @@ void MixedSolver::solve(int B, int sweeps) {
     Hps& h = H_;
     cudaStream_t st = h.stream();
     const size_t cells = size_t(h.num_leaves()) * h.leaf_n() * h.leaf_n();
-    ck(cudaMemsetAsync(u64_, 0, sizeof(double) * cells * B, st), "clear u");
     ck(cudaMemsetAsync(uG_begin_, 0, uG_bytes_, st), "clear interface state");
     ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, st), "clear residuals");
     mx_root(st, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
     for (int p = 0; p <= sweeps; ++p) {
-        residual(B, rmax_ + size_t(p) * bmax_);
-        pass(B);
+        residual(B, rmax_ + size_t(p) * bmax_, p == 0);
+        pass(B, p == 0);
     }
+}
+
+int MixedSolver::take_error() {
+    int v = 0;
+    ck(cudaStreamSynchronize(H_.stream()), "mixed solver");
+    ck(cudaMemcpy(&v, d_err_, sizeof(int), cudaMemcpyDeviceToHost), "mixed error flag");
+    if (v) ck(cudaMemset(d_err_, 0, sizeof(int)), "mixed error flag");
+    return v;
 }
 
 }  // namespace efgb
