@@ -2,14 +2,19 @@
 """Benchmark of the GB300 HPS solver: prints ONE JSON line.
 
 Workload (default): uniform quadtree of level 7 with 16x16-cell patches (2048^2 = 4.19 M dofs),
-Poisson on [-1,1]^2; each step is one request -- a seeded load f (sum of 8 Gaussian bumps) and
-Dirichlet data (6 Fourier modes per side) -- solved on the factored tree: upwards stage (leaf
-particular Neumann data + merges of h), root Dirichlet data, downwards stage (u_Gamma = S g + w)
-and leaf solves.  The build stage (leaf DtN + all merges) is timed once and reported as build_s.
+Poisson on [-1,1]^2, requests = seeded loads f (sum of 8 Gaussian bumps) and Dirichlet data (6
+Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed once (build_s).
 
-  value  -- solves/s with the inputs resident in HBM (device-to-device staging of each request)
-  e2e    -- solves/s through the reference-facing C ABI with pinned host buffers: upwards(f_host),
-            solve(a, b, r host), get_leaf_u(u_host) per step
+  value  -- solves/s of the batched mixed-precision form: each step is one block of --batch
+            requests solved on the factored tree by FP32 HPS passes (batched node GEMMs, FP32 leaf
+            eigen-solves) with --sweeps FP64 refinement sweeps (FP64 leaf residual + interface flux
+            mismatch), to <= 1e-10 relative of the FP64 HPS solution (rel_err_vs_fp64, measured);
+            inputs resident in HBM
+  e2e    -- the same form through the C ABI call ef_hps_mixed_solve on pinned host buffers, the
+            host<->device copies of every block inside the timed region
+  plain_fp64 -- the plain FP64 form one request at a time (device-resident solves/s, p50/p99, and
+            e2e through the reference-facing upwards/solve/get_leaf_u calls)
+  many_rhs_L6 -- 512 right-hand sides on a uniform level-6 tree: one mixed block vs 512 plain solves
   --impl reference -- the FP64 CPU oracle (a restatement of the reference's HPS path, same LAPACK
             calls) on the same workload, rank 0 only, on the host cores.
 """
@@ -53,10 +58,14 @@ def make_request(seed, X, Y, bpts):
     return f, np.ones_like(r), np.zeros_like(r), r
 
 
-def workload_desc(level, n):
+def workload_desc(level, n, batch=1, sweeps=0):
     N = n * 2 ** level
-    return (f"uniform quadtree level {level}, {n}x{n} cells per patch ({N}^2 = {N * N / 1e6:.2f} M dofs), "
-            f"Poisson on [-1,1]^2, one right-hand side per step (Gaussian-bump load, Fourier Dirichlet data)")
+    w = (f"uniform quadtree level {level}, {n}x{n} cells per patch ({N}^2 = {N * N / 1e6:.2f} M dofs), "
+         f"Poisson on [-1,1]^2")
+    if batch > 1 or sweeps:
+        return w + (f"; each step one block of {batch} requests (Gaussian-bump loads, Fourier Dirichlet data) "
+                    f"solved by FP32 HPS passes with {sweeps} FP64 refinement sweep(s) to <=1e-10 of the FP64 HPS")
+    return w + ", one right-hand side per step (Gaussian-bump load, Fourier Dirichlet data)"
 
 
 # ------------------------------------------------------------------------------------------------
@@ -257,11 +266,16 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def _events(torch, k):
+    return [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
     import ellipticforest_gb300 as ef
     from ellipticforest_gb300 import build as efbuild
+    from ellipticforest_gb300._lib import check, dptr, load
     from ellipticforest_gb300.hps import kernel_launches
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -271,16 +285,17 @@ def run_gb300(args):
     if world > 1:
         dist.init_process_group("nccl")
     efbuild.build()
+    lib = load()
     stream = torch.cuda.current_stream()
 
-    level, n = args.level, args.n
+    level, n, B, sweeps = args.level, args.n, args.batch, args.sweeps
     root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, DOM[0], DOM[1], n, DOM[2], DOM[3]))
     mesh = ef.Mesh().uniform(level, root)
     hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
     hps.set_stream(stream.cuda_stream)
     hps.setupStage()
 
-    # build stage (timed once, sections profiled with CUDA events)
+    # ---- build stage (timed once, sections profiled with CUDA events) ----
     hps.profile_enable(True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -292,27 +307,70 @@ def run_gb300(args):
     hps.profile_enable(False)
     build_flops = sum(v["flops"] for v in build_prof.values())
 
-    # requests
     X, Y = mesh.cell_centres()
     bpts = hps.boundary_points()
-    P = 4
-    reqs = [make_request(1000 + i + 97 * rank, X, Y, bpts) for i in range(P)]
-    dev = [tuple(torch.from_numpy(x).cuda() for x in rq) for rq in reqs]
-    host = []
-    for rq in reqs:
-        hs = tuple(torch.from_numpy(x).pin_memory() for x in rq)
-        host.append(tuple(h.numpy() for h in hs))
-    u_host = torch.empty(X.size, dtype=torch.float64).pin_memory().numpy()
     dofs = X.size
+    P = 4
+    reqs = [make_request(1000 + i + 97 * rank, X, Y, bpts) for i in range(P)]  # (f, a, b, r)
 
-    def device_step(i):
+    # ---- plain FP64 form, one request at a time, inputs resident in HBM ----
+    dev = [tuple(torch.from_numpy(x).cuda() for x in rq) for rq in reqs]
+
+    def plain_step(i):
         f, a, b, r = dev[i % P]
         hps.load_device_async(f.data_ptr(), a.data_ptr(), b.data_ptr(), r.data_ptr())
         hps.solve_device_async(True)
 
-    # warm-up
     for i in range(args.warmup):
-        device_step(i)
+        plain_step(i)
+    torch.cuda.synchronize()
+    Kp = args.plain_steps
+    ev = _events(torch, Kp + 1)
+    ev[0].record(stream)
+    for i in range(Kp):
+        plain_step(i)
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    plain_lat = [ev[i].elapsed_time(ev[i + 1]) for i in range(Kp)]
+    plain_value = Kp / (ev[0].elapsed_time(ev[-1]) / 1e3)
+    # FP64 reference solutions of the P distinct requests (also the plain form's e2e, through the
+    # reference-facing upwards/solve/get_leaf_u calls with pinned host buffers)
+    host = []
+    for rq in reqs:
+        hs = tuple(torch.from_numpy(x).pin_memory() for x in rq)
+        host.append(tuple(h.numpy() for h in hs))
+    u_host = torch.empty(dofs, dtype=torch.float64).pin_memory().numpy()
+    ref_u = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(P):
+        f, a, b, r = host[i]
+        hps.upwards_array(f)
+        hps.solve_arrays(a, b, r)
+        check(lib.ef_hps_get_leaf_u(hps.handle, dptr(u_host)))
+        ref_u.append(u_host.copy())
+    plain_e2e = P / (time.perf_counter() - t0)
+    # plain-form roofline: its dominant section over the plain steps
+    hps.profile_enable(True)
+    hps.profile_reset()
+    for i in range(Kp):
+        plain_step(i)
+    plain_prof = hps.profile()
+    hps.profile_reset()
+    hps.profile_enable(False)
+    p_tot = sum(v["ms"] for v in plain_prof.values())
+    p_dom = max(plain_prof, key=lambda k: plain_prof[k]["ms"])
+    p_ach = plain_prof[p_dom]["bytes"] / (plain_prof[p_dom]["ms"] / 1e3) / 1e9
+
+    # ---- batched mixed-precision form: the headline ----
+    hps.mixed_init(B)
+    F = np.stack([reqs[i % P][0] for i in range(B)])
+    A = np.stack([reqs[i % P][1] for i in range(B)])
+    R = np.stack([reqs[i % P][3] for i in range(B)])
+    u_mixed = hps.mixed_solve(F, A, R, sweeps)  # also leaves the block's inputs resident in HBM
+    rel_err = max(float(np.abs(u_mixed[i] - ref_u[i]).max() / np.abs(ref_u[i]).max()) for i in range(P))
+    for _ in range(args.warmup):
+        hps.mixed_solve_async(B, sweeps)
     torch.cuda.synchronize()
 
     gpu_uuid = None
@@ -326,67 +384,69 @@ def run_gb300(args):
     clocks.start()
     time.sleep(0.3)
 
-    # timed region: exactly K device-resident steps
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    # timed region: exactly K device-resident steps, each one block of B requests
+    K = args.steps
+    ev = _events(torch, K + 1)
     l0 = kernel_launches()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     ev[0].record(stream)
-    for i in range(args.steps):
-        device_step(i)
+    for i in range(K):
+        hps.mixed_solve_async(B, sweeps)
         ev[i + 1].record(stream)
     torch.cuda.synchronize()
     launches = kernel_launches() - l0
-    lat = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    lat = [ev[i].elapsed_time(ev[i + 1]) for i in range(K)]
     elapsed = ev[0].elapsed_time(ev[-1]) / 1e3
     if world > 1:
         t = torch.tensor([elapsed], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
         dist.barrier()
-    value = world * args.steps / elapsed
+    value = world * K * B / elapsed
 
-    # e2e through the reference-facing C ABI with pinned host buffers
+    # e2e: the C ABI call a user makes (ef_hps_mixed_solve) on pinned host buffers, with the
+    # host<->device copies of every block inside the timed region
+    Fh = torch.from_numpy(F).pin_memory()
+    Ah = torch.from_numpy(A).pin_memory()
+    Rh = torch.from_numpy(R).pin_memory()
+    Uh = torch.empty_like(Fh).pin_memory()
+    Fn, An, Rn, Un = Fh.numpy(), Ah.numpy(), Rh.numpy(), Uh.numpy()
+    Ke = max(2, K // 4)
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    from ellipticforest_gb300._lib import check, dptr, load
-    lib = load()
     t0 = time.perf_counter()
-    e0.record(stream)
-    for i in range(args.steps):
-        f, a, b, r = host[i % P]
-        hps.upwards_array(f)
-        hps.solve_arrays(a, b, r)
-        check(lib.ef_hps_get_leaf_u(hps.handle, dptr(u_host)))
-    e1.record(stream)
-    torch.cuda.synchronize()
+    for i in range(Ke):
+        check(lib.ef_hps_mixed_solve(hps.handle, B, sweeps, dptr(Fn), dptr(An), dptr(Rn), dptr(Un)))
     e2e_wall = time.perf_counter() - t0
-    e2e_value = world * args.steps / max(e2e_wall, e0.elapsed_time(e1) / 1e3)
+    e2e_value = world * Ke * B / e2e_wall
     clk = clocks.stop()
+    assert np.array_equal(Uh.numpy()[0], u_mixed[0])
 
-    # per-section kernel timing (CUDA events on the library's stream) over K profiled steps
+    # per-section kernel timing of the mixed form (CUDA events on the library's stream)
     hps.profile_enable(True)
     hps.profile_reset()
-    for i in range(args.steps):
-        device_step(i)
+    for i in range(max(2, K // 4)):
+        hps.mixed_solve_async(B, sweeps)
     prof = hps.profile()
     hps.profile_enable(False)
-    solve_secs = {k: v for k, v in prof.items()}
-    tot_ms = sum(v["ms"] for v in solve_secs.values())
-    dom_name = max(solve_secs, key=lambda k: solve_secs[k]["ms"])
-    d = solve_secs[dom_name]
+    ksteps = max(2, K // 4)
+    tot_ms = sum(v["ms"] for v in prof.values())
+    dom_name = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom_name]
     hbm_peak, peak_kind = load_peaks()
     achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
     fp64_peak = measure_fp64_peak(torch)
-    fp64_solve = sum(v["flops"] for v in solve_secs.values()) / (tot_ms / 1e3) / 1e12
 
-    # correctness spot check on the manufactured solution u = sin x + sin y
+    # correctness spot check of the plain form on the manufactured solution u = sin x + sin y
     hps.upwards_array(-(np.sin(X) + np.sin(Y)))
     bx = np.concatenate([np.sin(x) + np.sin(y) for x, y in bpts])
     hps.solve_arrays(np.ones_like(bx), np.zeros_like(bx), bx)
     err = float(np.abs(hps.leaf_solution() - (np.sin(X) + np.sin(Y))).max())
+
+    extras = {}
+    if not args.no_extras:
+        extras["many_rhs_L6"] = many_rhs(ef, torch, stream, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -398,17 +458,33 @@ def run_gb300(args):
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "steps": K, "warmup": args.warmup, "ms_per_step": elapsed / K * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded Gaussian-bump loads, Fourier Dirichlet data)",
-            "config": {"workload": workload_desc(level, n), "leaves": 4 ** level, "dofs": dofs,
+            "config": {"workload": workload_desc(level, n, B, sweeps), "leaves": 4 ** level, "dofs": dofs,
+                       "batch": B, "sweeps": sweeps,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "operators (3.5 GiB) far exceed L2; every solve streams them from HBM"},
+                       "l2": "FP32 operators (1.75 GiB) and the block's leaf arrays far exceed L2"},
             "build_s": build_s, "mdof_per_s": value * dofs / 1e6,
-            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "note": "every request of a block completes with its block"},
+            "rel_err_vs_fp64": rel_err,
+            "speedup_vs_plain_fp64": value / plain_value,
+            "plain_fp64": {
+                "solves_per_s": plain_value, "mdof_per_s": plain_value * dofs / 1e6,
+                "latency_ms": {"p50": float(np.percentile(plain_lat, 50)),
+                               "p99": float(np.percentile(plain_lat, 99))},
+                "e2e_solves_per_s": plain_e2e,
+                "roofline": {"bound": "hbm", "kernel": p_dom, "achieved": p_ach, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": p_ach / hbm_peak,
+                             "traffic": (TRAFFIC_RATIO[p_dom] * plain_prof[p_dom]["bytes"] /
+                                         max(plain_prof[p_dom]["launches"], 1) if p_dom in TRAFFIC_RATIO else None),
+                             "share_of_solve": plain_prof[p_dom]["ms"] / p_tot},
+                "kernels_ms_per_solve": {k: v["ms"] / Kp for k, v in sorted(plain_prof.items())},
+            },
             "e2e": {"value": e2e_value, "unit": "solves/s",
-                    "h2d_bytes_per_step": int(8 * (dofs + 3 * 4 * hps.M)),
-                    "d2h_bytes_per_step": int(8 * dofs)},
+                    "h2d_bytes_per_step": int(B * 8 * (dofs + 2 * 4 * hps.M)),
+                    "d2h_bytes_per_step": int(B * 8 * dofs)},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
@@ -416,15 +492,17 @@ def run_gb300(args):
                                      if dom_name in TRAFFIC_RATIO else None),
                          "algorithmic_bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                         "share_of_solve": d["ms"] / tot_ms},
-            "fp64": {"solve_tflops": fp64_solve, "build_tflops": build_flops / build_s / 1e12,
-                     "build_flops": build_flops, "dgemm_peak_tflops_measured": fp64_peak,
+                         "share_of_step": d["ms"] / tot_ms},
+            "fp64": {"build_tflops": build_flops / build_s / 1e12, "build_flops": build_flops,
+                     "dgemm_peak_tflops_measured": fp64_peak,
                      "build_frac_of_dgemm": build_flops / build_s / 1e12 / fp64_peak},
             "build_sections_ms": {k: v["ms"] for k, v in sorted(build_prof.items())},
-            "kernels_ms_per_solve": {k: v["ms"] / args.steps for k, v in sorted(solve_secs.items())},
+            "kernels_ms_per_step": {k: v["ms"] / ksteps for k, v in sorted(prof.items())},
+            "kernels_tflops": {k: v["flops"] / (v["ms"] / 1e3) / 1e12 for k, v in sorted(prof.items()) if v["ms"]},
             "check_max_err_vs_exact": err,
             "clocks": clk,
         }
+        out.update(extras)
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)
@@ -432,15 +510,71 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def many_rhs(ef, torch, stream, args):
+    """512 right-hand sides on one factored uniform level-6 tree of 16x16 patches (1024^2 dofs):
+    one mixed block of 512 against 512 plain FP64 solves one at a time."""
+    level, n, nrhs = 6, 16, 512
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, DOM[0], DOM[1], n, DOM[2], DOM[3]))
+    mesh = ef.Mesh().uniform(level, root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hps.set_stream(stream.cuda_stream)
+    hps.buildStage()
+    X, Y = mesh.cell_centres()
+    bpts = hps.boundary_points()
+    P = 8
+    reqs = [make_request(5000 + i, X, Y, bpts) for i in range(P)]
+    F = np.stack([reqs[i % P][0] for i in range(nrhs)])
+    A = np.stack([reqs[i % P][1] for i in range(nrhs)])
+    R = np.stack([reqs[i % P][3] for i in range(nrhs)])
+    ref = []
+    for i in range(P):
+        hps.upwards_array(reqs[i][0])
+        hps.solve_arrays(reqs[i][1], reqs[i][2], reqs[i][3])
+        ref.append(hps.leaf_solution())
+    dev = [tuple(torch.from_numpy(x).cuda() for x in rq) for rq in reqs]
+    for i in range(3):
+        f, a, b, r = dev[i % P]
+        hps.load_device_async(f.data_ptr(), a.data_ptr(), b.data_ptr(), r.data_ptr())
+        hps.solve_device_async(True)
+    torch.cuda.synchronize()
+    e0, e1 = _events(torch, 2)
+    e0.record(stream)
+    for i in range(nrhs):
+        f, a, b, r = dev[i % P]
+        hps.load_device_async(f.data_ptr(), a.data_ptr(), b.data_ptr(), r.data_ptr())
+        hps.solve_device_async(True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain = nrhs / (e0.elapsed_time(e1) / 1e3)
+    hps.mixed_init(nrhs)
+    U = hps.mixed_solve(F, A, R, 1)
+    err = max(float(np.abs(U[i] - ref[i]).max() / np.abs(ref[i]).max()) for i in range(P))
+    hps.mixed_solve_async(nrhs, 1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(3):
+        hps.mixed_solve_async(nrhs, 1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mixed = 3 * nrhs / (e0.elapsed_time(e1) / 1e3)
+    return {"workload": "uniform level 6, 16x16 patches (1024^2 dofs), 512 right-hand sides, 1 sweep",
+            "mixed_block_solves_per_s": mixed, "plain_fp64_serial_solves_per_s": plain,
+            "speedup": mixed / plain, "rel_err_vs_fp64": err, "mdof_per_s": mixed * mesh.cell_centres()[0].size / 1e6}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--n", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=32, help="requests per block of the mixed form")
+    ap.add_argument("--sweeps", type=int, default=1, help="FP64 refinement sweeps of the mixed form")
+    ap.add_argument("--plain-steps", type=int, default=30, help="timed steps of the plain FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the 512-RHS level-6 case")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -266,6 +266,8 @@ int ef_hps_set_option(ef_hps* h, const char* key, int value) {
     } else if (k == "homogeneous-rhs") {
         h->homogeneous_rhs = value != 0;
         h->hps->set_homogeneous_rhs(value != 0);
+    } else if (k == "cuda-graphs") {
+        h->hps->set_graphs(value != 0);
     } else {
         return fail(EF_ERR_INVALID, "unknown option key: " + k);
     }

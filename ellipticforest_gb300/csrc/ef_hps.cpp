@@ -662,9 +662,20 @@ void Hps::downwards() {
 }
 
 void Hps::solve_async() {
-    upwards();
-    root_from_bc();
-    downwards();
+    const long long key = (homogeneous_ ? 1 : 0) | (bc_general_ ? 2 : 0);
+    graph_solve_.run(st_, key, graphs_ && !prof_, [&] {
+        upwards();
+        root_from_bc();
+        downwards();
+    });
+}
+
+void GraphCache::clear() {
+    for (auto& e : entries_)
+        if (e.exec) cudaGraphExecDestroy(e.exec);
+    entries_.clear();
+    if (cap_) cudaStreamDestroy(cap_);
+    cap_ = nullptr;
 }
 
 double Hps::build_flops() const {

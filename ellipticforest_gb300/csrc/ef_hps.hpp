@@ -71,6 +71,100 @@ struct LeafTypeHost {
 
 class MixedSolver;
 
+// Replays a fixed launch sequence through a CUDA graph.  The first call with a key runs eagerly (so
+// one-time kernel attributes and lazy allocations happen outside a capture), the second captures
+// the sequence on a private non-blocking stream, later calls launch the instantiated graph on the
+// caller's stream.  A sequence that cannot be captured keeps running eagerly.
+class GraphCache {
+public:
+    GraphCache() = default;
+    ~GraphCache() { clear(); }
+    GraphCache(const GraphCache&) = delete;
+    GraphCache& operator=(const GraphCache&) = delete;
+    // body() launches on `stream`, which is switched to the capture stream while capturing
+    template <class F>
+    void run(cudaStream_t& stream, long long key, bool enabled, F&& body);
+    void clear();
+    long long replays() const { return replays_; }
+
+private:
+    struct Entry {
+        long long key;
+        bool failed;
+        cudaGraphExec_t exec;
+        long long launches;  // kernels of the captured sequence, added to the counter per replay
+    };
+    std::vector<Entry> entries_;
+    cudaStream_t cap_ = nullptr;
+    long long replays_ = 0;
+};
+
+template <class F>
+void GraphCache::run(cudaStream_t& stream, long long key, bool enabled, F&& body) {
+    if (!enabled) { body(); return; }
+    Entry* e = nullptr;
+    for (auto& x : entries_)
+        if (x.key == key) { e = &x; break; }
+    if (!e) {
+        entries_.push_back(Entry{key, false, nullptr, 0});
+        body();
+        return;
+    }
+    if (e->failed) { body(); return; }
+    if (!e->exec) {
+        if (!cap_ && cudaStreamCreateWithFlags(&cap_, cudaStreamNonBlocking) != cudaSuccess) {
+            cap_ = nullptr;
+            e->failed = true;
+            (void)cudaGetLastError();
+            body();
+            return;
+        }
+        cudaStream_t orig = stream;
+        // the capture stream starts after the caller's pending work
+        cudaEvent_t ev = nullptr;
+        bool ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess &&
+                  cudaEventRecord(ev, orig) == cudaSuccess && cudaStreamWaitEvent(cap_, ev, 0) == cudaSuccess;
+        if (ev) cudaEventDestroy(ev);
+        cudaGraph_t g = nullptr;
+        if (ok) ok = cudaStreamBeginCapture(cap_, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        const long long l0 = g_kernel_launches.load();
+        if (ok) {
+            stream = cap_;
+            try {
+                body();
+            } catch (...) {
+                stream = orig;
+                cudaStreamEndCapture(cap_, &g);
+                if (g) cudaGraphDestroy(g);
+                (void)cudaGetLastError();
+                throw;
+            }
+            stream = orig;
+            ok = cudaStreamEndCapture(cap_, &g) == cudaSuccess && g;
+        }
+        // launches counted while capturing belong to the replays
+        e->launches = g_kernel_launches.load() - l0;
+        g_kernel_launches -= e->launches;
+        if (ok) ok = cudaGraphInstantiate(&e->exec, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+        if (!ok) {
+            e->failed = true;
+            e->exec = nullptr;
+            (void)cudaGetLastError();
+            body();
+            return;
+        }
+    }
+    if (cudaGraphLaunch(e->exec, stream) != cudaSuccess) {
+        (void)cudaGetLastError();
+        e->failed = true;
+        body();
+        return;
+    }
+    g_kernel_launches += e->launches;
+    ++replays_;
+}
+
 class Hps {
 public:
     friend class MixedSolver;
@@ -80,6 +174,9 @@ public:
     Hps& operator=(const Hps&) = delete;
 
     void set_stream(cudaStream_t st) { st_ = st; }
+    // CUDA-graph replay of the solve sequences (on by default; profiling runs them eagerly)
+    void set_graphs(bool on) { graphs_ = on; }
+    bool graphs() const { return graphs_; }
     // FivePointStencil: per-leaf coefficients sampled at the reference's points (host arrays in leaf
     // order: alpha n*n, beta 4*n*n (W, E, S, N face of every cell), lambda n*n per leaf)
     void set_coefficients(const double* alpha, const double* beta, const double* lambda);
@@ -191,6 +288,8 @@ private:
         double bytes, flops;
     };
     bool prof_ = false;
+    bool graphs_ = true;
+    GraphCache graph_solve_;
     std::vector<ProfStat> stats_;
     std::vector<Mark> marks_;
     std::vector<cudaEvent_t> ev_free_;
@@ -268,6 +367,7 @@ private:
     int* d_err_ = nullptr;
     float* rleaf_ = nullptr;
     MixCoef* d_coef_ = nullptr;
+    GraphCache graphs_;
     char* uG_begin_ = nullptr;
     size_t uG_bytes_ = 0;
     float* tables_ = nullptr;

@@ -18,6 +18,8 @@
 // cell arrays are [B][leaves][n*n].
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "ef_kernels.cuh"
 
 namespace cg = cooperative_groups;
@@ -101,6 +103,10 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src, int nbytes
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes)
                  : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int nbytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
@@ -142,6 +148,12 @@ __device__ __forceinline__ void tma_load_tile(const CUtensorMap* tm, unsigned lo
 
 enum : int { MX_W = 0, MX_H = 1, MX_DOWN = 2 };
 
+// floats per A stage: rt rows of 32, rounded up to a 1024-byte multiple
+__host__ __device__ __forceinline__ int mx_astage_floats(int rt) { return ((rt * kKC * 4 + 1023) / 1024) * 256; }
+inline size_t mx_gemm_smem(int rt, int BN) {
+    return 1024 + size_t(kStages) * mx_astage_floats(rt) * 4 + size_t(kStages) * kKC * BN * 4 + kStages * 8;
+}
+
 template <int KIND>
 __host__ __device__ __forceinline__ void mx_shape(int s, int& rows_item, int& K) {
     if (KIND == MX_W) { rows_item = 4 * s; K = 4 * s; }
@@ -149,42 +161,75 @@ __host__ __device__ __forceinline__ void mx_shape(int s, int& rows_item, int& K)
     else { rows_item = 4 * s; K = 8 * s; }
 }
 
+// one tile of rt rows: its node, its row offset and the rows of X it multiplies
+struct MxTile {
+    int item, tl, row0, kb;
+    const float* X1;  // X rows k < kb
+    const float* X2;  // X rows k >= kb (indexed with the same k)
+};
+
+template <int KIND>
+__device__ __forceinline__ MxTile mx_tile(const MixItem* __restrict__ items, int s, int B, int rt, int tpi,
+                                          int tile) {
+    MxTile t;
+    t.item = tile / tpi;
+    t.tl = tile - t.item * tpi;
+    t.row0 = t.tl * rt;
+    const MixItem& it = items[t.item];
+    if (KIND == MX_W) { t.X1 = it.hd; t.X2 = t.X1; t.kb = 4 * s; }
+    else if (KIND == MX_DOWN) { t.X1 = it.gf; t.X2 = t.X1; t.kb = 8 * s; }
+    else {
+        int c, q, Ia, Ib;
+        mx_ext_map(t.row0, s, c, q);
+        mx_child_ifaces(c, Ia, Ib);
+        t.X1 = it.w + (long long)Ia * s * B;
+        t.X2 = it.w + (long long)(Ib - 1) * s * B;  // row k >= s of [w_Ia; w_Ib] is w_Ib[k - s]
+        t.kb = s;
+    }
+    return t;
+}
+
+// Work list of a CTA: a split launch (ksplit > 1, one cluster per tile) gives each CTA one K range of
+// one tile; otherwise the CTA strides over tiles (persistent), so the TMA pipeline runs on across
+// tile boundaries and each epilogue overlaps the next tile's loads.
 template <int BN, int KIND>
 __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtensorMap tmA,
                                                  const MixItem* __restrict__ items, int s, int B, int rt,
-                                                 int ksplit, int* __restrict__ err) {
+                                                 int ksplit, int ntiles, int* __restrict__ err) {
     constexpr int TXN = BN / 4;
-    __shared__ __align__(1024) float As[kStages][kRT * kKC];
-    __shared__ __align__(16) float Xs[kStages][kKC * BN];
-    __shared__ __align__(8) unsigned long long full[kStages];
+    // dynamic shared memory: kStages A stages of rt x 32 floats (1024-byte aligned for the 128-byte
+    // swizzle), kStages X stages of 32 x BN floats, kStages mbarriers
+    extern __shared__ unsigned char mx_smem[];
+    const int astage = mx_astage_floats(rt);
+    float* As0 = reinterpret_cast<float*>(mx_smem + ((1024u - (smem_u32(mx_smem) & 1023u)) & 1023u));
+    float* Xs0 = As0 + kStages * astage;
+    unsigned long long* full = reinterpret_cast<unsigned long long*>(Xs0 + kStages * kKC * BN);
     const int tid = threadIdx.x, nt = blockDim.x;
     const int tx = tid % TXN, ty = tid / TXN;
     const int rq = rt / 4;  // thread rows: ty + i*rq, i < 4
     int rows_item, K;
     mx_shape<KIND>(s, rows_item, K);
     const int tpi = rows_item / rt;
-    const int tile = blockIdx.x / ksplit, kp = blockIdx.x - tile * ksplit;
-    const int item = tile / tpi, tl = tile - item * tpi, row0 = tl * rt;
-    const MixItem& it = items[item];
-    const int b0 = blockIdx.y * BN;
-    const float* X1;
-    const float* X2;
-    int kb;
-    int hc_c = 0;
-    if (KIND == MX_W) { X1 = it.hd; X2 = X1; kb = K; }
-    else if (KIND == MX_DOWN) { X1 = it.gf; X2 = X1; kb = K; }
-    else {
-        int q, Ia, Ib;
-        mx_ext_map(row0, s, hc_c, q);
-        mx_child_ifaces(hc_c, Ia, Ib);
-        X1 = it.w + (long long)Ia * s * B;
-        X2 = it.w + (long long)(Ib - 1) * s * B;  // row k >= s of [w_Ia; w_Ib] is w_Ib[k - s]
-        kb = s;
-    }
     const int nkc = (K + kKC - 1) / kKC;
-    const int cpp = (nkc + ksplit - 1) / ksplit;
-    const int c0 = min(nkc, kp * cpp), c1 = min(nkc, c0 + cpp);
-    const int yrow = item * rows_item + row0;
+    const bool vecx = (B & 3) == 0;
+    int first_tile, tile_step, nunits, cpu, cbase;
+    if (ksplit > 1) {
+        const int kp = blockIdx.x % ksplit;
+        const int cpp = (nkc + ksplit - 1) / ksplit;
+        first_tile = blockIdx.x / ksplit;
+        tile_step = 0;
+        nunits = 1;
+        cbase = min(nkc, kp * cpp);
+        cpu = min(nkc, cbase + cpp) - cbase;
+    } else {
+        first_tile = blockIdx.x;
+        tile_step = gridDim.x;
+        nunits = first_tile < ntiles ? (ntiles - 1 - first_tile) / tile_step + 1 : 0;
+        cbase = 0;
+        cpu = nkc;
+    }
+    const int total = cpu > 0 ? nunits * cpu : 0;
+    const int b0 = blockIdx.y * BN;
     const unsigned tile_bytes = unsigned(rt) * kKC * sizeof(float);
 
     if (tid == 0) {
@@ -194,15 +239,29 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
     }
     __syncthreads();
 
-    auto issue = [&](int c, int st) {
-        if (tid == 0) tma_load_tile(&tmA, &full[st], As[st], c * kKC, yrow, tile_bytes);
+    auto issue = [&](int v, int st) {
+        const int unit = v / cpu, ch = v - unit * cpu;
+        const MxTile t = mx_tile<KIND>(items, s, B, rt, tpi, first_tile + unit * tile_step);
+        const int c = cbase + ch;
+        if (tid == 0)
+            tma_load_tile(&tmA, &full[st], As0 + st * astage, c * kKC, t.item * rows_item + t.row0, tile_bytes);
         const int k0 = c * kKC;
-        for (int e = tid; e < kKC * BN; e += nt) {
-            const int k = e / BN, col = e - (e / BN) * BN;
-            const int gk = k0 + k, gb = b0 + col;
-            const bool ok = gk < K && gb < B;
-            const float* src = ok ? ((gk < kb ? X1 : X2) + (long long)gk * B + gb) : X1;
-            cp_async4(&Xs[st][e], src, ok ? 4 : 0);
+        if (vecx) {
+            for (int e = tid; e < kKC * TXN; e += nt) {
+                const int k = e / TXN, col = (e - (e / TXN) * TXN) * 4;
+                const int gk = k0 + k, gb = b0 + col;
+                const bool ok = gk < K && gb < B;
+                const float* src = ok ? ((gk < t.kb ? t.X1 : t.X2) + (long long)gk * B + gb) : t.X1;
+                cp_async16(Xs0 + st * (kKC * BN) + k * BN + col, src, ok ? 16 : 0);
+            }
+        } else {
+            for (int e = tid; e < kKC * BN; e += nt) {
+                const int k = e / BN, col = e - (e / BN) * BN;
+                const int gk = k0 + k, gb = b0 + col;
+                const bool ok = gk < K && gb < B;
+                const float* src = ok ? ((gk < t.kb ? t.X1 : t.X2) + (long long)gk * B + gb) : t.X1;
+                cp_async4(Xs0 + st * (kKC * BN) + e, src, ok ? 4 : 0);
+            }
         }
     };
 
@@ -212,21 +271,101 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
 
+    auto epilogue = [&](int tile) {
+        const MxTile t = mx_tile<KIND>(items, s, B, rt, tpi, tile);
+        const MixItem& it = items[t.item];
+        if (KIND == MX_DOWN && blockIdx.y == 0) {
+            // exterior points of the parent go to the children unchanged; each tile copies its share
+            const int tot = 8 * s * B, per = (tot + tpi - 1) / tpi;
+            const int e0 = t.tl * per, e1 = min(tot, e0 + per);
+            for (int e = e0 + tid; e < e1; e += nt) {
+                const int p = e / B, bb = e - (e / B) * B;
+                int c, q;
+                mx_ext_map(p, s, c, q);
+                it.gc[c][(long long)q * B + bb] = it.gf[e];
+            }
+        }
+        const int bq = b0 + 4 * tx;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = t.row0 + ty + i * rq;
+            const long long rb = (long long)r * B + bq;
+            float v[4] = {acc[i][0], acc[i][1], acc[i][2], acc[i][3]};
+            float* dst0;
+            float* dst1 = nullptr;
+            if (KIND == MX_W) {
+                dst0 = it.w + rb;
+            } else if (KIND == MX_H) {
+                int c, q;
+                mx_ext_map(r, s, c, q);
+                const float* hp = it.hc[c] + (long long)q * B + bq;
+                if (vecx && bq < B) {
+                    const float4 hv = *reinterpret_cast<const float4*>(hp);
+                    v[0] += hv.x; v[1] += hv.y; v[2] += hv.z; v[3] += hv.w;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (bq + j < B) v[j] += hp[j];
+                }
+                dst0 = it.h + rb;
+            } else {
+                const int I = r / s, o = r - (r / s) * s;
+                const float* wp = it.w + rb;
+                if (vecx && bq < B) {
+                    const float4 wv = *reinterpret_cast<const float4*>(wp);
+                    v[0] += wv.x; v[1] += wv.y; v[2] += wv.z; v[3] += wv.w;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (bq + j < B) v[j] += wp[j];
+                }
+                dst0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + bq;
+                dst1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + bq;
+                double* ug = it.uG + rb;
+                if (vecx && bq < B) {
+                    double2 u0 = reinterpret_cast<double2*>(ug)[0], u1 = reinterpret_cast<double2*>(ug)[1];
+                    u0.x += f2d_bits(v[0]); u0.y += f2d_bits(v[1]);
+                    u1.x += f2d_bits(v[2]); u1.y += f2d_bits(v[3]);
+                    reinterpret_cast<double2*>(ug)[0] = u0;
+                    reinterpret_cast<double2*>(ug)[1] = u1;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (bq + j < B) ug[j] += f2d_bits(v[j]);
+                }
+            }
+            if (vecx) {
+                if (bq < B) {
+                    const float4 o4 = make_float4(v[0], v[1], v[2], v[3]);
+                    *reinterpret_cast<float4*>(dst0) = o4;
+                    if (KIND == MX_DOWN) *reinterpret_cast<float4*>(dst1) = o4;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (bq + j < B) {
+                        dst0[j] = v[j];
+                        if (KIND == MX_DOWN) dst1[j] = v[j];
+                    }
+            }
+        }
+    };
+
     int issued = 0;
     for (int p = 0; p < kStages - 1; ++p) {
-        if (c0 + p < c1) { issue(c0 + p, p); ++issued; }
+        if (p < total) { issue(p, p); ++issued; }
         cp_async_commit();
     }
-    bool failed = false;
-    for (int c = c0; c < c1; ++c) {
-        const int u = c - c0, st = u % kStages;
+    int fail_v = -1;
+    for (int v = 0; v < total; ++v) {
+        const int st = v % kStages;
         cp_async_wait<kStages - 2>();
-        const bool ok = mbar_wait(&full[st], unsigned(u / kStages) & 1u);
-        if (__syncthreads_or(!ok)) { failed = true; break; }
-        if (c + kStages - 1 < c1) { issue(c + kStages - 1, (u + kStages - 1) % kStages); ++issued; }
+        const bool ok = mbar_wait(&full[st], unsigned(v / kStages) & 1u);
+        if (__syncthreads_or(!ok)) { fail_v = v; break; }
+        if (v + kStages - 1 < total) { issue(v + kStages - 1, (v + kStages - 1) % kStages); ++issued; }
         cp_async_commit();
-        const float* as = As[st];
-        const float* xs = Xs[st];
+        const float* as = As0 + st * astage;
+        const float* xs = Xs0 + st * (kKC * BN);
 #pragma unroll
         for (int k4 = 0; k4 < kKC / 4; ++k4) {
             float4 a[4];
@@ -248,76 +387,44 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
                 }
             }
         }
+        if (ksplit == 1 && v % cpu == cpu - 1) {
+            epilogue(first_tile + (v / cpu) * tile_step);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        }
     }
     cp_async_wait<0>();
-    if (failed) {
+    if (fail_v >= 0) {
         // let the tiles still in flight land before this CTA's shared memory goes away
-        const int u_end = issued;
-        for (int u = 0; u < u_end; ++u) (void)mbar_wait(&full[u % kStages], unsigned(u / kStages) & 1u);
+        for (int v = fail_v; v < issued; ++v) (void)mbar_wait(&full[v % kStages], unsigned(v / kStages) & 1u);
         if (tid == 0) atomicExch(err, 1);
     }
     __syncthreads();
+    if (ksplit == 1) return;
 
-    if (ksplit > 1) {
-        // partial tiles -> rank 0 of the cluster through distributed shared memory
-        cg::cluster_group cluster = cg::this_cluster();
-        float* red = &As[0][0];
+    // partial tiles -> rank 0 of the cluster through distributed shared memory
+    cg::cluster_group cluster = cg::this_cluster();
+    float* red = As0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-            *reinterpret_cast<float4*>(red + (ty + i * rq) * BN + 4 * tx) =
-                make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
-        cluster.sync();
-        const bool lead = cluster.block_rank() == 0;
-        if (lead) {
-            for (int rk = 1; rk < ksplit; ++rk) {
-                const float* rr = cluster.map_shared_rank(red, rk);
+    for (int i = 0; i < 4; ++i)
+        *reinterpret_cast<float4*>(red + (ty + i * rq) * BN + 4 * tx) =
+            make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    cluster.sync();
+    const bool lead = cluster.block_rank() == 0;
+    if (lead) {
+        for (int rk = 1; rk < ksplit; ++rk) {
+            const float* rr = cluster.map_shared_rank(red, rk);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float4 v = *reinterpret_cast<const float4*>(rr + (ty + i * rq) * BN + 4 * tx);
-                    acc[i][0] += v.x; acc[i][1] += v.y; acc[i][2] += v.z; acc[i][3] += v.w;
-                }
-            }
-        }
-        cluster.sync();
-        if (!lead) return;
-    }
-    if (failed) return;
-
-    // epilogue
-    if (KIND == MX_DOWN && blockIdx.y == 0) {
-        // exterior points of the parent go to the children unchanged; each tile copies its share
-        const int tot = 8 * s * B, per = (tot + tpi - 1) / tpi;
-        const int e0 = tl * per, e1 = min(tot, e0 + per);
-        for (int e = e0 + tid; e < e1; e += nt) {
-            const int p = e / B, bb = e - (e / B) * B;
-            int c, q;
-            mx_ext_map(p, s, c, q);
-            it.gc[c][(long long)q * B + bb] = it.gf[e];
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int r = row0 + ty + i * rq;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int b = b0 + 4 * tx + j;
-            if (b >= B) continue;
-            const long long rb = (long long)r * B + b;
-            if (KIND == MX_W) {
-                it.w[rb] = acc[i][j];
-            } else if (KIND == MX_H) {
-                int c, q;
-                mx_ext_map(r, s, c, q);
-                it.h[rb] = acc[i][j] + it.hc[c][(long long)q * B + b];
-            } else {
-                const int I = r / s, o = r - (r / s) * s;
-                const float uu = acc[i][j] + it.w[rb];
-                it.gc[mx_lower_child(I)][(long long)mx_q_lower(I, o, s) * B + b] = uu;
-                it.gc[mx_upper_child(I)][(long long)mx_q_upper(I, o, s) * B + b] = uu;
-                it.uG[rb] += f2d_bits(uu);
+            for (int i = 0; i < 4; ++i) {
+                const float4 v = *reinterpret_cast<const float4*>(rr + (ty + i * rq) * BN + 4 * tx);
+                acc[i][0] += v.x; acc[i][1] += v.y; acc[i][2] += v.z; acc[i][3] += v.w;
             }
         }
     }
+    cluster.sync();
+    if (lead && fail_v < 0) epilogue(first_tile);
 }
 
 // ---- FP64 residual -------------------------------------------------------------------------------
@@ -401,12 +508,13 @@ __global__ void k_mx_uncoarsen(const T* const* vin, T* const* vout, int nf, int 
 // with float4 operand reads from shared memory (V depends on n only, so one copy serves all types).
 // NEUMANN writes h32 = DtN(0, q); SOLVE adds the solution of (g32, q) to the FP64 state u64 (or
 // stores it there when accumulate is 0).
-template <int MODE>
+template <int MODE, int NT>
 __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict__ types,
-                                                   const MixLeaf* __restrict__ leaves, int L, int B, int n,
+                                                   const MixLeaf* __restrict__ leaves, int L, int B, int n_arg,
                                                    int ipc, const float* __restrict__ q, double* __restrict__ u64,
                                                    int accumulate) {
     extern __shared__ __align__(16) float smf[];
+    const int n = NT ? NT : n_arg;  // NT > 0: leaf size known at compile time (loops unrolled)
     const int nn = n * n, nb = n / 4, tpi = nb * nb;
     const int istride = 2 * nn + 16;
     float* VS = smf;
@@ -464,7 +572,8 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
     };
     // acc[a][c] += P[t][4pa + a] * Q[t][4pc + c] over t < n (both row-major n x n in shared memory)
     auto outer = [&](const float* P, int pa, const float* Q, int pc) {
-        for (int t = 0; t < n; ++t) {
+#pragma unroll
+        for (int t = 0; t < (NT ? NT : n); ++t) {
             const float4 x = *reinterpret_cast<const float4*>(P + t * n + 4 * pa);
             const float4 y = *reinterpret_cast<const float4*>(Q + t * n + 4 * pc);
             const float xa[4] = {x.x, x.y, x.z, x.w};
@@ -538,7 +647,8 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
             else if (side == 2) { i = pos; j = 0; }
             else { i = pos; j = n - 1; }
             float u = 0.f;
-            for (int l = 0; l < n; ++l) u = fmaf(W[l * n + i], VT[l * n + j], u);
+#pragma unroll
+            for (int l = 0; l < (NT ? NT : n); ++l) u = fmaf(W[l * n + i], VT[l * n + j], u);
             const float sg = (side == 0 || side == 2) ? 1.0f : -1.0f;
             lf.h32[(long long)r * B + b] = sg * (side < 2 ? dtn_x : dtn_y) * u;
         }
@@ -554,12 +664,15 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
 // Items (leaf, b) with b fastest; each thread owns 4 consecutive cells of one row.  zero_state: u is
 // identically zero (the first residual).  The largest |r| (as FP32) of every item goes to
 // rleaf[b][leaf] (reduced per request by k_mx_rmax).
+template <int NT>
 __global__ void __launch_bounds__(256) k_mx_leaf_residual(const MixCoef* __restrict__ coefs,
-                                                          const MixLeaf* __restrict__ leaves, int L, int B, int n,
-                                                          int ipc, int zero_state, const double* __restrict__ f,
+                                                          const MixLeaf* __restrict__ leaves, int L, int B,
+                                                          int n_arg, int ipc, int zero_state,
+                                                          const double* __restrict__ f,
                                                           const double* __restrict__ u64, float* __restrict__ q,
                                                           float* __restrict__ rleaf) {
     __shared__ unsigned smax[256];
+    const int n = NT ? NT : n_arg;
     const int nn = n * n, tpi = nn / 4;
     const int tpe = tpi < 256 ? tpi : 256;
     const int slot = threadIdx.x / tpe, lt = threadIdx.x - slot * tpe;
@@ -708,24 +821,35 @@ inline unsigned mx_grid(long long tot) {
     return unsigned(b < 1 ? 1 : b);
 }
 
-template <int KIND>
-void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B, int* err) {
-    int rows_item, K;
-    mx_shape<KIND>(s, rows_item, K);
-    const int rt = mx_tile_rows(KIND == MX_H ? 1 : 0, s);
-    const int tiles = nitems * (rows_item / rt);
-    const int BN = B <= 8 ? 8 : (B <= 16 ? 16 : 32);
+template <int BN, int KIND>
+int mx_gemm_slots(int rt) {
+    static int slots[65] = {0};
+    if (!slots[rt]) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int threads = (rt / 4) * (BN / 4);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_gemm<BN, KIND>, threads, mx_gemm_smem(rt, BN));
+        slots[rt] = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+    }
+    return slots[rt];
+}
+
+template <int BN, int KIND>
+void mx_gemm_launch(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int ntiles, int s, int B, int rt,
+                    int ksplit, int* err) {
     const int chunks = (B + BN - 1) / BN;
-    const int nkc = (K + kKC - 1) / kKC;
-    int ksplit = 1;
-    // Split K only while fewer than ~4 CTAs per SM are in flight, and keep at least 8 chunks per
-    // CTA (the TMA pipeline and the cluster reduction cost a few microseconds per CTA).  Chosen from
-    // the tile count alone so that every request's sums are grouped the same way whatever the batch.
-    while (ksplit < 8 && (long long)tiles * ksplit < 608 && nkc >= 16 * ksplit) ksplit *= 2;
+    unsigned gx;
+    if (ksplit > 1) {
+        gx = unsigned(ntiles * ksplit);
+    } else {
+        const int slots = mx_gemm_slots<BN, KIND>(rt) / chunks;
+        gx = unsigned(std::max(1, std::min(ntiles, slots)));
+    }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(unsigned(tiles * ksplit), unsigned(chunks));
+    cfg.gridDim = dim3(gx, unsigned(chunks));
     cfg.blockDim = dim3(unsigned((rt / 4) * (BN / 4)));
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = mx_gemm_smem(rt, BN);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -734,9 +858,25 @@ void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int n
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = ksplit > 1 ? 1 : 0;
-    if (BN == 8) cudaLaunchKernelEx(&cfg, k_mx_gemm<8, KIND>, tm, items, s, B, rt, ksplit, err);
-    else if (BN == 16) cudaLaunchKernelEx(&cfg, k_mx_gemm<16, KIND>, tm, items, s, B, rt, ksplit, err);
-    else cudaLaunchKernelEx(&cfg, k_mx_gemm<32, KIND>, tm, items, s, B, rt, ksplit, err);
+    cudaLaunchKernelEx(&cfg, k_mx_gemm<BN, KIND>, tm, items, s, B, rt, ksplit, ntiles, err);
+}
+
+template <int KIND>
+void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B, int* err) {
+    int rows_item, K;
+    mx_shape<KIND>(s, rows_item, K);
+    const int rt = mx_tile_rows(KIND == MX_H ? 1 : 0, s);
+    const int tiles = nitems * (rows_item / rt);
+    const int BN = B <= 8 ? 8 : (B <= 16 ? 16 : 32);
+    const int nkc = (K + kKC - 1) / kKC;
+    // Split K (one cluster of ksplit CTAs per tile) only while fewer than ~4 CTAs per SM would be in
+    // flight and every CTA keeps at least 8 chunks.  Chosen from the tile count alone so that every
+    // request's sums are grouped the same way whatever the batch size.
+    int ksplit = 1;
+    while (ksplit < 8 && (long long)tiles * ksplit < 608 && nkc >= 16 * ksplit) ksplit *= 2;
+    if (BN == 8) mx_gemm_launch<8, KIND>(st, tm, items, tiles, s, B, rt, ksplit, err);
+    else if (BN == 16) mx_gemm_launch<16, KIND>(st, tm, items, tiles, s, B, rt, ksplit, err);
+    else mx_gemm_launch<32, KIND>(st, tm, items, tiles, s, B, rt, ksplit, err);
     ++g_kernel_launches;
 }
 
@@ -787,21 +927,39 @@ void mx_convert(cudaStream_t st, const MixConv* items, int nitems, int s) {
     ++g_kernel_launches;
 }
 
+template <int MODE, int NT>
+void mx_leaf32_launch(cudaStream_t st, unsigned grid, unsigned threads, size_t smem, const LeafType32* types,
+                      const MixLeaf* leaves, int L, int B, int n, int ipc, const float* q, double* u64,
+                      int accumulate) {
+    static size_t configured = 48 * 1024;
+    if (smem > configured) {
+        cudaFuncSetAttribute(k_mx_leaf32<MODE, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        configured = smem;
+    }
+    k_mx_leaf32<MODE, NT><<<grid, threads, smem, st>>>(types, leaves, L, B, n, ipc, q, u64, accumulate);
+}
+
+template <int MODE>
+void mx_leaf32_mode(cudaStream_t st, unsigned grid, unsigned threads, size_t smem, const LeafType32* types,
+                    const MixLeaf* leaves, int L, int B, int n, int ipc, const float* q, double* u64,
+                    int accumulate) {
+    if (n == 16) mx_leaf32_launch<MODE, 16>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
+    else if (n == 8) mx_leaf32_launch<MODE, 8>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
+    else if (n == 32) mx_leaf32_launch<MODE, 32>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
+    else mx_leaf32_launch<MODE, 0>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
+}
+
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate) {
     const int nb = n / 4, tpi = nb * nb, ipc = tpi >= 256 ? 1 : 256 / tpi;
     const size_t smem = (size_t(2) * n * n + size_t(ipc) * (2 * n * n + 16)) * sizeof(float);
-    static size_t configured = 48 * 1024;
-    if (smem > configured) {
-        cudaFuncSetAttribute(k_mx_leaf32<LEAF_NEUMANN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        cudaFuncSetAttribute(k_mx_leaf32<LEAF_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        configured = smem;
-    }
     const long long items = (long long)L * B;
     const unsigned grid = unsigned((items + ipc - 1) / ipc);
     const unsigned threads = unsigned(ipc * tpi);
-    if (mode == LEAF_NEUMANN) k_mx_leaf32<LEAF_NEUMANN><<<grid, threads, smem, st>>>(types, leaves, L, B, n, ipc, q, u64, 0);
-    else k_mx_leaf32<LEAF_SOLVE><<<grid, threads, smem, st>>>(types, leaves, L, B, n, ipc, q, u64, accumulate);
+    if (mode == LEAF_NEUMANN)
+        mx_leaf32_mode<LEAF_NEUMANN>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, 0);
+    else
+        mx_leaf32_mode<LEAF_SOLVE>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
     ++g_kernel_launches;
 }
 
@@ -810,8 +968,15 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leav
     const int tpi = n * n / 4, tpe = tpi < 256 ? tpi : 256, ipc = 256 / tpe;
     const long long items = (long long)L * B;
     const unsigned grid = unsigned((items + ipc - 1) / ipc);
-    k_mx_leaf_residual<<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q,
-                                                             rmax ? rleaf : nullptr);
+    float* rl = rmax ? rleaf : nullptr;
+    if (n == 16)
+        k_mx_leaf_residual<16><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
+    else if (n == 8)
+        k_mx_leaf_residual<8><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
+    else if (n == 32)
+        k_mx_leaf_residual<32><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
+    else
+        k_mx_leaf_residual<0><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
     ++g_kernel_launches;
     if (rmax) {
         k_mx_rmax<<<B, 256, 0, st>>>(rleaf, L, rmax);

@@ -296,7 +296,7 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
     h.pb("mx_leaf_residual");
     mx_leaf_residual(st, d_coef_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
                      rleaf_, rmax);
-    h.pe(L * B * nn * 20.0, L * B * nn * 12.0);
+    h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0);
     h.pb("mx_interface");
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         for (auto& s : hsteps_)
@@ -358,15 +358,16 @@ void MixedSolver::solve(int B, int sweeps) {
     if (B < 1 || B > bmax_) throw std::invalid_argument("mixed solver: batch size out of range");
     if (sweeps < 0 || sweeps + 1 > kMaxPasses) throw std::invalid_argument("mixed solver: too many sweeps");
     Hps& h = H_;
-    cudaStream_t st = h.stream();
-    const size_t cells = size_t(h.num_leaves()) * h.leaf_n() * h.leaf_n();
-    ck(cudaMemsetAsync(uG_begin_, 0, uG_bytes_, st), "clear interface state");
-    ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, st), "clear residuals");
-    mx_root(st, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
-    for (int p = 0; p <= sweeps; ++p) {
-        residual(B, rmax_ + size_t(p) * bmax_, p == 0);
-        pass(B, p == 0);
-    }
+    graphs_.run(h.st_, (long long)B * 64 + sweeps, h.graphs() && !h.prof_, [&] {
+        cudaStream_t s = h.stream();
+        ck(cudaMemsetAsync(uG_begin_, 0, uG_bytes_, s), "clear interface state");
+        ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, s), "clear residuals");
+        mx_root(s, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
+        for (int p = 0; p <= sweeps; ++p) {
+            residual(B, rmax_ + size_t(p) * bmax_, p == 0);
+            pass(B, p == 0);
+        }
+    });
 }
 
 int MixedSolver::take_error() {

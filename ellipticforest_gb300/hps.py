@@ -326,6 +326,10 @@ class HPSAlgorithm:
     def set_stream(self, cuda_stream_ptr: int):
         check(_lib.load().ef_hps_set_stream(self._h, C.c_void_p(cuda_stream_ptr)))
 
+    def set_graphs(self, on: bool):
+        """CUDA-graph replay of the device-resident solve sequences (default on)."""
+        check(_lib.load().ef_hps_set_option(self._h, b"cuda-graphs", int(bool(on))))
+
     # -- stages --------------------------------------------------------------------------------
     def setupStage(self):
         check(_lib.load().ef_hps_setup(self._h))

@@ -72,7 +72,9 @@ int ef_hps_create(const ef_mesh* mesh, int solver_type, double lambda, ef_hps** 
  * (x_i, y_j -/+ dy/2) (4*n*n per leaf: all W values, then E, S, N), lambda(x_i, y_j) (n*n). */
 int ef_hps_set_coefficients(ef_hps* hps, const double* alpha, const double* beta,
                             const double* lambda);
-/* Option keys of the reference: "cache-operators", "homogeneous-rhs" (HPSAlgorithm.hpp:134,532). */
+/* Option keys of the reference: "cache-operators", "homogeneous-rhs" (HPSAlgorithm.hpp:134,532).
+ * Added key "cuda-graphs" (default 1): replay the device-resident solve sequences
+ * (ef_hps_solve_device_async, ef_hps_mixed_solve*) as CUDA graphs after their first two calls. */
 int ef_hps_set_option(ef_hps* hps, const char* key, int value);
 /* Use an external CUDA stream (cudaStream_t) for all work of this handle; NULL = default stream. */
 int ef_hps_set_stream(ef_hps* hps, void* cuda_stream);

@@ -83,3 +83,31 @@ def test_mixed_result_same_alone_and_in_a_block(ef):
     for k in (0, 5, 10):
         alone = hps.mixed_solve(F[k:k + 1], A[k:k + 1], R[k:k + 1], sweeps=1)
         assert np.array_equal(alone[0], block[k])
+
+
+def test_graph_replay_matches_eager(ef):
+    """The captured solve sequences (plain FP64 and mixed) give the eager results bit for bit."""
+    import torch
+    mesh, hps = make(ef, ("uniform", 3), 16, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, 3, 31)
+    f = torch.from_numpy(F[0]).cuda()
+    a = torch.from_numpy(A[0]).cuda()
+    b = torch.zeros_like(a)
+    r = torch.from_numpy(R[0]).cuda()
+    hps.set_graphs(False)
+    hps.load_device_async(f.data_ptr(), a.data_ptr(), b.data_ptr(), r.data_ptr())
+    hps.solve_device_async(True)
+    hps.synchronize()
+    eager = hps.leaf_solution().copy()
+    hps.set_graphs(True)
+    for _ in range(3):  # eager first call, capture, replay
+        hps.load_device_async(f.data_ptr(), a.data_ptr(), b.data_ptr(), r.data_ptr())
+        hps.solve_device_async(True)
+        hps.synchronize()
+        assert np.array_equal(hps.leaf_solution(), eager)
+    hps.mixed_init(3)
+    hps.set_graphs(False)
+    ref = hps.mixed_solve(F, A, R, sweeps=1)
+    hps.set_graphs(True)
+    for _ in range(3):
+        assert np.array_equal(hps.mixed_solve(F, A, R, sweeps=1), ref)
