@@ -15,6 +15,9 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
   plain_fp64 -- the plain FP64 form one request at a time (device-resident solves/s, p50/p99, and
             e2e through the reference-facing upwards/solve/get_leaf_u calls)
   many_rhs_L6 -- 512 right-hand sides on a uniform level-6 tree: one mixed block vs 512 plain solves
+  serving -- 2000 Poisson-arrival requests over three resident trees (uniform L4, adaptive max level
+            7, uniform L7) through the serving loop (continuous same-tree batching, p50/p99 latency)
+            against the same requests one at a time through the plain FP64 path
   --impl reference -- the FP64 CPU oracle (a restatement of the reference's HPS path, same LAPACK
             calls) on the same workload, rank 0 only, on the host cores.
 """
@@ -447,6 +450,7 @@ def run_gb300(args):
     extras = {}
     if not args.no_extras:
         extras["many_rhs_L6"] = many_rhs(ef, torch, stream, args)
+        extras["serving"] = serving(ef, torch, stream, (mesh, hps), args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -510,6 +514,140 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def make_request_box(seed, X, Y, bpts, box):
+    """make_request on a tree over `box`: the bumps and modes live on the box mapped to [-1,1]^2."""
+    x0, x1, y0, y1 = box
+    sx = lambda x: 2 * (x - x0) / (x1 - x0) - 1
+    sy = lambda y: 2 * (y - y0) / (y1 - y0) - 1
+    return make_request(seed, sx(X), sy(Y), [(sx(x), sy(y)) for x, y in bpts])
+
+
+def serving(ef, torch, stream, main_tree, args):
+    """Poisson-arrival stream of 2000 requests (seeded) over three resident trees -- uniform L4,
+    the adaptive tree of refineByFunction(|sin x + sin y| > 1.2, 0, 7) on [-10,10]^2, uniform L7 --
+    answered by the serving loop (continuous same-tree batching, two lanes per tree, HBM budget), against
+    the same requests one at a time through the plain FP64 path's C ABI calls."""
+    import threading
+    from ellipticforest_gb300._lib import check, dptr, load
+    lib = load()
+    trees = []
+    r4 = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -1.0, 1.0, 16, -1.0, 1.0))
+    m4 = ef.Mesh().uniform(4, r4)
+    h4 = ef.HPSAlgorithm(m4, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    h4.set_stream(stream.cuda_stream)
+    h4.buildStage()
+    trees.append(("uniform L4", m4, h4, (-1.0, 1.0, -1.0, 1.0)))
+    rc = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -10.0, 10.0, 16, -10.0, 10.0))
+    mc = ef.Mesh().refineByFunction(lambda x, y: abs(-(np.sin(x) + np.sin(y))), 1.2, 0, 7, rc)
+    hc = ef.HPSAlgorithm(mc, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hc.set_stream(stream.cuda_stream)
+    hc.buildStage()
+    trees.append((f"adaptive max_level 7 ({hc.num_leaves} leaves)", mc, hc, (-10.0, 10.0, -10.0, 10.0)))
+    mesh7, h7 = main_tree
+    trees.append(("uniform L7", mesh7, h7, DOM))
+    T = len(trees)
+    P = 6
+    pool, outs = [], []
+    RING = 64
+    for t, (_, mesh, hps, box) in enumerate(trees):
+        X, Y = mesh.cell_centres()
+        bp = hps.boundary_points()
+        reqs = []
+        for i in range(P):
+            f, a, b, r = make_request_box(7000 + 31 * t + i, X, Y, bp, box)
+            reqs.append(tuple(torch.from_numpy(v).pin_memory().numpy() for v in (f, a, r)))
+        pool.append(reqs)
+        outs.append([torch.empty(X.size, dtype=torch.float64).pin_memory().numpy() for _ in range(RING)])
+    rng = np.random.default_rng(2024)
+    NREQ = 2000
+    plan = [(int(rng.integers(0, T)), int(rng.integers(0, P))) for _ in range(NREQ)]
+    budget = 64 << 30
+    srv = ef.Server([h for _, _, h, _ in trees], bmax=[32, 32, 32], lanes=2, hbm_budget_bytes=budget,
+                    sweeps=args.sweeps)
+    lanes = [srv.lanes(t) for t in range(T)]
+
+    def run_stream(rate):
+        """Submit the plan at Poisson times of the given rate (inf: all at once); ring slots are
+        reused once their previous request has completed."""
+        ids = [None] * NREQ
+        lat = [None] * NREQ
+        slot_owner = [[None] * RING for _ in range(T)]
+        counts = [0] * T
+        gaps = rng.exponential(1.0 / rate, NREQ) if np.isfinite(rate) else np.zeros(NREQ)
+        t0 = time.perf_counter()
+        due = t0
+        for k, (t, i) in enumerate(plan):
+            due += gaps[k]
+            while time.perf_counter() < due:
+                pass
+            s = counts[t] % RING
+            counts[t] += 1
+            prev = slot_owner[t][s]
+            if prev is not None and lat[prev] is None:
+                _, lat[prev] = srv.wait(ids[prev])
+            f, a, r = pool[t][i]
+            ids[k] = srv.submit(t, f, a, r, outs[t][s])
+            slot_owner[t][s] = k
+        for k in range(NREQ):
+            if lat[k] is None:
+                _, lat[k] = srv.wait(ids[k])
+        wall = time.perf_counter() - t0
+        return wall, np.array(lat)
+
+    # warm-up (graphs captured for the block sizes that occur), then saturation, then the stream
+    run_stream(float("inf"))
+    wall_sat, _ = run_stream(float("inf"))
+    sat = NREQ / wall_sat
+    st0 = srv.stats()
+    rate = 0.7 * sat
+    wall, lat = run_stream(rate)
+    st1 = srv.stats()
+    # correctness: the last result of every tree against its plain FP64 solution
+    errs = []
+    for t, (_, mesh, hps, _) in enumerate(trees):
+        k = max(j for j, (tt, _) in enumerate(plan) if tt == t)
+        i = plan[k][1]
+        s = (sum(1 for tt, _ in plan[:k] if tt == t)) % RING
+        f, a, r = pool[t][i]
+        hps.upwards_array(f)
+        hps.solve_arrays(a, np.zeros_like(a), r)
+        ref = hps.leaf_solution()
+        errs.append(float(np.abs(outs[t][s] - ref).max() / np.abs(ref).max()))
+    srv.close()
+    # plain FP64 serial GPU path: the same requests one at a time through the C ABI
+    u = [torch.empty(m.cell_centres()[0].size, dtype=torch.float64).pin_memory().numpy() for _, m, _, _ in trees]
+    for t, (_, _, hps, _) in enumerate(trees):  # warm
+        f, a, r = pool[t][0]
+        hps.upwards_array(f)
+        hps.solve_arrays(a, np.zeros_like(a), r)
+    zeros = [np.zeros_like(pool[t][0][1]) for t in range(T)]
+    plain_lat = []
+    t0 = time.perf_counter()
+    for t, i in plan:
+        hps = trees[t][2]
+        f, a, r = pool[t][i]
+        ts = time.perf_counter()
+        hps.upwards_array(f)
+        hps.solve_arrays(a, zeros[t], r)
+        check(lib.ef_hps_get_leaf_u(hps.handle, dptr(u[t])))
+        plain_lat.append(time.perf_counter() - ts)
+    plain_wall = time.perf_counter() - t0
+    return {
+        "workload": ("2000 requests, seeded Poisson arrivals at 0.7x the saturated rate, uniformly over 3 resident "
+                     "trees: " + "; ".join(f"{nm} ({m.cell_centres()[0].size} dofs)" for nm, m, _, _ in trees)),
+        "lanes_per_tree": lanes, "bmax": 32, "hbm_budget_bytes": budget, "sweeps": args.sweeps,
+        "arrival_rate_per_s": rate, "solves_per_s": NREQ / wall,
+        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
+        "saturated_solves_per_s": sat,
+        "blocks": st1["blocks"] - st0["blocks"], "max_block": st1["max_block"],
+        "plain_fp64_serial": {"solves_per_s": NREQ / plain_wall,
+                              "latency_ms": {"p50": float(np.percentile(plain_lat, 50) * 1e3),
+                                             "p99": float(np.percentile(plain_lat, 99) * 1e3)}},
+        "speedup_saturated_vs_plain_serial": sat / (NREQ / plain_wall),
+        "rel_err_vs_fp64_last_per_tree": errs,
+    }
+
+
 def many_rhs(ef, torch, stream, args):
     """512 right-hand sides on one factored uniform level-6 tree of 16x16 patches (1024^2 dofs):
     one mixed block of 512 against 512 plain FP64 solves one at a time."""
@@ -547,17 +685,17 @@ def many_rhs(ef, torch, stream, args):
     torch.cuda.synchronize()
     plain = nrhs / (e0.elapsed_time(e1) / 1e3)
     hps.mixed_init(nrhs)
-    U = hps.mixed_solve(F, A, R, 1)
+    U = hps.mixed_solve(F, A, R, args.sweeps)
     err = max(float(np.abs(U[i] - ref[i]).max() / np.abs(ref[i]).max()) for i in range(P))
-    hps.mixed_solve_async(nrhs, 1)
+    hps.mixed_solve_async(nrhs, args.sweeps)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(3):
-        hps.mixed_solve_async(nrhs, 1)
+        hps.mixed_solve_async(nrhs, args.sweeps)
     e1.record(stream)
     torch.cuda.synchronize()
     mixed = 3 * nrhs / (e0.elapsed_time(e1) / 1e3)
-    return {"workload": "uniform level 6, 16x16 patches (1024^2 dofs), 512 right-hand sides, 1 sweep",
+    return {"workload": f"uniform level 6, 16x16 patches (1024^2 dofs), 512 right-hand sides, {args.sweeps} sweeps",
             "mixed_block_solves_per_s": mixed, "plain_fp64_serial_solves_per_s": plain,
             "speedup": mixed / plain, "rel_err_vs_fp64": err, "mdof_per_s": mixed * mesh.cell_centres()[0].size / 1e6}
 
@@ -571,7 +709,9 @@ def main():
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--n", type=int, default=16)
     ap.add_argument("--batch", type=int, default=32, help="requests per block of the mixed form")
-    ap.add_argument("--sweeps", type=int, default=1, help="FP64 refinement sweeps of the mixed form")
+    ap.add_argument("--sweeps", type=int, default=2,
+                    help="FP64 refinement sweeps of the mixed form (2 keeps every L7 result within 1e-10 of "
+                         "the FP64 HPS; against a sparse direct solve of the 5-point system it is 2e-12)")
     ap.add_argument("--plain-steps", type=int, default=30, help="timed steps of the plain FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 512-RHS level-6 case")

@@ -66,6 +66,15 @@ SIGNATURES = {
     "ef_hps_mixed_solve_async": (C.c_int, [_vp, C.c_int, C.c_int]),
     "ef_hps_mixed_solve": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, _dp]),
     "ef_hps_mixed_residuals": (C.c_int, [_vp, C.c_int, _dp]),
+    "ef_server_create": (C.c_int, [C.POINTER(_vp), C.POINTER(C.c_int), C.c_int, C.c_int, C.c_longlong, C.c_int,
+                                   C.POINTER(_vp)]),
+    "ef_server_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "ef_server_submit": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
+    "ef_server_poll": (C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "ef_server_wait": (C.c_int, [_vp, C.c_longlong, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "ef_server_stats": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_longlong)]),
+    "ef_server_destroy": (C.c_int, [_vp]),
     "ef_kernel_launches": (C.c_int, [C.POINTER(C.c_longlong)]),
     "ef_hps_profile_enable": (C.c_int, [_vp, C.c_int]),
     "ef_hps_profile_count": (C.c_int, [_vp, C.POINTER(C.c_int)]),

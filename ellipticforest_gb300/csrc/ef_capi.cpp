@@ -16,9 +16,14 @@
 #include "ef_hps.hpp"
 #include "ef_kernels.cuh"
 #include "ef_mesh.hpp"
+#include "ef_server.hpp"
 
 struct ef_mesh {
     efgb::Mesh mesh;
+};
+
+struct ef_server {
+    std::unique_ptr<efgb::Server> srv;
 };
 
 struct ef_hps {
@@ -601,6 +606,79 @@ int ef_fv5_map_d2n(int n, double xl, double xu, double yl, double yu, const doub
     return guarded([&] {
         return run_single_patch_fp(n, xl, xu, yl, yu, alpha, beta, lambda, efgb::LEAF_MAPD2N, g, f, h,
                                    size_t(4) * n);
+    });
+}
+
+// ---- serving loop ----------------------------------------------------------------------------
+
+int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lanes_per_tree,
+                     long long hbm_budget_bytes, int sweeps, ef_server** out) {
+    if (!trees || !bmax || !out || ntrees < 1) return fail(EF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    std::vector<efgb::Server::TreeSpec> specs;
+    for (int t = 0; t < ntrees; ++t) {
+        if (!trees[t]) return fail(EF_ERR_INVALID, "null tree handle");
+        if (!trees[t]->hps->built()) return fail(EF_ERR_STATE, "server tree before build stage");
+        specs.push_back(efgb::Server::TreeSpec{trees[t]->hps.get(), bmax[t]});
+    }
+    return guarded([&] {
+        auto s = std::make_unique<ef_server>();
+        s->srv = std::make_unique<efgb::Server>(specs, lanes_per_tree, hbm_budget_bytes, sweeps);
+        *out = s.release();
+        return EF_OK;
+    });
+}
+
+int ef_server_info(ef_server* server, int tree, int* lanes, long long* device_bytes) {
+    if (!server) return fail(EF_ERR_INVALID, "null server");
+    return guarded([&] {
+        if (lanes) *lanes = server->srv->lanes(tree);
+        if (device_bytes) *device_bytes = server->srv->device_bytes();
+        return EF_OK;
+    });
+}
+
+int ef_server_submit(ef_server* server, int tree, const double* f, const double* a, const double* r, double* u,
+                     long long* id) {
+    if (!server || !id) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        *id = server->srv->submit(tree, f, a, r, u);
+        return EF_OK;
+    });
+}
+
+int ef_server_poll(ef_server* server, long long id, int* done, double* latency_s) {
+    if (!server || !done) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        *done = server->srv->poll(id, latency_s);
+        return EF_OK;
+    });
+}
+
+int ef_server_wait(ef_server* server, long long id, double timeout_s, int* done, double* latency_s) {
+    if (!server || !done) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        *done = server->srv->wait(id, timeout_s, latency_s);
+        return EF_OK;
+    });
+}
+
+int ef_server_stats(ef_server* server, long long* submitted, long long* completed, long long* blocks,
+                    long long* max_block) {
+    if (!server) return fail(EF_ERR_INVALID, "null server");
+    const efgb::Server::Stats st = server->srv->stats();
+    if (submitted) *submitted = st.submitted;
+    if (completed) *completed = st.completed;
+    if (blocks) *blocks = st.batches;
+    if (max_block) *max_block = st.max_batch;
+    return EF_OK;
+}
+
+int ef_server_destroy(ef_server* server) {
+    if (!server) return EF_OK;
+    return guarded([&] {
+        delete server;
+        return EF_OK;
     });
 }
 

@@ -92,7 +92,7 @@ cudaEvent_t Hps::ev_get() {
     return e;
 }
 
-void Hps::pb(const char* name) {
+void Hps::pb(const char* name, cudaStream_t st) {
     if (!prof_) return;
     int idx = -1;
     for (size_t i = 0; i < stats_.size(); ++i)
@@ -104,19 +104,19 @@ void Hps::pb(const char* name) {
     open_stat_ = idx;
     open_ev_ = ev_get();
     open_launch0_ = g_kernel_launches.load();
-    check(cudaEventRecord(open_ev_, st_), "cudaEventRecord");
+    check(cudaEventRecord(open_ev_, st), "cudaEventRecord");
 }
 
-void Hps::pe(double bytes, double flops) {
+void Hps::pe(double bytes, double flops, cudaStream_t st) {
     if (!prof_ || open_stat_ < 0) return;
     cudaEvent_t b = ev_get();
-    check(cudaEventRecord(b, st_), "cudaEventRecord");
+    check(cudaEventRecord(b, st), "cudaEventRecord");
     marks_.push_back(Mark{open_stat_, open_ev_, b, g_kernel_launches.load() - open_launch0_, bytes, flops});
     open_stat_ = -1;
 }
 
 const std::vector<Hps::ProfStat>& Hps::profile_read() {
-    check(cudaStreamSynchronize(st_), "profile sync");
+    check(cudaDeviceSynchronize(), "profile sync");  // sections may sit on several streams
     for (auto& m : marks_) {
         float ms = 0;
         check(cudaEventElapsedTime(&ms, m.a, m.b), "cudaEventElapsedTime");

@@ -297,8 +297,10 @@ private:
     cudaEvent_t open_ev_ = nullptr;
     long long open_launch0_ = 0;
     cudaEvent_t ev_get();
-    void pb(const char* name);                 // begin section
-    void pe(double bytes, double flops);       // end section
+    void pb(const char* name) { pb(name, st_); }                 // begin section
+    void pe(double bytes, double flops) { pe(bytes, flops, st_); }  // end section
+    void pb(const char* name, cudaStream_t st);
+    void pe(double bytes, double flops, cudaStream_t st);
 };
 
 // Mixed-precision many-RHS solver on a built FP64 Hps (FISHPACK90 leaves, Dirichlet root data):
@@ -306,12 +308,17 @@ private:
 // flux mismatches) and FP32 correction passes, see ef_mixed.cu.
 class MixedSolver {
 public:
-    MixedSolver(Hps& hps, int bmax);
+    // share: another solver of the same tree whose FP32 operators (and TMA descriptors) this one
+    // reuses, so that several lanes of one tree hold the operators once
+    MixedSolver(Hps& hps, int bmax, const MixedSolver* share = nullptr);
     ~MixedSolver();
     MixedSolver(const MixedSolver&) = delete;
     MixedSolver& operator=(const MixedSolver&) = delete;
 
     int bmax() const { return bmax_; }
+    // stream of this solver's launches (default: the tree's stream at construction)
+    void set_stream(cudaStream_t st) { st_ = st; }
+    cudaStream_t stream() const { return st_; }
     // Resident inputs: f [B][L][n*n], a and r [B][4M] (b == 0 assumed); output u [B][L][n*n].
     double* f() const { return f_; }
     double* a() const { return a_; }
@@ -355,6 +362,8 @@ private:
 
     Hps& H_;
     int bmax_;
+    cudaStream_t st_;
+    const MixedSolver* share_;
     char* arena_ = nullptr;
     size_t bytes_ = 0;
     std::vector<MNode> mn_;

@@ -19,6 +19,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "ef_kernels.cuh"
 
@@ -823,16 +824,16 @@ inline unsigned mx_grid(long long tot) {
 
 template <int BN, int KIND>
 int mx_gemm_slots(int rt) {
-    static int slots[65] = {0};
-    if (!slots[rt]) {
+    static std::atomic<int> slots[65];
+    if (!slots[rt].load()) {
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int threads = (rt / 4) * (BN / 4);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_gemm<BN, KIND>, threads, mx_gemm_smem(rt, BN));
-        slots[rt] = (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+        slots[rt].store((sms > 0 ? sms : 1) * (per > 0 ? per : 1));
     }
-    return slots[rt];
+    return slots[rt].load();
 }
 
 template <int BN, int KIND>

@@ -57,7 +57,9 @@ CUtensorMap make_map(float* base, long long rows, int cols, int box_rows) {
 
 }  // namespace
 
-MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
+MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
+    : H_(hps), bmax_(bmax), st_(hps.stream()), share_(share) {
+    if (share && &share->H_ != &hps) throw std::invalid_argument("mixed solver: operators shared across trees");
     if (!hps.built()) throw std::invalid_argument("mixed solver: build the FP64 tree first");
     if (hps.solver_type() != SOLVER_FISHPACK90)
         throw std::invalid_argument("mixed solver: FISHPACK90 (constant coefficient) leaves only");
@@ -130,11 +132,12 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
             groups_[gi].cnt = int(g.nodes.size());
             groups_[gi].d_items = cv.get<MixItem>(g.nodes.size());
             groups_[gi].d_conv = cv.get<MixConv>(g.nodes.size());
-            // FP32 operators of the group back to back: one row-major matrix per kind
+            // FP32 operators of the group back to back: one row-major matrix per kind (or the
+            // operators of the lane this one shares them with)
             const size_t s = g.s, cnt = g.nodes.size();
-            float* S = cv.get<float>(cnt * 32 * s * s);
-            float* Xi = cv.get<float>(cnt * 16 * s * s);
-            float* H32 = cv.get<float>(cnt * 16 * s * s);
+            float* S = share ? share->groups_[gi].S32 : cv.get<float>(cnt * 32 * s * s);
+            float* Xi = share ? share->groups_[gi].Xi32 : cv.get<float>(cnt * 16 * s * s);
+            float* H32 = share ? share->groups_[gi].H32 : cv.get<float>(cnt * 16 * s * s);
             groups_[gi].S32 = S;
             groups_[gi].Xi32 = Xi;
             groups_[gi].H32 = H32;
@@ -175,7 +178,7 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
     MxCarver real;
     real.base = arena_;
     layout(real);
-    cudaStream_t st = hps.stream();
+    cudaStream_t st = st_;
     ck(cudaMemsetAsync(arena_, 0, bytes_, st), "memset(mixed arena)");
 
     // leaf tables in FP32
@@ -261,7 +264,14 @@ MixedSolver::MixedSolver(Hps& hps, int bmax) : H_(hps), bmax_(bmax) {
     fill_steps(hsteps_, hps.step_nodes_t_, hps.step_index_t_, true);
     fill_steps(gsteps_, hps.step_nodes_g_, hps.step_index_g_, false);
     // FP32 operator copies and the TMA descriptors that stream them
-    for (auto& g : groups_) {
+    for (size_t gi = 0; gi < groups_.size(); ++gi) {
+        MGroup& g = groups_[gi];
+        if (share) {
+            g.tmS = share->groups_[gi].tmS;
+            g.tmXi = share->groups_[gi].tmXi;
+            g.tmH = share->groups_[gi].tmH;
+            continue;
+        }
         mx_convert(st, g.d_conv, g.cnt, g.s);
         const long long cnt = g.cnt, s = g.s;
         if (mx_tile_rows(0, g.s) == 0 || mx_tile_rows(1, g.s) == 0)
@@ -281,85 +291,85 @@ MixedSolver::~MixedSolver() {
 
 void MixedSolver::residual(int B, double* rmax, bool zero_state) {
     Hps& h = H_;
-    cudaStream_t st = h.stream();
+    cudaStream_t st = st_;
     const int maxL = h.mesh().max_level;
     const double L = h.num_leaves(), nn = double(h.leaf_n()) * h.leaf_n();
     // exact Dirichlet data of every node from the root data and the interface state
-    h.pb("mx_interface");
+    h.pb("mx_interface", st);
     for (int lvl = 0; lvl < maxL; ++lvl) {
         for (auto& s : gsteps_)
             if (s.level == lvl) mx_uncoarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
         for (auto& g : groups_)
             if (g.level == lvl) mx_scatter64(st, g.d_items, g.cnt, g.s, B);
     }
-    h.pe(0, 0);
-    h.pb("mx_leaf_residual");
+    h.pe(0, 0, st);
+    h.pb("mx_leaf_residual", st);
     mx_leaf_residual(st, d_coef_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
                      rleaf_, rmax);
-    h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0);
-    h.pb("mx_interface");
+    h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
+    h.pb("mx_interface", st);
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         for (auto& s : hsteps_)
             if (s.level == lvl + 1) mx_coarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
         for (auto& g : groups_)
             if (g.level == lvl) mx_flux_up(st, g.d_items, g.cnt, g.s, B);
     }
-    h.pe(0, 0);
+    h.pe(0, 0, st);
 }
 
 void MixedSolver::pass(int B, bool first) {
     Hps& h = H_;
-    cudaStream_t st = h.stream();
+    cudaStream_t st = st_;
     const int maxL = h.mesh().max_level;
     const int L = h.num_leaves(), n = h.leaf_n();
     const double items = double(L) * B, nn = double(n) * n;
-    h.pb("mx_leaf_neumann");
+    h.pb("mx_leaf_neumann", st);
     mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr, 0);
-    h.pe(items * (nn * 4 + 4 * n * 4), items * 2.0 * (3 * nn * n + 4 * nn));
+    h.pe(items * (nn * 4 + 4 * n * 4), items * 2.0 * (3 * nn * n + 4 * nn), st);
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
-        h.pb("mx_interface");
+        h.pb("mx_interface", st);
         for (auto& s : hsteps_)
             if (s.level == lvl + 1) mx_coarsen(st, false, s.in32, s.out32, s.count, s.nf, B);
         for (auto& g : groups_)
             if (g.level == lvl) mx_hdiff(st, g.d_items, g.cnt, g.s, B);
-        h.pe(0, 0);
+        h.pe(0, 0, st);
         for (auto& g : groups_) {
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
-            h.pb("mx_gemm_w");
+            h.pb("mx_gemm_w", st);
             mx_gemm(st, 0, g.tmXi, g.d_items, g.cnt, g.s, B, d_err_);
-            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B);
-            h.pb("mx_gemm_h");
+            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
+            h.pb("mx_gemm_h", st);
             mx_gemm(st, 1, g.tmH, g.d_items, g.cnt, g.s, B, d_err_);
-            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B);
+            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
         }
     }
     // homogeneous root data for the correction
     ck(cudaMemsetAsync(mn_[0].g32, 0, sizeof(float) * 4 * size_t(h.root_M()) * B, st), "root g32");
     for (int lvl = 0; lvl < maxL; ++lvl) {
-        h.pb("mx_interface");
+        h.pb("mx_interface", st);
         for (auto& s : gsteps_)
             if (s.level == lvl) mx_uncoarsen(st, false, s.in32, s.out32, s.count, s.nf, B);
-        h.pe(0, 0);
+        h.pe(0, 0, st);
         for (auto& g : groups_) {
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
-            h.pb("mx_gemm_down");
+            h.pb("mx_gemm_down", st);
             mx_gemm(st, 2, g.tmS, g.d_items, g.cnt, g.s, B, d_err_);
-            h.pe(c * 32 * s2 * 4, c * 2.0 * 32 * s2 * B);
+            h.pe(c * 32 * s2 * 4, c * 2.0 * 32 * s2 * B, st);
         }
     }
-    h.pb("mx_leaf_solve");
+    h.pb("mx_leaf_solve", st);
     mx_leaf32(st, LEAF_SOLVE, d_types32_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
-    h.pe(items * nn * (4 + 16), items * 2.0 * 4 * nn * n);
+    h.pe(items * nn * (4 + 16), items * 2.0 * 4 * nn * n, st);
 }
 
 void MixedSolver::solve(int B, int sweeps) {
     if (B < 1 || B > bmax_) throw std::invalid_argument("mixed solver: batch size out of range");
     if (sweeps < 0 || sweeps + 1 > kMaxPasses) throw std::invalid_argument("mixed solver: too many sweeps");
     Hps& h = H_;
-    graphs_.run(h.st_, (long long)B * 64 + sweeps, h.graphs() && !h.prof_, [&] {
-        cudaStream_t s = h.stream();
+    graphs_.run(st_, (long long)B * 64 + sweeps, h.graphs() && !h.prof_, [&] {
+        cudaStream_t s = st_;
         ck(cudaMemsetAsync(uG_begin_, 0, uG_bytes_, s), "clear interface state");
         ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, s), "clear residuals");
         mx_root(s, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
@@ -372,9 +382,9 @@ void MixedSolver::solve(int B, int sweeps) {
 
 int MixedSolver::take_error() {
     int v = 0;
-    ck(cudaStreamSynchronize(H_.stream()), "mixed solver");
-    ck(cudaMemcpy(&v, d_err_, sizeof(int), cudaMemcpyDeviceToHost), "mixed error flag");
-    if (v) ck(cudaMemset(d_err_, 0, sizeof(int)), "mixed error flag");
+    ck(cudaMemcpyAsync(&v, d_err_, sizeof(int), cudaMemcpyDeviceToHost, st_), "mixed error flag");
+    ck(cudaStreamSynchronize(st_), "mixed solver");
+    if (v) ck(cudaMemsetAsync(d_err_, 0, sizeof(int), st_), "mixed error flag");
     return v;
 }
 

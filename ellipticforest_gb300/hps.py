@@ -502,3 +502,86 @@ class HPSAlgorithm:
 
     def synchronize(self):
         check(_lib.load().ef_hps_synchronize(self._h))
+
+
+class Server:
+    """Serving loop over several built trees (no counterpart in the reference).
+
+    Requests (tree index, load f, root data a u = r) are answered by the batched mixed-precision
+    solver; the scheduler thread of the library forms a block from every request of a tree that has
+    arrived whenever one of the tree's lanes is free, and overlaps blocks of different lanes and trees
+    on the GPU.  Lanes beyond the first per tree are created only while the device memory of all
+    lanes fits hbm_budget_bytes (0: no limit)."""
+
+    def __init__(self, trees, bmax, lanes: int = 2, hbm_budget_bytes: int = 0, sweeps: int = 1):
+        trees = list(trees)
+        bmax = [int(b) for b in (bmax if hasattr(bmax, "__len__") else [bmax] * len(trees))]
+        if len(bmax) != len(trees):
+            raise ValueError("Server: one bmax per tree")
+        self._trees = trees
+        lib = _lib.load()
+        arr = (C.c_void_p * len(trees))(*[t.handle for t in trees])
+        bm = (C.c_int * len(trees))(*bmax)
+        h = C.c_void_p()
+        check(lib.ef_server_create(arr, bm, len(trees), int(lanes), int(hbm_budget_bytes), int(sweeps), C.byref(h)))
+        self._h = h
+        self._live = {}  # id -> arrays kept alive until completion
+
+    def lanes(self, tree: int) -> int:
+        n = C.c_int()
+        check(_lib.load().ef_server_info(self._h, int(tree), C.byref(n), None))
+        return n.value
+
+    def device_bytes(self) -> int:
+        b = C.c_longlong()
+        check(_lib.load().ef_server_info(self._h, 0, None, C.byref(b)))
+        return b.value
+
+    def submit(self, tree: int, f, a, r, out=None) -> int:
+        """Queue one request; returns its id.  `out` (optional, float64 [leaves*n*n]) receives u;
+        page-locked arrays keep the copies asynchronous."""
+        t = self._trees[tree]
+        cells = t.num_leaves * t.n * t.n
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        if out is None:
+            out = np.empty(cells)
+        if f.size != cells or a.size != 4 * t.M or r.size != 4 * t.M or out.size != cells or out.dtype != np.float64:
+            raise ValueError("Server.submit: bad shapes")
+        rid = C.c_longlong()
+        check(_lib.load().ef_server_submit(self._h, int(tree), dptr(f), dptr(a), dptr(r), dptr(out), C.byref(rid)))
+        self._live[rid.value] = (f, a, r, out)
+        return rid.value
+
+    def poll(self, rid: int):
+        """(done, latency_s)"""
+        d, lat = C.c_int(), C.c_double()
+        check(_lib.load().ef_server_poll(self._h, int(rid), C.byref(d), C.byref(lat)))
+        return bool(d.value), lat.value
+
+    def wait(self, rid: int, timeout: float = 120.0):
+        """(u, latency_s) of request rid; raises TimeoutError after `timeout` seconds."""
+        d, lat = C.c_int(), C.c_double()
+        check(_lib.load().ef_server_wait(self._h, int(rid), float(timeout), C.byref(d), C.byref(lat)))
+        if not d.value:
+            raise TimeoutError(f"request {rid} not done after {timeout} s")
+        arrays = self._live.pop(rid)
+        return arrays[3], lat.value
+
+    def stats(self) -> dict:
+        v = [C.c_longlong() for _ in range(4)]
+        check(_lib.load().ef_server_stats(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("submitted", "completed", "blocks", "max_block"), [x.value for x in v]))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(_lib.load().ef_server_destroy(self._h))
+            self._h = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

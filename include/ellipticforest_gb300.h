@@ -185,6 +185,36 @@ int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, double x_upper, 
                         double y_upper, double lambda, const double* g_dev, const double* f_dev,
                         double* u_dev, void* cuda_stream);
 
+/* ---- Serving loop over several resident trees ------------------------------------------------ */
+
+/* No counterpart in the reference (its drivers solve one right-hand side per call).  A server keeps
+ * several built trees resident and answers requests (tree index, load f, root data a u = r) with
+ * the batched mixed-precision solver (results refined to the FP64 HPS solution by `sweeps` FP64
+ * sweeps).  Every tree gets up to lanes_per_tree lanes -- a block solver of up to bmax[t] requests
+ * with its own CUDA stream; lanes beyond the first of each tree are only created while the device
+ * memory of all lanes stays within hbm_budget_bytes (<= 0: no limit).  A scheduler thread forms a
+ * block from every request of a tree that has arrived whenever one of its lanes is free
+ * (continuous batching) and overlaps the blocks of different lanes and trees on the GPU.  A
+ * request's result does not depend on the other requests of its block.  The trees must outlive
+ * the server and must not be rebuilt while it exists. */
+typedef struct ef_server ef_server;
+int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lanes_per_tree,
+                     long long hbm_budget_bytes, int sweeps, ef_server** out);
+/* lanes created for tree t (after the budget) and device bytes held by all lanes */
+int ef_server_info(ef_server* server, int tree, int* lanes, long long* device_bytes);
+/* f (leaves*n*n), a and r (4M, WESN root face centres) and u (leaves*n*n) are host arrays that
+ * must stay valid until the request completes; page-locked memory keeps the copies asynchronous. */
+int ef_server_submit(ef_server* server, int tree, const double* f, const double* a, const double* r,
+                     double* u, long long* id);
+/* done = 1 and latency_s = seconds from submit to the result in u, or done = 0 (pending / time-out).
+ * A completed id is reported once. */
+int ef_server_poll(ef_server* server, long long id, int* done, double* latency_s);
+int ef_server_wait(ef_server* server, long long id, double timeout_s, int* done, double* latency_s);
+int ef_server_stats(ef_server* server, long long* submitted, long long* completed, long long* blocks,
+                    long long* max_block);
+/* waits for the requests already submitted, then frees the lanes */
+int ef_server_destroy(ef_server* server);
+
 #ifdef __cplusplus
 }
 #endif
