@@ -277,13 +277,21 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
         const MixItem& it = items[t.item];
         if (KIND == MX_DOWN && blockIdx.y == 0) {
             // exterior points of the parent go to the children unchanged; each tile copies its share
-            const int tot = 8 * s * B, per = (tot + tpi - 1) / tpi;
-            const int e0 = t.tl * per, e1 = min(tot, e0 + per);
-            for (int e = e0 + tid; e < e1; e += nt) {
-                const int p = e / B, bb = e - (e / B) * B;
+            // of the 8s exterior rows, one warp per row (float4 along the batch when B % 4 == 0)
+            const int rows = 8 * s, per = (rows + tpi - 1) / tpi;
+            const int p0 = t.tl * per, p1 = min(rows, p0 + per);
+            const int warp = tid >> 5, lane = tid & 31, nw = (nt + 31) >> 5;
+            for (int p = p0 + warp; p < p1; p += nw) {
                 int c, q;
                 mx_ext_map(p, s, c, q);
-                it.gc[c][(long long)q * B + bb] = it.gf[e];
+                const float* src = it.gf + (long long)p * B;
+                float* dst = it.gc[c] + (long long)q * B;
+                if (vecx) {
+                    for (int b4 = lane; b4 < (B >> 2); b4 += 32)
+                        reinterpret_cast<float4*>(dst)[b4] = reinterpret_cast<const float4*>(src)[b4];
+                } else {
+                    for (int bb = lane; bb < B; bb += 32) dst[bb] = src[bb];
+                }
             }
         }
         const int bq = b0 + 4 * tx;
@@ -720,9 +728,10 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual(const MixCoef* __restr
                 const double right = j0 + 4 < n ? uu[e + 4] : 0.0;
                 const double ym[4] = {left, c[0], c[1], c[2]};
                 const double yp[4] = {c[1], c[2], c[3], right};
+                // r = ((f - cc u_C) - cx (u_W + u_E)) - cy (u_S + u_N): 5 FP64 operations
 #pragma unroll
                 for (int t = 0; t < 4; ++t)
-                    rr[t] = d2f_bits(fv[t] - fma(cc, c[t], fma(cy, ym[t] + yp[t], cx * (up[t] + dn[t]))));
+                    rr[t] = d2f_bits(fma(-cy, ym[t] + yp[t], fma(-cx, up[t] + dn[t], fma(-cc, c[t], fv[t]))));
             }
             const bool edge_row = i == 0 || i == n - 1;
 #pragma unroll
@@ -746,14 +755,26 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual(const MixCoef* __restr
             else if (k < 2 * n) { i = n - 1; j = k - n; }
             else { const int m = k - 2 * n; i = 1 + (m >> 1); j = (m & 1) ? n - 1 : 0; }
             const int e = i * n + j;
-            const double uc = zero_state ? 0.0 : uu[e];
-            const double xm = i > 0 ? (zero_state ? 0.0 : uu[e - n]) : fma(2.0, gW[(long long)j * B], -uc);
-            const double xp = i < n - 1 ? (zero_state ? 0.0 : uu[e + n]) : fma(2.0, gE[(long long)j * B], -uc);
-            const double ym = j > 0 ? (zero_state ? 0.0 : uu[e - 1]) : fma(2.0, gS[(long long)i * B], -uc);
-            const double yp = j < n - 1 ? (zero_state ? 0.0 : uu[e + 1]) : fma(2.0, gN[(long long)i * B], -uc);
-            const float r = d2f_bits(ff[e] - fma(cc, uc, fma(cy, ym + yp, cx * (xm + xp))));
-            q[base + e] = r;
-            mx = fmaxf(mx, fabsf(r));
+            double r;
+            if (zero_state) {
+                // u = 0: only the ghost terms 2g of the missing neighbours remain
+                double gx = 0.0, gy = 0.0;
+                if (i == 0) gx = gW[(long long)j * B];
+                else if (i == n - 1) gx = gE[(long long)j * B];
+                if (j == 0) gy = gS[(long long)i * B];
+                else if (j == n - 1) gy = gN[(long long)i * B];
+                r = fma(-2.0 * cy, gy, fma(-2.0 * cx, gx, ff[e]));
+            } else {
+                const double uc = uu[e];
+                const double xm = i > 0 ? uu[e - n] : fma(2.0, gW[(long long)j * B], -uc);
+                const double xp = i < n - 1 ? uu[e + n] : fma(2.0, gE[(long long)j * B], -uc);
+                const double ym = j > 0 ? uu[e - 1] : fma(2.0, gS[(long long)i * B], -uc);
+                const double yp = j < n - 1 ? uu[e + 1] : fma(2.0, gN[(long long)i * B], -uc);
+                r = fma(-cy, ym + yp, fma(-cx, xm + xp, fma(-cc, uc, ff[e])));
+            }
+            const float rf = d2f_bits(r);
+            q[base + e] = rf;
+            mx = fmaxf(mx, fabsf(rf));
         }
         atomicMax(&smax[slot], __float_as_uint(mx));
         for (int r = lt; r < 4 * n; r += tpe) {
@@ -764,9 +785,9 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual(const MixCoef* __restr
             else if (side == 2) cell = pos * n;
             else cell = pos * n + n - 1;
             const double gv = lf.g64[(long long)r * B + b];
-            const double ue = zero_state ? 0.0 : uu[cell];
-            const double dtn = side < 2 ? cf.dtn_x : cf.dtn_y;
-            lf.h64[(long long)r * B + b] = (side == 0 || side == 2) ? dtn * (ue - gv) : (-dtn) * (ue - gv);
+            const double dtn = (side == 0 || side == 2) ? (side < 2 ? cf.dtn_x : cf.dtn_y)
+                                                        : -(side < 2 ? cf.dtn_x : cf.dtn_y);
+            lf.h64[(long long)r * B + b] = zero_state ? -dtn * gv : dtn * (uu[cell] - gv);
         }
     }
     __syncthreads();
