@@ -15,6 +15,8 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
   plain_fp64 -- the plain FP64 form one request at a time (device-resident solves/s, p50/p99, and
             e2e through the reference-facing upwards/solve/get_leaf_u calls)
   many_rhs_L6 -- 512 right-hand sides on a uniform level-6 tree: one mixed block vs 512 plain solves
+  variable_coefficient_L5 -- config 3 (FivePointStencil leaves, variable beta): build, plain FP64
+            solves/s, discretisation error, and the mixed block form against the FP64 HPS
   serving -- 2000 Poisson-arrival requests over three resident trees (uniform L4, adaptive max level
             7, uniform L7) through the serving loop (continuous same-tree batching, p50/p99 latency)
             against the same requests one at a time through the plain FP64 path
@@ -24,6 +26,7 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -451,6 +454,7 @@ def run_gb300(args):
     if not args.no_extras:
         extras["many_rhs_L6"] = many_rhs(ef, torch, stream, args)
         extras["serving"] = serving(ef, torch, stream, (mesh, hps), args)
+        extras["variable_coefficient_L5"] = variable_coefficient(ef, torch, stream, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -648,6 +652,89 @@ def serving(ef, torch, stream, main_tree, args):
     }
 
 
+def variable_coefficient(ef, torch, stream, args):
+    """Config 3: alpha div(beta grad u) + lambda u = f on [-1,1]^2 with alpha = 1,
+    beta = 1 + 0.5 sin(pi x) cos(pi y), lambda = -1, uniform level 5 of 32x32 FivePointStencil leaves
+    (1024^2 dofs), manufactured u = sin(2 pi x) sin(pi y): build, plain FP64 solves and the mixed
+    block form against the FP64 HPS per result."""
+    PI = np.pi
+    beta = lambda x, y: 1.0 + 0.5 * np.sin(PI * x) * np.cos(PI * y)
+    solver = ef.FiniteVolumeSolver(alpha_function=lambda x, y: 1.0 + 0.0 * x, beta_function=beta,
+                                   lambda_function=lambda x, y: -1.0 + 0.0 * x, solver_type=ef.FivePointStencil)
+    uex = lambda x, y: np.sin(2 * PI * x) * np.sin(PI * y)
+
+    def fex(x, y):
+        bx = 0.5 * PI * np.cos(PI * x) * np.cos(PI * y)
+        by = -0.5 * PI * np.sin(PI * x) * np.sin(PI * y)
+        ux = 2 * PI * np.cos(2 * PI * x) * np.sin(PI * y)
+        uy = PI * np.sin(2 * PI * x) * np.cos(PI * y)
+        return beta(x, y) * (-5 * PI ** 2) * uex(x, y) + bx * ux + by * uy - uex(x, y)
+
+    level, n = 5, 32
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, -1.0, 1.0, n, -1.0, 1.0))
+    mesh = ef.Mesh().uniform(level, root)
+    hps = ef.HPSAlgorithm(mesh, solver)
+    hps.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hps.buildStage()
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    X, Y = mesh.cell_centres()
+    bp = hps.boundary_points()
+    f = fex(X, Y)
+    r = np.concatenate([uex(x, y) for x, y in bp])
+    a = np.ones_like(r)
+    hps.upwards_array(f)
+    hps.solve_arrays(a, np.zeros_like(a), r)
+    u64 = hps.leaf_solution()
+    disc_err = float(np.abs(u64 - uex(X, Y)).max())
+    dev = tuple(torch.from_numpy(v).cuda() for v in (f, a, np.zeros_like(a), r))
+    for _ in range(3):
+        hps.load_device_async(*[t.data_ptr() for t in dev])
+        hps.solve_device_async(True)
+    torch.cuda.synchronize()
+    K = 10
+    e0, e1 = _events(torch, 2)
+    e0.record(stream)
+    for _ in range(K):
+        hps.load_device_async(*[t.data_ptr() for t in dev])
+        hps.solve_device_async(True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain = K / (e0.elapsed_time(e1) / 1e3)
+    # mixed block: the manufactured request plus seeded bump/Fourier requests
+    B = 16
+    reqs = [(f, a, r)]
+    for i in range(3):
+        fq, aq, _, rq = make_request(9000 + i, X, Y, bp)
+        reqs.append((fq, aq, rq))
+    F = np.stack([reqs[i % 4][0] for i in range(B)])
+    A = np.stack([reqs[i % 4][1] for i in range(B)])
+    R = np.stack([reqs[i % 4][2] for i in range(B)])
+    refs = []
+    for q in reqs:
+        hps.upwards_array(q[0])
+        hps.solve_arrays(q[1], np.zeros_like(q[1]), q[2])
+        refs.append(hps.leaf_solution())
+    hps.mixed_init(B)
+    U = hps.mixed_solve(F, A, R, args.sweeps)
+    errs = [float(np.abs(U[i] - refs[i]).max() / np.abs(refs[i]).max()) for i in range(4)]
+    hps.mixed_solve_async(B, args.sweeps)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(3):
+        hps.mixed_solve_async(B, args.sweeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mixed = 3 * B / (e0.elapsed_time(e1) / 1e3)
+    return {"workload": "config 3: variable beta, lambda = -1, uniform level 5 of 32x32 FivePointStencil leaves "
+                        "(1024^2 dofs), manufactured u = sin(2 pi x) sin(pi y)",
+            "build_s": build_s, "plain_fp64_solves_per_s": plain, "max_err_vs_manufactured": disc_err,
+            "mixed_block": {"batch": B, "sweeps": args.sweeps, "solves_per_s": mixed,
+                            "speedup_vs_plain": mixed / plain, "rel_err_vs_fp64_per_request": errs}}
+
+
 def many_rhs(ef, torch, stream, args):
     """512 right-hand sides on one factored uniform level-6 tree of 16x16 patches (1024^2 dofs):
     one mixed block of 512 against 512 plain FP64 solves one at a time."""
@@ -718,6 +805,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    gc.disable()  # no collector pauses inside the timed loops (nothing here builds reference cycles)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -146,6 +146,7 @@ void GraphCache::run(cudaStream_t& stream, long long key, bool enabled, F&& body
         e->launches = g_kernel_launches.load() - l0;
         g_kernel_launches -= e->launches;
         if (ok) ok = cudaGraphInstantiate(&e->exec, g, 0) == cudaSuccess;
+        if (ok) ok = cudaGraphUpload(e->exec, stream) == cudaSuccess;  // first launch pays no upload
         if (g) cudaGraphDestroy(g);
         if (!ok) {
             e->failed = true;
@@ -376,6 +377,10 @@ private:
     int* d_err_ = nullptr;
     float* rleaf_ = nullptr;
     MixCoef* d_coef_ = nullptr;
+    MixFp* d_fps_ = nullptr;  // FivePointStencil leaves only
+    float* fp_band32_ = nullptr;
+    float* fp_bcoef32_ = nullptr;
+    double* fp_coef64_ = nullptr;
     GraphCache graphs_;
     char* uG_begin_ = nullptr;
     size_t uG_bytes_ = 0;

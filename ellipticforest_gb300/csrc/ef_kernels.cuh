@@ -183,6 +183,23 @@ struct MixCoef {
 void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leaves, int L, int B, int n,
                       int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g);
+// rmax[b] = max over leaves of rleaf[b][leaf]
+void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax);
+
+// Variable-coefficient (FivePointStencil) leaves of the mixed form (ef_mixed_fp.cu), indexed by leaf.
+struct MixFp {
+    float* band;    // n*n rows x (2n+1): FP32 copy of the FP64 band LU, U's diagonal stored inverted
+    float* bcoef;   // 4n boundary coupling coefficients (WESN)
+    double* coef;   // 5 x n*n FP64 stencil coefficients cW, cE, cS, cN, cC
+    double dtn_x, dtn_y;
+};
+void mx_fp_convert(cudaStream_t st, const FpLeaf* src, const MixFp* dst, int L);
+size_t mx_fp_leaf_smem(int n);
+// batched FP32 band solves, one CTA per (leaf, 32 requests); modes LEAF_NEUMANN / LEAF_SOLVE
+void mx_fp_leaf32(cudaStream_t st, int mode, const MixFp* fps, const MixLeaf* leaves, int L, int B, int n,
+                  const float* q, double* u64, int accumulate);
+void mx_fp_residual(cudaStream_t st, const MixFp* fps, const MixLeaf* leaves, int L, int B, int n, int zero_state,
+                    const double* f, const double* u64, float* q, float* rleaf, double* rmax);
 
 // ------------------------------------------------------------------------------------------------
 // Merge / upward / downward kernels

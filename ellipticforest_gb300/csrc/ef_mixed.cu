@@ -1000,10 +1000,12 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leav
     else
         k_mx_leaf_residual<0><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
     ++g_kernel_launches;
-    if (rmax) {
-        k_mx_rmax<<<B, 256, 0, st>>>(rleaf, L, rmax);
-        ++g_kernel_launches;
-    }
+    if (rmax) mx_rmax(st, rleaf, L, B, rmax);
+}
+
+void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax) {
+    k_mx_rmax<<<B, 256, 0, st>>>(rleaf, L, rmax);
+    ++g_kernel_launches;
 }
 
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g) {

@@ -61,12 +61,13 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     : H_(hps), bmax_(bmax), st_(hps.stream()), share_(share) {
     if (share && &share->H_ != &hps) throw std::invalid_argument("mixed solver: operators shared across trees");
     if (!hps.built()) throw std::invalid_argument("mixed solver: build the FP64 tree first");
-    if (hps.solver_type() != SOLVER_FISHPACK90)
-        throw std::invalid_argument("mixed solver: FISHPACK90 (constant coefficient) leaves only");
+    const bool fp = hps.solver_type() == SOLVER_FIVE_POINT;
     if (bmax < 1 || bmax > 1024) throw std::invalid_argument("mixed solver: bmax must be in [1, 1024]");
     const int N = hps.num_nodes(), L = hps.num_leaves(), n = hps.leaf_n();
     if ((long long)L * bmax >= (1LL << 31) || 12LL * hps.node(0).nx * bmax >= (1LL << 31))
         throw std::invalid_argument("mixed solver: leaves x bmax too large for 32-bit item indices");
+    if (fp && n > 32)
+        throw std::invalid_argument("mixed solver: FivePointStencil leaves of at most 32 x 32 cells");
     if (n % 4 != 0 || n > 64)
         throw std::invalid_argument("mixed solver: the leaf size must be a multiple of 4 and at most 64");
     const size_t nn = size_t(n) * n, B = size_t(bmax);
@@ -124,6 +125,13 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         d_coef_ = cv.get<MixCoef>(hps.types_.size());
         d_types32_ = cv.get<LeafType32>(hps.types_.size());
         d_leaves_ = cv.get<MixLeaf>(L);
+        if (fp) {
+            // FP32 band factors and FP64 stencil tables, shared by the lanes of one tree
+            d_fps_ = cv.get<MixFp>(L);
+            fp_band32_ = share ? share->fp_band32_ : cv.get<float>(size_t(L) * nn * (2 * n + 1));
+            fp_bcoef32_ = share ? share->fp_bcoef32_ : cv.get<float>(size_t(L) * 4 * n);
+            fp_coef64_ = share ? share->fp_coef64_ : cv.get<double>(size_t(L) * 5 * nn);
+        }
         groups_.assign(hps.groups_.size(), MGroup());
         for (size_t gi = 0; gi < hps.groups_.size(); ++gi) {
             const Group& g = hps.groups_[gi];
@@ -181,9 +189,17 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     cudaStream_t st = st_;
     ck(cudaMemsetAsync(arena_, 0, bytes_, st), "memset(mixed arena)");
 
-    // leaf tables in FP32
-    std::vector<LeafType32> t32(hps.types_.size());
-    {
+    if (fp) {
+        std::vector<MixFp> fl(L);
+        for (int k = 0; k < L; ++k)
+            fl[k] = MixFp{fp_band32_ + size_t(k) * nn * (2 * n + 1), fp_bcoef32_ + size_t(k) * 4 * n,
+                          fp_coef64_ + size_t(k) * 5 * nn, 2.0 / hps.types_[k].dx, 2.0 / hps.types_[k].dy};
+        ck(cudaMemcpy(d_fps_, fl.data(), L * sizeof(MixFp), cudaMemcpyHostToDevice), "mixed fp leaves");
+        if (!share) mx_fp_convert(st, hps.d_fp_, d_fps_, L);
+    }
+    // leaf tables in FP32 (constant-coefficient leaves)
+    std::vector<LeafType32> t32(fp ? 0 : hps.types_.size());
+    if (!fp) {
         std::vector<double> V(nn), D(nn);
         std::vector<float> Vf(nn), Df(nn);
         float* tab = nullptr;
@@ -304,8 +320,12 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
     }
     h.pe(0, 0, st);
     h.pb("mx_leaf_residual", st);
-    mx_leaf_residual(st, d_coef_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
-                     rleaf_, rmax);
+    if (d_fps_)
+        mx_fp_residual(st, d_fps_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
+                       rleaf_, rmax);
+    else
+        mx_leaf_residual(st, d_coef_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
+                         rleaf_, rmax);
     h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
     h.pb("mx_interface", st);
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
@@ -324,7 +344,8 @@ void MixedSolver::pass(int B, bool first) {
     const int L = h.num_leaves(), n = h.leaf_n();
     const double items = double(L) * B, nn = double(n) * n;
     h.pb("mx_leaf_neumann", st);
-    mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr, 0);
+    if (d_fps_) mx_fp_leaf32(st, LEAF_NEUMANN, d_fps_, d_leaves_, L, B, n, q32_, nullptr, 0);
+    else mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr, 0);
     h.pe(items * (nn * 4 + 4 * n * 4), items * 2.0 * (3 * nn * n + 4 * nn), st);
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         h.pb("mx_interface", st);
@@ -360,7 +381,8 @@ void MixedSolver::pass(int B, bool first) {
         }
     }
     h.pb("mx_leaf_solve", st);
-    mx_leaf32(st, LEAF_SOLVE, d_types32_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
+    if (d_fps_) mx_fp_leaf32(st, LEAF_SOLVE, d_fps_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
+    else mx_leaf32(st, LEAF_SOLVE, d_types32_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
     h.pe(items * nn * (4 + 16), items * 2.0 * 4 * nn * n, st);
 }
 

@@ -111,3 +111,28 @@ def test_graph_replay_matches_eager(ef):
     hps.set_graphs(True)
     for _ in range(3):
         assert np.array_equal(hps.mixed_solve(F, A, R, sweeps=1), ref)
+
+
+@pytest.mark.parametrize("level,n", [(3, 16), (2, 32)])
+def test_mixed_five_point_variable_coefficients(ef, level, n):
+    """Config-3 coefficients (alpha = 1, beta = 1 + 0.5 sin(pi x) cos(pi y), lambda = -1) on
+    FivePointStencil leaves: FP32 band solves + FP64 variable-coefficient residual reach the FP64
+    HPS solution, and a request's result is the same alone and in a block."""
+    PI = np.pi
+    solver = ef.FiniteVolumeSolver(alpha_function=lambda x, y: 1.0 + 0.0 * x,
+                                   beta_function=lambda x, y: 1.0 + 0.5 * np.sin(PI * x) * np.cos(PI * y),
+                                   lambda_function=lambda x, y: -1.0 + 0.0 * x,
+                                   solver_type=ef.FivePointStencil)
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, -1.0, 1.0, n, -1.0, 1.0))
+    mesh = ef.Mesh().uniform(level, root)
+    hps = ef.HPSAlgorithm(mesh, solver)
+    hps.buildStage()
+    F, A, R = requests(hps, mesh, 5, 41)
+    ref = fp64_solutions(hps, F, A, R)
+    hps.mixed_init(5)
+    u = hps.mixed_solve(F, A, R, sweeps=2)
+    for k in range(5):
+        err = np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= TOL, (k, err)
+    alone = hps.mixed_solve(F[3:4], A[3:4], R[3:4], sweeps=2)
+    assert np.array_equal(alone[0], u[3])
