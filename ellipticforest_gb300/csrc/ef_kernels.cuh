@@ -188,14 +188,15 @@ void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax);
 
 // Variable-coefficient (FivePointStencil) leaves of the mixed form (ef_mixed_fp.cu), indexed by leaf.
 struct MixFp {
-    float* band;    // n*n rows x (2n+1): FP32 copy of the FP64 band LU, U's diagonal stored inverted
+    float* blocks;  // n block rows x {L_jj^-1, L_j,j-1, U_jj^-1, U_j,j+1} (n x n each) of the band LU, FP32
     float* bcoef;   // 4n boundary coupling coefficients (WESN)
     double* coef;   // 5 x n*n FP64 stencil coefficients cW, cE, cS, cN, cC
     double dtn_x, dtn_y;
 };
-void mx_fp_convert(cudaStream_t st, const FpLeaf* src, const MixFp* dst, int L);
+// stencil table, FP32 boundary coefficients and the block rows of the band LU (from the FP64 factors)
+void mx_fp_convert(cudaStream_t st, const FpLeaf* src, const MixFp* dst, int L, int n);
 size_t mx_fp_leaf_smem(int n);
-// batched FP32 band solves, one CTA per (leaf, 32 requests); modes LEAF_NEUMANN / LEAF_SOLVE
+// block triangular solves, one CTA per (leaf, group of requests); modes LEAF_NEUMANN / LEAF_SOLVE
 void mx_fp_leaf32(cudaStream_t st, int mode, const MixFp* fps, const MixLeaf* leaves, int L, int B, int n,
                   const float* q, double* u64, int accumulate);
 void mx_fp_residual(cudaStream_t st, const MixFp* fps, const MixLeaf* leaves, int L, int B, int n, int zero_state,

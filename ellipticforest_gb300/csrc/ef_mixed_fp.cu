@@ -1,12 +1,14 @@
 // Mixed-precision passes for variable-coefficient leaves (FiniteVolumeSolverType::FivePointStencil).
 //
 // The FP64 band LU of every leaf's 5-point operator (factored once at build time, see ef_leaf_fp.cu)
-// is copied to FP32 with the diagonal of U stored inverted, and the FP64 stencil coefficients
-// cW, cE, cS, cN, cC of FiniteVolumeSolver.cpp:66-100 are tabulated per cell.  A block of B requests
-// is then solved per leaf with one lane per request: the band rows are read once per leaf and
-// shared by the block, the work vectors of the block live in shared memory.  The FP64 residual uses
-// the tabulated coefficients with the same ghost treatment as the reference's boundary rows
-// (cpp:100-184): a missing neighbour is 2g - u_C.
+// has bandwidth n, so with the cells split into n blocks of n rows the triangular solves are
+//     forward   y_j = L_jj^{-1} (q_j - L_{j,j-1} y_{j-1})
+//     backward  x_j = U_jj^{-1} (y_j - U_{j,j+1} x_{j+1})
+// At set-up the diagonal blocks are inverted in FP64 and the four n x n blocks of every block row
+// are stored in FP32; a block of requests is then solved per leaf by 2n small GEMMs over the
+// requests, with the work vectors in shared memory.  The FP64 stencil coefficients cW, cE, cS, cN,
+// cC of FiniteVolumeSolver.cpp:66-100 are tabulated per cell for the residual, which uses the same
+// ghost treatment as the reference's boundary rows (cpp:100-184): a missing neighbour is 2g - u_C.
 #include "ef_kernels.cuh"
 
 namespace efgb {
@@ -33,18 +35,12 @@ __device__ __forceinline__ float d2f_bits_fp(double x) {
     return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
 }
 
-// one CTA per leaf: FP32 band (inverted U diagonal), FP32 boundary coefficients, FP64 stencil table
+// one CTA per leaf: FP32 boundary coefficients, FP64 stencil table
 __global__ void __launch_bounds__(256) k_mx_fp_convert(const FpLeaf* __restrict__ src, const MixFp* __restrict__ dst) {
     const FpLeaf lf = src[blockIdx.x];
     const MixFp mf = dst[blockIdx.x];
-    const int n = lf.n, N = n * n, w = 2 * n + 1;
+    const int n = lf.n, N = n * n;
     const double dx2 = lf.dx * lf.dx, dy2 = lf.dy * lf.dy;
-    for (long long e = threadIdx.x; e < (long long)N * w; e += blockDim.x) {
-        const long long row = e / w, col = e - row * w;
-        const double v = lf.band[e];
-        mf.band[e] = float(col == n ? 1.0 / v : v);
-        (void)row;
-    }
     for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) mf.bcoef[e] = float(lf.bcoef[e]);
     for (int r = threadIdx.x; r < N; r += blockDim.x) {
         const double a = lf.alpha[r];
@@ -57,95 +53,158 @@ __global__ void __launch_bounds__(256) k_mx_fp_convert(const FpLeaf* __restrict_
     }
 }
 
-constexpr int kFpLanes = 32;   // requests per CTA (one lane each)
-constexpr int kFpPad = 33;     // row stride of the shared work array (conflict-free transposes)
+// Block rows of the band LU (CTA = (block j, leaf), thread = column k of the n x n blocks), in FP64,
+// stored FP32 as blocks[j][4][n][n] = { L_jj^{-1}, L_{j,j-1}, U_jj^{-1}, U_{j,j+1} } (row-major).
+// Band row r holds columns r-n .. r+n at positions 0 .. 2n (L multipliers | U).
+__global__ void k_mx_fp_blocks(const FpLeaf* __restrict__ src, const MixFp* __restrict__ dst) {
+    const FpLeaf lf = src[blockIdx.y];
+    const int n = lf.n, w = 2 * n + 1, j = blockIdx.x, k = threadIdx.x;
+    if (k >= n) return;
+    const double* band = lf.band + (long long)j * n * w;  // first row of block row j
+    float* out = dst[blockIdx.y].blocks + (long long)j * 4 * n * n;
+    float* Linv = out;
+    float* Lsub = out + n * n;
+    float* Uinv = out + 2 * n * n;
+    float* Usup = out + 3 * n * n;
+    // column k of L_jj^{-1} (unit lower): x_a = delta_ak - sum_{b<a} L[a][b] x_b, L[a][b] at n - (a - b)
+    double x[64];
+    for (int a = 0; a < n; ++a) {
+        double v = (a == k) ? 1.0 : 0.0;
+        if (a > k)
+            for (int bb = k; bb < a; ++bb) v = fma(-band[(long long)a * w + n - (a - bb)], x[bb], v);
+        x[a] = a < k ? 0.0 : v;
+        Linv[a * n + k] = float(x[a]);
+    }
+    // column k of U_jj^{-1} (upper): x_a = (delta_ak - sum_{b>a} U[a][b] x_b) / U[a][a], U[a][b] at n + (b - a)
+    for (int a = n - 1; a >= 0; --a) {
+        double v = (a == k) ? 1.0 : 0.0;
+        if (a < k)
+            for (int bb = a + 1; bb <= k; ++bb) v = fma(-band[(long long)a * w + n + (bb - a)], x[bb], v);
+        x[a] = a > k ? 0.0 : v / band[(long long)a * w + n];
+        Uinv[a * n + k] = float(x[a]);
+    }
+    // off-diagonal blocks: L_{j,j-1}[a][b] (b >= a) at position b - a; U_{j,j+1}[a][b] (b <= a) at 2n + b - a
+    for (int a = 0; a < n; ++a) {
+        Lsub[a * n + k] = (j > 0 && k >= a) ? float(band[(long long)a * w + (k - a)]) : 0.0f;
+        Usup[a * n + k] = (j < n - 1 && k <= a) ? float(band[(long long)a * w + 2 * n + k - a]) : 0.0f;
+    }
+}
 
-// FP32 band solves of one leaf for up to 32 requests (blockIdx.y selects the group of 32).
-// NEUMANN: g = 0, load q, write h32 = DtN(0, q).  SOLVE: load q + boundary terms of g32, add (or
-// store, accumulate == 0) the solution to u64.
+// Block solve of one leaf for a group of BN requests (blockIdx.y): 2n steps, each two n x n x BN
+// products with the block matrices staged in shared memory.  NEUMANN: g = 0, load q, write
+// h32 = DtN(0, q).  SOLVE: load q + boundary terms of g32, add (or store, accumulate == 0) the
+// solution to u64.
 template <int MODE>
-__global__ void __launch_bounds__(32) k_mx_fp_leaf32(const MixFp* __restrict__ fps, const MixLeaf* __restrict__ leaves,
-                                                     int L, int B, int n, const float* __restrict__ q,
-                                                     double* __restrict__ u64, int accumulate) {
-    extern __shared__ float ys[];  // N rows x kFpPad
-    const int leaf = blockIdx.x, lane = threadIdx.x;
-    const int b0 = blockIdx.y * kFpLanes, nb = min(kFpLanes, B - b0);
-    const int b = b0 + lane;
-    const bool act = lane < nb;
+__global__ void __launch_bounds__(256) k_mx_fp_leaf32(const MixFp* __restrict__ fps, const MixLeaf* __restrict__ leaves,
+                                                      int L, int B, int n, int BN, const float* __restrict__ q,
+                                                      double* __restrict__ u64, int accumulate) {
+    extern __shared__ __align__(16) float fsm[];
+    const int N = n * n, ld = BN + 1;
+    float* Y = fsm;                 // N x ld
+    float* M1 = Y + N * ld;         // n x n
+    float* M2 = M1 + n * n;         // n x n
+    float* T = M2 + n * n;          // n x ld
+    const int leaf = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+    const int b0 = blockIdx.y * BN, nb = min(BN, B - b0);
     const MixFp mf = fps[leaf];
     const MixLeaf lf = leaves[leaf];
-    const int N = n * n, w = 2 * n + 1;
     const long long nn = N;
-    // load the block's q (coalesced along cells, transposed into rows x requests)
-    for (int r0 = 0; r0 < N; r0 += 32) {
-        const int r = r0 + lane;
-        for (int bb = 0; bb < nb; ++bb)
-            if (r < N) ys[r * kFpPad + bb] = q[((long long)(b0 + bb) * L + leaf) * nn + r];
+    // load the group's q: cells along threads (coalesced), transposed into rows x requests
+    for (int e = tid; e < N * nb; e += nt) {
+        const int bb = e / N, r = e - bb * N;
+        Y[r * ld + bb] = q[((long long)(b0 + bb) * L + leaf) * nn + r];
     }
-    __syncwarp();
-    if (MODE == LEAF_SOLVE && act) {
-        for (int side = 0; side < 4; ++side)
-            for (int pos = 0; pos < n; ++pos) {
-                int r;
-                if (side == 0) r = pos;
-                else if (side == 1) r = (n - 1) * n + pos;
-                else if (side == 2) r = pos * n;
-                else r = pos * n + n - 1;
-                ys[r * kFpPad + lane] += -2.0f * mf.bcoef[side * n + pos] * lf.g32[(long long)(side * n + pos) * B + b];
-            }
-    }
-    __syncwarp();
-    const float* band = mf.band;
-    // forward: y_k -= sum_{d=1..n} L[k][k-d] y_{k-d}
-    for (int k = 1; k < N; ++k) {
-        const float* row = band + (long long)k * w + n;
-        float s0 = 0.f, s1 = 0.f;
-        const int dmax = min(n, k);
-        int d = 1;
-        for (; d + 1 <= dmax; d += 2) {
-            s0 = fmaf(__ldg(row - d), ys[(k - d) * kFpPad + lane], s0);
-            s1 = fmaf(__ldg(row - d - 1), ys[(k - d - 1) * kFpPad + lane], s1);
-        }
-        if (d <= dmax) s0 = fmaf(__ldg(row - d), ys[(k - d) * kFpPad + lane], s0);
-        ys[k * kFpPad + lane] -= s0 + s1;
-    }
-    // backward: x_k = (y_k - sum_{e=1..n} U[k][k+e] x_{k+e}) * (1 / U[k][k])
-    for (int k = N - 1; k >= 0; --k) {
-        const float* row = band + (long long)k * w + n;
-        float s0 = 0.f, s1 = 0.f;
-        const int emax = min(n, N - 1 - k);
-        int e = 1;
-        for (; e + 1 <= emax; e += 2) {
-            s0 = fmaf(__ldg(row + e), ys[(k + e) * kFpPad + lane], s0);
-            s1 = fmaf(__ldg(row + e + 1), ys[(k + e + 1) * kFpPad + lane], s1);
-        }
-        if (e <= emax) s0 = fmaf(__ldg(row + e), ys[(k + e) * kFpPad + lane], s0);
-        ys[k * kFpPad + lane] = (ys[k * kFpPad + lane] - (s0 + s1)) * __ldg(row);
-    }
-    __syncwarp();
+    __syncthreads();
     if (MODE == LEAF_SOLVE) {
-        for (int r0 = 0; r0 < N; r0 += 32) {
-            const int r = r0 + lane;
-            if (r >= N) continue;
-            for (int bb = 0; bb < nb; ++bb) {
-                double* dst = u64 + ((long long)(b0 + bb) * L + leaf) * nn + r;
-                const double v = f2d_bits_fp(ys[r * kFpPad + bb]);
-                *dst = accumulate ? *dst + v : v;
+        for (int e = tid; e < 4 * n * nb; e += nt) {
+            const int bb = e % nb, t = e / nb, side = t / n, pos = t - side * n;
+            int r;
+            if (side == 0) r = pos;
+            else if (side == 1) r = (n - 1) * n + pos;
+            else if (side == 2) r = pos * n;
+            else r = pos * n + n - 1;
+            // a corner cell gets two terms from two threads: add them in a fixed order (side 0/1 first)
+            if (side >= 2 && (pos == 0 || pos == n - 1)) continue;
+            float v = -2.0f * mf.bcoef[side * n + pos] * lf.g32[(long long)(side * n + pos) * B + b0 + bb];
+            if (side < 2 && (pos == 0 || pos == n - 1)) {
+                const int s2 = pos == 0 ? 2 : 3, p2 = side == 0 ? 0 : n - 1;
+                v += -2.0f * mf.bcoef[s2 * n + p2] * lf.g32[(long long)(s2 * n + p2) * B + b0 + bb];
             }
+            Y[r * ld + bb] += v;
         }
-    } else if (act) {
-        // Neumann data of FiniteVolumeSolver.cpp:296-353 with g = 0
-        for (int side = 0; side < 4; ++side)
-            for (int pos = 0; pos < n; ++pos) {
-                int cell;
-                if (side == 0) cell = pos;
-                else if (side == 1) cell = (n - 1) * n + pos;
-                else if (side == 2) cell = pos * n;
-                else cell = pos * n + n - 1;
-                const float dtn = float(side < 2 ? mf.dtn_x : mf.dtn_y);
-                const float sg = (side == 0 || side == 2) ? 1.0f : -1.0f;
-                lf.h32[(long long)(side * n + pos) * B + b] = sg * dtn * ys[cell * kFpPad + lane];
+        __syncthreads();
+    }
+    const float* blocks = mf.blocks;
+    const int outs = n * nb;
+    // one product: dst[a][bb] (= base[a][bb] -) sum_c Mat[a][c] src[c][bb]
+    auto gemm = [&](const float* Mat, const float* src, int src_ld, float* dst, int dst_ld, const float* base,
+                    int base_ld, bool sub) {
+        for (int o = tid; o < outs; o += nt) {
+            const int a = o / nb, bb = o - a * nb;
+            const float* mr = Mat + a * n;
+            float s0 = 0.f, s1 = 0.f;
+            int c = 0;
+            for (; c + 1 < n; c += 2) {
+                s0 = fmaf(mr[c], src[c * src_ld + bb], s0);
+                s1 = fmaf(mr[c + 1], src[(c + 1) * src_ld + bb], s1);
             }
+            if (c < n) s0 = fmaf(mr[c], src[c * src_ld + bb], s0);
+            const float s = s0 + s1;
+            dst[a * dst_ld + bb] = sub ? base[a * base_ld + bb] - s : s;
+        }
+    };
+    auto stage = [&](const float* g1, const float* g2) {
+        for (int e = tid; e < n * n; e += nt) {
+            M1[e] = g1[e];
+            M2[e] = g2[e];
+        }
+    };
+    // forward sweep
+    for (int j = 0; j < n; ++j) {
+        const float* bj = blocks + (long long)j * 4 * n * n;
+        stage(bj, bj + n * n);  // L_jj^{-1}, L_{j,j-1}
+        __syncthreads();
+        float* Yj = Y + j * n * ld;
+        if (j > 0) gemm(M2, Yj - n * ld, ld, T, ld, Yj, ld, true);
+        else
+            for (int o = tid; o < outs; o += nt) { const int a = o / nb, bb = o - a * nb; T[a * ld + bb] = Yj[a * ld + bb]; }
+        __syncthreads();
+        gemm(M1, T, ld, Yj, ld, nullptr, 0, false);
+        __syncthreads();
+    }
+    // backward sweep
+    for (int j = n - 1; j >= 0; --j) {
+        const float* bj = blocks + (long long)j * 4 * n * n;
+        stage(bj + 2 * n * n, bj + 3 * n * n);  // U_jj^{-1}, U_{j,j+1}
+        __syncthreads();
+        float* Yj = Y + j * n * ld;
+        if (j < n - 1) gemm(M2, Yj + n * ld, ld, T, ld, Yj, ld, true);
+        else
+            for (int o = tid; o < outs; o += nt) { const int a = o / nb, bb = o - a * nb; T[a * ld + bb] = Yj[a * ld + bb]; }
+        __syncthreads();
+        gemm(M1, T, ld, Yj, ld, nullptr, 0, false);
+        __syncthreads();
+    }
+    if (MODE == LEAF_SOLVE) {
+        for (int e = tid; e < N * nb; e += nt) {
+            const int bb = e / N, r = e - bb * N;
+            double* dst = u64 + ((long long)(b0 + bb) * L + leaf) * nn + r;
+            const double v = f2d_bits_fp(Y[r * ld + bb]);
+            *dst = accumulate ? *dst + v : v;
+        }
+    } else {
+        // Neumann data of FiniteVolumeSolver.cpp:296-353 with g = 0
+        for (int e = tid; e < 4 * n * nb; e += nt) {
+            const int bb = e % nb, t = e / nb, side = t / n, pos = t - side * n;
+            int cell;
+            if (side == 0) cell = pos;
+            else if (side == 1) cell = (n - 1) * n + pos;
+            else if (side == 2) cell = pos * n;
+            else cell = pos * n + n - 1;
+            const float dtn = float(side < 2 ? mf.dtn_x : mf.dtn_y);
+            const float sg = (side == 0 || side == 2) ? 1.0f : -1.0f;
+            lf.h32[(long long)(side * n + pos) * B + b0 + bb] = sg * dtn * Y[cell * ld + bb];
+        }
     }
 }
 
@@ -246,16 +305,29 @@ __global__ void __launch_bounds__(256) k_mx_fp_residual(const MixFp* __restrict_
 
 }  // namespace
 
-void mx_fp_convert(cudaStream_t st, const FpLeaf* src, const MixFp* dst, int L) {
+void mx_fp_blocks(cudaStream_t st, const FpLeaf* src, const MixFp* dst, int L, int n) {
     if (L <= 0) return;
-    k_mx_fp_convert<<<L, 256, 0, st>>>(src, dst);
+    k_mx_fp_blocks<<<dim3(unsigned(n), unsigned(L)), 32 * ((n + 31) / 32), 0, st>>>(src, dst);
     ++g_kernel_launches;
 }
 
-size_t mx_fp_leaf_smem(int n) { return size_t(n) * n * kFpPad * sizeof(float); }
+void mx_fp_convert(cudaStream_t st, const FpLeaf* src, const MixFp* dst, int L, int n) {
+    if (L <= 0) return;
+    k_mx_fp_convert<<<L, 256, 0, st>>>(src, dst);
+    ++g_kernel_launches;
+    mx_fp_blocks(st, src, dst, L, n);
+}
+
+int mx_fp_group(int n) { return n <= 16 ? 32 : 16; }
+
+size_t mx_fp_leaf_smem(int n) {
+    const int BN = mx_fp_group(n), ld = BN + 1;
+    return (size_t(n) * n * ld + 2 * size_t(n) * n + size_t(n) * ld) * sizeof(float);
+}
 
 void mx_fp_leaf32(cudaStream_t st, int mode, const MixFp* fps, const MixLeaf* leaves, int L, int B, int n,
                   const float* q, double* u64, int accumulate) {
+    const int BN = mx_fp_group(n);
     const size_t smem = mx_fp_leaf_smem(n);
     static size_t configured = 48 * 1024;
     if (smem > configured) {
@@ -263,11 +335,11 @@ void mx_fp_leaf32(cudaStream_t st, int mode, const MixFp* fps, const MixLeaf* le
         cudaFuncSetAttribute(k_mx_fp_leaf32<LEAF_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
-    dim3 grid(unsigned(L), unsigned((B + kFpLanes - 1) / kFpLanes));
+    dim3 grid(unsigned(L), unsigned((B + BN - 1) / BN));
     if (mode == LEAF_NEUMANN)
-        k_mx_fp_leaf32<LEAF_NEUMANN><<<grid, kFpLanes, smem, st>>>(fps, leaves, L, B, n, q, u64, 0);
+        k_mx_fp_leaf32<LEAF_NEUMANN><<<grid, 256, smem, st>>>(fps, leaves, L, B, n, BN, q, u64, 0);
     else
-        k_mx_fp_leaf32<LEAF_SOLVE><<<grid, kFpLanes, smem, st>>>(fps, leaves, L, B, n, q, u64, accumulate);
+        k_mx_fp_leaf32<LEAF_SOLVE><<<grid, 256, smem, st>>>(fps, leaves, L, B, n, BN, q, u64, accumulate);
     ++g_kernel_launches;
 }
 

@@ -128,7 +128,7 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         if (fp) {
             // FP32 band factors and FP64 stencil tables, shared by the lanes of one tree
             d_fps_ = cv.get<MixFp>(L);
-            fp_band32_ = share ? share->fp_band32_ : cv.get<float>(size_t(L) * nn * (2 * n + 1));
+            fp_band32_ = share ? share->fp_band32_ : cv.get<float>(size_t(L) * 4 * nn * n);
             fp_bcoef32_ = share ? share->fp_bcoef32_ : cv.get<float>(size_t(L) * 4 * n);
             fp_coef64_ = share ? share->fp_coef64_ : cv.get<double>(size_t(L) * 5 * nn);
         }
@@ -192,10 +192,10 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     if (fp) {
         std::vector<MixFp> fl(L);
         for (int k = 0; k < L; ++k)
-            fl[k] = MixFp{fp_band32_ + size_t(k) * nn * (2 * n + 1), fp_bcoef32_ + size_t(k) * 4 * n,
+            fl[k] = MixFp{fp_band32_ + size_t(k) * 4 * nn * n, fp_bcoef32_ + size_t(k) * 4 * n,
                           fp_coef64_ + size_t(k) * 5 * nn, 2.0 / hps.types_[k].dx, 2.0 / hps.types_[k].dy};
         ck(cudaMemcpy(d_fps_, fl.data(), L * sizeof(MixFp), cudaMemcpyHostToDevice), "mixed fp leaves");
-        if (!share) mx_fp_convert(st, hps.d_fp_, d_fps_, L);
+        if (!share) mx_fp_convert(st, hps.d_fp_, d_fps_, L, n);
     }
     // leaf tables in FP32 (constant-coefficient leaves)
     std::vector<LeafType32> t32(fp ? 0 : hps.types_.size());
