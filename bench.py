@@ -15,6 +15,8 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
   plain_fp64 -- the plain FP64 form one request at a time (device-resident solves/s, p50/p99, and
             e2e through the reference-facing upwards/solve/get_leaf_u calls)
   many_rhs_L6 -- 512 right-hand sides on a uniform level-6 tree: one mixed block vs 512 plain solves
+  adaptive_L7 -- config 2 (refineByFunction tree, 7 750 leaves): build, plain FP64 solves/s, error
+            against the exact solution, and the mixed block form
   variable_coefficient_L5 -- config 3 (FivePointStencil leaves, variable beta): build, plain FP64
             solves/s, discretisation error, and the mixed block form against the FP64 HPS
   serving -- 2000 Poisson-arrival requests over three resident trees (uniform L4, adaptive max level
@@ -453,7 +455,9 @@ def run_gb300(args):
     extras = {}
     if not args.no_extras:
         extras["many_rhs_L6"] = many_rhs(ef, torch, stream, args)
-        extras["serving"] = serving(ef, torch, stream, (mesh, hps), args)
+        c2 = build_config2(ef, torch, stream)
+        extras["adaptive_L7"] = adaptive(ef, torch, stream, args, c2)
+        extras["serving"] = serving(ef, torch, stream, (mesh, hps), args, c2)
         extras["variable_coefficient_L5"] = variable_coefficient(ef, torch, stream, args)
 
     cpu = None
@@ -526,7 +530,81 @@ def make_request_box(seed, X, Y, bpts, box):
     return make_request(seed, sx(X), sy(Y), [(sx(x), sy(y)) for x, y in bpts])
 
 
-def serving(ef, torch, stream, main_tree, args):
+def build_config2(ef, torch, stream):
+    """Config-2 tree: refineByFunction(|sin x + sin y| > 1.2, min 0, max 7) on [-10,10]^2, 16x16
+    patches, FISHPACK90 leaves; returns (mesh, hps, build seconds)."""
+    rc = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -10.0, 10.0, 16, -10.0, 10.0))
+    mesh = ef.Mesh().refineByFunction(lambda x, y: abs(np.sin(x) + np.sin(y)) > 1.2, 1.2, 0, 7, rc)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hps.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hps.buildStage()
+    torch.cuda.synchronize()
+    return mesh, hps, time.perf_counter() - t0
+
+
+def adaptive(ef, torch, stream, args, c2):
+    """Config 2: the adaptive tree with f = -(sin x + sin y), g = sin x + sin y: build, plain FP64
+    solves/s and error against the exact solution, and the mixed block form against FP64."""
+    mesh, hps, build_s = c2
+    X, Y = mesh.cell_centres()
+    bp = hps.boundary_points()
+    f = -(np.sin(X) + np.sin(Y))
+    r = np.concatenate([np.sin(x) + np.sin(y) for x, y in bp])
+    a = np.ones_like(r)
+    hps.upwards_array(f)
+    hps.solve_arrays(a, np.zeros_like(a), r)
+    u64 = hps.leaf_solution()
+    err = float(np.abs(u64 - (np.sin(X) + np.sin(Y))).max())
+    dev = tuple(torch.from_numpy(v).cuda() for v in (f, a, np.zeros_like(a), r))
+    for _ in range(3):
+        hps.load_device_async(*[t.data_ptr() for t in dev])
+        hps.solve_device_async(True)
+    torch.cuda.synchronize()
+    K = 20
+    e0, e1 = _events(torch, 2)
+    e0.record(stream)
+    for _ in range(K):
+        hps.load_device_async(*[t.data_ptr() for t in dev])
+        hps.solve_device_async(True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain = K / (e0.elapsed_time(e1) / 1e3)
+    B = 32
+    reqs = [(f, a, r)]
+    for i in range(3):
+        fq, aq, _, rq = make_request_box(8000 + i, X, Y, bp, (-10.0, 10.0, -10.0, 10.0))
+        reqs.append((fq, aq, rq))
+    refs = []
+    for q in reqs:
+        hps.upwards_array(q[0])
+        hps.solve_arrays(q[1], np.zeros_like(q[1]), q[2])
+        refs.append(hps.leaf_solution())
+    F = np.stack([reqs[i % 4][0] for i in range(B)])
+    A = np.stack([reqs[i % 4][1] for i in range(B)])
+    R = np.stack([reqs[i % 4][2] for i in range(B)])
+    hps.mixed_init(B)
+    U = hps.mixed_solve(F, A, R, args.sweeps)
+    errs = [float(np.abs(U[i] - refs[i]).max() / np.abs(refs[i]).max()) for i in range(4)]
+    hps.mixed_solve_async(B, args.sweeps)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(3):
+        hps.mixed_solve_async(B, args.sweeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mixed = 3 * B / (e0.elapsed_time(e1) / 1e3)
+    hps.mixed_init(1)  # release the block's memory
+    return {"workload": "config 2: refineByFunction(|sin x + sin y| > 1.2, 0, 7) on [-10,10]^2, 16x16 patches, "
+                        "f = -(sin x + sin y), g = sin x + sin y",
+            "leaves": hps.num_leaves, "dofs": int(X.size), "build_s": build_s,
+            "plain_fp64_solves_per_s": plain, "max_err_vs_exact": err,
+            "mixed_block": {"batch": B, "sweeps": args.sweeps, "solves_per_s": mixed,
+                            "speedup_vs_plain": mixed / plain, "rel_err_vs_fp64_per_request": errs}}
+
+
+def serving(ef, torch, stream, main_tree, args, c2):
     """Poisson-arrival stream of 2000 requests (seeded) over three resident trees -- uniform L4,
     the adaptive tree of refineByFunction(|sin x + sin y| > 1.2, 0, 7) on [-10,10]^2, uniform L7 --
     answered by the serving loop (continuous same-tree batching, two lanes per tree, HBM budget), against
@@ -541,11 +619,7 @@ def serving(ef, torch, stream, main_tree, args):
     h4.set_stream(stream.cuda_stream)
     h4.buildStage()
     trees.append(("uniform L4", m4, h4, (-1.0, 1.0, -1.0, 1.0)))
-    rc = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -10.0, 10.0, 16, -10.0, 10.0))
-    mc = ef.Mesh().refineByFunction(lambda x, y: abs(-(np.sin(x) + np.sin(y))), 1.2, 0, 7, rc)
-    hc = ef.HPSAlgorithm(mc, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
-    hc.set_stream(stream.cuda_stream)
-    hc.buildStage()
+    mc, hc, _ = c2
     trees.append((f"adaptive max_level 7 ({hc.num_leaves} leaves)", mc, hc, (-10.0, 10.0, -10.0, 10.0)))
     mesh7, h7 = main_tree
     trees.append(("uniform L7", mesh7, h7, DOM))

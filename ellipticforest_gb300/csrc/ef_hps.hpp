@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -290,6 +291,9 @@ private:
     };
     bool prof_ = false;
     bool graphs_ = true;
+    // K split of the mixed form's node GEMMs per group and kind (W, H, DOWN), chosen once per tree by
+    // MixedSolver::tune and shared by every block solver of the tree
+    std::vector<std::array<int, 3>> mx_split_;
     GraphCache graph_solve_;
     std::vector<ProfStat> stats_;
     std::vector<Mark> marks_;
@@ -360,6 +364,9 @@ private:
     };
     void residual(int B, double* rmax, bool zero_state);
     void pass(int B, bool first);
+    // times the K-split candidates of every node GEMM (CUDA events, block of min(bmax, 32)) and keeps
+    // the fastest per group and kind in the tree
+    void tune();
 
     Hps& H_;
     int bmax_;

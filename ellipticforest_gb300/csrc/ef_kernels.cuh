@@ -166,8 +166,12 @@ void mx_hdiff(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 // (scattered to the children and added to u_Gamma).  The group's operators are contiguous row-major
 // matrices read through the TMA tensor map tm (32 columns x mx_tile_rows rows per box, 128-byte
 // swizzle); err is set when a TMA wait times out.
+// ksplit: CTAs of the thread-block cluster that split K for one tile (0: a heuristic from the tile
+// count; the choice never depends on B, so a request's sums are grouped the same way in any block)
 void mx_gemm(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
-             int* err);
+             int* err, int ksplit);
+// largest K split worth trying for a GEMM kind at interface size s (every CTA keeps >= 2 chunks)
+int mx_gemm_max_split(int kind, int s);
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);

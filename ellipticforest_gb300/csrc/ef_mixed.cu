@@ -884,7 +884,8 @@ void mx_gemm_launch(cudaStream_t st, const CUtensorMap& tm, const MixItem* items
 }
 
 template <int KIND>
-void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B, int* err) {
+void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B, int* err,
+             int ksplit_req) {
     int rows_item, K;
     mx_shape<KIND>(s, rows_item, K);
     const int rt = mx_tile_rows(KIND == MX_H ? 1 : 0, s);
@@ -895,7 +896,12 @@ void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int n
     // flight and every CTA keeps at least 8 chunks.  Chosen from the tile count alone so that every
     // request's sums are grouped the same way whatever the batch size.
     int ksplit = 1;
-    while (ksplit < 8 && (long long)tiles * ksplit < 608 && nkc >= 16 * ksplit) ksplit *= 2;
+    if (ksplit_req > 0) {
+        ksplit = std::min(ksplit_req, 8);
+        while (ksplit > 1 && nkc < 2 * ksplit) ksplit /= 2;
+    } else {
+        while (ksplit < 8 && (long long)tiles * ksplit < 608 && nkc >= 16 * ksplit) ksplit *= 2;
+    }
     if (BN == 8) mx_gemm_launch<8, KIND>(st, tm, items, tiles, s, B, rt, ksplit, err);
     else if (BN == 16) mx_gemm_launch<16, KIND>(st, tm, items, tiles, s, B, rt, ksplit, err);
     else mx_gemm_launch<32, KIND>(st, tm, items, tiles, s, B, rt, ksplit, err);
@@ -911,10 +917,18 @@ void mx_hdiff(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
 }
 
 void mx_gemm(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
-             int* err) {
-    if (kind == 0) mx_gemm<MX_W>(st, tm, items, nitems, s, B, err);
-    else if (kind == 1) mx_gemm<MX_H>(st, tm, items, nitems, s, B, err);
-    else mx_gemm<MX_DOWN>(st, tm, items, nitems, s, B, err);
+             int* err, int ksplit) {
+    if (kind == 0) mx_gemm<MX_W>(st, tm, items, nitems, s, B, err, ksplit);
+    else if (kind == 1) mx_gemm<MX_H>(st, tm, items, nitems, s, B, err, ksplit);
+    else mx_gemm<MX_DOWN>(st, tm, items, nitems, s, B, err, ksplit);
+}
+
+int mx_gemm_max_split(int kind, int s) {
+    const int K = kind == 0 ? 4 * s : (kind == 1 ? 2 * s : 8 * s);
+    const int nkc = (K + kKC - 1) / kKC;
+    int k = 1;
+    while (k < 8 && nkc >= 4 * k) k *= 2;
+    return k;
 }
 
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {

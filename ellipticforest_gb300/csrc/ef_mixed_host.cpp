@@ -298,6 +298,44 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     }
     ck(cudaGetLastError(), "mixed convert");
     ck(cudaStreamSynchronize(st), "mixed setup");
+    if (hps.mx_split_.size() != groups_.size()) tune();
+}
+
+void MixedSolver::tune() {
+    Hps& h = H_;
+    const int B = std::min(bmax_, 32);
+    std::vector<std::array<int, 3>> best(groups_.size(), std::array<int, 3>{1, 1, 1});
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ck(cudaEventCreate(&e0), "tune event");
+    ck(cudaEventCreate(&e1), "tune event");
+    for (size_t gi = 0; gi < groups_.size(); ++gi) {
+        const MGroup& g = groups_[gi];
+        for (int kind = 0; kind < 3; ++kind) {
+            const CUtensorMap& tm = kind == 0 ? g.tmXi : (kind == 1 ? g.tmH : g.tmS);
+            const int kmax = mx_gemm_max_split(kind, g.s);
+            float best_ms = 1e30f;
+            for (int ks = 1; ks <= kmax; ks *= 2) {
+                mx_gemm(st_, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ks);  // warm-up
+                ck(cudaEventRecord(e0, st_), "tune event");
+                for (int r = 0; r < 3; ++r) mx_gemm(st_, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ks);
+                ck(cudaEventRecord(e1, st_), "tune event");
+                ck(cudaEventSynchronize(e1), "tune sync");
+                float ms = 0.f;
+                ck(cudaEventElapsedTime(&ms, e0, e1), "tune time");
+                if (ms < best_ms * 0.97f) {  // a larger split must win clearly
+                    best_ms = ms;
+                    best[gi][kind] = ks;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ck(cudaGetLastError(), "mixed tune");
+    if (take_error()) throw std::runtime_error("mixed solver: an operator tile copy did not complete while tuning");
+    // the tuning launches wrote the pass buffers and the interface state: start clean
+    ck(cudaMemsetAsync(arena_, 0, size_t(uG_begin_ - arena_) + uG_bytes_, st_), "clear after tune");
+    h.mx_split_ = best;
 }
 
 MixedSolver::~MixedSolver() {
@@ -354,14 +392,16 @@ void MixedSolver::pass(int B, bool first) {
         for (auto& g : groups_)
             if (g.level == lvl) mx_hdiff(st, g.d_items, g.cnt, g.s, B);
         h.pe(0, 0, st);
-        for (auto& g : groups_) {
+        for (size_t gi = 0; gi < groups_.size(); ++gi) {
+            const MGroup& g = groups_[gi];
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
+            const std::array<int, 3> ks = h.mx_split_.empty() ? std::array<int, 3>{0, 0, 0} : h.mx_split_[gi];
             h.pb("mx_gemm_w", st);
-            mx_gemm(st, 0, g.tmXi, g.d_items, g.cnt, g.s, B, d_err_);
+            mx_gemm(st, 0, g.tmXi, g.d_items, g.cnt, g.s, B, d_err_, ks[0]);
             h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
             h.pb("mx_gemm_h", st);
-            mx_gemm(st, 1, g.tmH, g.d_items, g.cnt, g.s, B, d_err_);
+            mx_gemm(st, 1, g.tmH, g.d_items, g.cnt, g.s, B, d_err_, ks[1]);
             h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
         }
     }
@@ -372,11 +412,12 @@ void MixedSolver::pass(int B, bool first) {
         for (auto& s : gsteps_)
             if (s.level == lvl) mx_uncoarsen(st, false, s.in32, s.out32, s.count, s.nf, B);
         h.pe(0, 0, st);
-        for (auto& g : groups_) {
+        for (size_t gi = 0; gi < groups_.size(); ++gi) {
+            const MGroup& g = groups_[gi];
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
             h.pb("mx_gemm_down", st);
-            mx_gemm(st, 2, g.tmS, g.d_items, g.cnt, g.s, B, d_err_);
+            mx_gemm(st, 2, g.tmS, g.d_items, g.cnt, g.s, B, d_err_, h.mx_split_.empty() ? 0 : h.mx_split_[gi][2]);
             h.pe(c * 32 * s2 * 4, c * 2.0 * 32 * s2 * B, st);
         }
     }
