@@ -19,6 +19,8 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
             against the exact solution, and the mixed block form
   variable_coefficient_L5 -- config 3 (FivePointStencil leaves, variable beta): build, plain FP64
             solves/s, discretisation error, and the mixed block form against the FP64 HPS
+  mixed_build -- FP32 merges with the interface LU of the top 3 levels in FP64 (uniform L7, config
+            2): build seconds, the FP64 sweeps needed for 1e-10 and the block rate
   serving -- 2000 Poisson-arrival requests over three resident trees (uniform L4, adaptive max level
             7, uniform L7) through the serving loop (continuous same-tree batching, p50/p99 latency)
             against the same requests one at a time through the plain FP64 path
@@ -458,6 +460,8 @@ def run_gb300(args):
         c2 = build_config2(ef, torch, stream)
         extras["adaptive_L7"] = adaptive(ef, torch, stream, args, c2)
         extras["serving"] = serving(ef, torch, stream, (mesh, hps), args, c2)
+        extras["mixed_build"] = mixed_build(ef, torch, stream, args, (mesh, hps, DOM, build_s),
+                                            (c2[0], c2[1], (-10.0, 10.0, -10.0, 10.0), c2[2]))
         extras["variable_coefficient_L5"] = variable_coefficient(ef, torch, stream, args)
 
     cpu = None
@@ -602,6 +606,65 @@ def adaptive(ef, torch, stream, args, c2):
             "plain_fp64_solves_per_s": plain, "max_err_vs_exact": err,
             "mixed_block": {"batch": B, "sweeps": args.sweeps, "solves_per_s": mixed,
                             "speedup_vs_plain": mixed / plain, "rel_err_vs_fp64_per_request": errs}}
+
+
+def mixed_build(ef, torch, stream, args, main, c2):
+    """Mixed-precision build (FP32 merges, interface LU of the top 3 levels in FP64) of the uniform
+    L7 tree and of the config-2 tree: build seconds and TFLOP/s, the fewest FP64 sweeps that keep
+    every result within 1e-10 of the FP64-built tree's solution, and the block rate at that count."""
+    out = {}
+    for name, (mesh64, hps64, box, build64_s) in (("uniform_L7", main), ("adaptive_L7", c2)):
+        root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, box[0], box[1], 16, box[2], box[3]))
+        mesh = (ef.Mesh().uniform(7, root) if name == "uniform_L7" else
+                ef.Mesh().refineByFunction(lambda x, y: abs(np.sin(x) + np.sin(y)) > 1.2, 1.2, 0, 7, root))
+        hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+        hps.set_stream(stream.cuda_stream)
+        hps.profile_enable(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hps.buildStageMixed(3)
+        torch.cuda.synchronize()
+        tb = time.perf_counter() - t0
+        prof = hps.profile()
+        hps.profile_enable(False)
+        flops = sum(v["flops"] for v in prof.values())
+        X, Y = mesh.cell_centres()
+        bp = hps.boundary_points()
+        reqs = [make_request_box(6000 + i, X, Y, bp, box) for i in range(4)]
+        refs = []
+        for f, a, b, r in reqs:
+            hps64.upwards_array(f)
+            hps64.solve_arrays(a, b, r)
+            refs.append(hps64.leaf_solution())
+        B = 32
+        F = np.stack([reqs[i % 4][0] for i in range(B)])
+        A = np.stack([reqs[i % 4][1] for i in range(B)])
+        R = np.stack([reqs[i % 4][3] for i in range(B)])
+        hps.mixed_init(B)
+        sweeps, err = None, None
+        for sw in (2, 3, 4):
+            U = hps.mixed_solve(F, A, R, sw)
+            err = max(float(np.abs(U[i] - refs[i]).max() / np.abs(refs[i]).max()) for i in range(4))
+            if err <= 1e-10:
+                sweeps = sw
+                break
+        rate = None
+        if sweeps is not None:
+            hps.mixed_solve_async(B, sweeps)
+            torch.cuda.synchronize()
+            e0, e1 = _events(torch, 2)
+            e0.record(stream)
+            for _ in range(3):
+                hps.mixed_solve_async(B, sweeps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            rate = 3 * B / (e0.elapsed_time(e1) / 1e3)
+        out[name] = {"build_s": tb, "fp64_build_s": build64_s, "build_speedup": build64_s / tb,
+                     "build_tflops": flops / tb / 1e12, "fp64_levels": 3,
+                     "sections_ms": {k: v["ms"] for k, v in sorted(prof.items())},
+                     "sweeps_for_1e-10": sweeps, "rel_err_vs_fp64": err, "block_solves_per_s": rate}
+        del hps
+    return out
 
 
 def serving(ef, torch, stream, main_tree, args, c2):

@@ -311,6 +311,18 @@ int ef_hps_build(ef_hps* h) {
     });
 }
 
+int ef_hps_build_mixed(ef_hps* h, int fp64_levels) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    return guarded([&] {
+        h->mixed.reset();
+        h->hps->build_mixed(fp64_levels);
+        if (h->hps->singular_count() > 0)
+            return fail(EF_ERR_SINGULAR, std::to_string(h->hps->singular_count()) +
+                                             " interface matrices had a zero pivot");
+        return EF_OK;
+    });
+}
+
 int ef_hps_upwards(ef_hps* h, const double* f_host) {
     if (!h || !f_host) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "upwards stage before build stage");
@@ -445,7 +457,7 @@ int ef_hps_synchronize(ef_hps* h) {
 
 int ef_hps_mixed_init(ef_hps* h, int bmax) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
-    if (!h->hps->built()) return fail(EF_ERR_STATE, "mixed solver before build stage");
+    if (!h->hps->built() && !h->hps->built32()) return fail(EF_ERR_STATE, "mixed solver before build stage");
     return guarded([&] {
         h->mixed.reset();
         h->mixed = std::make_unique<efgb::MixedSolver>(*h->hps, bmax);
@@ -618,7 +630,8 @@ int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lane
     std::vector<efgb::Server::TreeSpec> specs;
     for (int t = 0; t < ntrees; ++t) {
         if (!trees[t]) return fail(EF_ERR_INVALID, "null tree handle");
-        if (!trees[t]->hps->built()) return fail(EF_ERR_STATE, "server tree before build stage");
+        if (!trees[t]->hps->built() && !trees[t]->hps->built32())
+            return fail(EF_ERR_STATE, "server tree before build stage");
         specs.push_back(efgb::Server::TreeSpec{trees[t]->hps.get(), bmax[t]});
     }
     return guarded([&] {

@@ -78,6 +78,7 @@ Hps::~Hps() {
     for (auto& m : marks_) { ev_free_.push_back(m.a); ev_free_.push_back(m.b); }
     for (cudaEvent_t e : ev_free_) cudaEventDestroy(e);
     if (arena_) cudaFree(arena_);
+    if (arena32_) cudaFree(arena32_);
     if (d_rootA_) cudaFree(d_rootA_);
 }
 

@@ -191,6 +191,11 @@ public:
 
     // Stages (synchronous to the host at their end unless noted).
     void build();                                  // HPSAlgorithm::buildStage
+    // Mixed-precision build (no counterpart in the reference): every merge in FP32 except the
+    // interface LU of the top `fp64_levels` tree levels, factored in FP64 and rounded to FP32.  Fills
+    // the FP32 operator set the mixed block solver reads; the plain FP64 solve needs build().
+    void build_mixed(int fp64_levels);
+    bool built32() const { return built32_; }
     void upwards();                                // HPSAlgorithm::upwardsStage on leaf_f()
     void root_from_bc();                           // root g from bc_a/b/r (HPSAlgorithm.hpp:402-420)
     void downwards();                              // split1to4 + leafSolve for every node
@@ -289,6 +294,34 @@ private:
         long long launches;
         double bytes, flops;
     };
+    // FP32 operator set of the mixed build (ef_build32.cpp)
+    struct Node32 {
+        float *T = nullptr, *Tc = nullptr, *X = nullptr, *RHS = nullptr, *H = nullptr;
+        std::vector<float*> Tsteps;
+    };
+    struct Group32 {
+        MergeItem32* d_items = nullptr;
+        float** d_X = nullptr;
+        float** d_RHS = nullptr;
+        const float** d_gA = nullptr;
+        const float** d_gB = nullptr;
+        const float** d_gB2 = nullptr;
+        float** d_gC = nullptr;
+    };
+    struct Step32 {
+        const float** d_in = nullptr;
+        float** d_out = nullptr;
+    };
+    void allocate32();
+    std::vector<Node32> n32_;
+    std::vector<Group32> g32_;
+    std::vector<Step32> t32_;
+    const double** d_tT64_ = nullptr;
+    float** d_tT32_ = nullptr;
+    char* arena32_ = nullptr;
+    size_t arena32_bytes_ = 0;
+    bool built32_ = false;
+
     bool prof_ = false;
     bool graphs_ = true;
     // K split of the mixed form's node GEMMs per group and kind (W, H, DOWN), chosen once per tree by

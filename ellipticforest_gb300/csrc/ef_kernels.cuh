@@ -32,25 +32,31 @@ extern std::atomic<long long> g_kernel_launches;
 // ------------------------------------------------------------------------------------------------
 // Batched FP64 dense linear algebra (pointer arrays, uniform shapes and offsets per launch)
 // ------------------------------------------------------------------------------------------------
-struct GemmArgs {
-    const double* const* A; long long offA; int lda;
-    const double* const* B; long long offB; int ldb;
-    double* const* C; long long offC; int ldc;
+template <class Real>
+struct GemmArgsT {
+    const Real* const* A; long long offA; int lda;
+    const Real* const* B; long long offB; int ldb;
+    Real* const* C; long long offC; int ldc;
     // optional: rows k >= kb of B come from B2 (row k - kb, same ldb)
-    const double* const* B2 = nullptr;
+    const Real* const* B2 = nullptr;
     long long offB2 = 0;
     int kb = 1 << 30;
 };
+using GemmArgs = GemmArgsT<double>;
+using GemmArgs32 = GemmArgsT<float>;
 
-// C = alpha*A*B + beta*C for each batch item (row-major).
+// C = alpha*A*B + beta*C for each batch item (row-major); FP64 (plain form) and FP32 (mixed build).
 void dgemm_batched(cudaStream_t st, int M, int N, int K, double alpha, const GemmArgs& a,
                    double beta, int batch);
+void sgemm_batched(cudaStream_t st, int M, int N, int K, float alpha, const GemmArgs32& a, float beta,
+                   int batch);
 
 // In-place LU with partial pivoting of the square n x n matrices A[b] (row-major, lda).
 // piv[b][j] is the 0-based row swapped with row j (LAPACK dgetrf semantics, 0-based);
 // info[b] = first zero pivot (1-based) or 0.  A, piv: device arrays of device pointers.
 void dgetrf_batched(cudaStream_t st, int n, double* const* A, int lda, int* const* piv, int* info,
                     int batch);
+void sgetrf_batched(cudaStream_t st, int n, float* const* A, int lda, int* const* piv, int* info, int batch);
 
 // perm[b][i] = original row that ends at position i after applying piv[b][0..n).
 void piv_to_perm(cudaStream_t st, int n, int* const* piv, int* const* perm, int batch);
@@ -58,6 +64,8 @@ void piv_to_perm(cudaStream_t st, int n, int* const* piv, int* const* perm, int 
 // B[b] <- U^{-1} L^{-1} B[b]  (B already row-permuted), n x nrhs, ldb.
 void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* LU, int lda,
                         double* const* B, int ldb, int batch);
+void slu_solve_permuted(cudaStream_t st, int n, int nrhs, const float* const* LU, int lda, float* const* B,
+                        int ldb, int batch);
 
 // ------------------------------------------------------------------------------------------------
 // Leaf patch kernels (constant-coefficient Helmholtz u_xx + u_yy + lambda u = f, Dirichlet data on
@@ -142,12 +150,14 @@ struct MixItem {
     float* mout;          // = m, written by the residual
 };
 
-struct MixConv {  // FP64 operators -> FP32 copies
-    const double* RHS;
-    const double* H;
+struct MixConv {  // operators -> FP32 copies in the group layout
+    const double* RHS;    // FP64-built [S | X^-1] (or null)
+    const double* H;      // FP64-built compact H (or null)
     float* S;
     float* Xi;
     float* H32;
+    const float* RHS32;   // FP32-built [S | X^-1] (used when non-null)
+    const float* Hsrc32;  // FP32-built compact H
 };
 
 // Rows per tile of the FP32 node GEMMs (kind 0: X^{-1} and S, 4s rows per node; kind 1: compact H,
@@ -209,21 +219,24 @@ void mx_fp_residual(cudaStream_t st, const MixFp* fps, const MixLeaf* leaves, in
 // ------------------------------------------------------------------------------------------------
 // Merge / upward / downward kernels
 // ------------------------------------------------------------------------------------------------
-struct MergeItem {
-    const double* Tc[4];  // children's (coarsened) T, 4s x 4s
-    double* X;            // 4s x 4s (LU in place)
-    int* piv;             // 4s
-    int* perm;            // 4s
-    double* RHS;          // 4s x 12s  = [S (WESN columns) | X^{-1}]
-    double* H;            // 8s x 2s compact: row p holds the two interface blocks adjacent to c(p)
-    double* T;            // 8s x 8s, WESN
-    const double* hc[4];  // children's (coarsened) h, 4s
-    double* h;            // own h, 8s
-    double* hd;           // 4s, interface differences of the children's h
-    double* w;            // 4s
-    const double* gf;     // own full-size g, 8s
-    double* gc[4];        // children's g (at coarsened size), 4s
+template <class Real>
+struct MergeItemT {
+    const Real* Tc[4];  // children's (coarsened) T, 4s x 4s
+    Real* X;            // 4s x 4s (LU in place)
+    int* piv;           // 4s
+    int* perm;          // 4s
+    Real* RHS;          // 4s x 12s  = [S (WESN columns) | X^{-1}]
+    Real* H;            // 8s x 2s compact: row p holds the two interface blocks adjacent to c(p)
+    Real* T;            // 8s x 8s, WESN
+    const Real* hc[4];  // children's (coarsened) h, 4s
+    Real* h;            // own h, 8s
+    Real* hd;           // 4s, interface differences of the children's h
+    Real* w;            // 4s
+    const Real* gf;     // own full-size g, 8s
+    Real* gc[4];        // children's g (at coarsened size), 4s
 };
+using MergeItem = MergeItemT<double>;
+using MergeItem32 = MergeItemT<float>;
 
 // X, H and T (= T_LHS) from the children (build, step 1).
 void merge_gather_xht(cudaStream_t st, const MergeItem* items, int nitems, int s);
@@ -232,6 +245,13 @@ void merge_gather_rhs(cudaStream_t st, const MergeItem* items, int nitems, int s
 
 // Per-side coarsening of T (4nf x 4nf -> 4nc x 4nc): L21 T L12  (SpecialMatrices.hpp:93-173).
 void coarsen_T(cudaStream_t st, const double* const* Tin, double* const* Tout, int nitems, int nf);
+// FP32 versions of the build gathers for the mixed-precision build
+void merge_gather_xht32(cudaStream_t st, const MergeItem32* items, int nitems, int s);
+void merge_gather_rhs32(cudaStream_t st, const MergeItem32* items, int nitems, int s);
+void coarsen_T32(cudaStream_t st, const float* const* Tin, float* const* Tout, int nitems, int nf);
+// element-wise precision changes of `count` items of `len` values each
+void widen_batched(cudaStream_t st, const float* const* in, double* const* out, long long len, int count);
+void narrow_batched(cudaStream_t st, const double* const* in, float* const* out, long long len, int count);
 // Per-side fine-to-coarse averaging of h (4nf -> 4nc).
 void coarsen_vec(cudaStream_t st, const double* const* vin, double* const* vout, int nitems, int nf);
 // Per-side coarse-to-fine interpolation of g (4nc -> 4nf).

@@ -1,4 +1,4 @@
-// Batched FP64 dense linear algebra for the HPS merges (plain FP64 form).
+// Batched dense linear algebra for the HPS merges: FP64 (plain form) and FP32 (mixed build).
 //
 // Replaces the reference's per-node LAPACK/BLAS calls (Matrix.hpp:789-952: dgemv, dgemm and dgesv
 // on transposed copies) with grouped launches over every merge of one tree level.  On GB300 the
@@ -17,23 +17,24 @@ namespace {
 constexpr int TM = 64, TN = 64, TK = 16;
 constexpr int NB = 32;  // LU / triangular-solve block size
 
-__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, GemmArgs a,
-                                               double beta, int b0) {
+template <class Real>
+__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, Real alpha, GemmArgsT<Real> a,
+                                               Real beta, int b0) {
     const int b = b0 + blockIdx.z;
-    const double* __restrict__ A = a.A[b] + a.offA;
-    const double* __restrict__ B = a.B[b] + a.offB;
-    const double* __restrict__ B2 = a.B2 ? a.B2[b] + a.offB2 : B;
+    const Real* __restrict__ A = a.A[b] + a.offA;
+    const Real* __restrict__ B = a.B[b] + a.offB;
+    const Real* __restrict__ B2 = a.B2 ? a.B2[b] + a.offB2 : B;
     const int kb = a.B2 ? a.kb : (1 << 30);
-    double* C = a.C[b] + a.offC;
+    Real* C = a.C[b] + a.offC;
     const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
-    __shared__ double As[TK][TM + 1];
-    __shared__ double Bs[TK][TN];
+    __shared__ Real As[TK][TM + 1];
+    __shared__ Real Bs[TK][TN];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    double acc[4][4];
+    Real acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < 4; ++j) acc[i][j] = Real(0);
 
     for (int k0 = 0; k0 < K; k0 += TK) {
 #pragma unroll
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             const int e = tid + 256 * r;
             const int row = e >> 4, kk = e & 15;
             const int gm = m0 + row, gk = k0 + kk;
-            As[kk][row] = (gm < M && gk < K) ? A[(long long)gm * a.lda + gk] : 0.0;
+            As[kk][row] = (gm < M && gk < K) ? A[(long long)gm * a.lda + gk] : Real(0);
         }
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -50,12 +51,12 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             const int gk = k0 + kk, gn = n0 + col;
             Bs[kk][col] = (gk < K && gn < N)
                               ? (gk < kb ? B[(long long)gk * a.ldb + gn] : B2[(long long)(gk - kb) * a.ldb + gn])
-                              : 0.0;
+                              : Real(0);
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < TK; ++kk) {
-            double av[4], bv[4];
+            Real av[4], bv[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
 #pragma unroll
@@ -75,45 +76,46 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
         for (int j = 0; j < 4; ++j) {
             const int col = n0 + tx + 16 * j;
             if (col >= N) continue;
-            double* c = C + (long long)row * a.ldc + col;
-            *c = (beta == 0.0) ? alpha * acc[i][j] : fma(alpha, acc[i][j], beta * *c);
+            Real* c = C + (long long)row * a.ldc + col;
+            *c = (beta == Real(0)) ? alpha * acc[i][j] : fma(alpha, acc[i][j], beta * *c);
         }
     }
 }
 
 // Unblocked LU with partial pivoting of the panel A[k:n, k:k+jb] (LAPACK dgetf2 on a panel).
 // One CTA per matrix.  Row swaps are applied inside the panel columns only.
-__global__ void __launch_bounds__(1024) k_getf2_panel(int n, int k, int jb, double* const* Aarr,
+template <class Real>
+__global__ void __launch_bounds__(1024) k_getf2_panel(int n, int k, int jb, Real* const* Aarr,
                                                       int lda, int* const* pivarr, int* info) {
-    double* __restrict__ A = Aarr[blockIdx.x];
+    Real* __restrict__ A = Aarr[blockIdx.x];
     int* __restrict__ piv = pivarr[blockIdx.x];
-    __shared__ double s_val[32];
+    __shared__ Real s_val[32];
     __shared__ int s_idx[32];
     __shared__ int s_p;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
     for (int j = k; j < k + jb; ++j) {
-        double best = -1.0;
+        Real best = Real(-1);
         int bi = INT_MAX;
         for (int i = j + tid; i < n; i += blockDim.x) {
-            const double v = fabs(A[(long long)i * lda + j]);
+            const Real v = fabs(A[(long long)i * lda + j]);
             if (v > best) { best = v; bi = i; }
             else if (bi == INT_MAX) { bi = i; }
         }
         // (value, index) reduction: the larger value wins, ties go to the smaller index (idamax).
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, best, off);
+            const Real ov = __shfl_down_sync(0xffffffffu, best, off);
             const int oi = __shfl_down_sync(0xffffffffu, bi, off);
             if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
         }
         if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
         __syncthreads();
         if (wid == 0) {
-            best = (lane < nw) ? s_val[lane] : -2.0;
+            best = (lane < nw) ? s_val[lane] : Real(-2);
             bi = (lane < nw) ? s_idx[lane] : INT_MAX;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
-                const double ov = __shfl_down_sync(0xffffffffu, best, off);
+                const Real ov = __shfl_down_sync(0xffffffffu, best, off);
                 const int oi = __shfl_down_sync(0xffffffffu, bi, off);
                 if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
             }
@@ -121,23 +123,23 @@ __global__ void __launch_bounds__(1024) k_getf2_panel(int n, int k, int jb, doub
                 const int p = (bi >= j && bi < n) ? bi : j;
                 s_p = p;
                 piv[j] = p;
-                if (!(A[(long long)p * lda + j] != 0.0) && info[blockIdx.x] == 0) info[blockIdx.x] = j + 1;
+                if (!(A[(long long)p * lda + j] != Real(0)) && info[blockIdx.x] == 0) info[blockIdx.x] = j + 1;
             }
         }
         __syncthreads();
         const int p = s_p;
         if (p != j) {
             for (int c = tid; c < jb; c += blockDim.x) {
-                double* a = A + (long long)j * lda + k + c;
-                double* b = A + (long long)p * lda + k + c;
-                const double t = *a; *a = *b; *b = t;
+                Real* a = A + (long long)j * lda + k + c;
+                Real* b = A + (long long)p * lda + k + c;
+                const Real t = *a; *a = *b; *b = t;
             }
         }
         __syncthreads();
-        const double pv = A[(long long)j * lda + j];
-        if (pv != 0.0) {
-            if (fabs(pv) >= DBL_MIN) {
-                const double r = 1.0 / pv;
+        const Real pv = A[(long long)j * lda + j];
+        if (pv != Real(0)) {
+            if (fabs(pv) >= (sizeof(Real) == 8 ? Real(DBL_MIN) : Real(FLT_MIN))) {
+                const Real r = Real(1) / pv;
                 for (int i = j + 1 + tid; i < n; i += blockDim.x) A[(long long)i * lda + j] *= r;
             } else {
                 for (int i = j + 1 + tid; i < n; i += blockDim.x) A[(long long)i * lda + j] /= pv;
@@ -158,9 +160,10 @@ __global__ void __launch_bounds__(1024) k_getf2_panel(int n, int k, int jb, doub
 }
 
 // Apply the swaps piv[k..k+jb) to the columns outside the panel (LAPACK dlaswp).
-__global__ void k_laswp_outside(int n, int k, int jb, double* const* Aarr, int lda,
+template <class Real>
+__global__ void k_laswp_outside(int n, int k, int jb, Real* const* Aarr, int lda,
                                 int* const* pivarr) {
-    double* __restrict__ A = Aarr[blockIdx.y];
+    Real* __restrict__ A = Aarr[blockIdx.y];
     const int* __restrict__ piv = pivarr[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n - jb) return;
@@ -168,9 +171,9 @@ __global__ void k_laswp_outside(int n, int k, int jb, double* const* Aarr, int l
     for (int j = k; j < k + jb; ++j) {
         const int p = piv[j];
         if (p != j) {
-            double* a = A + (long long)j * lda + c;
-            double* b = A + (long long)p * lda + c;
-            const double tmp = *a; *a = *b; *b = tmp;
+            Real* a = A + (long long)j * lda + c;
+            Real* b = A + (long long)p * lda + c;
+            const Real tmp = *a; *a = *b; *b = tmp;
         }
     }
 }
@@ -178,13 +181,13 @@ __global__ void k_laswp_outside(int n, int k, int jb, double* const* Aarr, int l
 // Triangular solve of the jb rows [brow0, brow0+jb) x columns [bcol0, bcol0+ncols) of B with the
 // jb x jb diagonal block of LU at (k, k).  LOWER: unit lower, forward substitution;
 // !LOWER: upper non-unit, backward substitution.  One thread per column.
-template <bool LOWER>
-__global__ void __launch_bounds__(256) k_trsm_block(int k, int jb, const double* const* LUarr,
-                                                    int lda, double* const* Barr, int ldb,
+template <class Real, bool LOWER>
+__global__ void __launch_bounds__(256) k_trsm_block(int k, int jb, const Real* const* LUarr,
+                                                    int lda, Real* const* Barr, int ldb,
                                                     int brow0, int bcol0, int ncols) {
-    const double* __restrict__ LU = LUarr[blockIdx.y];
-    double* __restrict__ B = Barr[blockIdx.y];
-    __shared__ double L[NB][NB + 1];
+    const Real* __restrict__ LU = LUarr[blockIdx.y];
+    Real* __restrict__ B = Barr[blockIdx.y];
+    __shared__ Real L[NB][NB + 1];
     for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
         const int r = e / jb, c = e % jb;
         L[r][c] = LU[(long long)(k + r) * lda + k + c];
@@ -192,25 +195,25 @@ __global__ void __launch_bounds__(256) k_trsm_block(int k, int jb, const double*
     __syncthreads();
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= ncols) return;
-    double* Bc = B + (long long)brow0 * ldb + bcol0 + col;
-    double x[NB];
+    Real* Bc = B + (long long)brow0 * ldb + bcol0 + col;
+    Real x[NB];
 #pragma unroll
-    for (int i = 0; i < NB; ++i) x[i] = (i < jb) ? Bc[(long long)i * ldb] : 0.0;
+    for (int i = 0; i < NB; ++i) x[i] = (i < jb) ? Bc[(long long)i * ldb] : Real(0);
     if (LOWER) {
 #pragma unroll
         for (int i = 1; i < NB; ++i) {
-            double acc = x[i];
+            Real acc = x[i];
 #pragma unroll
             for (int t = 0; t < i; ++t) acc -= L[i][t] * x[t];
-            x[i] = (i < jb) ? acc : 0.0;
+            x[i] = (i < jb) ? acc : Real(0);
         }
     } else {
 #pragma unroll
         for (int i = NB - 1; i >= 0; --i) {
             if (i < jb) {
-                double acc = x[i];
+                Real acc = x[i];
 #pragma unroll
-                for (int t = i + 1; t < NB; ++t) acc -= (t < jb ? L[i][t] : 0.0) * x[t];
+                for (int t = i + 1; t < NB; ++t) acc -= (t < jb ? L[i][t] : Real(0)) * x[t];
                 x[i] = acc / L[i][i];
             }
         }
@@ -236,66 +239,62 @@ __global__ void k_piv_to_perm(int n, int* const* pivarr, int* const* permarr) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
 }
 
-}  // namespace
 
-void dgemm_batched(cudaStream_t st, int M, int N, int K, double alpha, const GemmArgs& a,
-                   double beta, int batch) {
+template <class Real>
+void gemm_batched_t(cudaStream_t st, int M, int N, int K, Real alpha, const GemmArgsT<Real>& a, Real beta,
+                    int batch) {
     if (M <= 0 || N <= 0 || batch <= 0) return;
-    if (K <= 0 && beta == 1.0) return;
+    if (K <= 0 && beta == Real(1)) return;
     for (int b0 = 0; b0 < batch; b0 += 65535) {
         const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
         dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, nb);
-        k_dgemm<<<grid, 256, 0, st>>>(M, N, K, alpha, a, beta, b0);
+        k_dgemm<Real><<<grid, 256, 0, st>>>(M, N, K, alpha, a, beta, b0);
         ++g_kernel_launches;
     }
 }
 
-void dgetrf_batched(cudaStream_t st, int n, double* const* A, int lda, int* const* piv, int* info,
-                    int batch) {
+template <class Real>
+void getrf_batched_t(cudaStream_t st, int n, Real* const* A, int lda, int* const* piv, int* info, int batch) {
     for (int k = 0; k < n; k += NB) {
         const int jb = (n - k < NB) ? n - k : NB;
         const int threads = (n - k >= 512) ? 1024 : 256;
-        k_getf2_panel<<<batch, threads, 0, st>>>(n, k, jb, A, lda, piv, info);
+        k_getf2_panel<Real><<<batch, threads, 0, st>>>(n, k, jb, A, lda, piv, info);
         ++g_kernel_launches;
         if (n - jb > 0) {
             dim3 g((n - jb + 255) / 256, batch);
-            k_laswp_outside<<<g, 256, 0, st>>>(n, k, jb, A, lda, piv);
+            k_laswp_outside<Real><<<g, 256, 0, st>>>(n, k, jb, A, lda, piv);
             ++g_kernel_launches;
         }
         const int rest = n - k - jb;
         if (rest > 0) {
             // U12 = L11^{-1} A12
             dim3 g((rest + 255) / 256, batch);
-            k_trsm_block<true><<<g, 256, 0, st>>>(k, jb, (const double* const*)A, lda, A, lda, k,
-                                                  k + jb, rest);
+            k_trsm_block<Real, true><<<g, 256, 0, st>>>(k, jb, (const Real* const*)A, lda, A, lda, k, k + jb, rest);
+            ++g_kernel_launches;
             // A22 -= L21 U12
-            GemmArgs ga{(const double* const*)A, (long long)(k + jb) * lda + k, lda,
-                        (const double* const*)A, (long long)k * lda + k + jb, lda,
-                        A, (long long)(k + jb) * lda + k + jb, lda};
-            dgemm_batched(st, rest, rest, jb, -1.0, ga, 1.0, batch);
+            GemmArgsT<Real> ga{(const Real* const*)A, (long long)(k + jb) * lda + k, lda,
+                               (const Real* const*)A, (long long)k * lda + k + jb, lda,
+                               A, (long long)(k + jb) * lda + k + jb, lda};
+            gemm_batched_t<Real>(st, rest, rest, jb, Real(-1), ga, Real(1), batch);
         }
     }
 }
 
-void piv_to_perm(cudaStream_t st, int n, int* const* piv, int* const* perm, int batch) {
-    k_piv_to_perm<<<batch, 256, n * sizeof(int), st>>>(n, piv, perm);
-    ++g_kernel_launches;
-}
-
-void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* LU, int lda,
-                        double* const* B, int ldb, int batch) {
+template <class Real>
+void lu_solve_permuted_t(cudaStream_t st, int n, int nrhs, const Real* const* LU, int lda, Real* const* B, int ldb,
+                         int batch) {
     // forward: L y = P b
     for (int k = 0; k < n; k += NB) {
         const int jb = (n - k < NB) ? n - k : NB;
         dim3 g((nrhs + 255) / 256, batch);
-        k_trsm_block<true><<<g, 256, 0, st>>>(k, jb, LU, lda, B, ldb, k, 0, nrhs);
+        k_trsm_block<Real, true><<<g, 256, 0, st>>>(k, jb, LU, lda, B, ldb, k, 0, nrhs);
         ++g_kernel_launches;
         const int rest = n - k - jb;
         if (rest > 0) {
-            GemmArgs ga{LU, (long long)(k + jb) * lda + k, lda,
-                        (const double* const*)B, (long long)k * ldb, ldb,
-                        B, (long long)(k + jb) * ldb, ldb};
-            dgemm_batched(st, rest, nrhs, jb, -1.0, ga, 1.0, batch);
+            GemmArgsT<Real> ga{LU, (long long)(k + jb) * lda + k, lda,
+                               (const Real* const*)B, (long long)k * ldb, ldb,
+                               B, (long long)(k + jb) * ldb, ldb};
+            gemm_batched_t<Real>(st, rest, nrhs, jb, Real(-1), ga, Real(1), batch);
         }
     }
     // backward: U x = y
@@ -303,15 +302,43 @@ void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* L
     for (int k = last; k >= 0; k -= NB) {
         const int jb = (n - k < NB) ? n - k : NB;
         dim3 g((nrhs + 255) / 256, batch);
-        k_trsm_block<false><<<g, 256, 0, st>>>(k, jb, LU, lda, B, ldb, k, 0, nrhs);
+        k_trsm_block<Real, false><<<g, 256, 0, st>>>(k, jb, LU, lda, B, ldb, k, 0, nrhs);
         ++g_kernel_launches;
         if (k > 0) {
-            GemmArgs ga{LU, (long long)k, lda,
-                        (const double* const*)B, (long long)k * ldb, ldb,
-                        B, 0, ldb};
-            dgemm_batched(st, k, nrhs, jb, -1.0, ga, 1.0, batch);
+            GemmArgsT<Real> ga{LU, (long long)k, lda,
+                               (const Real* const*)B, (long long)k * ldb, ldb,
+                               B, 0, ldb};
+            gemm_batched_t<Real>(st, k, nrhs, jb, Real(-1), ga, Real(1), batch);
         }
     }
+}
+
+}  // namespace
+
+void dgemm_batched(cudaStream_t st, int M, int N, int K, double alpha, const GemmArgs& a, double beta, int batch) {
+    gemm_batched_t<double>(st, M, N, K, alpha, a, beta, batch);
+}
+void sgemm_batched(cudaStream_t st, int M, int N, int K, float alpha, const GemmArgs32& a, float beta, int batch) {
+    gemm_batched_t<float>(st, M, N, K, alpha, a, beta, batch);
+}
+void dgetrf_batched(cudaStream_t st, int n, double* const* A, int lda, int* const* piv, int* info, int batch) {
+    getrf_batched_t<double>(st, n, A, lda, piv, info, batch);
+}
+void sgetrf_batched(cudaStream_t st, int n, float* const* A, int lda, int* const* piv, int* info, int batch) {
+    getrf_batched_t<float>(st, n, A, lda, piv, info, batch);
+}
+void dlu_solve_permuted(cudaStream_t st, int n, int nrhs, const double* const* LU, int lda, double* const* B,
+                        int ldb, int batch) {
+    lu_solve_permuted_t<double>(st, n, nrhs, LU, lda, B, ldb, batch);
+}
+void slu_solve_permuted(cudaStream_t st, int n, int nrhs, const float* const* LU, int lda, float* const* B,
+                        int ldb, int batch) {
+    lu_solve_permuted_t<float>(st, n, nrhs, LU, lda, B, ldb, batch);
+}
+
+void piv_to_perm(cudaStream_t st, int n, int* const* piv, int* const* perm, int batch) {
+    k_piv_to_perm<<<batch, 256, n * sizeof(int), st>>>(n, piv, perm);
+    ++g_kernel_launches;
 }
 
 }  // namespace efgb

@@ -41,8 +41,9 @@ __device__ __forceinline__ void child_ifaces(int c, int& Ia, int& Ib) {
     Ib = (c < 2) ? 2 : 3;
 }
 
-__global__ void k_gather_xht(const MergeItem* __restrict__ items, int s) {
-    const MergeItem& it = items[blockIdx.y];
+template <class Real>
+__global__ void k_gather_xht(const MergeItemT<Real>* __restrict__ items, int s) {
+    const MergeItemT<Real>& it = items[blockIdx.y];
     const long long m2 = 2LL * s, m4 = 4LL * s, m8 = 8LL * s;
     const long long nX = m4 * m4, nH = m8 * m2, nT = m8 * m8;
     const long long tot = nX + nH + nT;
@@ -51,7 +52,7 @@ __global__ void k_gather_xht(const MergeItem* __restrict__ items, int s) {
         if (e < nX) {
             const int r = int(e / m4), cc = int(e - (e / m4) * m4);
             const int I = r / s, o = r - I * s, J = cc / s, oj = cc - J * s;
-            double v = 0.0;
+            Real v = Real(0);
             // X(I,J) = -sum_c sigma(I,c) Tc[q(c,I)][q(c,J)]
             const int cl = lower_child(I), cu = upper_child(I);
             double sj;
@@ -77,29 +78,30 @@ __global__ void k_gather_xht(const MergeItem* __restrict__ items, int s) {
             int c, q, c2, q2;
             ext_map(p, s, c, q);
             ext_map(pp, s, c2, q2);
-            it.T[f] = (c == c2) ? it.Tc[c][(long long)q * m4 + q2] : 0.0;
+            it.T[f] = (c == c2) ? it.Tc[c][(long long)q * m4 + q2] : Real(0);
         }
     }
 }
 
-__global__ void k_gather_rhs(const MergeItem* __restrict__ items, int s) {
-    const MergeItem& it = items[blockIdx.y];
+template <class Real>
+__global__ void k_gather_rhs(const MergeItemT<Real>* __restrict__ items, int s) {
+    const MergeItemT<Real>& it = items[blockIdx.y];
     const long long m4 = 4LL * s, m12 = 12LL * s;
     const long long tot = m4 * m12;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
          e += (long long)gridDim.x * blockDim.x) {
         const int r = int(e / m12), col = int(e - (e / m12) * m12);
         const int src = it.perm[r];
-        double v;
+        Real v;
         if (col < 8 * s) {
             const int I = src / s, o = src - I * s;
             int c, q;
             ext_map(col, s, c, q);
             double sg;
             const int qi = iface_q(c, I, o, s, sg);
-            v = (qi >= 0) ? sg * it.Tc[c][(long long)qi * m4 + q] : 0.0;
+            v = (qi >= 0) ? Real(sg) * it.Tc[c][(long long)qi * m4 + q] : Real(0);
         } else {
-            v = (col - 8 * s == src) ? 1.0 : 0.0;
+            v = (col - 8 * s == src) ? Real(1) : Real(0);
         }
         it.RHS[e] = v;
     }
@@ -122,9 +124,10 @@ __device__ __forceinline__ int l12_col(int j, int nf, int* rows, double* w) {
     return k;
 }
 
-__global__ void k_coarsen_T(const double* const* Tin, double* const* Tout, int nf) {
-    const double* __restrict__ A = Tin[blockIdx.y];
-    double* __restrict__ B = Tout[blockIdx.y];
+template <class Real>
+__global__ void k_coarsen_T(const Real* const* Tin, Real* const* Tout, int nf) {
+    const Real* __restrict__ A = Tin[blockIdx.y];
+    Real* __restrict__ B = Tout[blockIdx.y];
     const int nc = nf / 2, mf = 4 * nf, mc = 4 * nc;
     const long long tot = (long long)mc * mc;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
@@ -134,15 +137,23 @@ __global__ void k_coarsen_T(const double* const* Tin, double* const* Tout, int n
         int rows[6];
         double w[6];
         const int k = l12_col(j, nf, rows, w);
-        double acc = 0.0;
+        Real acc = Real(0);
         for (int rr = 0; rr < 2; ++rr) {
-            const double* row = A + (long long)(a * nf + 2 * i + rr) * mf + b * nf;
-            double t = 0.0;
-            for (int q = 0; q < k; ++q) t = fma(row[rows[q]], w[q], t);
-            acc = fma(0.5, t, acc);
+            const Real* row = A + (long long)(a * nf + 2 * i + rr) * mf + b * nf;
+            Real t = Real(0);
+            for (int q = 0; q < k; ++q) t = fma(row[rows[q]], Real(w[q]), t);
+            acc = fma(Real(0.5), t, acc);
         }
         B[e] = acc;
     }
+}
+
+template <class In, class Out>
+__global__ void k_convert_batched(const In* const* in, Out* const* out, long long len) {
+    const In* a = in[blockIdx.y];
+    Out* b = out[blockIdx.y];
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len; e += (long long)gridDim.x * blockDim.x)
+        b[e] = Out(a[e]);
 }
 
 __global__ void k_coarsen_vec(const double* const* vin, double* const* vout, int nf) {
@@ -360,24 +371,52 @@ inline int grid_for(long long tot, int per_item_items) {
 
 }  // namespace
 
-void merge_gather_xht(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+template <class Real>
+void gather_xht_t(cudaStream_t st, const MergeItemT<Real>* items, int nitems, int s) {
     const long long tot = 16LL * s * s + 32LL * s * s + 64LL * s * s;
     dim3 g(grid_for(tot, nitems), nitems);
-    k_gather_xht<<<g, 256, 0, st>>>(items, s);
+    k_gather_xht<Real><<<g, 256, 0, st>>>(items, s);
     ++g_kernel_launches;
 }
 
-void merge_gather_rhs(cudaStream_t st, const MergeItem* items, int nitems, int s) {
+template <class Real>
+void gather_rhs_t(cudaStream_t st, const MergeItemT<Real>* items, int nitems, int s) {
     const long long tot = 48LL * s * s;
     dim3 g(grid_for(tot, nitems), nitems);
-    k_gather_rhs<<<g, 256, 0, st>>>(items, s);
+    k_gather_rhs<Real><<<g, 256, 0, st>>>(items, s);
     ++g_kernel_launches;
 }
 
-void coarsen_T(cudaStream_t st, const double* const* Tin, double* const* Tout, int nitems, int nf) {
+template <class Real>
+void coarsen_T_t(cudaStream_t st, const Real* const* Tin, Real* const* Tout, int nitems, int nf) {
     const long long tot = 4LL * nf * 4LL * nf / 4;
     dim3 g(grid_for(tot, nitems), nitems);
-    k_coarsen_T<<<g, 256, 0, st>>>(Tin, Tout, nf);
+    k_coarsen_T<Real><<<g, 256, 0, st>>>(Tin, Tout, nf);
+    ++g_kernel_launches;
+}
+
+void merge_gather_xht(cudaStream_t st, const MergeItem* items, int nitems, int s) { gather_xht_t(st, items, nitems, s); }
+void merge_gather_rhs(cudaStream_t st, const MergeItem* items, int nitems, int s) { gather_rhs_t(st, items, nitems, s); }
+void coarsen_T(cudaStream_t st, const double* const* Tin, double* const* Tout, int nitems, int nf) {
+    coarsen_T_t(st, Tin, Tout, nitems, nf);
+}
+void merge_gather_xht32(cudaStream_t st, const MergeItem32* items, int nitems, int s) {
+    gather_xht_t(st, items, nitems, s);
+}
+void merge_gather_rhs32(cudaStream_t st, const MergeItem32* items, int nitems, int s) {
+    gather_rhs_t(st, items, nitems, s);
+}
+void coarsen_T32(cudaStream_t st, const float* const* Tin, float* const* Tout, int nitems, int nf) {
+    coarsen_T_t(st, Tin, Tout, nitems, nf);
+}
+void widen_batched(cudaStream_t st, const float* const* in, double* const* out, long long len, int count) {
+    if (count <= 0) return;
+    k_convert_batched<float, double><<<dim3(grid_for(len, count), count), 256, 0, st>>>(in, out, len);
+    ++g_kernel_launches;
+}
+void narrow_batched(cudaStream_t st, const double* const* in, float* const* out, long long len, int count) {
+    if (count <= 0) return;
+    k_convert_batched<double, float><<<dim3(grid_for(len, count), count), 256, 0, st>>>(in, out, len);
     ++g_kernel_launches;
 }
 

@@ -816,15 +816,16 @@ __global__ void k_mx_convert(const MixConv* __restrict__ items, int s) {
     const long long nS = m4 * 8 * s, nX = m4 * m4, nH = 16LL * s * s;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nS + nX + nH;
          e += (long long)gridDim.x * blockDim.x) {
+        const bool f32 = it.RHS32 != nullptr;
         if (e < nS) {
             const long long r = e / (8 * s), c = e - r * (8 * s);
-            it.S[e] = float(it.RHS[r * m12 + c]);
+            it.S[e] = f32 ? it.RHS32[r * m12 + c] : float(it.RHS[r * m12 + c]);
         } else if (e < nS + nX) {
             const long long f = e - nS, r = f / m4, c = f - r * m4;
-            it.Xi[f] = float(it.RHS[r * m12 + 8 * s + c]);
+            it.Xi[f] = f32 ? it.RHS32[r * m12 + 8 * s + c] : float(it.RHS[r * m12 + 8 * s + c]);
         } else {
             const long long f = e - nS - nX;
-            it.H32[f] = float(it.H[f]);
+            it.H32[f] = f32 ? it.Hsrc32[f] : float(it.H[f]);
         }
     }
 }

@@ -60,7 +60,7 @@ CUtensorMap make_map(float* base, long long rows, int cols, int box_rows) {
 MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     : H_(hps), bmax_(bmax), st_(hps.stream()), share_(share) {
     if (share && &share->H_ != &hps) throw std::invalid_argument("mixed solver: operators shared across trees");
-    if (!hps.built()) throw std::invalid_argument("mixed solver: build the FP64 tree first");
+    if (!hps.built() && !hps.built32()) throw std::invalid_argument("mixed solver: build the tree first");
     const bool fp = hps.solver_type() == SOLVER_FIVE_POINT;
     if (bmax < 1 || bmax > 1024) throw std::invalid_argument("mixed solver: bmax must be in [1, 1024]");
     const int N = hps.num_nodes(), L = hps.num_leaves(), n = hps.leaf_n();
@@ -246,7 +246,8 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
                 it.gc64[c] = ch.g64;
                 it.hc64[c] = ch.hc64;
             }
-            conv[i] = MixConv{hps.nodes_[id].RHS, hps.nodes_[id].H, m.S, m.Xi, m.H32};
+            conv[i] = hps.built32() ? MixConv{nullptr, nullptr, m.S, m.Xi, m.H32, hps.n32_[id].RHS, hps.n32_[id].H}
+                                    : MixConv{hps.nodes_[id].RHS, hps.nodes_[id].H, m.S, m.Xi, m.H32, nullptr, nullptr};
         }
         ck(cudaMemcpy(groups_[gi].d_items, items.data(), items.size() * sizeof(MixItem), cudaMemcpyHostToDevice), "mix items");
         ck(cudaMemcpy(groups_[gi].d_conv, conv.data(), conv.size() * sizeof(MixConv), cudaMemcpyHostToDevice), "mix conv");

@@ -21,7 +21,8 @@ Server::Server(const std::vector<TreeSpec>& trees, int lanes_per_tree, long long
         // first lane of every tree (holds the tree's FP32 operators), then further lanes round-robin
         // while the budget allows
         for (size_t t = 0; t < trees.size(); ++t) {
-            if (!trees[t].hps || !trees[t].hps->built()) throw std::invalid_argument("server: tree not built");
+            if (!trees[t].hps || (!trees[t].hps->built() && !trees[t].hps->built32()))
+                throw std::invalid_argument("server: tree not built");
             trees_[t].hps = trees[t].hps;
             trees_[t].bmax = trees[t].bmax;
             Lane l;

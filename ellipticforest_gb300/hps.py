@@ -338,6 +338,12 @@ class HPSAlgorithm:
         self._apply_options()
         check(_lib.load().ef_hps_build(self._h))
 
+    def buildStageMixed(self, fp64_levels: int = 3):
+        """Mixed-precision build (no counterpart in the reference): FP32 merges with the interface
+        LU of the top `fp64_levels` levels in FP64; prepares the tree for mixed_* and Server only."""
+        self._apply_options()
+        check(_lib.load().ef_hps_build_mixed(self._h, int(fp64_levels)))
+
     def upwardsStage(self, rhs, vectorized: bool = True, patch_callback: bool = False):
         """``rhs`` is f(x, y) (sampled at leaf cell centres, HPSAlgorithm.hpp:241-249) or, with
         ``patch_callback=True``, a function that sets ``patch.f`` on each leaf patch."""

@@ -84,6 +84,12 @@ int ef_hps_info(const ef_hps* hps, int* num_leaves, int* leaf_n, int* root_M, lo
 int ef_hps_setup(ef_hps* hps);
 /* HPSAlgorithm::buildStage (HPSAlgorithm.hpp:120-161): leaf DtN maps and all 4-to-1 merges. */
 int ef_hps_build(ef_hps* hps);
+/* Mixed-precision build (no counterpart in the reference): the same merges with FP32 operators,
+ * except the interface LU of the top fp64_levels tree levels (FP64, factors rounded to FP32).  It
+ * prepares the tree for the mixed block solver and the server only (ef_hps_mixed_*, ef_server_*);
+ * the plain FP64 stages need ef_hps_build.  When both builds exist the mixed solver reads the
+ * FP32-built operators. */
+int ef_hps_build_mixed(ef_hps* hps, int fp64_levels);
 /* HPSAlgorithm::upwardsStage (HPSAlgorithm.hpp:225-272) with the load f sampled at leaf cell
  * centres, host array of num_leaves * n * n doubles. */
 int ef_hps_upwards(ef_hps* hps, const double* f_host);

@@ -136,3 +136,26 @@ def test_mixed_five_point_variable_coefficients(ef, level, n):
         assert err <= TOL, (k, err)
     alone = hps.mixed_solve(F[3:4], A[3:4], R[3:4], sweeps=2)
     assert np.array_equal(alone[0], u[3])
+
+
+@pytest.mark.parametrize("kind,n,fp64_levels", [(("uniform", 4), 16, 3), (("uniform", 4), 16, 0),
+                                                 (("adaptive", None, 0, 5), 8, 2)])
+def test_mixed_build_reaches_fp64_solution(ef, kind, n, fp64_levels):
+    """FP32 merges (interface LU of the top levels in FP64) feed the mixed solver; the FP64
+    refinement still reaches the FP64 HPS solution of a separately FP64-built tree."""
+    dom = (-1.0, 1.0, -1.0, 1.0) if kind[0] == "uniform" else (0.0, 1.0, 0.0, 1.0)
+    if kind[0] == "adaptive":
+        kind = ("adaptive", lambda x, y: y > 0.45 and x > 0.45, kind[2], kind[3])
+    mesh, hps64 = make(ef, kind, n, dom)
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, dom[0], dom[1], n, dom[2], dom[3]))
+    mesh32 = (ef.Mesh().uniform(kind[1], root) if kind[0] == "uniform"
+              else ef.Mesh().refineByFunction(kind[1], 0.0, kind[2], kind[3], root))
+    hps32 = ef.HPSAlgorithm(mesh32, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hps32.buildStageMixed(fp64_levels)
+    F, A, R = requests(hps64, mesh, 3, 17)
+    ref = fp64_solutions(hps64, F, A, R)
+    hps32.mixed_init(3)
+    u = hps32.mixed_solve(F, A, R, sweeps=3)
+    for k in range(3):
+        err = np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= TOL, (k, err)
