@@ -285,6 +285,12 @@ int ef_hps_set_stream(ef_hps* h, void* stream) {
     return EF_OK;
 }
 
+int ef_hps_root_factorizations(const ef_hps* h, long long* count) {
+    if (!h || !count) return fail(EF_ERR_INVALID, "null argument");
+    *count = h->hps->root_factorizations();
+    return EF_OK;
+}
+
 int ef_hps_info(const ef_hps* h, int* nleaves, int* n, int* M, long long* bytes) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (nleaves) *nleaves = h->hps->num_leaves();

@@ -219,6 +219,8 @@ public:
     const Mesh& mesh() const { return mesh_; }
     bool built() const { return built_; }
     int singular_count() const { return singular_; }
+    // LU factorisations of the general root matrix diag(a) + diag(b) T so far (cached across solves)
+    long long root_factorizations() const { return root_factorizations_; }
     size_t device_bytes() const { return arena_bytes_; }
 
     // Counters for the roofline: flops of the build by kernel family (FP64).
@@ -276,7 +278,11 @@ private:
     double *d_bca_ = nullptr, *d_bcb_ = nullptr, *d_bcr_ = nullptr;
     // general (b != 0) root solve
     double *d_rootA_ = nullptr, *d_rootrhs_ = nullptr;
-    int *d_rootpiv_ = nullptr, *d_rootperm_ = nullptr, *d_rootinfo_ = nullptr;
+    int *d_rootpiv_ = nullptr, *d_rootperm_ = nullptr, *d_rootinfo_ = nullptr, *d_rootflag_ = nullptr;
+    double *d_roota_ = nullptr, *d_rootb_ = nullptr;  // (a, b) of the cached root LU
+    bool root_lu_valid_ = false;
+    int root_flag_host_ = 0;
+    long long root_factorizations_ = 0;
     double** d_rootA_arr_ = nullptr;
     double** d_rootrhs_arr_ = nullptr;
     int** d_rootpiv_arr_ = nullptr;

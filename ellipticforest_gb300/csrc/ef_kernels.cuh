@@ -273,6 +273,9 @@ void root_assemble(cudaStream_t st, int m, const double* a, const double* b, con
                    double* A);
 void root_rhs(cudaStream_t st, int m, const double* b, const double* r, const double* h,
               const int* perm, double* rhs);
+// flag = 1 when (a, b) equal (a0, b0) bit for bit, else 0
+void root_same(cudaStream_t st, int m, const double* a, const double* b, const double* a0, const double* b0,
+               int* flag);
 
 void fill_zero(cudaStream_t st, double* p, long long n);
 

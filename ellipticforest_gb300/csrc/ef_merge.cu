@@ -355,6 +355,20 @@ __global__ void k_root_rhs(int m, const double* b, const double* r, const double
     }
 }
 
+__global__ void k_root_same(int m, const double* a, const double* b, const double* a0, const double* b0,
+                            int* flag) {
+    __shared__ int diff;
+    if (threadIdx.x == 0) diff = 0;
+    __syncthreads();
+    int d = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+        d |= (__double_as_longlong(a[i]) != __double_as_longlong(a0[i])) |
+             (__double_as_longlong(b[i]) != __double_as_longlong(b0[i]));
+    if (d) atomicOr(&diff, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) *flag = diff ? 0 : 1;
+}
+
 __global__ void k_fill_zero(double* p, long long n) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
          e += (long long)gridDim.x * blockDim.x)
@@ -486,6 +500,12 @@ void root_assemble(cudaStream_t st, int m, const double* a, const double* b, con
 void root_rhs(cudaStream_t st, int m, const double* b, const double* r, const double* h,
               const int* perm, double* rhs) {
     k_root_rhs<<<(m + 255) / 256, 256, 0, st>>>(m, b, r, h, perm, rhs);
+    ++g_kernel_launches;
+}
+
+void root_same(cudaStream_t st, int m, const double* a, const double* b, const double* a0, const double* b0,
+               int* flag) {
+    k_root_same<<<1, 1024, 0, st>>>(m, a, b, a0, b0, flag);
     ++g_kernel_launches;
 }
 

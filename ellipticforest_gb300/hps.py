@@ -8,6 +8,7 @@ this module only samples the user's callbacks at the reference's sampling points
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Callable, Optional
 
 import numpy as np
@@ -182,6 +183,47 @@ class FiniteVolumeNodeFactory:
     (midpoint halving, FiniteVolumeNodeFactory.cpp:15-66)."""
 
 
+def _vtk_array(fh, vtype, name, comps, values):
+    v = np.asarray(values)
+    lo, hi = (float(v.min()), float(v.max())) if v.size else (0.0, 0.0)
+    fh.write(f'        <DataArray type="{vtype}" Name="{name}" NumberOfComponents="{comps}" format="ascii" '
+             f'RangeMin="{lo!r}" RangeMax="{hi!r}">\n')
+    fh.write(" ".join(repr(float(x)) if vtype.startswith("Float") else str(int(x)) for x in v.ravel()))
+    fh.write("\n        </DataArray>\n")
+
+
+def _write_quad_vtu(filename, corners, funcs):
+    """VTK XML unstructured grid of quads; corners [ncells, 8] = (x, y) of 4 corners per cell."""
+    nc = corners.shape[0]
+    pts = np.zeros((4 * nc, 3))
+    pts[:, :2] = corners.reshape(4 * nc, 2)
+    with open(filename, "w") as fh:
+        fh.write('<?xml version="1.0"?>\n<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian">\n'
+                 f'  <UnstructuredGrid>\n    <Piece NumberOfPoints="{4 * nc}" NumberOfCells="{nc}">\n      <Points>\n')
+        _vtk_array(fh, "Float64", "Points", 3, pts)
+        fh.write("      </Points>\n      <Cells>\n")
+        _vtk_array(fh, "Int64", "connectivity", 1, np.arange(4 * nc))
+        _vtk_array(fh, "Int64", "offsets", 1, 4 * np.arange(1, nc + 1))
+        _vtk_array(fh, "UInt8", "types", 1, np.full(nc, 9))
+        fh.write("      </Cells>\n      <CellData>\n")
+        for name, v in funcs:
+            if v.size != nc:
+                raise ValueError(f"toVTK: cell data {name!r} has {v.size} values for {nc} cells")
+            _vtk_array(fh, "Float64", name, 1, v)
+        fh.write("      </CellData>\n    </Piece>\n  </UnstructuredGrid>\n</VTKFile>\n")
+
+
+def _write_pvtu(filename, piece, funcs):
+    with open(filename, "w") as fh:
+        fh.write('<?xml version="1.0"?>\n<VTKFile type="PUnstructuredGrid" version="0.1" byte_order="LittleEndian">\n'
+                 '  <PUnstructuredGrid GhostLevel="0">\n    <PPoints>\n'
+                 '      <PDataArray type="Float64" Name="Points" NumberOfComponents="3"/>\n    </PPoints>\n'
+                 '    <PCellData>\n')
+        for name, _ in funcs:
+            fh.write(f'      <PDataArray type="Float64" Name="{name}" NumberOfComponents="1"/>\n')
+        fh.write(f'    </PCellData>\n    <Piece Source="{piece}"/>\n  </PUnstructuredGrid>\n</VTKFile>\n')
+
+
 class Mesh:
     """Mesh<FiniteVolumePatch> (Mesh.hpp) backed by the library's flat quadtree."""
 
@@ -238,6 +280,44 @@ class Mesh:
         v = C.c_int()
         check(_lib.load().ef_mesh_num_leaves(self._h, C.byref(v)))
         return v.value
+
+    # -- VTK output (Mesh.hpp:357-424) -------------------------------------------------------------
+    def addMeshFunction(self, values, name: Optional[str] = None):
+        """Cell data for toVTK: an array in leaf order (cell j + i*n, e.g. HPSAlgorithm.leaf_solution())
+        or a vectorised f(x, y) sampled at the leaf cell centres."""
+        if not hasattr(self, "_mesh_functions"):
+            self._mesh_functions = []
+        if callable(values):
+            X, Y = self.cell_centres()
+            values = values(X, Y)
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        self._mesh_functions.append((name or f"mesh_function_{len(self._mesh_functions)}", v))
+
+    def clearMeshFunctions(self):
+        self._mesh_functions = []
+
+    def toVTK(self, baseFilename: str, number: int = -1):
+        """<base>-mesh[-NNNN].pvtu + -0.vtu (one quad per leaf cell, mesh functions as cell data) and
+        <base>-quadtree[-NNNN].vtu (one quad per leaf patch with its level), VTK XML, ASCII."""
+        tag = "" if number == -1 else f"-{number:04d}"
+        n = self.root_patch.grid().nx()
+        corners, boxes, levels = [], [], []
+        for k, p in enumerate(self.patches):
+            g = p.grid()
+            x0 = g.xLower() + np.arange(n) * g.dx()
+            y0 = g.yLower() + np.arange(n) * g.dy()
+            X0, Y0 = np.meshgrid(x0, y0, indexing="ij")
+            X0, Y0 = X0.ravel(), Y0.ravel()
+            corners.append(np.stack([X0, Y0, X0 + g.dx(), Y0, X0 + g.dx(), Y0 + g.dy(), X0, Y0 + g.dy()], axis=1))
+            boxes.append([g.xLower(), g.yLower(), g.xUpper(), g.yLower(), g.xUpper(), g.yUpper(), g.xLower(), g.yUpper()])
+            levels.append(self.leaf(k)[0])
+        funcs = getattr(self, "_mesh_functions", [])
+        mesh = f"{baseFilename}-mesh{tag}"
+        _write_quad_vtu(mesh + "-0.vtu", np.concatenate(corners), funcs)
+        _write_pvtu(mesh + ".pvtu", os.path.basename(mesh) + "-0.vtu", funcs)
+        nl = len(self.patches)
+        _write_quad_vtu(f"{baseFilename}-quadtree{tag}.vtu", np.array(boxes, dtype=np.float64).reshape(nl, 8),
+                        [("level", np.array(levels, dtype=np.float64)), ("leaf", np.arange(nl, dtype=np.float64))])
 
     def num_nodes(self) -> int:
         v = C.c_int()
@@ -325,6 +405,13 @@ class HPSAlgorithm:
 
     def set_stream(self, cuda_stream_ptr: int):
         check(_lib.load().ef_hps_set_stream(self._h, C.c_void_p(cuda_stream_ptr)))
+
+    @property
+    def root_factorizations(self) -> int:
+        """LU factorisations of the general root matrix so far (reused while a and b are unchanged)."""
+        v = C.c_longlong()
+        check(_lib.load().ef_hps_root_factorizations(self._h, C.byref(v)))
+        return v.value
 
     def set_graphs(self, on: bool):
         """CUDA-graph replay of the device-resident solve sequences (default on)."""

@@ -5,6 +5,8 @@
 // library's refine-and-balance (ef_mesh_create_refined); the nodes are host objects for drivers.
 #pragma once
 
+#include "VTK.hpp"
+
 #include <algorithm>
 #include <map>
 #include <memory>
@@ -202,6 +204,55 @@ public:
     // leaves in pre-order (the order of the library's leaf arrays)
     std::vector<Node<PatchType>*>& leaves() { return leaves_; }
 
+    // Mesh.hpp:357-390: cell data for toVTK, in leaf order with cell index j + i*ny (as vectorU)
+    void addMeshFunction(Vector<double>& meshFunction) {
+        const std::string nm = meshFunction.name().empty() ? "mesh_function_" + std::to_string(mesh_functions_.size())
+                                                           : meshFunction.name();
+        mesh_functions_.push_back(VTKCellArray{nm, meshFunction.data()});
+    }
+    void addMeshFunction(std::function<double(double x, double y)> meshFunction, std::string meshFunctionName) {
+        VTKCellArray a{meshFunctionName, {}};
+        iterateCells([&](double x, double y) { a.values.push_back(meshFunction(x, y)); });
+        mesh_functions_.push_back(std::move(a));
+    }
+    void clearMeshFunctions() { mesh_functions_.clear(); }
+
+    // Mesh.hpp:398-424: <base>-mesh[-NNNN].pvtu with its piece <base>-mesh[-NNNN]-0.vtu (one quad per
+    // leaf cell, the added mesh functions as cell data) and <base>-quadtree[-NNNN].vtu (one quad per leaf
+    // patch, its level and leaf index as cell data).
+    void toVTK(std::string baseFilename, int number = -1) {
+        std::string tag;
+        if (number != -1) {
+            char buffer[32];
+            std::snprintf(buffer, sizeof(buffer), "-%04i", number);
+            tag = buffer;
+        }
+        std::vector<double> cells, boxes;
+        std::vector<double> level, index;
+        for (std::size_t k = 0; k < leaves_.size(); ++k) {
+            auto& g = leaves_[k]->data.grid();
+            const double dx = g.dx(), dy = g.dy();
+            for (std::size_t i = 0; i < g.nx(); ++i)
+                for (std::size_t j = 0; j < g.ny(); ++j) {
+                    const double x0 = g.xLower() + i * dx, y0 = g.yLower() + j * dy;
+                    const double q[8] = {x0, y0, x0 + dx, y0, x0 + dx, y0 + dy, x0, y0 + dy};
+                    cells.insert(cells.end(), q, q + 8);
+                }
+            const double b[8] = {g.xLower(), g.yLower(), g.xUpper(), g.yLower(), g.xUpper(), g.yUpper(), g.xLower(),
+                                 g.yUpper()};
+            boxes.insert(boxes.end(), b, b + 8);
+            level.push_back(double(leaves_[k]->level));
+            index.push_back(double(k));
+        }
+        const std::string mesh = baseFilename + "-mesh" + tag;
+        const std::size_t slash = mesh.find_last_of('/');
+        writeQuadVTU(mesh + "-0.vtu", cells, mesh_functions_);
+        writePVTU(mesh + ".pvtu", (slash == std::string::npos ? mesh : mesh.substr(slash + 1)) + "-0.vtu",
+                  mesh_functions_);
+        writeQuadVTU(baseFilename + "-quadtree" + tag + ".vtu", boxes,
+                     {VTKCellArray{"level", level}, VTKCellArray{"leaf", index}});
+    }
+
 private:
     static int tramp(double x, double y, void* ctx) {
         return (*static_cast<std::function<bool(double, double)>*>(ctx))(x, y) ? 1 : 0;
@@ -251,6 +302,7 @@ private:
 
     ef_mesh* handle_ = nullptr;
     std::vector<Node<PatchType>*> leaves_;
+    std::vector<VTKCellArray> mesh_functions_;
 };
 
 }  // namespace EllipticForest

@@ -79,6 +79,10 @@ int ef_hps_set_option(ef_hps* hps, const char* key, int value);
 /* Use an external CUDA stream (cudaStream_t) for all work of this handle; NULL = default stream. */
 int ef_hps_set_stream(ef_hps* hps, void* cuda_stream);
 int ef_hps_info(const ef_hps* hps, int* num_leaves, int* leaf_n, int* root_M, long long* device_bytes);
+/* Number of LU factorisations of the general root matrix diag(a) + diag(b) T_root made so far.  The
+ * reference factors it on every solve with b != 0 (HPSAlgorithm.hpp:402-420); here the factors are
+ * reused while a and b are bit-identical to the last factored pair and the tree was not rebuilt. */
+int ef_hps_root_factorizations(const ef_hps* hps, long long* count);
 
 /* HPSAlgorithm::setupStage (HPSAlgorithm.hpp:91-106): nothing to do; validates the handle. */
 int ef_hps_setup(ef_hps* hps);

@@ -1,8 +1,9 @@
 // Driver written against the C++ drop-in exactly as a reference user would (the API sequence of
 // the reference's examples/elliptic-single: app + options, grid and root patch, node factory,
 // Mesh::refineByFunction, FiniteVolumeSolver, HPSAlgorithm setup/build/upwards/solve, traversal of
-// the leaf patches).  Solves  u_xx + u_yy = f  with u = sin x + sin y and writes the leaf solutions
-// (pre-order leaf order, cell j + i*ny) to the file given by --out=<path>.
+// the leaf patches, Mesh::toVTK).  Solves  u_xx + u_yy = f  with u = sin x + sin y and writes the
+// leaf solutions (pre-order leaf order, cell j + i*ny) to the file given by --out=<path>, and the VTK
+// files <path>-vtk-mesh.pvtu / -mesh-0.vtu / -quadtree.vtu.
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -72,6 +73,11 @@ int main(int argc, char** argv) {
         }
         return 1;
     });
+    // Mesh::toVTK as in the reference's examples: the leaf solution and the exact solution as cell data
+    uMesh.name() = "u";
+    mesh.addMeshFunction(uMesh);
+    mesh.addMeshFunction([](double x, double y) { return uExact(x, y); }, "u_exact");
+    mesh.toVTK(out + "-vtk");
     std::FILE* fp = std::fopen(out.c_str(), "wb");
     if (!fp) return 2;
     std::fwrite(uMesh.dataPointer(), sizeof(double), uMesh.size(), fp);

@@ -59,3 +59,14 @@ def test_dropin_driver_matches_oracle(driver, tmp_path, n, lo, hi, min_level, ma
     uo = _oracle(n, lo, hi, min_level, max_level)
     assert u.size == uo.size == info["dofs"]
     assert np.abs(u - uo).max() <= 1e-12 * np.abs(uo).max()
+    # Mesh::toVTK: one quad per leaf cell with the solution as cell data, one quad per leaf patch
+    import xml.etree.ElementTree as ET
+    piece = ET.parse(f"{out}-vtk-mesh-0.vtu").getroot().find("UnstructuredGrid/Piece")
+    assert int(piece.get("NumberOfCells")) == u.size
+    arrays = {a.get("Name"): a for a in piece.iter("DataArray")}
+    uv = np.array(arrays["u"].text.split(), dtype=np.float64)
+    assert np.array_equal(uv, u)
+    assert "u_exact" in arrays and arrays["types"].text.split()[0] == "9"
+    assert ET.parse(f"{out}-vtk-mesh.pvtu").getroot().find("PUnstructuredGrid/Piece").get("Source").endswith("-0.vtu")
+    quad = ET.parse(f"{out}-vtk-quadtree.vtu").getroot().find("UnstructuredGrid/Piece")
+    assert int(quad.get("NumberOfCells")) == info["leaves"]

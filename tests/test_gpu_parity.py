@@ -313,3 +313,34 @@ def test_linearity_large(ef):
         hps.solveStage(bc)
         sols.append(hps.leaf_solution())
     assert rel(sols[0] + sols[1], sols[2]) <= 1e-12
+
+
+def test_robin_root_lu_is_reused_while_a_b_are_unchanged(ef):
+    """Repeated Robin solves on one tree: the general root matrix is factored once while (a, b) stay
+    the same, each result still matches the oracle, and changing b re-factors it."""
+    dom = (0.0, 2.0, 0.0, 2.0)
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(4, *dom))
+    mesh = ef.Mesh().uniform(3, root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hps.buildStage()
+    M = hps.M
+    a, b = np.ones(4 * M), np.full(4 * M, 0.25)
+    rng = np.random.default_rng(8)
+    X, Y = mesh.cell_centres()
+    base = hps.root_factorizations
+    for k in range(3):
+        f = np.sin(X + k) * np.cos(Y)
+        r = rng.standard_normal(4 * M)
+        hps.upwards_array(f)
+        hps.solve_arrays(a, b, r)
+        u = hps.leaf_solution()
+        om = O.Mesh().uniform(3, O.FiniteVolumePatch(O.FiniteVolumeGrid(4, *dom)))
+        oh = O.HPSAlgorithm(om, O.FiniteVolumeSolver(solver_type=O.FISHPACK90))
+        oh.buildStage()
+        oh.upwards_with_data(f)
+        oh.solve_with_data(a, b, r)
+        assert rel(u, O.leaf_solution(oh)) <= REL
+    assert hps.root_factorizations - base == 1
+    hps.upwards_array(np.sin(X))
+    hps.solve_arrays(a, np.full(4 * M, 0.5), rng.standard_normal(4 * M))
+    assert hps.root_factorizations - base == 2
