@@ -329,6 +329,30 @@ int ef_hps_build_mixed(ef_hps* h, int fp64_levels) {
     });
 }
 
+int ef_hps_save(const ef_hps* h, const char* path) {
+    if (!h || !path) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->hps->built()) return fail(EF_ERR_STATE, "save before build stage");
+    return guarded([&] {
+        h->hps->save(path);
+        return EF_OK;
+    });
+}
+
+int ef_hps_load(const char* path, ef_mesh** mesh_out, ef_hps** hps_out) {
+    if (!path || !mesh_out || !hps_out) return fail(EF_ERR_INVALID, "null argument");
+    *mesh_out = nullptr;
+    *hps_out = nullptr;
+    return guarded([&] {
+        auto h = std::make_unique<ef_hps>();
+        h->hps = efgb::Hps::load(path);
+        auto m = std::make_unique<ef_mesh>();
+        m->mesh = h->hps->mesh();
+        *mesh_out = m.release();
+        *hps_out = h.release();
+        return EF_OK;
+    });
+}
+
 int ef_hps_upwards(ef_hps* h, const double* f_host) {
     if (!h || !f_host) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "upwards stage before build stage");

@@ -10,6 +10,7 @@
 
 #include <array>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -196,6 +197,9 @@ public:
     // the FP32 operator set the mixed block solver reads; the plain FP64 solve needs build().
     void build_mixed(int fp64_levels);
     bool built32() const { return built32_; }
+    // A built tree's solve-time operators to a file and back (ef_serial.cpp).
+    void save(const char* path) const;
+    static std::unique_ptr<Hps> load(const char* path);
     void upwards();                                // HPSAlgorithm::upwardsStage on leaf_f()
     void root_from_bc();                           // root g from bc_a/b/r (HPSAlgorithm.hpp:402-420)
     void downwards();                              // split1to4 + leafSolve for every node

@@ -378,6 +378,36 @@ class HPSAlgorithm:
         if patch_solver.solver_type == FivePointStencil:
             self._set_coefficients()
 
+    def save(self, path: str):
+        """Solve-time operators of the built tree and its mesh to `path` (no reference counterpart)."""
+        check(_lib.load().ef_hps_save(self._h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path: str) -> "HPSAlgorithm":
+        """A built tree saved by save(): its mesh and a handle that solves without re-merging."""
+        lib = _lib.load()
+        mh, hh = C.c_void_p(), C.c_void_p()
+        check(lib.ef_hps_load(str(path).encode(), C.byref(mh), C.byref(hh)))
+        self = cls.__new__(cls)
+        self._h = hh
+        nl, n, M, nb = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        check(lib.ef_hps_info(hh, C.byref(nl), C.byref(n), C.byref(M), C.byref(nb)))
+        self.num_leaves, self.n, self.M, self.device_bytes = nl.value, n.value, M.value, nb.value
+        mesh = Mesh()
+        mesh._h = mh
+        boxes = []
+        for k in range(nl.value):
+            boxes.append(mesh.leaf(k)[3])
+        bx = np.array(boxes)
+        mesh.root_patch = FiniteVolumePatch(FiniteVolumeGrid(n.value, bx[:, 0].min(), bx[:, 1].max(), n.value,
+                                                             bx[:, 2].min(), bx[:, 3].max()))
+        mesh.patches = [FiniteVolumePatch(FiniteVolumeGrid(n.value, b[0], b[1], n.value, b[2], b[3])) for b in boxes]
+        self.mesh = mesh
+        self.patch_solver = FiniteVolumeSolver(solver_type=FISHPACK90)
+        self.options = {"cache-operators": False, "homogeneous-rhs": False}
+        self._apply_options()
+        return self
+
     def _set_coefficients(self):
         """Samples alpha, beta, lambda on every leaf (FiniteVolumeSolver.cpp:66-79) into the library."""
         parts = [sample_coefficients(self.patch_solver, p.grid()) for p in self.mesh.patches]

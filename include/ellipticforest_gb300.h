@@ -94,6 +94,13 @@ int ef_hps_build(ef_hps* hps);
  * the plain FP64 stages need ef_hps_build.  When both builds exist the mixed solver reads the
  * FP32-built operators. */
 int ef_hps_build_mixed(ef_hps* hps, int fp64_levels);
+
+/* Save a built tree's solve-time operators (every merge node's T, [S | X^-1] and compact H; for
+ * FivePointStencil leaves also their coefficients and band LU factors) with its mesh to `path`, and
+ * load it back into a new mesh and a built handle that solves bit-identically without re-merging.
+ * No counterpart in the reference.  A damaged file returns EF_ERR_INVALID (checksummed payload). */
+int ef_hps_save(const ef_hps* hps, const char* path);
+int ef_hps_load(const char* path, ef_mesh** mesh_out, ef_hps** hps_out);
 /* HPSAlgorithm::upwardsStage (HPSAlgorithm.hpp:225-272) with the load f sampled at leaf cell
  * centres, host array of num_leaves * n * n doubles. */
 int ef_hps_upwards(ef_hps* hps, const double* f_host);

@@ -319,7 +319,7 @@ def test_robin_root_lu_is_reused_while_a_b_are_unchanged(ef):
     """Repeated Robin solves on one tree: the general root matrix is factored once while (a, b) stay
     the same, each result still matches the oracle, and changing b re-factors it."""
     dom = (0.0, 2.0, 0.0, 2.0)
-    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(4, *dom))
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(4, dom[0], dom[1], 4, dom[2], dom[3]))
     mesh = ef.Mesh().uniform(3, root)
     hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
     hps.buildStage()
@@ -334,7 +334,7 @@ def test_robin_root_lu_is_reused_while_a_b_are_unchanged(ef):
         hps.upwards_array(f)
         hps.solve_arrays(a, b, r)
         u = hps.leaf_solution()
-        om = O.Mesh().uniform(3, O.FiniteVolumePatch(O.FiniteVolumeGrid(4, *dom)))
+        om = O.Mesh().uniform(3, O.FiniteVolumePatch(O.FiniteVolumeGrid(4, dom[0], dom[1], 4, dom[2], dom[3])))
         oh = O.HPSAlgorithm(om, O.FiniteVolumeSolver(solver_type=O.FISHPACK90))
         oh.buildStage()
         oh.upwards_with_data(f)
@@ -344,3 +344,40 @@ def test_robin_root_lu_is_reused_while_a_b_are_unchanged(ef):
     hps.upwards_array(np.sin(X))
     hps.solve_arrays(a, np.full(4 * M, 0.5), rng.standard_normal(4 * M))
     assert hps.root_factorizations - base == 2
+
+
+@pytest.mark.parametrize("solver", ["fishpack", "five_point"])
+def test_save_load_solves_bit_identically(ef, tmp_path, solver):
+    """A built tree saved to a file and loaded into a new handle solves bit for bit like the
+    original, without re-merging; a damaged file is rejected."""
+    if solver == "fishpack":
+        root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(8, -1.0, 1.0, 8, -1.0, 1.0))
+        mesh = ef.Mesh().refineByFunction(lambda x, y: x * x + y * y < 0.3, 0.0, 1, 4, root)
+        hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    else:
+        root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(8, -1.0, 1.0, 8, -1.0, 1.0))
+        mesh = ef.Mesh().uniform(2, root)
+        hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(
+            beta_function=lambda x, y: 1.0 + 0.5 * np.sin(np.pi * x) * np.cos(np.pi * y),
+            lambda_function=lambda x, y: -1.0 + 0.0 * x, solver_type=ef.FivePointStencil))
+    hps.buildStage()
+    X, Y = mesh.cell_centres()
+    f = np.sin(3 * X) * np.cos(2 * Y)
+    r = np.concatenate([np.cos(x + 2 * y) for x, y in hps.boundary_points()])
+    a = np.ones_like(r)
+    hps.upwards_array(f)
+    hps.solve_arrays(a, np.zeros_like(a), r)
+    u = hps.leaf_solution()
+    path = tmp_path / "tree.efgb"
+    hps.save(path)
+    h2 = ef.HPSAlgorithm.load(path)
+    assert h2.num_leaves == hps.num_leaves and h2.M == hps.M
+    h2.upwards_array(f)
+    h2.solve_arrays(a, np.zeros_like(a), r)
+    assert np.array_equal(h2.leaf_solution(), u)
+    blob = bytearray(path.read_bytes())
+    blob[len(blob) // 2] ^= 0x40
+    bad = tmp_path / "bad.efgb"
+    bad.write_bytes(bytes(blob))
+    with pytest.raises(RuntimeError):
+        ef.HPSAlgorithm.load(bad)
