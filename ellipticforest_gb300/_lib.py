@@ -69,6 +69,7 @@ SIGNATURES = {
     "ef_hps_build_mixed": (C.c_int, [_vp, C.c_int]),
     "ef_hps_root_factorizations": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
     "ef_hps_save": (C.c_int, [_vp, C.c_char_p]),
+    "ef_hps_build_from": (C.c_int, [_vp, _vp, C.POINTER(C.c_int)]),
     "ef_hps_load": (C.c_int, [C.c_char_p, C.POINTER(_vp), C.POINTER(_vp)]),
     "ef_server_create": (C.c_int, [C.POINTER(_vp), C.POINTER(C.c_int), C.c_int, C.c_int, C.c_longlong, C.c_int,
                                    C.POINTER(_vp)]),

@@ -329,6 +329,19 @@ int ef_hps_build_mixed(ef_hps* h, int fp64_levels) {
     });
 }
 
+int ef_hps_build_from(ef_hps* h, const ef_hps* old, int* reused) {
+    if (!h || !old) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        h->mixed.reset();
+        h->hps->build_from(*old->hps);
+        if (reused) *reused = h->hps->reused_merges();
+        if (h->hps->singular_count() > 0)
+            return fail(EF_ERR_SINGULAR, std::to_string(h->hps->singular_count()) +
+                                             " interface matrices had a zero pivot (dgesv INFO != 0)");
+        return EF_OK;
+    });
+}
+
 int ef_hps_save(const ef_hps* h, const char* path) {
     if (!h || !path) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "save before build stage");

@@ -197,6 +197,10 @@ public:
     // the FP32 operator set the mixed block solver reads; the plain FP64 solve needs build().
     void build_mixed(int fp64_levels);
     bool built32() const { return built32_; }
+    // Local re-factorisation after a mesh change (ef_incremental.cpp): merge nodes whose subtree is the
+    // same in `old` copy its operators, the others merge; equal to build() bit for bit.
+    void build_from(const Hps& old);
+    int reused_merges() const { return reused_; }
     // A built tree's solve-time operators to a file and back (ef_serial.cpp).
     void save(const char* path) const;
     static std::unique_ptr<Hps> load(const char* path);
@@ -331,6 +335,7 @@ private:
     char* arena32_ = nullptr;
     size_t arena32_bytes_ = 0;
     bool built32_ = false;
+    int reused_ = 0;
 
     bool prof_ = false;
     bool graphs_ = true;

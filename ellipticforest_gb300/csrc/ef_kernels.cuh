@@ -278,5 +278,7 @@ void root_same(cudaStream_t st, int m, const double* a, const double* b, const d
                int* flag);
 
 void fill_zero(cudaStream_t st, double* p, long long n);
+// dst[k][0..len[k]) = src[k][0..len[k]) for k < count
+void copy_batched(cudaStream_t st, const double* const* src, double* const* dst, const long long* len, int count);
 
 }  // namespace efgb

@@ -369,6 +369,14 @@ __global__ void k_root_same(int m, const double* a, const double* b, const doubl
     if (threadIdx.x == 0) *flag = diff ? 0 : 1;
 }
 
+__global__ void k_copy_batched(const double* const* src, double* const* dst, const long long* len) {
+    const double* a = src[blockIdx.y];
+    double* b = dst[blockIdx.y];
+    const long long n = len[blockIdx.y];
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        b[e] = a[e];
+}
+
 __global__ void k_fill_zero(double* p, long long n) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
          e += (long long)gridDim.x * blockDim.x)
@@ -507,6 +515,14 @@ void root_same(cudaStream_t st, int m, const double* a, const double* b, const d
                int* flag) {
     k_root_same<<<1, 1024, 0, st>>>(m, a, b, a0, b0, flag);
     ++g_kernel_launches;
+}
+
+void copy_batched(cudaStream_t st, const double* const* src, double* const* dst, const long long* len, int count) {
+    for (int k0 = 0; k0 < count; k0 += 65535) {
+        const int c = count - k0 < 65535 ? count - k0 : 65535;
+        k_copy_batched<<<dim3(64, c), 256, 0, st>>>(src + k0, dst + k0, len + k0);
+        ++g_kernel_launches;
+    }
 }
 
 void fill_zero(cudaStream_t st, double* p, long long n) {

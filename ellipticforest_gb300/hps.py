@@ -455,6 +455,14 @@ class HPSAlgorithm:
         self._apply_options()
         check(_lib.load().ef_hps_build(self._h))
 
+    def buildStageFrom(self, old: "HPSAlgorithm") -> int:
+        """Build reusing the merges of `old` (a built tree on another mesh of the same domain) whose
+        subtrees are unchanged; returns the number of reused merges (no reference counterpart)."""
+        self._apply_options()
+        n = C.c_int()
+        check(_lib.load().ef_hps_build_from(self._h, old._h, C.byref(n)))
+        return n.value
+
     def buildStageMixed(self, fp64_levels: int = 3):
         """Mixed-precision build (no counterpart in the reference): FP32 merges with the interface
         LU of the top `fp64_levels` levels in FP64; prepares the tree for mixed_* and Server only."""

@@ -95,6 +95,14 @@ int ef_hps_build(ef_hps* hps);
  * FP32-built operators. */
 int ef_hps_build_mixed(ef_hps* hps, int fp64_levels);
 
+/* Local re-factorisation after a mesh change (no counterpart in the reference; it rebuilds every
+ * merge): build `hps`, created on a new mesh of the same domain, patch size and lambda, reusing the
+ * operators of every merge node whose subtree is unchanged in the built `old` handle; only the
+ * changed nodes (the ancestors of changed leaves) merge.  The operators equal those of
+ * ef_hps_build bit for bit.  FISHPACK90 leaves.  `reused` (may be NULL) receives the number of
+ * merges copied from `old`. */
+int ef_hps_build_from(ef_hps* hps, const ef_hps* old, int* reused);
+
 /* Save a built tree's solve-time operators (every merge node's T, [S | X^-1] and compact H; for
  * FivePointStencil leaves also their coefficients and band LU factors) with its mesh to `path`, and
  * load it back into a new mesh and a built handle that solves bit-identically without re-merging.
