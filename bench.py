@@ -19,6 +19,7 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
             against the exact solution, and the mixed block form
   variable_coefficient_L5 -- config 3 (FivePointStencil leaves, variable beta): build, plain FP64
             solves/s, discretisation error, and the mixed block form against the FP64 HPS
+  incremental_rebuild -- a localised mesh change re-merged from the config-2 tree vs a fresh build
   mixed_build -- FP32 merges with the interface LU of the top 3 levels in FP64 (uniform L7, config
             2): build seconds, the FP64 sweeps needed for 1e-10 and the block rate
   serving -- 2000 Poisson-arrival requests over three resident trees (uniform L4, adaptive max level
@@ -459,6 +460,7 @@ def run_gb300(args):
         extras["many_rhs_L6"] = many_rhs(ef, torch, stream, args)
         c2 = build_config2(ef, torch, stream)
         extras["adaptive_L7"] = adaptive(ef, torch, stream, args, c2)
+        extras["incremental_rebuild"] = incremental(ef, torch, stream, c2)
         extras["serving"] = serving(ef, torch, stream, (mesh, hps), args, c2)
         extras["mixed_build"] = mixed_build(ef, torch, stream, args, (mesh, hps, DOM, build_s),
                                             (c2[0], c2[1], (-10.0, 10.0, -10.0, 10.0), c2[2]))
@@ -665,6 +667,37 @@ def mixed_build(ef, torch, stream, args, main, c2):
                      "sweeps_for_1e-10": sweeps, "rel_err_vs_fp64": err, "block_solves_per_s": rate}
         del hps
     return out
+
+
+def incremental(ef, torch, stream, c2):
+    """Local re-factorisation: the config-2 tree after an extra refined disk (a localised mesh change)
+    built fresh and incrementally from the config-2 tree (operators of unchanged subtrees reused)."""
+    _, old, _ = c2
+    pred = lambda x, y: abs(np.sin(x) + np.sin(y)) > 1.2 or (x - 3.0) ** 2 + (y - 3.0) ** 2 < 0.5
+
+    def tree():
+        rc = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -10.0, 10.0, 16, -10.0, 10.0))
+        mesh = ef.Mesh().refineByFunction(pred, 1.2, 0, 7, rc)
+        h = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+        h.set_stream(stream.cuda_stream)
+        return mesh, h
+    mesh, fresh = tree()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fresh.buildStage()
+    torch.cuda.synchronize()
+    t_fresh = time.perf_counter() - t0
+    _, inc = tree()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reused = inc.buildStageFrom(old)
+    torch.cuda.synchronize()
+    t_inc = time.perf_counter() - t0
+    same = bool(np.array_equal(fresh.root_T(), inc.root_T()))
+    return {"workload": "config-2 tree plus a refined disk (x-3)^2+(y-3)^2 < 0.5 at level 7",
+            "leaves": fresh.num_leaves, "merges": mesh.num_nodes() - mesh.num_leaves(), "reused_merges": reused,
+            "fresh_build_s": t_fresh, "incremental_build_s": t_inc, "speedup": t_fresh / t_inc,
+            "root_T_bit_identical": same}
 
 
 def serving(ef, torch, stream, main_tree, args, c2):
