@@ -28,6 +28,8 @@ namespace efgb {
 
 // Number of kernels this library has launched (all handles, all streams).
 extern std::atomic<long long> g_kernel_launches;
+// LU panels of matrices with >= 512 rows left use the cooperative multi-CTA panel (default on)
+extern std::atomic<bool> g_cooperative_lu;
 
 // ------------------------------------------------------------------------------------------------
 // Batched FP64 dense linear algebra (pointer arrays, uniform shapes and offsets per launch)

@@ -3,6 +3,9 @@
 // Replaces the reference's per-node LAPACK/BLAS calls (Matrix.hpp:789-952: dgemv, dgemm and dgesv
 // on transposed copies) with grouped launches over every merge of one tree level.  On GB300 the
 // FP64 pipe, not HBM, bounds these kernels; they are tiled for register reuse.
+#include <cooperative_groups.h>
+
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -11,6 +14,7 @@
 namespace efgb {
 
 std::atomic<long long> g_kernel_launches{0};
+std::atomic<bool> g_cooperative_lu{true};
 
 namespace {
 
@@ -159,6 +163,136 @@ __global__ void __launch_bounds__(1024) k_getf2_panel(int n, int k, int jb, Real
     }
 }
 
+// Panel LU of large matrices spread over P CTAs per matrix (cooperative launch, one grid-wide barrier
+// per column).  Rows are not moved during the panel: every CTA owns a slice of the physical rows and
+// keeps their logical positions and "not yet a pivot" flags, so the pivot search, the scaling and the
+// rank-1 updates are those of the single-CTA kernel (ties go to the smaller logical index, as in
+// idamax); piv holds the LAPACK swap sequence, applied to the panel columns afterwards.
+constexpr int kCoopRows = 1024;  // rows per CTA at most (shared memory for their bookkeeping)
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_getf2_coop(int n, int k, int jb, Real* const* Aarr, int lda,
+                                                    int* const* pivarr, int* info, int P, Real* pval, int* ppos) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const int mat = blockIdx.x / P, part = blockIdx.x - mat * P;
+    Real* __restrict__ A = Aarr[mat];
+    int* __restrict__ piv = pivarr[mat];
+    const int rows = n - k, per = (rows + P - 1) / P;
+    const int r0 = k + part * per, r1 = min(n, r0 + per);
+    __shared__ int lpos[kCoopRows];
+    __shared__ unsigned char act[kCoopRows];
+    __shared__ Real s_val[32];
+    __shared__ int s_idx[32];
+    __shared__ int s_phys[32];
+    __shared__ Real s_prow[32];
+    __shared__ int s_pphys, s_plog;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    for (int r = r0 + tid; r < r1; r += blockDim.x) {
+        lpos[r - r0] = r;
+        act[r - r0] = 1;
+    }
+    __syncthreads();
+    // (value, logical index) of the largest |A[r][j]| over this CTA's active rows
+    // (value, logical index, physical row) of the largest |A[r][j]| over this CTA's active rows, to
+    // the candidate tables (logical indices in ppos slots 0/1, physical rows in slots 2/3)
+    auto local_max = [&](int j, int slot) {
+        Real best = Real(-1);
+        int bi = INT_MAX, bp = -1;
+        for (int r = r0 + tid; r < r1; r += blockDim.x) {
+            if (!act[r - r0]) continue;
+            const Real v = fabs(A[(long long)r * lda + j]);
+            const int li = lpos[r - r0];
+            if (v > best || (v == best && li < bi)) { best = v; bi = li; bp = r; }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const Real ov = __shfl_down_sync(0xffffffffu, best, off);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            const int op = __shfl_down_sync(0xffffffffu, bp, off);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; bp = op; }
+        }
+        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; s_phys[wid] = bp; }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < nw; ++w)
+                if (s_val[w] > best || (s_val[w] == best && s_idx[w] < bi)) { best = s_val[w]; bi = s_idx[w]; bp = s_phys[w]; }
+            pval[((long long)slot * gridDim.x) + blockIdx.x] = best;
+            ppos[((long long)slot * gridDim.x) + blockIdx.x] = bi;
+            ppos[((long long)(2 + slot) * gridDim.x) + blockIdx.x] = bp;
+        }
+        __syncthreads();
+    };
+    local_max(k, 0);
+    for (int j = k; j < k + jb; ++j) {
+        const int slot = (j - k) & 1;
+        grid.sync();
+        // every CTA of the matrix reduces the P candidates the same way; the owner of the pivot row
+        // publishes its physical index through the candidate table
+        if (tid == 0) {
+            Real best = Real(-1);
+            int bi = INT_MAX, bp = -1;
+            for (int t = 0; t < P; ++t) {
+                const Real v = pval[(long long)slot * gridDim.x + mat * P + t];
+                const int li = ppos[(long long)slot * gridDim.x + mat * P + t];
+                if (v > best || (v == best && li < bi)) {
+                    best = v;
+                    bi = li;
+                    bp = ppos[(long long)(2 + slot) * gridDim.x + mat * P + t];
+                }
+            }
+            s_plog = bi;
+            s_pphys = bp;
+        }
+        __syncthreads();
+        const int plog = s_plog, pphys = s_pphys;
+        if (part == 0 && tid == 0) {
+            piv[j] = plog;
+            if (!(A[(long long)pphys * lda + j] != Real(0)) && info[mat] == 0) info[mat] = j + 1;
+        }
+        // the pivot row leaves the active set; the row at logical position j moves to plog
+        for (int r = r0 + tid; r < r1; r += blockDim.x) {
+            const int l = r - r0;
+            if (r == pphys) { act[l] = 0; lpos[l] = j; }
+            else if (act[l] && lpos[l] == j) lpos[l] = plog;
+        }
+        for (int c = tid; c < k + jb - j; c += blockDim.x) s_prow[c] = A[(long long)pphys * lda + j + c];
+        __syncthreads();
+        const Real pv = s_prow[0];
+        const bool big = fabs(pv) >= (sizeof(Real) == 8 ? Real(DBL_MIN) : Real(FLT_MIN));
+        const Real rinv = Real(1) / pv;
+        const int nc = k + jb - j - 1;
+        for (int r = r0 + tid; r < r1; r += blockDim.x) {
+            if (!act[r - r0]) continue;
+            Real* row = A + (long long)r * lda;
+            Real l = row[j];
+            if (pv != Real(0)) l = big ? l * rinv : l / pv;
+            row[j] = l;
+            for (int c = 1; c <= nc; ++c) row[j + c] -= l * s_prow[c];
+        }
+        __syncthreads();
+        if (j + 1 < k + jb) local_max(j + 1, (j + 1 - k) & 1);
+    }
+}
+
+// Apply the swaps piv[k..k+jb) to the columns [c0, c0 + ncols) (LAPACK dlaswp).
+template <class Real>
+__global__ void k_laswp_cols(int k, int jb, Real* const* Aarr, int lda, int* const* pivarr, int c0, int ncols) {
+    Real* __restrict__ A = Aarr[blockIdx.y];
+    const int* __restrict__ piv = pivarr[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncols) return;
+    const int c = c0 + t;
+    for (int j = k; j < k + jb; ++j) {
+        const int p = piv[j];
+        if (p != j) {
+            Real* a = A + (long long)j * lda + c;
+            Real* b = A + (long long)p * lda + c;
+            const Real tmp = *a; *a = *b; *b = tmp;
+        }
+    }
+}
+
 // Apply the swaps piv[k..k+jb) to the columns outside the panel (LAPACK dlaswp).
 template <class Real>
 __global__ void k_laswp_outside(int n, int k, int jb, Real* const* Aarr, int lda,
@@ -253,13 +387,72 @@ void gemm_batched_t(cudaStream_t st, int M, int N, int K, Real alpha, const Gemm
     }
 }
 
+// CTAs per matrix for the cooperative panel of a matrix with `rows` rows left (0: single-CTA panel)
+template <class Real>
+int coop_parts(int rows, int batch) {
+    static int capacity = -1;
+    if (capacity < 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_getf2_coop<Real>, 256, 0);
+        capacity = coop ? sms * per : 0;
+    }
+    if (rows < 512 || capacity <= 0 || !g_cooperative_lu.load()) return 0;
+    int P = std::min(capacity / batch, (rows + 31) / 32);
+    while ((rows + P - 1) / P > kCoopRows) ++P;
+    if (P < 2 || P * batch > capacity) return 0;
+    return P;
+}
+
+template <class Real>
+struct CoopScratch {  // candidate tables of the cooperative panel: 4 slots x grid
+    Real* val = nullptr;
+    int* pos = nullptr;
+    int size = 0;
+};
+
 template <class Real>
 void getrf_batched_t(cudaStream_t st, int n, Real* const* A, int lda, int* const* piv, int* info, int batch) {
+    static CoopScratch<Real> scratch;
     for (int k = 0; k < n; k += NB) {
         const int jb = (n - k < NB) ? n - k : NB;
-        const int threads = (n - k >= 512) ? 1024 : 256;
-        k_getf2_panel<Real><<<batch, threads, 0, st>>>(n, k, jb, A, lda, piv, info);
-        ++g_kernel_launches;
+        const int P = coop_parts<Real>(n - k, batch);
+        if (P > 0) {
+            const int grid = P * batch;
+            if (scratch.size < grid) {
+                cudaStreamSynchronize(st);
+                if (scratch.val) cudaFree(scratch.val);
+                if (scratch.pos) cudaFree(scratch.pos);
+                cudaMalloc(&scratch.val, 4 * size_t(grid) * sizeof(Real));
+                cudaMalloc(&scratch.pos, 4 * size_t(grid) * sizeof(int));
+                scratch.size = grid;
+            }
+            int nn = n, kk = k, jj = jb, ld = lda, PP = P;
+            Real* const* AA = A;
+            int* const* pp = piv;
+            int* inf = info;
+            Real* pv = scratch.val;
+            int* ps = scratch.pos;
+            void* args[] = {&nn, &kk, &jj, (void*)&AA, &ld, (void*)&pp, &inf, &PP, &pv, &ps};
+            if (cudaLaunchCooperativeKernel((const void*)k_getf2_coop<Real>, dim3(grid), dim3(256), args, 0, st) ==
+                cudaSuccess) {
+                ++g_kernel_launches;
+                dim3 gp((jb + 31) / 32, batch);
+                k_laswp_cols<Real><<<gp, 32, 0, st>>>(k, jb, A, lda, piv, k, jb);
+                ++g_kernel_launches;
+            } else {
+                (void)cudaGetLastError();  // refused (co-residency): the single-CTA panel
+                k_getf2_panel<Real><<<batch, 1024, 0, st>>>(n, k, jb, A, lda, piv, info);
+                ++g_kernel_launches;
+            }
+        } else {
+            const int threads = (n - k >= 512) ? 1024 : 256;
+            k_getf2_panel<Real><<<batch, threads, 0, st>>>(n, k, jb, A, lda, piv, info);
+            ++g_kernel_launches;
+        }
         if (n - jb > 0) {
             dim3 g((n - jb + 255) / 256, batch);
             k_laswp_outside<Real><<<g, 256, 0, st>>>(n, k, jb, A, lda, piv);

@@ -74,7 +74,10 @@ int ef_hps_set_coefficients(ef_hps* hps, const double* alpha, const double* beta
                             const double* lambda);
 /* Option keys of the reference: "cache-operators", "homogeneous-rhs" (HPSAlgorithm.hpp:134,532).
  * Added key "cuda-graphs" (default 1): replay the device-resident solve sequences
- * (ef_hps_solve_device_async, ef_hps_mixed_solve*) as CUDA graphs after their first two calls. */
+ * (ef_hps_solve_device_async, ef_hps_mixed_solve*) as CUDA graphs after their first two calls.
+ * Added key "cooperative-lu" (default 1, process-wide): LU panels of interface matrices with >= 512
+ * rows left run on many CTAs (one grid barrier per column); 0 keeps one CTA per panel.  Both give
+ * the same factors bit for bit. */
 int ef_hps_set_option(ef_hps* hps, const char* key, int value);
 /* Use an external CUDA stream (cudaStream_t) for all work of this handle; NULL = default stream. */
 int ef_hps_set_stream(ef_hps* hps, void* cuda_stream);

@@ -409,3 +409,19 @@ def test_incremental_build_equals_fresh_build(ef):
         out.append(h.leaf_solution())
     assert np.array_equal(out[0], out[1])
     assert np.array_equal(fresh.root_T(), inc.root_T())
+
+
+def test_cooperative_lu_panel_matches_single_cta(ef):
+    """The multi-CTA LU panel (matrices with >= 512 rows left: here the root X of a 256^2 tree and
+    the first panels of its children's merges) gives the single-CTA factors bit for bit."""
+    from ellipticforest_gb300._lib import check, load
+    Ts = []
+    for coop in (1, 0):
+        root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -1.0, 1.0, 16, -1.0, 1.0))
+        mesh = ef.Mesh().uniform(4, root)
+        hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+        check(load().ef_hps_set_option(hps.handle, b"cooperative-lu", coop))
+        hps.buildStage()
+        Ts.append(hps.root_T())
+    check(load().ef_hps_set_option(hps.handle, b"cooperative-lu", 1))
+    assert np.array_equal(Ts[0], Ts[1])
