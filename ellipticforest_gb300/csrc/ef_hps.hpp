@@ -432,6 +432,7 @@ private:
     int* d_err_ = nullptr;
     float* rleaf_ = nullptr;
     MixCoef* d_coef_ = nullptr;
+    int res_form_ = 0;  // residual kernel form: 0 when all leaf types have dx = dy and lambda = 0
     MixFp* d_fps_ = nullptr;  // FivePointStencil leaves only
     float* fp_band32_ = nullptr;
     float* fp_bcoef32_ = nullptr;

@@ -190,13 +190,21 @@ void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* 
 void mx_uncoarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate);
-// FP64 stencil constants of a leaf type: cx = 1/dx^2, cy = 1/dy^2, cc = lambda - 2cx - 2cy, 2/dx, 2/dy
+// Stencil constants of a leaf type for the residual: cx = 1/dx^2, cy = 1/dy^2 and |lambda| as 64-bit
+// significands m (leading bit 63) with c = m 2^(e - 64) (lmm = 0 when lambda = 0), the sign of lambda,
+// iso when cx == cy; FP32 copies of cx, cy for the first residual; the FP64 edge-flux factors 2/dx,
+// 2/dy
 struct MixCoef {
-    double cx, cy, cc, dtn_x, dtn_y;
+    double dtn_x, dtn_y;
+    unsigned long long cxm, cym, lmm;
+    int ecx, ecy, elm, lm_neg, iso;
+    float cx32, cy32;
 };
-// FP64 residual of every leaf (n % 4 == 0); zero_state when u is identically zero; rleaf [B][L]
+// Residual of every leaf (n % 4 == 0, n <= 64): exact fixed-point second differences and 128-bit
+// integer products (more accurate than an FP64 stencil); form 0 when every leaf type has cx = cy and lambda = 0, else 1;
+// zero_state when u is identically zero; rleaf [B][L]
 // scratch for the per-request maximum rmax (may be null)
-void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leaves, int L, int B, int n,
+void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const MixLeaf* leaves, int L, int B, int n,
                       int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g);
 // rmax[b] = max over leaves of rleaf[b][leaf]

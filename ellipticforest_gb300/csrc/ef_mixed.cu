@@ -48,7 +48,8 @@ __device__ __forceinline__ void mx_child_ifaces(int c, int& Ia, int& Ib) {
 // float <-> double by integer bit manipulation.  GB300's FP64 pipe, which also converts between the
 // two widths, runs at a small fraction of its FP32 and integer rates; these stay off it.  Values
 // below the smallest normal number of the target type become signed zeros; d2f_bits rounds toward
-// zero.
+// zero, d2f_rn_bits to nearest (ties to even) -- residuals use the latter, since a one-signed
+// rounding of every residual entry biases the correction it drives.
 __device__ __forceinline__ double f2d_bits(float x) {
     const unsigned b = __float_as_uint(x);
     const unsigned e = (b >> 23) & 0xffu;
@@ -65,6 +66,24 @@ __device__ __forceinline__ float d2f_bits(double x) {
     if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
     const int e32 = e - 896;
     if (e32 <= 0) return __uint_as_float(sign);
+    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
+}
+__device__ __forceinline__ float d2f_rn_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = int((b >> 52) & 0x7ffull);
+    unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+    int e32 = e - 896;
+    if (e32 <= 0) return __uint_as_float(sign);
+    const unsigned rest = unsigned(b & 0x1fffffffull);
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) {
+        if (++m >> 23) {
+            m = 0u;
+            ++e32;
+        }
+    }
     if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
     return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
 }
@@ -474,7 +493,7 @@ __global__ void k_mx_flux_up(const MixItem* __restrict__ items, int s, int B) {
             const int I = r / s, o = r - I * s;
             const double ml = it.hc64[mx_lower_child(I)][mx_q_lower(I, o, s) * B + b];
             const double mu = it.hc64[mx_upper_child(I)][mx_q_upper(I, o, s) * B + b];
-            it.mout[f] = d2f_bits(ml - mu);
+            it.mout[f] = d2f_rn_bits(ml - mu);
         }
     }
 }
@@ -664,133 +683,394 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
     }
 }
 
-// FP64 leaf residual r = f - (cx (u_W + u_E) + cy (u_S + u_N) + cc u_C) (stored as the next pass's
-// FP32 load), where a neighbour across the patch edge is the ghost value 2g - u_C of the Dirichlet
-// face data (the discrete operator of FiniteVolumeSolver.cpp:27-223), and the leaf's edge fluxes
-// h = +-(2/d)(u_edge - g) (FP64).  GB300's FP64 pipe is narrow, so the kernel runs in two phases
-// that keep its FP64 instruction stream free of predicated-off work: every cell with the interior
-// formula (missing neighbours read as 0), then the 4n-4 boundary cells again with their ghosts.
-// Items (leaf, b) with b fastest; each thread owns 4 consecutive cells of one row.  zero_state: u is
-// identically zero (the first residual).  The largest |r| (as FP32) of every item goes to
-// rleaf[b][leaf] (reduced per request by k_mx_rmax).
-template <int NT>
-__global__ void __launch_bounds__(256) k_mx_leaf_residual(const MixCoef* __restrict__ coefs,
+// Leaf residual r = f - (cx (u_W + u_E) + cy (u_S + u_N) + cc u_C) (stored as the next pass's FP32
+// load), where a neighbour across the patch edge is the ghost value 2g - u_C of the Dirichlet face
+// data (the discrete operator of FiniteVolumeSolver.cpp:27-223), and the leaf's edge fluxes
+// h = +-(2/d)(u_edge - g) (FP64).
+//
+// GB300's FP64 pipe is narrow (about 2 FMA per clock per SM, and it also carries the 64-bit
+// integer <-> floating-point conversions), so the residual runs in 64-bit integer arithmetic on the
+// integer pipes instead, and more accurately than an FP64 evaluation:
+//  - the item's u and ghost values become fixed point on one scale 2^(Eu - 1081), Eu the largest
+//    biased exponent among them, so |M| < 2^59 and every value within 2^6 of the largest is exact
+//    (smaller ones keep all bits above 2^-59 of the largest);
+//  - the second differences Sx = M_W + M_E - 2 M_C and Sy = M_S + M_N - 2 M_C (ghosts 2 M_g - M_C)
+//    are exact integer sums below 2^62: the cancellation that costs an FP64 stencil its digits
+//    happens without rounding;
+//  - the products cx Sx, cy Sy, lambda M_C are exact 128-bit products with the coefficients'
+//    64-bit significands, shifted to the fixed scale 2^sc on which the item's largest |f| is just
+//    below 2^61; r = F - P is one exact subtraction, rounded to FP32 at the end.  The error is a
+//    few units of 2^sc, about 2^-59 of the item's largest |f| (an FP64 stencil errs by 2^-53 of
+//    |u|/h^2).  A cell whose products do not fit on that scale (f small against the stencil
+//    terms, as for f = 0) forms the same exact sum on the scale of its own largest term.
+// Items (leaf, b) with b fastest; each thread owns 4 consecutive cells of one row; the fixed-point
+// tile of an item lives in shared memory, and the ghost data and edge fluxes ([4n][B] in HBM) pass
+// through shared memory so that a block's consecutive requests read and write them together.
+// The largest |r| (as FP32) of every item goes to rleaf[b][leaf] (reduced per request by k_mx_rmax).
+// Values below 2^-1022 (FP64 subnormals) of f count as zero; a non-finite u, g or f makes the
+// item's residual NaN.
+__device__ __forceinline__ int fx_bexp(double v) {
+    return int((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ff;
+}
+// v · 2^(1075 - E - 6) = v · 2^(1081 - E) for E >= 1 the largest exponent of its group: |M| < 2^59
+// (truncated toward zero); with a general shift, v · 2^-sc has shift e - 1075 - sc
+__device__ __forceinline__ long long fx_shift(double v, int E_off) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    int e = int(bits >> 52) & 0x7ff;
+    unsigned long long m = bits & 0xfffffffffffffull;
+    if (e) m |= 1ull << 52;
+    else e = 1;
+    const int sh = e - E_off;
+    const unsigned long long a = sh >= 0 ? (m << sh) : (sh > -64 ? (m >> -sh) : 0ull);
+    return (bits >> 63) ? -(long long)a : (long long)a;
+}
+__device__ __forceinline__ long long fx_from(double v, int E) { return fx_shift(v, E - 6); }
+// v · 2^-sc for FP64 data (subnormals count as zero); the caller keeps e - 1075 - sc <= 8
+__device__ __forceinline__ long long fx_scaled(double v, int sc) {
+    return fx_bexp(v) ? fx_shift(v, 1075 + sc) : 0ll;
+}
+// |S| · m as a 128-bit product (hi, lo)
+__device__ __forceinline__ void fx_mul128(unsigned long long a, unsigned long long m, unsigned long long& hi,
+                                          unsigned long long& lo) {
+    hi = __umul64hi(a, m);
+    lo = a * m;
+}
+// v = (hi:lo) · 2^-d (d may be negative), truncated; false when v would reach 2^61
+__device__ __forceinline__ bool fx_shr128(unsigned long long hi, unsigned long long lo, int d, unsigned long long& v) {
+    if (d >= 128) { v = 0ull; return true; }
+    if (d >= 64) { v = hi >> (d - 64); return v < (1ull << 61); }
+    if (d > 0) {
+        if (hi >> d) return false;
+        v = (hi << (64 - d)) | (lo >> d);
+        return v < (1ull << 61);
+    }
+    if (hi) return false;
+    if (d <= -61) return lo == 0ull ? (v = 0ull, true) : false;
+    if (lo >> (61 + d)) return false;
+    v = lo << -d;
+    return true;
+}
+// number of significant bits of (hi:lo)
+__device__ __forceinline__ int fx_bitlen128(unsigned long long hi, unsigned long long lo) {
+    return hi ? 128 - __clzll((long long)hi) : (lo ? 64 - __clzll((long long)lo) : 0);
+}
+// R · 2^sc as FP32, rounded to nearest (ties to even); below the normal range -> signed zero,
+// above -> inf
+__device__ __forceinline__ float fx_to_float(long long R, int sc) {
+    const unsigned sgn = R < 0 ? 0x80000000u : 0u;
+    const unsigned long long a = R < 0 ? 0ull - (unsigned long long)R : (unsigned long long)R;
+    if (a == 0ull) return 0.f;
+    const int lz = __clzll((long long)a);
+    const unsigned long long nrm = a << lz;
+    unsigned m = unsigned(nrm >> 40);  // 24 bits, leading one at bit 23
+    const unsigned long long rest = nrm & 0xffffffffffull;
+    int be = 127 + 63 - lz + sc;
+    if (rest > 0x8000000000ull || (rest == 0x8000000000ull && (m & 1u))) {
+        if (++m >> 24) {
+            m >>= 1;
+            ++be;
+        }
+    }
+    if (be <= 0) return __uint_as_float(sgn);
+    if (be >= 255) return __uint_as_float(sgn | 0x7f800000u);
+    return __uint_as_float(sgn | (unsigned(be) << 23) | (m & 0x7fffffu));
+}
+// FP64 of D · 2^sc rounded to nearest (ties to even); |D| < 2^63, result inside the normal range
+__device__ __forceinline__ double fx_to_double(long long D, int sc) {
+    const unsigned long long sgn = D < 0 ? 1ull << 63 : 0ull;
+    const unsigned long long a = D < 0 ? 0ull - (unsigned long long)D : (unsigned long long)D;
+    if (a == 0ull) return 0.0;
+    const int lz = __clzll((long long)a);
+    const unsigned long long nrm = a << lz;
+    unsigned long long m = nrm >> 11;
+    const unsigned long long rest = nrm & 0x7ffull;
+    if (rest > 0x400ull || (rest == 0x400ull && (m & 1ull))) ++m;
+    int be = 1023 + 63 - lz + sc;
+    if (m >> 53) { m >>= 1; ++be; }
+    if (be <= 0) return __longlong_as_double((long long)sgn);
+    if (be >= 2047) return __longlong_as_double((long long)(sgn | 0x7ff0000000000000ull));
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (m & 0xfffffffffffffull)));
+}
+
+// FORM 0: every leaf type has cx = cy and lambda = 0 (one product per cell); FORM 1: general
+template <int NT, int FORM>
+__global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(const MixCoef* __restrict__ coefs,
                                                           const MixLeaf* __restrict__ leaves, int L, int B,
-                                                          int n_arg, int ipc, int zero_state,
-                                                          const double* __restrict__ f,
+                                                          int n_arg, int ipc, const double* __restrict__ f,
                                                           const double* __restrict__ u64, float* __restrict__ q,
                                                           float* __restrict__ rleaf) {
-    __shared__ unsigned smax[256];
+    // per item: n*n fixed-point cells, 4n fixed-point ghosts, 4n FP64 ghosts (later the fluxes)
+    extern __shared__ long long fx_tile[];
+    __shared__ unsigned smax[64];
+    __shared__ int seu[64], sef[64];
+    __shared__ const double* sg[64];
+    __shared__ double* sh[64];
     const int n = NT ? NT : n_arg;
-    const int nn = n * n, tpi = nn / 4;
+    const int nn = n * n, tpi = nn / 4, n4 = 4 * n;
     const int tpe = tpi < 256 ? tpi : 256;
     const int slot = threadIdx.x / tpe, lt = threadIdx.x - slot * tpe;
-    const int item0 = blockIdx.x * ipc;
-    const int item = item0 + slot;
-    const bool act = slot < ipc && (long long)item < (long long)L * B;
-    if (threadIdx.x < ipc) smax[threadIdx.x] = 0u;
+    const long long items = (long long)L * B;
+    const int item0 = blockIdx.x * ipc, item = item0 + slot;
+    const bool act = slot < ipc && (long long)item < items;
+    if (threadIdx.x < ipc) {
+        smax[threadIdx.x] = 0u;
+        seu[threadIdx.x] = 1;
+        sef[threadIdx.x] = 1;
+        const int it = item0 + int(threadIdx.x);
+        if ((long long)it < items) {
+            const int lf = it / B, bb = it - lf * B;
+            sg[threadIdx.x] = leaves[lf].g64 + bb;
+            sh[threadIdx.x] = leaves[lf].h64 + bb;
+        }
+    }
     __syncthreads();
     const int leaf = act ? item / B : 0;
     const int b = act ? item - leaf * B : 0;
-    const MixLeaf lf = leaves[leaf];
-    const MixCoef cf = coefs[lf.type];
-    const double cx = cf.cx, cy = cf.cy, cc = cf.cc;
+    const MixCoef cf = coefs[leaves[leaf].type];
     const long long base = ((long long)b * L + leaf) * nn;
     const double* uu = u64 + base;
     const double* ff = f + base;
-    float mx = 0.f;
+    long long* tile = fx_tile + (long long)slot * (nn + 2 * n4);
+    long long* gfx = tile + nn;
+    double* gd = reinterpret_cast<double*>(gfx + n4);
+    const int nact = (long long)item0 + ipc <= items ? ipc : int(items - item0);
+    // (0) ghost data of the block's items, requests fastest: the items of a block are consecutive
+    // requests of one leaf whenever B is a multiple of ipc, so these reads coalesce
+    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
+        const int k = idx / nact, s = idx - k * nact;
+        reinterpret_cast<double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k] = sg[s][(long long)k * B];
+    }
+    __syncthreads();
+    // (1) scales: largest biased exponents of u and the ghosts (Eu), and of f (Ef)
+    int eu = 1, ef = 1;
     if (act) {
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
-            const int e = 4 * e4, i = e / n, j0 = e - (e / n) * n;
+            const double2 f01 = *reinterpret_cast<const double2*>(ff + 4 * e4);
+            const double2 f23 = *reinterpret_cast<const double2*>(ff + 4 * e4 + 2);
+            ef = max(max(ef, max(fx_bexp(f01.x), fx_bexp(f01.y))), max(fx_bexp(f23.x), fx_bexp(f23.y)));
+            const double2 c01 = *reinterpret_cast<const double2*>(uu + 4 * e4);
+            const double2 c23 = *reinterpret_cast<const double2*>(uu + 4 * e4 + 2);
+            eu = max(max(eu, max(fx_bexp(c01.x), fx_bexp(c01.y))), max(fx_bexp(c23.x), fx_bexp(c23.y)));
+        }
+        for (int k = lt; k < n4; k += tpe) eu = max(eu, fx_bexp(gd[k]));
+    }
+    // items of a power-of-two width own whole warps or aligned parts of one: reduce by shuffles first
+    const bool seg = (tpe & (tpe - 1)) == 0;
+    if (seg)
+        for (int o = 1; o < tpe && o < 32; o <<= 1) {
+            eu = max(eu, __shfl_xor_sync(0xffffffffu, eu, o));
+            ef = max(ef, __shfl_xor_sync(0xffffffffu, ef, o));
+        }
+    if (act && (!seg || (lt & 31) == 0)) {
+        atomicMax(&seu[slot], eu);
+        atomicMax(&sef[slot], ef);
+    }
+    __syncthreads();
+    const int Eu = seu[slot], Ef = sef[slot];
+    const int T = max(Eu, Ef);
+    // (2) fixed-point u and ghosts
+    if (act) {
+        for (int e4 = lt; e4 < tpi; e4 += tpe) {
+            const double2 c01 = *reinterpret_cast<const double2*>(uu + 4 * e4);
+            const double2 c23 = *reinterpret_cast<const double2*>(uu + 4 * e4 + 2);
+            reinterpret_cast<longlong2*>(tile + 4 * e4)[0] = make_longlong2(fx_from(c01.x, Eu), fx_from(c01.y, Eu));
+            reinterpret_cast<longlong2*>(tile + 4 * e4)[1] = make_longlong2(fx_from(c23.x, Eu), fx_from(c23.y, Eu));
+        }
+        for (int k = lt; k < n4; k += tpe) gfx[k] = fx_from(gd[k], Eu);
+    }
+    __syncthreads();
+    // (3) exact second differences and products, one subtraction
+    float mx = 0.f;
+    if (act) {
+        const bool bad = Eu == 0x7ff || Ef == 0x7ff;
+        const bool lam = FORM != 0 && cf.lmm != 0ull, iso = FORM == 0 || cf.iso != 0;
+        // common fixed scale 2^sc with |F| < 2^61; the 128-bit products carry 2^(Eu - 1081 + e - 64)
+        // and shift right by d to it; F and up to three terms below 2^61 sum without overflow
+        const int sc = Ef - 1083;
+        const int dx = sc - (Eu - 1145 + cf.ecx), dy = sc - (Eu - 1145 + cf.ecy), dl = sc - (Eu - 1145 + cf.elm);
+        for (int e4 = lt; e4 < tpi; e4 += tpe) {
+            const int e = 4 * e4, i = e / n, j0 = e - i * n;
+            long long c[4], xm[4], xp[4];
+            {
+                const longlong2 a = reinterpret_cast<const longlong2*>(tile + e)[0];
+                const longlong2 d = reinterpret_cast<const longlong2*>(tile + e)[1];
+                c[0] = a.x; c[1] = a.y; c[2] = d.x; c[3] = d.y;
+            }
+            if (i > 0) {
+                const longlong2 a = reinterpret_cast<const longlong2*>(tile + e - n)[0];
+                const longlong2 d = reinterpret_cast<const longlong2*>(tile + e - n)[1];
+                xm[0] = a.x; xm[1] = a.y; xm[2] = d.x; xm[3] = d.y;
+            } else {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) xm[t] = 2 * gfx[j0 + t] - c[t];
+            }
+            if (i < n - 1) {
+                const longlong2 a = reinterpret_cast<const longlong2*>(tile + e + n)[0];
+                const longlong2 d = reinterpret_cast<const longlong2*>(tile + e + n)[1];
+                xp[0] = a.x; xp[1] = a.y; xp[2] = d.x; xp[3] = d.y;
+            } else {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) xp[t] = 2 * gfx[n + j0 + t] - c[t];
+            }
+            const long long left = j0 > 0 ? tile[e - 1] : 2 * gfx[2 * n + i] - c[0];
+            const long long right = j0 + 4 < n ? tile[e + 4] : 2 * gfx[3 * n + i] - c[3];
+            const long long ym[4] = {left, c[0], c[1], c[2]};
+            const long long yp[4] = {c[1], c[2], c[3], right};
             const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
             const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
             const double fv[4] = {f01.x, f01.y, f23.x, f23.y};
             float rr[4];
-            if (zero_state) {
-#pragma unroll
-                for (int t = 0; t < 4; ++t) rr[t] = d2f_bits(fv[t]);
-            } else {
-                double c[4], up[4] = {0.0, 0.0, 0.0, 0.0}, dn[4] = {0.0, 0.0, 0.0, 0.0};
-                const double2 c01 = *reinterpret_cast<const double2*>(uu + e);
-                const double2 c23 = *reinterpret_cast<const double2*>(uu + e + 2);
-                c[0] = c01.x; c[1] = c01.y; c[2] = c23.x; c[3] = c23.y;
-                if (i > 0) {
-                    const double2 a = *reinterpret_cast<const double2*>(uu + e - n);
-                    const double2 bq = *reinterpret_cast<const double2*>(uu + e - n + 2);
-                    up[0] = a.x; up[1] = a.y; up[2] = bq.x; up[3] = bq.y;
-                }
-                if (i < n - 1) {
-                    const double2 a = *reinterpret_cast<const double2*>(uu + e + n);
-                    const double2 bq = *reinterpret_cast<const double2*>(uu + e + n + 2);
-                    dn[0] = a.x; dn[1] = a.y; dn[2] = bq.x; dn[3] = bq.y;
-                }
-                const double left = j0 > 0 ? uu[e - 1] : 0.0;
-                const double right = j0 + 4 < n ? uu[e + 4] : 0.0;
-                const double ym[4] = {left, c[0], c[1], c[2]};
-                const double yp[4] = {c[1], c[2], c[3], right};
-                // r = ((f - cc u_C) - cx (u_W + u_E)) - cy (u_S + u_N): 5 FP64 operations
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    rr[t] = d2f_bits(fma(-cy, ym[t] + yp[t], fma(-cx, up[t] + dn[t], fma(-cc, c[t], fv[t]))));
-            }
-            const bool edge_row = i == 0 || i == n - 1;
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                const int j = j0 + t;
-                const bool interior = !edge_row && j > 0 && j < n - 1;
-                mx = fmaxf(mx, interior ? fabsf(rr[t]) : 0.f);
+                const long long sx = xm[t] + xp[t] - 2 * c[t], sy = ym[t] + yp[t] - 2 * c[t];
+                // terms (S, significand, shift, sign): cx = cy takes one product of the exact sum
+                // (|sx + sy| < 1.5 * 2^62)
+                const long long s0 = iso ? sx + sy : sx;
+                unsigned long long h0, l0, h1 = 0ull, l1 = 0ull, h2 = 0ull, l2 = 0ull, v;
+                fx_mul128(s0 < 0 ? 0ull - (unsigned long long)s0 : (unsigned long long)s0, cf.cxm, h0, l0);
+                if (!iso) fx_mul128(sy < 0 ? 0ull - (unsigned long long)sy : (unsigned long long)sy, cf.cym, h1, l1);
+                if (lam) fx_mul128(c[t] < 0 ? 0ull - (unsigned long long)c[t] : (unsigned long long)c[t], cf.lmm, h2, l2);
+                const bool n0 = s0 < 0, n1 = sy < 0, n2 = (c[t] < 0) != (cf.lm_neg != 0);
+                const long long F = fx_scaled(fv[t], sc);
+                long long R = F;
+                bool fits = fx_shr128(h0, l0, dx, v);
+                R -= n0 ? -(long long)v : (long long)v;
+                if (!iso) {
+                    fits = fx_shr128(h1, l1, dy, v) && fits;
+                    R -= n1 ? -(long long)v : (long long)v;
+                }
+                if (lam) {
+                    fits = fx_shr128(h2, l2, dl, v) && fits;
+                    R -= n2 ? -(long long)v : (long long)v;
+                }
+                float r;
+                if (fits) {
+                    r = fx_to_float(R, sc);
+                } else {
+                    // the same exact sum on the coarser scale 2^sc2 of this cell's largest term
+                    int top = sc + 61;
+                    top = max(top, sc - dx + fx_bitlen128(h0, l0));
+                    if (!iso) top = max(top, sc - dy + fx_bitlen128(h1, l1));
+                    if (lam) top = max(top, sc - dl + fx_bitlen128(h2, l2));
+                    const int sc2 = top - 61;
+                    R = fx_scaled(fv[t], sc2);
+                    fx_shr128(h0, l0, dx + sc2 - sc, v);
+                    R -= n0 ? -(long long)v : (long long)v;
+                    if (!iso) {
+                        fx_shr128(h1, l1, dy + sc2 - sc, v);
+                        R -= n1 ? -(long long)v : (long long)v;
+                    }
+                    if (lam) {
+                        fx_shr128(h2, l2, dl + sc2 - sc, v);
+                        R -= n2 ? -(long long)v : (long long)v;
+                    }
+                    r = fx_to_float(R, sc2);
+                }
+                rr[t] = bad ? __int_as_float(0x7fffffff) : r;
+                mx = fmaxf(mx, fabsf(rr[t]));
             }
             *reinterpret_cast<float4*>(q + base + e) = make_float4(rr[0], rr[1], rr[2], rr[3]);
         }
-    }
-    __syncthreads();  // the boundary phase rewrites cells stored by other threads of the block
-    if (act) {
-        const double* gW = lf.g64 + b;
-        const double* gE = lf.g64 + (long long)n * B + b;
-        const double* gS = lf.g64 + 2LL * n * B + b;
-        const double* gN = lf.g64 + 3LL * n * B + b;
-        for (int k = lt; k < 4 * n - 4; k += tpe) {
-            int i, j;
-            if (k < n) { i = 0; j = k; }
-            else if (k < 2 * n) { i = n - 1; j = k - n; }
-            else { const int m = k - 2 * n; i = 1 + (m >> 1); j = (m & 1) ? n - 1 : 0; }
-            const int e = i * n + j;
-            double r;
-            if (zero_state) {
-                // u = 0: only the ghost terms 2g of the missing neighbours remain
-                double gx = 0.0, gy = 0.0;
-                if (i == 0) gx = gW[(long long)j * B];
-                else if (i == n - 1) gx = gE[(long long)j * B];
-                if (j == 0) gy = gS[(long long)i * B];
-                else if (j == n - 1) gy = gN[(long long)i * B];
-                r = fma(-2.0 * cy, gy, fma(-2.0 * cx, gx, ff[e]));
-            } else {
-                const double uc = uu[e];
-                const double xm = i > 0 ? uu[e - n] : fma(2.0, gW[(long long)j * B], -uc);
-                const double xp = i < n - 1 ? uu[e + n] : fma(2.0, gE[(long long)j * B], -uc);
-                const double ym = j > 0 ? uu[e - 1] : fma(2.0, gS[(long long)i * B], -uc);
-                const double yp = j < n - 1 ? uu[e + 1] : fma(2.0, gN[(long long)i * B], -uc);
-                r = fma(-cy, ym + yp, fma(-cx, xm + xp, fma(-cc, uc, ff[e])));
-            }
-            const float rf = d2f_bits(r);
-            q[base + e] = rf;
-            mx = fmaxf(mx, fabsf(rf));
+        // (4) edge fluxes of the state, h = +-(2/d)(u_edge - g): the difference of the fixed-point
+        // values is exact, then one rounding to FP64
+        for (int r = lt; r < n4; r += tpe) {
+            const int side = r / n, pos = r - side * n;
+            const int cell = side == 0 ? pos : side == 1 ? (n - 1) * n + pos : side == 2 ? pos * n : pos * n + n - 1;
+            const double d = side < 2 ? cf.dtn_x : cf.dtn_y;
+            const double dv = fx_to_double(tile[cell] - gfx[r], Eu - 1081);
+            gd[r] = (side == 0 || side == 2) ? d * dv : -d * dv;
         }
-        atomicMax(&smax[slot], __float_as_uint(mx));
-        for (int r = lt; r < 4 * n; r += tpe) {
-            const int side = r / n, pos = r - (r / n) * n;
-            int cell;
-            if (side == 0) cell = pos;
-            else if (side == 1) cell = (n - 1) * n + pos;
-            else if (side == 2) cell = pos * n;
-            else cell = pos * n + n - 1;
-            const double gv = lf.g64[(long long)r * B + b];
-            const double dtn = (side == 0 || side == 2) ? (side < 2 ? cf.dtn_x : cf.dtn_y)
-                                                        : -(side < 2 ? cf.dtn_x : cf.dtn_y);
-            lf.h64[(long long)r * B + b] = zero_state ? -dtn * gv : dtn * (uu[cell] - gv);
+    }
+    if (seg)
+        for (int o = 1; o < tpe && o < 32; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (act && (!seg || (lt & 31) == 0)) atomicMax(&smax[slot], __float_as_uint(mx));
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
+        const int k = idx / nact, s = idx - k * nact;
+        sh[s][(long long)k * B] = reinterpret_cast<const double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k];
+    }
+    if (rleaf && act && lt == 0) rleaf[(long long)b * L + leaf] = __uint_as_float(smax[slot]);
+}
+
+// First residual (u identically zero): r = f - 2 cx g_x - 2 cy g_y on the edge cells, r = f inside,
+// and the edge fluxes h = -+(2/d) g.  This right-hand side only feeds the first FP32 pass, so it is
+// formed in FP32 (the FP64 data converted by bit operations, rounding to nearest); the fluxes stay
+// FP64.  Same item layout and ghost/flux staging as k_mx_leaf_residual.
+template <int NT>
+__global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __restrict__ coefs,
+                                                           const MixLeaf* __restrict__ leaves, int L, int B,
+                                                           int n_arg, int ipc, const double* __restrict__ f,
+                                                           float* __restrict__ q, float* __restrict__ rleaf) {
+    extern __shared__ double r0_gd[];  // per item: 4n ghost values, later the fluxes
+    __shared__ unsigned smax[64];
+    __shared__ const double* sg[64];
+    __shared__ double* sh[64];
+    const int n = NT ? NT : n_arg;
+    const int nn = n * n, tpi = nn / 4, n4 = 4 * n;
+    const int tpe = tpi < 256 ? tpi : 256;
+    const int slot = threadIdx.x / tpe, lt = threadIdx.x - slot * tpe;
+    const long long items = (long long)L * B;
+    const int item0 = blockIdx.x * ipc, item = item0 + slot;
+    const bool act = slot < ipc && (long long)item < items;
+    if (threadIdx.x < ipc) {
+        smax[threadIdx.x] = 0u;
+        const int it = item0 + int(threadIdx.x);
+        if ((long long)it < items) {
+            const int lf = it / B, bb = it - lf * B;
+            sg[threadIdx.x] = leaves[lf].g64 + bb;
+            sh[threadIdx.x] = leaves[lf].h64 + bb;
         }
     }
     __syncthreads();
+    const int nact = (long long)item0 + ipc <= items ? ipc : int(items - item0);
+    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
+        const int k = idx / nact, s = idx - k * nact;
+        r0_gd[s * n4 + k] = sg[s][(long long)k * B];
+    }
+    __syncthreads();
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
+    const MixCoef cf = coefs[leaves[leaf].type];
+    double* gd = r0_gd + slot * n4;
+    float mx = 0.f;
+    if (act) {
+        const long long base = ((long long)b * L + leaf) * nn;
+        const double* ff = f + base;
+        const float cx2 = 2.0f * cf.cx32, cy2 = 2.0f * cf.cy32;
+        for (int e4 = lt; e4 < tpi; e4 += tpe) {
+            const int e = 4 * e4, i = e / n, j0 = e - i * n;
+            const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
+            const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
+            float rr[4] = {d2f_rn_bits(f01.x), d2f_rn_bits(f01.y), d2f_rn_bits(f23.x), d2f_rn_bits(f23.y)};
+            if (i == 0)
+#pragma unroll
+                for (int t = 0; t < 4; ++t) rr[t] = fmaf(-cx2, d2f_rn_bits(gd[j0 + t]), rr[t]);
+            if (i == n - 1)
+#pragma unroll
+                for (int t = 0; t < 4; ++t) rr[t] = fmaf(-cx2, d2f_rn_bits(gd[n + j0 + t]), rr[t]);
+            if (j0 == 0) rr[0] = fmaf(-cy2, d2f_rn_bits(gd[2 * n + i]), rr[0]);
+            if (j0 + 4 == n) rr[3] = fmaf(-cy2, d2f_rn_bits(gd[3 * n + i]), rr[3]);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) mx = fmaxf(mx, fabsf(rr[t]));
+            *reinterpret_cast<float4*>(q + base + e) = make_float4(rr[0], rr[1], rr[2], rr[3]);
+        }
+    }
+    __syncthreads();  // the ghost values are read above before the fluxes replace them
+    if (act)
+        for (int r = lt; r < n4; r += tpe) {
+            const int side = r / n;
+            const double d = side < 2 ? cf.dtn_x : cf.dtn_y;
+            gd[r] = (side == 0 || side == 2) ? -d * gd[r] : d * gd[r];
+        }
+    const bool seg = (tpe & (tpe - 1)) == 0;
+    if (seg)
+        for (int o = 1; o < tpe && o < 32; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (act && (!seg || (lt & 31) == 0)) atomicMax(&smax[slot], __float_as_uint(mx));
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
+        const int k = idx / nact, s = idx - k * nact;
+        sh[s][(long long)k * B] = r0_gd[s * n4 + k];
+    }
     if (rleaf && act && lt == 0) rleaf[(long long)b * L + leaf] = __uint_as_float(smax[slot]);
 }
 
@@ -1000,20 +1280,43 @@ void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf
     ++g_kernel_launches;
 }
 
-void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, const MixLeaf* leaves, int L, int B, int n,
+template <int FORM>
+void mx_residual_launch(cudaStream_t st, unsigned grid, unsigned threads, size_t smem, const MixCoef* coefs,
+                        const MixLeaf* leaves, int L, int B, int n, int ipc, const double* f, const double* u64,
+                        float* q, float* rl) {
+    if (n == 16)
+        k_mx_leaf_residual<16, FORM><<<grid, threads, smem, st>>>(coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    else if (n == 8)
+        k_mx_leaf_residual<8, FORM><<<grid, threads, smem, st>>>(coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    else if (n == 32)
+        k_mx_leaf_residual<32, FORM><<<grid, threads, smem, st>>>(coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    else
+        k_mx_leaf_residual<0, FORM><<<grid, threads, smem, st>>>(coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+}
+
+void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const MixLeaf* leaves, int L, int B, int n,
                       int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax) {
     const int tpi = n * n / 4, tpe = tpi < 256 ? tpi : 256, ipc = 256 / tpe;
     const long long items = (long long)L * B;
     const unsigned grid = unsigned((items + ipc - 1) / ipc);
+    // fixed-point tiles: n <= 64 keeps them within the default 48 KB of shared memory
+    const size_t smem = size_t(ipc) * (size_t(n) * n + 8 * size_t(n)) * sizeof(long long);
+    if (n % 4 != 0 || smem > 48 * 1024) throw std::invalid_argument("leaf residual: leaf size out of range");
     float* rl = rmax ? rleaf : nullptr;
-    if (n == 16)
-        k_mx_leaf_residual<16><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
-    else if (n == 8)
-        k_mx_leaf_residual<8><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
-    else if (n == 32)
-        k_mx_leaf_residual<32><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
-    else
-        k_mx_leaf_residual<0><<<grid, unsigned(ipc * tpe), 0, st>>>(coefs, leaves, L, B, n, ipc, zero_state, f, u64, q, rl);
+    if (zero_state) {
+        const size_t smem0 = size_t(ipc) * 4 * size_t(n) * sizeof(double);
+        if (n == 16)
+            k_mx_leaf_residual0<16><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
+        else if (n == 8)
+            k_mx_leaf_residual0<8><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
+        else
+            k_mx_leaf_residual0<0><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
+        ++g_kernel_launches;
+        if (rmax) mx_rmax(st, rleaf, L, B, rmax);
+        return;
+    }
+    if (form == 0) mx_residual_launch<0>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    else mx_residual_launch<1>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }

@@ -23,14 +23,21 @@ __device__ __forceinline__ double f2d_bits_fp(float x) {
     const unsigned long long e64 = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
     return __longlong_as_double((long long)(sign | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
 }
-__device__ __forceinline__ float d2f_bits_fp(double x) {
+__device__ __forceinline__ float d2f_bits_fp(double x) {  // rounded to nearest, ties to even
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned sign = (unsigned)(b >> 63) << 31;
     const int e = int((b >> 52) & 0x7ffull);
-    const unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
+    unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
     if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
-    const int e32 = e - 896;
+    int e32 = e - 896;
     if (e32 <= 0) return __uint_as_float(sign);
+    const unsigned rest = unsigned(b & 0x1fffffffull);
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) {
+        if (++m >> 23) {
+            m = 0u;
+            ++e32;
+        }
+    }
     if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
     return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
 }

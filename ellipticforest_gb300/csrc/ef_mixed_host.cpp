@@ -11,6 +11,16 @@
 namespace efgb {
 
 namespace {
+// c = m 2^(e - 64) with m a 64-bit significand (leading bit 63); c = 0 gives m = 0
+void significand64(double c, unsigned long long& m, int& e) {
+    int ex = 0;
+    const double fr = std::frexp(c, &ex);  // c = fr 2^ex, fr in [0.5, 1)
+    m = c == 0.0 ? 0ull : (unsigned long long)std::ldexp(fr, 64);
+    e = c == 0.0 ? 0 : ex;
+}
+}  // namespace
+
+namespace {
 
 struct MxCarver {
     char* base = nullptr;
@@ -217,8 +227,18 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         std::vector<MixCoef> co(hps.types_.size());
         for (size_t t = 0; t < co.size(); ++t) {
             const double dx = hps.types_[t].dx, dy = hps.types_[t].dy;
-            const double cx = 1.0 / (dx * dx), cy = 1.0 / (dy * dy);
-            co[t] = MixCoef{cx, cy, -(2.0 * cx + 2.0 * cy) + hps.lambda_, 2.0 / dx, 2.0 / dy};
+            const double cx = 1.0 / (dx * dx), cy = 1.0 / (dy * dy), lm = hps.lambda_;
+            MixCoef& c = co[t];
+            c.dtn_x = 2.0 / dx;
+            c.dtn_y = 2.0 / dy;
+            significand64(cx, c.cxm, c.ecx);
+            significand64(cy, c.cym, c.ecy);
+            significand64(std::fabs(lm), c.lmm, c.elm);
+            c.lm_neg = lm < 0.0 ? 1 : 0;
+            c.iso = cx == cy ? 1 : 0;
+            c.cx32 = float(cx);
+            c.cy32 = float(cy);
+            if (!c.iso || c.lmm) res_form_ = 1;
         }
         ck(cudaMemcpy(d_coef_, co.data(), co.size() * sizeof(MixCoef), cudaMemcpyHostToDevice), "mixed coefs");
     }
@@ -363,7 +383,7 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
         mx_fp_residual(st, d_fps_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
                        rleaf_, rmax);
     else
-        mx_leaf_residual(st, d_coef_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
+        mx_leaf_residual(st, d_coef_, res_form_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
                          rleaf_, rmax);
     h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
     h.pb("mx_interface", st);

@@ -159,3 +159,28 @@ def test_mixed_build_reaches_fp64_solution(ef, kind, n, fp64_levels):
     for k in range(3):
         err = np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max()
         assert err <= TOL, (k, err)
+
+
+@pytest.mark.parametrize("dom,lam,zero_f", [((0.0, 2.0, 0.0, 1.0), 0.0, False),
+                                            ((-1.0, 1.0, -1.0, 1.0), -2.5, False),
+                                            ((0.0, 2.0, 0.0, 1.0), -2.5, True),
+                                            ((-1.0, 1.0, -1.0, 1.0), 0.0, True)])
+def test_mixed_residual_forms_one_sweep(ef, dom, lam, zero_f):
+    """The leaf residual's forms: rectangular cells (cx != cy, one product per direction), a
+    Helmholtz lambda (a third product), and f = 0 (Laplace data: every product exceeds the scale of f,
+    so each cell sums on the scale of its largest term) -- one refinement sweep reaches the FP64
+    solution."""
+    n = 8
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, dom[0], dom[1], n, dom[2], dom[3]))
+    mesh = ef.Mesh().uniform(4, root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90,
+                                                      lambda_function=lambda x, y: lam))
+    hps.buildStage()
+    F, A, R = requests(hps, mesh, 3, 31)
+    if zero_f:
+        F[:] = 0.0
+    ref = fp64_solutions(hps, F, A, R)
+    hps.mixed_init(3)
+    u = hps.mixed_solve(F, A, R, sweeps=1)
+    for k in range(3):
+        assert np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max() <= TOL, k
