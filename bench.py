@@ -7,11 +7,13 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
 
   value  -- solves/s of the batched mixed-precision form: each step is one block of --batch
             requests solved on the factored tree by FP32 HPS passes (batched node GEMMs, FP32 leaf
-            eigen-solves) with --sweeps FP64 refinement sweeps (FP64 leaf residual + interface flux
-            mismatch), to <= 1e-10 relative of the FP64 HPS solution (rel_err_vs_fp64, measured);
-            inputs resident in HBM
-  e2e    -- the same form through the C ABI call ef_hps_mixed_solve on pinned host buffers, the
-            host<->device copies of every block inside the timed region
+            eigen-solves) with --sweeps refinement sweeps (exact fixed-point leaf residual + FP64
+            interface flux mismatch), to <= 1e-10 relative of the FP64 HPS solution (rel_err_vs_fp64,
+            measured); inputs resident in HBM
+  e2e    -- the same form through the C ABI call ef_hps_mixed_solve_blocks on pinned host buffers
+            (K blocks in one call, two lanes alternating so one block's copies overlap the other's
+            solve), the host<->device copies of every block inside the timed region; the one-block
+            ef_hps_mixed_solve rate is reported beside it
   plain_fp64 -- the plain FP64 form one request at a time (device-resident solves/s, p50/p99, and
             e2e through the reference-facing upwards/solve/get_leaf_u calls)
   many_rhs_L6 -- 512 right-hand sides on a uniform level-6 tree: one mixed block vs 512 plain solves
@@ -75,7 +77,7 @@ def workload_desc(level, n, batch=1, sweeps=0):
          f"Poisson on [-1,1]^2")
     if batch > 1 or sweeps:
         return w + (f"; each step one block of {batch} requests (Gaussian-bump loads, Fourier Dirichlet data) "
-                    f"solved by FP32 HPS passes with {sweeps} FP64 refinement sweep(s) to <=1e-10 of the FP64 HPS")
+                    f"solved by FP32 HPS passes with {sweeps} refinement sweep(s) to <=1e-10 of the FP64 HPS")
     return w + ", one right-hand side per step (Gaussian-bump load, Fourier Dirichlet data)"
 
 
@@ -422,17 +424,34 @@ def run_gb300(args):
     Fh = torch.from_numpy(F).pin_memory()
     Ah = torch.from_numpy(A).pin_memory()
     Rh = torch.from_numpy(R).pin_memory()
-    Uh = torch.empty_like(Fh).pin_memory()
-    Fn, An, Rn, Un = Fh.numpy(), Ah.numpy(), Rh.numpy(), Uh.numpy()
+    Uh = [torch.empty_like(Fh).pin_memory() for _ in range(2)]
+    Fn, An, Rn, Un = Fh.numpy(), Ah.numpy(), Rh.numpy(), [x.numpy() for x in Uh]
+    # (1) one block per call (ef_hps_mixed_solve: copy in, solve, copy out, synchronise)
     Ke = max(2, K // 4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(Ke):
-        check(lib.ef_hps_mixed_solve(hps.handle, B, sweeps, dptr(Fn), dptr(An), dptr(Rn), dptr(Un)))
+        check(lib.ef_hps_mixed_solve(hps.handle, B, sweeps, dptr(Fn), dptr(An), dptr(Rn), dptr(Un[0])))
+    e2e_single = world * Ke * B / (time.perf_counter() - t0)
+    assert np.array_equal(Un[0][0], u_mixed[0])
+    # (2) the headline e2e: K blocks through one pipelined call (ef_hps_mixed_solve_blocks), every
+    # block's inputs copied in and its results copied out inside the call; two lanes alternate so
+    # that one block's copies overlap the other's solve
+    import ctypes as C
+    nbk = K
+    batch_arr = (C.c_int * nbk)(*([B] * nbk))
+    f_arr = (C.c_void_p * nbk)(*([Fn.ctypes.data] * nbk))
+    a_arr = (C.c_void_p * nbk)(*([An.ctypes.data] * nbk))
+    r_arr = (C.c_void_p * nbk)(*([Rn.ctypes.data] * nbk))
+    u_arr = (C.c_void_p * nbk)(*[Un[k & 1].ctypes.data for k in range(nbk)])
+    check(lib.ef_hps_mixed_solve_blocks(hps.handle, 2, batch_arr, sweeps, f_arr, a_arr, r_arr, u_arr))  # lane 2 set-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    check(lib.ef_hps_mixed_solve_blocks(hps.handle, nbk, batch_arr, sweeps, f_arr, a_arr, r_arr, u_arr))
     e2e_wall = time.perf_counter() - t0
-    e2e_value = world * Ke * B / e2e_wall
+    e2e_value = world * nbk * B / e2e_wall
     clk = clocks.stop()
-    assert np.array_equal(Uh.numpy()[0], u_mixed[0])
+    assert np.array_equal(Un[0][0], u_mixed[0]) and np.array_equal(Un[1][0], u_mixed[0])
 
     # per-section kernel timing of the mixed form (CUDA events on the library's stream)
     hps.profile_enable(True)
@@ -502,7 +521,9 @@ def run_gb300(args):
             },
             "e2e": {"value": e2e_value, "unit": "solves/s",
                     "h2d_bytes_per_step": int(B * 8 * (dofs + 2 * 4 * hps.M)),
-                    "d2h_bytes_per_step": int(B * 8 * dofs)},
+                    "d2h_bytes_per_step": int(B * 8 * dofs),
+                    "api": "ef_hps_mixed_solve_blocks (K blocks per call, two lanes, pinned host arrays)",
+                    "one_block_per_call_solves_per_s": e2e_single},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
@@ -591,13 +612,13 @@ def adaptive(ef, torch, stream, args, c2):
     A = np.stack([reqs[i % 4][1] for i in range(B)])
     R = np.stack([reqs[i % 4][2] for i in range(B)])
     hps.mixed_init(B)
-    U = hps.mixed_solve(F, A, R, args.sweeps)
+    U = hps.mixed_solve(F, A, R, args.adaptive_sweeps)
     errs = [float(np.abs(U[i] - refs[i]).max() / np.abs(refs[i]).max()) for i in range(4)]
-    hps.mixed_solve_async(B, args.sweeps)
+    hps.mixed_solve_async(B, args.adaptive_sweeps)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(3):
-        hps.mixed_solve_async(B, args.sweeps)
+        hps.mixed_solve_async(B, args.adaptive_sweeps)
     e1.record(stream)
     torch.cuda.synchronize()
     mixed = 3 * B / (e0.elapsed_time(e1) / 1e3)
@@ -606,7 +627,7 @@ def adaptive(ef, torch, stream, args, c2):
                         "f = -(sin x + sin y), g = sin x + sin y",
             "leaves": hps.num_leaves, "dofs": int(X.size), "build_s": build_s,
             "plain_fp64_solves_per_s": plain, "max_err_vs_exact": err,
-            "mixed_block": {"batch": B, "sweeps": args.sweeps, "solves_per_s": mixed,
+            "mixed_block": {"batch": B, "sweeps": args.adaptive_sweeps, "solves_per_s": mixed,
                             "speedup_vs_plain": mixed / plain, "rel_err_vs_fp64_per_request": errs}}
 
 
@@ -736,8 +757,9 @@ def serving(ef, torch, stream, main_tree, args, c2):
     NREQ = 2000
     plan = [(int(rng.integers(0, T)), int(rng.integers(0, P))) for _ in range(NREQ)]
     budget = 64 << 30
+    tree_sweeps = [args.sweeps, args.adaptive_sweeps, args.sweeps]
     srv = ef.Server([h for _, _, h, _ in trees], bmax=[32, 32, 32], lanes=2, hbm_budget_bytes=budget,
-                    sweeps=args.sweeps)
+                    sweeps=tree_sweeps)
     lanes = [srv.lanes(t) for t in range(T)]
 
     def run_stream(rate):
@@ -809,7 +831,7 @@ def serving(ef, torch, stream, main_tree, args, c2):
     return {
         "workload": ("2000 requests, seeded Poisson arrivals at 0.7x the saturated rate, uniformly over 3 resident "
                      "trees: " + "; ".join(f"{nm} ({m.cell_centres()[0].size} dofs)" for nm, m, _, _ in trees)),
-        "lanes_per_tree": lanes, "bmax": 32, "hbm_budget_bytes": budget, "sweeps": args.sweeps,
+        "lanes_per_tree": lanes, "bmax": 32, "hbm_budget_bytes": budget, "sweeps_per_tree": tree_sweeps,
         "arrival_rate_per_s": rate, "solves_per_s": NREQ / wall,
         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
         "saturated_solves_per_s": sat,
@@ -966,9 +988,11 @@ def main():
     ap.add_argument("--level", type=int, default=7)
     ap.add_argument("--n", type=int, default=16)
     ap.add_argument("--batch", type=int, default=32, help="requests per block of the mixed form")
-    ap.add_argument("--sweeps", type=int, default=2,
-                    help="FP64 refinement sweeps of the mixed form (2 keeps every L7 result within 1e-10 of "
-                         "the FP64 HPS; against a sparse direct solve of the 5-point system it is 2e-12)")
+    ap.add_argument("--sweeps", type=int, default=1,
+                    help="refinement sweeps of the mixed form on uniform trees (one keeps the L7 results "
+                         "within 1e-10 of the FP64 HPS, and within 3e-11 of a sparse direct solve)")
+    ap.add_argument("--adaptive-sweeps", type=int, default=2,
+                    help="refinement sweeps on the adaptive config-2 tree (one sweep leaves up to 2e-10 there)")
     ap.add_argument("--plain-steps", type=int, default=30, help="timed steps of the plain FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 512-RHS level-6 case")

@@ -74,6 +74,9 @@ SIGNATURES = {
     "ef_server_create": (C.c_int, [C.POINTER(_vp), C.POINTER(C.c_int), C.c_int, C.c_int, C.c_longlong, C.c_int,
                                    C.POINTER(_vp)]),
     "ef_server_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "ef_server_set_sweeps": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "ef_hps_mixed_solve_blocks": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p),
+                                            C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "ef_server_submit": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
     "ef_server_poll": (C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "ef_server_wait": (C.c_int, [_vp, C.c_longlong, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),

@@ -29,6 +29,14 @@ struct ef_server {
 struct ef_hps {
     std::unique_ptr<efgb::Hps> hps;
     std::unique_ptr<efgb::MixedSolver> mixed;
+    // second lane of ef_hps_mixed_solve_blocks (shares mixed's FP32 operators) and its stream
+    std::unique_ptr<efgb::MixedSolver> mixed2;
+    cudaStream_t stream2 = nullptr;
+    ~ef_hps() {
+        if (stream2) cudaStreamSynchronize(stream2);
+        mixed2.reset();
+        if (stream2) cudaStreamDestroy(stream2);
+    }
     bool cache_operators = false;
     bool homogeneous_rhs = false;
     bool upward_done = false;
@@ -504,6 +512,8 @@ int ef_hps_mixed_init(ef_hps* h, int bmax) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->hps->built() && !h->hps->built32()) return fail(EF_ERR_STATE, "mixed solver before build stage");
     return guarded([&] {
+        if (h->stream2) cudaStreamSynchronize(h->stream2);
+        h->mixed2.reset();
         h->mixed.reset();
         h->mixed = std::make_unique<efgb::MixedSolver>(*h->hps, bmax);
         return EF_OK;
@@ -550,6 +560,57 @@ int ef_hps_mixed_solve(ef_hps* h, int batch, int sweeps, const double* f, const 
         if (st) return st;
         st = cuda_status(cudaStreamSynchronize(s), "mixed solve");
         if (!st && X.take_error()) return fail(EF_ERR_CUDA, "mixed solve: an operator tile copy did not complete");
+        return st;
+    });
+}
+
+int ef_hps_mixed_solve_blocks(ef_hps* h, int nblocks, const int* batch, int sweeps, const double* const* f,
+                              const double* const* a, const double* const* r, double* const* u) {
+    if (!h || !batch || !f || !a || !r || !u || nblocks < 0) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    for (int k = 0; k < nblocks; ++k) {
+        if (batch[k] < 1 || batch[k] > h->mixed->bmax()) return fail(EF_ERR_INVALID, "batch size out of range");
+        if (!f[k] || !a[k] || !r[k] || !u[k]) return fail(EF_ERR_INVALID, "null block array");
+    }
+    return guarded([&] {
+        efgb::Hps& H = *h->hps;
+        if (nblocks > 1 && !h->mixed2) {
+            if (!h->stream2) {
+                int st = cuda_status(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking), "lane stream");
+                if (st) return st;
+            }
+            h->mixed2 = std::make_unique<efgb::MixedSolver>(H, h->mixed->bmax(), h->mixed.get());
+            h->mixed2->set_stream(h->stream2);
+        }
+        // the second lane must not start before work already queued on the tree's stream
+        if (nblocks > 1) {
+            cudaEvent_t ready;
+            int st = cuda_status(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "lane event");
+            if (!st) st = cuda_status(cudaEventRecord(ready, h->mixed->stream()), "lane event");
+            if (!st) st = cuda_status(cudaStreamWaitEvent(h->stream2, ready, 0), "lane event");
+            cudaEventDestroy(ready);
+            if (st) return st;
+        }
+        const size_t cells1 = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();
+        const size_t m1 = 4 * size_t(H.root_M());
+        for (int k = 0; k < nblocks; ++k) {
+            efgb::MixedSolver& X = (k & 1) ? *h->mixed2 : *h->mixed;
+            cudaStream_t s = X.stream();
+            const size_t cells = cells1 * batch[k], m = m1 * batch[k];
+            int st = cuda_status(cudaMemcpyAsync(X.f(), f[k], cells * 8, cudaMemcpyHostToDevice, s), "copy f");
+            if (!st) st = cuda_status(cudaMemcpyAsync(X.a(), a[k], m * 8, cudaMemcpyHostToDevice, s), "copy a");
+            if (!st) st = cuda_status(cudaMemcpyAsync(X.r(), r[k], m * 8, cudaMemcpyHostToDevice, s), "copy r");
+            if (st) return st;
+            X.solve(batch[k], sweeps);
+            st = cuda_status(cudaGetLastError(), "mixed solve launch");
+            if (!st) st = cuda_status(cudaMemcpyAsync(u[k], X.u(), cells * 8, cudaMemcpyDeviceToHost, s), "copy u");
+            if (st) return st;
+        }
+        int st = EF_OK;
+        int err = 0;
+        if (nblocks > 0) err |= h->mixed->take_error();  // synchronises the lane's stream
+        if (nblocks > 1) err |= h->mixed2->take_error();
+        if (err) return fail(EF_ERR_CUDA, "mixed solve: an operator tile copy did not complete");
         return st;
     });
 }
@@ -683,6 +744,14 @@ int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lane
         auto s = std::make_unique<ef_server>();
         s->srv = std::make_unique<efgb::Server>(specs, lanes_per_tree, hbm_budget_bytes, sweeps);
         *out = s.release();
+        return EF_OK;
+    });
+}
+
+int ef_server_set_sweeps(ef_server* server, int tree, int sweeps) {
+    if (!server) return fail(EF_ERR_INVALID, "null server");
+    return guarded([&] {
+        server->srv->set_sweeps(tree, sweeps);
         return EF_OK;
     });
 }

@@ -11,8 +11,7 @@ void sck(cudaError_t e, const char* what) {
 }
 }  // namespace
 
-Server::Server(const std::vector<TreeSpec>& trees, int lanes_per_tree, long long hbm_budget, int sweeps)
-    : sweeps_(sweeps) {
+Server::Server(const std::vector<TreeSpec>& trees, int lanes_per_tree, long long hbm_budget, int sweeps) {
     if (trees.empty()) throw std::invalid_argument("server: no trees");
     if (lanes_per_tree < 1 || lanes_per_tree > 8) throw std::invalid_argument("server: lanes per tree must be in [1, 8]");
     if (sweeps < 0 || sweeps + 1 > MixedSolver::kMaxPasses) throw std::invalid_argument("server: sweeps out of range");
@@ -25,6 +24,7 @@ Server::Server(const std::vector<TreeSpec>& trees, int lanes_per_tree, long long
                 throw std::invalid_argument("server: tree not built");
             trees_[t].hps = trees[t].hps;
             trees_[t].bmax = trees[t].bmax;
+            trees_[t].sweeps.store(sweeps);
             Lane l;
             l.ms = std::make_unique<MixedSolver>(*trees[t].hps, trees[t].bmax);
             bytes_ += (long long)l.ms->device_bytes();
@@ -124,6 +124,12 @@ int Server::wait(long long id, double timeout, double* latency) {
     }
 }
 
+void Server::set_sweeps(int tree, int sweeps) {
+    if (tree < 0 || tree >= int(trees_.size())) throw std::invalid_argument("server: tree index out of range");
+    if (sweeps < 0 || sweeps + 1 > MixedSolver::kMaxPasses) throw std::invalid_argument("server: sweeps out of range");
+    trees_[tree].sweeps.store(sweeps);
+}
+
 Server::Stats Server::stats() {
     std::lock_guard<std::mutex> g(mu_);
     return stats_;
@@ -140,7 +146,7 @@ void Server::launch(Tree& t, Lane& l) {
         sck(cudaMemcpyAsync(X.a() + b * m, q.a, m * 8, cudaMemcpyHostToDevice, l.st), "server copy a");
         sck(cudaMemcpyAsync(X.r() + b * m, q.r, m * 8, cudaMemcpyHostToDevice, l.st), "server copy r");
     }
-    X.solve(B, sweeps_);
+    X.solve(B, t.sweeps.load());
     sck(cudaGetLastError(), "server block solve");
     for (int b = 0; b < B; ++b)
         sck(cudaMemcpyAsync(l.batch[b].u, X.u() + b * cells, cells * 8, cudaMemcpyDeviceToHost, l.st), "server copy u");

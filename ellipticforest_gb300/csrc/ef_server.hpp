@@ -12,6 +12,7 @@
 // each request's data independently in a fixed order).
 #pragma once
 
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -52,6 +53,8 @@ public:
     // waits up to timeout seconds; returns 1 when done, 0 on time-out
     int wait(long long id, double timeout, double* latency);
     Stats stats();
+    // FP64 refinement sweeps of the tree's later blocks (the creation value until set)
+    void set_sweeps(int tree, int sweeps);
     int lanes(int tree) const { return int(trees_.at(tree).lanes.size()); }
     long long device_bytes() const { return bytes_; }
 
@@ -73,6 +76,7 @@ private:
     struct Tree {
         Hps* hps = nullptr;
         int bmax = 1;
+        std::atomic<int> sweeps{1};
         std::vector<Lane> lanes;
         std::deque<Req> queue;
     };
@@ -81,7 +85,6 @@ private:
     void launch(Tree& t, Lane& l);
 
     std::vector<Tree> trees_;
-    int sweeps_;
     long long bytes_ = 0;
     std::mutex mu_;
     std::condition_variable cv_work_, cv_done_;

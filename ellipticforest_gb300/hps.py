@@ -588,6 +588,25 @@ class HPSAlgorithm:
         check(_lib.load().ef_hps_mixed_solve(self._h, B, int(sweeps), dptr(f), dptr(a), dptr(r), dptr(u)))
         return u
 
+    def mixed_solve_blocks(self, blocks, sweeps: int = 1, out=None):
+        """Pipelined form of mixed_solve for many blocks: blocks is a sequence of (f, a, r) arrays
+        shaped as for mixed_solve (each block at most mixed_bmax requests); the blocks alternate
+        between two lanes so that host copies overlap the solves.  Returns (or fills) one u array per
+        block.  Page-locked arrays keep the copies asynchronous."""
+        blocks = [tuple(np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64) for x in blk) for blk in blocks]
+        nb = len(blocks)
+        for f, a, r in blocks:
+            B = f.shape[0]
+            if f.shape[1] != self.num_leaves * self.n * self.n or a.shape != (B, 4 * self.M) or r.shape != (B, 4 * self.M):
+                raise ValueError("mixed_solve_blocks: bad shapes")
+        us = out if out is not None else [np.empty_like(f) for f, _, _ in blocks]
+        batch = (C.c_int * nb)(*[f.shape[0] for f, _, _ in blocks])
+        ptr = lambda xs: (C.c_void_p * nb)(*[x.ctypes.data for x in xs])
+        check(_lib.load().ef_hps_mixed_solve_blocks(self._h, nb, batch, int(sweeps), ptr([b[0] for b in blocks]),
+                                                    ptr([b[1] for b in blocks]), ptr([b[2] for b in blocks]),
+                                                    ptr(us)))
+        return us
+
     def mixed_residuals(self, passes: int) -> np.ndarray:
         out = np.empty((passes, self.mixed_bmax))
         check(_lib.load().ef_hps_mixed_residuals(self._h, int(passes), dptr(out)))
@@ -642,9 +661,10 @@ class Server:
     solver; the scheduler thread of the library forms a block from every request of a tree that has
     arrived whenever one of the tree's lanes is free, and overlaps blocks of different lanes and trees
     on the GPU.  Lanes beyond the first per tree are created only while the device memory of all
-    lanes fits hbm_budget_bytes (0: no limit)."""
+    lanes fits hbm_budget_bytes (0: no limit).  sweeps: FP64 refinement sweeps per block, one value
+    for every tree or one per tree."""
 
-    def __init__(self, trees, bmax, lanes: int = 2, hbm_budget_bytes: int = 0, sweeps: int = 1):
+    def __init__(self, trees, bmax, lanes: int = 2, hbm_budget_bytes: int = 0, sweeps=1):
         trees = list(trees)
         bmax = [int(b) for b in (bmax if hasattr(bmax, "__len__") else [bmax] * len(trees))]
         if len(bmax) != len(trees):
@@ -654,9 +674,18 @@ class Server:
         arr = (C.c_void_p * len(trees))(*[t.handle for t in trees])
         bm = (C.c_int * len(trees))(*bmax)
         h = C.c_void_p()
-        check(lib.ef_server_create(arr, bm, len(trees), int(lanes), int(hbm_budget_bytes), int(sweeps), C.byref(h)))
+        sw = [int(x) for x in (sweeps if hasattr(sweeps, "__len__") else [sweeps] * len(trees))]
+        if len(sw) != len(trees):
+            raise ValueError("Server: one sweeps value per tree")
+        check(lib.ef_server_create(arr, bm, len(trees), int(lanes), int(hbm_budget_bytes), sw[0], C.byref(h)))
         self._h = h
+        for t, x in enumerate(sw):
+            self.set_sweeps(t, x)
         self._live = {}  # id -> arrays kept alive until completion
+
+    def set_sweeps(self, tree: int, sweeps: int) -> None:
+        """FP64 refinement sweeps of the tree's blocks from the next block on."""
+        check(_lib.load().ef_server_set_sweeps(self._h, int(tree), int(sweeps)))
 
     def lanes(self, tree: int) -> int:
         n = C.c_int()

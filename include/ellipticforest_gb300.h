@@ -154,6 +154,13 @@ int ef_hps_mixed_solve_async(ef_hps* hps, int batch, int sweeps);
 /* Host convenience form: copies the inputs in, solves, copies u out (synchronous). */
 int ef_hps_mixed_solve(ef_hps* hps, int batch, int sweeps, const double* f_host, const double* a_host,
                        const double* r_host, double* u_host);
+/* Pipelined host form for many blocks: block k (batch[k] <= bmax requests, host arrays f[k], a[k],
+ * r[k] in and u[k] out, each laid out as for ef_hps_mixed_solve) runs on one of two lanes that
+ * share the tree's FP32 operators, alternating, each lane on its own stream, so the copies of one
+ * block overlap the solve of the other (page-locked host memory keeps the copies asynchronous).
+ * Returns when every block's u is on the host.  The second lane holds its own block buffers. */
+int ef_hps_mixed_solve_blocks(ef_hps* hps, int nblocks, const int* batch, int sweeps, const double* const* f_host,
+                              const double* const* a_host, const double* const* r_host, double* const* u_host);
 /* max |leaf residual| per request before each pass: passes x bmax doubles (synchronous). */
 int ef_hps_mixed_residuals(ef_hps* hps, int passes, double* out_host);
 
@@ -228,6 +235,8 @@ int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, double x_upper, 
 typedef struct ef_server ef_server;
 int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lanes_per_tree,
                      long long hbm_budget_bytes, int sweeps, ef_server** out);
+/* FP64 refinement sweeps of tree t's blocks from the next block on (creation value: sweeps) */
+int ef_server_set_sweeps(ef_server* server, int tree, int sweeps);
 /* lanes created for tree t (after the budget) and device bytes held by all lanes */
 int ef_server_info(ef_server* server, int tree, int* lanes, long long* device_bytes);
 /* f (leaves*n*n), a and r (4M, WESN root face centres) and u (leaves*n*n) are host arrays that

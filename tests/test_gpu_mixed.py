@@ -184,3 +184,14 @@ def test_mixed_residual_forms_one_sweep(ef, dom, lam, zero_f):
     u = hps.mixed_solve(F, A, R, sweeps=1)
     for k in range(3):
         assert np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max() <= TOL, k
+
+
+def test_mixed_solve_blocks_matches_single_blocks(ef):
+    """The pipelined two-lane form returns, block by block, exactly what one block at a time gives."""
+    mesh, hps = make(ef, ("uniform", 3), 16, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, 10, 41)
+    hps.mixed_init(4)
+    blocks = [(F[0:4], A[0:4], R[0:4]), (F[4:8], A[4:8], R[4:8]), (F[8:10], A[8:10], R[8:10])]
+    got = hps.mixed_solve_blocks(blocks, sweeps=1)
+    for (f, a, r), u in zip(blocks, got):
+        assert np.array_equal(u, hps.mixed_solve(f, a, r, sweeps=1))

@@ -45,7 +45,8 @@ def test_server_mix_equals_alone(ef):
     N = 40
     plan = [(int(rng.integers(0, 2)), 100 + k) for k in range(N)]
     reqs = [request(*trees[t], seed) for t, seed in plan]
-    srv = ef.Server([h for _, h in trees], bmax=[6, 5], lanes=2, sweeps=1)
+    sweeps = [1, 2]  # per tree: the adaptive tree gets a second refinement sweep
+    srv = ef.Server([h for _, h in trees], bmax=[6, 5], lanes=2, sweeps=sweeps)
     assert srv.lanes(0) == 2 and srv.lanes(1) == 2
     ids = [None] * N
 
@@ -67,7 +68,7 @@ def test_server_mix_equals_alone(ef):
     for k, (t, _) in enumerate(plan):
         mesh, hps = trees[t]
         f, a, r = reqs[k]
-        alone = hps.mixed_solve(f[None], a[None], r[None], sweeps=1)[0]
+        alone = hps.mixed_solve(f[None], a[None], r[None], sweeps=sweeps[t])[0]
         assert np.array_equal(results[k][0], alone), k
         hps.upwards_array(f)
         hps.solve_arrays(a, np.zeros_like(a), r)
