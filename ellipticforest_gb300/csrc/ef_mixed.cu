@@ -698,11 +698,11 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
 //    are exact integer sums below 2^62: the cancellation that costs an FP64 stencil its digits
 //    happens without rounding;
 //  - the products cx Sx, cy Sy, lambda M_C are exact 128-bit products with the coefficients'
-//    64-bit significands, shifted to the fixed scale 2^sc on which the item's largest |f| is just
-//    below 2^61; r = F - P is one exact subtraction, rounded to FP32 at the end.  The error is a
-//    few units of 2^sc, about 2^-59 of the item's largest |f| (an FP64 stencil errs by 2^-53 of
-//    |u|/h^2).  A cell whose products do not fit on that scale (f small against the stencil
-//    terms, as for f = 0) forms the same exact sum on the scale of its own largest term.
+//    64-bit significands, shifted to one fixed scale 2^sc per item on which the item's largest |f|
+//    and largest product are just below 2^61 (a first sweep over the tile measures the largest
+//    second difference); r = F - P is one exact subtraction, rounded to FP32 at the end.  The
+//    error is a few units of 2^sc, about 2^-59 of the item's largest term (an FP64 stencil errs
+//    by 2^-53 of |u|/h^2 per cell).
 // Items (leaf, b) with b fastest; each thread owns 4 consecutive cells of one row; the fixed-point
 // tile of an item lives in shared memory, and the ghost data and edge fluxes ([4n][B] in HBM) pass
 // through shared memory so that a block's consecutive requests read and write them together.
@@ -729,30 +729,18 @@ __device__ __forceinline__ long long fx_from(double v, int E) { return fx_shift(
 __device__ __forceinline__ long long fx_scaled(double v, int sc) {
     return fx_bexp(v) ? fx_shift(v, 1075 + sc) : 0ll;
 }
-// |S| · m as a 128-bit product (hi, lo)
-__device__ __forceinline__ void fx_mul128(unsigned long long a, unsigned long long m, unsigned long long& hi,
-                                          unsigned long long& lo) {
-    hi = __umul64hi(a, m);
-    lo = a * m;
+// number of significant bits of |S|
+__device__ __forceinline__ int fx_bitlen64(long long S) {
+    const unsigned long long a = S < 0 ? 0ull - (unsigned long long)S : (unsigned long long)S;
+    return a ? 64 - __clzll((long long)a) : 0;
 }
-// v = (hi:lo) · 2^-d (d may be negative), truncated; false when v would reach 2^61
-__device__ __forceinline__ bool fx_shr128(unsigned long long hi, unsigned long long lo, int d, unsigned long long& v) {
-    if (d >= 128) { v = 0ull; return true; }
-    if (d >= 64) { v = hi >> (d - 64); return v < (1ull << 61); }
-    if (d > 0) {
-        if (hi >> d) return false;
-        v = (hi << (64 - d)) | (lo >> d);
-        return v < (1ull << 61);
-    }
-    if (hi) return false;
-    if (d <= -61) return lo == 0ull ? (v = 0ull, true) : false;
-    if (lo >> (61 + d)) return false;
-    v = lo << -d;
-    return true;
-}
-// number of significant bits of (hi:lo)
-__device__ __forceinline__ int fx_bitlen128(unsigned long long hi, unsigned long long lo) {
-    return hi ? 128 - __clzll((long long)hi) : (lo ? 64 - __clzll((long long)lo) : 0);
+// S · m / 2^d with the exact 128-bit product |S| · m (m a 64-bit significand), truncated toward
+// zero, negated when neg; 1 <= d and the caller keeps the result below 2^61
+__device__ __forceinline__ long long fx_term(long long S, unsigned long long m, int d, bool neg) {
+    const unsigned long long a = S < 0 ? 0ull - (unsigned long long)S : (unsigned long long)S;
+    const unsigned long long hi = __umul64hi(a, m), lo = a * m;
+    const unsigned long long v = d >= 128 ? 0ull : d >= 64 ? hi >> (d - 64) : (hi << (64 - d)) | (lo >> d);
+    return ((S < 0) != neg) ? -(long long)v : (long long)v;
 }
 // R · 2^sc as FP32, rounded to nearest (ties to even); below the normal range -> signed zero,
 // above -> inf
@@ -802,7 +790,7 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     // per item: n*n fixed-point cells, 4n fixed-point ghosts, 4n FP64 ghosts (later the fluxes)
     extern __shared__ long long fx_tile[];
     __shared__ unsigned smax[64];
-    __shared__ int seu[64], sef[64];
+    __shared__ int seu[64], sef[64], sbx[64], sby[64];
     __shared__ const double* sg[64];
     __shared__ double* sh[64];
     const int n = NT ? NT : n_arg;
@@ -816,6 +804,8 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
         smax[threadIdx.x] = 0u;
         seu[threadIdx.x] = 1;
         sef[threadIdx.x] = 1;
+        sbx[threadIdx.x] = 0;
+        sby[threadIdx.x] = 0;
         const int it = item0 + int(threadIdx.x);
         if ((long long)it < items) {
             const int lf = it / B, bb = it - lf * B;
@@ -880,93 +870,91 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     }
     __syncthreads();
     // (3) exact second differences and products, one subtraction
+    const bool lam = FORM != 0 && cf.lmm != 0ull, iso = FORM == 0 || cf.iso != 0;
+    // the cell's fixed-point centre and second differences (iso: sx = Sx + Sy, the y term unused)
+    auto diffs = [&](int e, long long (&c)[4], long long (&sx)[4], long long (&sy)[4]) {
+        const int i = e / n, j0 = e - i * n;
+        long long xm[4], xp[4];
+        {
+            const longlong2 a = reinterpret_cast<const longlong2*>(tile + e)[0];
+            const longlong2 d = reinterpret_cast<const longlong2*>(tile + e)[1];
+            c[0] = a.x; c[1] = a.y; c[2] = d.x; c[3] = d.y;
+        }
+        if (i > 0) {
+            const longlong2 a = reinterpret_cast<const longlong2*>(tile + e - n)[0];
+            const longlong2 d = reinterpret_cast<const longlong2*>(tile + e - n)[1];
+            xm[0] = a.x; xm[1] = a.y; xm[2] = d.x; xm[3] = d.y;
+        } else {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) xm[t] = 2 * gfx[j0 + t] - c[t];
+        }
+        if (i < n - 1) {
+            const longlong2 a = reinterpret_cast<const longlong2*>(tile + e + n)[0];
+            const longlong2 d = reinterpret_cast<const longlong2*>(tile + e + n)[1];
+            xp[0] = a.x; xp[1] = a.y; xp[2] = d.x; xp[3] = d.y;
+        } else {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) xp[t] = 2 * gfx[n + j0 + t] - c[t];
+        }
+        const long long left = j0 > 0 ? tile[e - 1] : 2 * gfx[2 * n + i] - c[0];
+        const long long right = j0 + 4 < n ? tile[e + 4] : 2 * gfx[3 * n + i] - c[3];
+        const long long ym[4] = {left, c[0], c[1], c[2]};
+        const long long yp[4] = {c[1], c[2], c[3], right};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            sx[t] = xm[t] + xp[t] - 2 * c[t];
+            sy[t] = ym[t] + yp[t] - 2 * c[t];
+            if (iso) sx[t] += sy[t];  // |Sx + Sy| < 1.5 * 2^62
+        }
+    };
+    // (3a) bit length of the item's largest second difference (per direction)
+    int bx = 0, by = 0;
+    if (act)
+        for (int e4 = lt; e4 < tpi; e4 += tpe) {
+            long long c[4], sx[4], sy[4];
+            diffs(4 * e4, c, sx, sy);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                bx = max(bx, fx_bitlen64(sx[t]));
+                if (!iso) by = max(by, fx_bitlen64(sy[t]));
+            }
+        }
+    if (seg)
+        for (int o = 1; o < tpe && o < 32; o <<= 1) {
+            bx = max(bx, __shfl_xor_sync(0xffffffffu, bx, o));
+            by = max(by, __shfl_xor_sync(0xffffffffu, by, o));
+        }
+    if (act && (!seg || (lt & 31) == 0)) {
+        atomicMax(&sbx[slot], bx);
+        atomicMax(&sby[slot], by);
+    }
+    __syncthreads();
+    // (3b) common fixed scale 2^sc: |F| < 2^61 and every product < 2^61 (a term carries
+    // 2^(Eu - 1081) times a coefficient below 2^e_coef), so F and up to three terms sum without
+    // overflow and the error is a few units of 2^sc, 2^-59 of the item's largest term
     float mx = 0.f;
     if (act) {
         const bool bad = Eu == 0x7ff || Ef == 0x7ff;
-        const bool lam = FORM != 0 && cf.lmm != 0ull, iso = FORM == 0 || cf.iso != 0;
-        // common fixed scale 2^sc with |F| < 2^61; the 128-bit products carry 2^(Eu - 1081 + e - 64)
-        // and shift right by d to it; F and up to three terms below 2^61 sum without overflow
-        const int sc = Ef - 1083;
+        int top = sbx[slot] + Eu - 1081 + cf.ecx;
+        if (!iso) top = max(top, sby[slot] + Eu - 1081 + cf.ecy);
+        if (lam) top = max(top, 59 + Eu - 1081 + cf.elm);
+        const int sc = max(Ef - 1083, top - 61);
+        // the 128-bit products carry 2^(Eu - 1145 + e_coef): right shifts d >= 3 to the common scale
         const int dx = sc - (Eu - 1145 + cf.ecx), dy = sc - (Eu - 1145 + cf.ecy), dl = sc - (Eu - 1145 + cf.elm);
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
-            const int e = 4 * e4, i = e / n, j0 = e - i * n;
-            long long c[4], xm[4], xp[4];
-            {
-                const longlong2 a = reinterpret_cast<const longlong2*>(tile + e)[0];
-                const longlong2 d = reinterpret_cast<const longlong2*>(tile + e)[1];
-                c[0] = a.x; c[1] = a.y; c[2] = d.x; c[3] = d.y;
-            }
-            if (i > 0) {
-                const longlong2 a = reinterpret_cast<const longlong2*>(tile + e - n)[0];
-                const longlong2 d = reinterpret_cast<const longlong2*>(tile + e - n)[1];
-                xm[0] = a.x; xm[1] = a.y; xm[2] = d.x; xm[3] = d.y;
-            } else {
-#pragma unroll
-                for (int t = 0; t < 4; ++t) xm[t] = 2 * gfx[j0 + t] - c[t];
-            }
-            if (i < n - 1) {
-                const longlong2 a = reinterpret_cast<const longlong2*>(tile + e + n)[0];
-                const longlong2 d = reinterpret_cast<const longlong2*>(tile + e + n)[1];
-                xp[0] = a.x; xp[1] = a.y; xp[2] = d.x; xp[3] = d.y;
-            } else {
-#pragma unroll
-                for (int t = 0; t < 4; ++t) xp[t] = 2 * gfx[n + j0 + t] - c[t];
-            }
-            const long long left = j0 > 0 ? tile[e - 1] : 2 * gfx[2 * n + i] - c[0];
-            const long long right = j0 + 4 < n ? tile[e + 4] : 2 * gfx[3 * n + i] - c[3];
-            const long long ym[4] = {left, c[0], c[1], c[2]};
-            const long long yp[4] = {c[1], c[2], c[3], right};
+            const int e = 4 * e4;
+            long long c[4], sx[4], sy[4];
+            diffs(e, c, sx, sy);
             const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
             const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
             const double fv[4] = {f01.x, f01.y, f23.x, f23.y};
             float rr[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                const long long sx = xm[t] + xp[t] - 2 * c[t], sy = ym[t] + yp[t] - 2 * c[t];
-                // terms (S, significand, shift, sign): cx = cy takes one product of the exact sum
-                // (|sx + sy| < 1.5 * 2^62)
-                const long long s0 = iso ? sx + sy : sx;
-                unsigned long long h0, l0, h1 = 0ull, l1 = 0ull, h2 = 0ull, l2 = 0ull, v;
-                fx_mul128(s0 < 0 ? 0ull - (unsigned long long)s0 : (unsigned long long)s0, cf.cxm, h0, l0);
-                if (!iso) fx_mul128(sy < 0 ? 0ull - (unsigned long long)sy : (unsigned long long)sy, cf.cym, h1, l1);
-                if (lam) fx_mul128(c[t] < 0 ? 0ull - (unsigned long long)c[t] : (unsigned long long)c[t], cf.lmm, h2, l2);
-                const bool n0 = s0 < 0, n1 = sy < 0, n2 = (c[t] < 0) != (cf.lm_neg != 0);
-                const long long F = fx_scaled(fv[t], sc);
-                long long R = F;
-                bool fits = fx_shr128(h0, l0, dx, v);
-                R -= n0 ? -(long long)v : (long long)v;
-                if (!iso) {
-                    fits = fx_shr128(h1, l1, dy, v) && fits;
-                    R -= n1 ? -(long long)v : (long long)v;
-                }
-                if (lam) {
-                    fits = fx_shr128(h2, l2, dl, v) && fits;
-                    R -= n2 ? -(long long)v : (long long)v;
-                }
-                float r;
-                if (fits) {
-                    r = fx_to_float(R, sc);
-                } else {
-                    // the same exact sum on the coarser scale 2^sc2 of this cell's largest term
-                    int top = sc + 61;
-                    top = max(top, sc - dx + fx_bitlen128(h0, l0));
-                    if (!iso) top = max(top, sc - dy + fx_bitlen128(h1, l1));
-                    if (lam) top = max(top, sc - dl + fx_bitlen128(h2, l2));
-                    const int sc2 = top - 61;
-                    R = fx_scaled(fv[t], sc2);
-                    fx_shr128(h0, l0, dx + sc2 - sc, v);
-                    R -= n0 ? -(long long)v : (long long)v;
-                    if (!iso) {
-                        fx_shr128(h1, l1, dy + sc2 - sc, v);
-                        R -= n1 ? -(long long)v : (long long)v;
-                    }
-                    if (lam) {
-                        fx_shr128(h2, l2, dl + sc2 - sc, v);
-                        R -= n2 ? -(long long)v : (long long)v;
-                    }
-                    r = fx_to_float(R, sc2);
-                }
-                rr[t] = bad ? __int_as_float(0x7fffffff) : r;
+                long long R = fx_scaled(fv[t], sc) - fx_term(sx[t], cf.cxm, dx, false);
+                if (!iso) R -= fx_term(sy[t], cf.cym, dy, false);
+                if (lam) R -= fx_term(c[t], cf.lmm, dl, cf.lm_neg != 0);
+                rr[t] = bad ? __int_as_float(0x7fffffff) : fx_to_float(R, sc);
                 mx = fmaxf(mx, fabsf(rr[t]));
             }
             *reinterpret_cast<float4*>(q + base + e) = make_float4(rr[0], rr[1], rr[2], rr[3]);
