@@ -907,16 +907,19 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
             if (iso) sx[t] += sy[t];  // |Sx + Sy| < 1.5 * 2^62
         }
     };
-    // (3a) bit length of the item's largest second difference (per direction)
+    // (3a) bit length of the item's largest second difference (per direction).  With the leaf size
+    // fixed at compile time every thread owns one group of 4 cells (n*n/4 <= 256): its differences
+    // stay in registers for (3b)
+    constexpr bool ONE = NT != 0 && NT * NT / 4 <= 256;
     int bx = 0, by = 0;
+    long long c1[4], sx1[4], sy1[4];
     if (act)
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
-            long long c[4], sx[4], sy[4];
-            diffs(4 * e4, c, sx, sy);
+            diffs(4 * e4, c1, sx1, sy1);
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                bx = max(bx, fx_bitlen64(sx[t]));
-                if (!iso) by = max(by, fx_bitlen64(sy[t]));
+                bx = max(bx, fx_bitlen64(sx1[t]));
+                if (!iso) by = max(by, fx_bitlen64(sy1[t]));
             }
         }
     if (seg)
@@ -944,7 +947,16 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
             const int e = 4 * e4;
             long long c[4], sx[4], sy[4];
-            diffs(e, c, sx, sy);
+            if (ONE) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    c[t] = c1[t];
+                    sx[t] = sx1[t];
+                    sy[t] = sy1[t];
+                }
+            } else {
+                diffs(e, c, sx, sy);
+            }
             const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
             const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
             const double fv[4] = {f01.x, f01.y, f23.x, f23.y};
