@@ -47,9 +47,9 @@ __device__ __forceinline__ void mx_child_ifaces(int c, int& Ia, int& Ib) {
 
 // float <-> double by integer bit manipulation.  GB300's FP64 pipe, which also converts between the
 // two widths, runs at a small fraction of its FP32 and integer rates; these stay off it.  Values
-// below the smallest normal number of the target type become signed zeros; d2f_bits rounds toward
-// zero, d2f_rn_bits to nearest (ties to even) -- residuals use the latter, since a one-signed
-// rounding of every residual entry biases the correction it drives.
+// below the smallest normal number of the target type become signed zeros; d2f_rn_bits rounds to
+// nearest (ties to even): a one-signed rounding of every residual entry would bias the correction
+// it drives.
 __device__ __forceinline__ double f2d_bits(float x) {
     const unsigned b = __float_as_uint(x);
     const unsigned e = (b >> 23) & 0xffu;
@@ -58,34 +58,20 @@ __device__ __forceinline__ double f2d_bits(float x) {
     const unsigned long long e64 = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
     return __longlong_as_double((long long)(sign | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
 }
-__device__ __forceinline__ float d2f_bits(double x) {
+__device__ __forceinline__ float d2f_rn_bits(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    const int e = int((b >> 52) & 0x7ffull);
-    const unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
+    const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = int(hi >> 20) & 0x7ff;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
     if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
     const int e32 = e - 896;
     if (e32 <= 0) return __uint_as_float(sign);
     if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
-}
-__device__ __forceinline__ float d2f_rn_bits(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    const int e = int((b >> 52) & 0x7ffull);
-    unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
-    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
-    int e32 = e - 896;
-    if (e32 <= 0) return __uint_as_float(sign);
-    const unsigned rest = unsigned(b & 0x1fffffffull);
-    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) {
-        if (++m >> 23) {
-            m = 0u;
-            ++e32;
-        }
-    }
-    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
+    const unsigned rest = lo & 0x1fffffffu;
+    // a carry out of the significand steps the exponent (up to the infinity pattern)
+    const unsigned up = (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | ((unsigned(e32) << 23) + m + up));
 }
 
 // ---- FP32 pass, upward ---------------------------------------------------------------------------
@@ -113,7 +99,6 @@ __global__ void k_mx_hdiff(const MixItem* __restrict__ items, int s, int B) {
 //   H    : h  = H [w_Ia; w_Ib] + hc rows 8s, K 2s (compact H; a tile never spans two children)
 //   DOWN : u  = S gf + w           rows 4s, K 8s; u goes to both children and into u_Gamma (FP64)
 constexpr int kKC = 32;      // K columns per stage (128 bytes of FP32: one swizzle row)
-constexpr int kRT = 64;      // rows per tile (at most)
 constexpr int kStages = 3;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -824,11 +809,14 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     long long* gfx = tile + nn;
     double* gd = reinterpret_cast<double*>(gfx + n4);
     const int nact = (long long)item0 + ipc <= items ? ipc : int(items - item0);
+    // items per block, a compile-time constant for the fixed leaf sizes
+    const int IPC = NT ? 256 / (NT * NT / 4 < 256 ? NT * NT / 4 : 256) : ipc;
     // (0) ghost data of the block's items, requests fastest: the items of a block are consecutive
     // requests of one leaf whenever B is a multiple of ipc, so these reads coalesce
-    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
-        const int k = idx / nact, s = idx - k * nact;
-        reinterpret_cast<double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k] = sg[s][(long long)k * B];
+    for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
+        const int k = idx / IPC, s = idx - k * IPC;
+        if (s < nact)
+            reinterpret_cast<double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k] = sg[s][(long long)k * B];
     }
     __syncthreads();
     // (1) scales: largest biased exponents of u and the ghosts (Eu), and of f (Ef)
@@ -985,9 +973,10 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
         for (int o = 1; o < tpe && o < 32; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (act && (!seg || (lt & 31) == 0)) atomicMax(&smax[slot], __float_as_uint(mx));
     __syncthreads();
-    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
-        const int k = idx / nact, s = idx - k * nact;
-        sh[s][(long long)k * B] = reinterpret_cast<const double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k];
+    for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
+        const int k = idx / IPC, s = idx - k * IPC;
+        if (s < nact)
+            sh[s][(long long)k * B] = reinterpret_cast<const double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k];
     }
     if (rleaf && act && lt == 0) rleaf[(long long)b * L + leaf] = __uint_as_float(smax[slot]);
 }
@@ -1001,7 +990,7 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
                                                            const MixLeaf* __restrict__ leaves, int L, int B,
                                                            int n_arg, int ipc, const double* __restrict__ f,
                                                            float* __restrict__ q, float* __restrict__ rleaf) {
-    extern __shared__ double r0_gd[];  // per item: 4n ghost values, later the fluxes
+    extern __shared__ double r0_gd[];  // per item: 4n ghost values, later the fluxes; then 4n floats
     __shared__ unsigned smax[64];
     __shared__ const double* sg[64];
     __shared__ double* sh[64];
@@ -1023,20 +1012,27 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
     }
     __syncthreads();
     const int nact = (long long)item0 + ipc <= items ? ipc : int(items - item0);
-    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
-        const int k = idx / nact, s = idx - k * nact;
-        r0_gd[s * n4 + k] = sg[s][(long long)k * B];
+    const int IPC = NT ? 256 / (NT * NT / 4 < 256 ? NT * NT / 4 : 256) : ipc;
+    float* gt = reinterpret_cast<float*>(r0_gd + IPC * n4);  // per item: the ghost terms -2 c g (FP32)
+    for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
+        const int k = idx / IPC, s = idx - k * IPC;
+        if (s < nact) {
+            const double g = sg[s][(long long)k * B];
+            r0_gd[s * n4 + k] = g;
+            const MixCoef& c = coefs[leaves[(item0 + s) / B].type];
+            gt[s * n4 + k] = -2.0f * (k < 2 * n ? c.cx32 : c.cy32) * d2f_rn_bits(g);
+        }
     }
     __syncthreads();
     const int leaf = act ? item / B : 0;
     const int b = act ? item - leaf * B : 0;
     const MixCoef cf = coefs[leaves[leaf].type];
     double* gd = r0_gd + slot * n4;
+    const float* gts = gt + slot * n4;
     float mx = 0.f;
     if (act) {
         const long long base = ((long long)b * L + leaf) * nn;
         const double* ff = f + base;
-        const float cx2 = 2.0f * cf.cx32, cy2 = 2.0f * cf.cy32;
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
             const int e = 4 * e4, i = e / n, j0 = e - i * n;
             const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
@@ -1044,12 +1040,12 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
             float rr[4] = {d2f_rn_bits(f01.x), d2f_rn_bits(f01.y), d2f_rn_bits(f23.x), d2f_rn_bits(f23.y)};
             if (i == 0)
 #pragma unroll
-                for (int t = 0; t < 4; ++t) rr[t] = fmaf(-cx2, d2f_rn_bits(gd[j0 + t]), rr[t]);
+                for (int t = 0; t < 4; ++t) rr[t] += gts[j0 + t];
             if (i == n - 1)
 #pragma unroll
-                for (int t = 0; t < 4; ++t) rr[t] = fmaf(-cx2, d2f_rn_bits(gd[n + j0 + t]), rr[t]);
-            if (j0 == 0) rr[0] = fmaf(-cy2, d2f_rn_bits(gd[2 * n + i]), rr[0]);
-            if (j0 + 4 == n) rr[3] = fmaf(-cy2, d2f_rn_bits(gd[3 * n + i]), rr[3]);
+                for (int t = 0; t < 4; ++t) rr[t] += gts[n + j0 + t];
+            if (j0 == 0) rr[0] += gts[2 * n + i];
+            if (j0 + 4 == n) rr[3] += gts[3 * n + i];
 #pragma unroll
             for (int t = 0; t < 4; ++t) mx = fmaxf(mx, fabsf(rr[t]));
             *reinterpret_cast<float4*>(q + base + e) = make_float4(rr[0], rr[1], rr[2], rr[3]);
@@ -1067,9 +1063,9 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
         for (int o = 1; o < tpe && o < 32; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (act && (!seg || (lt & 31) == 0)) atomicMax(&smax[slot], __float_as_uint(mx));
     __syncthreads();
-    for (int idx = threadIdx.x; idx < n4 * nact; idx += blockDim.x) {
-        const int k = idx / nact, s = idx - k * nact;
-        sh[s][(long long)k * B] = r0_gd[s * n4 + k];
+    for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
+        const int k = idx / IPC, s = idx - k * IPC;
+        if (s < nact) sh[s][(long long)k * B] = r0_gd[s * n4 + k];
     }
     if (rleaf && act && lt == 0) rleaf[(long long)b * L + leaf] = __uint_as_float(smax[slot]);
 }
@@ -1304,7 +1300,7 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
     if (n % 4 != 0 || smem > 48 * 1024) throw std::invalid_argument("leaf residual: leaf size out of range");
     float* rl = rmax ? rleaf : nullptr;
     if (zero_state) {
-        const size_t smem0 = size_t(ipc) * 4 * size_t(n) * sizeof(double);
+        const size_t smem0 = size_t(ipc) * 4 * size_t(n) * (sizeof(double) + sizeof(float));
         if (n == 16)
             k_mx_leaf_residual0<16><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
         else if (n == 8)
