@@ -190,14 +190,13 @@ void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* 
 void mx_uncoarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate);
-// Stencil constants of a leaf type for the residual: cx = 1/dx^2, cy = 1/dy^2 and |lambda| as 64-bit
-// significands m (leading bit 63) with c = m 2^(e - 64) (lmm = 0 when lambda = 0), the sign of lambda,
-// iso when cx == cy; FP32 copies of cx, cy for the first residual; the FP64 edge-flux factors 2/dx,
-// 2/dy
+// Stencil constants of a leaf type for the residual: cx = 1/dx^2, cy = 1/dy^2 and lambda as signed
+// 63-bit significands m (|m| in [2^62, 2^63)) with c = m 2^(e - 63) (lmm = 0 when lambda = 0), iso
+// when cx == cy; FP32 copies of cx, cy for the first residual; the FP64 edge-flux factors 2/dx, 2/dy
 struct MixCoef {
     double dtn_x, dtn_y;
-    unsigned long long cxm, cym, lmm;
-    int ecx, ecy, elm, lm_neg, iso;
+    long long cxm, cym, lmm;
+    int ecx, ecy, elm, iso;
     float cx32, cy32;
 };
 // Residual of every leaf (n % 4 == 0, n <= 64): exact fixed-point second differences and 128-bit

@@ -714,39 +714,14 @@ __device__ __forceinline__ long long fx_from(double v, int E) { return fx_shift(
 __device__ __forceinline__ long long fx_scaled(double v, int sc) {
     return fx_bexp(v) ? fx_shift(v, 1075 + sc) : 0ll;
 }
-// number of significant bits of |S|
-__device__ __forceinline__ int fx_bitlen64(long long S) {
-    const unsigned long long a = S < 0 ? 0ull - (unsigned long long)S : (unsigned long long)S;
-    return a ? 64 - __clzll((long long)a) : 0;
-}
-// S · m / 2^d with the exact 128-bit product |S| · m (m a 64-bit significand), truncated toward
-// zero, negated when neg; 1 <= d and the caller keeps the result below 2^61
-__device__ __forceinline__ long long fx_term(long long S, unsigned long long m, int d, bool neg) {
-    const unsigned long long a = S < 0 ? 0ull - (unsigned long long)S : (unsigned long long)S;
-    const unsigned long long hi = __umul64hi(a, m), lo = a * m;
-    const unsigned long long v = d >= 128 ? 0ull : d >= 64 ? hi >> (d - 64) : (hi << (64 - d)) | (lo >> d);
-    return ((S < 0) != neg) ? -(long long)v : (long long)v;
-}
-// R · 2^sc as FP32, rounded to nearest (ties to even); below the normal range -> signed zero,
-// above -> inf
-__device__ __forceinline__ float fx_to_float(long long R, int sc) {
-    const unsigned sgn = R < 0 ? 0x80000000u : 0u;
-    const unsigned long long a = R < 0 ? 0ull - (unsigned long long)R : (unsigned long long)R;
-    if (a == 0ull) return 0.f;
-    const int lz = __clzll((long long)a);
-    const unsigned long long nrm = a << lz;
-    unsigned m = unsigned(nrm >> 40);  // 24 bits, leading one at bit 23
-    const unsigned long long rest = nrm & 0xffffffffffull;
-    int be = 127 + 63 - lz + sc;
-    if (rest > 0x8000000000ull || (rest == 0x8000000000ull && (m & 1u))) {
-        if (++m >> 24) {
-            m >>= 1;
-            ++be;
-        }
-    }
-    if (be <= 0) return __uint_as_float(sgn);
-    if (be >= 255) return __uint_as_float(sgn | 0x7f800000u);
-    return __uint_as_float(sgn | (unsigned(be) << 23) | (m & 0x7fffffu));
+// S · m / 2^d with the exact signed 128-bit product S · m (m a signed 63-bit significand), rounded
+// toward minus infinity; d >= 1 and the caller keeps the result below 2^61 in magnitude
+__device__ __forceinline__ long long fx_term(long long S, long long m, int d) {
+    const long long hi = __mul64hi(S, m);
+    const unsigned long long lo = (unsigned long long)S * (unsigned long long)m;
+    return d >= 128 ? (hi < 0 ? -1ll : 0ll)
+           : d >= 64 ? hi >> (d - 64)
+                     : (long long)(((unsigned long long)hi << (64 - d)) | (lo >> d));
 }
 // FP64 of D · 2^sc rounded to nearest (ties to even); |D| < 2^63, result inside the normal range
 __device__ __forceinline__ double fx_to_double(long long D, int sc) {
@@ -858,7 +833,7 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     }
     __syncthreads();
     // (3) exact second differences and products, one subtraction
-    const bool lam = FORM != 0 && cf.lmm != 0ull, iso = FORM == 0 || cf.iso != 0;
+    const bool lam = FORM != 0 && cf.lmm != 0, iso = FORM == 0 || cf.iso != 0;
     // the cell's fixed-point centre and second differences (iso: sx = Sx + Sy, the y term unused)
     auto diffs = [&](int e, long long (&c)[4], long long (&sx)[4], long long (&sy)[4]) {
         const int i = e / n, j0 = e - i * n;
@@ -904,11 +879,15 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     if (act)
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
             diffs(4 * e4, c1, sx1, sy1);
+            // OR of the one's-complement magnitudes has the bit length of the largest (to one bit)
+            unsigned long long ox = 0ull, oy = 0ull;
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                bx = max(bx, fx_bitlen64(sx1[t]));
-                if (!iso) by = max(by, fx_bitlen64(sy1[t]));
+                ox |= (unsigned long long)(sx1[t] ^ (sx1[t] >> 63));
+                if (!iso) oy |= (unsigned long long)(sy1[t] ^ (sy1[t] >> 63));
             }
+            bx = max(bx, ox ? 65 - __clzll((long long)ox) : 1);
+            if (!iso) by = max(by, oy ? 65 - __clzll((long long)oy) : 1);
         }
     if (seg)
         for (int o = 1; o < tpe && o < 32; o <<= 1) {
@@ -930,8 +909,12 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
         if (!iso) top = max(top, sby[slot] + Eu - 1081 + cf.ecy);
         if (lam) top = max(top, 59 + Eu - 1081 + cf.elm);
         const int sc = max(Ef - 1083, top - 61);
-        // the 128-bit products carry 2^(Eu - 1145 + e_coef): right shifts d >= 3 to the common scale
-        const int dx = sc - (Eu - 1145 + cf.ecx), dy = sc - (Eu - 1145 + cf.ecy), dl = sc - (Eu - 1145 + cf.elm);
+        // the 128-bit products carry 2^(Eu - 1144 + e_coef) (63-bit significands): right shifts d >= 2
+        // to the common scale; the result leaves through one int64 -> FP32 conversion and two exact
+        // power-of-two scalings
+        const int dx = sc - (Eu - 1144 + cf.ecx), dy = sc - (Eu - 1144 + cf.ecy), dl = sc - (Eu - 1144 + cf.elm);
+        const int sa = max(-126, min(127, sc)), sb = max(-126, min(127, sc - sa));
+        const float pa = __uint_as_float(unsigned(127 + sa) << 23), pb = __uint_as_float(unsigned(127 + sb) << 23);
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
             const int e = 4 * e4;
             long long c[4], sx[4], sy[4];
@@ -951,10 +934,10 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
             float rr[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                long long R = fx_scaled(fv[t], sc) - fx_term(sx[t], cf.cxm, dx, false);
-                if (!iso) R -= fx_term(sy[t], cf.cym, dy, false);
-                if (lam) R -= fx_term(c[t], cf.lmm, dl, cf.lm_neg != 0);
-                rr[t] = bad ? __int_as_float(0x7fffffff) : fx_to_float(R, sc);
+                long long R = fx_scaled(fv[t], sc) - fx_term(sx[t], cf.cxm, dx);
+                if (!iso) R -= fx_term(sy[t], cf.cym, dy);
+                if (lam) R -= fx_term(c[t], cf.lmm, dl);
+                rr[t] = bad ? __int_as_float(0x7fffffff) : __fmul_rn(__fmul_rn(__ll2float_rn(R), pa), pb);
                 mx = fmaxf(mx, fabsf(rr[t]));
             }
             *reinterpret_cast<float4*>(q + base + e) = make_float4(rr[0], rr[1], rr[2], rr[3]);

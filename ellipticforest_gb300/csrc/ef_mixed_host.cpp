@@ -11,11 +11,11 @@
 namespace efgb {
 
 namespace {
-// c = m 2^(e - 64) with m a 64-bit significand (leading bit 63); c = 0 gives m = 0
-void significand64(double c, unsigned long long& m, int& e) {
+// c = m 2^(e - 63) with m a signed 63-bit significand (|m| in [2^62, 2^63), exact); c = 0 gives m = 0
+void significand63(double c, long long& m, int& e) {
     int ex = 0;
-    const double fr = std::frexp(c, &ex);  // c = fr 2^ex, fr in [0.5, 1)
-    m = c == 0.0 ? 0ull : (unsigned long long)std::ldexp(fr, 64);
+    const double fr = std::frexp(c, &ex);  // c = fr 2^ex, |fr| in [0.5, 1)
+    m = c == 0.0 ? 0ll : (long long)std::ldexp(fr, 63);
     e = c == 0.0 ? 0 : ex;
 }
 }  // namespace
@@ -231,10 +231,9 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             MixCoef& c = co[t];
             c.dtn_x = 2.0 / dx;
             c.dtn_y = 2.0 / dy;
-            significand64(cx, c.cxm, c.ecx);
-            significand64(cy, c.cym, c.ecy);
-            significand64(std::fabs(lm), c.lmm, c.elm);
-            c.lm_neg = lm < 0.0 ? 1 : 0;
+            significand63(cx, c.cxm, c.ecx);
+            significand63(cy, c.cym, c.ecy);
+            significand63(lm, c.lmm, c.elm);
             c.iso = cx == cy ? 1 : 0;
             c.cx32 = float(cx);
             c.cy32 = float(cy);
