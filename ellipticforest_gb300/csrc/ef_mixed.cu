@@ -651,19 +651,32 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
             row[1] = v1;
         }
     } else {
+        // edge values u[i][j] = sum_l U1T[l][i] VT[l][j], four consecutive points of one side per
+        // step: W/E (i = 0, n-1) take a broadcast U1T[l][i] and a float4 of VT row l, S/N (j = 0,
+        // n-1) a float4 of U1T row l and a broadcast VT[l][j]; same sums, in the same order, as one
+        // point at a time
         const float dtn_x = 2.0f / ty.dx, dtn_y = 2.0f / ty.dy;
-        for (int r = lt; r < 4 * n; r += tpi) {
-            const int side = r / n, pos = r - (r / n) * n;
-            int i, j;
-            if (side == 0) { i = 0; j = pos; }
-            else if (side == 1) { i = n - 1; j = pos; }
-            else if (side == 2) { i = pos; j = 0; }
-            else { i = pos; j = n - 1; }
-            float u = 0.f;
+        for (int g4 = lt; g4 < n; g4 += tpi) {
+            const int side = (4 * g4) / n, p0 = 4 * g4 - side * n;
+            const int fixed = side == 0 || side == 2 ? 0 : n - 1;
+            const float* vec = side < 2 ? VT + p0 : W + p0;       // float4 along the side
+            const float* sca = side < 2 ? W + fixed : VT + fixed;  // broadcast per l
+            float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (int l = 0; l < (NT ? NT : n); ++l) u = fmaf(W[l * n + i], VT[l * n + j], u);
-            const float sg = (side == 0 || side == 2) ? 1.0f : -1.0f;
-            lf.h32[(long long)r * B + b] = sg * (side < 2 ? dtn_x : dtn_y) * u;
+            for (int l = 0; l < (NT ? NT : n); ++l) {
+                const float4 v = *reinterpret_cast<const float4*>(vec + l * n);
+                const float a = sca[l * n];
+                u.x = fmaf(a, v.x, u.x);
+                u.y = fmaf(a, v.y, u.y);
+                u.z = fmaf(a, v.z, u.z);
+                u.w = fmaf(a, v.w, u.w);
+            }
+            const float sc = ((side == 0 || side == 2) ? 1.0f : -1.0f) * (side < 2 ? dtn_x : dtn_y);
+            float* hp = lf.h32 + (long long)(side * n + p0) * B + b;
+            hp[0] = sc * u.x;
+            hp[(long long)B] = sc * u.y;
+            hp[2LL * B] = sc * u.z;
+            hp[3LL * B] = sc * u.w;
         }
     }
 }
