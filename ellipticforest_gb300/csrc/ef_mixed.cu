@@ -515,31 +515,42 @@ __global__ void k_mx_uncoarsen(const T* const* vin, T* const* vout, int nf, int 
 }
 
 // ---- leaves --------------------------------------------------------------------------------------
-// FP32 eigenbasis leaf pass over the items (leaf, b), b fastest.  One item is an n x n patch handled
-// by (n/4)^2 threads that each own a 4 x 4 block of every product
+// FP32 eigenbasis leaf pass over the items (leaf, b), b fastest.  A group of (n/4)^2 threads owns
+// two items; each thread owns a 4 x 4 block of every product of both
 //   WT = (V^T F)^T,  G = Dinv o (V^T F V),  U1T = (V G)^T,  u = V G V^T
-// with float4 operand reads from shared memory (V depends on n only, so one copy serves all types).
+// with float4 operand reads from shared memory.  One operand of every product is V (it depends on
+// n only, so one copy serves all leaf types): read once for the two items, it makes 3 shared loads
+// per 32 FMA instead of 4 -- the products are bound by shared-memory wavefronts (a 128-bit load
+// costs four).  Each stage overwrites its item's single buffer in place between two barriers, so
+// an item holds n*n floats of shared memory.  Every sum runs over t = 0 .. n-1 in order.
 // NEUMANN writes h32 = DtN(0, q); SOLVE adds the solution of (g32, q) to the FP64 state u64 (or
 // stores it there when accumulate is 0).
 template <int MODE, int NT>
-__global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict__ types,
+__global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restrict__ types,
                                                    const MixLeaf* __restrict__ leaves, int L, int B, int n_arg,
                                                    int ipc, const float* __restrict__ q, double* __restrict__ u64,
                                                    int accumulate) {
     extern __shared__ __align__(16) float smf[];
     const int n = NT ? NT : n_arg;  // NT > 0: leaf size known at compile time (loops unrolled)
     const int nn = n * n, nb = n / 4, tpi = nb * nb;
-    const int istride = 2 * nn + 16;
+    const int istride = nn + 16;
     float* VS = smf;
     float* VT = smf + nn;
     const int tid = threadIdx.x;
-    const int slot = tid / tpi, lt = tid - slot * tpi;
-    const int item = blockIdx.x * ipc + slot;
-    const bool act = slot < ipc && (long long)item < (long long)L * B;
-    const int leaf = act ? item / B : 0;
-    const int b = act ? item - leaf * B : 0;
-    const MixLeaf lf = leaves[leaf];
-    const LeafType32 ty = types[lf.type];
+    const int grp = tid / tpi, lt = tid - grp * tpi;
+    const int bi = lt / nb, bj = lt - (lt / nb) * nb;
+    // only the indices stay in registers; the leaf and type records are read where they are used
+    int leaf[2], b[2];
+    bool act[2];
+    float* X[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int item = blockIdx.x * ipc + 2 * grp + k;
+        act[k] = 2 * grp + k < ipc && (long long)item < (long long)L * B;
+        leaf[k] = act[k] ? item / B : 0;
+        b[k] = act[k] ? item - leaf[k] * B : 0;
+        X[k] = smf + 2 * nn + (2 * grp + k) * istride;
+    }
     {
         const float* V0 = types[0].V;
         for (int e = tid; e < nn; e += blockDim.x) {
@@ -548,12 +559,13 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
             VT[(e % n) * n + e / n] = v;
         }
     }
-    float* F = smf + 2 * nn + slot * istride;
-    float* W = F + nn;
-    const int bi = lt / nb, bj = lt - (lt / nb) * nb;
-    if (act) {
-        const float* qq = q + ((long long)b * L + leaf) * nn;
-        const float cx = 1.0f / (ty.dx * ty.dx), cy = 1.0f / (ty.dy * ty.dy);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (!act[k]) continue;
+        const float* qq = q + ((long long)b[k] * L + leaf[k]) * nn;
+        const MixLeaf lfk = leaves[leaf[k]];
+        const LeafType32 tyk = types[lfk.type];
+        const float cx = 1.0f / (tyk.dx * tyk.dx), cy = 1.0f / (tyk.dy * tyk.dy);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int r = 4 * bi + i;
@@ -564,119 +576,153 @@ __global__ void __launch_bounds__(256) k_mx_leaf32(const LeafType32* __restrict_
                 for (int j = 0; j < 4; ++j) {
                     const int c = 4 * bj + j;
                     float acc = 0.f;
-                    if (r == 0) acc += cx * lf.g32[(long long)(0 * n + c) * B + b];
-                    else if (r == n - 1) acc += cx * lf.g32[(long long)(1 * n + c) * B + b];
-                    if (c == 0) acc += cy * lf.g32[(long long)(2 * n + r) * B + b];
-                    else if (c == n - 1) acc += cy * lf.g32[(long long)(3 * n + r) * B + b];
+                    if (r == 0) acc += cx * lfk.g32[(long long)(0 * n + c) * B + b[k]];
+                    else if (r == n - 1) acc += cx * lfk.g32[(long long)(1 * n + c) * B + b[k]];
+                    if (c == 0) acc += cy * lfk.g32[(long long)(2 * n + r) * B + b[k]];
+                    else if (c == n - 1) acc += cy * lfk.g32[(long long)(3 * n + r) * B + b[k]];
                     t[j] += -2.0f * acc;
                 }
                 v = make_float4(t[0], t[1], t[2], t[3]);
             }
-            *reinterpret_cast<float4*>(F + r * n + 4 * bj) = v;
+            *reinterpret_cast<float4*>(X[k] + r * n + 4 * bj) = v;
         }
     }
     __syncthreads();
-    float acc[4][4];
+    float acc[2][4][4];
     auto zero = [&]() {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 2; ++k)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[k][i][j] = 0.f;
     };
-    // acc[a][c] += P[t][4pa + a] * Q[t][4pc + c] over t < n (both row-major n x n in shared memory)
-    auto outer = [&](const float* P, int pa, const float* Q, int pc) {
+    auto fma4 = [&](int k, const float4& x, const float4& y) {
+        const float xa[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            acc[k][a][0] = fmaf(xa[a], y.x, acc[k][a][0]);
+            acc[k][a][1] = fmaf(xa[a], y.y, acc[k][a][1]);
+            acc[k][a][2] = fmaf(xa[a], y.z, acc[k][a][2]);
+            acc[k][a][3] = fmaf(xa[a], y.w, acc[k][a][3]);
+        }
+    };
+    // acc[k][a][c] += V[t][4 bi + a] * X_k[t][4 bj + c] over t < n
+    auto outer_vp = [&](const float* V) {
 #pragma unroll
         for (int t = 0; t < (NT ? NT : n); ++t) {
-            const float4 x = *reinterpret_cast<const float4*>(P + t * n + 4 * pa);
-            const float4 y = *reinterpret_cast<const float4*>(Q + t * n + 4 * pc);
-            const float xa[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                acc[a][0] = fmaf(xa[a], y.x, acc[a][0]);
-                acc[a][1] = fmaf(xa[a], y.y, acc[a][1]);
-                acc[a][2] = fmaf(xa[a], y.z, acc[a][2]);
-                acc[a][3] = fmaf(xa[a], y.w, acc[a][3]);
-            }
+            const float4 x = *reinterpret_cast<const float4*>(V + t * n + 4 * bi);
+            const float4 y0 = *reinterpret_cast<const float4*>(X[0] + t * n + 4 * bj);
+            const float4 y1 = *reinterpret_cast<const float4*>(X[1] + t * n + 4 * bj);
+            fma4(0, x, y0);
+            fma4(1, x, y1);
         }
     };
-    // (1) WT[j][k] = sum_i V[i][k] F[i][j]
-    if (act) {
-        zero();
-        outer(VS, bi, F, bj);
+    // acc[k][a][c] += X_k[t][4 bi + a] * V[t][4 bj + c] over t < n
+    auto outer_vq = [&](const float* V) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            *reinterpret_cast<float4*>(W + (4 * bj + j) * n + 4 * bi) =
-                make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
-    }
-    __syncthreads();
-    // (2) G[k][l] = Dinv[k][l] sum_j WT[j][k] V[j][l]  -> F
-    if (act) {
-        zero();
-        outer(W, bi, VS, bj);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float4 d = *reinterpret_cast<const float4*>(ty.Dinv + (4 * bi + k) * n + 4 * bj);
-            *reinterpret_cast<float4*>(F + (4 * bi + k) * n + 4 * bj) =
-                make_float4(acc[k][0] * d.x, acc[k][1] * d.y, acc[k][2] * d.z, acc[k][3] * d.w);
+        for (int t = 0; t < (NT ? NT : n); ++t) {
+            const float4 y = *reinterpret_cast<const float4*>(V + t * n + 4 * bj);
+            const float4 x0 = *reinterpret_cast<const float4*>(X[0] + t * n + 4 * bi);
+            const float4 x1 = *reinterpret_cast<const float4*>(X[1] + t * n + 4 * bi);
+            fma4(0, x0, y);
+            fma4(1, x1, y);
         }
-    }
-    __syncthreads();
-    // (3) U1T[l][i] = sum_k VT[k][i] G[k][l]  -> W
-    if (act) {
-        zero();
-        outer(VT, bi, F, bj);
+    };
+    // X_k[4 bj + c][4 bi + a] = acc[k][a][c] (the transposed block)
+    auto store_t = [&]() {
 #pragma unroll
-        for (int l = 0; l < 4; ++l)
-            *reinterpret_cast<float4*>(W + (4 * bj + l) * n + 4 * bi) =
-                make_float4(acc[0][l], acc[1][l], acc[2][l], acc[3][l]);
-    }
+        for (int k = 0; k < 2; ++k)
+            if (act[k])
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    *reinterpret_cast<float4*>(X[k] + (4 * bj + c) * n + 4 * bi) =
+                        make_float4(acc[k][0][c], acc[k][1][c], acc[k][2][c], acc[k][3][c]);
+    };
+    // (1) WT[j][k] = sum_i V[i][k] F[i][j]
+    zero();
+    outer_vp(VS);
     __syncthreads();
-    if (!act) return;
+    store_t();
+    __syncthreads();
+    // (2) G[k][l] = Dinv[k][l] sum_j WT[j][k] V[j][l]
+    zero();
+    outer_vq(VS);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+        if (act[k]) {
+            const float* Dinv = types[leaves[leaf[k]].type].Dinv;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float4 d = *reinterpret_cast<const float4*>(Dinv + (4 * bi + a) * n + 4 * bj);
+                *reinterpret_cast<float4*>(X[k] + (4 * bi + a) * n + 4 * bj) =
+                    make_float4(acc[k][a][0] * d.x, acc[k][a][1] * d.y, acc[k][a][2] * d.z, acc[k][a][3] * d.w);
+            }
+        }
+    __syncthreads();
+    // (3) U1T[l][i] = sum_k VT[k][i] G[k][l]
+    zero();
+    outer_vp(VT);
+    __syncthreads();
+    store_t();
+    __syncthreads();
     if (MODE == LEAF_SOLVE) {
         // (4) u[i][j] = sum_l U1T[l][i] VT[l][j]
         zero();
-        outer(W, bi, VT, bj);
-        double* uu = u64 + ((long long)b * L + leaf) * nn;
+        outer_vq(VT);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            double2* row = reinterpret_cast<double2*>(uu + (4 * bi + i) * n + 4 * bj);
-            double2 v0 = make_double2(f2d_bits(acc[i][0]), f2d_bits(acc[i][1]));
-            double2 v1 = make_double2(f2d_bits(acc[i][2]), f2d_bits(acc[i][3]));
-            if (accumulate) {
-                const double2 o0 = row[0], o1 = row[1];
-                v0.x += o0.x; v0.y += o0.y;
-                v1.x += o1.x; v1.y += o1.y;
+        for (int k = 0; k < 2; ++k) {
+            if (!act[k]) continue;
+            double* uu = u64 + ((long long)b[k] * L + leaf[k]) * nn;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                double2* row = reinterpret_cast<double2*>(uu + (4 * bi + i) * n + 4 * bj);
+                double2 v0 = make_double2(f2d_bits(acc[k][i][0]), f2d_bits(acc[k][i][1]));
+                double2 v1 = make_double2(f2d_bits(acc[k][i][2]), f2d_bits(acc[k][i][3]));
+                if (accumulate) {
+                    const double2 o0 = row[0], o1 = row[1];
+                    v0.x += o0.x; v0.y += o0.y;
+                    v1.x += o1.x; v1.y += o1.y;
+                }
+                row[0] = v0;
+                row[1] = v1;
             }
-            row[0] = v0;
-            row[1] = v1;
         }
     } else {
         // edge values u[i][j] = sum_l U1T[l][i] VT[l][j], four consecutive points of one side per
         // step: W/E (i = 0, n-1) take a broadcast U1T[l][i] and a float4 of VT row l, S/N (j = 0,
-        // n-1) a float4 of U1T row l and a broadcast VT[l][j]; same sums, in the same order, as one
-        // point at a time
-        const float dtn_x = 2.0f / ty.dx, dtn_y = 2.0f / ty.dy;
-        for (int g4 = lt; g4 < n; g4 += tpi) {
-            const int side = (4 * g4) / n, p0 = 4 * g4 - side * n;
-            const int fixed = side == 0 || side == 2 ? 0 : n - 1;
-            const float* vec = side < 2 ? VT + p0 : W + p0;       // float4 along the side
-            const float* sca = side < 2 ? W + fixed : VT + fixed;  // broadcast per l
-            float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+        // n-1) a float4 of U1T row l and a broadcast VT[l][j]; the same sums in the same order as
+        // one point at a time
 #pragma unroll
-            for (int l = 0; l < (NT ? NT : n); ++l) {
-                const float4 v = *reinterpret_cast<const float4*>(vec + l * n);
-                const float a = sca[l * n];
-                u.x = fmaf(a, v.x, u.x);
-                u.y = fmaf(a, v.y, u.y);
-                u.z = fmaf(a, v.z, u.z);
-                u.w = fmaf(a, v.w, u.w);
+        for (int k = 0; k < 2; ++k) {
+            if (!act[k]) continue;
+            const MixLeaf lfk = leaves[leaf[k]];
+            const LeafType32 tyk = types[lfk.type];
+            const float dtn_x = 2.0f / tyk.dx, dtn_y = 2.0f / tyk.dy;
+            const float* W = X[k];
+            for (int g4 = lt; g4 < n; g4 += tpi) {
+                const int side = (4 * g4) / n, p0 = 4 * g4 - side * n;
+                const int fixed = side == 0 || side == 2 ? 0 : n - 1;
+                const float* vec = side < 2 ? VT + p0 : W + p0;       // float4 along the side
+                const float* sca = side < 2 ? W + fixed : VT + fixed;  // broadcast per l
+                float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int l = 0; l < (NT ? NT : n); ++l) {
+                    const float4 v = *reinterpret_cast<const float4*>(vec + l * n);
+                    const float a = sca[l * n];
+                    u.x = fmaf(a, v.x, u.x);
+                    u.y = fmaf(a, v.y, u.y);
+                    u.z = fmaf(a, v.z, u.z);
+                    u.w = fmaf(a, v.w, u.w);
+                }
+                const float sc = ((side == 0 || side == 2) ? 1.0f : -1.0f) * (side < 2 ? dtn_x : dtn_y);
+                float* hp = lfk.h32 + (long long)(side * n + p0) * B + b[k];
+                hp[0] = sc * u.x;
+                hp[(long long)B] = sc * u.y;
+                hp[2LL * B] = sc * u.z;
+                hp[3LL * B] = sc * u.w;
             }
-            const float sc = ((side == 0 || side == 2) ? 1.0f : -1.0f) * (side < 2 ? dtn_x : dtn_y);
-            float* hp = lf.h32 + (long long)(side * n + p0) * B + b;
-            hp[0] = sc * u.x;
-            hp[(long long)B] = sc * u.y;
-            hp[2LL * B] = sc * u.z;
-            hp[3LL * B] = sc * u.w;
         }
     }
 }
@@ -1260,11 +1306,12 @@ void mx_leaf32_mode(cudaStream_t st, unsigned grid, unsigned threads, size_t sme
 
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate) {
-    const int nb = n / 4, tpi = nb * nb, ipc = tpi >= 256 ? 1 : 256 / tpi;
-    const size_t smem = (size_t(2) * n * n + size_t(ipc) * (2 * n * n + 16)) * sizeof(float);
+    // groups of (n/4)^2 threads, two items per group, up to 256 threads per block
+    const int nb = n / 4, tpi = nb * nb, groups = tpi >= 256 ? 1 : 256 / tpi, ipc = 2 * groups;
+    const size_t smem = (size_t(2) * n * n + size_t(ipc) * (n * n + 16)) * sizeof(float);
     const long long items = (long long)L * B;
     const unsigned grid = unsigned((items + ipc - 1) / ipc);
-    const unsigned threads = unsigned(ipc * tpi);
+    const unsigned threads = unsigned(groups * tpi);
     if (mode == LEAF_NEUMANN)
         mx_leaf32_mode<LEAF_NEUMANN>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, 0);
     else
