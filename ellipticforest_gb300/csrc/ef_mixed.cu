@@ -1113,8 +1113,8 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
 }
 
 // rmax[b] = max over leaves of rleaf[b][leaf]
-__global__ void __launch_bounds__(256) k_mx_rmax(const float* __restrict__ rleaf, int L, double* __restrict__ rmax) {
-    __shared__ float red[256];
+__global__ void __launch_bounds__(1024) k_mx_rmax(const float* __restrict__ rleaf, int L, double* __restrict__ rmax) {
+    __shared__ float red[1024];
     const float* p = rleaf + (long long)blockIdx.x * L;
     float m = 0.f;
     for (int l = threadIdx.x; l < L; l += blockDim.x) m = fmaxf(m, p[l]);
@@ -1361,7 +1361,7 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
 }
 
 void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax) {
-    k_mx_rmax<<<B, 256, 0, st>>>(rleaf, L, rmax);
+    k_mx_rmax<<<B, 1024, 0, st>>>(rleaf, L, rmax);
     ++g_kernel_launches;
 }
 
