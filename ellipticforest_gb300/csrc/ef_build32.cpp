@@ -31,8 +31,8 @@ void ck32(cudaError_t e, const char* what) {
 }
 
 template <class T>
-void upload(T* dst, const std::vector<T>& src, const char* what) {
-    if (!src.empty()) ck32(cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice), what);
+void upload(cudaStream_t st, T* dst, const std::vector<T>& src, const char* what) {
+    if (!src.empty()) ck32(upload_sync(st, dst, src.data(), src.size() * sizeof(T)), what);
 }
 
 }  // namespace
@@ -93,8 +93,8 @@ void Hps::allocate32() {
     // pointer tables
     std::vector<const double*> t64(types_.size());
     for (size_t t = 0; t < types_.size(); ++t) t64[t] = types_[t].T;
-    upload(d_tT64_, t64, "type T64");
-    upload(d_tT32_, typeT, "type T32");
+    upload(st_, d_tT64_, t64, "type T64");
+    upload(st_, d_tT32_, typeT, "type T32");
     static const int cb[8] = {0, 2, 1, 3, 0, 1, 2, 3};
     static const int ia[4] = {0, 1, 0, 1}, ib[4] = {2, 2, 3, 3};
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
@@ -129,13 +129,13 @@ void Hps::allocate32() {
             }
         }
         const Group32& g3 = g32_[gi];
-        upload(g3.d_items, mi, "items32");
-        upload(g3.d_X, X, "X32");
-        upload(g3.d_RHS, R, "RHS32");
-        upload(g3.d_gA, gA, "gA32");
-        upload(g3.d_gB, gB, "gB32");
-        upload(g3.d_gB2, gB2, "gB2_32");
-        upload(g3.d_gC, gC, "gC32");
+        upload(st_, g3.d_items, mi, "items32");
+        upload(st_, g3.d_X, X, "X32");
+        upload(st_, g3.d_RHS, R, "RHS32");
+        upload(st_, g3.d_gA, gA, "gA32");
+        upload(st_, g3.d_gB, gB, "gB32");
+        upload(st_, g3.d_gB2, gB2, "gB2_32");
+        upload(st_, g3.d_gC, gC, "gC32");
     }
     for (size_t k = 0; k < tsteps_.size(); ++k) {
         const int t = step_index_t_[k];
@@ -146,8 +146,8 @@ void Hps::allocate32() {
             in.push_back(t == 0 ? m.T : m.Tsteps[t - 1]);
             out.push_back(m.Tsteps[t]);
         }
-        upload(t32_[k].d_in, in, "tin32");
-        upload(t32_[k].d_out, out, "tout32");
+        upload(st_, t32_[k].d_in, in, "tin32");
+        upload(st_, t32_[k].d_out, out, "tout32");
     }
 }
 

@@ -359,39 +359,39 @@ void Hps::upload_tables() {
             fl[k] = FpLeaf{n_, types_[k].dx, types_[k].dy, c, c + nn, c + 5 * nn, fp_band_[k], fp_bcoef_[k],
                            d_fpinfo_ + k};
         }
-        check(cudaMemcpy(d_fp_, fl.data(), fl.size() * sizeof(FpLeaf), cudaMemcpyHostToDevice), "upload fp leaves");
+        check(upload_sync(st_, d_fp_, fl.data(), fl.size() * sizeof(FpLeaf)), "upload fp leaves");
     } else {
         // leaf types: sine basis and inverse eigenvalue table
         std::vector<LeafType> hty(types_.size());
         std::vector<double> V(nn), Dinv(nn);
         for (size_t t = 0; t < types_.size(); ++t) {
             leaf_tables(n_, types_[t].dx, types_[t].dy, lambda_, V.data(), Dinv.data());
-            check(cudaMemcpy(d_V_ + t * nn, V.data(), nn * 8, cudaMemcpyHostToDevice), "upload V");
-            check(cudaMemcpy(d_Dinv_ + t * nn, Dinv.data(), nn * 8, cudaMemcpyHostToDevice), "upload Dinv");
+            check(upload_sync(st_, d_V_ + t * nn, V.data(), nn * 8), "upload V");
+            check(upload_sync(st_, d_Dinv_ + t * nn, Dinv.data(), nn * 8), "upload Dinv");
             hty[t] = LeafType{n_, types_[t].dx, types_[t].dy, d_V_ + t * nn, d_Dinv_ + t * nn};
         }
-        check(cudaMemcpy(d_types_, hty.data(), hty.size() * sizeof(LeafType), cudaMemcpyHostToDevice),
+        check(upload_sync(st_, d_types_, hty.data(), hty.size() * sizeof(LeafType)),
               "upload types");
     }
 
     std::vector<LeafItem> items;
     for (size_t t = 0; t < types_.size(); ++t)
         for (int u = 0; u < 4 * n_; ++u) items.push_back(LeafItem{int(t), u, nullptr, nullptr, types_[t].T});
-    check(cudaMemcpy(d_items_dtn_, items.data(), items.size() * sizeof(LeafItem), cudaMemcpyHostToDevice),
+    check(upload_sync(st_, d_items_dtn_, items.data(), items.size() * sizeof(LeafItem)),
           "upload dtn items");
     items.clear();
     for (int k = 0; k < L; ++k) {
         const NodeDev& nd = nodes_[mesh_.leaves[k]];
         items.push_back(LeafItem{nd.leaf_type, 0, d_f_ + size_t(k) * nn, nullptr, nd.h});
     }
-    check(cudaMemcpy(d_items_neu_, items.data(), items.size() * sizeof(LeafItem), cudaMemcpyHostToDevice),
+    check(upload_sync(st_, d_items_neu_, items.data(), items.size() * sizeof(LeafItem)),
           "upload neumann items");
     items.clear();
     for (int k = 0; k < L; ++k) {
         const NodeDev& nd = nodes_[mesh_.leaves[k]];
         items.push_back(LeafItem{nd.leaf_type, 0, d_f_ + size_t(k) * nn, nd.g, d_u_ + size_t(k) * nn});
     }
-    check(cudaMemcpy(d_items_solve_, items.data(), items.size() * sizeof(LeafItem), cudaMemcpyHostToDevice),
+    check(upload_sync(st_, d_items_solve_, items.data(), items.size() * sizeof(LeafItem)),
           "upload solve items");
 
     for (auto& g : groups_) {
@@ -414,13 +414,13 @@ void Hps::upload_tables() {
             m.h = nd.h; m.w = nd.w; m.gf = nd.gf; m.hd = nd.hd;
             X[i] = nd.X; R[i] = nd.RHS; H[i] = nd.H; T[i] = nd.T; P[i] = nd.piv; Q[i] = nd.perm;
         }
-        check(cudaMemcpy(g.d_items, mi.data(), cnt * sizeof(MergeItem), cudaMemcpyHostToDevice), "items");
-        check(cudaMemcpy(g.d_X, X.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "X");
-        check(cudaMemcpy(g.d_RHS, R.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "RHS");
-        check(cudaMemcpy(g.d_H, H.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "H");
-        check(cudaMemcpy(g.d_T, T.data(), cnt * sizeof(double*), cudaMemcpyHostToDevice), "T");
-        check(cudaMemcpy(g.d_piv, P.data(), cnt * sizeof(int*), cudaMemcpyHostToDevice), "piv");
-        check(cudaMemcpy(g.d_perm, Q.data(), cnt * sizeof(int*), cudaMemcpyHostToDevice), "perm");
+        check(upload_sync(st_, g.d_items, mi.data(), cnt * sizeof(MergeItem)), "items");
+        check(upload_sync(st_, g.d_X, X.data(), cnt * sizeof(double*)), "X");
+        check(upload_sync(st_, g.d_RHS, R.data(), cnt * sizeof(double*)), "RHS");
+        check(upload_sync(st_, g.d_H, H.data(), cnt * sizeof(double*)), "H");
+        check(upload_sync(st_, g.d_T, T.data(), cnt * sizeof(double*)), "T");
+        check(upload_sync(st_, g.d_piv, P.data(), cnt * sizeof(int*)), "piv");
+        check(upload_sync(st_, g.d_perm, Q.data(), cnt * sizeof(int*)), "perm");
         // split GEMM tables: row block b of the parent's WESN exterior belongs to child c(b)
         // (W: alpha, gamma; E: beta, omega; S: alpha, beta; N: gamma, omega), whose interfaces are
         // alpha: I0, I2; beta: I1, I2; gamma: I0, I3; omega: I1, I3.
@@ -440,10 +440,10 @@ void Hps::upload_tables() {
                     gC[8 * i + b] = nd.T + size_t(b) * sz * 8 * sz;
                 }
             }
-            check(cudaMemcpy(g.d_gA, gA.data(), gA.size() * sizeof(void*), cudaMemcpyHostToDevice), "gA");
-            check(cudaMemcpy(g.d_gB, gB.data(), gB.size() * sizeof(void*), cudaMemcpyHostToDevice), "gB");
-            check(cudaMemcpy(g.d_gB2, gB2.data(), gB2.size() * sizeof(void*), cudaMemcpyHostToDevice), "gB2");
-            check(cudaMemcpy(g.d_gC, gC.data(), gC.size() * sizeof(void*), cudaMemcpyHostToDevice), "gC");
+            check(upload_sync(st_, g.d_gA, gA.data(), gA.size() * sizeof(void*)), "gA");
+            check(upload_sync(st_, g.d_gB, gB.data(), gB.size() * sizeof(void*)), "gB");
+            check(upload_sync(st_, g.d_gB2, gB2.data(), gB2.size() * sizeof(void*)), "gB2");
+            check(upload_sync(st_, g.d_gC, gC.data(), gC.size() * sizeof(void*)), "gC");
         }
     }
     for (size_t k = 0; k < tsteps_.size(); ++k) {
@@ -458,10 +458,10 @@ void Hps::upload_tables() {
             hout.push_back(nd.hsteps[t]);
         }
         const size_t c = in.size();
-        check(cudaMemcpy(tsteps_[k].d_in, in.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "tin");
-        check(cudaMemcpy(tsteps_[k].d_out, out.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "tout");
-        check(cudaMemcpy(hsteps_[k].d_in, hin.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "hin");
-        check(cudaMemcpy(hsteps_[k].d_out, hout.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "hout");
+        check(upload_sync(st_, tsteps_[k].d_in, in.data(), c * sizeof(void*)), "tin");
+        check(upload_sync(st_, tsteps_[k].d_out, out.data(), c * sizeof(void*)), "tout");
+        check(upload_sync(st_, hsteps_[k].d_in, hin.data(), c * sizeof(void*)), "hin");
+        check(upload_sync(st_, hsteps_[k].d_out, hout.data(), c * sizeof(void*)), "hout");
     }
     for (size_t k = 0; k < gsteps_.size(); ++k) {
         const int t = step_index_g_[k];
@@ -473,8 +473,8 @@ void Hps::upload_tables() {
             out.push_back(nd.gsteps[t]);
         }
         const size_t c = in.size();
-        check(cudaMemcpy(gsteps_[k].d_in, in.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "gin");
-        check(cudaMemcpy(gsteps_[k].d_out, out.data(), c * sizeof(void*), cudaMemcpyHostToDevice), "gout");
+        check(upload_sync(st_, gsteps_[k].d_in, in.data(), c * sizeof(void*)), "gin");
+        check(upload_sync(st_, gsteps_[k].d_out, out.data(), c * sizeof(void*)), "gout");
     }
     check(cudaStreamSynchronize(st_), "upload sync");
 }
@@ -625,10 +625,10 @@ void Hps::root_from_bc() {
         d_rootrhs_arr_ = cv.get<double*>(1);
         d_rootpiv_arr_ = cv.get<int*>(1);
         d_rootperm_arr_ = cv.get<int*>(1);
-        check(cudaMemcpy(d_rootA_arr_, &d_rootA_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
-        check(cudaMemcpy(d_rootrhs_arr_, &d_rootrhs_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
-        check(cudaMemcpy(d_rootpiv_arr_, &d_rootpiv_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
-        check(cudaMemcpy(d_rootperm_arr_, &d_rootperm_, sizeof(void*), cudaMemcpyHostToDevice), "root arr");
+        check(upload_sync(st_, d_rootA_arr_, &d_rootA_, sizeof(void*)), "root arr");
+        check(upload_sync(st_, d_rootrhs_arr_, &d_rootrhs_, sizeof(void*)), "root arr");
+        check(upload_sync(st_, d_rootpiv_arr_, &d_rootpiv_, sizeof(void*)), "root arr");
+        check(upload_sync(st_, d_rootperm_arr_, &d_rootperm_, sizeof(void*)), "root arr");
     }
     // g = (diag(a) + diag(b) T)^{-1} (r - diag(b) h)   (HPSAlgorithm.hpp:402-420).  The reference
     // re-assembles and re-factors the 4M x 4M matrix on every solve; here its LU is kept while a and

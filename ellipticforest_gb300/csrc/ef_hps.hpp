@@ -21,6 +21,16 @@ namespace efgb {
 
 enum SolverType : int { SOLVER_FIVE_POINT = 0, SOLVER_FISHPACK90 = 1 };
 
+// Set-up upload ordered on the stream that later kernels run on: a plain cudaMemcpy runs on the
+// legacy default stream, which a non-blocking stream does not wait for (and a pageable copy may
+// return before its DMA is done), so tables uploaded that way could be read stale or overwritten by
+// an earlier asynchronous clear of the same stream.  Copies, then synchronises the stream.
+inline cudaError_t upload_sync(cudaStream_t st, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return cudaSuccess;
+    const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+}
+
 // Orthonormal sine basis V (n x n, V[i][k]) of the 1-D Dirichlet-ghost operator and the inverse
 // 2-D eigenvalue table Dinv[k][l] = 1 / (mu_x[k] + mu_y[l] + lambda) of one patch geometry.
 void leaf_tables(int n, double dx, double dy, double lambda, double* V, double* Dinv);

@@ -158,7 +158,7 @@ void Hps::build_from(const Hps& old) {
         std::memcpy(&host[c_dst + k * sizeof(void*)], &cdst[k], sizeof(void*));
         std::memcpy(&host[c_len + k * sizeof(long long)], &clen[k], sizeof(long long));
     }
-    cki(cudaMemcpy(dev, host.data(), host.size(), cudaMemcpyHostToDevice), "incremental tables");
+    cki(upload_sync(st_, dev, host.data(), host.size()), "incremental tables");
     auto at = [&](size_t off) { return dev + off; };
 
     build_leaf_types();

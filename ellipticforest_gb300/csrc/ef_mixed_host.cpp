@@ -204,7 +204,7 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         for (int k = 0; k < L; ++k)
             fl[k] = MixFp{fp_band32_ + size_t(k) * 4 * nn * n, fp_bcoef32_ + size_t(k) * 4 * n,
                           fp_coef64_ + size_t(k) * 5 * nn, 2.0 / hps.types_[k].dx, 2.0 / hps.types_[k].dy};
-        ck(cudaMemcpy(d_fps_, fl.data(), L * sizeof(MixFp), cudaMemcpyHostToDevice), "mixed fp leaves");
+        ck(upload_sync(st_, d_fps_, fl.data(), L * sizeof(MixFp)), "mixed fp leaves");
         if (!share) mx_fp_convert(st, hps.d_fp_, d_fps_, L, n);
     }
     // leaf tables in FP32 (constant-coefficient leaves)
@@ -218,12 +218,12 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         for (size_t t = 0; t < t32.size(); ++t) {
             leaf_tables(n, hps.types_[t].dx, hps.types_[t].dy, hps.lambda_, V.data(), D.data());
             for (size_t e = 0; e < nn; ++e) { Vf[e] = float(V[e]); Df[e] = float(D[e]); }
-            ck(cudaMemcpy(tab + 2 * nn * t, Vf.data(), nn * 4, cudaMemcpyHostToDevice), "upload V32");
-            ck(cudaMemcpy(tab + 2 * nn * t + nn, Df.data(), nn * 4, cudaMemcpyHostToDevice), "upload D32");
+            ck(upload_sync(st_, tab + 2 * nn * t, Vf.data(), nn * 4), "upload V32");
+            ck(upload_sync(st_, tab + 2 * nn * t + nn, Df.data(), nn * 4), "upload D32");
             t32[t] = LeafType32{n, float(hps.types_[t].dx), float(hps.types_[t].dy), tab + 2 * nn * t,
                                 tab + 2 * nn * t + nn};
         }
-        ck(cudaMemcpy(d_types32_, t32.data(), t32.size() * sizeof(LeafType32), cudaMemcpyHostToDevice), "types32");
+        ck(upload_sync(st_, d_types32_, t32.data(), t32.size() * sizeof(LeafType32)), "types32");
         std::vector<MixCoef> co(hps.types_.size());
         for (size_t t = 0; t < co.size(); ++t) {
             const double dx = hps.types_[t].dx, dy = hps.types_[t].dy;
@@ -239,14 +239,14 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             c.cy32 = float(cy);
             if (!c.iso || c.lmm) res_form_ = 1;
         }
-        ck(cudaMemcpy(d_coef_, co.data(), co.size() * sizeof(MixCoef), cudaMemcpyHostToDevice), "mixed coefs");
+        ck(upload_sync(st_, d_coef_, co.data(), co.size() * sizeof(MixCoef)), "mixed coefs");
     }
     std::vector<MixLeaf> leaves(L);
     for (int k = 0; k < L; ++k) {
         const int id = mesh.leaves[k];
         leaves[k] = MixLeaf{hps.nodes_[id].leaf_type, mn_[id].g32, mn_[id].h32, mn_[id].g64, mn_[id].h64};
     }
-    ck(cudaMemcpy(d_leaves_, leaves.data(), L * sizeof(MixLeaf), cudaMemcpyHostToDevice), "mix leaves");
+    ck(upload_sync(st_, d_leaves_, leaves.data(), L * sizeof(MixLeaf)), "mix leaves");
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
         const Group& g = hps.groups_[gi];
         std::vector<MixItem> items(g.nodes.size());
@@ -268,8 +268,8 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             conv[i] = hps.built32() ? MixConv{nullptr, nullptr, m.S, m.Xi, m.H32, hps.n32_[id].RHS, hps.n32_[id].H}
                                     : MixConv{hps.nodes_[id].RHS, hps.nodes_[id].H, m.S, m.Xi, m.H32, nullptr, nullptr};
         }
-        ck(cudaMemcpy(groups_[gi].d_items, items.data(), items.size() * sizeof(MixItem), cudaMemcpyHostToDevice), "mix items");
-        ck(cudaMemcpy(groups_[gi].d_conv, conv.data(), conv.size() * sizeof(MixConv), cudaMemcpyHostToDevice), "mix conv");
+        ck(upload_sync(st_, groups_[gi].d_items, items.data(), items.size() * sizeof(MixItem)), "mix items");
+        ck(upload_sync(st_, groups_[gi].d_conv, conv.data(), conv.size() * sizeof(MixConv)), "mix conv");
     }
     auto fill_steps = [&](std::vector<MStep>& steps, const std::vector<std::vector<int>>& nodes,
                           const std::vector<int>& index, bool up) {
@@ -291,10 +291,10 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
                 }
             }
             const size_t c = i32.size() * sizeof(void*);
-            ck(cudaMemcpy(steps[k].in32, i32.data(), c, cudaMemcpyHostToDevice), "steps");
-            ck(cudaMemcpy(steps[k].out32, o32.data(), c, cudaMemcpyHostToDevice), "steps");
-            ck(cudaMemcpy(steps[k].in64, i64.data(), c, cudaMemcpyHostToDevice), "steps");
-            ck(cudaMemcpy(steps[k].out64, o64.data(), c, cudaMemcpyHostToDevice), "steps");
+            ck(upload_sync(st_, steps[k].in32, i32.data(), c), "steps");
+            ck(upload_sync(st_, steps[k].out32, o32.data(), c), "steps");
+            ck(upload_sync(st_, steps[k].in64, i64.data(), c), "steps");
+            ck(upload_sync(st_, steps[k].out64, o64.data(), c), "steps");
         }
     };
     fill_steps(hsteps_, hps.step_nodes_t_, hps.step_index_t_, true);

@@ -106,6 +106,8 @@ void Hps::save(const char* path) const {
     }
     fl.hashing = true;
     std::vector<unsigned char> buf;
+    // the copies below run on the default stream: finish the tree's own stream first
+    cks(cudaStreamSynchronize(st_), "save sync");
     walk_payload(const_cast<Hps&>(*this), [&](double* p, size_t n) { dev_to_file(fl, p, n, buf); });
     if (solver_type_ == SOLVER_FIVE_POINT) {
         const size_t L = mesh_.leaves.size(), nn = size_t(n_) * n_;
@@ -157,6 +159,7 @@ std::unique_ptr<Hps> Hps::load(const char* path) {
     fl.hashing = false;
     const uint64_t want = fl.hash;
     if (fl.get<uint64_t>() != want) throw std::invalid_argument("load: checksum mismatch (corrupted file)");
+    cks(cudaDeviceSynchronize(), "load sync");  // the default-stream uploads are done before any kernel reads them
     h->built_ = true;
     return h;
 }
