@@ -75,6 +75,9 @@ SIGNATURES = {
                                    C.POINTER(_vp)]),
     "ef_server_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     "ef_server_set_sweeps": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "ef_hps_mixed_lane": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "ef_hps_mixed_lane_solve_async": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
     "ef_hps_mixed_solve_blocks": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p),
                                             C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "ef_server_submit": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),

@@ -564,6 +564,59 @@ int ef_hps_mixed_solve(ef_hps* h, int batch, int sweeps, const double* f, const 
     });
 }
 
+namespace {
+// the second lane (shares the FP32 operators of h->mixed, own stream), created on first use; it starts
+// after the work already queued on the tree's stream
+int lane2(ef_hps* h) {
+    if (!h->mixed2) {
+        if (!h->stream2) {
+            const int st = cuda_status(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking), "lane stream");
+            if (st) return st;
+        }
+        h->mixed2 = std::make_unique<efgb::MixedSolver>(*h->hps, h->mixed->bmax(), h->mixed.get());
+        h->mixed2->set_stream(h->stream2);
+    }
+    cudaEvent_t ready;
+    int st = cuda_status(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "lane event");
+    if (!st) st = cuda_status(cudaEventRecord(ready, h->mixed->stream()), "lane event");
+    if (!st) st = cuda_status(cudaStreamWaitEvent(h->stream2, ready, 0), "lane event");
+    cudaEventDestroy(ready);
+    return st;
+}
+
+efgb::MixedSolver* lane_solver(ef_hps* h, int lane) { return lane == 0 ? h->mixed.get() : h->mixed2.get(); }
+}  // namespace
+
+int ef_hps_mixed_lane(ef_hps* h, int lane, double** f, double** a, double** r, double** u, void** stream) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    if (lane != 0 && lane != 1) return fail(EF_ERR_INVALID, "lane must be 0 or 1");
+    return guarded([&] {
+        if (lane == 1) {
+            const int st = lane2(h);
+            if (st) return st;
+        }
+        efgb::MixedSolver* X = lane_solver(h, lane);
+        if (f) *f = X->f();
+        if (a) *a = X->a();
+        if (r) *r = X->r();
+        if (u) *u = X->u();
+        if (stream) *stream = (void*)X->stream();
+        return EF_OK;
+    });
+}
+
+int ef_hps_mixed_lane_solve_async(ef_hps* h, int lane, int batch, int sweeps) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    if (lane != 0 && lane != 1) return fail(EF_ERR_INVALID, "lane must be 0 or 1");
+    if (lane == 1 && !h->mixed2) return fail(EF_ERR_STATE, "lane 1 not set up (ef_hps_mixed_lane)");
+    return guarded([&] {
+        lane_solver(h, lane)->solve(batch, sweeps);
+        return cuda_status(cudaGetLastError(), "mixed solve launch");
+    });
+}
+
 int ef_hps_mixed_solve_blocks(ef_hps* h, int nblocks, const int* batch, int sweeps, const double* const* f,
                               const double* const* a, const double* const* r, double* const* u) {
     if (!h || !batch || !f || !a || !r || !u || nblocks < 0) return fail(EF_ERR_INVALID, "null argument");
@@ -574,21 +627,8 @@ int ef_hps_mixed_solve_blocks(ef_hps* h, int nblocks, const int* batch, int swee
     }
     return guarded([&] {
         efgb::Hps& H = *h->hps;
-        if (nblocks > 1 && !h->mixed2) {
-            if (!h->stream2) {
-                int st = cuda_status(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking), "lane stream");
-                if (st) return st;
-            }
-            h->mixed2 = std::make_unique<efgb::MixedSolver>(H, h->mixed->bmax(), h->mixed.get());
-            h->mixed2->set_stream(h->stream2);
-        }
-        // the second lane must not start before work already queued on the tree's stream
         if (nblocks > 1) {
-            cudaEvent_t ready;
-            int st = cuda_status(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "lane event");
-            if (!st) st = cuda_status(cudaEventRecord(ready, h->mixed->stream()), "lane event");
-            if (!st) st = cuda_status(cudaStreamWaitEvent(h->stream2, ready, 0), "lane event");
-            cudaEventDestroy(ready);
+            const int st = lane2(h);
             if (st) return st;
         }
         const size_t cells1 = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();

@@ -617,8 +617,18 @@ class HPSAlgorithm:
         check(_lib.load().ef_hps_mixed_buffers(self._h, *[C.byref(p) for p in ptrs]))
         return [p.value for p in ptrs]  # f, a, r, u
 
-    def mixed_solve_async(self, batch: int, sweeps: int = 1):
-        check(_lib.load().ef_hps_mixed_solve_async(self._h, int(batch), int(sweeps)))
+    def mixed_solve_async(self, batch: int, sweeps: int = 1, lane: int = 0):
+        if lane == 0:
+            check(_lib.load().ef_hps_mixed_solve_async(self._h, int(batch), int(sweeps)))
+        else:
+            check(_lib.load().ef_hps_mixed_lane_solve_async(self._h, int(lane), int(batch), int(sweeps)))
+
+    def mixed_lane(self, lane: int):
+        """Device pointers (f, a, r, u) and the CUDA stream (int) of lane 0 or 1; lane 1 shares the
+        FP32 operators and is created by the first call for it."""
+        ptrs = [C.c_void_p() for _ in range(5)]
+        check(_lib.load().ef_hps_mixed_lane(self._h, int(lane), *[C.byref(p) for p in ptrs]))
+        return [p.value or 0 for p in ptrs]
 
     def profile_enable(self, on: bool = True):
         check(_lib.load().ef_hps_profile_enable(self._h, int(on)))

@@ -161,6 +161,14 @@ int ef_hps_mixed_solve(ef_hps* hps, int batch, int sweeps, const double* f_host,
  * Returns when every block's u is on the host.  The second lane holds its own block buffers. */
 int ef_hps_mixed_solve_blocks(ef_hps* hps, int nblocks, const int* batch, int sweeps, const double* const* f_host,
                               const double* const* a_host, const double* const* r_host, double* const* u_host);
+/* Device-resident lanes: lane 0 is the solver of ef_hps_mixed_init (the tree's stream), lane 1 (set
+ * up by the first call for it) shares its FP32 operators and runs on its own stream, so two blocks
+ * can be in flight at once.  Returns the lane's resident buffers (as ef_hps_mixed_buffers) and its
+ * stream (a cudaStream_t); lane 1 starts after the work queued on the tree's stream at that call. */
+int ef_hps_mixed_lane(ef_hps* hps, int lane, double** f_dev, double** a_dev, double** r_dev, double** u_dev,
+                      void** stream);
+/* 1 + sweeps passes on the first `batch` requests of the lane's resident buffers, on its stream. */
+int ef_hps_mixed_lane_solve_async(ef_hps* hps, int lane, int batch, int sweeps);
 /* max |leaf residual| per request before each pass: passes x bmax doubles (synchronous). */
 int ef_hps_mixed_residuals(ef_hps* hps, int passes, double* out_host);
 
