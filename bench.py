@@ -12,7 +12,7 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
             measured); inputs resident in HBM; --lanes 2 (default) alternates the steps over two lanes
             sharing the operators, so two blocks are in flight
   e2e    -- the same form through the C ABI call ef_hps_mixed_solve_blocks on pinned host buffers
-            (K blocks in one call, two lanes alternating so one block's copies overlap the other's
+            (K blocks in one call, three lanes rotating so two blocks' copies overlap a third's
             solve), the host<->device copies of every block inside the timed region; the one-block
             ef_hps_mixed_solve rate is reported beside it
   plain_fp64 -- the plain FP64 form one request at a time (device-resident solves/s, p50/p99, and
@@ -443,7 +443,7 @@ def run_gb300(args):
     Fh = torch.from_numpy(F).pin_memory()
     Ah = torch.from_numpy(A).pin_memory()
     Rh = torch.from_numpy(R).pin_memory()
-    Uh = [torch.empty_like(Fh).pin_memory() for _ in range(2)]
+    Uh = [torch.empty_like(Fh).pin_memory() for _ in range(3)]
     Fn, An, Rn, Un = Fh.numpy(), Ah.numpy(), Rh.numpy(), [x.numpy() for x in Uh]
     # (1) one block per call (ef_hps_mixed_solve: copy in, solve, copy out, synchronise)
     Ke = max(2, K // 4)
@@ -454,23 +454,24 @@ def run_gb300(args):
     e2e_single = world * Ke * B / (time.perf_counter() - t0)
     assert np.array_equal(Un[0][0], u_mixed[0])
     # (2) the headline e2e: K blocks through one pipelined call (ef_hps_mixed_solve_blocks), every
-    # block's inputs copied in and its results copied out inside the call; two lanes alternate so
-    # that one block's copies overlap the other's solve
+    # block's inputs copied in and its results copied out inside the call; three lanes rotate so
+    # that two blocks' copies overlap a third block's solve
     import ctypes as C
     nbk = K
     batch_arr = (C.c_int * nbk)(*([B] * nbk))
     f_arr = (C.c_void_p * nbk)(*([Fn.ctypes.data] * nbk))
     a_arr = (C.c_void_p * nbk)(*([An.ctypes.data] * nbk))
     r_arr = (C.c_void_p * nbk)(*([Rn.ctypes.data] * nbk))
-    u_arr = (C.c_void_p * nbk)(*[Un[k & 1].ctypes.data for k in range(nbk)])
-    check(lib.ef_hps_mixed_solve_blocks(hps.handle, 2, batch_arr, sweeps, f_arr, a_arr, r_arr, u_arr))  # lane 2 set-up
+    u_arr = (C.c_void_p * nbk)(*[Un[k % 3].ctypes.data for k in range(nbk)])  # one host output per lane
+    # set-up and graph capture of the pipelined call's three lanes (two calls per lane)
+    check(lib.ef_hps_mixed_solve_blocks(hps.handle, min(nbk, 6), batch_arr, sweeps, f_arr, a_arr, r_arr, u_arr))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     check(lib.ef_hps_mixed_solve_blocks(hps.handle, nbk, batch_arr, sweeps, f_arr, a_arr, r_arr, u_arr))
     e2e_wall = time.perf_counter() - t0
     e2e_value = world * nbk * B / e2e_wall
     clk = clocks.stop()
-    assert np.array_equal(Un[0][0], u_mixed[0]) and np.array_equal(Un[1][0], u_mixed[0])
+    assert all(np.array_equal(x[0], u_mixed[0]) for x in Un)
 
     # per-section kernel timing of the mixed form (CUDA events on the library's stream)
     hps.profile_enable(True)
@@ -542,7 +543,7 @@ def run_gb300(args):
             "e2e": {"value": e2e_value, "unit": "solves/s",
                     "h2d_bytes_per_step": int(B * 8 * (dofs + 2 * 4 * hps.M)),
                     "d2h_bytes_per_step": int(B * 8 * dofs),
-                    "api": "ef_hps_mixed_solve_blocks (K blocks per call, two lanes, pinned host arrays)",
+                    "api": "ef_hps_mixed_solve_blocks (K blocks per call, three lanes, pinned host arrays)",
                     "one_block_per_call_solves_per_s": e2e_single},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,

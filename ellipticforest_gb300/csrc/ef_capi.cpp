@@ -29,13 +29,20 @@ struct ef_server {
 struct ef_hps {
     std::unique_ptr<efgb::Hps> hps;
     std::unique_ptr<efgb::MixedSolver> mixed;
-    // second lane of ef_hps_mixed_solve_blocks (shares mixed's FP32 operators) and its stream
-    std::unique_ptr<efgb::MixedSolver> mixed2;
-    cudaStream_t stream2 = nullptr;
+    // further lanes 1.. (share mixed's FP32 operators), each with its own stream
+    static constexpr int kMaxLanes = 4;
+    std::unique_ptr<efgb::MixedSolver> lanes[kMaxLanes];
+    cudaStream_t lane_st[kMaxLanes] = {};
+    void drop_lanes() {
+        for (int k = 1; k < kMaxLanes; ++k) {
+            if (lane_st[k]) cudaStreamSynchronize(lane_st[k]);
+            lanes[k].reset();
+        }
+    }
     ~ef_hps() {
-        if (stream2) cudaStreamSynchronize(stream2);
-        mixed2.reset();
-        if (stream2) cudaStreamDestroy(stream2);
+        drop_lanes();
+        for (int k = 1; k < kMaxLanes; ++k)
+            if (lane_st[k]) cudaStreamDestroy(lane_st[k]);
     }
     bool cache_operators = false;
     bool homogeneous_rhs = false;
@@ -512,8 +519,7 @@ int ef_hps_mixed_init(ef_hps* h, int bmax) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->hps->built() && !h->hps->built32()) return fail(EF_ERR_STATE, "mixed solver before build stage");
     return guarded([&] {
-        if (h->stream2) cudaStreamSynchronize(h->stream2);
-        h->mixed2.reset();
+        h->drop_lanes();
         h->mixed.reset();
         h->mixed = std::make_unique<efgb::MixedSolver>(*h->hps, bmax);
         return EF_OK;
@@ -565,35 +571,35 @@ int ef_hps_mixed_solve(ef_hps* h, int batch, int sweeps, const double* f, const 
 }
 
 namespace {
-// the second lane (shares the FP32 operators of h->mixed, own stream), created on first use; it starts
+// lane k >= 1 (shares the FP32 operators of h->mixed, own stream), created on first use; it starts
 // after the work already queued on the tree's stream
-int lane2(ef_hps* h) {
-    if (!h->mixed2) {
-        if (!h->stream2) {
-            const int st = cuda_status(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking), "lane stream");
+int ensure_lane(ef_hps* h, int k) {
+    if (!h->lanes[k]) {
+        if (!h->lane_st[k]) {
+            const int st = cuda_status(cudaStreamCreateWithFlags(&h->lane_st[k], cudaStreamNonBlocking), "lane stream");
             if (st) return st;
         }
-        h->mixed2 = std::make_unique<efgb::MixedSolver>(*h->hps, h->mixed->bmax(), h->mixed.get());
-        h->mixed2->set_stream(h->stream2);
+        h->lanes[k] = std::make_unique<efgb::MixedSolver>(*h->hps, h->mixed->bmax(), h->mixed.get());
+        h->lanes[k]->set_stream(h->lane_st[k]);
     }
     cudaEvent_t ready;
     int st = cuda_status(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "lane event");
     if (!st) st = cuda_status(cudaEventRecord(ready, h->mixed->stream()), "lane event");
-    if (!st) st = cuda_status(cudaStreamWaitEvent(h->stream2, ready, 0), "lane event");
+    if (!st) st = cuda_status(cudaStreamWaitEvent(h->lane_st[k], ready, 0), "lane event");
     cudaEventDestroy(ready);
     return st;
 }
 
-efgb::MixedSolver* lane_solver(ef_hps* h, int lane) { return lane == 0 ? h->mixed.get() : h->mixed2.get(); }
+efgb::MixedSolver* lane_solver(ef_hps* h, int lane) { return lane == 0 ? h->mixed.get() : h->lanes[lane].get(); }
 }  // namespace
 
 int ef_hps_mixed_lane(ef_hps* h, int lane, double** f, double** a, double** r, double** u, void** stream) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
-    if (lane != 0 && lane != 1) return fail(EF_ERR_INVALID, "lane must be 0 or 1");
+    if (lane < 0 || lane >= ef_hps::kMaxLanes) return fail(EF_ERR_INVALID, "lane out of range");
     return guarded([&] {
-        if (lane == 1) {
-            const int st = lane2(h);
+        if (lane > 0) {
+            const int st = ensure_lane(h, lane);
             if (st) return st;
         }
         efgb::MixedSolver* X = lane_solver(h, lane);
@@ -609,8 +615,8 @@ int ef_hps_mixed_lane(ef_hps* h, int lane, double** f, double** a, double** r, d
 int ef_hps_mixed_lane_solve_async(ef_hps* h, int lane, int batch, int sweeps) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
-    if (lane != 0 && lane != 1) return fail(EF_ERR_INVALID, "lane must be 0 or 1");
-    if (lane == 1 && !h->mixed2) return fail(EF_ERR_STATE, "lane 1 not set up (ef_hps_mixed_lane)");
+    if (lane < 0 || lane >= ef_hps::kMaxLanes) return fail(EF_ERR_INVALID, "lane out of range");
+    if (lane > 0 && !h->lanes[lane]) return fail(EF_ERR_STATE, "lane not set up (ef_hps_mixed_lane)");
     return guarded([&] {
         lane_solver(h, lane)->solve(batch, sweeps);
         return cuda_status(cudaGetLastError(), "mixed solve launch");
@@ -627,14 +633,16 @@ int ef_hps_mixed_solve_blocks(ef_hps* h, int nblocks, const int* batch, int swee
     }
     return guarded([&] {
         efgb::Hps& H = *h->hps;
-        if (nblocks > 1) {
-            const int st = lane2(h);
+        // three lanes: while one lane solves, the copy engines serve the other two in both directions
+        const int nl = nblocks < 3 ? (nblocks < 1 ? 1 : nblocks) : 3;
+        for (int k = 1; k < nl; ++k) {
+            const int st = ensure_lane(h, k);
             if (st) return st;
         }
         const size_t cells1 = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();
         const size_t m1 = 4 * size_t(H.root_M());
         for (int k = 0; k < nblocks; ++k) {
-            efgb::MixedSolver& X = (k & 1) ? *h->mixed2 : *h->mixed;
+            efgb::MixedSolver& X = *lane_solver(h, k % nl);
             cudaStream_t s = X.stream();
             const size_t cells = cells1 * batch[k], m = m1 * batch[k];
             int st = cuda_status(cudaMemcpyAsync(X.f(), f[k], cells * 8, cudaMemcpyHostToDevice, s), "copy f");
@@ -648,8 +656,7 @@ int ef_hps_mixed_solve_blocks(ef_hps* h, int nblocks, const int* batch, int swee
         }
         int st = EF_OK;
         int err = 0;
-        if (nblocks > 0) err |= h->mixed->take_error();  // synchronises the lane's stream
-        if (nblocks > 1) err |= h->mixed2->take_error();
+        for (int k = 0; k < nl && k < nblocks; ++k) err |= lane_solver(h, k)->take_error();  // synchronises the lane
         if (err) return fail(EF_ERR_CUDA, "mixed solve: an operator tile copy did not complete");
         return st;
     });

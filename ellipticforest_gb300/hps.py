@@ -590,8 +590,8 @@ class HPSAlgorithm:
 
     def mixed_solve_blocks(self, blocks, sweeps: int = 1, out=None):
         """Pipelined form of mixed_solve for many blocks: blocks is a sequence of (f, a, r) arrays
-        shaped as for mixed_solve (each block at most mixed_bmax requests); the blocks alternate
-        between two lanes so that host copies overlap the solves.  Returns (or fills) one u array per
+        shaped as for mixed_solve (each block at most mixed_bmax requests); the blocks rotate over
+        three lanes so that host copies overlap the solves.  Returns (or fills) one u array per
         block.  Page-locked arrays keep the copies asynchronous."""
         blocks = [tuple(np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64) for x in blk) for blk in blocks]
         nb = len(blocks)
@@ -624,8 +624,8 @@ class HPSAlgorithm:
             check(_lib.load().ef_hps_mixed_lane_solve_async(self._h, int(lane), int(batch), int(sweeps)))
 
     def mixed_lane(self, lane: int):
-        """Device pointers (f, a, r, u) and the CUDA stream (int) of lane 0 or 1; lane 1 shares the
-        FP32 operators and is created by the first call for it."""
+        """Device pointers (f, a, r, u) and the CUDA stream (int) of lane 0..3; lanes >= 1 share the
+        FP32 operators and are created by the first call for them."""
         ptrs = [C.c_void_p() for _ in range(5)]
         check(_lib.load().ef_hps_mixed_lane(self._h, int(lane), *[C.byref(p) for p in ptrs]))
         return [p.value or 0 for p in ptrs]

@@ -155,16 +155,17 @@ int ef_hps_mixed_solve_async(ef_hps* hps, int batch, int sweeps);
 int ef_hps_mixed_solve(ef_hps* hps, int batch, int sweeps, const double* f_host, const double* a_host,
                        const double* r_host, double* u_host);
 /* Pipelined host form for many blocks: block k (batch[k] <= bmax requests, host arrays f[k], a[k],
- * r[k] in and u[k] out, each laid out as for ef_hps_mixed_solve) runs on one of two lanes that
- * share the tree's FP32 operators, alternating, each lane on its own stream, so the copies of one
- * block overlap the solve of the other (page-locked host memory keeps the copies asynchronous).
- * Returns when every block's u is on the host.  The second lane holds its own block buffers. */
+ * r[k] in and u[k] out, each laid out as for ef_hps_mixed_solve) runs on lane k mod 3 (lanes share
+ * the tree's FP32 operators, each has its own stream and block buffers), so the host copies of two
+ * blocks overlap the solve of a third (page-locked host memory keeps the copies asynchronous).
+ * Returns when every block's u is on the host. */
 int ef_hps_mixed_solve_blocks(ef_hps* hps, int nblocks, const int* batch, int sweeps, const double* const* f_host,
                               const double* const* a_host, const double* const* r_host, double* const* u_host);
-/* Device-resident lanes: lane 0 is the solver of ef_hps_mixed_init (the tree's stream), lane 1 (set
- * up by the first call for it) shares its FP32 operators and runs on its own stream, so two blocks
- * can be in flight at once.  Returns the lane's resident buffers (as ef_hps_mixed_buffers) and its
- * stream (a cudaStream_t); lane 1 starts after the work queued on the tree's stream at that call. */
+/* Device-resident lanes 0..3: lane 0 is the solver of ef_hps_mixed_init (the tree's stream), lanes
+ * 1..3 (each set up by the first call for it) share its FP32 operators and run on their own streams,
+ * so several blocks can be in flight at once.  Returns the lane's resident buffers (as
+ * ef_hps_mixed_buffers) and its stream (a cudaStream_t); a lane >= 1 starts after the work queued on
+ * the tree's stream at that call. */
 int ef_hps_mixed_lane(ef_hps* hps, int lane, double** f_dev, double** a_dev, double** r_dev, double** u_dev,
                       void** stream);
 /* 1 + sweeps passes on the first `batch` requests of the lane's resident buffers, on its stream. */
