@@ -367,8 +367,9 @@ private:
 };
 
 // Mixed-precision many-RHS solver on a built FP64 Hps (FISHPACK90 leaves, Dirichlet root data):
-// FP32 copies of S, X^{-1}, H and the leaf tables; FP64 residual (5-point leaf residual + interface
-// flux mismatches) and FP32 correction passes, see ef_mixed.cu.
+// FP32 copies of S, X^{-1}, H and the leaf tables; an exact residual (5-point leaf residual in
+// fixed-point integer arithmetic + FP64 interface flux mismatches) and FP32 correction passes, see
+// ef_mixed.cu.
 class MixedSolver {
 public:
     // share: another solver of the same tree whose FP32 operators (and TMA descriptors) this one

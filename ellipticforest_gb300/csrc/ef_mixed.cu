@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
     if (lead && fail_v < 0) epilogue(first_tile);
 }
 
-// ---- FP64 residual -------------------------------------------------------------------------------
+// ---- residual: interface data of the state -------------------------------------------------------
 // children's exact Dirichlet data: exterior from the parent, interfaces from the FP64 state
 __global__ void k_mx_scatter64(const MixItem* __restrict__ items, int s, int B) {
     const MixItem& it = items[blockIdx.y];

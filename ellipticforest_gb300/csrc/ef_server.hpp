@@ -53,7 +53,7 @@ public:
     // waits up to timeout seconds; returns 1 when done, 0 on time-out
     int wait(long long id, double timeout, double* latency);
     Stats stats();
-    // FP64 refinement sweeps of the tree's later blocks (the creation value until set)
+    // refinement sweeps of the tree's later blocks (the creation value until set)
     void set_sweeps(int tree, int sweeps);
     int lanes(int tree) const { return int(trees_.at(tree).lanes.size()); }
     long long device_bytes() const { return bytes_; }

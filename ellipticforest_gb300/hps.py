@@ -671,7 +671,7 @@ class Server:
     solver; the scheduler thread of the library forms a block from every request of a tree that has
     arrived whenever one of the tree's lanes is free, and overlaps blocks of different lanes and trees
     on the GPU.  Lanes beyond the first per tree are created only while the device memory of all
-    lanes fits hbm_budget_bytes (0: no limit).  sweeps: FP64 refinement sweeps per block, one value
+    lanes fits hbm_budget_bytes (0: no limit).  sweeps: refinement sweeps per block, one value
     for every tree or one per tree."""
 
     def __init__(self, trees, bmax, lanes: int = 2, hbm_budget_bytes: int = 0, sweeps=1):
@@ -694,7 +694,7 @@ class Server:
         self._live = {}  # id -> arrays kept alive until completion
 
     def set_sweeps(self, tree: int, sweeps: int) -> None:
-        """FP64 refinement sweeps of the tree's blocks from the next block on."""
+        """Refinement sweeps of the tree's blocks from the next block on."""
         check(_lib.load().ef_server_set_sweeps(self._h, int(tree), int(sweeps)))
 
     def lanes(self, tree: int) -> int:

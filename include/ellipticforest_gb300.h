@@ -142,10 +142,10 @@ int ef_hps_synchronize(ef_hps* hps);
 
 /* ---- Mixed precision, many right-hand sides (no counterpart in the reference) ---------------
  * After ef_hps_build: FP32 copies of the merge operators and leaf tables; each solve runs FP32
- * HPS passes on a block of up to bmax requests and refines them against an FP64 residual (the
- * 5-point residual of every leaf cell plus the flux mismatch at every merge interface), so the
- * result converges to the FP64 HPS solution.  FISHPACK90 leaves and Dirichlet root data
- * (b == 0) only. */
+ * HPS passes on a block of up to bmax requests and refines them against the exact residual (the
+ * 5-point residual of every leaf cell, evaluated in fixed-point integer arithmetic, plus the FP64
+ * flux mismatch at every merge interface), so the result converges to the FP64 HPS solution.
+ * Dirichlet root data (b == 0) only. */
 int ef_hps_mixed_init(ef_hps* hps, int bmax);
 /* Resident buffers: f [B][num_leaves*n*n], a and r [B][4M] (root data, a u = r), u [B][...]. */
 int ef_hps_mixed_buffers(ef_hps* hps, double** f_dev, double** a_dev, double** r_dev, double** u_dev);
@@ -244,7 +244,7 @@ int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, double x_upper, 
 typedef struct ef_server ef_server;
 int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lanes_per_tree,
                      long long hbm_budget_bytes, int sweeps, ef_server** out);
-/* FP64 refinement sweeps of tree t's blocks from the next block on (creation value: sweeps) */
+/* refinement sweeps of tree t's blocks from the next block on (creation value: sweeps) */
 int ef_server_set_sweeps(ef_server* server, int tree, int sweeps);
 /* lanes created for tree t (after the budget) and device bytes held by all lanes */
 int ef_server_info(ef_server* server, int tree, int* lanes, long long* device_bytes);

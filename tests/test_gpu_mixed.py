@@ -1,4 +1,4 @@
-"""Mixed-precision many-RHS form: FP32 HPS passes refined against the FP64 residual must reach the
+"""Mixed-precision many-RHS form: FP32 HPS passes refined against the exact residual must reach the
 FP64 HPS solution to <= 1e-10 relative, on uniform and adaptive trees, and a request's result must
 not depend on the other requests of its block."""
 import numpy as np
