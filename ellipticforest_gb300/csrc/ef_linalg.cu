@@ -276,6 +276,133 @@ __global__ void __launch_bounds__(256) k_getf2_coop(int n, int k, int jb, Real* 
 }
 
 // Apply the swaps piv[k..k+jb) to the columns [c0, c0 + ncols) (LAPACK dlaswp).
+// Panel LU of a large matrix on a thread-block cluster of P CTAs (P <= 8) per matrix: CTA c holds the
+// panel rows [c R, (c+1) R) of A[k:n, k:k+jb] in its shared memory, so a column costs two cluster
+// barriers instead of grid-wide ones.  Per column: every CTA offers the largest |a| of its rows (ties
+// to the smaller row) -> barrier -> every CTA combines the P candidates read through distributed
+// shared memory (the same winner everywhere), copies the pivot row, and the owner of the pivot row
+// keeps the old row j -> barrier -> the two owners write the exchanged rows, every CTA scales its
+// rows below j and applies the rank-1 update with its copy of the pivot row.  The element operations
+// and their order are those of k_getf2_panel (bit-identical factors and pivots); rows are exchanged
+// in shared memory and written back at the end, so only the columns outside the panel still need
+// the row swaps.
+template <class Real>
+__global__ void __launch_bounds__(256) k_getf2_cluster(int n, int k, int jb, Real* const* Aarr, int lda,
+                                                       int* const* pivarr, int* info, int P, int R) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char cl_smem[];
+    Real* rows = reinterpret_cast<Real*>(cl_smem);  // R x jb, row-major
+    Real* prow = rows + (size_t)R * jb;            // copy of the pivot row
+    Real* jrow = prow + jb;                        // old row j (owner of the pivot row)
+    __shared__ Real s_val[32];
+    __shared__ int s_idx[32];
+    __shared__ Real c_val;
+    __shared__ int c_idx;
+    const int mat = blockIdx.x / P;
+    const int c = int(cluster.block_rank());
+    Real* __restrict__ A = Aarr[mat];
+    int* __restrict__ piv = pivarr[mat];
+    const int m = n - k;                  // panel height
+    const int r0 = c * R, r1 = min(m, r0 + R);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    for (int e = tid; e < (r1 - r0) * jb; e += blockDim.x) {
+        const int i = e / jb, cc = e - i * jb;
+        rows[e] = A[(long long)(k + r0 + i) * lda + k + cc];
+    }
+    __syncthreads();
+    for (int j = 0; j < jb; ++j) {
+        // (1) this CTA's candidate among its rows i >= j
+        Real best = Real(-1);
+        int bi = INT_MAX;
+        for (int i = max(j, r0) + tid; i < r1; i += blockDim.x) {
+            const Real v = fabs(rows[(size_t)(i - r0) * jb + j]);
+            if (v > best) { best = v; bi = i; }
+            else if (bi == INT_MAX) { bi = i; }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const Real ov = __shfl_down_sync(0xffffffffu, best, off);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { s_val[wid] = best; s_idx[wid] = bi; }
+        __syncthreads();
+        if (wid == 0) {
+            best = (lane < nw) ? s_val[lane] : Real(-2);
+            bi = (lane < nw) ? s_idx[lane] : INT_MAX;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const Real ov = __shfl_down_sync(0xffffffffu, best, off);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+            }
+            if (lane == 0) { c_val = best; c_idx = bi; }
+        }
+        cluster.sync();
+        // (2) the winner, the pivot row and (its owner) the old row j
+        if (wid == 0) {
+            best = (lane < P) ? *cluster.map_shared_rank(&c_val, lane) : Real(-2);
+            bi = (lane < P) ? *cluster.map_shared_rank(&c_idx, lane) : INT_MAX;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const Real ov = __shfl_down_sync(0xffffffffu, best, off);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+            }
+            if (lane == 0) s_idx[0] = (bi >= j && bi < m) ? bi : j;
+        }
+        __syncthreads();
+        const int p = s_idx[0];
+        const int cp = p / R, cj = j / R;
+        const Real* prem = cluster.map_shared_rank(rows, cp) + (size_t)(p - cp * R) * jb;
+        for (int cc = tid; cc < jb; cc += blockDim.x) prow[cc] = prem[cc];
+        if (c == cp && p != j) {
+            const Real* jrem = cluster.map_shared_rank(rows, cj) + (size_t)(j - cj * R) * jb;
+            for (int cc = tid; cc < jb; cc += blockDim.x) jrow[cc] = jrem[cc];
+        }
+        if (c == 0 && tid == 0) {
+            piv[k + j] = k + p;
+            if (!(prem[j] != Real(0)) && info[mat] == 0) info[mat] = k + j + 1;
+        }
+        cluster.sync();
+        if (p != j) {
+            if (c == cj)
+                for (int cc = tid; cc < jb; cc += blockDim.x) rows[(size_t)(j - r0) * jb + cc] = prow[cc];
+            if (c == cp)
+                for (int cc = tid; cc < jb; cc += blockDim.x) rows[(size_t)(p - r0) * jb + cc] = jrow[cc];
+        }
+        __syncthreads();
+        // (3) scale the column below the pivot, (4) rank-1 update of the panel's later columns
+        const Real pv = prow[j];
+        const int lo = max(j + 1, r0);
+        if (pv != Real(0)) {
+            if (fabs(pv) >= (sizeof(Real) == 8 ? Real(DBL_MIN) : Real(FLT_MIN))) {
+                const Real rcp = Real(1) / pv;
+                for (int i = lo + tid; i < r1; i += blockDim.x) rows[(size_t)(i - r0) * jb + j] *= rcp;
+            } else {
+                for (int i = lo + tid; i < r1; i += blockDim.x) rows[(size_t)(i - r0) * jb + j] /= pv;
+            }
+        }
+        __syncthreads();
+        const int nc = jb - j - 1;
+        if (nc > 0 && lo < r1) {
+            const int tot = (r1 - lo) * nc;
+            for (int e = tid; e < tot; e += blockDim.x) {
+                const int i = lo + e / nc, cc = j + 1 + e % nc;
+                Real* a = rows + (size_t)(i - r0) * jb;
+                a[cc] -= a[j] * prow[cc];
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < (r1 - r0) * jb; e += blockDim.x) {
+        const int i = e / jb, cc = e - i * jb;
+        A[(long long)(k + r0 + i) * lda + k + cc] = rows[e];
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
 template <class Real>
 __global__ void k_laswp_cols(int k, int jb, Real* const* Aarr, int lda, int* const* pivarr, int c0, int ncols) {
     Real* __restrict__ A = Aarr[blockIdx.y];
@@ -407,6 +534,51 @@ int coop_parts(int rows, int batch) {
     return P;
 }
 
+// CTAs per matrix for the cluster panel of a matrix with `rows` rows left: the smallest power of two
+// (2..8) that keeps a CTA's slice at <= 512 rows (FP64) / 1024 rows (FP32) -- 128 KB of shared
+// memory with a 32-column panel; 0 when the cluster panel does not apply
+template <class Real>
+int cluster_parts(int rows) {
+    if (rows < 512 || !g_cooperative_lu.load()) return 0;
+    const int rmax = sizeof(Real) == 8 ? 512 : 1024;
+    for (int P = 2; P <= 8; P *= 2)
+        if ((rows + P - 1) / P <= rmax) return P;
+    return 0;
+}
+
+template <class Real>
+bool launch_cluster_panel(cudaStream_t st, int n, int k, int jb, Real* const* A, int lda, int* const* piv,
+                          int* info, int batch, int P) {
+    const int R = (n - k + P - 1) / P;
+    const size_t smem = (size_t(R) * jb + 2 * size_t(jb)) * sizeof(Real);
+    static size_t configured = 0;
+    if (smem > configured) {
+        if (cudaFuncSetAttribute(k_getf2_cluster<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) !=
+            cudaSuccess) {
+            (void)cudaGetLastError();
+            return false;
+        }
+        configured = smem;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(P * batch));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(P);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_getf2_cluster<Real>, n, k, jb, A, lda, piv, info, P, R) != cudaSuccess) {
+        (void)cudaGetLastError();  // refused (cluster shape): the other panels
+        return false;
+    }
+    return true;
+}
+
 template <class Real>
 struct CoopScratch {  // candidate tables of the cooperative panel: 4 slots x grid
     Real* val = nullptr;
@@ -419,8 +591,10 @@ void getrf_batched_t(cudaStream_t st, int n, Real* const* A, int lda, int* const
     static CoopScratch<Real> scratch;
     for (int k = 0; k < n; k += NB) {
         const int jb = (n - k < NB) ? n - k : NB;
-        const int P = coop_parts<Real>(n - k, batch);
-        if (P > 0) {
+        const int Pc = cluster_parts<Real>(n - k);
+        if (Pc > 0 && launch_cluster_panel<Real>(st, n, k, jb, A, lda, piv, info, batch, Pc)) {
+            ++g_kernel_launches;  // rows exchanged in shared memory: no k_laswp_cols
+        } else if (const int P = coop_parts<Real>(n - k, batch); P > 0) {
             const int grid = P * batch;
             if (scratch.size < grid) {
                 cudaStreamSynchronize(st);
