@@ -195,3 +195,29 @@ def test_mixed_solve_blocks_matches_single_blocks(ef):
     got = hps.mixed_solve_blocks(blocks, sweeps=1)
     for (f, a, r), u in zip(blocks, got):
         assert np.array_equal(u, hps.mixed_solve(f, a, r, sweeps=1))
+
+
+def test_device_resident_lane_matches_lane0(ef):
+    """Lane 1 (shares lane 0's FP32 operators, own stream) solves its resident block to the same bits."""
+    torch = pytest.importorskip("torch")
+    mesh, hps = make(ef, ("uniform", 3), 16, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, 3, 51)
+    hps.mixed_init(3)
+    u0 = hps.mixed_solve(F, A, R, sweeps=1)
+    # the pipelined call leaves block k's inputs resident in lane k % 3: two blocks fill lanes 0, 1
+    hps.mixed_solve_blocks([(F, A, R), (F, A, R)], sweeps=1)
+    f1, a1, r1, u1p, st1 = hps.mixed_lane(1)
+    hps.mixed_solve_async(3, 1, lane=1)
+    torch.cuda.synchronize()
+    n = F.shape[1]
+    out = torch.empty(3 * n, dtype=torch.float64, device="cuda")
+    import ctypes
+    ctypes.CDLL(None)  # keep ctypes loaded
+    src = torch.cuda.ExternalStream(st1)
+    with torch.cuda.stream(src):
+        # copy lane 1's device result through torch (raw pointer wrapped by the CUDA array interface)
+        class _Arr:
+            __cuda_array_interface__ = {"shape": (3 * n,), "typestr": "<f8", "data": (u1p, False), "version": 3}
+        out.copy_(torch.as_tensor(_Arr(), device="cuda"))
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().reshape(3, n), u0)
