@@ -210,14 +210,10 @@ def test_device_resident_lane_matches_lane0(ef):
     hps.mixed_solve_async(3, 1, lane=1)
     torch.cuda.synchronize()
     n = F.shape[1]
-    out = torch.empty(3 * n, dtype=torch.float64, device="cuda")
-    import ctypes
-    ctypes.CDLL(None)  # keep ctypes loaded
-    src = torch.cuda.ExternalStream(st1)
-    with torch.cuda.stream(src):
-        # copy lane 1's device result through torch (raw pointer wrapped by the CUDA array interface)
-        class _Arr:
-            __cuda_array_interface__ = {"shape": (3 * n,), "typestr": "<f8", "data": (u1p, False), "version": 3}
-        out.copy_(torch.as_tensor(_Arr(), device="cuda"))
+
+    class _Lane1U:  # lane 1's device result, wrapped through the CUDA array interface
+        __cuda_array_interface__ = {"shape": (3 * n,), "typestr": "<f8", "data": (u1p, False), "version": 3}
+
+    out = torch.as_tensor(_Lane1U(), device="cuda").clone()
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy().reshape(3, n), u0)
