@@ -845,6 +845,14 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     const int nact = (long long)item0 + ipc <= items ? ipc : int(items - item0);
     // items per block, a compile-time constant for the fixed leaf sizes
     const int IPC = NT ? 256 / (NT * NT / 4 < 256 ? NT * NT / 4 : 256) : ipc;
+    // the first loads of f and u are issued before the ghost phase so that the latencies overlap
+    double2 pf01 = make_double2(0.0, 0.0), pf23 = pf01, pu01 = pf01, pu23 = pf01;
+    if (act) {
+        pf01 = *reinterpret_cast<const double2*>(ff + 4 * lt);
+        pf23 = *reinterpret_cast<const double2*>(ff + 4 * lt + 2);
+        pu01 = *reinterpret_cast<const double2*>(uu + 4 * lt);
+        pu23 = *reinterpret_cast<const double2*>(uu + 4 * lt + 2);
+    }
     // (0) ghost data of the block's items, requests fastest: the items of a block are consecutive
     // requests of one leaf whenever B is a multiple of ipc, so these reads coalesce
     for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
@@ -857,11 +865,11 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     int eu = 1, ef = 1;
     if (act) {
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
-            const double2 f01 = *reinterpret_cast<const double2*>(ff + 4 * e4);
-            const double2 f23 = *reinterpret_cast<const double2*>(ff + 4 * e4 + 2);
+            const double2 f01 = e4 == lt ? pf01 : *reinterpret_cast<const double2*>(ff + 4 * e4);
+            const double2 f23 = e4 == lt ? pf23 : *reinterpret_cast<const double2*>(ff + 4 * e4 + 2);
             ef = max(max(ef, max(fx_bexp(f01.x), fx_bexp(f01.y))), max(fx_bexp(f23.x), fx_bexp(f23.y)));
-            const double2 c01 = *reinterpret_cast<const double2*>(uu + 4 * e4);
-            const double2 c23 = *reinterpret_cast<const double2*>(uu + 4 * e4 + 2);
+            const double2 c01 = e4 == lt ? pu01 : *reinterpret_cast<const double2*>(uu + 4 * e4);
+            const double2 c23 = e4 == lt ? pu23 : *reinterpret_cast<const double2*>(uu + 4 * e4 + 2);
             eu = max(max(eu, max(fx_bexp(c01.x), fx_bexp(c01.y))), max(fx_bexp(c23.x), fx_bexp(c23.y)));
         }
         for (int k = lt; k < n4; k += tpe) eu = max(eu, fx_bexp(gd[k]));
@@ -1052,6 +1060,16 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
             sh[threadIdx.x] = leaves[lf].h64 + bb;
         }
     }
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
+    const long long base = ((long long)b * L + leaf) * nn;
+    const double* ff = f + base;
+    // the first four loads are issued before the ghost phase so that both latencies overlap
+    double2 p01 = make_double2(0.0, 0.0), p23 = p01;
+    if (act) {
+        p01 = *reinterpret_cast<const double2*>(ff + 4 * lt);
+        p23 = *reinterpret_cast<const double2*>(ff + 4 * lt + 2);
+    }
     __syncthreads();
     const int nact = (long long)item0 + ipc <= items ? ipc : int(items - item0);
     const int IPC = NT ? 256 / (NT * NT / 4 < 256 ? NT * NT / 4 : 256) : ipc;
@@ -1066,19 +1084,15 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
         }
     }
     __syncthreads();
-    const int leaf = act ? item / B : 0;
-    const int b = act ? item - leaf * B : 0;
     const MixCoef cf = coefs[leaves[leaf].type];
     double* gd = r0_gd + slot * n4;
     const float* gts = gt + slot * n4;
     float mx = 0.f;
     if (act) {
-        const long long base = ((long long)b * L + leaf) * nn;
-        const double* ff = f + base;
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
             const int e = 4 * e4, i = e / n, j0 = e - i * n;
-            const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
-            const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
+            const double2 f01 = e4 == lt ? p01 : *reinterpret_cast<const double2*>(ff + e);
+            const double2 f23 = e4 == lt ? p23 : *reinterpret_cast<const double2*>(ff + e + 2);
             float rr[4] = {d2f_rn_bits(f01.x), d2f_rn_bits(f01.y), d2f_rn_bits(f23.x), d2f_rn_bits(f23.y)};
             if (i == 0)
 #pragma unroll
