@@ -525,6 +525,21 @@ __global__ void k_mx_uncoarsen(const T* const* vin, T* const* vout, int nf, int 
 // an item holds n*n floats of shared memory.  Every sum runs over t = 0 .. n-1 in order.
 // NEUMANN writes h32 = DtN(0, q); SOLVE adds the solution of (g32, q) to the FP64 state u64 (or
 // stores it there when accumulate is 0).
+// Float offset of the 4-float chunk c4 of row `row` in an item buffer.  For n = 16 two rows share a
+// 128-byte line and the line's eight chunks are permuted by an XOR with the line index, so that a
+// quarter-warp's transposed block stores (rows 4 bj + c, chunk bi) and block stores (rows 4 bi + a,
+// chunk bj) reach all 32 banks -- row-major puts them four and two to a bank group -- while the
+// reads of one row stay a permutation of that row's chunks.
+template <int NT>
+__device__ __forceinline__ int mx_xoff(int row, int c4, int n) {
+    if (NT == 16) {
+        const int line = row >> 1;
+        const int h = ((line & 2) << 1) | ((line & 4) >> 1);
+        return (line << 5) + (((((row & 1) << 2) | c4) ^ h) << 2);
+    }
+    return row * n + 4 * c4;
+}
+
 template <int MODE, int NT>
 __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restrict__ types,
                                                    const MixLeaf* __restrict__ leaves, int L, int B, int n_arg,
@@ -584,7 +599,7 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
                 }
                 v = make_float4(t[0], t[1], t[2], t[3]);
             }
-            *reinterpret_cast<float4*>(X[k] + r * n + 4 * bj) = v;
+            *reinterpret_cast<float4*>(X[k] + mx_xoff<NT>(r, bj, n)) = v;
         }
     }
     __syncthreads();
@@ -612,8 +627,9 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
 #pragma unroll
         for (int t = 0; t < (NT ? NT : n); ++t) {
             const float4 x = *reinterpret_cast<const float4*>(V + t * n + 4 * bi);
-            const float4 y0 = *reinterpret_cast<const float4*>(X[0] + t * n + 4 * bj);
-            const float4 y1 = *reinterpret_cast<const float4*>(X[1] + t * n + 4 * bj);
+            const int o = mx_xoff<NT>(t, bj, n);
+            const float4 y0 = *reinterpret_cast<const float4*>(X[0] + o);
+            const float4 y1 = *reinterpret_cast<const float4*>(X[1] + o);
             fma4(0, x, y0);
             fma4(1, x, y1);
         }
@@ -623,8 +639,9 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
 #pragma unroll
         for (int t = 0; t < (NT ? NT : n); ++t) {
             const float4 y = *reinterpret_cast<const float4*>(V + t * n + 4 * bj);
-            const float4 x0 = *reinterpret_cast<const float4*>(X[0] + t * n + 4 * bi);
-            const float4 x1 = *reinterpret_cast<const float4*>(X[1] + t * n + 4 * bi);
+            const int o = mx_xoff<NT>(t, bi, n);
+            const float4 x0 = *reinterpret_cast<const float4*>(X[0] + o);
+            const float4 x1 = *reinterpret_cast<const float4*>(X[1] + o);
             fma4(0, x0, y);
             fma4(1, x1, y);
         }
@@ -636,7 +653,7 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
             if (act[k])
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    *reinterpret_cast<float4*>(X[k] + (4 * bj + c) * n + 4 * bi) =
+                    *reinterpret_cast<float4*>(X[k] + mx_xoff<NT>(4 * bj + c, bi, n)) =
                         make_float4(acc[k][0][c], acc[k][1][c], acc[k][2][c], acc[k][3][c]);
     };
     // (1) WT[j][k] = sum_i V[i][k] F[i][j]
@@ -656,7 +673,7 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 const float4 d = *reinterpret_cast<const float4*>(Dinv + (4 * bi + a) * n + 4 * bj);
-                *reinterpret_cast<float4*>(X[k] + (4 * bi + a) * n + 4 * bj) =
+                *reinterpret_cast<float4*>(X[k] + mx_xoff<NT>(4 * bi + a, bj, n)) =
                     make_float4(acc[k][a][0] * d.x, acc[k][a][1] * d.y, acc[k][a][2] * d.z, acc[k][a][3] * d.w);
             }
         }
@@ -704,13 +721,13 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
             for (int g4 = lt; g4 < n; g4 += tpi) {
                 const int side = (4 * g4) / n, p0 = 4 * g4 - side * n;
                 const int fixed = side == 0 || side == 2 ? 0 : n - 1;
-                const float* vec = side < 2 ? VT + p0 : W + p0;       // float4 along the side
-                const float* sca = side < 2 ? W + fixed : VT + fixed;  // broadcast per l
                 float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                 for (int l = 0; l < (NT ? NT : n); ++l) {
-                    const float4 v = *reinterpret_cast<const float4*>(vec + l * n);
-                    const float a = sca[l * n];
+                    // a float4 along the side and a broadcast value per l
+                    const float4 v = *reinterpret_cast<const float4*>(
+                        side < 2 ? VT + l * n + p0 : W + mx_xoff<NT>(l, p0 >> 2, n));
+                    const float a = side < 2 ? W[mx_xoff<NT>(l, fixed >> 2, n) + (fixed & 3)] : VT[l * n + fixed];
                     u.x = fmaf(a, v.x, u.x);
                     u.y = fmaf(a, v.y, u.y);
                     u.z = fmaf(a, v.z, u.z);
