@@ -211,6 +211,7 @@ __device__ __forceinline__ void group_dot_acc(const double* __restrict__ row, co
             a2 = fma(m2.x, v2.x, a2); a2 = fma(m2.y, v2.y, a2);
             a3 = fma(m3.x, v3.x, a3); a3 = fma(m3.y, v3.y, a3);
         }
+#pragma unroll 3
         for (; i < n2; i += LPR) {
             const double2 m0 = __ldcs(r2 + i), v0 = __ldg(x2 + i);
             a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
@@ -223,6 +224,7 @@ __device__ __forceinline__ void group_dot_acc(const double* __restrict__ row, co
             a2 = fma(__ldcs(row + i + 2 * LPR), __ldg(x + i + 2 * LPR), a2);
             a3 = fma(__ldcs(row + i + 3 * LPR), __ldg(x + i + 3 * LPR), a3);
         }
+#pragma unroll 3
         for (; i < len; i += LPR) a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
     }
 }
@@ -311,12 +313,13 @@ __global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__
     }
 }
 
-// lanes per row for a row (segment) of `len` doubles
+// lanes per row for a row (segment) of `len` doubles: at least four loads per lane where the row
+// allows, so that every lane has several independent loads in flight
 inline int pick_lpr(int len, bool vec) {
     const int units = vec ? len / 2 : len;
-    if (units >= 64) return 32;
-    if (units >= 32) return 16;
-    if (units >= 16) return 8;
+    if (units >= 128) return 32;
+    if (units >= 64) return 16;
+    if (units >= 32) return 8;
     return 4;
 }
 
