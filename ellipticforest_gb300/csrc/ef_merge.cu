@@ -5,6 +5,8 @@
 // (I2, I3) side, the upper child on its S or W side.  Parent exterior points are WESN with
 // W = [alpha_W; gamma_W], E = [beta_E; omega_E], S = [alpha_S; beta_S], N = [gamma_N; omega_N]
 // (the pi_WESN = {0,4,2,6,1,3,5,7} reorder of HPSAlgorithm.hpp:979-993).
+#include <algorithm>
+
 #include "ef_kernels.cuh"
 
 namespace efgb {
@@ -182,6 +184,9 @@ __global__ void k_uncoarsen_vec(const double* const* vin, double* const* vout, i
     }
 }
 
+// threads per CTA of the interface GEMVs
+constexpr int kGemvThreads = 128;
+
 // Group dot products: LPR consecutive lanes (LPR in {4, 8, 16, 32}) share one matrix row; the
 // row is streamed with evict-first loads, the vector is read through L1.
 template <int LPR>
@@ -191,42 +196,67 @@ __device__ __forceinline__ double group_sum(double v) {
     return v;
 }
 
-// accumulate row[0:len) . x[0:len) over the lanes of one group (sl = lane within the group).
-// VEC: row and x 16-byte aligned and len even -> double2 loads.
+// This lane's share of row[0:len) . x[0:len) for one group of LPR lanes (sl = lane within the
+// group), where x[i] = xa[i] for i < split and xb[i - split] after (split even when VEC).  Eight
+// independent row loads per lane and step keep enough bytes in flight at the occupancy these
+// kernels run at (a vector load serving four rows, with four times the registers, ran slower).
+// VEC: row, xa and xb 16-byte aligned and len even -> double2 loads.
 template <bool VEC, int LPR>
-__device__ __forceinline__ void group_dot_acc(const double* __restrict__ row, const double* __restrict__ x,
-                                              int len, int sl, double& a0, double& a1, double& a2, double& a3) {
+__device__ __forceinline__ double group_dot(const double* __restrict__ row, const double* __restrict__ xa,
+                                             const double* __restrict__ xb, int split, int len, int sl) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     if (VEC) {
         const double2* r2 = reinterpret_cast<const double2*>(row);
-        const double2* x2 = reinterpret_cast<const double2*>(x);
-        const int n2 = len >> 1;
+        const double2* xa2 = reinterpret_cast<const double2*>(xa);
+        const double2* xb2 = reinterpret_cast<const double2*>(xb) - (split >> 1);
+        const int n2 = len >> 1, s2 = split >> 1;
         int i = sl;
-        for (; i + 3 * LPR < n2; i += 4 * LPR) {
-            const double2 m0 = __ldcs(r2 + i), m1 = __ldcs(r2 + i + LPR);
-            const double2 m2 = __ldcs(r2 + i + 2 * LPR), m3 = __ldcs(r2 + i + 3 * LPR);
-            const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + LPR);
-            const double2 v2 = __ldg(x2 + i + 2 * LPR), v3 = __ldg(x2 + i + 3 * LPR);
-            a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
-            a1 = fma(m1.x, v1.x, a1); a1 = fma(m1.y, v1.y, a1);
-            a2 = fma(m2.x, v2.x, a2); a2 = fma(m2.y, v2.y, a2);
-            a3 = fma(m3.x, v3.x, a3); a3 = fma(m3.y, v3.y, a3);
+        for (; i + 7 * LPR < n2; i += 8 * LPR) {
+            double2 m[8], v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) m[u] = __ldcs(r2 + i + u * LPR);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = i + u * LPR;
+                v[u] = __ldg((k < s2 ? xa2 : xb2) + k);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u += 4) {
+                a0 = fma(m[u].x, v[u].x, a0); a0 = fma(m[u].y, v[u].y, a0);
+                a1 = fma(m[u + 1].x, v[u + 1].x, a1); a1 = fma(m[u + 1].y, v[u + 1].y, a1);
+                a2 = fma(m[u + 2].x, v[u + 2].x, a2); a2 = fma(m[u + 2].y, v[u + 2].y, a2);
+                a3 = fma(m[u + 3].x, v[u + 3].x, a3); a3 = fma(m[u + 3].y, v[u + 3].y, a3);
+            }
         }
-#pragma unroll 3
+#pragma unroll 7
         for (; i < n2; i += LPR) {
-            const double2 m0 = __ldcs(r2 + i), v0 = __ldg(x2 + i);
+            const double2 m0 = __ldcs(r2 + i), v0 = __ldg((i < s2 ? xa2 : xb2) + i);
             a0 = fma(m0.x, v0.x, a0); a0 = fma(m0.y, v0.y, a0);
         }
     } else {
+        const double* xbs = xb - split;
         int i = sl;
-        for (; i + 3 * LPR < len; i += 4 * LPR) {
-            a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
-            a1 = fma(__ldcs(row + i + LPR), __ldg(x + i + LPR), a1);
-            a2 = fma(__ldcs(row + i + 2 * LPR), __ldg(x + i + 2 * LPR), a2);
-            a3 = fma(__ldcs(row + i + 3 * LPR), __ldg(x + i + 3 * LPR), a3);
+        for (; i + 7 * LPR < len; i += 8 * LPR) {
+            double m[8], v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) m[u] = __ldcs(row + i + u * LPR);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = i + u * LPR;
+                v[u] = __ldg((k < split ? xa : xbs) + k);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u += 4) {
+                a0 = fma(m[u], v[u], a0);
+                a1 = fma(m[u + 1], v[u + 1], a1);
+                a2 = fma(m[u + 2], v[u + 2], a2);
+                a3 = fma(m[u + 3], v[u + 3], a3);
+            }
         }
-#pragma unroll 3
-        for (; i < len; i += LPR) a0 = fma(__ldcs(row + i), __ldg(x + i), a0);
+#pragma unroll 7
+        for (; i < len; i += LPR) a0 = fma(__ldcs(row + i), __ldg((i < split ? xa : xbs) + i), a0);
     }
+    return (a0 + a1) + (a2 + a3);
 }
 
 // hDiff = h_upper - h_lower per interface point (HPSAlgorithm.hpp:1061-1081)
@@ -240,30 +270,30 @@ __global__ void k_hdiff(const MergeItem* __restrict__ items, int s) {
     it.hd[r] = it.hc[upper_child(I)][q_upper(I, o, s)] - it.hc[lower_child(I)][q_lower(I, o, s)];
 }
 
-// Row index handled by this thread's lane group; groups never leave early (full-warp shuffles).
+// Row handled by this thread's lane group; groups never leave early (full-warp shuffles).
 template <int LPR>
 __device__ __forceinline__ long long group_row() {
-    return blockIdx.x * (long long)(256 / LPR) + threadIdx.x / LPR;
+    return blockIdx.x * (long long)(kGemvThreads / LPR) + threadIdx.x / LPR;
 }
 
 // w = X^{-1} hDiff (the X^{-1} block of RHS, columns [8s, 12s))
 template <bool VEC, int LPR>
-__global__ void __launch_bounds__(256) k_gemv_w(const MergeItem* __restrict__ items, int s, long long nrows) {
+__global__ void __launch_bounds__(kGemvThreads) k_gemv_w(const MergeItem* __restrict__ items, int s, long long nrows) {
     const int sl = threadIdx.x & (LPR - 1);
     const long long g = group_row<LPR>();
     const bool ok = g < nrows;
     const int m4 = 4 * s;
     const int item = ok ? int(g / m4) : 0, r = ok ? int(g - (long long)item * m4) : 0;
     const MergeItem& it = items[item];
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    if (ok) group_dot_acc<VEC, LPR>(it.RHS + (long long)r * (12LL * s) + 8 * s, it.hd, m4, sl, a0, a1, a2, a3);
-    const double acc = group_sum<LPR>((a0 + a1) + (a2 + a3));
+    const double part = ok ? group_dot<VEC, LPR>(it.RHS + (long long)r * (12LL * s) + 8 * s, it.hd, it.hd, m4, m4, sl) : 0.0;
+    const double acc = group_sum<LPR>(part);
     if (ok && sl == 0) it.w[r] = acc;
 }
 
-// h = H w + h_update (HPSAlgorithm.hpp:1098-1117), compact H rows already in WESN order
+// h = H w + h_update (HPSAlgorithm.hpp:1098-1117), compact H rows already in WESN order; the
+// compact H row p is contiguous: its first s entries multiply w on interface Ia, the rest Ib
 template <bool VEC, int LPR>
-__global__ void __launch_bounds__(256) k_gemv_h(const MergeItem* __restrict__ items, int s, long long nrows) {
+__global__ void __launch_bounds__(kGemvThreads) k_gemv_h(const MergeItem* __restrict__ items, int s, long long nrows) {
     const int sl = threadIdx.x & (LPR - 1);
     const long long g = group_row<LPR>();
     const bool ok = g < nrows;
@@ -273,21 +303,16 @@ __global__ void __launch_bounds__(256) k_gemv_h(const MergeItem* __restrict__ it
     int c, q, Ia, Ib;
     ext_map(p, s, c, q);
     child_ifaces(c, Ia, Ib);
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    if (ok) {
-        const double* row = it.H + (long long)p * (2LL * s);
-        group_dot_acc<VEC, LPR>(row, it.w + Ia * s, s, sl, a0, a1, a2, a3);
-        group_dot_acc<VEC, LPR>(row + s, it.w + Ib * s, s, sl, a0, a1, a2, a3);
-    }
-    const double acc = group_sum<LPR>((a0 + a1) + (a2 + a3));
+    const double part = ok ? group_dot<VEC, LPR>(it.H + (long long)p * (2LL * s), it.w + Ia * s, it.w + Ib * s, s, 2 * s, sl) : 0.0;
+    const double acc = group_sum<LPR>(part);
     if (ok && sl == 0) it.h[p] = acc + it.hc[c][q];
 }
 
 // u_Gamma = S g + w (HPSAlgorithm.hpp:1197-1204) scattered to the children's interface data; the
 // leading threads also copy the exterior data of the children (HPSAlgorithm.hpp:1214-1227)
 template <bool VEC, int LPR>
-__global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__ items, int s,
-                                                   long long nrows, int nitems, int add_w) {
+__global__ void __launch_bounds__(kGemvThreads) k_gemv_down(const MergeItem* __restrict__ items, int s,
+                                                            long long nrows, int nitems, int add_w) {
     const int m4 = 4 * s, m8 = 8 * s;
     const long long ext = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (ext < (long long)nitems * m8) {
@@ -302,9 +327,8 @@ __global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__
     const bool ok = g < nrows;
     const int item = ok ? int(g / m4) : 0, r = ok ? int(g - (long long)item * m4) : 0;
     const MergeItem& it = items[item];
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    if (ok) group_dot_acc<VEC, LPR>(it.RHS + (long long)r * (12LL * s), it.gf, m8, sl, a0, a1, a2, a3);
-    const double acc = group_sum<LPR>((a0 + a1) + (a2 + a3));
+    const double part = ok ? group_dot<VEC, LPR>(it.RHS + (long long)r * (12LL * s), it.gf, it.gf, m8, m8, sl) : 0.0;
+    const double acc = group_sum<LPR>(part);
     if (ok && sl == 0) {
         const double u = add_w ? acc + it.w[r] : acc;
         const int I = r / s, o = r - I * s;
@@ -313,22 +337,21 @@ __global__ void __launch_bounds__(256) k_gemv_down(const MergeItem* __restrict__
     }
 }
 
-// lanes per row for a row (segment) of `len` doubles: at least four loads per lane where the row
-// allows, so that every lane has several independent loads in flight
+// lanes per row for a row of `len` doubles: eight loads per lane where the row allows
 inline int pick_lpr(int len, bool vec) {
     const int units = vec ? len / 2 : len;
-    if (units >= 128) return 32;
-    if (units >= 64) return 16;
-    if (units >= 32) return 8;
+    if (units >= 256) return 32;
+    if (units >= 128) return 16;
+    if (units >= 64) return 8;
     return 4;
 }
 
-#define EF_LPR_DISPATCH(KERNEL, VEC, LPR, GRID, ...)                                     \
-    do {                                                                                 \
-        if (LPR == 32) KERNEL<VEC, 32><<<GRID, 256, 0, st>>>(__VA_ARGS__);               \
-        else if (LPR == 16) KERNEL<VEC, 16><<<GRID, 256, 0, st>>>(__VA_ARGS__);          \
-        else if (LPR == 8) KERNEL<VEC, 8><<<GRID, 256, 0, st>>>(__VA_ARGS__);            \
-        else KERNEL<VEC, 4><<<GRID, 256, 0, st>>>(__VA_ARGS__);                          \
+#define EF_LPR_DISPATCH(KERNEL, VEC, LPR, GRID, ...)                                       \
+    do {                                                                                    \
+        if (LPR == 32) KERNEL<VEC, 32><<<GRID, kGemvThreads, 0, st>>>(__VA_ARGS__);         \
+        else if (LPR == 16) KERNEL<VEC, 16><<<GRID, kGemvThreads, 0, st>>>(__VA_ARGS__);    \
+        else if (LPR == 8) KERNEL<VEC, 8><<<GRID, kGemvThreads, 0, st>>>(__VA_ARGS__);      \
+        else KERNEL<VEC, 4><<<GRID, kGemvThreads, 0, st>>>(__VA_ARGS__);                    \
     } while (0)
 
 __global__ void k_root_diag(int m, const double* a, const double* b, const double* r,
@@ -463,35 +486,34 @@ void upward_hdiff(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     ++g_kernel_launches;
 }
 
+inline unsigned gemv_blocks(long long threads) {
+    return unsigned(std::max(1LL, (threads + kGemvThreads - 1) / kGemvThreads));
+}
+
 void upward_w(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     const long long rows = (long long)nitems * 4 * s;
     const bool vec = (s % 2 == 0);
     const int lpr = pick_lpr(4 * s, vec);
-    const unsigned blocks = unsigned((rows * lpr + 255) / 256);
-    if (vec) EF_LPR_DISPATCH(k_gemv_w, true, lpr, blocks, items, s, rows);
-    else EF_LPR_DISPATCH(k_gemv_w, false, lpr, blocks, items, s, rows);
+    if (vec) EF_LPR_DISPATCH(k_gemv_w, true, lpr, gemv_blocks(rows * lpr), items, s, rows);
+    else EF_LPR_DISPATCH(k_gemv_w, false, lpr, gemv_blocks(rows * lpr), items, s, rows);
     ++g_kernel_launches;
 }
 
 void upward_h(cudaStream_t st, const MergeItem* items, int nitems, int s) {
     const long long rows = (long long)nitems * 8 * s;
     const bool vec = (s % 2 == 0);
-    const int lpr = pick_lpr(s, vec);
-    const unsigned blocks = unsigned((rows * lpr + 255) / 256);
-    if (vec) EF_LPR_DISPATCH(k_gemv_h, true, lpr, blocks, items, s, rows);
-    else EF_LPR_DISPATCH(k_gemv_h, false, lpr, blocks, items, s, rows);
+    const int lpr = pick_lpr(2 * s, vec);
+    if (vec) EF_LPR_DISPATCH(k_gemv_h, true, lpr, gemv_blocks(rows * lpr), items, s, rows);
+    else EF_LPR_DISPATCH(k_gemv_h, false, lpr, gemv_blocks(rows * lpr), items, s, rows);
     ++g_kernel_launches;
 }
 
+// the grid also covers the exterior copy (one element per thread)
 void downward(cudaStream_t st, const MergeItem* items, int nitems, int s, int add_w) {
     const long long rows = (long long)nitems * 4 * s;
     const bool vec = (s % 2 == 0);
     const int lpr = pick_lpr(8 * s, vec);
-    // enough CTAs for the rows and for the exterior copy (one element per thread)
-    long long blocks = (rows * lpr + 255) / 256;
-    const long long eblocks = ((long long)nitems * 8 * s + 255) / 256;
-    if (eblocks > blocks) blocks = eblocks;
-    const unsigned nb = unsigned(blocks);
+    const unsigned nb = gemv_blocks(std::max(rows * lpr, (long long)nitems * 8 * s));
     if (vec) EF_LPR_DISPATCH(k_gemv_down, true, lpr, nb, items, s, rows, nitems, add_w);
     else EF_LPR_DISPATCH(k_gemv_down, false, lpr, nb, items, s, rows, nitems, add_w);
     ++g_kernel_launches;
