@@ -244,10 +244,20 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
     }
     __syncthreads();
 
-    auto issue = [&](int v, int st) {
-        const int unit = v / cpu, ch = v - unit * cpu;
-        const MxTile t = mx_tile<KIND>(items, s, B, rt, tpi, first_tile + unit * tile_step);
-        const int c = cbase + ch;
+    // the issuing side walks the work list in order: its tile is looked up once per unit and its
+    // chunk advances by a counter (no divisions, no item reads on the way to each copy)
+    int iss_unit = 0, iss_ch = 0;
+    MxTile iss_t = {};
+    if (total > 0) iss_t = mx_tile<KIND>(items, s, B, rt, tpi, first_tile);
+    auto issue = [&](int st) {
+        if (iss_ch == cpu) {
+            iss_ch = 0;
+            ++iss_unit;
+            iss_t = mx_tile<KIND>(items, s, B, rt, tpi, first_tile + iss_unit * tile_step);
+        }
+        const MxTile& t = iss_t;
+        const int c = cbase + iss_ch;
+        ++iss_ch;
         if (tid == 0)
             tma_load_tile(&tmA, &full[st], As0 + st * astage, c * kKC, t.item * rows_item + t.row0, tile_bytes);
         const int k0 = c * kKC;
@@ -366,16 +376,21 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
 
     int issued = 0;
     for (int p = 0; p < kStages - 1; ++p) {
-        if (p < total) { issue(p, p); ++issued; }
+        if (p < total) { issue(p); ++issued; }
         cp_async_commit();
     }
     int fail_v = -1;
+    // consumer position: stage st of phase parity ph; the unit's chunk counter cch triggers the epilogue
+    int st = 0, cch = 0, cunit = 0;
+    unsigned ph = 0;
     for (int v = 0; v < total; ++v) {
-        const int st = v % kStages;
         cp_async_wait<kStages - 2>();
-        const bool ok = mbar_wait(&full[st], unsigned(v / kStages) & 1u);
+        const bool ok = mbar_wait(&full[st], ph);
         if (__syncthreads_or(!ok)) { fail_v = v; break; }
-        if (v + kStages - 1 < total) { issue(v + kStages - 1, (v + kStages - 1) % kStages); ++issued; }
+        if (v + kStages - 1 < total) {
+            issue(st == 0 ? kStages - 1 : st - 1);
+            ++issued;
+        }
         cp_async_commit();
         const float* as = As0 + st * astage;
         const float* xs = Xs0 + st * (kKC * BN);
@@ -400,12 +415,18 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
                 }
             }
         }
-        if (ksplit == 1 && v % cpu == cpu - 1) {
-            epilogue(first_tile + (v / cpu) * tile_step);
+        if (ksplit == 1 && ++cch == cpu) {
+            epilogue(first_tile + cunit * tile_step);
+            cch = 0;
+            ++cunit;
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        }
+        if (++st == kStages) {
+            st = 0;
+            ph ^= 1u;
         }
     }
     cp_async_wait<0>();
