@@ -188,6 +188,8 @@ void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int 
 void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
 void mx_uncoarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
+// rows 0..7 of the 16 x 16 leaf eigenbasis (row-major, FP32) for the n = 16 leaf passes
+void mx_set_basis16(cudaStream_t st, const float* V);
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate);
 // Stencil constants of a leaf type for the residual: cx = 1/dx^2, cy = 1/dy^2 and lambda as signed

@@ -765,6 +765,177 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
     }
 }
 
+// ---- 16 x 16 leaves: register-resident sine transforms ---------------------------------------------
+// The eigenbasis V[i][k] = c_k sin(pi (k + 1)(i + 1/2) / 16) satisfies V[15 - i][k] = (-1)^k V[i][k],
+// so its rows 0..7 (in constant memory: every FMA takes its coefficient as the constant operand,
+// with no shared-memory traffic) define the whole basis, and each 16-point transform is 128 FMAs on
+// even/odd combinations instead of 256.
+__constant__ float c_mxV16[8 * 16];
+
+// Analysis X[k] = sum_j V[j][k] x[j] over the spatial index: out(k, X[k]) for the even modes (from
+// x[j] + x[15 - j]), then the odd ones (from x[j] - x[15 - j]), so that outputs leave as they are made
+template <class Out>
+__device__ __forceinline__ void mx_dst16_fwd(const float (&x)[16], Out&& out) {
+    float P[8], M[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        P[j] = x[j] + x[15 - j];
+        M[j] = x[j] - x[15 - j];
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+        float a = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a = fmaf(c_mxV16[j * 16 + k], P[j], a);
+        out(k, a);
+    }
+#pragma unroll
+    for (int k = 1; k < 16; k += 2) {
+        float a = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a = fmaf(c_mxV16[j * 16 + k], M[j], a);
+        out(k, a);
+    }
+}
+// Synthesis of the pair x[i], x[15 - i] (i < 8) from X: x[i] = sum_k V[i][k] X[k] = e + o, x[15 - i]
+// = e - o with e, o the sums over the even and odd modes
+__device__ __forceinline__ void mx_dst16_pair(const float (&X)[16], int i, float& lo, float& hi) {
+    float e = 0.f, o = 0.f;
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+        e = fmaf(c_mxV16[i * 16 + k], X[k], e);
+        o = fmaf(c_mxV16[i * 16 + k + 1], X[k + 1], o);
+    }
+    lo = e + o;
+    hi = e - o;
+}
+
+// FP32 leaf pass for n = 16: a 16-thread group per item (leaf, b), thread t owning row t (x index).
+//   A = F V (rows), G = Dinv o (V^T A) (columns), C = V G (columns), u = C V^T (rows)
+// Two transposes per item pass through a 16 x 17 shared buffer (conflict-free both ways) under
+// __syncwarp only: an item never leaves its half-warp.  NEUMANN writes h32 = DtN(0, q) from the
+// edges of u; SOLVE adds the solution of (g32, q) to the FP64 state u64 (or stores it when
+// accumulate is 0).
+template <int MODE>
+__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
+                                                   const MixLeaf* __restrict__ leaves, int L, int B,
+                                                   const float* __restrict__ q, double* __restrict__ u64,
+                                                   int accumulate) {
+    __shared__ float buf[16 * 272];
+    __shared__ float Vs[16 * 17];
+    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
+    const long long item = (long long)blockIdx.x * 16 + slot;
+    const bool act = item < (long long)L * B;
+    const int leaf = act ? int(item / B) : 0;
+    const int b = act ? int(item - (long long)leaf * B) : 0;
+    float* bf = buf + slot * 272;
+    if (MODE == LEAF_NEUMANN) {
+        // the full basis, for the edge sums whose basis row depends on the thread
+        const int i = tid >> 4, k = tid & 15;
+        const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
+        __syncthreads();
+    }
+    const int type = leaves[leaf].type;
+    float x[16], X[16];
+    // (1) row t of the load; the solve adds the Dirichlet terms -2 (cx g_x + cy g_y) of the edge cells
+    if (act) {
+        const float4* qr = reinterpret_cast<const float4*>(q + ((long long)b * L + leaf) * 256 + t * 16);
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4) {
+            const float4 v = qr[c4];
+            x[4 * c4] = v.x; x[4 * c4 + 1] = v.y; x[4 * c4 + 2] = v.z; x[4 * c4 + 3] = v.w;
+        }
+        if (MODE == LEAF_SOLVE) {
+            const float* g = leaves[leaf].g32 + b;
+            const float dx = types[type].dx, dy = types[type].dy;
+            const float cx = 1.0f / (dx * dx), cy = 1.0f / (dy * dy);
+            const float gs = g[(long long)(2 * 16 + t) * B], gn = g[(long long)(3 * 16 + t) * B];
+            if (t == 0 || t == 15) {
+                const long long side = t == 0 ? 0 : 16;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float acc = cx * g[(side + j) * B];
+                    if (j == 0) acc += cy * gs;
+                    else if (j == 15) acc += cy * gn;
+                    x[j] += -2.0f * acc;
+                }
+            } else {
+                x[0] += -2.0f * (cy * gs);
+                x[15] += -2.0f * (cy * gn);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) x[j] = 0.f;
+    }
+    // (2) A[t][l] = sum_j F[t][j] V[j][l]; transpose: this thread takes column l = t
+    mx_dst16_fwd(x, [&](int l, float v) { bf[t * 17 + l] = v; });
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = bf[i * 17 + t];
+    // (3) G[k][t] = Dinv[k][t] sum_i V[i][k] A[i][t]
+    {
+        const float* Dinv = types[type].Dinv + t;
+        mx_dst16_fwd(x, [&](int k, float v) { X[k] = v * __ldg(Dinv + k * 16); });
+    }
+    // (4) C[i][t] = sum_k V[i][k] G[k][t]; transpose back: buffer row t holds column t of C
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        float lo, hi;
+        mx_dst16_pair(X, i, lo, hi);
+        bf[t * 17 + i] = lo;
+        bf[t * 17 + 15 - i] = hi;
+    }
+    __syncwarp();
+    if (MODE == LEAF_SOLVE) {
+        // (5) u[t][j] = sum_l C[t][l] V[j][l], written as the pairs (2c, 2c + 1) and (14 - 2c, 15 - 2c)
+#pragma unroll
+        for (int l = 0; l < 16; ++l) X[l] = bf[l * 17 + t];
+        double2* row = reinterpret_cast<double2*>(u64 + ((long long)b * L + leaf) * 256 + t * 16);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float a0, a15, a1, a14;
+            mx_dst16_pair(X, 2 * c, a0, a15);
+            mx_dst16_pair(X, 2 * c + 1, a1, a14);
+            if (act) {
+                double2 v = make_double2(f2d_bits(a0), f2d_bits(a1));
+                double2 w = make_double2(f2d_bits(a14), f2d_bits(a15));
+                if (accumulate) {
+                    const double2 ov = row[c], ow = row[7 - c];
+                    v.x += ov.x; v.y += ov.y;
+                    w.x += ow.x; w.y += ow.y;
+                }
+                row[c] = v;
+                row[7 - c] = w;
+            }
+        }
+    } else {
+        // (5) edge values: S/N at i = t from row t of C, W/E at j = t from rows 0 and 15 of C
+        float e = 0.f, o = 0.f, uw = 0.f, ue = 0.f;
+#pragma unroll
+        for (int l = 0; l < 16; l += 2) {
+            e = fmaf(c_mxV16[l], bf[l * 17 + t], e);
+            o = fmaf(c_mxV16[l + 1], bf[(l + 1) * 17 + t], o);
+        }
+#pragma unroll
+        for (int l = 0; l < 16; ++l) {
+            const float v = Vs[t * 17 + l];
+            uw = fmaf(bf[l * 17], v, uw);
+            ue = fmaf(bf[l * 17 + 15], v, ue);
+        }
+        if (act) {
+            const float dtn_x = 2.0f / types[type].dx, dtn_y = 2.0f / types[type].dy;
+            float* h = leaves[leaf].h32 + b;
+            h[(long long)(0 * 16 + t) * B] = dtn_x * uw;
+            h[(long long)(1 * 16 + t) * B] = -dtn_x * ue;
+            h[(long long)(2 * 16 + t) * B] = dtn_y * (e + o);
+            h[(long long)(3 * 16 + t) * B] = -dtn_y * (e - o);
+        }
+    }
+}
+
 // Leaf residual r = f - (cx (u_W + u_E) + cy (u_S + u_N) + cc u_C) (stored as the next pass's FP32
 // load), where a neighbour across the patch edge is the ghost value 2g - u_C of the Dirichlet face
 // data (the discrete operator of FiniteVolumeSolver.cpp:27-223), and the leaf's edge fluxes
@@ -1356,8 +1527,22 @@ void mx_leaf32_mode(cudaStream_t st, unsigned grid, unsigned threads, size_t sme
     else mx_leaf32_launch<MODE, 0>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
 }
 
+void mx_set_basis16(cudaStream_t st, const float* V) {
+    // rows 0..7 of the 16 x 16 basis (row-major); the copy is ordered on st
+    if (cudaMemcpyToSymbolAsync(c_mxV16, V, sizeof(float) * 8 * 16, 0, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        throw std::runtime_error("mixed solver: leaf basis upload failed");
+}
+
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate) {
+    if (n == 16) {
+        const unsigned grid16 = unsigned(((long long)L * B + 15) / 16);
+        if (mode == LEAF_NEUMANN) k_mx_leaf16<LEAF_NEUMANN><<<grid16, 256, 0, st>>>(types, leaves, L, B, q, u64, 0);
+        else k_mx_leaf16<LEAF_SOLVE><<<grid16, 256, 0, st>>>(types, leaves, L, B, q, u64, accumulate);
+        ++g_kernel_launches;
+        return;
+    }
     // groups of (n/4)^2 threads, two items per group, up to 256 threads per block
     const int nb = n / 4, tpi = nb * nb, groups = tpi >= 256 ? 1 : 256 / tpi, ipc = 2 * groups;
     const size_t smem = (size_t(2) * n * n + size_t(ipc) * (n * n + 16)) * sizeof(float);

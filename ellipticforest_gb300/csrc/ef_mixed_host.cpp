@@ -224,6 +224,7 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
                                 tab + 2 * nn * t + nn};
         }
         ck(upload_sync(st_, d_types32_, t32.data(), t32.size() * sizeof(LeafType32)), "types32");
+        if (n == 16) mx_set_basis16(st_, Vf.data());  // V depends on n only: the last type's copy serves all
         std::vector<MixCoef> co(hps.types_.size());
         for (size_t t = 0; t < co.size(); ++t) {
             const double dx = hps.types_[t].dx, dy = hps.types_[t].dy;
