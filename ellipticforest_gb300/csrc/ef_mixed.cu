@@ -890,25 +890,31 @@ __global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(c
     }
     __syncwarp();
     if (MODE == LEAF_SOLVE) {
-        // (5) u[t][j] = sum_l C[t][l] V[j][l], written as the pairs (2c, 2c + 1) and (14 - 2c, 15 - 2c)
+        // (5) u[t][j] = sum_l C[t][l] V[j][l], staged in the buffer (row t)
 #pragma unroll
         for (int l = 0; l < 16; ++l) X[l] = bf[l * 17 + t];
-        double2* row = reinterpret_cast<double2*>(u64 + ((long long)b * L + leaf) * 256 + t * 16);
+        __syncwarp();
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            float a0, a15, a1, a14;
-            mx_dst16_pair(X, 2 * c, a0, a15);
-            mx_dst16_pair(X, 2 * c + 1, a1, a14);
-            if (act) {
-                double2 v = make_double2(f2d_bits(a0), f2d_bits(a1));
-                double2 w = make_double2(f2d_bits(a14), f2d_bits(a15));
+        for (int i = 0; i < 8; ++i) {
+            float lo, hi;
+            mx_dst16_pair(X, i, lo, hi);
+            bf[t * 17 + i] = lo;
+            bf[t * 17 + 15 - i] = hi;
+        }
+        __syncwarp();
+        // (6) the FP64 state, coalesced: thread t takes the value pairs 2 (t + 16 m), m < 8
+        if (act) {
+            double2* st = reinterpret_cast<double2*>(u64 + ((long long)b * L + leaf) * 256);
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+                const int e2 = t + 16 * m, i = e2 >> 3, j = (e2 & 7) * 2;
+                double2 v = make_double2(f2d_bits(bf[i * 17 + j]), f2d_bits(bf[i * 17 + j + 1]));
                 if (accumulate) {
-                    const double2 ov = row[c], ow = row[7 - c];
-                    v.x += ov.x; v.y += ov.y;
-                    w.x += ow.x; w.y += ow.y;
+                    const double2 o = st[e2];
+                    v.x += o.x;
+                    v.y += o.y;
                 }
-                row[c] = v;
-                row[7 - c] = w;
+                st[e2] = v;
             }
         }
     } else {
