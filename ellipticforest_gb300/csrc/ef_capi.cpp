@@ -130,6 +130,7 @@ int run_single_patch(int solver_type, int n, double xl, double xu, double yl, do
     if (e == cudaSuccess)
         e = cudaMemcpy(ditems, items.data(), nitems * sizeof(efgb::LeafItem), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
+        if (n == 16) efgb::leaf_set_basis16(0);
         efgb::leaf_eigen(0, mode, dty, ditems, nitems, n);
         e = cudaGetLastError();
     }

@@ -372,6 +372,7 @@ void Hps::upload_tables() {
         }
         check(upload_sync(st_, d_types_, hty.data(), hty.size() * sizeof(LeafType)),
               "upload types");
+        if (n_ == 16) leaf_set_basis16(st_);
     }
 
     std::vector<LeafItem> items;

@@ -10,6 +10,10 @@
 //     U = V [ (V^T F V) ./ (mu_x[k] + mu_y[l] + lambda) ] V^T.
 // The Neumann data follow FiniteVolumeSolver.cpp:296-353: h_W = (2/dx)(u_W - g_W),
 // h_E = -(2/dx)(u_E - g_E), h_S = (2/dy)(u_S - g_S), h_N = -(2/dy)(u_N - g_N).
+#include <atomic>
+#include <cmath>
+#include <stdexcept>
+
 #include "ef_kernels.cuh"
 
 namespace efgb {
@@ -110,6 +114,170 @@ __global__ void __launch_bounds__(256) k_leaf_eigen(const LeafType* __restrict__
     }
 }
 
+// ---- 16 x 16 leaves: register-resident sine transforms in FP64 ---------------------------------------
+// V[15 - i][k] = (-1)^k V[i][k], and for the odd modes k = 2m + 1 also V[7 - i][k] = (-1)^m V[i][k]
+// (those columns are the 8-point basis), so rows 0..7 of V (constant memory: the FMA's constant
+// operand) define the basis and a 16-point transform costs 96 FMAs and 24 additions instead of 256
+// FMAs: the FP64 pipe (about 2 FMAs per clock per SM) bounds these passes.
+__constant__ double c_V16d[8 * 16];
+
+// X[k] = sum_j V[j][k] x[j]; out(k, X[k])
+template <class Out>
+__device__ __forceinline__ void dst16d_fwd(const double (&x)[16], Out&& out) {
+    double P[8], M[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        P[j] = x[j] + x[15 - j];
+        M[j] = x[j] - x[15 - j];
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+        double a = 0.0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a = fma(c_V16d[j * 16 + k], P[j], a);
+        out(k, a);
+    }
+    double Q[4], R[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        Q[j] = M[j] + M[7 - j];
+        R[j] = M[j] - M[7 - j];
+    }
+#pragma unroll
+    for (int k = 1; k < 16; k += 2) {
+        const bool modd = ((k >> 1) & 1) != 0;  // k = 2m + 1 with m odd
+        double a = 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) a = fma(c_V16d[j * 16 + k], modd ? R[j] : Q[j], a);
+        out(k, a);
+    }
+}
+// x[i], x[15 - i], x[7 - i], x[8 + i] (i < 4) of x = V X
+__device__ __forceinline__ void dst16d_quad(const double (&X)[16], int i, double& a, double& b, double& c,
+                                            double& d) {
+    double ei = 0.0, e7 = 0.0, oe = 0.0, oo = 0.0;
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+        ei = fma(c_V16d[i * 16 + k], X[k], ei);
+        e7 = fma(c_V16d[(7 - i) * 16 + k], X[k], e7);
+    }
+#pragma unroll
+    for (int k = 1; k < 16; k += 4) {
+        oe = fma(c_V16d[i * 16 + k], X[k], oe);
+        oo = fma(c_V16d[i * 16 + k + 2], X[k + 2], oo);
+    }
+    const double oi = oe + oo, o7 = oe - oo;
+    a = ei + oi;
+    b = ei - oi;
+    c = e7 + o7;
+    d = e7 - o7;
+}
+
+// Plain FP64 leaf pass for n = 16 (NEUMANN, SOLVE): 16 threads per item, thread t owning row t;
+// the same contractions as k_leaf_eigen, U = V [(V^T F V) ./ D] V^T, with two transposes through
+// a 16 x 17 shared buffer under __syncwarp.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_leaf16d(const LeafType* __restrict__ types,
+                                                 const LeafItem* __restrict__ items, int nitems) {
+    __shared__ double buf[16 * 272];
+    __shared__ double Vs[16 * 17];
+    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
+    const int idx = blockIdx.x * 16 + slot;
+    const bool act = idx < nitems;
+    const LeafItem it = items[act ? idx : 0];
+    const LeafType ty = types[it.type];
+    double* bf = buf + slot * 272;
+    if (MODE == LEAF_NEUMANN) {
+        const int i = tid >> 4, k = tid & 15;
+        const double v = c_V16d[(i < 8 ? i : 15 - i) * 16 + k];
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
+        __syncthreads();
+    }
+    double x[16], X[16];
+    // (1) row t of f; the solve adds -2 (cx g_x + cy g_y) on the edge cells
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = (act && it.f != nullptr) ? it.f[t * 16 + j] : 0.0;
+    if (MODE == LEAF_SOLVE && act && it.g != nullptr) {
+        const double cx = 1.0 / (ty.dx * ty.dx), cy = 1.0 / (ty.dy * ty.dy);
+        const double gs = it.g[2 * 16 + t], gn = it.g[3 * 16 + t];
+        if (t == 0 || t == 15) {
+            const int side = t == 0 ? 0 : 16;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                double acc = cx * it.g[side + j];
+                if (j == 0) acc = acc + cy * gs;
+                else if (j == 15) acc = acc + cy * gn;
+                x[j] += -2.0 * acc;
+            }
+        } else {
+            x[0] += -2.0 * (cy * gs);
+            x[15] += -2.0 * (cy * gn);
+        }
+    }
+    // (2) A = F V by rows; transpose
+    dst16d_fwd(x, [&](int l, double v) { bf[t * 17 + l] = v; });
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) x[i] = bf[i * 17 + t];
+    // (3) G[k][t] = Dinv[k][t] (V^T A)[k][t]
+    dst16d_fwd(x, [&](int k, double v) { X[k] = v * __ldg(ty.Dinv + k * 16 + t); });
+    // (4) C = V G by columns; transpose back (buffer row t = column t of C)
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        double a, b, c, d;
+        dst16d_quad(X, i, a, b, c, d);
+        bf[t * 17 + i] = a;
+        bf[t * 17 + 15 - i] = b;
+        bf[t * 17 + 7 - i] = c;
+        bf[t * 17 + 8 + i] = d;
+    }
+    __syncwarp();
+    if (MODE == LEAF_SOLVE) {
+        // (5) U[t][j] = sum_l C[t][l] V[j][l], staged, then written coalesced
+#pragma unroll
+        for (int l = 0; l < 16; ++l) X[l] = bf[l * 17 + t];
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            double a, b, c, d;
+            dst16d_quad(X, i, a, b, c, d);
+            bf[t * 17 + i] = a;
+            bf[t * 17 + 15 - i] = b;
+            bf[t * 17 + 7 - i] = c;
+            bf[t * 17 + 8 + i] = d;
+        }
+        __syncwarp();
+        if (act)
+#pragma unroll
+            for (int m = 0; m < 16; ++m) {
+                const int e = t + 16 * m;
+                it.out[e] = bf[(e >> 4) * 17 + (e & 15)];
+            }
+    } else {
+        // (5) edge values: S/N at i = t (row t of C), W/E at j = t (rows 0 and 15 of C)
+        double e = 0.0, o = 0.0, uw = 0.0, ue = 0.0;
+#pragma unroll
+        for (int l = 0; l < 16; l += 2) {
+            e = fma(c_V16d[l], bf[l * 17 + t], e);
+            o = fma(c_V16d[l + 1], bf[(l + 1) * 17 + t], o);
+        }
+#pragma unroll
+        for (int l = 0; l < 16; ++l) {
+            const double v = Vs[t * 17 + l];
+            uw = fma(bf[l * 17], v, uw);
+            ue = fma(bf[l * 17 + 15], v, ue);
+        }
+        if (act) {
+            const double dtn_x = 2.0 / ty.dx, dtn_y = 2.0 / ty.dy;
+            it.out[0 * 16 + t] = dtn_x * uw;
+            it.out[1 * 16 + t] = (-dtn_x) * ue;
+            it.out[2 * 16 + t] = dtn_y * (e + o);
+            it.out[3 * 16 + t] = (-dtn_y) * (e - o);
+        }
+    }
+}
+
 template <int MODE>
 void launch_leaf(cudaStream_t st, const LeafType* types, const LeafItem* items, int nitems, int nmax) {
     const size_t smem = size_t(3) * nmax * nmax * sizeof(double);
@@ -124,9 +292,31 @@ void launch_leaf(cudaStream_t st, const LeafType* types, const LeafItem* items, 
 
 }  // namespace
 
+void leaf_set_basis16(cudaStream_t st) {
+    static std::atomic<bool> done{false};
+    if (done.load()) return;
+    double V[8 * 16];
+    for (int i = 0; i < 8; ++i)
+        for (int k = 0; k < 16; ++k) {
+            const double c = (k == 15) ? std::sqrt(1.0 / 16) : std::sqrt(2.0 / 16);
+            V[i * 16 + k] = c * std::sin(M_PI * (k + 1) * (i + 0.5) / 16);
+        }
+    if (cudaMemcpyToSymbolAsync(c_V16d, V, sizeof(V), 0, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        throw std::runtime_error("leaf basis upload failed");
+    done.store(true);
+}
+
 void leaf_eigen(cudaStream_t st, int mode, const LeafType* types, const LeafItem* items, int nitems,
                 int nmax) {
     if (nitems <= 0) return;
+    if (nmax == 16 && (mode == LEAF_NEUMANN || mode == LEAF_SOLVE)) {
+        const unsigned grid = unsigned((nitems + 15) / 16);
+        if (mode == LEAF_NEUMANN) k_leaf16d<LEAF_NEUMANN><<<grid, 256, 0, st>>>(types, items, nitems);
+        else k_leaf16d<LEAF_SOLVE><<<grid, 256, 0, st>>>(types, items, nitems);
+        ++g_kernel_launches;
+        return;
+    }
     if (mode == LEAF_DTN_COLUMN) launch_leaf<LEAF_DTN_COLUMN>(st, types, items, nitems, nmax);
     else if (mode == LEAF_NEUMANN) launch_leaf<LEAF_NEUMANN>(st, types, items, nitems, nmax);
     else if (mode == LEAF_SOLVE) launch_leaf<LEAF_SOLVE>(st, types, items, nitems, nmax);
