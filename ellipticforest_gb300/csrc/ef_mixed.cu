@@ -198,7 +198,7 @@ __device__ __forceinline__ MxTile mx_tile(const MixItem* __restrict__ items, int
 // one tile; otherwise the CTA strides over tiles (persistent), so the TMA pipeline runs on across
 // tile boundaries and each epilogue overlaps the next tile's loads.
 template <int BN, int KIND>
-__global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __grid_constant__ CUtensorMap tmA,
                                                  const MixItem* __restrict__ items, int s, int B, int rt,
                                                  int ksplit, int ntiles, int* __restrict__ err) {
     constexpr int TXN = BN / 4;
@@ -294,21 +294,60 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
             // of the 8s exterior rows, one warp per row (float4 along the batch when B % 4 == 0)
             const int rows = 8 * s, per = (rows + tpi - 1) / tpi;
             const int p0 = t.tl * per, p1 = min(rows, p0 + per);
-            const int warp = tid >> 5, lane = tid & 31, nw = (nt + 31) >> 5;
-            for (int p = p0 + warp; p < p1; p += nw) {
-                int c, q;
-                mx_ext_map(p, s, c, q);
-                const float* src = it.gf + (long long)p * B;
-                float* dst = it.gc[c] + (long long)q * B;
-                if (vecx) {
-                    for (int b4 = lane; b4 < (B >> 2); b4 += 32)
-                        reinterpret_cast<float4*>(dst)[b4] = reinterpret_cast<const float4*>(src)[b4];
-                } else {
+            if (vecx) {
+                // (row, float4) pairs over all threads, four loads in flight before their stores
+                const int w4 = B >> 2, tot = (p1 - p0) * w4;
+                for (int e0 = tid; e0 < tot; e0 += 4 * nt) {
+                    float4 v[4];
+                    float4* d[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int e = e0 + u * nt;
+                        d[u] = nullptr;
+                        if (e < tot) {
+                            const int p = p0 + e / w4, b4 = e - (e / w4) * w4;
+                            int c, q;
+                            mx_ext_map(p, s, c, q);
+                            v[u] = reinterpret_cast<const float4*>(it.gf + (long long)p * B)[b4];
+                            d[u] = reinterpret_cast<float4*>(it.gc[c] + (long long)q * B) + b4;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (d[u]) *d[u] = v[u];
+                }
+            } else {
+                const int warp = tid >> 5, lane = tid & 31, nw = (nt + 31) >> 5;
+                for (int p = p0 + warp; p < p1; p += nw) {
+                    int c, q;
+                    mx_ext_map(p, s, c, q);
+                    const float* src = it.gf + (long long)p * B;
+                    float* dst = it.gc[c] + (long long)q * B;
                     for (int bb = lane; bb < B; bb += 32) dst[bb] = src[bb];
                 }
             }
         }
         const int bq = b0 + 4 * tx;
+        // the rows' epilogue operands (h_ext for H; w and u_Gamma for DOWN) are all loaded before
+        // any store: the compiler cannot move a load above a store to another array of the item
+        float4 pre4[4];
+        double2 preu0[4], preu1[4];
+        if (vecx && bq < B && KIND != MX_W) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = t.row0 + ty + i * rq;
+                const long long rb = (long long)r * B + bq;
+                if (KIND == MX_H) {
+                    int c, q;
+                    mx_ext_map(r, s, c, q);
+                    pre4[i] = *reinterpret_cast<const float4*>(it.hc[c] + (long long)q * B + bq);
+                } else {
+                    pre4[i] = *reinterpret_cast<const float4*>(it.w + rb);
+                    preu0[i] = reinterpret_cast<const double2*>(it.uG + rb)[0];
+                    preu1[i] = reinterpret_cast<const double2*>(it.uG + rb)[1];
+                }
+            }
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int r = t.row0 + ty + i * rq;
@@ -323,7 +362,7 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
                 mx_ext_map(r, s, c, q);
                 const float* hp = it.hc[c] + (long long)q * B + bq;
                 if (vecx && bq < B) {
-                    const float4 hv = *reinterpret_cast<const float4*>(hp);
+                    const float4 hv = pre4[i];
                     v[0] += hv.x; v[1] += hv.y; v[2] += hv.z; v[3] += hv.w;
                 } else {
 #pragma unroll
@@ -335,7 +374,7 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
                 const int I = r / s, o = r - (r / s) * s;
                 const float* wp = it.w + rb;
                 if (vecx && bq < B) {
-                    const float4 wv = *reinterpret_cast<const float4*>(wp);
+                    const float4 wv = pre4[i];
                     v[0] += wv.x; v[1] += wv.y; v[2] += wv.z; v[3] += wv.w;
                 } else {
 #pragma unroll
@@ -346,7 +385,7 @@ __global__ void __launch_bounds__(128) k_mx_gemm(const __grid_constant__ CUtenso
                 dst1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + bq;
                 double* ug = it.uG + rb;
                 if (vecx && bq < B) {
-                    double2 u0 = reinterpret_cast<double2*>(ug)[0], u1 = reinterpret_cast<double2*>(ug)[1];
+                    double2 u0 = preu0[i], u1 = preu1[i];
                     u0.x += f2d_bits(v[0]); u0.y += f2d_bits(v[1]);
                     u1.x += f2d_bits(v[2]); u1.y += f2d_bits(v[3]);
                     reinterpret_cast<double2*>(ug)[0] = u0;
