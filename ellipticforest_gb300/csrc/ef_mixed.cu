@@ -87,6 +87,23 @@ __global__ void k_mx_hdiff(const MixItem* __restrict__ items, int s, int B) {
     }
 }
 
+// the same with four requests per thread (B % 4 == 0): three float4 loads in flight, a quarter of
+// the threads and blocks
+__global__ void k_mx_hdiff4(const MixItem* __restrict__ items, int s, int B) {
+    const MixItem& it = items[blockIdx.y];
+    const int B4 = B >> 2, tot = 4 * s * B4;
+    for (int e4 = blockIdx.x * blockDim.x + threadIdx.x; e4 < tot; e4 += gridDim.x * blockDim.x) {
+        const int r = e4 / B4, b = (e4 - r * B4) * 4;
+        const int I = r / s, o = r - I * s;
+        const long long rb = (long long)r * B + b;
+        const float4 hu = *reinterpret_cast<const float4*>(it.hc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + b);
+        const float4 hl = *reinterpret_cast<const float4*>(it.hc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + b);
+        const float4 m = *reinterpret_cast<const float4*>(it.m + rb);
+        *reinterpret_cast<float4*>(it.hd + rb) =
+            make_float4(hu.x - hl.x - m.x, hu.y - hl.y - m.y, hu.z - hl.z - m.z, hu.w - hl.w - m.w);
+    }
+}
+
 // ---- FP32 node GEMMs: Y[rows][B] = A[rows][K] X[K][B] over all nodes of one group -----------------
 //
 // The operators of a group are stored back to back (one row-major matrix of cnt * rows_item rows)
@@ -522,6 +539,35 @@ __global__ void k_mx_scatter64(const MixItem* __restrict__ items, int s, int B) 
     }
 }
 
+// the same with four requests per thread (B % 4 == 0): 32-byte loads and stores, every load of a
+// thread issued before its stores
+__global__ void k_mx_scatter64_4(const MixItem* __restrict__ items, int s, int B) {
+    const MixItem& it = items[blockIdx.y];
+    const int m4 = 4 * s, m8 = 8 * s, B4 = B >> 2;
+    for (int e4 = blockIdx.x * blockDim.x + threadIdx.x; e4 < (m8 + m4) * B4; e4 += gridDim.x * blockDim.x) {
+        const int row = e4 / B4, b = (e4 - row * B4) * 4;
+        if (row < m8) {
+            int c, q;
+            mx_ext_map(row, s, c, q);
+            const double2* src = reinterpret_cast<const double2*>(it.gf64 + (long long)row * B + b);
+            const double2 v0 = src[0], v1 = src[1];
+            double2* dst = reinterpret_cast<double2*>(it.gc64[c] + (long long)q * B + b);
+            dst[0] = v0;
+            dst[1] = v1;
+        } else {
+            const int r = row - m8, I = r / s, o = r - (r / s) * s;
+            const double2* src = reinterpret_cast<const double2*>(it.uG + (long long)r * B + b);
+            const double2 v0 = src[0], v1 = src[1];
+            double2* d0 = reinterpret_cast<double2*>(it.gc64[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + b);
+            double2* d1 = reinterpret_cast<double2*>(it.gc64[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + b);
+            d0[0] = v0;
+            d0[1] = v1;
+            d1[0] = v0;
+            d1[1] = v1;
+        }
+    }
+}
+
 // interface flux mismatch (becomes the next pass's jump) and the node's boundary flux
 __global__ void k_mx_flux_up(const MixItem* __restrict__ items, int s, int B) {
     const MixItem& it = items[blockIdx.y];
@@ -539,6 +585,32 @@ __global__ void k_mx_flux_up(const MixItem* __restrict__ items, int s, int B) {
             const double ml = it.hc64[mx_lower_child(I)][mx_q_lower(I, o, s) * B + b];
             const double mu = it.hc64[mx_upper_child(I)][mx_q_upper(I, o, s) * B + b];
             it.mout[f] = d2f_rn_bits(ml - mu);
+        }
+    }
+}
+
+// the same with four requests per thread (B % 4 == 0)
+__global__ void k_mx_flux_up4(const MixItem* __restrict__ items, int s, int B) {
+    const MixItem& it = items[blockIdx.y];
+    const int m4 = 4 * s, m8 = 8 * s, B4 = B >> 2;
+    for (int e4 = blockIdx.x * blockDim.x + threadIdx.x; e4 < (m8 + m4) * B4; e4 += gridDim.x * blockDim.x) {
+        const int row = e4 / B4, b = (e4 - row * B4) * 4;
+        if (row < m8) {
+            int c, q;
+            mx_ext_map(row, s, c, q);
+            const double2* src = reinterpret_cast<const double2*>(it.hc64[c] + (long long)q * B + b);
+            const double2 v0 = src[0], v1 = src[1];
+            double2* dst = reinterpret_cast<double2*>(it.h64 + (long long)row * B + b);
+            dst[0] = v0;
+            dst[1] = v1;
+        } else {
+            const int r = row - m8, I = r / s, o = r - (r / s) * s;
+            const double2* pl = reinterpret_cast<const double2*>(it.hc64[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + b);
+            const double2* pu = reinterpret_cast<const double2*>(it.hc64[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + b);
+            const double2 l0 = pl[0], l1 = pl[1], u0 = pu[0], u1 = pu[1];
+            *reinterpret_cast<float4*>(it.mout + (long long)r * B + b) =
+                make_float4(d2f_rn_bits(l0.x - u0.x), d2f_rn_bits(l0.y - u0.y), d2f_rn_bits(l1.x - u1.x),
+                            d2f_rn_bits(l1.y - u1.y));
         }
     }
 }
@@ -1498,8 +1570,13 @@ void mx_gemm(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int n
 }  // namespace
 
 void mx_hdiff(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
-    dim3 g1(mx_grid(4LL * s * B), nitems);
-    k_mx_hdiff<<<g1, 256, 0, st>>>(items, s, B);
+    if (B % 4 == 0) {
+        dim3 g4(mx_grid((long long)s * B), nitems);
+        k_mx_hdiff4<<<g4, 256, 0, st>>>(items, s, B);
+    } else {
+        dim3 g1(mx_grid(4LL * s * B), nitems);
+        k_mx_hdiff<<<g1, 256, 0, st>>>(items, s, B);
+    }
     ++g_kernel_launches;
 }
 
@@ -1519,14 +1596,24 @@ int mx_gemm_max_split(int kind, int s) {
 }
 
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
-    dim3 g(mx_grid(12LL * s * B), nitems);
-    k_mx_scatter64<<<g, 256, 0, st>>>(items, s, B);
+    if (B % 4 == 0) {
+        dim3 g(mx_grid(3LL * s * B), nitems);
+        k_mx_scatter64_4<<<g, 256, 0, st>>>(items, s, B);
+    } else {
+        dim3 g(mx_grid(12LL * s * B), nitems);
+        k_mx_scatter64<<<g, 256, 0, st>>>(items, s, B);
+    }
     ++g_kernel_launches;
 }
 
 void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
-    dim3 g(mx_grid(12LL * s * B), nitems);
-    k_mx_flux_up<<<g, 256, 0, st>>>(items, s, B);
+    if (B % 4 == 0) {
+        dim3 g(mx_grid(3LL * s * B), nitems);
+        k_mx_flux_up4<<<g, 256, 0, st>>>(items, s, B);
+    } else {
+        dim3 g(mx_grid(12LL * s * B), nitems);
+        k_mx_flux_up<<<g, 256, 0, st>>>(items, s, B);
+    }
     ++g_kernel_launches;
 }
 
