@@ -1217,8 +1217,8 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     // (2) fixed-point u and ghosts
     if (act) {
         for (int e4 = lt; e4 < tpi; e4 += tpe) {
-            const double2 c01 = *reinterpret_cast<const double2*>(uu + 4 * e4);
-            const double2 c23 = *reinterpret_cast<const double2*>(uu + 4 * e4 + 2);
+            const double2 c01 = e4 == lt ? pu01 : *reinterpret_cast<const double2*>(uu + 4 * e4);
+            const double2 c23 = e4 == lt ? pu23 : *reinterpret_cast<const double2*>(uu + 4 * e4 + 2);
             reinterpret_cast<longlong2*>(tile + 4 * e4)[0] = make_longlong2(fx_from(c01.x, Eu), fx_from(c01.y, Eu));
             reinterpret_cast<longlong2*>(tile + 4 * e4)[1] = make_longlong2(fx_from(c23.x, Eu), fx_from(c23.y, Eu));
         }
@@ -1321,8 +1321,8 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
             } else {
                 diffs(e, c, sx, sy);
             }
-            const double2 f01 = *reinterpret_cast<const double2*>(ff + e);
-            const double2 f23 = *reinterpret_cast<const double2*>(ff + e + 2);
+            const double2 f01 = e4 == lt ? pf01 : *reinterpret_cast<const double2*>(ff + e);
+            const double2 f23 = e4 == lt ? pf23 : *reinterpret_cast<const double2*>(ff + e + 2);
             const double fv[4] = {f01.x, f01.y, f23.x, f23.y};
             float rr[4];
 #pragma unroll
