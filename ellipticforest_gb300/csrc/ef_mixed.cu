@@ -1688,6 +1688,66 @@ void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf
     ++g_kernel_launches;
 }
 
+// First residual for 16 x 16 leaves: 16 threads per item (16 items per block), each converting 16
+// cells read as coalesced 16-byte pairs; the item's ghost terms pass through shared memory under
+// __syncwarp.  The same arithmetic in the same order as k_mx_leaf_residual0.
+__global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __restrict__ coefs,
+                                                           const MixLeaf* __restrict__ leaves, int L, int B,
+                                                           const double* __restrict__ f, float* __restrict__ q,
+                                                           float* __restrict__ rleaf) {
+    __shared__ float gts[16 * 64];
+    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
+    const long long item = (long long)blockIdx.x * 16 + slot;
+    const bool act = item < (long long)L * B;
+    const int leaf = act ? int(item / B) : 0;
+    const int b = act ? int(item - (long long)leaf * B) : 0;
+    const MixLeaf lf = leaves[leaf];
+    const MixCoef cf = coefs[lf.type];
+    const long long base = ((long long)b * L + leaf) * 256;
+    const double2* f2 = reinterpret_cast<const double2*>(f + base);
+    // the cells' loads first, then the ghost data at position t of every side
+    double2 fv[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) fv[m] = act ? f2[t + 16 * m] : make_double2(0.0, 0.0);
+    double gv[4];
+#pragma unroll
+    for (int side = 0; side < 4; ++side) gv[side] = act ? lf.g64[(long long)(side * 16 + t) * B + b] : 0.0;
+    float* gt = gts + slot * 64;
+#pragma unroll
+    for (int side = 0; side < 4; ++side)
+        gt[side * 16 + t] = -2.0f * (side < 2 ? cf.cx32 : cf.cy32) * d2f_rn_bits(gv[side]);
+    if (act) {
+        // edge fluxes of the zero state, h = -+(2/d) g
+        double* h = lf.h64 + b;
+        h[(long long)(0 * 16 + t) * B] = -cf.dtn_x * gv[0];
+        h[(long long)(1 * 16 + t) * B] = cf.dtn_x * gv[1];
+        h[(long long)(2 * 16 + t) * B] = -cf.dtn_y * gv[2];
+        h[(long long)(3 * 16 + t) * B] = cf.dtn_y * gv[3];
+    }
+    __syncwarp();
+    float mx = 0.f;
+    float2* q2 = reinterpret_cast<float2*>(q + base);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int e2 = t + 16 * m, i = e2 >> 3, j = (e2 & 7) * 2;
+        float r0 = d2f_rn_bits(fv[m].x), r1 = d2f_rn_bits(fv[m].y);
+        if (i == 0) {
+            r0 += gt[j];
+            r1 += gt[j + 1];
+        } else if (i == 15) {
+            r0 += gt[16 + j];
+            r1 += gt[16 + j + 1];
+        }
+        if (j == 0) r0 += gt[32 + i];
+        if (j == 14) r1 += gt[48 + i];
+        mx = fmaxf(mx, fmaxf(fabsf(r0), fabsf(r1)));
+        if (act) q2[e2] = make_float2(r0, r1);
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (rleaf && act && t == 0) rleaf[(long long)b * L + leaf] = mx;
+}
+
 template <int FORM>
 void mx_residual_launch(cudaStream_t st, unsigned grid, unsigned threads, size_t smem, const MixCoef* coefs,
                         const MixLeaf* leaves, int L, int B, int n, int ipc, const double* f, const double* u64,
@@ -1714,7 +1774,7 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
     if (zero_state) {
         const size_t smem0 = size_t(ipc) * 4 * size_t(n) * (sizeof(double) + sizeof(float));
         if (n == 16)
-            k_mx_leaf_residual0<16><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
+            k_mx_leaf_residual0_16<<<unsigned((items + 15) / 16), 256, 0, st>>>(coefs, leaves, L, B, f, q, rl);
         else if (n == 8)
             k_mx_leaf_residual0<8><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
         else
