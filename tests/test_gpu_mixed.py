@@ -64,6 +64,21 @@ def test_mixed_reaches_fp64_solution_uniform(ef, kind, n):
     assert np.all(res[2, :3] < res[0, :3] * 1e-8)
 
 
+def test_mixed_ragged_items_16x16(ef):
+    # 16 x 16 leaves run 16 items per block in the leaf and first-residual kernels: an adaptive tree
+    # of 88 leaves with 3 requests leaves the last block half empty
+    fn = lambda x, y: (x - 0.7) ** 2 + (y - 0.7) ** 2 < 0.04
+    mesh, hps = make(ef, ("adaptive", fn, 0, 4), 16, (0.0, 1.0, 0.0, 1.0))
+    B = 3
+    assert (mesh.num_leaves() * B) % 16 != 0
+    F, A, R = requests(hps, mesh, B, 21)
+    ref = fp64_solutions(hps, F, A, R)
+    hps.mixed_init(B)
+    u = hps.mixed_solve(F, A, R, sweeps=2)
+    for k in range(B):
+        assert np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max() <= TOL
+
+
 def test_mixed_reaches_fp64_solution_adaptive(ef):
     fn = lambda x, y: y > 0.45 and x > 0.45
     mesh, hps = make(ef, ("adaptive", fn, 0, 5), 8, (0.0, 1.0, 0.0, 1.0))

@@ -176,6 +176,8 @@ ADAPTIVE_CASES = {
     "wedge": ((lambda x, y: y > 0.45 and x > 0.45), (0.0, 1.0, 0.0, 1.0), 4, 0, 6),
     "disk": ((lambda x, y: (x - 0.7) ** 2 + (y - 0.7) ** 2 < 0.04), (0.0, 1.0, 0.0, 1.0), 4, 0, 6),
     "ring": ((lambda x, y: abs(x * x + y * y - 0.5) < 0.05), (-1.0, 1.0, -1.0, 1.0), 8, 1, 5),
+    # 16 x 16 leaves (register-transform leaf kernels), 88 leaves: the last 16-leaf block is ragged
+    "disk16": ((lambda x, y: (x - 0.7) ** 2 + (y - 0.7) ** 2 < 0.04), (0.0, 1.0, 0.0, 1.0), 16, 0, 4),
 }
 
 
