@@ -647,7 +647,14 @@ __global__ void k_mx_uncoarsen(const T* const* vin, T* const* vout, int nf, int 
 }
 
 // ---- leaves --------------------------------------------------------------------------------------
-// FP32 eigenbasis leaf pass over the items (leaf, b), b fastest.  A group of (n/4)^2 threads owns
+// float offset of the 4-float chunk c4 of row `row` in an item buffer (row-major)
+template <int NT>
+__device__ __forceinline__ int mx_xoff(int row, int c4, int n) {
+    return row * (NT ? NT : n) + 4 * c4;
+}
+
+// FP32 eigenbasis leaf pass over the items (leaf, b), b fastest, for leaf sizes other than 16 (16 x 16
+// leaves run k_mx_leaf16).  A group of (n/4)^2 threads owns
 // two items; each thread owns a 4 x 4 block of every product of both
 //   WT = (V^T F)^T,  G = Dinv o (V^T F V),  U1T = (V G)^T,  u = V G V^T
 // with float4 operand reads from shared memory.  One operand of every product is V (it depends on
@@ -657,21 +664,6 @@ __global__ void k_mx_uncoarsen(const T* const* vin, T* const* vout, int nf, int 
 // an item holds n*n floats of shared memory.  Every sum runs over t = 0 .. n-1 in order.
 // NEUMANN writes h32 = DtN(0, q); SOLVE adds the solution of (g32, q) to the FP64 state u64 (or
 // stores it there when accumulate is 0).
-// Float offset of the 4-float chunk c4 of row `row` in an item buffer.  For n = 16 two rows share a
-// 128-byte line and the line's eight chunks are permuted by an XOR with the line index, so that a
-// quarter-warp's transposed block stores (rows 4 bj + c, chunk bi) and block stores (rows 4 bi + a,
-// chunk bj) reach all 32 banks -- row-major puts them four and two to a bank group -- while the
-// reads of one row stay a permutation of that row's chunks.
-template <int NT>
-__device__ __forceinline__ int mx_xoff(int row, int c4, int n) {
-    if (NT == 16) {
-        const int line = row >> 1;
-        const int h = ((line & 2) << 1) | ((line & 4) >> 1);
-        return (line << 5) + (((((row & 1) << 2) | c4) ^ h) << 2);
-    }
-    return row * n + 4 * c4;
-}
-
 template <int MODE, int NT>
 __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restrict__ types,
                                                    const MixLeaf* __restrict__ leaves, int L, int B, int n_arg,
@@ -1653,8 +1645,8 @@ template <int MODE>
 void mx_leaf32_mode(cudaStream_t st, unsigned grid, unsigned threads, size_t smem, const LeafType32* types,
                     const MixLeaf* leaves, int L, int B, int n, int ipc, const float* q, double* u64,
                     int accumulate) {
-    if (n == 16) mx_leaf32_launch<MODE, 16>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
-    else if (n == 8) mx_leaf32_launch<MODE, 8>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
+    // 16 x 16 leaves never come here (k_mx_leaf16)
+    if (n == 8) mx_leaf32_launch<MODE, 8>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
     else if (n == 32) mx_leaf32_launch<MODE, 32>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
     else mx_leaf32_launch<MODE, 0>(st, grid, threads, smem, types, leaves, L, B, n, ipc, q, u64, accumulate);
 }
