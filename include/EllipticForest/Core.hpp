@@ -1,7 +1,7 @@
 // Host-side core of the C++ drop-in: the one-rank communicator shim, options, timers, logger, the
-// application singleton and the small Vector/Matrix containers drivers touch.
+// application singleton and the small Vector/Matrix containers user programs touch.
 //
-// Mirrors the driver-facing parts of the reference's src/EllipticForestApp.hpp:39-137,
+// Mirrors the parts user programs call of the reference's src/EllipticForestApp.hpp:39-137,
 // src/Options.hpp:27-33 (std::variant<std::string,bool,int,double> options), src/Timer.hpp,
 // src/Logger.hpp:31-58, src/MPI.hpp (MPIObject) and src/Vector.hpp / src/Matrix.hpp.  There is no
 // MPI, PETSc or p4est: every object lives on one process driving one GPU.
