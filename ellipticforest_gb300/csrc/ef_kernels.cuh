@@ -97,8 +97,8 @@ struct LeafItem {
 
 void leaf_eigen(cudaStream_t st, int mode, const LeafType* types_dev, const LeafItem* items_dev,
                 int nitems, int nmax);
-// rows 0..7 of the 16 x 16 sine basis into constant memory (once per process); required before
-// leaf_eigen runs NEUMANN or SOLVE on 16 x 16 leaves
+// rows 0..7 of the 16 x 16 sine basis into constant memory (ordered on st, synchronous); required
+// before leaf_eigen runs NEUMANN or SOLVE on 16 x 16 leaves
 void leaf_set_basis16(cudaStream_t st);
 
 // Variable-coefficient leaf (FivePointStencil): coefficients sampled per cell, banded LU of the

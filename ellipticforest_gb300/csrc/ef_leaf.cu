@@ -10,7 +10,6 @@
 //     U = V [ (V^T F V) ./ (mu_x[k] + mu_y[l] + lambda) ] V^T.
 // The Neumann data follow FiniteVolumeSolver.cpp:296-353: h_W = (2/dx)(u_W - g_W),
 // h_E = -(2/dx)(u_E - g_E), h_S = (2/dy)(u_S - g_S), h_N = -(2/dy)(u_N - g_N).
-#include <atomic>
 #include <cmath>
 #include <stdexcept>
 
@@ -293,8 +292,8 @@ void launch_leaf(cudaStream_t st, const LeafType* types, const LeafItem* items, 
 }  // namespace
 
 void leaf_set_basis16(cudaStream_t st) {
-    static std::atomic<bool> done{false};
-    if (done.load()) return;
+    // uploaded by every tree set-up and single-patch call (1 KB): the values never change, and a
+    // context reset by the caller cannot leave the table empty
     double V[8 * 16];
     for (int i = 0; i < 8; ++i)
         for (int k = 0; k < 16; ++k) {
@@ -304,7 +303,6 @@ void leaf_set_basis16(cudaStream_t st) {
     if (cudaMemcpyToSymbolAsync(c_V16d, V, sizeof(V), 0, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         throw std::runtime_error("leaf basis upload failed");
-    done.store(true);
 }
 
 void leaf_eigen(cudaStream_t st, int mode, const LeafType* types, const LeafItem* items, int nitems,
