@@ -97,6 +97,10 @@ struct LeafItem {
 
 void leaf_eigen(cudaStream_t st, int mode, const LeafType* types_dev, const LeafItem* items_dev,
                 int nitems, int nmax);
+// same as leaf_eigen, but every size runs the contraction kernel that reads the basis V from the
+// LeafType table (never the constant-memory 16 x 16 basis): for callers that cannot upload it
+void leaf_eigen_tables(cudaStream_t st, int mode, const LeafType* types_dev, const LeafItem* items_dev,
+                       int nitems, int nmax);
 // rows 0..7 of the 16 x 16 sine basis into constant memory (ordered on st, synchronous); required
 // before leaf_eigen runs NEUMANN or SOLVE on 16 x 16 leaves
 void leaf_set_basis16(cudaStream_t st);

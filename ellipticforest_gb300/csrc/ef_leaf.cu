@@ -280,11 +280,9 @@ __global__ void __launch_bounds__(256) k_leaf16d(const LeafType* __restrict__ ty
 template <int MODE>
 void launch_leaf(cudaStream_t st, const LeafType* types, const LeafItem* items, int nitems, int nmax) {
     const size_t smem = size_t(3) * nmax * nmax * sizeof(double);
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_leaf_eigen<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        configured = true;
-    }
+    // set on every call (cheap, and the current device may change between calls); a once-only flag
+    // would be shared unsynchronised by host threads
+    cudaFuncSetAttribute(k_leaf_eigen<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     k_leaf_eigen<MODE><<<nitems, 256, smem, st>>>(types, items);
     ++g_kernel_launches;
 }
@@ -315,6 +313,12 @@ void leaf_eigen(cudaStream_t st, int mode, const LeafType* types, const LeafItem
         ++g_kernel_launches;
         return;
     }
+    leaf_eigen_tables(st, mode, types, items, nitems, nmax);
+}
+
+void leaf_eigen_tables(cudaStream_t st, int mode, const LeafType* types, const LeafItem* items, int nitems,
+                       int nmax) {
+    if (nitems <= 0) return;
     if (mode == LEAF_DTN_COLUMN) launch_leaf<LEAF_DTN_COLUMN>(st, types, items, nitems, nmax);
     else if (mode == LEAF_NEUMANN) launch_leaf<LEAF_NEUMANN>(st, types, items, nitems, nmax);
     else if (mode == LEAF_SOLVE) launch_leaf<LEAF_SOLVE>(st, types, items, nitems, nmax);

@@ -1,17 +1,17 @@
 // Single-patch solve that allocates nothing (ef_fv_solve_noalloc).
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is being captured into a
-// graph (allocation is not permitted there), plugins inside a host framework that owns all device
-// memory through its own pool and forbids raw allocations, and real-time loops that must not
-// allocate after start-up.  For them this entry point keeps its scratch -- the patch's sine basis,
-// its inverse eigenvalue table and the one-item launch descriptors -- in a file-scope device array
-// of fixed size instead of allocating it per call like ef_fv_solve does.  The caller passes device
+// Some callers cannot call cudaMalloc: plugins inside a host framework that owns all device memory
+// through its own pool and forbids raw allocations, and real-time loops that must not allocate
+// after start-up.  For them this entry point keeps its scratch -- the patch's sine basis, its
+// inverse eigenvalue table and the one-item launch descriptors -- in a file-scope device array of
+// fixed size instead of allocating it per call like ef_fv_solve does.  The caller passes device
 // pointers for the inputs and the output.
 //
 // The array is sized for patches of at most kNoAllocMaxN = 64 cells per side (about 66 KB) and
 // every GPU that loads this library holds it until the process exits.  All calls share it: each
 // call overwrites every entry it reads before use, so nothing needs clearing between calls, but two
 // calls whose work overlaps on the GPU (different streams, or other threads) race on it.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -63,6 +63,32 @@ __global__ void k_noalloc_tables(int n, double dx, double dy, double lambda, con
 
 std::mutex g_symbol_mutex;
 double* g_symbol_addr[64] = {nullptr};
+unsigned long long g_symbol_ctx[64] = {0};  // context id the cached address belongs to
+
+// Id of the calling thread's current context (cuCtxGetId through the runtime's driver entry point, no
+// link against libcuda); 0 when unavailable.  A cudaDeviceReset by the caller makes a new primary
+// context whose id differs, so the cached address is looked up again.
+unsigned long long current_ctx_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* p = nullptr;
+        void* q = nullptr;
+        cudaDriverEntryPointQueryResult r1{}, r2{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &r1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2) != cudaSuccess ||
+            r1 != cudaDriverEntryPointSuccess || r2 != cudaDriverEntryPointSuccess || !p || !q)
+            return 0;
+        get_current = reinterpret_cast<GetCurrent>(p);
+        get_id = reinterpret_cast<GetId>(q);
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -94,10 +120,11 @@ extern "C" int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, doubl
     }
     double* scratch;
     {
-        // once per device, with that device current: host code needs the device address of the
-        // array (its host-side name is only a stand-in)
+        // once per device (and again after a context reset), with that device current: host code
+        // needs the device address of the array (its host-side name is only a stand-in)
         std::lock_guard<std::mutex> lock(g_symbol_mutex);
-        if (!g_symbol_addr[dev]) {
+        const unsigned long long ctx = current_ctx_id();
+        if (!g_symbol_addr[dev] || ctx == 0 || ctx != g_symbol_ctx[dev]) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess || !p) {
@@ -106,6 +133,8 @@ extern "C" int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, doubl
                 return EF_ERR_CUDA;
             }
             g_symbol_addr[dev] = static_cast<double*>(p);
+            // the look-up itself creates the primary context if there was none yet
+            g_symbol_ctx[dev] = ctx != 0 ? ctx : current_ctx_id();
         }
         scratch = g_symbol_addr[dev];
     }
@@ -113,7 +142,9 @@ extern "C" int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, doubl
     const double dx = (x_upper - x_lower) / n, dy = (y_upper - y_lower) / n;
     k_noalloc_tables<<<1, 256, 0, st>>>(n, dx, dy, lambda, g_dev, f_dev, u_dev, scratch);
     ++efgb::g_kernel_launches;
-    efgb::leaf_eigen(st, efgb::LEAF_SOLVE, reinterpret_cast<const efgb::LeafType*>(scratch + kTypeOffset),
+    // the table-reading kernel for every n: the 16 x 16 fast kernel reads a constant-memory basis
+    // that only the allocating entry points upload
+    efgb::leaf_eigen_tables(st, efgb::LEAF_SOLVE, reinterpret_cast<const efgb::LeafType*>(scratch + kTypeOffset),
                      reinterpret_cast<const efgb::LeafItem*>(scratch + kItemOffset), 1, n);
     e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -6,6 +6,8 @@
 
 #include <cstdio>
 #include <memory>
+#include <stdexcept>
+#include <string>
 
 #include "Mesh.hpp"
 
@@ -156,15 +158,31 @@ public:
     }
 
     // The per-node hooks of the reference (HPSAlgorithm.hpp:497-596).  On the GPU every tree level
-    // is merged, upward-passed and split by grouped kernels, so these are not called per node.
-    virtual void merge4to1(PatchType&, PatchType&, PatchType&, PatchType&, PatchType&) {}
-    virtual void upwards4to1(PatchType&, PatchType&, PatchType&, PatchType&, PatchType&) {}
-    virtual void split1to4(PatchType&, PatchType&, PatchType&, PatchType&, PatchType&) {}
-    virtual void leafSolve(PatchType&) {}
+    // is merged, upward-passed and split by grouped kernels over all of its nodes, and the operators
+    // stay in device memory, so there is no per-node call a subclass could take over.  The hooks are
+    // therefore `final`: a subclass that overrides one (as the reference allows) fails to compile
+    // ("overriding final function") instead of being silently ignored.  Calling one directly throws.
+    virtual void merge4to1(PatchType& tau, PatchType& alpha, PatchType& beta, PatchType& gamma,
+                           PatchType& omega) final {
+        noPerNodeHook("merge4to1");
+    }
+    virtual void upwards4to1(PatchType& tau, PatchType& alpha, PatchType& beta, PatchType& gamma,
+                             PatchType& omega) final {
+        noPerNodeHook("upwards4to1");
+    }
+    virtual void split1to4(PatchType& tau, PatchType& alpha, PatchType& beta, PatchType& gamma,
+                           PatchType& omega) final {
+        noPerNodeHook("split1to4");
+    }
+    virtual void leafSolve(PatchType& patch) final { noPerNodeHook("leafSolve"); }
 
     ef_hps* handle() { return h_; }
 
 private:
+    [[noreturn]] static void noPerNodeHook(const char* name) {
+        throw std::logic_error(std::string("[HPSAlgorithm::") + name +
+                               "] per-node hooks do not run on the GPU path: every tree level runs as grouped kernels");
+    }
     void ensureHandle() {
         if (h_) return;
         efCheck(ef_hps_create(mesh.handle(), patch_solver.efType(), patch_solver.efLambda(), &h_),

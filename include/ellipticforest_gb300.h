@@ -216,15 +216,16 @@ int ef_fv5_map_d2n(int n, double x_lower, double x_upper, double y_lower, double
 /* ---- Single patch without allocation -------------------------------------------------------- */
 
 /* No counterpart in the reference.  The solve of ef_fv_solve for callers that cannot allocate
- * device memory -- code running during CUDA stream capture, plugins whose host framework owns all
- * device memory, real-time loops that must not allocate after start-up.  It calls no cudaMalloc,
- * cudaFree or allocating library routine: its scratch (sine basis, eigenvalue table, launch
- * descriptors) lives in a fixed device array of about 66 KB that every GPU loading this library
- * holds until exit, which limits n to 64.  g_dev (4n), f_dev (n*n, NULL = zero load) and u_dev
- * (n*n) are device pointers owned by the caller; the work is queued on cuda_stream (NULL = default
- * stream) and the call returns without synchronising.  The first call on each device looks up the
- * array's device address (with that device current) and should come before any stream capture.
- * All calls share the array, so calls whose work overlaps on the GPU race. */
+ * device memory: plugins inside a host framework that owns all device memory through its own pool
+ * and forbids raw allocations, and real-time loops that must not allocate after start-up.  It calls
+ * no cudaMalloc, cudaFree or allocating library routine: its scratch (sine basis, eigenvalue table,
+ * launch descriptors) lives in a fixed device array of about 66 KB that every GPU loading this
+ * library holds until exit, which limits n to 64 (larger n returns EF_ERR_INVALID).  g_dev (4n),
+ * f_dev (n*n, NULL = zero load) and u_dev (n*n) are device pointers owned by the caller; the work
+ * is queued on cuda_stream (NULL = default stream) and the call returns without synchronising.
+ * The first call on each device (and the first after a cudaDeviceReset) looks up the array's
+ * device address with that device current; make that first call before any stream capture.  All
+ * calls share the array, so calls whose work overlaps on the GPU race. */
 int ef_fv_solve_noalloc(int solver_type, int n, double x_lower, double x_upper, double y_lower,
                         double y_upper, double lambda, const double* g_dev, const double* f_dev,
                         double* u_dev, void* cuda_stream);

@@ -84,3 +84,27 @@ def to_leaf_order(U: np.ndarray, level: int, n: int) -> np.ndarray:
             rec(lvl + 1, 2 * ix + (c & 1), 2 * iy + (c >> 1))
     rec(0, 0, 0)
     return np.concatenate(out)
+
+
+def solve_poisson_dst(F: np.ndarray, gW, gE, gS, gN, xl: float, xu: float, yl: float, yu: float,
+                      lam: float = 0.0) -> np.ndarray:
+    """Direct solve of the same global system for constant coefficients (alpha = beta = 1, constant
+    lambda) by the sine transform that diagonalises it: with the Dirichlet ghost ``2 g - u`` the 1-D
+    second difference has the eigenvectors sin(pi (k+1)(i+1/2)/N) (the orthonormal DST-II basis) and
+    eigenvalues -(4/d^2) sin^2(pi (k+1)/(2N)).  O(N^2 log N) instead of a sparse LU, so the level-7
+    grid (2048^2 cells) solves in seconds; pinned against ``solve_dirichlet`` (sparse LU) in the
+    tests.  F is the load at cell centres [nx, ny] (x index outer); g* the face data per side.
+    """
+    import scipy.fft as fft
+    nx, ny = F.shape
+    dx, dy = (xu - xl) / nx, (yu - yl) / ny
+    R = np.array(F, dtype=np.float64, copy=True)
+    R[0, :] += -2.0 * gW / dx ** 2
+    R[-1, :] += -2.0 * gE / dx ** 2
+    R[:, 0] += -2.0 * gS / dy ** 2
+    R[:, -1] += -2.0 * gN / dy ** 2
+    mx = -(4.0 / dx ** 2) * np.sin(np.pi * (np.arange(nx) + 1) / (2 * nx)) ** 2
+    my = -(4.0 / dy ** 2) * np.sin(np.pi * (np.arange(ny) + 1) / (2 * ny)) ** 2
+    Rh = fft.dstn(R, type=2, norm="ortho", workers=-1)
+    Uh = Rh / (mx[:, None] + my[None, :] + lam)
+    return fft.idstn(Uh, type=2, norm="ortho", workers=-1)

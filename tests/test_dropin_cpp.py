@@ -70,3 +70,25 @@ def test_dropin_driver_matches_oracle(driver, tmp_path, n, lo, hi, min_level, ma
     assert ET.parse(f"{out}-vtk-mesh.pvtu").getroot().find("PUnstructuredGrid/Piece").get("Source").endswith("-0.vtu")
     quad = ET.parse(f"{out}-vtk-quadtree.vtu").getroot().find("UnstructuredGrid/Piece")
     assert int(quad.get("NumberOfCells")) == info["leaves"]
+
+
+def test_overriding_a_per_node_hook_does_not_compile(tmp_path):
+    """The reference's per-node hooks (merge4to1, upwards4to1, split1to4, leafSolve) are virtual
+    customisation points; the drop-in runs whole tree levels as grouped kernels, so an override would
+    never be called.  They are final: a subclass that overrides one is a compile error, not a
+    silently ignored method."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    src = ROOT / "tests" / "cpp" / "override_hook.cpp"
+    res = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
+                         capture_output=True, text=True)
+    assert res.returncode != 0
+    assert "final" in res.stderr, res.stderr
+    # the same driver without the override compiles
+    ok = src.read_text().replace(" override {}", " {}").replace("void merge4to1", "void myMerge")
+    tmp = tmp_path / "no_override.cpp"
+    tmp.write_text(ok)
+    res = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), str(tmp)],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr

@@ -130,6 +130,25 @@ def test_uniform_hps_equals_global_five_point(L, n):
     assert np.abs(u - ug).max() <= 1e-12 * np.abs(ug).max()
 
 
+@pytest.mark.parametrize("nx,ny,lam", [(64, 64, 0.0), (96, 48, -3.0)])
+def test_sine_transform_direct_solve_equals_sparse_lu(nx, ny, lam):
+    # the fast direct solve used at level 7 against the sparse LU of the same global system
+    rng = np.random.default_rng(nx + ny)
+    dom = (-1.0, 2.0, 0.5, 1.5)
+    F = rng.standard_normal((nx, ny))
+    gW, gE, gS, gN = rng.standard_normal(ny), rng.standard_normal(ny), rng.standard_normal(nx), rng.standard_normal(nx)
+    U = G.solve_poisson_dst(F, gW, gE, gS, gN, *dom, lam=lam)
+    A, cW, cE, cS, cN, x, y = G.assemble(nx, ny, *dom, lam=lambda X, Y: lam + 0.0 * X)
+    R = F.copy()
+    R[0, :] += -2.0 * cW[0, :] * gW
+    R[-1, :] += -2.0 * cE[-1, :] * gE
+    R[:, 0] += -2.0 * cS[:, 0] * gS
+    R[:, -1] += -2.0 * cN[:, -1] * gN
+    import scipy.sparse.linalg as spla
+    Us = spla.spsolve(A.tocsc(), R.ravel())
+    assert np.abs(U.ravel() - Us).max() <= 1e-12 * np.abs(Us).max()
+
+
 def test_adaptive_hps_second_order():
     f = lambda x, y: -u_exact(x, y)
     errs = []
