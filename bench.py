@@ -266,9 +266,11 @@ def measure_fp64_peak(torch):
 
 
 # DRAM bytes per launch / algorithmic bytes per launch of the solve kernels, from one ncu capture
-# of the same kernels on the uniform L6 tree (profiles/k_gemv_down_uniform_L6.md); L7 launches
+# of the same kernels on the uniform L6 tree (the k_gemv_down summary under profiles/); L7 launches
 # stream 4x the bytes of L6 launches with the same access pattern.
-TRAFFIC_RATIO = {"downward": 1.005}
+# The mixed step's residual section runs the first residual (12 B per cell-request, DRAM 1.25x) and
+# the exact residual (20 B, DRAM 1.17x) once each per sweep (same L6 capture): 1.20x of its bytes.
+TRAFFIC_RATIO = {"downward": 1.005, "mx_leaf_residual": (1.25 * 12 + 1.17 * 20) / 32}
 
 
 def load_peaks():
@@ -524,6 +526,9 @@ def run_gb300(args):
             "data": "synthetic (seeded Gaussian-bump loads, Fourier Dirichlet data)",
             "config": {"workload": workload_desc(level, n, B, sweeps), "leaves": 4 ** level, "dofs": dofs,
                        "batch": B, "sweeps": sweeps, "lanes_in_flight": lanes,
+                       "rel_err_vs_fp64": rel_err, "tolerance": 1e-10,
+                       "plain_fp64_solves_per_s": plain_value,
+                       "speedup_vs_plain_fp64": value / plain_value,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "FP32 operators (1.75 GiB) and the block's leaf arrays far exceed L2"},
             "build_s": build_s, "mdof_per_s": value * dofs / 1e6,
@@ -552,9 +557,12 @@ def run_gb300(args):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
-                         "traffic": (TRAFFIC_RATIO[dom_name] * d["bytes"] / max(d["launches"], 1)
+                         "traffic": (TRAFFIC_RATIO[dom_name] * d["bytes"] / max(d["calls"], 1)
                                      if dom_name in TRAFFIC_RATIO else None),
-                         "algorithmic_bytes_per_launch": d["bytes"] / max(d["launches"], 1),
+                         "traffic_unit": "DRAM bytes per section call (its main kernel and its small "
+                                         "reduction launches), scaled from the L6 ncu capture",
+                         "algorithmic_bytes_per_call": d["bytes"] / max(d["calls"], 1),
+                         "launches_per_call": d["launches"] / max(d["calls"], 1),
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "share_of_step": d["ms"] / tot_ms},
             "fp64": {"build_tflops": build_flops / build_s / 1e12, "build_flops": build_flops,

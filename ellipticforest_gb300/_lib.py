@@ -103,6 +103,12 @@ SIGNATURES = {
                                _dp]),
     "ef_fv5_map_d2n": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp,
                                  _dp, _dp]),
+    "ef_mesh_level_count": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
+    "ef_mesh_subtree": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "ef_hps_split_sizes": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
+    "ef_hps_build_top": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "ef_hps_upwards_top": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "ef_hps_solve_top": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, C.POINTER(_vp)]),
     "ef_fv_solve_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                       C.c_double, _vp, _vp, _vp, _vp]),
 }

@@ -152,6 +152,7 @@ void Hps::allocate32() {
 }
 
 void Hps::build_mixed(int fp64_levels) {
+    top_level_ = -1;
     if (fp64_levels < 0) throw std::invalid_argument("mixed build: fp64_levels must be >= 0");
     if (!arena32_) allocate32();
     build_leaf_types();
@@ -204,7 +205,7 @@ void Hps::build_mixed(int fp64_levels) {
     }
     ck32(cudaGetLastError(), "mixed build launch");
     ck32(cudaStreamSynchronize(st_), "mixed build sync");
-    singular_ = 0;
+    singular_ = leaf_singular_;
     for (auto& g : groups_) {
         std::vector<int> info(g.nodes.size());
         ck32(cudaMemcpy(info.data(), g.d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "info");

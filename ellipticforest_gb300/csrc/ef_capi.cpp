@@ -129,13 +129,25 @@ int run_single_patch(int solver_type, int n, double xl, double xu, double yl, do
     if (e == cudaSuccess) e = cudaMemcpy(dty, &ty, sizeof(ty), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(ditems, items.data(), nitems * sizeof(efgb::LeafItem), cudaMemcpyHostToDevice);
+    int singular = 0;
     if (e == cudaSuccess) {
-        if (n == 16) efgb::leaf_set_basis16(0);
-        efgb::leaf_eigen(0, mode, dty, ditems, nitems, n);
+        if (mode == efgb::LEAF_DTN_COLUMN) {
+            // the DtN map by a pivoted dense LU of the 5-point operator (as in a tree build)
+            try {
+                singular = efgb::leaf_dtn_lu(0, n, lambda, {dx}, {dy}, {dout});
+            } catch (...) {
+                cudaFree(buf);
+                throw;
+            }
+        } else {
+            if (n == 16) efgb::leaf_set_basis16(0);
+            efgb::leaf_eigen(0, mode, dty, ditems, nitems, n);
+        }
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out_host, dout, out_count * 8, cudaMemcpyDeviceToHost);
     cudaFree(buf);
+    if (singular) return fail(EF_ERR_SINGULAR, "the 5-point operator of the patch is singular");
     return cuda_status(e, "single patch");
 }
 
@@ -254,6 +266,24 @@ int ef_mesh_leaf(const ef_mesh* mesh, int k, int* level, long long* ix, long lon
     return EF_OK;
 }
 
+int ef_mesh_level_count(const ef_mesh* mesh, int level, int* count) {
+    if (!mesh || !count) return fail(EF_ERR_INVALID, "null argument");
+    if (level < 0) return fail(EF_ERR_INVALID, "negative level");
+    *count = int(efgb::level_nodes(mesh->mesh, level).size());
+    return EF_OK;
+}
+
+int ef_mesh_subtree(const ef_mesh* mesh, int level, int index, ef_mesh** out) {
+    if (!mesh || !out) return fail(EF_ERR_INVALID, "null argument");
+    if (level < 0) return fail(EF_ERR_INVALID, "negative level");
+    return guarded([&] {
+        auto m = std::make_unique<ef_mesh>();
+        m->mesh = efgb::subtree_mesh(mesh->mesh, level, index);
+        *out = m.release();
+        return EF_OK;
+    });
+}
+
 int ef_mesh_destroy(ef_mesh* mesh) {
     delete mesh;
     return EF_OK;
@@ -363,6 +393,7 @@ int ef_hps_build_from(ef_hps* h, const ef_hps* old, int* reused) {
 int ef_hps_save(const ef_hps* h, const char* path) {
     if (!h || !path) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "save before build stage");
+    if (h->hps->top_level() >= 0) return fail(EF_ERR_STATE, "save of a tree built by ef_hps_build_top");
     return guarded([&] {
         h->hps->save(path);
         return EF_OK;
@@ -384,9 +415,61 @@ int ef_hps_load(const char* path, ef_mesh** mesh_out, ef_hps** hps_out) {
     });
 }
 
+int ef_hps_split_sizes(ef_hps* h, int level, int* sizes) {
+    if (!h || !sizes) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        const std::vector<int> v = h->hps->split_sizes(level);
+        std::memcpy(sizes, v.data(), v.size() * sizeof(int));
+        return EF_OK;
+    });
+}
+
+int ef_hps_build_top(ef_hps* h, int level, const double* const* T) {
+    if (!h || !T) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        h->mixed.reset();
+        h->drop_lanes();
+        h->hps->build_top(level, T);
+        if (h->hps->singular_count() > 0)
+            return fail(EF_ERR_SINGULAR, std::to_string(h->hps->singular_count()) +
+                                             " interface matrices had a zero pivot (dgesv INFO != 0)");
+        return EF_OK;
+    });
+}
+
+int ef_hps_upwards_top(ef_hps* h, int level, const double* const* hv) {
+    if (!h || !hv) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        h->hps->upwards_top(level, hv);
+        h->upward_done = true;
+        return EF_OK;
+    });
+}
+
+int ef_hps_solve_top(ef_hps* h, int level, const double* a, const double* b, const double* r, double* const* g) {
+    if (!h || !a || !b || !r || !g) return fail(EF_ERR_INVALID, "null argument");
+    if (h->hps->top_level() != level) return fail(EF_ERR_STATE, "solve_top before build_top at this level");
+    return guarded([&] {
+        efgb::Hps& H = *h->hps;
+        const size_t m = 4 * size_t(H.root_M());
+        bool general = false;
+        for (size_t i = 0; i < m; ++i)
+            if (b[i] != 0.0) { general = true; break; }
+        cudaStream_t s = H.stream();
+        int st = cuda_status(cudaMemcpyAsync(H.bc_a(), a, m * 8, cudaMemcpyHostToDevice, s), "copy a");
+        if (!st) st = cuda_status(cudaMemcpyAsync(H.bc_b(), b, m * 8, cudaMemcpyHostToDevice, s), "copy b");
+        if (!st) st = cuda_status(cudaMemcpyAsync(H.bc_r(), r, m * 8, cudaMemcpyHostToDevice, s), "copy r");
+        if (st) return st;
+        H.set_bc_general(general);
+        H.solve_top(level, g);
+        return EF_OK;
+    });
+}
+
 int ef_hps_upwards(ef_hps* h, const double* f_host) {
     if (!h || !f_host) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "upwards stage before build stage");
+    if (h->hps->top_level() >= 0) return fail(EF_ERR_STATE, "tree built by ef_hps_build_top: use ef_hps_upwards_top");
     return guarded([&] {
         efgb::Hps& H = *h->hps;
         const size_t cnt = size_t(H.num_leaves()) * H.leaf_n() * H.leaf_n();
@@ -406,6 +489,7 @@ int ef_hps_upwards(ef_hps* h, const double* f_host) {
 int ef_hps_solve(ef_hps* h, const double* a, const double* b, const double* r) {
     if (!h || !a || !b || !r) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "solve stage before build stage");
+    if (h->hps->top_level() >= 0) return fail(EF_ERR_STATE, "tree built by ef_hps_build_top: use ef_hps_solve_top");
     return guarded([&] {
         efgb::Hps& H = *h->hps;
         const size_t m = 4 * size_t(H.root_M());
@@ -429,6 +513,7 @@ int ef_hps_solve(ef_hps* h, const double* a, const double* b, const double* r) {
 int ef_hps_solve_root_dirichlet(ef_hps* h, const double* g) {
     if (!h || !g) return fail(EF_ERR_INVALID, "null argument");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "solve stage before build stage");
+    if (h->hps->top_level() >= 0) return fail(EF_ERR_STATE, "tree built by ef_hps_build_top: use ef_hps_solve_top");
     return guarded([&] {
         efgb::Hps& H = *h->hps;
         const size_t m = 4 * size_t(H.root_M());
@@ -504,6 +589,7 @@ int ef_hps_load_device_async(ef_hps* h, const double* f, const double* a, const 
 int ef_hps_solve_device_async(ef_hps* h, int b_is_zero) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->hps->built()) return fail(EF_ERR_STATE, "solve before build stage");
+    if (h->hps->top_level() >= 0) return fail(EF_ERR_STATE, "tree built by ef_hps_build_top: use ef_hps_solve_top");
     return guarded([&] {
         h->hps->set_bc_general(b_is_zero == 0);
         h->hps->solve_async();
@@ -519,6 +605,7 @@ int ef_hps_synchronize(ef_hps* h) {
 int ef_hps_mixed_init(ef_hps* h, int bmax) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
     if (!h->hps->built() && !h->hps->built32()) return fail(EF_ERR_STATE, "mixed solver before build stage");
+    if (h->hps->top_level() >= 0) return fail(EF_ERR_STATE, "mixed solver on a tree built by ef_hps_build_top");
     return guarded([&] {
         h->drop_lanes();
         h->mixed.reset();

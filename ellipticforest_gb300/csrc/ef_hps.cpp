@@ -503,6 +503,7 @@ void Hps::set_coefficients(const double* alpha, const double* beta, const double
 
 void Hps::build_leaf_types() {
     const double n = n_;
+    leaf_singular_ = 0;
     if (solver_type_ == SOLVER_FIVE_POINT) {
         if (!coef_set_) throw std::invalid_argument("FivePointStencil: leaf coefficients were not set");
         const double L = num_leaves(), N = n * n;
@@ -510,17 +511,46 @@ void Hps::build_leaf_types() {
         pb("leaf_factor");
         fp_factor(st_, d_fp_, num_leaves(), n_);
         pe(L * 8 * (6 * N + N * (2 * n + 1)), L * 2.0 * N * n * n);
+        pb("leaf_dtn");
+        leaf_run(LEAF_DTN_COLUMN, d_items_dtn_, nitems_dtn_);
+        pe(double(types_.size()) * 16 * n * n * 8, double(nitems_dtn_) * (6 * n * n * n + 8 * n * n));
+        return;
     }
+    // one DtN per distinct leaf geometry, by a pivoted dense LU of its 5-point operator
+    std::vector<double> dx, dy;
+    std::vector<double*> T;
+    for (const auto& ty : types_) {
+        dx.push_back(ty.dx);
+        dy.push_back(ty.dy);
+        T.push_back(ty.T);
+    }
+    const double nn = n * n, nt = double(types_.size());
     pb("leaf_dtn");
-    leaf_run(LEAF_DTN_COLUMN, d_items_dtn_, nitems_dtn_);
-    pe(double(types_.size()) * 16 * n * n * 8, double(nitems_dtn_) * (6 * n * n * n + 8 * n * n));
+    leaf_singular_ = leaf_dtn_lu(st_, n_, lambda_, dx, dy, T);
+    pe(nt * 8 * (2 * nn * nn + 2 * nn * 4 * n + 16 * n * n),
+       nt * (2.0 / 3.0 * nn * nn * nn + 2.0 * nn * nn * 4 * n));
 }
 
 void Hps::build() {
     root_lu_valid_ = false;
+    top_level_ = -1;
     build_leaf_types();
-    const int maxL = mesh_.max_level;
-    for (int lvl = maxL - 1; lvl >= 0; --lvl) {
+    merge_levels(mesh_.max_level - 1);
+    check(cudaGetLastError(), "build launch");
+    check(cudaStreamSynchronize(st_), "build sync");
+    singular_ = count_singular(mesh_.max_level) + leaf_singular_;
+    if (solver_type_ == SOLVER_FIVE_POINT) {
+        std::vector<int> info(num_leaves());
+        check(cudaMemcpy(info.data(), d_fpinfo_, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "fp info");
+        for (int v : info) singular_ += (v != 0);
+    }
+    built_ = true;
+}
+
+// every merge of the tree levels top .. 0, deepest first (HPSAlgorithm.hpp:497-518 per node): the
+// children's T of level top + 1 must be in place
+void Hps::merge_levels(int top) {
+    for (int lvl = top; lvl >= 0; --lvl) {
         for (size_t k = 0; k < tsteps_.size(); ++k)
             if (tsteps_[k].level == lvl + 1) {
                 const double nf = tsteps_[k].nf, cnt = tsteps_[k].count;
@@ -554,20 +584,18 @@ void Hps::build() {
             pe(c * 8 * (dm * dm / 2 + dm * 2 * dm + 2 * 4 * dm * dm), c * 2.0 * (2 * dm) * (2 * dm) * (dm / 2));
         }
     }
-    check(cudaGetLastError(), "build launch");
-    check(cudaStreamSynchronize(st_), "build sync");
-    singular_ = 0;
+}
+
+// interface LUs with a zero pivot among the merges of the levels below `below` (synchronous)
+int Hps::count_singular(int below) {
+    int bad = 0;
     for (auto& g : groups_) {
+        if (g.level >= below) continue;
         std::vector<int> info(g.nodes.size());
         check(cudaMemcpy(info.data(), g.d_info, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "info");
-        for (int v : info) singular_ += (v != 0);
+        for (int v : info) bad += (v != 0);
     }
-    if (solver_type_ == SOLVER_FIVE_POINT) {
-        std::vector<int> info(num_leaves());
-        check(cudaMemcpy(info.data(), d_fpinfo_, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "fp info");
-        for (int v : info) singular_ += (v != 0);
-    }
-    built_ = true;
+    return bad;
 }
 
 void Hps::upwards() {
@@ -576,8 +604,13 @@ void Hps::upwards() {
     leaf_run(LEAF_NEUMANN, d_items_neu_, num_leaves());
     pe(L * 8 * (n * n + 4 * n), L * (6 * n * n * n + 8 * n * n));
     if (homogeneous_) return;
-    const int maxL = mesh_.max_level;
-    for (int lvl = maxL - 1; lvl >= 0; --lvl) {
+    upward_levels(mesh_.max_level - 1);
+}
+
+// upwards4to1 (HPSAlgorithm.hpp:529-551) for the levels top .. 0: the children's h of level top + 1
+// must be in place
+void Hps::upward_levels(int top) {
+    for (int lvl = top; lvl >= 0; --lvl) {
         for (size_t k = 0; k < hsteps_.size(); ++k)
             if (hsteps_[k].level == lvl + 1) {
                 pb("coarsen_h");
@@ -660,14 +693,26 @@ void Hps::root_from_bc() {
 }
 
 void Hps::downwards() {
-    const int maxL = mesh_.max_level;
-    for (int lvl = 0; lvl < maxL; ++lvl) {
+    downward_levels(mesh_.max_level, false);
+    if (homogeneous_) fill_zero(st_, d_f_, (long long)num_leaves() * n_ * n_);
+    const double L = num_leaves(), n = n_;
+    pb("leaf_solve");
+    leaf_run(LEAF_SOLVE, d_items_solve_, num_leaves());
+    pe(L * 8 * (2 * n * n + 4 * n), L * 8 * n * n * n);
+}
+
+// split1to4 (HPSAlgorithm.hpp:562-577) from the root down to the nodes of level `bottom`; with
+// `uncoarsen_bottom` their g is also brought to their own size (uncoarsen_, :1165-1183)
+void Hps::downward_levels(int bottom, bool uncoarsen_bottom) {
+    for (int lvl = 0; lvl <= bottom; ++lvl) {
+        if (lvl == bottom && !uncoarsen_bottom) break;
         for (size_t k = 0; k < gsteps_.size(); ++k)
             if (gsteps_[k].level == lvl) {
                 pb("uncoarsen_g");
                 uncoarsen_vec(st_, gsteps_[k].d_in, gsteps_[k].d_out, gsteps_[k].count, gsteps_[k].nf);
                 pe(double(gsteps_[k].count) * 8 * 6 * gsteps_[k].nf, double(gsteps_[k].count) * 8 * gsteps_[k].nf);
             }
+        if (lvl == bottom) break;
         for (auto& g : groups_) {
             if (g.level != lvl) continue;
             const double c = double(g.nodes.size()), s = g.s;
@@ -676,11 +721,6 @@ void Hps::downwards() {
             pe(c * 8 * (32 * s * s + 8 * s + 4 * s + 16 * s), c * 2 * 32 * s * s);
         }
     }
-    if (homogeneous_) fill_zero(st_, d_f_, (long long)num_leaves() * n_ * n_);
-    const double L = num_leaves(), n = n_;
-    pb("leaf_solve");
-    leaf_run(LEAF_SOLVE, d_items_solve_, num_leaves());
-    pe(L * 8 * (2 * n * n + 4 * n), L * 8 * n * n * n);
 }
 
 void Hps::solve_async() {

@@ -214,6 +214,15 @@ public:
     // A built tree's solve-time operators to a file and back (ef_serial.cpp).
     void save(const char* path) const;
     static std::unique_ptr<Hps> load(const char* path);
+    // Subtree split (ef_subtree.cpp): this handle on the full mesh runs only the top `level` tree
+    // levels, on the T / h of the level-`level` nodes built and upward-passed elsewhere as subtrees
+    // of their own, and returns their g.  Every leaf must lie below `level`.
+    std::vector<int> split_nodes(int level) const;   // node ids at `level`, pre-order
+    std::vector<int> split_sizes(int level) const;   // 4m (length of h and g; T is 4m x 4m) per node
+    void build_top(int level, const double* const* T_host);
+    void upwards_top(int level, const double* const* h_host);
+    void solve_top(int level, double* const* g_host);  // root data from bc_a/b/r
+    int top_level() const { return top_level_; }      // -1 unless built by build_top
     void upwards();                                // HPSAlgorithm::upwardsStage on leaf_f()
     void root_from_bc();                           // root g from bc_a/b/r (HPSAlgorithm.hpp:402-420)
     void downwards();                              // split1to4 + leafSolve for every node
@@ -259,6 +268,10 @@ public:
     void profile_reset();
 
 private:
+    void merge_levels(int top);       // merges of levels top .. 0
+    void upward_levels(int top);      // upward pass of levels top .. 0
+    void downward_levels(int bottom, bool uncoarsen_bottom);  // split from the root to level `bottom`
+    int count_singular(int below);    // zero pivots among the merges of levels < below
     void plan();
     void allocate();
     void upload_tables();
@@ -311,6 +324,8 @@ private:
 
     bool built_ = false;
     int singular_ = 0;
+    int leaf_singular_ = 0;  // constant-coefficient leaf operators with a zero pivot (last build)
+    int top_level_ = -1;
 
     struct Mark {
         int stat;

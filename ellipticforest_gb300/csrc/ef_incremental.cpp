@@ -51,6 +51,7 @@ void Hps::build_from(const Hps& old) {
         old.mesh_.yl != mesh_.yl || old.mesh_.yu != mesh_.yu)
         throw std::invalid_argument("incremental build: domain, patch size or lambda differ");
     root_lu_valid_ = false;
+    top_level_ = -1;
     const std::vector<uint64_t> sn = signatures(mesh_), so = signatures(old.mesh_);
     std::map<std::tuple<int, int64_t, int64_t>, int> old_id;
     for (int id = 0; id < int(old.mesh_.nodes.size()); ++id) {
@@ -196,7 +197,7 @@ void Hps::build_from(const Hps& old) {
     }
     cki(cudaGetLastError(), "incremental build launch");
     cki(cudaStreamSynchronize(st_), "incremental build sync");
-    singular_ = 0;
+    singular_ = leaf_singular_;
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
         const Sub& sb = sub[gi];
         if (!sb.cnt) continue;

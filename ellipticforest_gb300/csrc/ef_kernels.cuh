@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <vector>
 #include <cstdint>
 
 namespace efgb {
@@ -101,6 +102,11 @@ void leaf_eigen(cudaStream_t st, int mode, const LeafType* types_dev, const Leaf
 // LeafType table (never the constant-memory 16 x 16 basis): for callers that cannot upload it
 void leaf_eigen_tables(cudaStream_t st, int mode, const LeafType* types_dev, const LeafItem* items_dev,
                        int nitems, int nmax);
+// Leaf DtN maps T[t] (4n x 4n, row-major, WESN) of the constant-coefficient leaf geometries
+// (dx[t], dy[t]) by a pivoted dense LU of their 5-point operators (ef_leaf_dtn.cu); synchronous,
+// returns the number of singular operators (zero pivot)
+int leaf_dtn_lu(cudaStream_t st, int n, double lambda, const std::vector<double>& dx, const std::vector<double>& dy,
+                const std::vector<double*>& T);
 // rows 0..7 of the 16 x 16 sine basis into constant memory (ordered on st, synchronous); required
 // before leaf_eigen runs NEUMANN or SOLVE on 16 x 16 leaves
 void leaf_set_basis16(cudaStream_t st);

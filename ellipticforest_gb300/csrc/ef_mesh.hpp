@@ -53,6 +53,11 @@ private:
     void build_nodes(const std::vector<Quad>& leaves);
 };
 
+// Node ids at `level` in pre-order (z-order), and the mesh of the subtree under the index-th of
+// them: its root box is that node's box and its leaves keep their patch boxes bit for bit.
+std::vector<int> level_nodes(const Mesh& m, int level);
+Mesh subtree_mesh(const Mesh& m, int level, int index);
+
 // Coarsest refinement of `leaves` in which face- and corner-neighbours differ by at most one level.
 std::vector<Quad> corner_balance(const std::vector<Quad>& leaves);
 

@@ -1,0 +1,118 @@
+// Device helpers shared by the mixed-precision kernels (ef_mixed.cu, ef_mixed_tc.cu): the merge
+// index maps, float <-> double conversions off the FP64 pipe, shared-memory addresses, cp.async,
+// bounded mbarrier waits and 2-D TMA tile loads.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace efgb {
+namespace {
+
+__device__ __forceinline__ int mx_lower_child(int I) { return (I == 1) ? 1 : (I == 3 ? 2 : 0); }
+__device__ __forceinline__ int mx_upper_child(int I) { return (I == 0) ? 2 : (I == 2 ? 1 : 3); }
+__device__ __forceinline__ int mx_q_lower(int I, int o, int s) { return (I < 2 ? 3 * s : s) + o; }
+__device__ __forceinline__ int mx_q_upper(int I, int o, int s) { return (I < 2 ? 2 * s : 0) + o; }
+__device__ __forceinline__ void mx_ext_map(int p, int s, int& c, int& q) {
+    const int side = p / (2 * s);
+    const int r = p - side * 2 * s;
+    const int hlf = r >= s ? 1 : 0;
+    c = side < 2 ? side + 2 * hlf : (side == 2 ? 0 : 2) + hlf;
+    q = side * s + (r - hlf * s);
+}
+__device__ __forceinline__ void mx_child_ifaces(int c, int& Ia, int& Ib) {
+    Ia = (c == 0 || c == 2) ? 0 : 1;
+    Ib = (c < 2) ? 2 : 3;
+}
+
+// float <-> double by integer bit manipulation.  GB300's FP64 pipe, which also converts between the
+// two widths, runs at a small fraction of its FP32 and integer rates; these stay off it.  Values
+// below the smallest normal number of the target type become signed zeros; d2f_rn_bits rounds to
+// nearest (ties to even): a one-signed rounding of every residual entry would bias the correction
+// it drives.
+__device__ __forceinline__ double f2d_bits(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long e64 = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(sign | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+__device__ __forceinline__ float d2f_rn_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = unsigned(b >> 32), lo = unsigned(b);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = int(hi >> 20) & 0x7ff;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+    const int e32 = e - 896;
+    if (e32 <= 0) return __uint_as_float(sign);
+    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
+    const unsigned rest = lo & 0x1fffffffu;
+    // a carry out of the significand steps the exponent (up to the infinity pattern)
+    const unsigned up = (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | ((unsigned(e32) << 23) + m + up));
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, int nbytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int nbytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+__device__ __forceinline__ long long global_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// bounded wait on an mbarrier phase: false after about a second without completion
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    long long t0 = 0;
+    for (unsigned it = 0;; ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (it == 0) t0 = global_ns();
+        else if ((it & 63) == 0 && global_ns() - t0 > 1000000000LL) return false;
+    }
+}
+// one TMA tile (32 columns x rows) of A into shared memory, completing on `bar`
+__device__ __forceinline__ void tma_load_tile(const CUtensorMap* tm, unsigned long long* bar, float* dst, int x,
+                                              int y, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+enum : int { MX_W = 0, MX_H = 1, MX_DOWN = 2 };
+
+template <int KIND>
+__host__ __device__ __forceinline__ void mx_shape(int s, int& rows_item, int& K) {
+    if (KIND == MX_W) { rows_item = 4 * s; K = 4 * s; }
+    else if (KIND == MX_H) { rows_item = 8 * s; K = 2 * s; }
+    else { rows_item = 4 * s; K = 8 * s; }
+}
+
+
+}  // namespace
+}  // namespace efgb

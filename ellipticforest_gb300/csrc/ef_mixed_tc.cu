@@ -1,0 +1,667 @@
+// Tensor-core (tcgen05) form of the mixed solver's node GEMMs Y[rows][B] = A[rows][K] X[K][B]
+// (the FP32 passes' mergeW / mergeH / applyS products, HPSAlgorithm.hpp:1059-1117, :1194-1230).
+//
+// Precision.  The operators are FP32; each entry a is split once, at set-up, into three bf16 parts
+// a = a1 + a2 + a3 (round to nearest at every step: a1 = bf16(a), a2 = bf16(a - a1),
+// a3 = bf16(a - a1 - a2); the three 8-bit significands cover FP32's 24 bits, so the sum is exact),
+// and the request block X the same way as it is staged.  Every product is formed from the six
+// partial products that reach 2^-24 of |a x|:
+//     D_hi += a1 x1                                  (TMEM accumulator 1)
+//     D_lo += a1 x2 + a2 x1 + a1 x3 + a2 x2 + a3 x1   (TMEM accumulator 2)
+// with tcgen05.mma kind::f16 (bf16 inputs, exact products, FP32 accumulation); y = D_hi + D_lo.
+// Keeping the small terms in their own accumulator stops them from being rounded against the large
+// running sum.  The dropped terms a2 x3, a3 x2, a3 x3 are below 2^-24 |a x|: the result carries the
+// error of an FP32 FMA chain, which the one FP64 refinement sweep is sized for (a 3-pass split-TF32
+// would round each product to ~2^-21).
+//
+// Layout.  The three planes of a group's operators (one back-to-back row-major matrix per kind, H
+// with each child's two runs of s rows made adjacent) are streamed by TMA in boxes of 128 rows x
+// 64 columns (one 128-byte swizzle row of bf16) -- the canonical K-major SWIZZLE_128B operand of
+// the MMA.  X is read as FP32 from the pass buffers ([K][B], requests fastest), split, and written
+// to shared memory in the same swizzled K-major form by the producer warps.  A tile is 128 rows; a
+// tile whose rows use several right-hand-side blocks (nodes of 4s < 128 rows, or the compact H's
+// four children) puts the blocks side by side in N (32 requests each) and keeps each row's own
+// block in the epilogue.
+//
+// Roles (192 threads): warps 0-3 stage X and run the epilogue (warp w reads TMEM lanes 32w..32w+31),
+// warp 4 allocates TMEM and lane 0 issues the TMA loads, warp 5 lane 0 issues the MMAs.  Stages
+// are handed over through mbarriers; the MMA issuer frees a stage with tcgen05.commit.  Every wait
+// gives up after about one second: the kernel then sets the error word, lets its copies and MMAs in
+// flight finish (bounded waits), frees its TMEM and returns.
+#include <cooperative_groups.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <stdexcept>
+
+#include "ef_kernels.cuh"
+#include "ef_mixed_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace efgb {
+
+namespace {
+
+constexpr int kTM = 128;                  // rows per tile (MMA M)
+constexpr int kTK = 64;                   // K per stage: 64 bf16 = one 128-byte swizzle row
+constexpr int kTB = 32;                   // requests per right-hand-side block (MMA N per block)
+constexpr int kPlaneA = kTM * kTK * 2;    // bytes of one A plane per stage (16 KB)
+constexpr int kPlaneX = kTB * kTK * 2;    // bytes of one X plane per block per stage (4 KB)
+constexpr int kTcThreads = 192;
+constexpr int kMaxSeg = 4;
+
+struct TcShape {
+    int rows_item, K, seg_rows, nseg;
+};
+
+__host__ __device__ inline TcShape tc_shape(int kind, int s) {
+    TcShape t;
+    if (kind == MX_W) { t.rows_item = 4 * s; t.K = 4 * s; t.seg_rows = 4 * s; }
+    else if (kind == MX_H) { t.rows_item = 8 * s; t.K = 2 * s; t.seg_rows = 2 * s; }
+    else { t.rows_item = 4 * s; t.K = 8 * s; t.seg_rows = 4 * s; }
+    t.nseg = t.seg_rows >= kTM ? 1 : kTM / t.seg_rows;
+    return t;
+}
+
+__host__ __device__ inline int tc_stages(int nseg) { return nseg <= 2 ? 3 : 2; }
+__host__ __device__ inline int tc_stage_bytes(int nseg) { return 3 * kPlaneA + 3 * nseg * kPlaneX; }
+inline size_t tc_smem_bytes(int nseg) {
+    return 1024 + size_t(tc_stages(nseg)) * tc_stage_bytes(nseg) + 256;
+}
+__host__ __device__ inline int tc_tmem_cols(int nseg) {
+    const int need = 2 * kTB * nseg;
+    return need <= 64 ? 64 : (need <= 128 ? 128 : 256);
+}
+
+// compact H row order of the planes: child c's rows [2s c, 2s c + 2s) are its W/E run and then its
+// S/N run; returns the row p of the WESN compact H (the exterior index) of permuted row pr
+__host__ __device__ inline int tc_h_unpermute(int pr, int s) {
+    const int c = pr / (2 * s), k = pr - c * 2 * s;
+    const int run = k >= s ? 1 : 0, o = k - run * s;
+    // alpha: W[0,s) S[4s,5s); beta: E[2s,3s) S[5s,6s); gamma: W[s,2s) N[6s,7s); omega: E[3s,4s) N[7s,8s)
+    const int base0[4] = {0, 2, 1, 3}, base1[4] = {4, 5, 6, 7};
+    return (run ? base1[c] : base0[c]) * s + o;
+}
+
+// ---- tcgen05 / TMEM wrappers ---------------------------------------------------------------------
+__device__ __forceinline__ void tmem_alloc(unsigned* dst, unsigned ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(dst)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// shared-memory matrix descriptor of a K-major SWIZZLE_128B operand: rows of 128 bytes, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1, swizzle mode 2 (128 bytes)
+__device__ __forceinline__ uint64_t tc_desc(unsigned saddr) {
+    uint64_t d = uint64_t((saddr & 0x3FFFFu) >> 4);
+    d |= uint64_t(1) << 16;            // leading byte offset (unused by swizzled K-major layouts)
+    d |= uint64_t(1024 >> 4) << 32;    // stride byte offset
+    d |= uint64_t(1) << 46;            // fixed constant 0b001
+    d |= uint64_t(2) << 61;            // 128-byte swizzle
+    return d;
+}
+// instruction descriptor of kind::f16: D FP32, A and B bf16, both K-major, M x N
+__host__ __device__ constexpr unsigned tc_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (unsigned(N >> 3) << 17) | (unsigned(M >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(unsigned dtmem, uint64_t a, uint64_t b, unsigned idesc, unsigned acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+// arrive on `bar` once every MMA this thread issued so far has completed
+__device__ __forceinline__ void tc_commit(unsigned long long* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 32 consecutive FP32 columns of the calling warp's 32 TMEM lanes (one lane per thread)
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false after about a second (raising the CTA's abort flag) or when another role of
+// the CTA has already given up
+__device__ __forceinline__ bool tc_wait(unsigned long long* bar, unsigned parity, volatile int* abort) {
+    long long t0 = 0;
+    for (unsigned it = 0;; ++it) {
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 31) == 0) {
+            if (*abort) return false;
+            if (it == 0) t0 = global_ns();
+            else if (global_ns() - t0 > 1000000000LL) {
+                *abort = 1;
+                return false;
+            }
+        }
+    }
+}
+__device__ __forceinline__ void tma_load_bf16(const CUtensorMap* tm, unsigned long long* bar, void* dst, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// bf16 parts of x (round to nearest at each step): x = p0 + p1 + p2 for every finite FP32 x
+__device__ __forceinline__ void split3(float x, __nv_bfloat16& p0, __nv_bfloat16& p1, __nv_bfloat16& p2) {
+    p0 = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p0);
+    p1 = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(p1);
+    p2 = __float2bfloat16_rn(r2);
+}
+__device__ __forceinline__ unsigned pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return unsigned(__bfloat16_as_ushort(lo)) | (unsigned(__bfloat16_as_ushort(hi)) << 16);
+}
+
+// right-hand-side block of segment `gseg` of a group (W, DOWN: one per node; H: one per child)
+struct TcSeg {
+    const float* X1;  // rows k < kb
+    const float* X2;  // rows k >= kb (indexed with the same k)
+    int kb;
+};
+template <int KIND>
+__device__ __forceinline__ TcSeg tc_seg(const MixItem* __restrict__ items, int s, int B, int gseg) {
+    TcSeg t;
+    if (KIND == MX_W) { t.X1 = items[gseg].hd; t.X2 = t.X1; t.kb = 4 * s; }
+    else if (KIND == MX_DOWN) { t.X1 = items[gseg].gf; t.X2 = t.X1; t.kb = 8 * s; }
+    else {
+        const MixItem& it = items[gseg >> 2];
+        int Ia, Ib;
+        mx_child_ifaces(gseg & 3, Ia, Ib);
+        t.X1 = it.w + (long long)Ia * s * B;
+        t.X2 = it.w + (long long)(Ib - 1) * s * B;  // row k >= s of [w_Ia; w_Ib] is w_Ib[k - s]
+        t.kb = s;
+    }
+    return t;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_mx_umma(const __grid_constant__ CUtensorMap tmA, const MixItem* __restrict__ items, int s, int B, int cnt,
+              int ksplit, int ntiles, int* __restrict__ err) {
+    const TcShape sh = tc_shape(KIND, s);
+    const int nseg = sh.nseg, K = sh.K, R = cnt * sh.rows_item;
+    const int nsegs_total = KIND == MX_H ? 4 * cnt : cnt;
+    const int NS = tc_stages(nseg), SB = tc_stage_bytes(nseg);
+    const int ncol = kTB * nseg, tcols = tc_tmem_cols(nseg);
+    const unsigned idesc = tc_idesc(kTM, ncol);
+    extern __shared__ unsigned char tc_smem[];
+    unsigned char* base = tc_smem + ((1024u - (smem_u32(tc_smem) & 1023u)) & 1023u);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(base + size_t(NS) * SB);
+    unsigned long long* a_full = bars;             // [NS] TMA transaction barriers
+    unsigned long long* x_full = bars + NS;        // [NS] 128 producer arrivals
+    unsigned long long* empty = bars + 2 * NS;     // [NS] MMA commit
+    unsigned long long* acc_full = bars + 3 * NS;  // MMA commit at the end of a unit
+    unsigned long long* acc_empty = acc_full + 1;  // 128 epilogue arrivals
+    unsigned long long* drain = acc_full + 2;      // MMA commit before TMEM is freed
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(acc_full + 3);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nkc = (K + kTK - 1) / kTK;
+    int first_tile, tile_step, nunits, cpu, cbase;
+    if (ksplit > 1) {
+        const int kp = blockIdx.x % ksplit, cpp = (nkc + ksplit - 1) / ksplit;
+        first_tile = blockIdx.x / ksplit;
+        tile_step = 0;
+        nunits = 1;
+        cbase = min(nkc, kp * cpp);
+        cpu = min(nkc, cbase + cpp) - cbase;
+    } else {
+        first_tile = blockIdx.x;
+        tile_step = gridDim.x;
+        nunits = first_tile < ntiles ? (ntiles - 1 - first_tile) / tile_step + 1 : 0;
+        cbase = 0;
+        cpu = nkc;
+    }
+    if (cpu <= 0) nunits = 0;
+    const int b0 = blockIdx.y * kTB;
+
+    if (tid == 0) {
+        for (int i = 0; i < NS; ++i) {
+            mbar_init(&a_full[i], 1);
+            mbar_init(&x_full[i], 128);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, 128);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    if (warp == 4) {
+        tmem_alloc(tmem_slot, unsigned(tcols));
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tmem_slot;
+
+    // per unit: the tile's rows [128 t, 128 t + 128) of the group and its first segment
+    auto tile_of = [&](int u) { return first_tile + u * tile_step; };
+    auto seg0_of = [&](int t) { return sh.seg_rows >= kTM ? (t * kTM) / sh.seg_rows : t * nseg; };
+
+    if (warp == 4) {
+        // ---- TMA producer: the three A planes of every stage ----
+        if (lane == 0) {
+            int st = 0;
+            unsigned ph = 0;
+            int issued = 0;
+            bool ok = true;
+            for (int u = 0; u < nunits && ok; ++u) {
+                const int row0 = tile_of(u) * kTM;
+                for (int c = 0; c < cpu && ok; ++c) {
+                    if (issued >= NS) ok = tc_wait(&empty[st], ph ^ 1u, abort_flag);
+                    if (!ok) break;
+                    unsigned char* sa = base + size_t(st) * SB;
+                    mbar_expect_tx(&a_full[st], 3u * kPlaneA);
+                    for (int p = 0; p < 3; ++p)
+                        tma_load_bf16(&tmA, &a_full[st], sa + p * kPlaneA, (cbase + c) * kTK, p * R + row0);
+                    ++issued;
+                    if (++st == NS) { st = 0; ph ^= 1u; }
+                }
+            }
+            if (!ok) {
+                // let the loads still in flight land before the shared memory goes away
+                int s2 = 0;
+                unsigned p2 = 0;
+                const int first = issued > NS ? issued - NS : 0;
+                for (int v = 0; v < issued; ++v) {
+                    if (v >= first) (void)tc_wait(&a_full[s2], p2, reinterpret_cast<volatile int*>(&first) /* never set */);
+                    if (++s2 == NS) { s2 = 0; p2 ^= 1u; }
+                }
+                atomicExch(err, 1);
+            }
+        }
+    } else if (warp == 5) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            int st = 0;
+            unsigned ph = 0;
+            bool ok = true;
+            const uint32_t a_base = smem_u32(base);
+            for (int u = 0; u < nunits && ok; ++u) {
+                if (u > 0) ok = tc_wait(acc_empty, unsigned(u - 1) & 1u, abort_flag);
+                for (int c = 0; c < cpu && ok; ++c) {
+                    ok = tc_wait(&a_full[st], ph, abort_flag) && tc_wait(&x_full[st], ph, abort_flag);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint32_t sa = a_base + uint32_t(st) * SB;
+                    const uint32_t sx = sa + 3u * kPlaneA;
+                    const int kleft = K - (cbase + c) * kTK;
+                    const int nk = kleft >= kTK ? kTK / 16 : (kleft + 15) / 16;
+                    for (int kk = 0; kk < nk; ++kk) {
+                        const uint32_t ko = uint32_t(kk) * 32u;
+                        const uint64_t a1 = tc_desc(sa + ko), a2 = tc_desc(sa + kPlaneA + ko),
+                                       a3 = tc_desc(sa + 2 * kPlaneA + ko);
+                        const uint32_t xp = uint32_t(nseg) * kPlaneX;
+                        const uint64_t x1 = tc_desc(sx + ko), x2 = tc_desc(sx + xp + ko), x3 = tc_desc(sx + 2 * xp + ko);
+                        const unsigned acc = (c > 0 || kk > 0) ? 1u : 0u;
+                        tc_mma(tmem, a1, x1, idesc, acc);
+                        tc_mma(tmem + unsigned(ncol), a1, x2, idesc, acc);
+                        tc_mma(tmem + unsigned(ncol), a2, x1, idesc, 1u);
+                        tc_mma(tmem + unsigned(ncol), a1, x3, idesc, 1u);
+                        tc_mma(tmem + unsigned(ncol), a2, x2, idesc, 1u);
+                        tc_mma(tmem + unsigned(ncol), a3, x1, idesc, 1u);
+                    }
+                    tc_commit(&empty[st]);
+                    if (++st == NS) { st = 0; ph ^= 1u; }
+                }
+                if (ok) tc_commit(acc_full);
+            }
+            // every MMA issued has completed before TMEM is freed
+            tc_commit(drain);
+            int never = 0;
+            if (!tc_wait(drain, 0u, reinterpret_cast<volatile int*>(&never))) atomicExch(err, 1);
+            if (!ok) atomicExch(err, 1);
+        }
+    } else {
+        // ---- warps 0-3: stage X (split into bf16 planes), then the epilogue of each unit ----
+        const int t = tid;  // 0..127 = TMEM lane of this thread's tile row
+        int st = 0;
+        unsigned ph = 0;
+        int staged = 0;
+        bool ok = true;
+        const bool vec = (B & 3) == 0;
+        for (int u = 0; u < nunits && ok; ++u) {
+            const int tile = tile_of(u);
+            const int gs0 = seg0_of(tile);
+            TcSeg seg[kMaxSeg];
+            bool sval[kMaxSeg];
+#pragma unroll
+            for (int j = 0; j < kMaxSeg; ++j) {
+                sval[j] = j < nseg && gs0 + j < nsegs_total;
+                if (sval[j]) seg[j] = tc_seg<KIND>(items, s, B, gs0 + j);
+            }
+            for (int c = 0; c < cpu && ok; ++c) {
+                if (staged >= NS) ok = tc_wait(&empty[st], ph ^ 1u, abort_flag);
+                if (!ok) break;
+                unsigned char* sx = base + size_t(st) * SB + 3 * kPlaneA;
+                const int k0 = (cbase + c) * kTK;
+                const int b = t & 31, n = b;
+                const int gb = b0 + b;
+                // pairs (k, k + 1) of one request: 32 per block, four pair rows per pass of the warps
+                for (int i = 0; i < 8 * nseg; ++i) {
+                    const int P = (t >> 5) + 4 * i;
+                    const int j = P >> 5, kp = P & 31;
+                    const int k = k0 + 2 * kp;
+                    float x0 = 0.f, x1 = 0.f;
+                    if (sval[j] && gb < B) {
+                        const TcSeg& sg = seg[j];
+                        if (k < K) x0 = (k < sg.kb ? sg.X1 : sg.X2)[(long long)k * B + gb];
+                        if (k + 1 < K) x1 = (k + 1 < sg.kb ? sg.X1 : sg.X2)[(long long)(k + 1) * B + gb];
+                    }
+                    __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
+                    split3(x0, p0a, p1a, p2a);
+                    split3(x1, p0b, p1b, p2b);
+                    const int kl = 2 * kp;
+                    const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
+                                         ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
+                    const unsigned xp = unsigned(nseg) * kPlaneX;
+                    *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
+                    *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
+                    *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+                }
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                mbar_arrive(&x_full[st]);
+                ++staged;
+                if (++st == NS) { st = 0; ph ^= 1u; }
+            }
+            if (!ok) break;
+            // ---- epilogue of the unit ----
+            ok = tc_wait(acc_full, unsigned(u) & 1u, abort_flag);
+            if (!ok) break;
+            tc_fence_after();
+            const int jrow = sh.seg_rows >= kTM ? 0 : t / sh.seg_rows;
+            float hi[32], lo[32];
+            const unsigned lane_off = unsigned(warp * 32) << 16;
+            tmem_ld32(tmem + lane_off + unsigned(jrow * kTB), hi);
+            tmem_ld32(tmem + lane_off + unsigned(ncol + jrow * kTB), lo);
+            tc_fence_before();
+            mbar_arrive(acc_empty);  // the accumulators may be overwritten by the next unit
+            float v[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) v[q] = hi[q] + lo[q];
+
+            if (ksplit > 1) {
+                // partial tiles -> rank 0 of the cluster through distributed shared memory, in rank
+                // order (deterministic); the stage memory is free once every MMA has completed
+                float* red = reinterpret_cast<float*>(base);
+#pragma unroll
+                for (int q = 0; q < 32; q += 4)
+                    *reinterpret_cast<float4*>(red + t * 32 + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+            }
+            if (ksplit > 1) break;  // the cluster reduction and the epilogue follow below
+
+            // ---- stores ----
+            const int grow = tile * kTM + t;
+            if (grow < R) {
+                const int item = grow / sh.rows_item, r = grow - item * sh.rows_item;
+                const MixItem& it = items[item];
+                const long long cb = (long long)b0;
+                if (KIND == MX_W) {
+                    float* dst = it.w + (long long)r * B + cb;
+                    if (vec) {
+#pragma unroll
+                        for (int q = 0; q < 32; q += 4)
+                            if (b0 + q < B) *reinterpret_cast<float4*>(dst + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                    } else {
+                        for (int q = 0; q < 32; ++q)
+                            if (b0 + q < B) dst[q] = v[q];
+                    }
+                } else if (KIND == MX_H) {
+                    const int p = tc_h_unpermute(r, s);
+                    int c, q2;
+                    mx_ext_map(p, s, c, q2);
+                    const float* hp = it.hc[c] + (long long)q2 * B + cb;
+                    float* dst = it.h + (long long)p * B + cb;
+                    for (int q = 0; q < 32; ++q)
+                        if (b0 + q < B) dst[q] = v[q] + hp[q];
+                } else {
+                    const int I = r / s, o = r - (r / s) * s;
+                    const float* wp = it.w + (long long)r * B + cb;
+                    float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
+                    float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
+                    double* ug = it.uG + (long long)r * B + cb;
+                    for (int q = 0; q < 32; ++q)
+                        if (b0 + q < B) {
+                            const float uv = v[q] + wp[q];
+                            d0[q] = uv;
+                            d1[q] = uv;
+                            ug[q] += f2d_bits(uv);
+                        }
+                }
+            }
+            if (KIND == MX_DOWN && blockIdx.y == 0) {
+                // exterior points of the parent go to the children unchanged: this tile copies its
+                // share of the exterior rows of the nodes it covers
+                const int rows = 8 * s;
+                int i0, i1, p0, p1;
+                if (sh.rows_item >= kTM) {
+                    const int tpi = sh.rows_item / kTM, item = tile / tpi, tl = tile - item * tpi;
+                    const int per = (rows + tpi - 1) / tpi;
+                    i0 = item; i1 = item + 1; p0 = tl * per; p1 = min(rows, p0 + per);
+                } else {
+                    const int ipt = kTM / sh.rows_item;
+                    i0 = tile * ipt; i1 = min(cnt, i0 + ipt); p0 = 0; p1 = rows;
+                }
+                for (int item = i0; item < i1; ++item) {
+                    const MixItem& it = items[item];
+                    const int tot = (p1 - p0) * B;
+                    for (int e = t; e < tot; e += 128) {
+                        const int p = p0 + e / B, bb = e - (e / B) * B;
+                        int c, q2;
+                        mx_ext_map(p, s, c, q2);
+                        it.gc[c][(long long)q2 * B + bb] = it.gf[(long long)p * B + bb];
+                    }
+                }
+            }
+        }
+        if (!ok) atomicExch(err, 1);
+    }
+
+    // ---- K split: rank 0 of the cluster adds the partial tiles and runs the epilogue ----
+    if (ksplit > 1) {
+        cg::cluster_group cluster = cg::this_cluster();
+        cluster.sync();
+        if (cluster.block_rank() == 0 && tid < 128 && nunits > 0 && !*abort_flag) {
+            const int t = tid;
+            float* red = reinterpret_cast<float*>(base);
+            float v[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) v[q] = red[t * 32 + q];
+            for (int rk = 1; rk < ksplit; ++rk) {
+                const float* rr = cluster.map_shared_rank(red, rk);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) v[q] += rr[t * 32 + q];
+            }
+            const int tile = first_tile;
+            const int grow = tile * kTM + t;
+            if (grow < R) {
+                const int item = grow / sh.rows_item, r = grow - item * sh.rows_item;
+                const MixItem& it = items[item];
+                const long long cb = (long long)b0;
+                if (KIND == MX_W) {
+                    float* dst = it.w + (long long)r * B + cb;
+                    for (int q = 0; q < 32; ++q)
+                        if (b0 + q < B) dst[q] = v[q];
+                } else if (KIND == MX_H) {
+                    const int p = tc_h_unpermute(r, s);
+                    int c, q2;
+                    mx_ext_map(p, s, c, q2);
+                    const float* hp = it.hc[c] + (long long)q2 * B + cb;
+                    float* dst = it.h + (long long)p * B + cb;
+                    for (int q = 0; q < 32; ++q)
+                        if (b0 + q < B) dst[q] = v[q] + hp[q];
+                } else {
+                    const int I = r / s, o = r - (r / s) * s;
+                    const float* wp = it.w + (long long)r * B + cb;
+                    float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
+                    float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
+                    double* ug = it.uG + (long long)r * B + cb;
+                    for (int q = 0; q < 32; ++q)
+                        if (b0 + q < B) {
+                            const float uv = v[q] + wp[q];
+                            d0[q] = uv;
+                            d1[q] = uv;
+                            ug[q] += f2d_bits(uv);
+                        }
+                }
+            }
+            if (KIND == MX_DOWN && blockIdx.y == 0) {
+                const int rows = 8 * s;
+                const int tpi = sh.rows_item >= kTM ? sh.rows_item / kTM : 1;
+                const int item = sh.rows_item >= kTM ? tile / tpi : tile, tl = sh.rows_item >= kTM ? tile - item * tpi : 0;
+                const int per = (rows + tpi - 1) / tpi;
+                const int p0 = tl * per, p1 = min(rows, p0 + per);
+                if (item < cnt) {
+                    const MixItem& it = items[item];
+                    const int tot = (p1 - p0) * B;
+                    for (int e = t; e < tot; e += 128) {
+                        const int p = p0 + e / B, bb = e - (e / B) * B;
+                        int c, q2;
+                        mx_ext_map(p, s, c, q2);
+                        it.gc[c][(long long)q2 * B + bb] = it.gf[(long long)p * B + bb];
+                    }
+                }
+            }
+        }
+        cluster.sync();
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 4) tmem_dealloc(tmem, unsigned(tcols));
+}
+
+// A planes of one group: dst[p][R][K] (bf16) with src[R][K] = dst[0] + dst[1] + dst[2]; H rows in the
+// child-major order of tc_h_unpermute
+__global__ void k_tc_split(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, long long R, int K,
+                           int s, int permute_h) {
+    const long long tot = R * K;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long row = e / K;
+        const int k = int(e - row * K);
+        long long srow = row;
+        if (permute_h) {
+            const long long node = row / (8 * s);
+            const int pr = int(row - node * 8 * s);
+            srow = node * 8 * s + tc_h_unpermute(pr, s);
+        }
+        __nv_bfloat16 p0, p1, p2;
+        split3(src[srow * K + k], p0, p1, p2);
+        dst[e] = p0;
+        dst[tot + e] = p1;
+        dst[2 * tot + e] = p2;
+    }
+}
+
+template <int KIND>
+void launch_umma(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int cnt, int s, int B, int* err,
+                 int ksplit) {
+    const TcShape sh = tc_shape(KIND, s);
+    const long long R = (long long)cnt * sh.rows_item;
+    const int ntiles = int((R + kTM - 1) / kTM);
+    const int chunks = (B + kTB - 1) / kTB;
+    const size_t smem = tc_smem_bytes(sh.nseg);
+    cudaFuncSetAttribute(k_mx_umma<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned gx;
+    if (ksplit > 1) gx = unsigned(ntiles * ksplit);
+    else gx = unsigned(std::max(1, std::min(ntiles, std::max(1, sms / chunks))));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(gx, unsigned(chunks));
+    cfg.blockDim = dim3(kTcThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(ksplit);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = ksplit > 1 ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k_mx_umma<KIND>, tm, items, s, B, cnt, ksplit, ntiles, err);
+    ++g_kernel_launches;
+}
+
+}  // namespace
+
+bool mx_tc_supported(int kind, int s) {
+    // s a power of two >= 16: K a multiple of 16, each right-hand-side block a power-of-two number
+    // of rows of at least 32, at most four blocks per tile
+    if (s < 16 || (s & (s - 1)) != 0) return false;
+    const TcShape sh = tc_shape(kind, s);
+    return sh.nseg <= kMaxSeg && sh.K % 16 == 0;
+}
+
+int mx_tc_max_split(int kind, int s) {
+    const TcShape sh = tc_shape(kind, s);
+    const int nkc = (sh.K + kTK - 1) / kTK;
+    int k = 1;
+    while (k < 8 && nkc / (2 * k) >= 2) k *= 2;
+    return k;
+}
+
+void mx_tc_split(cudaStream_t st, int kind, const float* src, void* dst, long long R, int K, int s) {
+    const long long tot = R * K;
+    const int grid = int(std::min<long long>((tot + 255) / 256, 8192));
+    k_tc_split<<<grid, 256, 0, st>>>(src, reinterpret_cast<__nv_bfloat16*>(dst), R, K, s, kind == MX_H ? 1 : 0);
+    ++g_kernel_launches;
+}
+
+void mx_gemm_tc(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
+                int* err, int ksplit) {
+    if (!mx_tc_supported(kind, s)) throw std::invalid_argument("tensor-core node GEMM: unsupported interface size");
+    if (ksplit < 1) ksplit = 1;
+    if (kind == MX_W) launch_umma<MX_W>(st, tm, items, nitems, s, B, err, ksplit);
+    else if (kind == MX_H) launch_umma<MX_H>(st, tm, items, nitems, s, B, err, ksplit);
+    else launch_umma<MX_DOWN>(st, tm, items, nitems, s, B, err, ksplit);
+}
+
+}  // namespace efgb

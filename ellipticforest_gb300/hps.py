@@ -281,6 +281,27 @@ class Mesh:
         check(_lib.load().ef_mesh_num_leaves(self._h, C.byref(v)))
         return v.value
 
+    # -- subtree split (no reference counterpart in this form; see subtree.py) -------------------
+    def level_count(self, level: int) -> int:
+        """Number of tree nodes at `level`."""
+        v = C.c_int()
+        check(_lib.load().ef_mesh_level_count(self._h, int(level), C.byref(v)))
+        return v.value
+
+    def subtree(self, level: int, index: int) -> "Mesh":
+        """The mesh of the subtree under the index-th node of `level` (z-order): its root patch is that
+        node's patch and every leaf patch box is this mesh's, bit for bit."""
+        h = C.c_void_p()
+        check(_lib.load().ef_mesh_subtree(self._h, int(level), int(index), C.byref(h)))
+        sub = Mesh()
+        sub._h = h
+        n = self.root_patch.grid().nx()
+        boxes = np.array([sub.leaf(k)[3] for k in range(sub.num_leaves())])
+        sub.root_patch = FiniteVolumePatch(FiniteVolumeGrid(n, boxes[:, 0].min(), boxes[:, 1].max(), n,
+                                                            boxes[:, 2].min(), boxes[:, 3].max()))
+        sub.patches = [FiniteVolumePatch(FiniteVolumeGrid(n, b[0], b[1], n, b[2], b[3])) for b in boxes]
+        return sub
+
     # -- VTK output (Mesh.hpp:357-424) -------------------------------------------------------------
     def addMeshFunction(self, values, name: Optional[str] = None):
         """Cell data for toVTK: an array in leaf order (cell j + i*n, e.g. HPSAlgorithm.leaf_solution())
@@ -462,6 +483,46 @@ class HPSAlgorithm:
         n = C.c_int()
         check(_lib.load().ef_hps_build_from(self._h, old._h, C.byref(n)))
         return n.value
+
+    # -- top of a subtree split (no reference counterpart in this form; see subtree.py) ----------
+    def split_sizes(self, level: int):
+        """4m per node of `level` (z-order): the length of its h and g; its T is 4m x 4m."""
+        cnt = self.mesh.level_count(level)
+        v = (C.c_int * cnt)()
+        check(_lib.load().ef_hps_split_sizes(self._h, int(level), v))
+        return list(v)
+
+    def buildStageTop(self, level: int, T_blocks):
+        """Merges of levels level-1 .. 0 from the root T of every level-`level` subtree."""
+        self._apply_options()
+        blocks = [np.ascontiguousarray(T, dtype=np.float64) for T in T_blocks]
+        arr = (C.c_void_p * len(blocks))(*[b.ctypes.data for b in blocks])
+        check(_lib.load().ef_hps_build_top(self._h, int(level), arr))
+
+    def upwardsStageTop(self, level: int, h_blocks):
+        """Upward pass of levels level-1 .. 0 from the root h of every level-`level` subtree."""
+        blocks = [np.ascontiguousarray(h, dtype=np.float64) for h in h_blocks]
+        arr = (C.c_void_p * len(blocks))(*[b.ctypes.data for b in blocks])
+        check(_lib.load().ef_hps_upwards_top(self._h, int(level), arr))
+
+    def solveStageTop(self, level: int, a, b, r):
+        """Root data a u + b du/dn = r, downward pass to `level`: the Dirichlet data of every
+        level-`level` subtree (list of arrays)."""
+        a, b, r = (np.ascontiguousarray(v, dtype=np.float64) for v in (a, b, r))
+        gs = [np.empty(m) for m in self.split_sizes(level)]
+        arr = (C.c_void_p * len(gs))(*[g.ctypes.data for g in gs])
+        check(_lib.load().ef_hps_solve_top(self._h, int(level), dptr(a), dptr(b), dptr(r), arr))
+        return gs
+
+    def root_data(self, bc):
+        """(a, b, r) of bc(side, x, y) -> (r, a, b) at the root face centres (HPSAlgorithm.hpp:375-400)."""
+        rs, as_, bs = [], [], []
+        for side, (x, y) in enumerate(self.boundary_points()):
+            r, a, b = bc(side, x, y)
+            rs.append(np.broadcast_to(np.asarray(r, dtype=np.float64), x.shape))
+            as_.append(np.broadcast_to(np.asarray(a, dtype=np.float64), x.shape))
+            bs.append(np.broadcast_to(np.asarray(b, dtype=np.float64), x.shape))
+        return np.concatenate(as_), np.concatenate(bs), np.concatenate(rs)
 
     def buildStageMixed(self, fp64_levels: int = 3):
         """Mixed-precision build (no counterpart in the reference): FP32 merges with the interface

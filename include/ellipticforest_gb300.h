@@ -213,6 +213,40 @@ int ef_fv5_map_d2n(int n, double x_lower, double x_upper, double y_lower, double
                    const double* alpha, const double* beta, const double* lambda,
                    const double* g_host, const double* f_host, double* h_host);
 
+/* ---- Subtree split across processes ---------------------------------------------------------- */
+
+/* The reference builds and solves one tree over MPI ranks: at the process boundary merge4to1 first
+ * broadcasts the children a rank does not own (src/Quadtree.hpp:470-496 merge, :146-148 broadcast of
+ * the patch) and split1to4 sends them back down.  Here the split is by subtrees: with 4^level
+ * processes, process p builds, upward-passes and solves the subtree under node p of `level` (in
+ * z-order) as a tree of its own (ef_mesh_subtree + the usual ef_hps_* calls), and one process
+ * runs the top `level` levels on a handle of the full mesh from the gathered level-`level`
+ * operators.  Results equal a single-handle build and solve bit for bit.  Transport of T, h and g
+ * between processes is the caller's (NCCL, peer copies or host memory).
+ *
+ * ef_mesh_level_count: number of nodes at `level`.  ef_mesh_subtree: the mesh of the subtree under
+ * the index-th node of `level`; its root box is that node's box and every patch box is the full
+ * mesh's, bit for bit. */
+int ef_mesh_level_count(const ef_mesh* mesh, int level, int* count);
+int ef_mesh_subtree(const ef_mesh* mesh, int level, int index, ef_mesh** out);
+
+/* On a handle of the full mesh (every leaf below `level`):
+ * ef_hps_split_sizes: 4m for every node of `level` in z-order (the length of its h and g; its T is
+ *   4m x 4m, row-major, WESN) -- the root side of the matching subtree handle is m.
+ * ef_hps_build_top: the merges of levels level-1 .. 0 (HPSAlgorithm.hpp:120-161 above the split)
+ *   from T[k] = root T of subtree k (ef_hps_get_root_T of its handle).
+ * ef_hps_upwards_top: the upward pass of levels level-1 .. 0 (HPSAlgorithm.hpp:178-272 above the
+ *   split) from h[k] = root h of subtree k after its upwards stage (ef_hps_get_root_h).
+ * ef_hps_solve_top: root data a u + b du/dn = r (4M each, as ef_hps_solve), then the downward pass
+ *   to `level`: g[k] receives the Dirichlet data of subtree k (4m), which its handle solves with
+ *   ef_hps_solve_root_dirichlet.
+ * A handle built this way accepts only the *_top calls (others return EF_ERR_STATE) until a
+ * regular build stage runs on it. */
+int ef_hps_split_sizes(ef_hps* h, int level, int* sizes);
+int ef_hps_build_top(ef_hps* h, int level, const double* const* T);
+int ef_hps_upwards_top(ef_hps* h, int level, const double* const* hv);
+int ef_hps_solve_top(ef_hps* h, int level, const double* a, const double* b, const double* r, double* const* g);
+
 /* ---- Single patch without allocation -------------------------------------------------------- */
 
 /* No counterpart in the reference.  The solve of ef_fv_solve for callers that cannot allocate

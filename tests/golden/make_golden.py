@@ -6,14 +6,16 @@ Reads (as text, nothing is compiled or run):
   * test/test_matrix.cpp:270-300            -- blockPermute known answer
   * test/test_finite_volume_grid.cpp:30-49  -- cell-centre coordinates
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py /path/to/reference-checkout
 """
 import json
 import re
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py /path/to/reference-checkout")
+REF = Path(sys.argv[1])
 OUT = Path(__file__).with_name("reference_known_answers.json")
 
 
