@@ -319,6 +319,8 @@ int ef_hps_set_option(ef_hps* h, const char* key, int value) {
         h->hps->set_homogeneous_rhs(value != 0);
     } else if (k == "cuda-graphs") {
         h->hps->set_graphs(value != 0);
+    } else if (k == "tensor-cores") {
+        h->hps->set_tensor_cores(value != 0);  // block solvers created from now on
     } else if (k == "cooperative-lu") {
         efgb::g_cooperative_lu.store(value != 0);  // process-wide
     } else {

@@ -190,6 +190,9 @@ public:
     // CUDA-graph replay of the solve sequences (on by default; profiling runs them eagerly)
     void set_graphs(bool on) { graphs_ = on; }
     bool graphs() const { return graphs_; }
+    // tcgen05 node GEMMs in the mixed solver (default on; block solvers created afterwards follow it)
+    void set_tensor_cores(bool on) { tensor_cores_ = on; }
+    bool tensor_cores() const { return tensor_cores_; }
     // FivePointStencil: per-leaf coefficients sampled at the reference's points (host arrays in leaf
     // order: alpha n*n, beta 4*n*n (W, E, S, N face of every cell), lambda n*n per leaf)
     void set_coefficients(const double* alpha, const double* beta, const double* lambda);
@@ -364,6 +367,8 @@ private:
 
     bool prof_ = false;
     bool graphs_ = true;
+    bool tensor_cores_ = true;
+    bool mx_split_tc_ = false;  // mx_split_ was tuned with the tensor-core path
     // K split of the mixed form's node GEMMs per group and kind (W, H, DOWN), chosen once per tree by
     // MixedSolver::tune and shared by every block solver of the tree
     std::vector<std::array<int, 3>> mx_split_;
@@ -428,6 +433,10 @@ private:
         MixConv* d_conv = nullptr;
         float *S32 = nullptr, *Xi32 = nullptr, *H32 = nullptr;
         CUtensorMap tmS{}, tmXi{}, tmH{};
+        // tensor-core path: three bf16 planes per operator kind and their tensor maps
+        bool tc = false;
+        void *S3 = nullptr, *Xi3 = nullptr, *H3 = nullptr;
+        CUtensorMap tmS3{}, tmXi3{}, tmH3{};
     };
     struct MStep {
         int level = 0, nf = 0, count = 0;
@@ -438,6 +447,8 @@ private:
     };
     void residual(int B, double* rmax, bool zero_state);
     void pass(int B, bool first);
+    // one node GEMM of a group (kind 0 W, 1 H, 2 DOWN) on the tensor-core or the FP32 CUDA-core path
+    void node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int ksplit);
     // times the K-split candidates of every node GEMM (CUDA events, block of min(bmax, 32)) and keeps
     // the fastest per group and kind in the tree
     void tune();

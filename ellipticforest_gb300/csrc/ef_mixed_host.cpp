@@ -65,6 +65,21 @@ CUtensorMap make_map(float* base, long long rows, int cols, int box_rows) {
     return tm;
 }
 
+// three stacked bf16 planes [3 rows][cols] read in boxes of 64 columns (128 bytes) x 128 rows,
+// 128-byte swizzle: the K-major operand tiles of the tensor-core node GEMMs
+CUtensorMap make_map_bf16(void* base, long long rows3, int cols) {
+    CUtensorMap tm;
+    const cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows3)};
+    const cuuint64_t strides[1] = {cuuint64_t(cols) * 2};
+    const cuuint32_t box[2] = {64u, 128u};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = encode_tiled()(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled (bf16) failed (" + std::to_string(int(r)) + ")");
+    return tm;
+}
+
 }  // namespace
 
 MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
@@ -159,6 +174,15 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             groups_[gi].S32 = S;
             groups_[gi].Xi32 = Xi;
             groups_[gi].H32 = H32;
+            // bf16 planes of the tensor-core path (3 x the FP32 element count, 2 bytes each)
+            const bool tc = hps.tensor_cores() && mx_tc_supported(0, g.s) && mx_tc_supported(1, g.s) &&
+                            mx_tc_supported(2, g.s);
+            groups_[gi].tc = tc;
+            if (tc) {
+                groups_[gi].S3 = share ? share->groups_[gi].S3 : (void*)cv.get<uint16_t>(3 * cnt * 32 * s * s);
+                groups_[gi].Xi3 = share ? share->groups_[gi].Xi3 : (void*)cv.get<uint16_t>(3 * cnt * 16 * s * s);
+                groups_[gi].H3 = share ? share->groups_[gi].H3 : (void*)cv.get<uint16_t>(3 * cnt * 16 * s * s);
+            }
             for (size_t i = 0; i < cnt; ++i) {
                 MNode& m = mn_[g.nodes[i]];
                 m.S = S ? S + i * 32 * s * s : nullptr;
@@ -307,6 +331,9 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             g.tmS = share->groups_[gi].tmS;
             g.tmXi = share->groups_[gi].tmXi;
             g.tmH = share->groups_[gi].tmH;
+            g.tmS3 = share->groups_[gi].tmS3;
+            g.tmXi3 = share->groups_[gi].tmXi3;
+            g.tmH3 = share->groups_[gi].tmH3;
             continue;
         }
         mx_convert(st, g.d_conv, g.cnt, g.s);
@@ -316,10 +343,19 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         g.tmS = make_map(g.S32, cnt * 4 * s, int(8 * s), mx_tile_rows(0, g.s));
         g.tmXi = make_map(g.Xi32, cnt * 4 * s, int(4 * s), mx_tile_rows(0, g.s));
         g.tmH = make_map(g.H32, cnt * 8 * s, int(2 * s), mx_tile_rows(1, g.s));
+        if (g.tc) {
+            mx_tc_split(st, 2, g.S32, g.S3, cnt * 4 * s, int(8 * s), g.s);
+            mx_tc_split(st, 0, g.Xi32, g.Xi3, cnt * 4 * s, int(4 * s), g.s);
+            mx_tc_split(st, 1, g.H32, g.H3, cnt * 8 * s, int(2 * s), g.s);
+            g.tmS3 = make_map_bf16(g.S3, 3 * cnt * 4 * s, int(8 * s));
+            g.tmXi3 = make_map_bf16(g.Xi3, 3 * cnt * 4 * s, int(4 * s));
+            g.tmH3 = make_map_bf16(g.H3, 3 * cnt * 8 * s, int(2 * s));
+        }
     }
     ck(cudaGetLastError(), "mixed convert");
     ck(cudaStreamSynchronize(st), "mixed setup");
-    if (hps.mx_split_.size() != groups_.size()) tune();
+    const bool any_tc = std::any_of(groups_.begin(), groups_.end(), [](const MGroup& g) { return g.tc; });
+    if (hps.mx_split_.size() != groups_.size() || hps.mx_split_tc_ != any_tc) tune();
 }
 
 void MixedSolver::tune() {
@@ -332,13 +368,12 @@ void MixedSolver::tune() {
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
         const MGroup& g = groups_[gi];
         for (int kind = 0; kind < 3; ++kind) {
-            const CUtensorMap& tm = kind == 0 ? g.tmXi : (kind == 1 ? g.tmH : g.tmS);
-            const int kmax = mx_gemm_max_split(kind, g.s);
+            const int kmax = g.tc ? mx_tc_max_split(kind, g.s) : mx_gemm_max_split(kind, g.s);
             float best_ms = 1e30f;
             for (int ks = 1; ks <= kmax; ks *= 2) {
-                mx_gemm(st_, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ks);  // warm-up
+                node_gemm(st_, g, kind, B, ks);  // warm-up
                 ck(cudaEventRecord(e0, st_), "tune event");
-                for (int r = 0; r < 3; ++r) mx_gemm(st_, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ks);
+                for (int r = 0; r < 3; ++r) node_gemm(st_, g, kind, B, ks);
                 ck(cudaEventRecord(e1, st_), "tune event");
                 ck(cudaEventSynchronize(e1), "tune sync");
                 float ms = 0.f;
@@ -357,6 +392,17 @@ void MixedSolver::tune() {
     // the tuning launches wrote the pass buffers and the interface state: start clean
     ck(cudaMemsetAsync(arena_, 0, size_t(uG_begin_ - arena_) + uG_bytes_, st_), "clear after tune");
     h.mx_split_ = best;
+    h.mx_split_tc_ = std::any_of(groups_.begin(), groups_.end(), [](const MGroup& g) { return g.tc; });
+}
+
+void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int ksplit) {
+    if (g.tc) {
+        const CUtensorMap& tm = kind == 0 ? g.tmXi3 : (kind == 1 ? g.tmH3 : g.tmS3);
+        mx_gemm_tc(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ksplit < 1 ? 1 : ksplit);
+    } else {
+        const CUtensorMap& tm = kind == 0 ? g.tmXi : (kind == 1 ? g.tmH : g.tmS);
+        mx_gemm(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ksplit);
+    }
 }
 
 MixedSolver::~MixedSolver() {
@@ -419,10 +465,10 @@ void MixedSolver::pass(int B, bool first) {
             const double c = g.cnt, s2 = double(g.s) * g.s;
             const std::array<int, 3> ks = h.mx_split_.empty() ? std::array<int, 3>{0, 0, 0} : h.mx_split_[gi];
             h.pb("mx_gemm_w", st);
-            mx_gemm(st, 0, g.tmXi, g.d_items, g.cnt, g.s, B, d_err_, ks[0]);
+            node_gemm(st, g, 0, B, ks[0]);
             h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
             h.pb("mx_gemm_h", st);
-            mx_gemm(st, 1, g.tmH, g.d_items, g.cnt, g.s, B, d_err_, ks[1]);
+            node_gemm(st, g, 1, B, ks[1]);
             h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
         }
     }
@@ -438,7 +484,7 @@ void MixedSolver::pass(int B, bool first) {
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
             h.pb("mx_gemm_down", st);
-            mx_gemm(st, 2, g.tmS, g.d_items, g.cnt, g.s, B, d_err_, h.mx_split_.empty() ? 0 : h.mx_split_[gi][2]);
+            node_gemm(st, g, 2, B, h.mx_split_.empty() ? 0 : h.mx_split_[gi][2]);
             h.pe(c * 32 * s2 * 4, c * 2.0 * 32 * s2 * B, st);
         }
     }

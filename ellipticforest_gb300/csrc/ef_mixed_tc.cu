@@ -304,11 +304,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             if (!ok) {
                 // let the loads still in flight land before the shared memory goes away
+                // (only the last NS loads can be pending: a stage is reloaded after its MMAs completed)
                 int s2 = 0;
                 unsigned p2 = 0;
+                volatile int never = 0;
                 const int first = issued > NS ? issued - NS : 0;
                 for (int v = 0; v < issued; ++v) {
-                    if (v >= first) (void)tc_wait(&a_full[s2], p2, reinterpret_cast<volatile int*>(&first) /* never set */);
+                    if (v >= first) (void)tc_wait(&a_full[s2], p2, &never);
                     if (++s2 == NS) { s2 = 0; p2 ^= 1u; }
                 }
                 atomicExch(err, 1);
@@ -352,8 +354,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             // every MMA issued has completed before TMEM is freed
             tc_commit(drain);
-            int never = 0;
-            if (!tc_wait(drain, 0u, reinterpret_cast<volatile int*>(&never))) atomicExch(err, 1);
+            volatile int never = 0;
+            if (!tc_wait(drain, 0u, &never)) atomicExch(err, 1);
             if (!ok) atomicExch(err, 1);
         }
     } else {
@@ -504,6 +506,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // ---- K split: rank 0 of the cluster adds the partial tiles and runs the epilogue ----
     if (ksplit > 1) {
         cg::cluster_group cluster = cg::this_cluster();
+        if (nunits == 0 && tid < 128) {
+            // a rank without K chunks adds zeros
+            float* red = reinterpret_cast<float*>(base);
+#pragma unroll
+            for (int q = 0; q < 32; q += 4) *reinterpret_cast<float4*>(red + tid * 32 + q) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         cluster.sync();
         if (cluster.block_rank() == 0 && tid < 128 && nunits > 0 && !*abort_flag) {
             const int t = tid;

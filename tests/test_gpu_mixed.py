@@ -232,3 +232,43 @@ def test_device_resident_lane_matches_lane0(ef):
     out = torch.as_tensor(_Lane1U(), device="cuda").clone()
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy().reshape(3, n), u0)
+
+
+def _set_tc(hps, on):
+    from ellipticforest_gb300._lib import check, load
+    check(load().ef_hps_set_option(hps.handle, b"tensor-cores", int(on)))
+
+
+@pytest.mark.parametrize("kind,n,B", [(("uniform", 4), 16, 5), (("uniform", 5), 16, 40), (("uniform", 3), 32, 8)])
+def test_tensor_core_gemms_match_cuda_core_gemms(ef, kind, n, B):
+    """The tcgen05 node GEMMs (three-way bf16 split of the FP32 operators and requests, six tensor
+    products, FP32 accumulation in TMEM) give an FP32 pass as accurate as the CUDA-core FP32 GEMMs, and
+    one FP64 sweep reaches the FP64 HPS solution to 1e-10; ragged request counts (B = 5, not a
+    multiple of 4; B = 40, two request blocks of 32) included."""
+    mesh, hps = make(ef, kind, n, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, B, 41)
+    ref = fp64_solutions(hps, F, A, R)
+    errs = {}
+    for tc in (0, 1):
+        _set_tc(hps, tc)
+        hps.mixed_init(B)
+        u0 = hps.mixed_solve(F, A, R, sweeps=0)
+        u1 = hps.mixed_solve(F, A, R, sweeps=1)
+        e0 = max(np.abs(u0[k] - ref[k]).max() / np.abs(ref[k]).max() for k in range(B))
+        e1 = max(np.abs(u1[k] - ref[k]).max() / np.abs(ref[k]).max() for k in range(B))
+        errs[tc] = (e0, e1)
+        assert e1 <= TOL, (tc, e0, e1)
+    _set_tc(hps, 1)
+    # one FP32 pass: the tensor-core products are no less accurate than the FP32 FMA chains
+    assert errs[1][0] <= 2.0 * errs[0][0] + 1e-12, errs
+
+
+def test_tensor_core_result_same_alone_and_in_a_block(ef):
+    mesh, hps = make(ef, ("uniform", 4), 16, (-1.0, 1.0, -1.0, 1.0))
+    _set_tc(hps, 1)
+    F, A, R = requests(hps, mesh, 9, 17)
+    hps.mixed_init(9)
+    block = hps.mixed_solve(F, A, R, sweeps=1)
+    for k in (0, 4, 8):
+        alone = hps.mixed_solve(F[k:k + 1], A[k:k + 1], R[k:k + 1], sweeps=1)
+        assert np.array_equal(alone[0], block[k])
