@@ -103,6 +103,8 @@ SIGNATURES = {
                                _dp]),
     "ef_fv5_map_d2n": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp,
                                  _dp, _dp]),
+    "ef_hps_mixed_set_root": (C.c_int, [_vp, _dp, _dp]),
+    "ef_server_set_root": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "ef_mesh_level_count": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "ef_mesh_subtree": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),
     "ef_hps_split_sizes": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),

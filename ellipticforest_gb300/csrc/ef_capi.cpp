@@ -47,6 +47,8 @@ struct ef_hps {
     bool cache_operators = false;
     bool homogeneous_rhs = false;
     bool upward_done = false;
+    // root operator of the block solvers (ef_hps_mixed_set_root), applied to lanes created later
+    std::vector<double> root_a, root_b;
 };
 
 namespace {
@@ -199,7 +201,10 @@ int run_single_patch_fp(int n, double xl, double xu, double yl, double yu, const
     cudaFree(buf);
     st = cuda_status(e, "single patch (five-point)");
     if (st) return st;
-    if (info) return fail(EF_ERR_SINGULAR, "five-point operator has a zero pivot at row " + std::to_string(info - 1));
+    if (info > 0) return fail(EF_ERR_SINGULAR, "five-point operator has a zero pivot at row " + std::to_string(info - 1));
+    if (info < 0)
+        return fail(EF_ERR_UNSUPPORTED, "five-point operator is not negative definite (pivot of the wrong sign at row " +
+                                            std::to_string(-info - 1) + "): the band LU without pivoting is not safe");
     return EF_OK;
 }
 
@@ -319,6 +324,13 @@ int ef_hps_set_option(ef_hps* h, const char* key, int value) {
         h->hps->set_homogeneous_rhs(value != 0);
     } else if (k == "cuda-graphs") {
         h->hps->set_graphs(value != 0);
+    } else if (k == "inject-wait-timeout") {
+        // failure-path test of the bounded TMA waits (process-wide): the node GEMMs' first wait runs
+        // out and the mixed solve returns EF_ERR_CUDA while the context stays usable
+        return guarded([&] {
+            efgb::mx_set_inject_timeout(value != 0);
+            return EF_OK;
+        });
     } else if (k == "tensor-cores") {
         h->hps->set_tensor_cores(value != 0);  // block solvers created from now on
     } else if (k == "cooperative-lu") {
@@ -360,6 +372,12 @@ int ef_hps_build(ef_hps* h) {
     return guarded([&] {
         h->mixed.reset();  // FP32 operator copies belong to the previous build
         h->hps->build();
+        if (h->hps->indefinite_count() > 0)
+            return fail(EF_ERR_UNSUPPORTED,
+                        std::to_string(h->hps->indefinite_count()) +
+                            " FivePointStencil leaf operators are not negative definite (lambda above the smallest "
+                            "eigenvalue of the diffusion part, or alpha*beta changing sign): the band LU without "
+                            "pivoting is not safe for them");
         if (h->hps->singular_count() > 0)
             return fail(EF_ERR_SINGULAR, std::to_string(h->hps->singular_count()) +
                                              " interface matrices had a zero pivot (dgesv INFO != 0)");
@@ -611,6 +629,8 @@ int ef_hps_mixed_init(ef_hps* h, int bmax) {
     return guarded([&] {
         h->drop_lanes();
         h->mixed.reset();
+        h->root_a.clear();
+        h->root_b.clear();
         h->mixed = std::make_unique<efgb::MixedSolver>(*h->hps, bmax);
         return EF_OK;
     });
@@ -671,6 +691,7 @@ int ensure_lane(ef_hps* h, int k) {
         }
         h->lanes[k] = std::make_unique<efgb::MixedSolver>(*h->hps, h->mixed->bmax(), h->mixed.get());
         h->lanes[k]->set_stream(h->lane_st[k]);
+        if (!h->root_b.empty()) h->lanes[k]->set_root_operator(h->root_a.data(), h->root_b.data());
     }
     cudaEvent_t ready;
     int st = cuda_status(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "lane event");
@@ -682,6 +703,22 @@ int ensure_lane(ef_hps* h, int k) {
 
 efgb::MixedSolver* lane_solver(ef_hps* h, int lane) { return lane == 0 ? h->mixed.get() : h->lanes[lane].get(); }
 }  // namespace
+
+int ef_hps_mixed_set_root(ef_hps* h, const double* a, const double* b) {
+    if (!h || !a || !b) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    return guarded([&] {
+        h->mixed->set_root_operator(a, b);
+        for (int k = 1; k < ef_hps::kMaxLanes; ++k)
+            if (h->lanes[k]) {
+                cudaStreamSynchronize(h->lane_st[k]);
+                h->lanes[k]->set_root_operator(a, b);
+            }
+        h->root_a.assign(a, a + 4 * size_t(h->hps->root_M()));
+        h->root_b.assign(b, b + 4 * size_t(h->hps->root_M()));
+        return EF_OK;
+    });
+}
 
 int ef_hps_mixed_lane(ef_hps* h, int lane, double** f, double** a, double** r, double** u, void** stream) {
     if (!h) return fail(EF_ERR_INVALID, "null handle");
@@ -881,6 +918,14 @@ int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lane
         auto s = std::make_unique<ef_server>();
         s->srv = std::make_unique<efgb::Server>(specs, lanes_per_tree, hbm_budget_bytes, sweeps);
         *out = s.release();
+        return EF_OK;
+    });
+}
+
+int ef_server_set_root(ef_server* server, int tree, const double* a, const double* b) {
+    if (!server || !a || !b) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        server->srv->set_root_operator(tree, a, b);
         return EF_OK;
     });
 }

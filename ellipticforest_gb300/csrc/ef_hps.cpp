@@ -542,7 +542,11 @@ void Hps::build() {
     if (solver_type_ == SOLVER_FIVE_POINT) {
         std::vector<int> info(num_leaves());
         check(cudaMemcpy(info.data(), d_fpinfo_, info.size() * sizeof(int), cudaMemcpyDeviceToHost), "fp info");
-        for (int v : info) singular_ += (v != 0);
+        indefinite_ = 0;
+        for (int v : info) {
+            singular_ += (v > 0);
+            indefinite_ += (v < 0);
+        }
     }
     built_ = true;
 }

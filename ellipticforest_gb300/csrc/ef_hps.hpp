@@ -249,6 +249,9 @@ public:
     const Mesh& mesh() const { return mesh_; }
     bool built() const { return built_; }
     int singular_count() const { return singular_; }
+    // FivePointStencil leaves whose operator is not (alpha-scaled) negative definite: the band LU
+    // without pivoting is not safe for them (last build)
+    int indefinite_count() const { return indefinite_; }
     // LU factorisations of the general root matrix diag(a) + diag(b) T so far (cached across solves)
     long long root_factorizations() const { return root_factorizations_; }
     size_t device_bytes() const { return arena_bytes_; }
@@ -327,7 +330,8 @@ private:
 
     bool built_ = false;
     int singular_ = 0;
-    int leaf_singular_ = 0;  // constant-coefficient leaf operators with a zero pivot (last build)
+    int leaf_singular_ = 0;
+    int indefinite_ = 0;  // constant-coefficient leaf operators with a zero pivot (last build)
     int top_level_ = -1;
 
     struct Mark {
@@ -413,6 +417,12 @@ public:
     size_t device_bytes() const { return bytes_; }
     // 1 + sweeps FP32 passes on B <= bmax requests; asynchronous on the Hps stream.
     void solve(int B, int sweeps);
+    // Root operator of every later block (HPSAlgorithm.hpp:402-420): a u + b du/dn = r with a, b
+    // (4M each, host) fixed and r per request.  b == 0 everywhere returns to Dirichlet data with the
+    // per-request a.  Otherwise the root data become part of the state and every pass solves for
+    // their correction with Z = (diag a + diag b T_root)^{-1}, factored in FP64 here (synchronous).
+    void set_root_operator(const double* a, const double* b);
+    bool robin() const { return robin_; }
     // synchronises the stream; 1 when a kernel gave up waiting on a TMA copy since the last call
     int take_error();
     static constexpr int kMaxPasses = 8;
@@ -478,6 +488,14 @@ private:
     char* uG_begin_ = nullptr;
     size_t uG_bytes_ = 0;
     float* tables_ = nullptr;
+    // Robin root data (set_root_operator)
+    bool robin_ = false;
+    char* robin_mem_ = nullptr;
+    double *ra64_ = nullptr, *rb64_ = nullptr;
+    float *rb32_ = nullptr, *Z32_ = nullptr, *rho32_ = nullptr, *rhs32_ = nullptr;
+    const float** zA_ = nullptr;
+    const float** zB_ = nullptr;
+    float** zC_ = nullptr;
 };
 
 }  // namespace efgb

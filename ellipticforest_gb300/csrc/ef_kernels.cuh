@@ -204,6 +204,9 @@ int mx_gemm_max_split(int kind, int s);
 bool mx_tc_supported(int kind, int s);
 int mx_tc_max_split(int kind, int s);
 void mx_tc_split(cudaStream_t st, int kind, const float* src, void* dst, long long rows, int K, int s);
+// failure-path test switch of both GEMM forms (process-wide): every CTA's first wait runs out
+void mx_set_inject_timeout(int on);
+void mx_tc_set_inject_timeout(int on);
 void mx_gemm_tc(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
                 int* err, int ksplit);
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
@@ -230,6 +233,14 @@ struct MixCoef {
 void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const MixLeaf* leaves, int L, int B, int n,
                       int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g);
+// Robin root data in the mixed form (fixed a, b per block solver; r per request, [B][m]):
+// rho = r - a g64 - b h64 (FP64 -> FP32); rhs = rho - b h32; g64 += dg
+void mx_root_residual(cudaStream_t st, int m, int B, const double* a, const double* b, const double* r,
+                      const double* g64, const double* h64, float* rho);
+void mx_root_rhs(cudaStream_t st, int m, int B, const float* b32, const float* rho, const float* h32, float* rhs);
+void mx_root_update(cudaStream_t st, int m, int B, const float* dg, double* g64);
+// Z = P I for the row order perm of an LU (its solve then gives the inverse)
+void mx_perm_identity(cudaStream_t st, int m, const int* perm, double* Z);
 // rmax[b] = max over leaves of rleaf[b][leaf]
 void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax);
 

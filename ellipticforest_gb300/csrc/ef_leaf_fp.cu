@@ -6,9 +6,19 @@
 // (beta_N + beta_S)/dy^2) + lambda_ij, subtracts c_side from the diagonal of boundary rows and adds
 // -2 c_side g to their right-hand side (FiniteVolumeSolver.cpp:27-223), and LU-factors it with
 // PETSc for every solve.  Here the same matrix is factored once per leaf at build time: with cell
-// index j + i*n it is banded (bandwidth n) and row diagonally dominant, so Gaussian elimination
-// without pivoting is stable; the factorisation runs in a shared-memory window of n+1 band rows
-// (n^4 work instead of n^6) and its band is kept in HBM for every later solve.
+// index j + i*n it is banded (bandwidth n); the factorisation runs in a shared-memory window of n+1
+// band rows (n^4 work instead of n^6) and its band is kept in HBM for every later solve.
+//
+// No pivoting.  The matrix is A = D S with D = diag(alpha) and S symmetric (the face couplings
+// beta/d^2 are shared by both cells of a face; S_ii = -sum beta/d^2 + lambda/alpha).  Gaussian
+// elimination of D S without pivoting produces the pivots alpha_r u_rr(S), and u_rr(S) < 0 for every
+// r exactly when S is negative definite -- then elimination without pivoting is backward stable (the
+// Cholesky-type bound), whatever lambda's sign.  Every pivot is checked: a pivot with
+// pivot * alpha_r >= 0 means S is not negative definite (lambda above the smallest eigenvalue of the
+// diffusion part, alpha beta changing sign, alpha = 0), where elimination without pivoting is not
+// safe; the factorisation flags it (info = -(r + 1)) and the build refuses the tree instead of
+// returning results that could depart from the reference's pivoted LU.  An exact zero pivot is
+// flagged as singular (info = r + 1).
 //
 // Coefficients arrive sampled per cell exactly as the reference samples them (cpp:66-79):
 // alpha(x_i, y_j), beta at the four faces (x_i -/+ dx/2, y_j), (x_i, y_j -/+ dy/2), lambda(x_i, y_j).
@@ -65,7 +75,10 @@ __global__ void __launch_bounds__(256) k_fp_factor(const FpLeaf* __restrict__ le
             lm[threadIdx.x] = l;
             ri[n - d] = l;
         }
-        if (piv == 0.0 && threadIdx.x == 0 && *lf.info == 0) *lf.info = k + 1;
+        if (threadIdx.x == 0 && *lf.info == 0) {
+            if (piv == 0.0) *lf.info = k + 1;
+            else if (!(piv * lf.alpha[k] < 0.0)) *lf.info = -(k + 1);  // not (scaled) negative definite
+        }
         __syncthreads();
         // A[k+d][k+e] -= l_d * A[k][k+e], e = 1..n  (positions: row k+d at n-d+e, row k at n+e)
         for (int t = threadIdx.x; t < rows * n; t += blockDim.x) {

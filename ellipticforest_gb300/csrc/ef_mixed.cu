@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <stdexcept>
 
 #include "ef_kernels.cuh"
 #include "ef_mixed_common.cuh"
@@ -77,7 +78,7 @@ constexpr int kStages = 3;
 // floats per A stage: rt rows of 32, rounded up to a 1024-byte multiple
 __host__ __device__ __forceinline__ int mx_astage_floats(int rt) { return ((rt * kKC * 4 + 1023) / 1024) * 256; }
 inline size_t mx_gemm_smem(int rt, int BN) {
-    return 1024 + size_t(kStages) * mx_astage_floats(rt) * 4 + size_t(kStages) * kKC * BN * 4 + kStages * 8;
+    return 1024 + size_t(kStages) * mx_astage_floats(rt) * 4 + size_t(kStages) * kKC * BN * 4 + (kStages + 1) * 8;
 }
 
 // one tile of rt rows: its node, its row offset and the rows of X it multiplies
@@ -151,8 +152,10 @@ __global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __g
     const int b0 = blockIdx.y * BN;
     const unsigned tile_bytes = unsigned(rt) * kKC * sizeof(float);
 
+    unsigned long long* never = full + kStages;  // nothing arrives on it (failure-path test)
     if (tid == 0) {
         for (int st = 0; st < kStages; ++st) mbar_init(&full[st], 1);
+        mbar_init(never, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     }
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __g
     unsigned ph = 0;
     for (int v = 0; v < total; ++v) {
         cp_async_wait<kStages - 2>();
-        const bool ok = mbar_wait(&full[st], ph);
+        const bool ok = (v == 0 && g_mx_inject_timeout) ? mbar_wait_ns(never, 0u, 1000000LL) : mbar_wait(&full[st], ph);
         if (__syncthreads_or(!ok)) { fail_v = v; break; }
         if (v + kStages - 1 < total) {
             issue(st == 0 ? kStages - 1 : st - 1);
@@ -1385,6 +1388,38 @@ __global__ void k_mx_root(int m, int B, const double* a, const double* r, double
     }
 }
 
+// Robin root data a u + b du/dn = r (HPSAlgorithm.hpp:402-420) in the mixed form.  The root's
+// Dirichlet data g are part of the FP64 state; the residual of the root condition is
+// rho = r - a g - b h with h the state's exact boundary flux (the root's FP64 edge flux), and a pass
+// solves for the correction's root data dg = Z (rho - b h_p) with Z = (diag a + diag b T_root)^{-1}
+// (FP32) and h_p the correction's particular flux at the root (the FP32 upward pass).
+__global__ void k_mx_root_residual(int m, int B, const double* __restrict__ a, const double* __restrict__ b,
+                                   const double* __restrict__ r, const double* __restrict__ g64,
+                                   const double* __restrict__ h64, float* __restrict__ rho) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * B; e += gridDim.x * blockDim.x) {
+        const int i = e / B, q = e - (e / B) * B;
+        rho[e] = d2f_rn_bits(r[(long long)q * m + i] - a[i] * g64[e] - b[i] * h64[e]);
+    }
+}
+__global__ void k_mx_root_rhs(int m, int B, const float* __restrict__ b32, const float* __restrict__ rho,
+                              const float* __restrict__ h32, float* __restrict__ rhs) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * B; e += gridDim.x * blockDim.x) {
+        const int i = e / B;
+        rhs[e] = rho[e] - b32[i] * h32[e];
+    }
+}
+// Z = P I: row r of the permuted identity has its one in column perm[r]
+__global__ void k_mx_perm_identity(int m, const int* __restrict__ perm, double* __restrict__ Z) {
+    const long long tot = (long long)m * m;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+        const int r = int(e / m), c = int(e - (e / m) * m);
+        Z[e] = perm[r] == c ? 1.0 : 0.0;
+    }
+}
+__global__ void k_mx_root_update(int m, int B, const float* __restrict__ dg, double* __restrict__ g64) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * B; e += gridDim.x * blockDim.x) g64[e] += f2d_bits(dg[e]);
+}
+
 inline unsigned mx_grid(long long tot) {
     long long b = (tot + 255) / 256;
     if (b > 8192) b = 8192;
@@ -1474,6 +1509,12 @@ void mx_gemm(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* it
     if (kind == 0) mx_gemm<MX_W>(st, tm, items, nitems, s, B, err, ksplit);
     else if (kind == 1) mx_gemm<MX_H>(st, tm, items, nitems, s, B, err, ksplit);
     else mx_gemm<MX_DOWN>(st, tm, items, nitems, s, B, err, ksplit);
+}
+
+void mx_set_inject_timeout(int on) {
+    if (cudaMemcpyToSymbol(g_mx_inject_timeout, &on, sizeof(int)) != cudaSuccess)
+        throw std::runtime_error("node GEMM: setting the failure-path test switch failed");
+    mx_tc_set_inject_timeout(on);
 }
 
 int mx_gemm_max_split(int kind, int s) {
@@ -1680,6 +1721,24 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
 
 void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax) {
     k_mx_rmax<<<B, 1024, 0, st>>>(rleaf, L, rmax);
+    ++g_kernel_launches;
+}
+
+void mx_root_residual(cudaStream_t st, int m, int B, const double* a, const double* b, const double* r,
+                      const double* g64, const double* h64, float* rho) {
+    k_mx_root_residual<<<mx_grid((long long)m * B), 256, 0, st>>>(m, B, a, b, r, g64, h64, rho);
+    ++g_kernel_launches;
+}
+void mx_root_rhs(cudaStream_t st, int m, int B, const float* b32, const float* rho, const float* h32, float* rhs) {
+    k_mx_root_rhs<<<mx_grid((long long)m * B), 256, 0, st>>>(m, B, b32, rho, h32, rhs);
+    ++g_kernel_launches;
+}
+void mx_perm_identity(cudaStream_t st, int m, const int* perm, double* Z) {
+    k_mx_perm_identity<<<mx_grid((long long)m * m), 256, 0, st>>>(m, perm, Z);
+    ++g_kernel_launches;
+}
+void mx_root_update(cudaStream_t st, int m, int B, const float* dg, double* g64) {
+    k_mx_root_update<<<mx_grid((long long)m * B), 256, 0, st>>>(m, B, dg, g64);
     ++g_kernel_launches;
 }
 

@@ -76,8 +76,8 @@ __device__ __forceinline__ long long global_ns() {
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-// bounded wait on an mbarrier phase: false after about a second without completion
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// bounded wait on an mbarrier phase: false after limit_ns without completion
+__device__ __forceinline__ bool mbar_wait_ns(unsigned long long* bar, unsigned parity, long long limit_ns) {
     const unsigned a = smem_u32(bar);
     long long t0 = 0;
     for (unsigned it = 0;; ++it) {
@@ -89,9 +89,20 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
             : "memory");
         if (ok) return true;
         if (it == 0) t0 = global_ns();
-        else if ((it & 63) == 0 && global_ns() - t0 > 1000000000LL) return false;
+        else if ((it & 63) == 0 && global_ns() - t0 > limit_ns) return false;
     }
 }
+// bounded wait on an mbarrier phase: false after about a second without completion
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    return mbar_wait_ns(bar, parity, 1000000000LL);
+}
+
+// Failure-path test switch of the node GEMMs (set from the host, per translation unit): when set, the
+// first consumer wait of every CTA is on an mbarrier that nothing arrives on, limited to 1 ms, and
+// the kernel then leaves through the same path as after a real timeout (copies in flight drained,
+// error word set).  Off in normal operation.
+static __device__ int g_mx_inject_timeout = 0;
+
 // one TMA tile (32 columns x rows) of A into shared memory, completing on `bar`
 __device__ __forceinline__ void tma_load_tile(const CUtensorMap* tm, unsigned long long* bar, float* dst, int x,
                                               int y, unsigned bytes) {

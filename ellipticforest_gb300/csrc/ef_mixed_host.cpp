@@ -408,6 +408,83 @@ void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, i
 MixedSolver::~MixedSolver() {
     if (arena_) cudaFree(arena_);
     if (tables_) cudaFree(tables_);
+    if (robin_mem_) cudaFree(robin_mem_);
+}
+
+void MixedSolver::set_root_operator(const double* a, const double* b) {
+    Hps& h = H_;
+    const int m = 4 * h.root_M();
+    bool general = false;
+    for (int i = 0; i < m; ++i)
+        if (b[i] != 0.0) { general = true; break; }
+    graphs_.clear();  // the captured sequences change with the root operator
+    if (!general) {
+        robin_ = false;
+        return;
+    }
+    if (!h.built()) throw std::invalid_argument("mixed solver: Robin root data need the FP64 build (root T)");
+    cudaStream_t st = st_;
+    const size_t mm = size_t(m) * m;
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    if (!robin_mem_) {
+        const size_t bytes = up(2 * m * 8) + up(m * 4) + up(mm * 4) + 2 * up(size_t(m) * bmax_ * 4) + up(3 * sizeof(void*));
+        ck(cudaMalloc(&robin_mem_, bytes), "cudaMalloc(mixed Robin root)");
+        char* p = robin_mem_;
+        ra64_ = reinterpret_cast<double*>(p); rb64_ = ra64_ + m; p += up(2 * m * 8);
+        rb32_ = reinterpret_cast<float*>(p); p += up(m * 4);
+        Z32_ = reinterpret_cast<float*>(p); p += up(mm * 4);
+        rho32_ = reinterpret_cast<float*>(p); p += up(size_t(m) * bmax_ * 4);
+        rhs32_ = reinterpret_cast<float*>(p); p += up(size_t(m) * bmax_ * 4);
+        zA_ = reinterpret_cast<const float**>(p);
+        zB_ = reinterpret_cast<const float**>(p + sizeof(void*));
+        zC_ = reinterpret_cast<float**>(p + 2 * sizeof(void*));
+        const void* ptrs[3] = {Z32_, rhs32_, mn_[0].g32};
+        ck(upload_sync(st, zA_, ptrs, sizeof(ptrs)), "Robin GEMM pointers");
+    }
+    std::vector<float> b32(m);
+    for (int i = 0; i < m; ++i) b32[i] = float(b[i]);
+    ck(upload_sync(st, ra64_, a, m * 8), "Robin a");
+    ck(upload_sync(st, rb64_, b, m * 8), "Robin b");
+    ck(upload_sync(st, rb32_, b32.data(), m * 4), "Robin b32");
+    // Z = (diag a + diag b T)^{-1} in FP64 (LU with partial pivoting, then the solve of P I), kept in FP32
+    char* tmp = nullptr;
+    const size_t tbytes = 2 * up(mm * 8) + 2 * up(size_t(m) * 4) + up(4) + up(4 * sizeof(void*));
+    ck(cudaMalloc(&tmp, tbytes), "cudaMalloc(Robin factor)");
+    double* A = reinterpret_cast<double*>(tmp);
+    double* Z = reinterpret_cast<double*>(tmp + up(mm * 8));
+    int* piv = reinterpret_cast<int*>(tmp + 2 * up(mm * 8));
+    int* perm = reinterpret_cast<int*>(tmp + 2 * up(mm * 8) + up(size_t(m) * 4));
+    int* info = reinterpret_cast<int*>(tmp + 2 * up(mm * 8) + 2 * up(size_t(m) * 4));
+    void** arr = reinterpret_cast<void**>(tmp + 2 * up(mm * 8) + 2 * up(size_t(m) * 4) + up(4));
+    int bad = 0;
+    try {
+        const void* pa[4] = {A, Z, piv, perm};
+        ck(upload_sync(st, arr, pa, sizeof(pa)), "Robin pointers");
+        ck(cudaMemsetAsync(info, 0, sizeof(int), st), "Robin info");
+        root_assemble(st, m, ra64_, rb64_, h.root_T(), A);
+        dgetrf_batched(st, m, reinterpret_cast<double* const*>(arr), m, reinterpret_cast<int* const*>(arr + 2), info, 1);
+        piv_to_perm(st, m, reinterpret_cast<int* const*>(arr + 2), reinterpret_cast<int* const*>(arr + 3), 1);
+        mx_perm_identity(st, m, perm, Z);
+        dlu_solve_permuted(st, m, m, reinterpret_cast<const double* const*>(arr), m,
+                           reinterpret_cast<double* const*>(arr + 1), m, 1);
+        const double* zin[1] = {Z};
+        float* zout[1] = {Z32_};
+        void** cv = arr;  // reuse the pointer slots for the narrowing copy
+        ck(cudaStreamSynchronize(st), "Robin factor");
+        ck(upload_sync(st, cv, zin, sizeof(zin)), "Robin narrow in");
+        ck(upload_sync(st, cv + 1, zout, sizeof(zout)), "Robin narrow out");
+        narrow_batched(st, reinterpret_cast<const double* const*>(cv), reinterpret_cast<float* const*>(cv + 1),
+                       (long long)mm, 1);
+        ck(cudaMemcpyAsync(&bad, info, sizeof(int), cudaMemcpyDeviceToHost, st), "Robin info");
+        ck(cudaStreamSynchronize(st), "Robin set-up");
+    } catch (...) {
+        cudaStreamSynchronize(st);
+        cudaFree(tmp);
+        throw;
+    }
+    cudaFree(tmp);
+    if (bad) throw std::invalid_argument("mixed solver: diag(a) + diag(b) T_root is singular");
+    robin_ = true;
 }
 
 void MixedSolver::residual(int B, double* rmax, bool zero_state) {
@@ -439,6 +516,8 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
         for (auto& g : groups_)
             if (g.level == lvl) mx_flux_up(st, g.d_items, g.cnt, g.s, B);
     }
+    // residual of the Robin root condition from the state's root data and exact boundary flux
+    if (robin_) mx_root_residual(st, 4 * h.root_M(), B, ra64_, rb64_, r_, mn_[0].g64, mn_[0].h64, rho32_);
     h.pe(0, 0, st);
 }
 
@@ -472,8 +551,19 @@ void MixedSolver::pass(int B, bool first) {
             h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
         }
     }
-    // homogeneous root data for the correction
-    ck(cudaMemsetAsync(mn_[0].g32, 0, sizeof(float) * 4 * size_t(h.root_M()) * B, st), "root g32");
+    const int mroot = 4 * h.root_M();
+    if (robin_) {
+        // the correction's root data dg = Z (rho - b h_p), added to the state's root data
+        h.pb("mx_root", st);
+        mx_root_rhs(st, mroot, B, rb32_, rho32_, mn_[0].h32, rhs32_);
+        GemmArgs32 ga{zA_, 0, mroot, zB_, 0, B, zC_, 0, B};
+        sgemm_batched(st, mroot, B, mroot, 1.0f, ga, 0.0f, 1);
+        mx_root_update(st, mroot, B, mn_[0].g32, mn_[0].g64);
+        h.pe(double(mroot) * mroot * 4, 2.0 * double(mroot) * mroot * B, st);
+    } else {
+        // homogeneous root data for the correction
+        ck(cudaMemsetAsync(mn_[0].g32, 0, sizeof(float) * size_t(mroot) * B, st), "root g32");
+    }
     for (int lvl = 0; lvl < maxL; ++lvl) {
         h.pb("mx_interface", st);
         for (auto& s : gsteps_)
@@ -502,7 +592,8 @@ void MixedSolver::solve(int B, int sweeps) {
         cudaStream_t s = st_;
         ck(cudaMemsetAsync(uG_begin_, 0, uG_bytes_, s), "clear interface state");
         ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, s), "clear residuals");
-        mx_root(s, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
+        if (robin_) ck(cudaMemsetAsync(mn_[0].g64, 0, sizeof(double) * 4 * size_t(h.root_M()) * B, s), "root g64");
+        else mx_root(s, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
         for (int p = 0; p <= sweeps; ++p) {
             residual(B, rmax_ + size_t(p) * bmax_, p == 0);
             pass(B, p == 0);

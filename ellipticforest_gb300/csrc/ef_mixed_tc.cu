@@ -10,9 +10,13 @@
 //     D_lo += a1 x2 + a2 x1 + a1 x3 + a2 x2 + a3 x1   (TMEM accumulator 2)
 // with tcgen05.mma kind::f16 (bf16 inputs, exact products, FP32 accumulation); y = D_hi + D_lo.
 // Keeping the small terms in their own accumulator stops them from being rounded against the large
-// running sum.  The dropped terms a2 x3, a3 x2, a3 x3 are below 2^-24 |a x|: the result carries the
-// error of an FP32 FMA chain, which the one FP64 refinement sweep is sized for (a 3-pass split-TF32
-// would round each product to ~2^-21).
+// running sum.  The dropped terms a2 x3, a3 x2, a3 x3 are below 2^-24 |a x|.  The tensor core's own
+// FP32 accumulation is not round-to-nearest (a first version that accumulated all of K in TMEM made
+// an FP32 pass 2.1x less accurate than CUDA-core FMA chains), so every 64-wide K chunk goes to a
+// fresh pair of TMEM accumulators (two pairs, alternating) and the epilogue warps add the chunk's
+// sums to FP32 registers with round-to-nearest: the pass is then at least as accurate as the FMA
+// chains, which the one FP64 refinement sweep is sized for (a 3-pass split-TF32 would round each
+// product to ~2^-21).
 //
 // Layout.  The three planes of a group's operators (one back-to-back row-major matrix per kind, H
 // with each child's two runs of s rows made adjacent) are streamed by TMA in boxes of 128 rows x
@@ -70,9 +74,10 @@ __host__ __device__ inline int tc_stage_bytes(int nseg) { return 3 * kPlaneA + 3
 inline size_t tc_smem_bytes(int nseg) {
     return 1024 + size_t(tc_stages(nseg)) * tc_stage_bytes(nseg) + 256;
 }
+// two chunk buffers x (D_hi, D_lo) x 32 nseg columns
 __host__ __device__ inline int tc_tmem_cols(int nseg) {
-    const int need = 2 * kTB * nseg;
-    return need <= 64 ? 64 : (need <= 128 ? 128 : 256);
+    const int need = 4 * kTB * nseg;
+    return need <= 128 ? 128 : (need <= 256 ? 256 : 512);
 }
 
 // compact H row order of the planes: child c's rows [2s c, 2s c + 2s) are its W/E run and then its
@@ -153,16 +158,17 @@ __device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parit
         : "memory");
     return ok != 0;
 }
-// bounded wait: false after about a second (raising the CTA's abort flag) or when another role of
-// the CTA has already given up
-__device__ __forceinline__ bool tc_wait(unsigned long long* bar, unsigned parity, volatile int* abort) {
+// bounded wait: false after limit_ns (about a second by default, raising the CTA's abort flag) or
+// when another role of the CTA has already given up
+__device__ __forceinline__ bool tc_wait(unsigned long long* bar, unsigned parity, volatile int* abort,
+                                        long long limit_ns = 1000000000LL) {
     long long t0 = 0;
     for (unsigned it = 0;; ++it) {
         if (mbar_try(bar, parity)) return true;
         if ((it & 31) == 0) {
             if (*abort) return false;
             if (it == 0) t0 = global_ns();
-            else if (global_ns() - t0 > 1000000000LL) {
+            else if (global_ns() - t0 > limit_ns) {
                 *abort = 1;
                 return false;
             }
@@ -230,10 +236,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     unsigned long long* a_full = bars;             // [NS] TMA transaction barriers
     unsigned long long* x_full = bars + NS;        // [NS] 128 producer arrivals
     unsigned long long* empty = bars + 2 * NS;     // [NS] MMA commit
-    unsigned long long* acc_full = bars + 3 * NS;  // MMA commit at the end of a unit
-    unsigned long long* acc_empty = acc_full + 1;  // 128 epilogue arrivals
-    unsigned long long* drain = acc_full + 2;      // MMA commit before TMEM is freed
-    unsigned* tmem_slot = reinterpret_cast<unsigned*>(acc_full + 3);
+    unsigned long long* acc_full = bars + 3 * NS;  // [2] MMA commit at the end of a chunk
+    unsigned long long* acc_empty = acc_full + 2;  // [2] 128 epilogue arrivals
+    unsigned long long* drain = acc_full + 4;      // MMA commit before TMEM is freed
+    unsigned long long* never = acc_full + 5;      // nothing arrives on it (failure-path test)
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(acc_full + 6);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -262,9 +269,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_init(&x_full[i], 128);
             mbar_init(&empty[i], 1);
         }
-        mbar_init(acc_full, 1);
-        mbar_init(acc_empty, 128);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 128);
+        }
         mbar_init(drain, 1);
+        mbar_init(never, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -323,34 +333,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             unsigned ph = 0;
             bool ok = true;
             const uint32_t a_base = smem_u32(base);
-            for (int u = 0; u < nunits && ok; ++u) {
-                if (u > 0) ok = tc_wait(acc_empty, unsigned(u - 1) & 1u, abort_flag);
-                for (int c = 0; c < cpu && ok; ++c) {
-                    ok = tc_wait(&a_full[st], ph, abort_flag) && tc_wait(&x_full[st], ph, abort_flag);
-                    if (!ok) break;
-                    tc_fence_after();
-                    const uint32_t sa = a_base + uint32_t(st) * SB;
-                    const uint32_t sx = sa + 3u * kPlaneA;
-                    const int kleft = K - (cbase + c) * kTK;
-                    const int nk = kleft >= kTK ? kTK / 16 : (kleft + 15) / 16;
-                    for (int kk = 0; kk < nk; ++kk) {
-                        const uint32_t ko = uint32_t(kk) * 32u;
-                        const uint64_t a1 = tc_desc(sa + ko), a2 = tc_desc(sa + kPlaneA + ko),
-                                       a3 = tc_desc(sa + 2 * kPlaneA + ko);
-                        const uint32_t xp = uint32_t(nseg) * kPlaneX;
-                        const uint64_t x1 = tc_desc(sx + ko), x2 = tc_desc(sx + xp + ko), x3 = tc_desc(sx + 2 * xp + ko);
-                        const unsigned acc = (c > 0 || kk > 0) ? 1u : 0u;
-                        tc_mma(tmem, a1, x1, idesc, acc);
-                        tc_mma(tmem + unsigned(ncol), a1, x2, idesc, acc);
-                        tc_mma(tmem + unsigned(ncol), a2, x1, idesc, 1u);
-                        tc_mma(tmem + unsigned(ncol), a1, x3, idesc, 1u);
-                        tc_mma(tmem + unsigned(ncol), a2, x2, idesc, 1u);
-                        tc_mma(tmem + unsigned(ncol), a3, x1, idesc, 1u);
-                    }
-                    tc_commit(&empty[st]);
-                    if (++st == NS) { st = 0; ph ^= 1u; }
+            if (g_mx_inject_timeout && nunits > 0) ok = tc_wait(never, 0u, abort_flag, 1000000LL);
+            const int total = nunits * cpu;
+            for (int gch = 0; gch < total && ok; ++gch) {
+                const int c = gch % cpu, bf = gch & 1;
+                // the chunk's accumulator pair was drained two chunks ago
+                if (gch >= 2) ok = tc_wait(&acc_empty[bf], unsigned((gch >> 1) - 1) & 1u, abort_flag);
+                if (ok) ok = tc_wait(&a_full[st], ph, abort_flag) && tc_wait(&x_full[st], ph, abort_flag);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t sa = a_base + uint32_t(st) * SB;
+                const uint32_t sx = sa + 3u * kPlaneA;
+                const unsigned dhi = tmem + unsigned(bf * 2 * ncol), dlo = dhi + unsigned(ncol);
+                const int kleft = K - (cbase + c) * kTK;
+                const int nk = kleft >= kTK ? kTK / 16 : (kleft + 15) / 16;
+                for (int kk = 0; kk < nk; ++kk) {
+                    const uint32_t ko = uint32_t(kk) * 32u;
+                    const uint64_t a1 = tc_desc(sa + ko), a2 = tc_desc(sa + kPlaneA + ko),
+                                   a3 = tc_desc(sa + 2 * kPlaneA + ko);
+                    const uint32_t xp = uint32_t(nseg) * kPlaneX;
+                    const uint64_t x1 = tc_desc(sx + ko), x2 = tc_desc(sx + xp + ko), x3 = tc_desc(sx + 2 * xp + ko);
+                    const unsigned acc = kk > 0 ? 1u : 0u;  // a fresh accumulator pair per chunk
+                    tc_mma(dhi, a1, x1, idesc, acc);
+                    tc_mma(dlo, a1, x2, idesc, acc);
+                    tc_mma(dlo, a2, x1, idesc, 1u);
+                    tc_mma(dlo, a1, x3, idesc, 1u);
+                    tc_mma(dlo, a2, x2, idesc, 1u);
+                    tc_mma(dlo, a3, x1, idesc, 1u);
                 }
-                if (ok) tc_commit(acc_full);
+                tc_commit(&empty[st]);
+                tc_commit(&acc_full[bf]);
+                if (++st == NS) { st = 0; ph ^= 1u; }
             }
             // every MMA issued has completed before TMEM is freed
             tc_commit(drain);
@@ -359,72 +372,95 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!ok) atomicExch(err, 1);
         }
     } else {
-        // ---- warps 0-3: stage X (split into bf16 planes), then the epilogue of each unit ----
+        // ---- warps 0-3: stage X (split into bf16 planes) one chunk ahead, add every chunk's
+        //      accumulators to the FP32 running sums, run the epilogue of each unit ----
         const int t = tid;  // 0..127 = TMEM lane of this thread's tile row
         int st = 0;
         unsigned ph = 0;
         int staged = 0;
         bool ok = true;
         const bool vec = (B & 3) == 0;
-        for (int u = 0; u < nunits && ok; ++u) {
-            const int tile = tile_of(u);
-            const int gs0 = seg0_of(tile);
-            TcSeg seg[kMaxSeg];
-            bool sval[kMaxSeg];
+        const int total = nunits * cpu;
+        TcSeg seg[kMaxSeg];
+        bool sval[kMaxSeg];
+        int seg_unit = -1;
+        auto stage = [&](int gch) -> bool {
+            const int u = gch / cpu, c = gch - u * cpu;
+            if (u != seg_unit) {
+                seg_unit = u;
+                const int gs0 = seg0_of(tile_of(u));
 #pragma unroll
-            for (int j = 0; j < kMaxSeg; ++j) {
-                sval[j] = j < nseg && gs0 + j < nsegs_total;
-                if (sval[j]) seg[j] = tc_seg<KIND>(items, s, B, gs0 + j);
-            }
-            for (int c = 0; c < cpu && ok; ++c) {
-                if (staged >= NS) ok = tc_wait(&empty[st], ph ^ 1u, abort_flag);
-                if (!ok) break;
-                unsigned char* sx = base + size_t(st) * SB + 3 * kPlaneA;
-                const int k0 = (cbase + c) * kTK;
-                const int b = t & 31, n = b;
-                const int gb = b0 + b;
-                // pairs (k, k + 1) of one request: 32 per block, four pair rows per pass of the warps
-                for (int i = 0; i < 8 * nseg; ++i) {
-                    const int P = (t >> 5) + 4 * i;
-                    const int j = P >> 5, kp = P & 31;
-                    const int k = k0 + 2 * kp;
-                    float x0 = 0.f, x1 = 0.f;
-                    if (sval[j] && gb < B) {
-                        const TcSeg& sg = seg[j];
-                        if (k < K) x0 = (k < sg.kb ? sg.X1 : sg.X2)[(long long)k * B + gb];
-                        if (k + 1 < K) x1 = (k + 1 < sg.kb ? sg.X1 : sg.X2)[(long long)(k + 1) * B + gb];
-                    }
-                    __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
-                    split3(x0, p0a, p1a, p2a);
-                    split3(x1, p0b, p1b, p2b);
-                    const int kl = 2 * kp;
-                    const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
-                                         ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
-                    const unsigned xp = unsigned(nseg) * kPlaneX;
-                    *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
-                    *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
-                    *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+                for (int j = 0; j < kMaxSeg; ++j) {
+                    sval[j] = j < nseg && gs0 + j < nsegs_total;
+                    if (sval[j]) seg[j] = tc_seg<KIND>(items, s, B, gs0 + j);
                 }
-                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                mbar_arrive(&x_full[st]);
-                ++staged;
-                if (++st == NS) { st = 0; ph ^= 1u; }
             }
-            if (!ok) break;
-            // ---- epilogue of the unit ----
-            ok = tc_wait(acc_full, unsigned(u) & 1u, abort_flag);
-            if (!ok) break;
+            if (staged >= NS && !tc_wait(&empty[st], ph ^ 1u, abort_flag)) return false;
+            unsigned char* sx = base + size_t(st) * SB + 3 * kPlaneA;
+            const int k0 = (cbase + c) * kTK;
+            const int b = t & 31, n = b;
+            const int gb = b0 + b;
+            // pairs (k, k + 1) of one request: 32 per block, four pair rows per pass of the warps
+            for (int i = 0; i < 8 * nseg; ++i) {
+                const int P = (t >> 5) + 4 * i;
+                const int j = P >> 5, kp = P & 31;
+                const int k = k0 + 2 * kp;
+                float x0 = 0.f, x1 = 0.f;
+                if (sval[j] && gb < B) {
+                    const TcSeg& sg = seg[j];
+                    if (k < K) x0 = (k < sg.kb ? sg.X1 : sg.X2)[(long long)k * B + gb];
+                    if (k + 1 < K) x1 = (k + 1 < sg.kb ? sg.X1 : sg.X2)[(long long)(k + 1) * B + gb];
+                }
+                __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
+                split3(x0, p0a, p1a, p2a);
+                split3(x1, p0b, p1b, p2b);
+                const int kl = 2 * kp;
+                const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
+                                     ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
+                const unsigned xp = unsigned(nseg) * kPlaneX;
+                *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
+                *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
+                *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_arrive(&x_full[st]);
+            ++staged;
+            if (++st == NS) { st = 0; ph ^= 1u; }
+            return true;
+        };
+        float rhi[32], rlo[32];
+#pragma unroll
+        for (int q = 0; q < 32; ++q) { rhi[q] = 0.f; rlo[q] = 0.f; }
+        const int jrow = sh.seg_rows >= kTM ? 0 : t / sh.seg_rows;
+        const unsigned lane_off = unsigned(warp * 32) << 16;
+        if (total > 0) ok = stage(0);
+        for (int gch = 0; gch < total && ok; ++gch) {
+            if (gch + 1 < total && !(ok = stage(gch + 1))) break;
+            // the chunk's sums: TMEM -> registers, added with round-to-nearest
+            const int bf = gch & 1;
+            if (!(ok = tc_wait(&acc_full[bf], unsigned(gch >> 1) & 1u, abort_flag))) break;
             tc_fence_after();
-            const int jrow = sh.seg_rows >= kTM ? 0 : t / sh.seg_rows;
             float hi[32], lo[32];
-            const unsigned lane_off = unsigned(warp * 32) << 16;
-            tmem_ld32(tmem + lane_off + unsigned(jrow * kTB), hi);
-            tmem_ld32(tmem + lane_off + unsigned(ncol + jrow * kTB), lo);
+            const unsigned col = unsigned(bf * 2 * ncol + jrow * kTB);
+            tmem_ld32(tmem + lane_off + col, hi);
+            tmem_ld32(tmem + lane_off + col + unsigned(ncol), lo);
             tc_fence_before();
-            mbar_arrive(acc_empty);  // the accumulators may be overwritten by the next unit
+            mbar_arrive(&acc_empty[bf]);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                rhi[q] += hi[q];
+                rlo[q] += lo[q];
+            }
+            if ((gch + 1) % cpu != 0) continue;
+            // ---- epilogue of the unit ----
+            const int tile = tile_of(gch / cpu);
             float v[32];
 #pragma unroll
-            for (int q = 0; q < 32; ++q) v[q] = hi[q] + lo[q];
+            for (int q = 0; q < 32; ++q) {
+                v[q] = rhi[q] + rlo[q];
+                rhi[q] = 0.f;
+                rlo[q] = 0.f;
+            }
 
             if (ksplit > 1) {
                 // partial tiles -> rank 0 of the cluster through distributed shared memory, in rank
@@ -661,6 +697,11 @@ void mx_tc_split(cudaStream_t st, int kind, const float* src, void* dst, long lo
     const int grid = int(std::min<long long>((tot + 255) / 256, 8192));
     k_tc_split<<<grid, 256, 0, st>>>(src, reinterpret_cast<__nv_bfloat16*>(dst), R, K, s, kind == MX_H ? 1 : 0);
     ++g_kernel_launches;
+}
+
+void mx_tc_set_inject_timeout(int on) {
+    if (cudaMemcpyToSymbol(g_mx_inject_timeout, &on, sizeof(int)) != cudaSuccess)
+        throw std::runtime_error("tensor-core GEMM: setting the failure-path test switch failed");
 }
 
 void mx_gemm_tc(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,

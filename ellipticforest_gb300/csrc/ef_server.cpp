@@ -130,6 +130,22 @@ void Server::set_sweeps(int tree, int sweeps) {
     trees_[tree].sweeps.store(sweeps);
 }
 
+void Server::set_root_operator(int tree, const double* a, const double* b) {
+    if (tree < 0 || tree >= int(trees_.size())) throw std::invalid_argument("server: tree index out of range");
+    if (!a || !b) throw std::invalid_argument("server: null root operator");
+    Tree& t = trees_[tree];
+    const size_t m = 4 * size_t(t.hps->root_M());
+    std::unique_lock<std::mutex> g(mu_);
+    for (const auto& kv : pending_)
+        if (kv.second == tree) throw std::invalid_argument("server: the tree has requests in flight");
+    t.root_a.assign(a, a + m);
+    t.root_b.assign(b, b + m);
+    t.root_pending = true;
+    cv_work_.notify_all();
+    cv_done_.wait(g, [&] { return !t.root_pending || !error_.empty(); });
+    if (!error_.empty()) throw std::runtime_error(error_);
+}
+
 Server::Stats Server::stats() {
     std::lock_guard<std::mutex> g(mu_);
     return stats_;
@@ -181,6 +197,25 @@ void Server::loop() {
                     l.busy = false;
                     progress = true;
                 }
+            // root operators waiting for their tree's lanes to be idle
+            for (auto& t : trees_) {
+                bool pend;
+                {
+                    std::lock_guard<std::mutex> g(mu_);
+                    pend = t.root_pending;
+                }
+                if (!pend) continue;
+                bool idle = true;
+                for (auto& l : t.lanes) idle = idle && !l.busy;
+                if (!idle) continue;
+                for (auto& l : t.lanes) l.ms->set_root_operator(t.root_a.data(), t.root_b.data());
+                {
+                    std::lock_guard<std::mutex> g(mu_);
+                    t.root_pending = false;
+                }
+                cv_done_.notify_all();
+                progress = true;
+            }
             // new blocks on free lanes: every request that has arrived, up to bmax
             for (auto& t : trees_)
                 for (auto& l : t.lanes) {

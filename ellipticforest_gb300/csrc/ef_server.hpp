@@ -55,6 +55,11 @@ public:
     Stats stats();
     // refinement sweeps of the tree's later blocks (the creation value until set)
     void set_sweeps(int tree, int sweeps);
+    // Root operator a u + b du/dn = r (a, b: 4M host arrays) of every lane of the tree, for the
+    // requests submitted from now on (their own `a` is then not read while b != 0); b == 0 returns to
+    // per-request Dirichlet data.  The tree must have no request in flight; applied by the
+    // scheduler thread between blocks, and this call returns once it is in place.
+    void set_root_operator(int tree, const double* a, const double* b);
     int lanes(int tree) const { return int(trees_.at(tree).lanes.size()); }
     long long device_bytes() const { return bytes_; }
 
@@ -79,6 +84,8 @@ private:
         std::atomic<int> sweeps{1};
         std::vector<Lane> lanes;
         std::deque<Req> queue;
+        std::vector<double> root_a, root_b;  // a root operator waiting for the scheduler
+        bool root_pending = false;
     };
 
     void loop();

@@ -636,6 +636,15 @@ class HPSAlgorithm:
         check(_lib.load().ef_hps_mixed_init(self._h, int(bmax)))
         self.mixed_bmax = int(bmax)
 
+    def mixed_set_root(self, a, b):
+        """Fixed root operator a u + b du/dn = r of the block solver (r per request); b = 0 returns
+        to per-request Dirichlet data (no reference counterpart: the reference solves one request)."""
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if a.shape != (4 * self.M,) or b.shape != (4 * self.M,):
+            raise ValueError("mixed_set_root: a and b must have 4M entries")
+        check(_lib.load().ef_hps_mixed_set_root(self._h, dptr(a), dptr(b)))
+
     def mixed_solve(self, f, a, r, sweeps: int = 1) -> np.ndarray:
         """Solve a block of requests: f [B, leaves*n*n], a and r [B, 4M] (a u = r on the root
         faces).  Returns u [B, leaves*n*n] refined to the FP64 HPS solution."""
@@ -753,6 +762,16 @@ class Server:
         for t, x in enumerate(sw):
             self.set_sweeps(t, x)
         self._live = {}  # id -> arrays kept alive until completion
+
+    def set_root(self, tree: int, a, b) -> None:
+        """Root operator a u + b du/dn = r of the tree's later requests (see HPSAlgorithm.mixed_set_root);
+        the tree must have no request in flight."""
+        t = self._trees[tree]
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if a.shape != (4 * t.M,) or b.shape != (4 * t.M,):
+            raise ValueError("Server.set_root: a and b must have 4M entries")
+        check(_lib.load().ef_server_set_root(self._h, int(tree), dptr(a), dptr(b)))
 
     def set_sweeps(self, tree: int, sweeps: int) -> None:
         """Refinement sweeps of the tree's blocks from the next block on."""

@@ -147,6 +147,14 @@ int ef_hps_synchronize(ef_hps* hps);
  * flux mismatch at every merge interface), so the result converges to the FP64 HPS solution.
  * Dirichlet root data (b == 0) only. */
 int ef_hps_mixed_init(ef_hps* hps, int bmax);
+/* Root operator of the block solvers (HPSAlgorithm.hpp:402-420 and the thermal driver's Neumann
+ * sides, examples/thermal/main.cpp:324-350): a u + b du/dn = r with a and b (4M each, WESN root face
+ * centres) fixed and r per request.  With b != 0 the root data become part of the refined state:
+ * every pass solves the root condition's residual with (diag a + diag b T_root)^{-1}, factored here
+ * in FP64 and applied in FP32; the per-request a arrays of the solve calls are then not read.
+ * b == 0 everywhere returns to per-request Dirichlet data.  Applies to the handle's block solvers
+ * and lanes until the next ef_hps_mixed_init.  EF_ERR_INVALID when the root matrix is singular. */
+int ef_hps_mixed_set_root(ef_hps* h, const double* a, const double* b);
 /* Resident buffers: f [B][num_leaves*n*n], a and r [B][4M] (root data, a u = r), u [B][...]. */
 int ef_hps_mixed_buffers(ef_hps* hps, double** f_dev, double** a_dev, double** r_dev, double** u_dev);
 /* 1 + sweeps passes on the first `batch` requests of the resident buffers, no host sync. */
@@ -281,6 +289,10 @@ int ef_server_create(ef_hps* const* trees, const int* bmax, int ntrees, int lane
                      long long hbm_budget_bytes, int sweeps, ef_server** out);
 /* refinement sweeps of tree t's blocks from the next block on (creation value: sweeps) */
 int ef_server_set_sweeps(ef_server* server, int tree, int sweeps);
+/* Root operator a u + b du/dn = r of one tree's lanes, as ef_hps_mixed_set_root, for the requests
+ * submitted afterwards (their a is then not read while b != 0).  The tree must have no request in
+ * flight (EF_ERR_INVALID otherwise); returns once the scheduler has put it in place. */
+int ef_server_set_root(ef_server* server, int tree, const double* a, const double* b);
 /* lanes created for tree t (after the budget) and device bytes held by all lanes */
 int ef_server_info(ef_server* server, int tree, int* lanes, long long* device_bytes);
 /* f (leaves*n*n), a and r (4M, WESN root face centres) and u (leaves*n*n) are host arrays that

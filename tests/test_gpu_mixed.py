@@ -272,3 +272,46 @@ def test_tensor_core_result_same_alone_and_in_a_block(ef):
     for k in (0, 4, 8):
         alone = hps.mixed_solve(F[k:k + 1], A[k:k + 1], R[k:k + 1], sweeps=1)
         assert np.array_equal(alone[0], block[k])
+
+
+def _root_operator(hps, pattern):
+    M = hps.M
+    if pattern == "thermal":  # Dirichlet on W/E, Neumann on S/N (examples/thermal/main.cpp:324-350)
+        a = np.concatenate([np.ones(2 * M), np.zeros(2 * M)])
+        b = np.concatenate([np.zeros(2 * M), np.ones(2 * M)])
+    else:                     # Robin everywhere
+        a = np.ones(4 * M)
+        b = np.full(4 * M, 0.25)
+    return a, b
+
+
+@pytest.mark.parametrize("pattern", ["thermal", "robin"])
+def test_mixed_robin_root_data_reach_fp64_solution(ef, pattern):
+    """a u + b du/dn = r with b != 0 in the block solver: the root data are refined with the rest of
+    the state (root condition residual, FP32 correction through (diag a + diag b T)^{-1}) and reach the
+    FP64 HPS solution (general root solve, HPSAlgorithm.hpp:402-420) to 1e-10 after one sweep; a
+    request's result is the same alone and in a block."""
+    mesh, hps = make(ef, ("uniform", 4), 16, (-1.0, 1.0, -1.0, 1.0))
+    a, b = _root_operator(hps, pattern)
+    F, _, R = requests(hps, mesh, 5, 77)
+    ref = []
+    for f, r in zip(F, R):
+        hps.upwards_array(f)
+        hps.solve_arrays(a, b, r)
+        ref.append(hps.leaf_solution())
+    hps.mixed_init(5)
+    hps.mixed_set_root(a, b)
+    A = np.zeros_like(R)  # not read while b != 0
+    u = hps.mixed_solve(F, A, R, sweeps=1)
+    for k in range(5):
+        err = np.abs(u[k] - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= TOL, (k, err)
+    alone = hps.mixed_solve(F[2:3], A[2:3], R[2:3], sweeps=1)
+    assert np.array_equal(alone[0], u[2])
+    # b = 0 returns to per-request Dirichlet data
+    hps.mixed_set_root(np.ones_like(a), np.zeros_like(b))
+    ud = hps.mixed_solve(F[:1], np.ones_like(R[:1]), R[:1], sweeps=1)
+    hps.upwards_array(F[0])
+    hps.solve_arrays(np.ones_like(a), np.zeros_like(b), R[0])
+    ref_d = hps.leaf_solution()
+    assert np.abs(ud[0] - ref_d).max() / np.abs(ref_d).max() <= TOL

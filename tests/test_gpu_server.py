@@ -90,3 +90,28 @@ def test_server_budget_limits_lanes(ef):
     srv.close()
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+def test_server_thermal_root_operator_mix_equals_alone(ef):
+    """A tree served with fixed Neumann sides (a = 0, b = 1 on S/N, Dirichlet on W/E, as the
+    reference's thermal driver solves its many right-hand sides): results within 1e-10 of the FP64
+    HPS solution and bit-identical to the same request alone."""
+    mesh, hps = tree(ef, "uniform")
+    M = hps.M
+    a = np.concatenate([np.ones(2 * M), np.zeros(2 * M)])
+    b = np.concatenate([np.zeros(2 * M), np.ones(2 * M)])
+    reqs = [request(mesh, hps, 300 + k) for k in range(12)]
+    srv = ef.Server([hps], bmax=5, lanes=2, sweeps=1)
+    srv.set_root(0, a, b)
+    ids = [srv.submit(0, f, np.zeros_like(r), r) for f, _, r in reqs]
+    results = [srv.wait(i)[0] for i in ids]
+    srv.close()
+    hps.mixed_init(1)
+    hps.mixed_set_root(a, b)
+    for k, (f, _, r) in enumerate(reqs):
+        alone = hps.mixed_solve(f[None], np.zeros_like(r)[None], r[None], sweeps=1)[0]
+        assert np.array_equal(results[k], alone), k
+        hps.upwards_array(f)
+        hps.solve_arrays(a, b, r)
+        ref = hps.leaf_solution()
+        assert np.abs(results[k] - ref).max() / np.abs(ref).max() <= 1e-10
