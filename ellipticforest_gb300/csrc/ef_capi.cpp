@@ -347,6 +347,13 @@ int ef_hps_set_stream(ef_hps* h, void* stream) {
     return EF_OK;
 }
 
+int ef_hps_build_info(const ef_hps* h, long long* merge_launches, long long* graph_replays) {
+    if (!h) return fail(EF_ERR_INVALID, "null handle");
+    if (merge_launches) *merge_launches = h->hps->build_launches();
+    if (graph_replays) *graph_replays = h->hps->build_replays();
+    return EF_OK;
+}
+
 int ef_hps_root_factorizations(const ef_hps* h, long long* count) {
     if (!h || !count) return fail(EF_ERR_INVALID, "null argument");
     *count = h->hps->root_factorizations();

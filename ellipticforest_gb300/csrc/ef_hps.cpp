@@ -535,7 +535,11 @@ void Hps::build() {
     root_lu_valid_ = false;
     top_level_ = -1;
     build_leaf_types();
-    merge_levels(mesh_.max_level - 1);
+    // the merges of every level (a fixed launch sequence for this tree) replay as a CUDA graph from
+    // the third build on (first eager, second captured); the leaf DtN maps above stay eager
+    const long long l0 = g_kernel_launches.load();
+    graph_build_.run(st_, 1, graphs_ && !prof_, [&] { merge_levels(mesh_.max_level - 1); });
+    build_launches_ = g_kernel_launches.load() - l0;
     check(cudaGetLastError(), "build launch");
     check(cudaStreamSynchronize(st_), "build sync");
     singular_ = count_singular(mesh_.max_level) + leaf_singular_;

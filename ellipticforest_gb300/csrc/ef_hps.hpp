@@ -145,11 +145,16 @@ void GraphCache::run(cudaStream_t& stream, long long key, bool enabled, F&& body
             try {
                 body();
             } catch (...) {
+                // a step that cannot be captured: drop the capture and run the sequence eagerly
+                // from now on (a real error then surfaces from the eager run)
                 stream = orig;
                 cudaStreamEndCapture(cap_, &g);
                 if (g) cudaGraphDestroy(g);
                 (void)cudaGetLastError();
-                throw;
+                g_kernel_launches -= g_kernel_launches.load() - l0;
+                e->failed = true;
+                body();
+                return;
             }
             stream = orig;
             ok = cudaStreamEndCapture(cap_, &g) == cudaSuccess && g;
@@ -226,6 +231,9 @@ public:
     void upwards_top(int level, const double* const* h_host);
     void solve_top(int level, double* const* g_host);  // root data from bc_a/b/r
     int top_level() const { return top_level_; }      // -1 unless built by build_top
+    // kernels launched by the merges of the last build(), and builds replayed from a CUDA graph
+    long long build_launches() const { return build_launches_; }
+    long long build_replays() const { return graph_build_.replays(); }
     void upwards();                                // HPSAlgorithm::upwardsStage on leaf_f()
     void root_from_bc();                           // root g from bc_a/b/r (HPSAlgorithm.hpp:402-420)
     void downwards();                              // split1to4 + leafSolve for every node
@@ -377,6 +385,8 @@ private:
     // MixedSolver::tune and shared by every block solver of the tree
     std::vector<std::array<int, 3>> mx_split_;
     GraphCache graph_solve_;
+    GraphCache graph_build_;
+    long long build_launches_ = 0;
     std::vector<ProfStat> stats_;
     std::vector<Mark> marks_;
     std::vector<cudaEvent_t> ev_free_;

@@ -220,6 +220,161 @@ __device__ __forceinline__ TcSeg tc_seg(const MixItem* __restrict__ items, int s
     return t;
 }
 
+// Epilogue of one tile row: v[q] = (A X)[row][b0 + q] for the 32 requests of this request block.
+// All loads of the row's operands are issued before its stores (the arrays of an item may alias as
+// far as the compiler knows); 16-byte accesses when B % 4 == 0.
+template <int KIND>
+__device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, int s, int B, int b0, int rows_item,
+                                             int grow, const float (&v)[32], bool vec) {
+    const int item = grow / rows_item, r = grow - item * rows_item;
+    const MixItem& it = items[item];
+    const int nb = min(32, B - b0);
+    const long long cb = (long long)b0;
+    if (KIND == MX_W) {
+        float* dst = it.w + (long long)r * B + cb;
+        if (vec) {
+#pragma unroll
+            for (int q = 0; q < 32; q += 4)
+                if (q < nb) *reinterpret_cast<float4*>(dst + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 32; ++q)
+                if (q < nb) dst[q] = v[q];
+        }
+    } else if (KIND == MX_H) {
+        const int p = tc_h_unpermute(r, s);
+        int c, q2;
+        mx_ext_map(p, s, c, q2);
+        const float* hp = it.hc[c] + (long long)q2 * B + cb;
+        float* dst = it.h + (long long)p * B + cb;
+        if (vec) {
+            float4 h4[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                h4[i] = 4 * i < nb ? *reinterpret_cast<const float4*>(hp + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (4 * i < nb)
+                    *reinterpret_cast<float4*>(dst + 4 * i) = make_float4(v[4 * i] + h4[i].x, v[4 * i + 1] + h4[i].y,
+                                                                          v[4 * i + 2] + h4[i].z, v[4 * i + 3] + h4[i].w);
+        } else {
+            float hv[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) hv[q] = q < nb ? hp[q] : 0.f;
+#pragma unroll
+            for (int q = 0; q < 32; ++q)
+                if (q < nb) dst[q] = v[q] + hv[q];
+        }
+    } else {
+        const int I = r / s, o = r - (r / s) * s;
+        const float* wp = it.w + (long long)r * B + cb;
+        float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
+        float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
+        double* ug = it.uG + (long long)r * B + cb;
+        // two halves of 16 requests, each with all of its loads ahead of its stores
+#pragma unroll
+        for (int hf = 0; hf < 2; ++hf) {
+            const int q0 = 16 * hf;
+            float uu[16];
+            if (vec) {
+                float4 w4[4];
+                double2 u2[8];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    w4[i] = q0 + 4 * i < nb ? *reinterpret_cast<const float4*>(wp + q0 + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    u2[i] = q0 + 2 * i < nb ? *reinterpret_cast<const double2*>(ug + q0 + 2 * i) : make_double2(0.0, 0.0);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    uu[4 * i] = v[q0 + 4 * i] + w4[i].x;
+                    uu[4 * i + 1] = v[q0 + 4 * i + 1] + w4[i].y;
+                    uu[4 * i + 2] = v[q0 + 4 * i + 2] + w4[i].z;
+                    uu[4 * i + 3] = v[q0 + 4 * i + 3] + w4[i].w;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (q0 + 4 * i < nb) {
+                        const float4 o4 = make_float4(uu[4 * i], uu[4 * i + 1], uu[4 * i + 2], uu[4 * i + 3]);
+                        *reinterpret_cast<float4*>(d0 + q0 + 4 * i) = o4;
+                        *reinterpret_cast<float4*>(d1 + q0 + 4 * i) = o4;
+                    }
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (q0 + 2 * i < nb)
+                        *reinterpret_cast<double2*>(ug + q0 + 2 * i) =
+                            make_double2(u2[i].x + f2d_bits(uu[2 * i]), u2[i].y + f2d_bits(uu[2 * i + 1]));
+            } else {
+                float wv[16];
+                double uv[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    wv[i] = q0 + i < nb ? wp[q0 + i] : 0.f;
+                    uv[i] = q0 + i < nb ? ug[q0 + i] : 0.0;
+                }
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    if (q0 + i < nb) {
+                        uu[i] = v[q0 + i] + wv[i];
+                        d0[q0 + i] = uu[i];
+                        d1[q0 + i] = uu[i];
+                        ug[q0 + i] = uv[i] + f2d_bits(uu[i]);
+                    }
+            }
+        }
+    }
+}
+
+// exterior points of a parent go to its children unchanged: rows [p0, p1) of one item, all
+// requests, spread over the 128 epilogue threads with four loads in flight before their stores
+__device__ __forceinline__ void tc_ext_copy(const MixItem& it, int s, int B, int p0, int p1, int t) {
+    if ((B & 3) == 0) {
+        const int w4 = B >> 2, tot = (p1 - p0) * w4;
+        for (int e0 = t; e0 < tot; e0 += 4 * 128) {
+            float4 val[4];
+            float4* dst[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * 128;
+                dst[u] = nullptr;
+                if (e < tot) {
+                    const int p = p0 + e / w4, b4 = e - (e / w4) * w4;
+                    int c, q;
+                    mx_ext_map(p, s, c, q);
+                    val[u] = reinterpret_cast<const float4*>(it.gf + (long long)p * B)[b4];
+                    dst[u] = reinterpret_cast<float4*>(it.gc[c] + (long long)q * B) + b4;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (dst[u]) *dst[u] = val[u];
+        }
+    } else {
+        const int tot = (p1 - p0) * B;
+        for (int e = t; e < tot; e += 128) {
+            const int p = p0 + e / B, bb = e - (e / B) * B;
+            int c, q;
+            mx_ext_map(p, s, c, q);
+            it.gc[c][(long long)q * B + bb] = it.gf[(long long)p * B + bb];
+        }
+    }
+}
+
+// the share of a DOWN tile: the exterior rows of the nodes its rows belong to (a node of >= 128
+// rows splits them over its tiles)
+__device__ __forceinline__ void tc_ext_copy_tile(const MixItem* __restrict__ items, int s, int B, int cnt,
+                                                 int rows_item, int tile, int t) {
+    const int rows = 8 * s;
+    if (rows_item >= kTM) {
+        const int tpi = rows_item / kTM, item = tile / tpi, tl = tile - item * tpi;
+        const int per = (rows + tpi - 1) / tpi;
+        tc_ext_copy(items[item], s, B, tl * per, min(rows, tl * per + per), t);
+    } else {
+        const int ipt = kTM / rows_item;
+        for (int item = tile * ipt; item < min(cnt, tile * ipt + ipt); ++item) tc_ext_copy(items[item], s, B, 0, rows, t);
+    }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_mx_umma(const __grid_constant__ CUtensorMap tmA, const MixItem* __restrict__ items, int s, int B, int cnt,
@@ -400,27 +555,40 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const int k0 = (cbase + c) * kTK;
             const int b = t & 31, n = b;
             const int gb = b0 + b;
-            // pairs (k, k + 1) of one request: 32 per block, four pair rows per pass of the warps
-            for (int i = 0; i < 8 * nseg; ++i) {
-                const int P = (t >> 5) + 4 * i;
-                const int j = P >> 5, kp = P & 31;
-                const int k = k0 + 2 * kp;
-                float x0 = 0.f, x1 = 0.f;
-                if (sval[j] && gb < B) {
-                    const TcSeg& sg = seg[j];
-                    if (k < K) x0 = (k < sg.kb ? sg.X1 : sg.X2)[(long long)k * B + gb];
-                    if (k + 1 < K) x1 = (k + 1 < sg.kb ? sg.X1 : sg.X2)[(long long)(k + 1) * B + gb];
+            // pairs (k, k + 1) of one request: 32 per block, four pair rows per pass of the warps;
+            // every load of the chunk is issued before the bf16 parts are written
+            float xv[2 * 8 * kMaxSeg];
+#pragma unroll
+            for (int i = 0; i < 8 * kMaxSeg; ++i) {
+                xv[2 * i] = 0.f;
+                xv[2 * i + 1] = 0.f;
+                if (i < 8 * nseg) {
+                    const int P = (t >> 5) + 4 * i;
+                    const int j = P >> 5, kp = P & 31;
+                    const int k = k0 + 2 * kp;
+                    if (sval[j] && gb < B) {
+                        const TcSeg& sg = seg[j];
+                        if (k < K) xv[2 * i] = (k < sg.kb ? sg.X1 : sg.X2)[(long long)k * B + gb];
+                        if (k + 1 < K) xv[2 * i + 1] = (k + 1 < sg.kb ? sg.X1 : sg.X2)[(long long)(k + 1) * B + gb];
+                    }
                 }
-                __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
-                split3(x0, p0a, p1a, p2a);
-                split3(x1, p0b, p1b, p2b);
-                const int kl = 2 * kp;
-                const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
-                                     ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
-                const unsigned xp = unsigned(nseg) * kPlaneX;
-                *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
-                *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
-                *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+            }
+            const unsigned xp = unsigned(nseg) * kPlaneX;
+#pragma unroll
+            for (int i = 0; i < 8 * kMaxSeg; ++i) {
+                if (i < 8 * nseg) {
+                    const int P = (t >> 5) + 4 * i;
+                    const int j = P >> 5, kp = P & 31;
+                    __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
+                    split3(xv[2 * i], p0a, p1a, p2a);
+                    split3(xv[2 * i + 1], p0b, p1b, p2b);
+                    const int kl = 2 * kp;
+                    const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
+                                         ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
+                    *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
+                    *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
+                    *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+                }
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_arrive(&x_full[st]);
@@ -474,67 +642,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
             // ---- stores ----
             const int grow = tile * kTM + t;
-            if (grow < R) {
-                const int item = grow / sh.rows_item, r = grow - item * sh.rows_item;
-                const MixItem& it = items[item];
-                const long long cb = (long long)b0;
-                if (KIND == MX_W) {
-                    float* dst = it.w + (long long)r * B + cb;
-                    if (vec) {
-#pragma unroll
-                        for (int q = 0; q < 32; q += 4)
-                            if (b0 + q < B) *reinterpret_cast<float4*>(dst + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
-                    } else {
-                        for (int q = 0; q < 32; ++q)
-                            if (b0 + q < B) dst[q] = v[q];
-                    }
-                } else if (KIND == MX_H) {
-                    const int p = tc_h_unpermute(r, s);
-                    int c, q2;
-                    mx_ext_map(p, s, c, q2);
-                    const float* hp = it.hc[c] + (long long)q2 * B + cb;
-                    float* dst = it.h + (long long)p * B + cb;
-                    for (int q = 0; q < 32; ++q)
-                        if (b0 + q < B) dst[q] = v[q] + hp[q];
-                } else {
-                    const int I = r / s, o = r - (r / s) * s;
-                    const float* wp = it.w + (long long)r * B + cb;
-                    float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
-                    float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
-                    double* ug = it.uG + (long long)r * B + cb;
-                    for (int q = 0; q < 32; ++q)
-                        if (b0 + q < B) {
-                            const float uv = v[q] + wp[q];
-                            d0[q] = uv;
-                            d1[q] = uv;
-                            ug[q] += f2d_bits(uv);
-                        }
-                }
-            }
-            if (KIND == MX_DOWN && blockIdx.y == 0) {
-                // exterior points of the parent go to the children unchanged: this tile copies its
-                // share of the exterior rows of the nodes it covers
-                const int rows = 8 * s;
-                int i0, i1, p0, p1;
-                if (sh.rows_item >= kTM) {
-                    const int tpi = sh.rows_item / kTM, item = tile / tpi, tl = tile - item * tpi;
-                    const int per = (rows + tpi - 1) / tpi;
-                    i0 = item; i1 = item + 1; p0 = tl * per; p1 = min(rows, p0 + per);
-                } else {
-                    const int ipt = kTM / sh.rows_item;
-                    i0 = tile * ipt; i1 = min(cnt, i0 + ipt); p0 = 0; p1 = rows;
-                }
-                for (int item = i0; item < i1; ++item) {
-                    const MixItem& it = items[item];
-                    const int tot = (p1 - p0) * B;
-                    for (int e = t; e < tot; e += 128) {
-                        const int p = p0 + e / B, bb = e - (e / B) * B;
-                        int c, q2;
-                        mx_ext_map(p, s, c, q2);
-                        it.gc[c][(long long)q2 * B + bb] = it.gf[(long long)p * B + bb];
-                    }
-                }
-            }
+            if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, vec);
+            if (KIND == MX_DOWN && blockIdx.y == 0) tc_ext_copy_tile(items, s, B, cnt, sh.rows_item, tile, t);
         }
         if (!ok) atomicExch(err, 1);
     }
@@ -562,54 +671,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             const int tile = first_tile;
             const int grow = tile * kTM + t;
-            if (grow < R) {
-                const int item = grow / sh.rows_item, r = grow - item * sh.rows_item;
-                const MixItem& it = items[item];
-                const long long cb = (long long)b0;
-                if (KIND == MX_W) {
-                    float* dst = it.w + (long long)r * B + cb;
-                    for (int q = 0; q < 32; ++q)
-                        if (b0 + q < B) dst[q] = v[q];
-                } else if (KIND == MX_H) {
-                    const int p = tc_h_unpermute(r, s);
-                    int c, q2;
-                    mx_ext_map(p, s, c, q2);
-                    const float* hp = it.hc[c] + (long long)q2 * B + cb;
-                    float* dst = it.h + (long long)p * B + cb;
-                    for (int q = 0; q < 32; ++q)
-                        if (b0 + q < B) dst[q] = v[q] + hp[q];
-                } else {
-                    const int I = r / s, o = r - (r / s) * s;
-                    const float* wp = it.w + (long long)r * B + cb;
-                    float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
-                    float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
-                    double* ug = it.uG + (long long)r * B + cb;
-                    for (int q = 0; q < 32; ++q)
-                        if (b0 + q < B) {
-                            const float uv = v[q] + wp[q];
-                            d0[q] = uv;
-                            d1[q] = uv;
-                            ug[q] += f2d_bits(uv);
-                        }
-                }
-            }
-            if (KIND == MX_DOWN && blockIdx.y == 0) {
-                const int rows = 8 * s;
-                const int tpi = sh.rows_item >= kTM ? sh.rows_item / kTM : 1;
-                const int item = sh.rows_item >= kTM ? tile / tpi : tile, tl = sh.rows_item >= kTM ? tile - item * tpi : 0;
-                const int per = (rows + tpi - 1) / tpi;
-                const int p0 = tl * per, p1 = min(rows, p0 + per);
-                if (item < cnt) {
-                    const MixItem& it = items[item];
-                    const int tot = (p1 - p0) * B;
-                    for (int e = t; e < tot; e += 128) {
-                        const int p = p0 + e / B, bb = e - (e / B) * B;
-                        int c, q2;
-                        mx_ext_map(p, s, c, q2);
-                        it.gc[c][(long long)q2 * B + bb] = it.gf[(long long)p * B + bb];
-                    }
-                }
-            }
+            if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, (B & 3) == 0);
+            if (KIND == MX_DOWN && blockIdx.y == 0) tc_ext_copy_tile(items, s, B, cnt, sh.rows_item, tile, t);
         }
         cluster.sync();
     }

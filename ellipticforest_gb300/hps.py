@@ -476,6 +476,12 @@ class HPSAlgorithm:
         self._apply_options()
         check(_lib.load().ef_hps_build(self._h))
 
+    def build_info(self):
+        """(kernels launched by the merges of the last build, builds replayed from a CUDA graph)"""
+        a, b = C.c_longlong(), C.c_longlong()
+        check(_lib.load().ef_hps_build_info(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def buildStageFrom(self, old: "HPSAlgorithm") -> int:
         """Build reusing the merges of `old` (a built tree on another mesh of the same domain) whose
         subtrees are unchanged; returns the number of reused merges (no reference counterpart)."""

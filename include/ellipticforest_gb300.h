@@ -91,6 +91,11 @@ int ef_hps_root_factorizations(const ef_hps* hps, long long* count);
 int ef_hps_setup(ef_hps* hps);
 /* HPSAlgorithm::buildStage (HPSAlgorithm.hpp:120-161): leaf DtN maps and all 4-to-1 merges. */
 int ef_hps_build(ef_hps* hps);
+/* Kernels launched by the merges of the last ef_hps_build (the leaf DtN maps excluded) and how many
+ * builds of this handle were replayed from a CUDA graph: with "cuda-graphs" on (default), the merge
+ * sequence of a tree runs eagerly on its first build, is captured on the second and replayed from
+ * the third on (a build is the same launch sequence every time; no counterpart in the reference). */
+int ef_hps_build_info(const ef_hps* h, long long* merge_launches, long long* graph_replays);
 /* Mixed-precision build (no counterpart in the reference): the same merges with FP32 operators,
  * except the interface LU of the top fp64_levels tree levels (FP64, factors rounded to FP32).  It
  * prepares the tree for the mixed block solver and the server only (ef_hps_mixed_*, ef_server_*);

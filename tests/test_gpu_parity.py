@@ -427,3 +427,30 @@ def test_cooperative_lu_panel_matches_single_cta(ef):
         Ts.append(hps.root_T())
     check(load().ef_hps_set_option(hps.handle, b"cooperative-lu", 1))
     assert np.array_equal(Ts[0], Ts[1])
+
+
+def test_build_graph_replay_equals_eager(ef):
+    """The merges of a build run as one captured CUDA graph from the third build of a handle on (the
+    first eager, the second captured): the same kernels, and the root T and a solve bit-identical to
+    an eager build."""
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(16, -1.0, 1.0, 16, -1.0, 1.0))
+    mesh = ef.Mesh().uniform(4, root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    f, bc = _random_problem(31)
+    hps.set_graphs(False)
+    hps.buildStage()
+    T0 = hps.root_T()
+    n0, rep0 = hps.build_info()
+    hps.upwardsStage(f)
+    hps.solveStage(bc)
+    u0 = hps.leaf_solution()
+    hps.set_graphs(True)
+    for _ in range(3):
+        hps.buildStage()
+    n1, rep1 = hps.build_info()
+    assert rep1 >= 1 and n1 == n0 > 0
+    assert np.array_equal(hps.root_T(), T0)
+    hps.set_graphs(False)
+    hps.upwardsStage(f)
+    hps.solveStage(bc)
+    assert np.array_equal(hps.leaf_solution(), u0)
