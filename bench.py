@@ -555,6 +555,10 @@ def run_gb300(args):
                     "api": "ef_hps_mixed_solve_blocks (K blocks per call, three lanes, pinned host arrays)",
                     "one_block_per_call_solves_per_s": e2e_single},
             "gpu_launches": int(launches),
+            "mixed_gemm_plan": {"columns": ["level", "s", "W", "H", "DOWN"],
+                                "codes": "> 0: FP32 CUDA-core GEMM with that K split; < 0: tcgen05 GEMM, K split -code",
+                                "groups": [list(r) for r in hps.mixed_gemm_plan()]},
+            "build_merge_launches": hps.build_info()[0],
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": (TRAFFIC_RATIO[dom_name] * d["bytes"] / max(d["calls"], 1)
@@ -1012,6 +1016,38 @@ def many_rhs(ef, torch, stream, args):
             "speedup": mixed / plain, "rel_err_vs_fp64": err, "mdof_per_s": mixed * mesh.cell_centres()[0].size / 1e6}
 
 
+def run_profile_only(args):
+    """The build (or the mixed blocks) of the headline tree alone, for an ncu launch list."""
+    import torch
+    import ellipticforest_gb300 as ef
+    from ellipticforest_gb300 import build as efbuild
+    efbuild.build()
+    stream = torch.cuda.current_stream()
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(args.n, DOM[0], DOM[1], args.n, DOM[2], DOM[3]))
+    mesh = ef.Mesh().uniform(args.level, root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
+    hps.set_stream(stream.cuda_stream)
+    hps.setupStage()
+    hps.buildStage()
+    torch.cuda.synchronize()
+    out = {"profile_only": args.profile_only, "level": args.level, "build_merge_launches": hps.build_info()[0]}
+    if args.profile_only == "mixed":
+        X, Y = mesh.cell_centres()
+        bpts = hps.boundary_points()
+        reqs = [make_request(1000 + i, X, Y, bpts) for i in range(4)]
+        B = args.batch
+        F = np.stack([reqs[i % 4][0] for i in range(B)])
+        A = np.stack([reqs[i % 4][1] for i in range(B)])
+        R = np.stack([reqs[i % 4][3] for i in range(B)])
+        hps.mixed_init(B)
+        hps.mixed_solve(F, A, R, args.sweeps)
+        for _ in range(args.steps):
+            hps.mixed_solve_async(B, args.sweeps)
+        torch.cuda.synchronize()
+        out["gemm_plan"] = hps.mixed_gemm_plan()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1031,12 +1067,17 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=30, help="timed steps of the plain FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 512-RHS level-6 case")
+    ap.add_argument("--profile-only", choices=["build", "mixed"], default=None,
+                    help="short run for a profiler's launch list: 'build' = set-up and one FP64 build of the "
+                         "tree; 'mixed' = build, block-solver set-up and --steps mixed blocks (no timing line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     gc.disable()  # no collector pauses inside the timed loops (nothing here builds reference cycles)
     if args.impl == "reference":
         run_reference(args)
+    elif args.profile_only:
+        run_profile_only(args)
     else:
         run_gb300(args)
 

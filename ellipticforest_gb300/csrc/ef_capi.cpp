@@ -332,7 +332,8 @@ int ef_hps_set_option(ef_hps* h, const char* key, int value) {
             return EF_OK;
         });
     } else if (k == "tensor-cores") {
-        h->hps->set_tensor_cores(value != 0);  // block solvers created from now on
+        if (value < 0 || value > 2) return fail(EF_ERR_INVALID, "tensor-cores: 0 off, 1 tuned, 2 forced");
+        h->hps->set_tensor_cores(value);  // block solvers created from now on
     } else if (k == "cooperative-lu") {
         efgb::g_cooperative_lu.store(value != 0);  // process-wide
     } else {
@@ -710,6 +711,17 @@ int ensure_lane(ef_hps* h, int k) {
 
 efgb::MixedSolver* lane_solver(ef_hps* h, int lane) { return lane == 0 ? h->mixed.get() : h->lanes[lane].get(); }
 }  // namespace
+
+int ef_hps_mixed_gemm_plan(ef_hps* h, int max_groups, int* table, int* ngroups) {
+    if (!h || !ngroups) return fail(EF_ERR_INVALID, "null argument");
+    if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");
+    const auto plan = h->mixed->gemm_plan();
+    *ngroups = int(plan.size());
+    if (table)
+        for (int i = 0; i < int(plan.size()) && i < max_groups; ++i)
+            for (int k = 0; k < 5; ++k) table[5 * i + k] = plan[i][k];
+    return EF_OK;
+}
 
 int ef_hps_mixed_set_root(ef_hps* h, const double* a, const double* b) {
     if (!h || !a || !b) return fail(EF_ERR_INVALID, "null argument");

@@ -195,9 +195,10 @@ public:
     // CUDA-graph replay of the solve sequences (on by default; profiling runs them eagerly)
     void set_graphs(bool on) { graphs_ = on; }
     bool graphs() const { return graphs_; }
-    // tcgen05 node GEMMs in the mixed solver (default on; block solvers created afterwards follow it)
-    void set_tensor_cores(bool on) { tensor_cores_ = on; }
-    bool tensor_cores() const { return tensor_cores_; }
+    // tcgen05 node GEMMs in the mixed solver for block solvers created afterwards: 0 off, 1 (default)
+    // wherever the autotuner times them faster than the CUDA-core GEMMs, 2 wherever supported
+    void set_tensor_cores(int mode) { tensor_cores_ = mode; }
+    int tensor_cores() const { return tensor_cores_; }
     // FivePointStencil: per-leaf coefficients sampled at the reference's points (host arrays in leaf
     // order: alpha n*n, beta 4*n*n (W, E, S, N face of every cell), lambda n*n per leaf)
     void set_coefficients(const double* alpha, const double* beta, const double* lambda);
@@ -379,8 +380,8 @@ private:
 
     bool prof_ = false;
     bool graphs_ = true;
-    bool tensor_cores_ = true;
-    bool mx_split_tc_ = false;  // mx_split_ was tuned with the tensor-core path
+    int tensor_cores_ = 1;
+    int mx_split_tc_ = -1;  // tensor-core mode mx_split_ was tuned with
     // K split of the mixed form's node GEMMs per group and kind (W, H, DOWN), chosen once per tree by
     // MixedSolver::tune and shared by every block solver of the tree
     std::vector<std::array<int, 3>> mx_split_;
@@ -432,6 +433,9 @@ public:
     // per-request a.  Otherwise the root data become part of the state and every pass solves for
     // their correction with Z = (diag a + diag b T_root)^{-1}, factored in FP64 here (synchronous).
     void set_root_operator(const double* a, const double* b);
+    // per node group: {level, s, code W, code H, code DOWN} of the tuned node GEMMs (code > 0: CUDA-core
+    // kernel with that K split, code < 0: tensor-core kernel with K split -code)
+    std::vector<std::array<int, 5>> gemm_plan() const;
     bool robin() const { return robin_; }
     // synchronises the stream; 1 when a kernel gave up waiting on a TMA copy since the last call
     int take_error();
@@ -467,8 +471,9 @@ private:
     };
     void residual(int B, double* rmax, bool zero_state);
     void pass(int B, bool first);
-    // one node GEMM of a group (kind 0 W, 1 H, 2 DOWN) on the tensor-core or the FP32 CUDA-core path
-    void node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int ksplit);
+    // one node GEMM of a group (kind 0 W, 1 H, 2 DOWN): code > 0 the FP32 CUDA-core kernel with K
+    // split `code` (0: its heuristic), code < 0 the tensor-core kernel with K split -code
+    void node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code);
     // times the K-split candidates of every node GEMM (CUDA events, block of min(bmax, 32)) and keeps
     // the fastest per group and kind in the tree
     void tune();

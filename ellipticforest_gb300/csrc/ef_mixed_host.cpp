@@ -175,7 +175,7 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             groups_[gi].Xi32 = Xi;
             groups_[gi].H32 = H32;
             // bf16 planes of the tensor-core path (3 x the FP32 element count, 2 bytes each)
-            const bool tc = hps.tensor_cores() && mx_tc_supported(0, g.s) && mx_tc_supported(1, g.s) &&
+            const bool tc = hps.tensor_cores() != 0 && mx_tc_supported(0, g.s) && mx_tc_supported(1, g.s) &&
                             mx_tc_supported(2, g.s);
             groups_[gi].tc = tc;
             if (tc) {
@@ -354,35 +354,52 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     }
     ck(cudaGetLastError(), "mixed convert");
     ck(cudaStreamSynchronize(st), "mixed setup");
-    const bool any_tc = std::any_of(groups_.begin(), groups_.end(), [](const MGroup& g) { return g.tc; });
-    if (hps.mx_split_.size() != groups_.size() || hps.mx_split_tc_ != any_tc) tune();
+    if (hps.mx_split_.size() != groups_.size() || hps.mx_split_tc_ != hps.tensor_cores()) tune();
 }
 
 void MixedSolver::tune() {
+    // per group and kind, the fastest of the CUDA-core GEMM (K split 1, 2, 4, ...: code > 0) and the
+    // tensor-core GEMM (code < 0: split -code), timed with CUDA events on a block of min(bmax, 32)
     Hps& h = H_;
     const int B = std::min(bmax_, 32);
     std::vector<std::array<int, 3>> best(groups_.size(), std::array<int, 3>{1, 1, 1});
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ck(cudaEventCreate(&e0), "tune event");
     ck(cudaEventCreate(&e1), "tune event");
+    auto time_code = [&](const MGroup& g, int kind, int code) {
+        node_gemm(st_, g, kind, B, code);  // warm-up
+        ck(cudaEventRecord(e0, st_), "tune event");
+        for (int r = 0; r < 3; ++r) node_gemm(st_, g, kind, B, code);
+        ck(cudaEventRecord(e1, st_), "tune event");
+        ck(cudaEventSynchronize(e1), "tune sync");
+        float ms = 0.f;
+        ck(cudaEventElapsedTime(&ms, e0, e1), "tune time");
+        return ms;
+    };
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
         const MGroup& g = groups_[gi];
         for (int kind = 0; kind < 3; ++kind) {
-            const int kmax = g.tc ? mx_tc_max_split(kind, g.s) : mx_gemm_max_split(kind, g.s);
             float best_ms = 1e30f;
-            for (int ks = 1; ks <= kmax; ks *= 2) {
-                node_gemm(st_, g, kind, B, ks);  // warm-up
-                ck(cudaEventRecord(e0, st_), "tune event");
-                for (int r = 0; r < 3; ++r) node_gemm(st_, g, kind, B, ks);
-                ck(cudaEventRecord(e1, st_), "tune event");
-                ck(cudaEventSynchronize(e1), "tune sync");
-                float ms = 0.f;
-                ck(cudaEventElapsedTime(&ms, e0, e1), "tune time");
-                if (ms < best_ms * 0.97f) {  // a larger split must win clearly
-                    best_ms = ms;
-                    best[gi][kind] = ks;
+            int best_code = 1;
+            const bool forced = g.tc && h.tensor_cores() == 2;
+            for (int pass = forced ? 1 : 0; pass < (g.tc ? 2 : 1); ++pass) {
+                const bool tc = pass == 1;
+                const int kmax = tc ? mx_tc_max_split(kind, g.s) : mx_gemm_max_split(kind, g.s);
+                float path_ms = 1e30f;
+                int path_code = 0;
+                for (int ks = 1; ks <= kmax; ks *= 2) {
+                    const float ms = time_code(g, kind, tc ? -ks : ks);
+                    if (ms < path_ms * 0.97f) {  // a larger split must win clearly
+                        path_ms = ms;
+                        path_code = tc ? -ks : ks;
+                    }
+                }
+                if (path_ms < best_ms) {
+                    best_ms = path_ms;
+                    best_code = path_code;
                 }
             }
+            best[gi][kind] = best_code;
         }
     }
     cudaEventDestroy(e0);
@@ -392,17 +409,28 @@ void MixedSolver::tune() {
     // the tuning launches wrote the pass buffers and the interface state: start clean
     ck(cudaMemsetAsync(arena_, 0, size_t(uG_begin_ - arena_) + uG_bytes_, st_), "clear after tune");
     h.mx_split_ = best;
-    h.mx_split_tc_ = std::any_of(groups_.begin(), groups_.end(), [](const MGroup& g) { return g.tc; });
+    h.mx_split_tc_ = h.tensor_cores();
 }
 
-void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int ksplit) {
-    if (g.tc) {
+void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code) {
+    if (g.tc && code < 0) {
         const CUtensorMap& tm = kind == 0 ? g.tmXi3 : (kind == 1 ? g.tmH3 : g.tmS3);
-        mx_gemm_tc(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ksplit < 1 ? 1 : ksplit);
+        mx_gemm_tc(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, -code);
     } else {
+        const int ksplit = code < 0 ? 0 : code;
         const CUtensorMap& tm = kind == 0 ? g.tmXi : (kind == 1 ? g.tmH : g.tmS);
         mx_gemm(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, ksplit);
     }
+}
+
+std::vector<std::array<int, 5>> MixedSolver::gemm_plan() const {
+    std::vector<std::array<int, 5>> out;
+    const Hps& h = H_;
+    for (size_t gi = 0; gi < groups_.size(); ++gi) {
+        const std::array<int, 3> c = h.mx_split_.size() == groups_.size() ? h.mx_split_[gi] : std::array<int, 3>{0, 0, 0};
+        out.push_back({groups_[gi].level, groups_[gi].s, c[0], c[1], c[2]});
+    }
+    return out;
 }
 
 MixedSolver::~MixedSolver() {

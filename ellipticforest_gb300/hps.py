@@ -642,6 +642,15 @@ class HPSAlgorithm:
         check(_lib.load().ef_hps_mixed_init(self._h, int(bmax)))
         self.mixed_bmax = int(bmax)
 
+    def mixed_gemm_plan(self):
+        """[(level, s, code W, code H, code DOWN)] of the tuned node GEMMs: code > 0 CUDA-core kernel
+        with that K split, code < 0 tensor-core kernel with K split -code."""
+        n = C.c_int()
+        check(_lib.load().ef_hps_mixed_gemm_plan(self._h, 0, None, C.byref(n)))
+        t = (C.c_int * (5 * n.value))()
+        check(_lib.load().ef_hps_mixed_gemm_plan(self._h, n.value, t, C.byref(n)))
+        return [tuple(t[5 * i:5 * i + 5]) for i in range(n.value)]
+
     def mixed_set_root(self, a, b):
         """Fixed root operator a u + b du/dn = r of the block solver (r per request); b = 0 returns
         to per-request Dirichlet data (no reference counterpart: the reference solves one request)."""

@@ -159,6 +159,12 @@ int ef_hps_mixed_init(ef_hps* hps, int bmax);
  * in FP64 and applied in FP32; the per-request a arrays of the solve calls are then not read.
  * b == 0 everywhere returns to per-request Dirichlet data.  Applies to the handle's block solvers
  * and lanes until the next ef_hps_mixed_init.  EF_ERR_INVALID when the root matrix is singular. */
+/* No counterpart in the reference.  The node-GEMM plan the block solver's autotuner chose (timed
+ * once per tree): per node group {level, s, W, H, DOWN}, each code > 0 = FP32 CUDA-core kernel with
+ * that K split, < 0 = tcgen05 tensor-core kernel with K split -code.  table: 5 * max_groups ints (or
+ * NULL to query the count in *ngroups). */
+int ef_hps_mixed_gemm_plan(ef_hps* h, int max_groups, int* table, int* ngroups);
+
 int ef_hps_mixed_set_root(ef_hps* h, const double* a, const double* b);
 /* Resident buffers: f [B][num_leaves*n*n], a and r [B][4M] (root data, a u = r), u [B][...]. */
 int ef_hps_mixed_buffers(ef_hps* hps, double** f_dev, double** a_dev, double** r_dev, double** u_dev);

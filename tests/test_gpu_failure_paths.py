@@ -103,7 +103,7 @@ def test_server_rejects_an_unknown_tree(ef, lib):
     del srv
 
 
-@pytest.mark.parametrize("tensor_cores", [0, 1])
+@pytest.mark.parametrize("tensor_cores", [0, 2])
 def test_bounded_tma_wait_runs_out_and_returns_an_error(ef, lib, tensor_cores):
     """The node GEMMs wait for their TMA copies with a limit.  With the failure-path test switch on,
     every CTA's first wait is on an mbarrier that nothing arrives on (limit 1 ms); the kernels drain
