@@ -382,6 +382,7 @@ def run_gb300(args):
     p_ach = plain_prof[p_dom]["bytes"] / (plain_prof[p_dom]["ms"] / 1e3) / 1e9
 
     # ---- batched mixed-precision form: the headline ----
+    check(lib.ef_hps_set_option(hps.handle, b"tensor-cores", args.tensor_cores))
     hps.mixed_init(B)
     F = np.stack([reqs[i % P][0] for i in range(B)])
     A = np.stack([reqs[i % P][1] for i in range(B)])
@@ -1039,6 +1040,8 @@ def run_profile_only(args):
         F = np.stack([reqs[i % 4][0] for i in range(B)])
         A = np.stack([reqs[i % 4][1] for i in range(B)])
         R = np.stack([reqs[i % 4][3] for i in range(B)])
+        from ellipticforest_gb300._lib import check as _check, load as _load
+        _check(_load().ef_hps_set_option(hps.handle, b"tensor-cores", args.tensor_cores))
         hps.mixed_init(B)
         hps.mixed_solve(F, A, R, args.sweeps)
         for _ in range(args.steps):
@@ -1067,6 +1070,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=30, help="timed steps of the plain FP64 form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 512-RHS level-6 case")
+    ap.add_argument("--tensor-cores", type=int, default=1, choices=[0, 1, 2],
+                    help="node GEMMs of the mixed form: 0 CUDA cores, 1 the faster per level (tuned), 2 tcgen05 wherever supported")
     ap.add_argument("--profile-only", choices=["build", "mixed"], default=None,
                     help="short run for a profiler's launch list: 'build' = set-up and one FP64 build of the "
                          "tree; 'mixed' = build, block-solver set-up and --steps mixed blocks (no timing line)")
