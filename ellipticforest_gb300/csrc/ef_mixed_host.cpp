@@ -388,7 +388,14 @@ void MixedSolver::tune() {
                 float path_ms = 1e30f;
                 int path_code = 0;
                 for (int ks = 1; ks <= kmax; ks *= 2) {
-                    const float ms = time_code(g, kind, tc ? -ks : ks);
+                    float ms;
+                    try {
+                        ms = time_code(g, kind, tc ? -ks : ks);
+                    } catch (const std::runtime_error&) {
+                        // a launch shape the device refuses (e.g. a cluster that does not fit): skip it
+                        (void)cudaGetLastError();
+                        continue;
+                    }
                     if (ms < path_ms * 0.97f) {  // a larger split must win clearly
                         path_ms = ms;
                         path_code = tc ? -ks : ks;

@@ -27,8 +27,10 @@
 // four children) puts the blocks side by side in N (32 requests each) and keeps each row's own
 // block in the epilogue.
 //
-// Roles (192 threads): warps 0-3 stage X and run the epilogue (warp w reads TMEM lanes 32w..32w+31),
-// warp 4 allocates TMEM and lane 0 issues the TMA loads, warp 5 lane 0 issues the MMAs.  Stages
+// Roles (320 threads): warps 0-3 add each chunk's accumulators to registers and run the epilogue
+// (warp w reads TMEM lanes 32w..32w+31; the operands a row's epilogue reads are prefetched when its
+// tile starts), warps 4-7 stage X (the next chunk's loads in flight while the current one is split
+// and written), warp 8 allocates TMEM and lane 0 issues the TMA loads, warp 9 lane 0 issues the MMAs.  Stages
 // are handed over through mbarriers; the MMA issuer frees a stage with tcgen05.commit.  Every wait
 // gives up after about one second: the kernel then sets the error word, lets its copies and MMAs in
 // flight finish (bounded waits), frees its TMEM and returns.
@@ -38,6 +40,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <stdexcept>
+#include <string>
 
 #include "ef_kernels.cuh"
 #include "ef_mixed_common.cuh"
@@ -53,7 +56,7 @@ constexpr int kTK = 64;                   // K per stage: 64 bf16 = one 128-byte
 constexpr int kTB = 32;                   // requests per right-hand-side block (MMA N per block)
 constexpr int kPlaneA = kTM * kTK * 2;    // bytes of one A plane per stage (16 KB)
 constexpr int kPlaneX = kTB * kTK * 2;    // bytes of one X plane per block per stage (4 KB)
-constexpr int kTcThreads = 192;
+constexpr int kTcThreads = 320;
 constexpr int kMaxSeg = 4;
 
 struct TcShape {
@@ -69,15 +72,14 @@ __host__ __device__ inline TcShape tc_shape(int kind, int s) {
     return t;
 }
 
-__host__ __device__ inline int tc_stages(int nseg) { return nseg <= 2 ? 3 : 2; }
-__host__ __device__ inline int tc_stage_bytes(int nseg) { return 3 * kPlaneA + 3 * nseg * kPlaneX; }
+__host__ __device__ constexpr int tc_stages(int nseg) { return nseg <= 2 ? 3 : 2; }
+__host__ __device__ constexpr int tc_stage_bytes(int nseg) { return 3 * kPlaneA + 3 * nseg * kPlaneX; }
 inline size_t tc_smem_bytes(int nseg) {
     return 1024 + size_t(tc_stages(nseg)) * tc_stage_bytes(nseg) + 256;
 }
 // two chunk buffers x (D_hi, D_lo) x 32 nseg columns
-__host__ __device__ inline int tc_tmem_cols(int nseg) {
-    const int need = 4 * kTB * nseg;
-    return need <= 128 ? 128 : (need <= 256 ? 256 : 512);
+__host__ __device__ constexpr int tc_tmem_cols(int nseg) {
+    return 4 * kTB * nseg <= 128 ? 128 : (4 * kTB * nseg <= 256 ? 256 : 512);
 }
 
 // compact H row order of the planes: child c's rows [2s c, 2s c + 2s) are its W/E run and then its
@@ -145,6 +147,19 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+// 16 consecutive FP32 columns of the calling warp's 32 TMEM lanes (one lane per thread)
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
@@ -220,12 +235,42 @@ __device__ __forceinline__ TcSeg tc_seg(const MixItem* __restrict__ items, int s
     return t;
 }
 
-// Epilogue of one tile row: v[q] = (A X)[row][b0 + q] for the 32 requests of this request block.
-// All loads of the row's operands are issued before its stores (the arrays of an item may alias as
-// far as the compiler knows); 16-byte accesses when B % 4 == 0.
+// Prefetch of the operand a row's epilogue reads (issued when the row's tile starts, so that its
+// latency hides behind the K loop): w for DOWN, the child's particular flux hc for H.
+template <int KIND>
+__device__ __forceinline__ void tc_prefetch_row(const MixItem* __restrict__ items, int s, int B, int b0, int rows_item,
+                                                int grow, float (&pre)[32], bool vec) {
+    if (KIND == MX_W) return;
+    const int item = grow / rows_item, r = grow - item * rows_item;
+    const MixItem& it = items[item];
+    const int nb = min(32, B - b0);
+    const float* src;
+    if (KIND == MX_H) {
+        int c, q2;
+        mx_ext_map(tc_h_unpermute(r, s), s, c, q2);
+        src = it.hc[c] + (long long)q2 * B + b0;
+    } else {
+        src = it.w + (long long)r * B + b0;
+    }
+    if (vec) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const float4 x = 4 * i < nb ? *reinterpret_cast<const float4*>(src + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
+            pre[4 * i] = x.x; pre[4 * i + 1] = x.y; pre[4 * i + 2] = x.z; pre[4 * i + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) pre[q] = q < nb ? src[q] : 0.f;
+    }
+}
+
+// Epilogue of one tile row: v[q] = (A X)[row][b0 + q] for the 32 requests of this request block,
+// pre[q] the prefetched operand (tc_prefetch_row).  The FP64 interface state of DOWN rows is read
+// and written in two halves of 16 requests, each with its loads ahead of its stores; 16-byte
+// accesses when B % 4 == 0.
 template <int KIND>
 __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, int s, int B, int b0, int rows_item,
-                                             int grow, const float (&v)[32], bool vec) {
+                                             int grow, const float (&v)[32], const float (&pre)[32], bool vec) {
     const int item = grow / rows_item, r = grow - item * rows_item;
     const MixItem& it = items[item];
     const int nb = min(32, B - b0);
@@ -242,56 +287,34 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
                 if (q < nb) dst[q] = v[q];
         }
     } else if (KIND == MX_H) {
-        const int p = tc_h_unpermute(r, s);
-        int c, q2;
-        mx_ext_map(p, s, c, q2);
-        const float* hp = it.hc[c] + (long long)q2 * B + cb;
-        float* dst = it.h + (long long)p * B + cb;
+        float* dst = it.h + (long long)tc_h_unpermute(r, s) * B + cb;
         if (vec) {
-            float4 h4[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                h4[i] = 4 * i < nb ? *reinterpret_cast<const float4*>(hp + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (4 * i < nb)
-                    *reinterpret_cast<float4*>(dst + 4 * i) = make_float4(v[4 * i] + h4[i].x, v[4 * i + 1] + h4[i].y,
-                                                                          v[4 * i + 2] + h4[i].z, v[4 * i + 3] + h4[i].w);
+            for (int q = 0; q < 32; q += 4)
+                if (q < nb)
+                    *reinterpret_cast<float4*>(dst + q) =
+                        make_float4(v[q] + pre[q], v[q + 1] + pre[q + 1], v[q + 2] + pre[q + 2], v[q + 3] + pre[q + 3]);
         } else {
-            float hv[32];
-#pragma unroll
-            for (int q = 0; q < 32; ++q) hv[q] = q < nb ? hp[q] : 0.f;
 #pragma unroll
             for (int q = 0; q < 32; ++q)
-                if (q < nb) dst[q] = v[q] + hv[q];
+                if (q < nb) dst[q] = v[q] + pre[q];
         }
     } else {
         const int I = r / s, o = r - (r / s) * s;
-        const float* wp = it.w + (long long)r * B + cb;
         float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
         float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
         double* ug = it.uG + (long long)r * B + cb;
-        // two halves of 16 requests, each with all of its loads ahead of its stores
 #pragma unroll
         for (int hf = 0; hf < 2; ++hf) {
             const int q0 = 16 * hf;
             float uu[16];
-            if (vec) {
-                float4 w4[4];
-                double2 u2[8];
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    w4[i] = q0 + 4 * i < nb ? *reinterpret_cast<const float4*>(wp + q0 + 4 * i) : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int i = 0; i < 16; ++i) uu[i] = v[q0 + i] + pre[q0 + i];
+            if (vec) {
+                double2 u2[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
                     u2[i] = q0 + 2 * i < nb ? *reinterpret_cast<const double2*>(ug + q0 + 2 * i) : make_double2(0.0, 0.0);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    uu[4 * i] = v[q0 + 4 * i] + w4[i].x;
-                    uu[4 * i + 1] = v[q0 + 4 * i + 1] + w4[i].y;
-                    uu[4 * i + 2] = v[q0 + 4 * i + 2] + w4[i].z;
-                    uu[4 * i + 3] = v[q0 + 4 * i + 3] + w4[i].w;
-                }
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
                     if (q0 + 4 * i < nb) {
@@ -305,17 +328,12 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
                         *reinterpret_cast<double2*>(ug + q0 + 2 * i) =
                             make_double2(u2[i].x + f2d_bits(uu[2 * i]), u2[i].y + f2d_bits(uu[2 * i + 1]));
             } else {
-                float wv[16];
                 double uv[16];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    wv[i] = q0 + i < nb ? wp[q0 + i] : 0.f;
-                    uv[i] = q0 + i < nb ? ug[q0 + i] : 0.0;
-                }
+                for (int i = 0; i < 16; ++i) uv[i] = q0 + i < nb ? ug[q0 + i] : 0.0;
 #pragma unroll
                 for (int i = 0; i < 16; ++i)
                     if (q0 + i < nb) {
-                        uu[i] = v[q0 + i] + wv[i];
                         d0[q0 + i] = uu[i];
                         d1[q0 + i] = uu[i];
                         ug[q0 + i] = uv[i] + f2d_bits(uu[i]);
@@ -326,15 +344,15 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
 }
 
 // exterior points of a parent go to its children unchanged: rows [p0, p1) of one item, all
-// requests, spread over the 128 epilogue threads with four loads in flight before their stores
+// requests, spread over the 128 epilogue threads with eight loads in flight before their stores
 __device__ __forceinline__ void tc_ext_copy(const MixItem& it, int s, int B, int p0, int p1, int t) {
     if ((B & 3) == 0) {
         const int w4 = B >> 2, tot = (p1 - p0) * w4;
-        for (int e0 = t; e0 < tot; e0 += 4 * 128) {
-            float4 val[4];
-            float4* dst[4];
+        for (int e0 = t; e0 < tot; e0 += 8 * 128) {
+            float4 val[8];
+            float4* dst[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 8; ++u) {
                 const int e = e0 + u * 128;
                 dst[u] = nullptr;
                 if (e < tot) {
@@ -346,7 +364,7 @@ __device__ __forceinline__ void tc_ext_copy(const MixItem& it, int s, int B, int
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 8; ++u)
                 if (dst[u]) *dst[u] = val[u];
         }
     } else {
@@ -375,21 +393,21 @@ __device__ __forceinline__ void tc_ext_copy_tile(const MixItem* __restrict__ ite
     }
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(kTcThreads, 1)
+template <int KIND, int NSEG>
+__global__ void __maxnreg__(200)
     k_mx_umma(const __grid_constant__ CUtensorMap tmA, const MixItem* __restrict__ items, int s, int B, int cnt,
               int ksplit, int ntiles, int* __restrict__ err) {
-    const TcShape sh = tc_shape(KIND, s);
-    const int nseg = sh.nseg, K = sh.K, R = cnt * sh.rows_item;
+    const TcShape sh = tc_shape(KIND, s);  // sh.nseg == NSEG (checked by the launcher)
+    const int K = sh.K, R = cnt * sh.rows_item;
     const int nsegs_total = KIND == MX_H ? 4 * cnt : cnt;
-    const int NS = tc_stages(nseg), SB = tc_stage_bytes(nseg);
-    const int ncol = kTB * nseg, tcols = tc_tmem_cols(nseg);
-    const unsigned idesc = tc_idesc(kTM, ncol);
+    constexpr int NS = tc_stages(NSEG), SB = tc_stage_bytes(NSEG);
+    constexpr int ncol = kTB * NSEG, tcols = tc_tmem_cols(NSEG);
+    constexpr unsigned idesc = tc_idesc(kTM, ncol);
     extern __shared__ unsigned char tc_smem[];
     unsigned char* base = tc_smem + ((1024u - (smem_u32(tc_smem) & 1023u)) & 1023u);
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(base + size_t(NS) * SB);
     unsigned long long* a_full = bars;             // [NS] TMA transaction barriers
-    unsigned long long* x_full = bars + NS;        // [NS] 128 producer arrivals
+    unsigned long long* x_full = bars + NS;        // [NS] 128 staging arrivals
     unsigned long long* empty = bars + 2 * NS;     // [NS] MMA commit
     unsigned long long* acc_full = bars + 3 * NS;  // [2] MMA commit at the end of a chunk
     unsigned long long* acc_empty = acc_full + 2;  // [2] 128 epilogue arrivals
@@ -416,7 +434,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         cpu = nkc;
     }
     if (cpu <= 0) nunits = 0;
+    const int total = nunits * cpu;
     const int b0 = blockIdx.y * kTB;
+    const bool vec = (B & 3) == 0;
 
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
@@ -434,7 +454,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     }
-    if (warp == 4) {
+    if (warp == 8) {
         tmem_alloc(tmem_slot, unsigned(tcols));
         tmem_relinquish();
     }
@@ -445,9 +465,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     // per unit: the tile's rows [128 t, 128 t + 128) of the group and its first segment
     auto tile_of = [&](int u) { return first_tile + u * tile_step; };
-    auto seg0_of = [&](int t) { return sh.seg_rows >= kTM ? (t * kTM) / sh.seg_rows : t * nseg; };
+    auto seg0_of = [&](int tl) { return sh.seg_rows >= kTM ? (tl * kTM) / sh.seg_rows : tl * NSEG; };
 
-    if (warp == 4) {
+    // epilogue state that the K-split reduction below still needs: the row's running sums (v holds
+    // the row's result at a unit's end) and its prefetched epilogue operand (w for DOWN, hc for H)
+    float v[32];
+    float pre[32];
+    bool ep_ok = true;
+
+    if (warp == 8) {
         // ---- TMA producer: the three A planes of every stage ----
         if (lane == 0) {
             int st = 0;
@@ -472,16 +498,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 // (only the last NS loads can be pending: a stage is reloaded after its MMAs completed)
                 int s2 = 0;
                 unsigned p2 = 0;
-                volatile int never = 0;
+                volatile int never_set = 0;
                 const int first = issued > NS ? issued - NS : 0;
-                for (int v = 0; v < issued; ++v) {
-                    if (v >= first) (void)tc_wait(&a_full[s2], p2, &never);
+                for (int q = 0; q < issued; ++q) {
+                    if (q >= first) (void)tc_wait(&a_full[s2], p2, &never_set);
                     if (++s2 == NS) { s2 = 0; p2 ^= 1u; }
                 }
                 atomicExch(err, 1);
             }
         }
-    } else if (warp == 5) {
+    } else if (warp == 9) {
         // ---- MMA issuer ----
         if (lane == 0) {
             int st = 0;
@@ -489,7 +515,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             bool ok = true;
             const uint32_t a_base = smem_u32(base);
             if (g_mx_inject_timeout && nunits > 0) ok = tc_wait(never, 0u, abort_flag, 1000000LL);
-            const int total = nunits * cpu;
             for (int gch = 0; gch < total && ok; ++gch) {
                 const int c = gch % cpu, bf = gch & 1;
                 // the chunk's accumulator pair was drained two chunks ago
@@ -502,11 +527,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const unsigned dhi = tmem + unsigned(bf * 2 * ncol), dlo = dhi + unsigned(ncol);
                 const int kleft = K - (cbase + c) * kTK;
                 const int nk = kleft >= kTK ? kTK / 16 : (kleft + 15) / 16;
+                constexpr uint32_t xp = uint32_t(NSEG) * kPlaneX;
                 for (int kk = 0; kk < nk; ++kk) {
                     const uint32_t ko = uint32_t(kk) * 32u;
                     const uint64_t a1 = tc_desc(sa + ko), a2 = tc_desc(sa + kPlaneA + ko),
                                    a3 = tc_desc(sa + 2 * kPlaneA + ko);
-                    const uint32_t xp = uint32_t(nseg) * kPlaneX;
                     const uint64_t x1 = tc_desc(sx + ko), x2 = tc_desc(sx + xp + ko), x3 = tc_desc(sx + 2 * xp + ko);
                     const unsigned acc = kk > 0 ? 1u : 0u;  // a fresh accumulator pair per chunk
                     tc_mma(dhi, a1, x1, idesc, acc);
@@ -522,114 +547,123 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             // every MMA issued has completed before TMEM is freed
             tc_commit(drain);
-            volatile int never = 0;
-            if (!tc_wait(drain, 0u, &never)) atomicExch(err, 1);
+            volatile int never_set = 0;
+            if (!tc_wait(drain, 0u, &never_set)) atomicExch(err, 1);
             if (!ok) atomicExch(err, 1);
         }
-    } else {
-        // ---- warps 0-3: stage X (split into bf16 planes) one chunk ahead, add every chunk's
-        //      accumulators to the FP32 running sums, run the epilogue of each unit ----
-        const int t = tid;  // 0..127 = TMEM lane of this thread's tile row
+    } else if (warp >= 4) {
+        // ---- warps 4-7: stage X, split into bf16 planes; the loads of the next chunk are in
+        //      flight while the current one is split and written ----
+        const int t = tid - 128;
+        const int b = t & 31, n = b, gb = b0 + b;
         int st = 0;
         unsigned ph = 0;
         int staged = 0;
         bool ok = true;
-        const bool vec = (B & 3) == 0;
-        const int total = nunits * cpu;
-        TcSeg seg[kMaxSeg];
-        bool sval[kMaxSeg];
+        TcSeg seg[NSEG];
+        bool sval[NSEG];
         int seg_unit = -1;
-        auto stage = [&](int gch) -> bool {
-            const int u = gch / cpu, c = gch - u * cpu;
+        constexpr int NP = 8 * NSEG;  // (k, k + 1) pairs of one request per thread and chunk
+        float xa[2 * NP], xb[2 * NP];
+        auto load = [&](int g, float (&xv)[2 * NP]) {
+            const int u = g / cpu, c = g - u * cpu;
             if (u != seg_unit) {
                 seg_unit = u;
                 const int gs0 = seg0_of(tile_of(u));
 #pragma unroll
-                for (int j = 0; j < kMaxSeg; ++j) {
-                    sval[j] = j < nseg && gs0 + j < nsegs_total;
-                    if (sval[j]) seg[j] = tc_seg<KIND>(items, s, B, gs0 + j);
+                for (int j = 0; j < NSEG; ++j) {
+                    sval[j] = gs0 + j < nsegs_total && gb < B;
+                    seg[j] = sval[j] ? tc_seg<KIND>(items, s, B, gs0 + j) : TcSeg{nullptr, nullptr, 0};
                 }
             }
+            const int k0 = (cbase + c) * kTK;
+#pragma unroll
+            for (int j = 0; j < NSEG; ++j)
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int k = k0 + 2 * ((t >> 5) + 4 * i);
+                    float x0 = 0.f, x1 = 0.f;
+                    if (sval[j]) {
+                        if (k < K) x0 = (k < seg[j].kb ? seg[j].X1 : seg[j].X2)[(long long)k * B + gb];
+                        if (k + 1 < K) x1 = (k + 1 < seg[j].kb ? seg[j].X1 : seg[j].X2)[(long long)(k + 1) * B + gb];
+                    }
+                    xv[2 * (8 * j + i)] = x0;
+                    xv[2 * (8 * j + i) + 1] = x1;
+                }
+        };
+        auto store = [&](const float (&xv)[2 * NP]) -> bool {
             if (staged >= NS && !tc_wait(&empty[st], ph ^ 1u, abort_flag)) return false;
             unsigned char* sx = base + size_t(st) * SB + 3 * kPlaneA;
-            const int k0 = (cbase + c) * kTK;
-            const int b = t & 31, n = b;
-            const int gb = b0 + b;
-            // pairs (k, k + 1) of one request: 32 per block, four pair rows per pass of the warps;
-            // every load of the chunk is issued before the bf16 parts are written
-            float xv[2 * 8 * kMaxSeg];
+            constexpr unsigned xp = unsigned(NSEG) * kPlaneX;
 #pragma unroll
-            for (int i = 0; i < 8 * kMaxSeg; ++i) {
-                xv[2 * i] = 0.f;
-                xv[2 * i + 1] = 0.f;
-                if (i < 8 * nseg) {
-                    const int P = (t >> 5) + 4 * i;
-                    const int j = P >> 5, kp = P & 31;
-                    const int k = k0 + 2 * kp;
-                    if (sval[j] && gb < B) {
-                        const TcSeg& sg = seg[j];
-                        if (k < K) xv[2 * i] = (k < sg.kb ? sg.X1 : sg.X2)[(long long)k * B + gb];
-                        if (k + 1 < K) xv[2 * i + 1] = (k + 1 < sg.kb ? sg.X1 : sg.X2)[(long long)(k + 1) * B + gb];
-                    }
-                }
-            }
-            const unsigned xp = unsigned(nseg) * kPlaneX;
+            for (int j = 0; j < NSEG; ++j)
 #pragma unroll
-            for (int i = 0; i < 8 * kMaxSeg; ++i) {
-                if (i < 8 * nseg) {
-                    const int P = (t >> 5) + 4 * i;
-                    const int j = P >> 5, kp = P & 31;
+                for (int i = 0; i < 8; ++i) {
+                    const int kl = 2 * ((t >> 5) + 4 * i);
                     __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
-                    split3(xv[2 * i], p0a, p1a, p2a);
-                    split3(xv[2 * i + 1], p0b, p1b, p2b);
-                    const int kl = 2 * kp;
+                    split3(xv[2 * (8 * j + i)], p0a, p1a, p2a);
+                    split3(xv[2 * (8 * j + i) + 1], p0b, p1b, p2b);
                     const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
                                          ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
                     *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
                     *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
                     *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
                 }
-            }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_arrive(&x_full[st]);
             ++staged;
             if (++st == NS) { st = 0; ph ^= 1u; }
             return true;
         };
-        float rhi[32], rlo[32];
+        if (total > 0) load(0, xa);
+        for (int g = 0; g < total && ok; g += 2) {
+            if (g + 1 < total) load(g + 1, xb);
+            ok = store(xa);
+            if (!ok || g + 1 >= total) break;
+            if (g + 2 < total) load(g + 2, xa);
+            ok = store(xb);
+        }
+        if (!ok) atomicExch(err, 1);
+    } else {
+        // ---- warps 0-3: add every chunk's accumulators to FP32 running sums (round to nearest),
+        //      run the epilogue of each unit with its operands prefetched at the unit's start ----
+        const int t = tid;  // 0..127 = TMEM lane of this thread's tile row
+        float rlo[32];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) { rhi[q] = 0.f; rlo[q] = 0.f; }
+        for (int q = 0; q < 32; ++q) { v[q] = 0.f; rlo[q] = 0.f; pre[q] = 0.f; }
         const int jrow = sh.seg_rows >= kTM ? 0 : t / sh.seg_rows;
         const unsigned lane_off = unsigned(warp * 32) << 16;
-        if (total > 0) ok = stage(0);
-        for (int gch = 0; gch < total && ok; ++gch) {
-            if (gch + 1 < total && !(ok = stage(gch + 1))) break;
-            // the chunk's sums: TMEM -> registers, added with round-to-nearest
+        for (int gch = 0; gch < total; ++gch) {
+            const int u = gch / cpu;
+            if (gch - u * cpu == 0) {
+                const int grow = tile_of(u) * kTM + t;
+                if (grow < R) tc_prefetch_row<KIND>(items, s, B, b0, sh.rows_item, grow, pre, vec);
+            }
             const int bf = gch & 1;
-            if (!(ok = tc_wait(&acc_full[bf], unsigned(gch >> 1) & 1u, abort_flag))) break;
+            if (!(ep_ok = tc_wait(&acc_full[bf], unsigned(gch >> 1) & 1u, abort_flag))) break;
             tc_fence_after();
-            float hi[32], lo[32];
             const unsigned col = unsigned(bf * 2 * ncol + jrow * kTB);
-            tmem_ld32(tmem + lane_off + col, hi);
-            tmem_ld32(tmem + lane_off + col + unsigned(ncol), lo);
+#pragma unroll
+            for (int hf = 0; hf < 2; ++hf) {
+                float hi[16], lo[16];
+                tmem_ld16(tmem + lane_off + col + unsigned(16 * hf), hi);
+                tmem_ld16(tmem + lane_off + col + unsigned(ncol + 16 * hf), lo);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    v[16 * hf + q] += hi[q];
+                    rlo[16 * hf + q] += lo[q];
+                }
+            }
             tc_fence_before();
             mbar_arrive(&acc_empty[bf]);
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                rhi[q] += hi[q];
-                rlo[q] += lo[q];
-            }
             if ((gch + 1) % cpu != 0) continue;
             // ---- epilogue of the unit ----
-            const int tile = tile_of(gch / cpu);
-            float v[32];
+            const int tile = tile_of(u);
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
-                v[q] = rhi[q] + rlo[q];
-                rhi[q] = 0.f;
+                v[q] += rlo[q];
                 rlo[q] = 0.f;
             }
-
             if (ksplit > 1) {
                 // partial tiles -> rank 0 of the cluster through distributed shared memory, in rank
                 // order (deterministic); the stage memory is free once every MMA has completed
@@ -637,15 +671,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                 for (int q = 0; q < 32; q += 4)
                     *reinterpret_cast<float4*>(red + t * 32 + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                break;  // the cluster reduction and the epilogue follow below
             }
-            if (ksplit > 1) break;  // the cluster reduction and the epilogue follow below
-
-            // ---- stores ----
             const int grow = tile * kTM + t;
-            if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, vec);
+            if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, pre, vec);
             if (KIND == MX_DOWN && blockIdx.y == 0) tc_ext_copy_tile(items, s, B, cnt, sh.rows_item, tile, t);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) v[q] = 0.f;
         }
-        if (!ok) atomicExch(err, 1);
+        if (!ep_ok) atomicExch(err, 1);
     }
 
     // ---- K split: rank 0 of the cluster adds the partial tiles and runs the epilogue ----
@@ -661,7 +695,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (cluster.block_rank() == 0 && tid < 128 && nunits > 0 && !*abort_flag) {
             const int t = tid;
             float* red = reinterpret_cast<float*>(base);
-            float v[32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) v[q] = red[t * 32 + q];
             for (int rk = 1; rk < ksplit; ++rk) {
@@ -671,7 +704,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             const int tile = first_tile;
             const int grow = tile * kTM + t;
-            if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, (B & 3) == 0);
+            if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, pre, vec);
             if (KIND == MX_DOWN && blockIdx.y == 0) tc_ext_copy_tile(items, s, B, cnt, sh.rows_item, tile, t);
         }
         cluster.sync();
@@ -680,7 +713,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 4) tmem_dealloc(tmem, unsigned(tcols));
+    if (warp == 8) tmem_dealloc(tmem, unsigned(tcols));
 }
 
 // A planes of one group: dst[p][R][K] (bf16) with src[R][K] = dst[0] + dst[1] + dst[2]; H rows in the
@@ -706,15 +739,15 @@ __global__ void k_tc_split(const float* __restrict__ src, __nv_bfloat16* __restr
     }
 }
 
-template <int KIND>
-void launch_umma(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int cnt, int s, int B, int* err,
-                 int ksplit) {
+template <int KIND, int NSEG>
+void launch_umma_n(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int cnt, int s, int B, int* err,
+                   int ksplit) {
     const TcShape sh = tc_shape(KIND, s);
     const long long R = (long long)cnt * sh.rows_item;
     const int ntiles = int((R + kTM - 1) / kTM);
     const int chunks = (B + kTB - 1) / kTB;
-    const size_t smem = tc_smem_bytes(sh.nseg);
-    cudaFuncSetAttribute(k_mx_umma<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const size_t smem = tc_smem_bytes(NSEG);
+    cudaFuncSetAttribute(k_mx_umma<KIND, NSEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -733,8 +766,22 @@ void launch_umma(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, i
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = ksplit > 1 ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, k_mx_umma<KIND>, tm, items, s, B, cnt, ksplit, ntiles, err);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_mx_umma<KIND, NSEG>, tm, items, s, B, cnt, ksplit, ntiles, err);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw std::runtime_error(std::string("tensor-core node GEMM launch (K split ") + std::to_string(ksplit) +
+                                 "): " + cudaGetErrorString(e));
+    }
     ++g_kernel_launches;
+}
+
+template <int KIND>
+void launch_umma(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int cnt, int s, int B, int* err,
+                 int ksplit) {
+    const int nseg = tc_shape(KIND, s).nseg;
+    if (nseg == 1) launch_umma_n<KIND, 1>(st, tm, items, cnt, s, B, err, ksplit);
+    else if (nseg == 2) launch_umma_n<KIND, 2>(st, tm, items, cnt, s, B, err, ksplit);
+    else launch_umma_n<KIND, 4>(st, tm, items, cnt, s, B, err, ksplit);
 }
 
 }  // namespace
