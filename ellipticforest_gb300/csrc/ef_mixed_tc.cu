@@ -27,10 +27,11 @@
 // four children) puts the blocks side by side in N (32 requests each) and keeps each row's own
 // block in the epilogue.
 //
-// Roles (320 threads): warps 0-3 add each chunk's accumulators to registers and run the epilogue
-// (warp w reads TMEM lanes 32w..32w+31; the operands a row's epilogue reads are prefetched when its
-// tile starts), warps 4-7 stage X (the next chunk's loads in flight while the current one is split
-// and written), warp 8 allocates TMEM and lane 0 issues the TMA loads, warp 9 lane 0 issues the MMAs.  Stages
+// Roles (256 threads, eight warps: two per SM sub-partition, so up to 255 registers a thread):
+// warps 0-3 add each chunk's accumulators to registers and run the epilogue (warp w reads TMEM lanes
+// 32w..32w+31; the operands a row's epilogue reads are prefetched when its tile starts), warps 4-6
+// stage X (the next chunk's loads in flight while the current one is split and written), warp 7
+// allocates TMEM, its lane 0 issues the TMA loads and its lane 1 the MMAs.  Stages
 // are handed over through mbarriers; the MMA issuer frees a stage with tcgen05.commit.  Every wait
 // gives up after about one second: the kernel then sets the error word, lets its copies and MMAs in
 // flight finish (bounded waits), frees its TMEM and returns.
@@ -56,7 +57,8 @@ constexpr int kTK = 64;                   // K per stage: 64 bf16 = one 128-byte
 constexpr int kTB = 32;                   // requests per right-hand-side block (MMA N per block)
 constexpr int kPlaneA = kTM * kTK * 2;    // bytes of one A plane per stage (16 KB)
 constexpr int kPlaneX = kTB * kTK * 2;    // bytes of one X plane per block per stage (4 KB)
-constexpr int kTcThreads = 320;
+constexpr int kTcThreads = 256;
+constexpr int kStageThreads = 96;  // warps 4-6
 constexpr int kMaxSeg = 4;
 
 struct TcShape {
@@ -394,7 +396,7 @@ __device__ __forceinline__ void tc_ext_copy_tile(const MixItem* __restrict__ ite
 }
 
 template <int KIND, int NSEG>
-__global__ void __maxnreg__(200)
+__global__ void __launch_bounds__(kTcThreads, 1)
     k_mx_umma(const __grid_constant__ CUtensorMap tmA, const MixItem* __restrict__ items, int s, int B, int cnt,
               int ksplit, int ntiles, int* __restrict__ err) {
     const TcShape sh = tc_shape(KIND, s);  // sh.nseg == NSEG (checked by the launcher)
@@ -441,7 +443,7 @@ __global__ void __maxnreg__(200)
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
             mbar_init(&a_full[i], 1);
-            mbar_init(&x_full[i], 128);
+            mbar_init(&x_full[i], kStageThreads);
             mbar_init(&empty[i], 1);
         }
         for (int i = 0; i < 2; ++i) {
@@ -454,7 +456,7 @@ __global__ void __maxnreg__(200)
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     }
-    if (warp == 8) {
+    if (warp == 7) {
         tmem_alloc(tmem_slot, unsigned(tcols));
         tmem_relinquish();
     }
@@ -473,8 +475,8 @@ __global__ void __maxnreg__(200)
     float pre[32];
     bool ep_ok = true;
 
-    if (warp == 8) {
-        // ---- TMA producer: the three A planes of every stage ----
+    if (warp == 7) {
+        // ---- lane 0: TMA producer of the three A planes of every stage ----
         if (lane == 0) {
             int st = 0;
             unsigned ph = 0;
@@ -507,9 +509,8 @@ __global__ void __maxnreg__(200)
                 atomicExch(err, 1);
             }
         }
-    } else if (warp == 9) {
-        // ---- MMA issuer ----
-        if (lane == 0) {
+        // ---- lane 1: MMA issuer (independent thread scheduling lets the two lanes wait apart) ----
+        if (lane == 1) {
             int st = 0;
             unsigned ph = 0;
             bool ok = true;
@@ -552,9 +553,9 @@ __global__ void __maxnreg__(200)
             if (!ok) atomicExch(err, 1);
         }
     } else if (warp >= 4) {
-        // ---- warps 4-7: stage X, split into bf16 planes; the loads of the next chunk are in
+        // ---- warps 4-6: stage X, split into bf16 planes; the loads of the next chunk are in
         //      flight while the current one is split and written ----
-        const int t = tid - 128;
+        const int t = tid - 128;  // 0 .. kStageThreads-1
         const int b = t & 31, n = b, gb = b0 + b;
         int st = 0;
         unsigned ph = 0;
@@ -563,7 +564,9 @@ __global__ void __maxnreg__(200)
         TcSeg seg[NSEG];
         bool sval[NSEG];
         int seg_unit = -1;
-        constexpr int NP = 8 * NSEG;  // (k, k + 1) pairs of one request per thread and chunk
+        constexpr int RPI = kStageThreads / 32;            // pair rows per pass of the warps
+        constexpr int NI = (32 + RPI - 1) / RPI;             // passes over the 32 pair rows of a block
+        constexpr int NP = NI * NSEG;  // (k, k + 1) pairs of one request per thread and chunk
         float xa[2 * NP], xb[2 * NP];
         auto load = [&](int g, float (&xv)[2 * NP]) {
             const int u = g / cpu, c = g - u * cpu;
@@ -580,15 +583,16 @@ __global__ void __maxnreg__(200)
 #pragma unroll
             for (int j = 0; j < NSEG; ++j)
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int k = k0 + 2 * ((t >> 5) + 4 * i);
+                for (int i = 0; i < NI; ++i) {
+                    const int kp = (t >> 5) + RPI * i;
+                    const int k = k0 + 2 * kp;
                     float x0 = 0.f, x1 = 0.f;
-                    if (sval[j]) {
+                    if (sval[j] && kp < 32) {
                         if (k < K) x0 = (k < seg[j].kb ? seg[j].X1 : seg[j].X2)[(long long)k * B + gb];
                         if (k + 1 < K) x1 = (k + 1 < seg[j].kb ? seg[j].X1 : seg[j].X2)[(long long)(k + 1) * B + gb];
                     }
-                    xv[2 * (8 * j + i)] = x0;
-                    xv[2 * (8 * j + i) + 1] = x1;
+                    xv[2 * (NI * j + i)] = x0;
+                    xv[2 * (NI * j + i) + 1] = x1;
                 }
         };
         auto store = [&](const float (&xv)[2 * NP]) -> bool {
@@ -598,11 +602,13 @@ __global__ void __maxnreg__(200)
 #pragma unroll
             for (int j = 0; j < NSEG; ++j)
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int kl = 2 * ((t >> 5) + 4 * i);
+                for (int i = 0; i < NI; ++i) {
+                    const int kp = (t >> 5) + RPI * i;
+                    if (kp >= 32) continue;
+                    const int kl = 2 * kp;
                     __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
-                    split3(xv[2 * (8 * j + i)], p0a, p1a, p2a);
-                    split3(xv[2 * (8 * j + i) + 1], p0b, p1b, p2b);
+                    split3(xv[2 * (NI * j + i)], p0a, p1a, p2a);
+                    split3(xv[2 * (NI * j + i) + 1], p0b, p1b, p2b);
                     const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
                                          ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
                     *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
@@ -713,7 +719,7 @@ __global__ void __maxnreg__(200)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 8) tmem_dealloc(tmem, unsigned(tcols));
+    if (warp == 7) tmem_dealloc(tmem, unsigned(tcols));
 }
 
 // A planes of one group: dst[p][R][K] (bf16) with src[R][K] = dst[0] + dst[1] + dst[2]; H rows in the
