@@ -458,7 +458,7 @@ private:
         float *S32 = nullptr, *Xi32 = nullptr, *H32 = nullptr;
         CUtensorMap tmS{}, tmXi{}, tmH{};
         // tensor-core path: three bf16 planes per operator kind and their tensor maps
-        bool tc = false;
+        bool tc[3] = {false, false, false};  // per kind (W, H, DOWN)
         void *S3 = nullptr, *Xi3 = nullptr, *H3 = nullptr;
         CUtensorMap tmS3{}, tmXi3{}, tmH3{};
     };

@@ -175,14 +175,15 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             groups_[gi].Xi32 = Xi;
             groups_[gi].H32 = H32;
             // bf16 planes of the tensor-core path (3 x the FP32 element count, 2 bytes each)
-            const bool tc = hps.tensor_cores() != 0 && mx_tc_supported(0, g.s) && mx_tc_supported(1, g.s) &&
-                            mx_tc_supported(2, g.s);
-            groups_[gi].tc = tc;
-            if (tc) {
+            // (per kind: W, H, DOWN)
+            for (int kind = 0; kind < 3; ++kind)
+                groups_[gi].tc[kind] = hps.tensor_cores() != 0 && mx_tc_supported(kind, g.s);
+            if (groups_[gi].tc[2])
                 groups_[gi].S3 = share ? share->groups_[gi].S3 : (void*)cv.get<uint16_t>(3 * cnt * 32 * s * s);
+            if (groups_[gi].tc[0])
                 groups_[gi].Xi3 = share ? share->groups_[gi].Xi3 : (void*)cv.get<uint16_t>(3 * cnt * 16 * s * s);
+            if (groups_[gi].tc[1])
                 groups_[gi].H3 = share ? share->groups_[gi].H3 : (void*)cv.get<uint16_t>(3 * cnt * 16 * s * s);
-            }
             for (size_t i = 0; i < cnt; ++i) {
                 MNode& m = mn_[g.nodes[i]];
                 m.S = S ? S + i * 32 * s * s : nullptr;
@@ -343,12 +344,16 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         g.tmS = make_map(g.S32, cnt * 4 * s, int(8 * s), mx_tile_rows(0, g.s));
         g.tmXi = make_map(g.Xi32, cnt * 4 * s, int(4 * s), mx_tile_rows(0, g.s));
         g.tmH = make_map(g.H32, cnt * 8 * s, int(2 * s), mx_tile_rows(1, g.s));
-        if (g.tc) {
+        if (g.tc[2]) {
             mx_tc_split(st, 2, g.S32, g.S3, cnt * 4 * s, int(8 * s), g.s);
-            mx_tc_split(st, 0, g.Xi32, g.Xi3, cnt * 4 * s, int(4 * s), g.s);
-            mx_tc_split(st, 1, g.H32, g.H3, cnt * 8 * s, int(2 * s), g.s);
             g.tmS3 = make_map_bf16(g.S3, 3 * cnt * 4 * s, int(8 * s));
+        }
+        if (g.tc[0]) {
+            mx_tc_split(st, 0, g.Xi32, g.Xi3, cnt * 4 * s, int(4 * s), g.s);
             g.tmXi3 = make_map_bf16(g.Xi3, 3 * cnt * 4 * s, int(4 * s));
+        }
+        if (g.tc[1]) {
+            mx_tc_split(st, 1, g.H32, g.H3, cnt * 8 * s, int(2 * s), g.s);
             g.tmH3 = make_map_bf16(g.H3, 3 * cnt * 8 * s, int(2 * s));
         }
     }
@@ -381,8 +386,8 @@ void MixedSolver::tune() {
         for (int kind = 0; kind < 3; ++kind) {
             float best_ms = 1e30f;
             int best_code = 1;
-            const bool forced = g.tc && h.tensor_cores() == 2;
-            for (int pass = forced ? 1 : 0; pass < (g.tc ? 2 : 1); ++pass) {
+            const bool forced = g.tc[kind] && h.tensor_cores() == 2;
+            for (int pass = forced ? 1 : 0; pass < (g.tc[kind] ? 2 : 1); ++pass) {
                 const bool tc = pass == 1;
                 const int kmax = tc ? mx_tc_max_split(kind, g.s) : mx_gemm_max_split(kind, g.s);
                 float path_ms = 1e30f;
@@ -420,7 +425,7 @@ void MixedSolver::tune() {
 }
 
 void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code) {
-    if (g.tc && code < 0) {
+    if (g.tc[kind] && code < 0) {
         const CUtensorMap& tm = kind == 0 ? g.tmXi3 : (kind == 1 ? g.tmH3 : g.tmS3);
         mx_gemm_tc(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, -code);
     } else {

@@ -59,7 +59,8 @@ constexpr int kPlaneA = kTM * kTK * 2;    // bytes of one A plane per stage (16 
 constexpr int kPlaneX = kTB * kTK * 2;    // bytes of one X plane per block per stage (4 KB)
 constexpr int kTcThreads = 256;
 constexpr int kStageThreads = 96;  // warps 4-6
-constexpr int kMaxSeg = 4;
+constexpr int kMaxSeg = 2;
+constexpr int kXRing = 3;  // FP32 request-block chunks in the staging ring
 
 struct TcShape {
     int rows_item, K, seg_rows, nseg;
@@ -74,10 +75,11 @@ __host__ __device__ inline TcShape tc_shape(int kind, int s) {
     return t;
 }
 
-__host__ __device__ constexpr int tc_stages(int nseg) { return nseg <= 2 ? 3 : 2; }
+__host__ __device__ constexpr int tc_stages(int nseg) { return nseg <= 1 ? 3 : 2; }
 __host__ __device__ constexpr int tc_stage_bytes(int nseg) { return 3 * kPlaneA + 3 * nseg * kPlaneX; }
+// stages, barriers (256 bytes), then the FP32 staging ring of the request blocks
 inline size_t tc_smem_bytes(int nseg) {
-    return 1024 + size_t(tc_stages(nseg)) * tc_stage_bytes(nseg) + 256;
+    return 1024 + size_t(tc_stages(nseg)) * tc_stage_bytes(nseg) + 256 + size_t(kXRing) * nseg * kTK * kTB * 4;
 }
 // two chunk buffers x (D_hi, D_lo) x 32 nseg columns
 __host__ __device__ constexpr int tc_tmem_cols(int nseg) {
@@ -162,6 +164,16 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+// AND of v over the n threads of named barrier `id` (all of them must call it)
+__device__ __forceinline__ bool bar_and(int id, int n, bool v) {
+    unsigned r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"(unsigned(v)), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
 }
 __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
@@ -553,10 +565,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!ok) atomicExch(err, 1);
         }
     } else if (warp >= 4) {
-        // ---- warps 4-6: stage X, split into bf16 planes; the loads of the next chunk are in
-        //      flight while the current one is split and written ----
+        // ---- warps 4-6: stage X.  FP32 request rows travel by cp.async into a ring of kXRing
+        //      chunks (kXRing - 1 chunks ahead of the one being split, so no global-load latency sits
+        //      on a chunk's path), then are split into bf16 planes in the swizzled K-major layout ----
         const int t = tid - 128;  // 0 .. kStageThreads-1
-        const int b = t & 31, n = b, gb = b0 + b;
+        float* ring = reinterpret_cast<float*>(base + size_t(NS) * SB + 256);
+        constexpr int RC = NSEG * kTK * kTB;  // floats of one ring chunk: [seg][k][request]
         int st = 0;
         unsigned ph = 0;
         int staged = 0;
@@ -564,71 +578,77 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         TcSeg seg[NSEG];
         bool sval[NSEG];
         int seg_unit = -1;
-        constexpr int RPI = kStageThreads / 32;            // pair rows per pass of the warps
-        constexpr int NI = (32 + RPI - 1) / RPI;             // passes over the 32 pair rows of a block
-        constexpr int NP = NI * NSEG;  // (k, k + 1) pairs of one request per thread and chunk
-        float xa[2 * NP], xb[2 * NP];
-        auto load = [&](int g, float (&xv)[2 * NP]) {
-            const int u = g / cpu, c = g - u * cpu;
-            if (u != seg_unit) {
-                seg_unit = u;
-                const int gs0 = seg0_of(tile_of(u));
+        auto issue = [&](int g) {
+            if (g < total) {
+                const int u = g / cpu, c = g - u * cpu;
+                if (u != seg_unit) {
+                    seg_unit = u;
+                    const int gs0 = seg0_of(tile_of(u));
 #pragma unroll
-                for (int j = 0; j < NSEG; ++j) {
-                    sval[j] = gs0 + j < nsegs_total && gb < B;
-                    seg[j] = sval[j] ? tc_seg<KIND>(items, s, B, gs0 + j) : TcSeg{nullptr, nullptr, 0};
+                    for (int j = 0; j < NSEG; ++j) {
+                        sval[j] = gs0 + j < nsegs_total;
+                        seg[j] = sval[j] ? tc_seg<KIND>(items, s, B, gs0 + j) : TcSeg{nullptr, nullptr, 0};
+                    }
+                }
+                const int k0 = (cbase + c) * kTK;
+                float* dst = ring + (g % kXRing) * RC;
+                if (vec) {
+                    // 16-byte pieces: 8 per row of 32 requests (B % 4 == 0: a piece is all in or all out)
+#pragma unroll
+                    for (int j = 0; j < NSEG; ++j)
+                        for (int e = t; e < kTK * 8; e += kStageThreads) {
+                            const int k = k0 + (e >> 3), p4 = (e & 7) * 4;
+                            const bool in = sval[j] && k < K && b0 + p4 < B;
+                            const float* src = in ? (k < seg[j].kb ? seg[j].X1 : seg[j].X2) + (long long)k * B + b0 + p4
+                                                  : reinterpret_cast<const float*>(items);
+                            cp_async16(dst + (j * kTK + (e >> 3)) * kTB + p4, src, in ? 16 : 0);
+                        }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < NSEG; ++j)
+                        for (int e = t; e < kTK * kTB; e += kStageThreads) {
+                            const int k = k0 + (e >> 5), q = e & 31;
+                            const bool in = sval[j] && k < K && b0 + q < B;
+                            const float* src = in ? (k < seg[j].kb ? seg[j].X1 : seg[j].X2) + (long long)k * B + b0 + q
+                                                  : reinterpret_cast<const float*>(items);
+                            cp_async4(dst + (j * kTK + (e >> 5)) * kTB + q, src, in ? 4 : 0);
+                        }
                 }
             }
-            const int k0 = (cbase + c) * kTK;
-#pragma unroll
-            for (int j = 0; j < NSEG; ++j)
-#pragma unroll
-                for (int i = 0; i < NI; ++i) {
-                    const int kp = (t >> 5) + RPI * i;
-                    const int k = k0 + 2 * kp;
-                    float x0 = 0.f, x1 = 0.f;
-                    if (sval[j] && kp < 32) {
-                        if (k < K) x0 = (k < seg[j].kb ? seg[j].X1 : seg[j].X2)[(long long)k * B + gb];
-                        if (k + 1 < K) x1 = (k + 1 < seg[j].kb ? seg[j].X1 : seg[j].X2)[(long long)(k + 1) * B + gb];
-                    }
-                    xv[2 * (NI * j + i)] = x0;
-                    xv[2 * (NI * j + i) + 1] = x1;
-                }
+            cp_async_commit();  // one group per chunk (empty past the end) keeps the counting simple
         };
-        auto store = [&](const float (&xv)[2 * NP]) -> bool {
-            if (staged >= NS && !tc_wait(&empty[st], ph ^ 1u, abort_flag)) return false;
+        for (int g = 0; g < kXRing - 1; ++g) issue(g);
+        for (int g = 0; g < total && ok; ++g) {
+            cp_async_wait<kXRing - 2>();                               // this thread's copies of chunk g
+            asm volatile("bar.sync 1, %0;\n" ::"n"(kStageThreads) : "memory");  // everyone's
+            issue(g + kXRing - 1);  // into the slot of chunk g - 1, which every thread has split
+            // the stage must be free; the staging threads leave together if any of them gives up (a
+            // thread left alone at the named barrier would wait forever)
+            const bool free_stage = staged < NS || tc_wait(&empty[st], ph ^ 1u, abort_flag);
+            if (!(ok = bar_and(2, kStageThreads, free_stage))) break;
+            const float* src = ring + (g % kXRing) * RC;
             unsigned char* sx = base + size_t(st) * SB + 3 * kPlaneA;
             constexpr unsigned xp = unsigned(NSEG) * kPlaneX;
-#pragma unroll
-            for (int j = 0; j < NSEG; ++j)
-#pragma unroll
-                for (int i = 0; i < NI; ++i) {
-                    const int kp = (t >> 5) + RPI * i;
-                    if (kp >= 32) continue;
-                    const int kl = 2 * kp;
-                    __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
-                    split3(xv[2 * (NI * j + i)], p0a, p1a, p2a);
-                    split3(xv[2 * (NI * j + i) + 1], p0b, p1b, p2b);
-                    const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
-                                         ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
-                    *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
-                    *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
-                    *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
-                }
+            // one (k, k + 1) pair of one request per item: NSEG x 32 pairs x 32 requests
+            for (int e = t; e < NSEG * 32 * kTB; e += kStageThreads) {
+                const int n = e & 31, kp = (e >> 5) & 31, j = e >> 10;
+                const float x0 = src[(j * kTK + 2 * kp) * kTB + n], x1 = src[(j * kTK + 2 * kp + 1) * kTB + n];
+                __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
+                split3(x0, p0a, p1a, p2a);
+                split3(x1, p0b, p1b, p2b);
+                const int kl = 2 * kp;
+                const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
+                                     ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
+                *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
+                *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
+                *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+            }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_arrive(&x_full[st]);
             ++staged;
             if (++st == NS) { st = 0; ph ^= 1u; }
-            return true;
-        };
-        if (total > 0) load(0, xa);
-        for (int g = 0; g < total && ok; g += 2) {
-            if (g + 1 < total) load(g + 1, xb);
-            ok = store(xa);
-            if (!ok || g + 1 >= total) break;
-            if (g + 2 < total) load(g + 2, xa);
-            ok = store(xb);
         }
+        cp_async_wait<0>();  // nothing of this thread's may land after the shared memory is gone
         if (!ok) atomicExch(err, 1);
     } else {
         // ---- warps 0-3: add every chunk's accumulators to FP32 running sums (round to nearest),
@@ -786,15 +806,15 @@ void launch_umma(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, i
                  int ksplit) {
     const int nseg = tc_shape(KIND, s).nseg;
     if (nseg == 1) launch_umma_n<KIND, 1>(st, tm, items, cnt, s, B, err, ksplit);
-    else if (nseg == 2) launch_umma_n<KIND, 2>(st, tm, items, cnt, s, B, err, ksplit);
-    else launch_umma_n<KIND, 4>(st, tm, items, cnt, s, B, err, ksplit);
+    else launch_umma_n<KIND, 2>(st, tm, items, cnt, s, B, err, ksplit);
 }
 
 }  // namespace
 
 bool mx_tc_supported(int kind, int s) {
     // s a power of two >= 16: K a multiple of 16, each right-hand-side block a power-of-two number
-    // of rows of at least 32, at most four blocks per tile
+    // of rows of at least 64, at most two blocks per tile (the compact H of s = 16 stays on the
+    // CUDA-core kernel)
     if (s < 16 || (s & (s - 1)) != 0) return false;
     const TcShape sh = tc_shape(kind, s);
     return sh.nseg <= kMaxSeg && sh.K % 16 == 0;
