@@ -31,6 +31,9 @@ namespace efgb {
 extern std::atomic<long long> g_kernel_launches;
 // LU panels of matrices with >= 512 rows left use the cooperative multi-CTA panel (default on)
 extern std::atomic<bool> g_cooperative_lu;
+// 16 x 16 leaves take the exact residual through the general leaf-size kernel (default off; the
+// kernel for 16 x 16 leaves gives bit-identical results)
+extern std::atomic<bool> g_general_residual;
 
 // ------------------------------------------------------------------------------------------------
 // Batched FP64 dense linear algebra (pointer arrays, uniform shapes and offsets per launch)

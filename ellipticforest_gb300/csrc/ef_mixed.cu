@@ -29,6 +29,8 @@ namespace cg = cooperative_groups;
 
 namespace efgb {
 
+std::atomic<bool> g_general_residual{false};
+
 namespace {
 
 // ---- FP32 pass, upward ---------------------------------------------------------------------------
@@ -1678,6 +1680,188 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __r
     if (rleaf && act && t == 0) rleaf[(long long)b * L + leaf] = mx;
 }
 
+// Exact residual for 16 x 16 leaves: the arithmetic of k_mx_leaf_residual (same scales, exact
+// second differences, 128-bit products, one rounding; bit-identical results) with 16 threads per
+// item and 16 items per block, and no block barrier:
+//  - lane t first owns column t of its item: the 16 lanes load the item's rows as 128-byte
+//    segments, convert their cells to fixed point and write them into the item's tile in shared
+//    memory, whose rows -1 and 16 receive the W and E ghost cells 2 M_g - M_C;
+//  - after __syncwarp lane t owns row t: its cells, the rows above and below (ghost rows at the
+//    W and E faces) and its own S and N ghost cells give both second differences in registers,
+//    and the rest of the cell's work (products, subtraction, rounding, the store of q) follows in
+//    that layout;
+//  - the item's largest exponents and bit lengths reduce over its 16 lanes by shuffles.
+// The tile's rows are 18 words apart (144 B), so the row reads (16-byte vectors) and the column
+// writes (8-byte) are both free of bank conflicts.  f is loaded in the row layout (16-byte vectors).
+// FORM 0 keeps the cells' second differences in registers between the bit-length sweep and the
+// products; FORM 1 (two differences and the lambda term) recomputes them from the tile.
+template <int FORM>
+__global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict__ coefs,
+                                                       const MixLeaf* __restrict__ leaves, int L, int B,
+                                                       const double* __restrict__ f, const double* __restrict__ u64,
+                                                       float* __restrict__ q, float* __restrict__ rleaf) {
+    constexpr int RS = 18, TS = 18 * RS;
+    __shared__ __align__(16) long long tiles[16 * TS];
+    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
+    const long long item = (long long)blockIdx.x * 16 + slot;
+    const bool act = item < (long long)L * B;
+    const int leaf = act ? int(item / B) : 0;
+    const int b = act ? int(item - (long long)leaf * B) : 0;
+    const MixLeaf lf = leaves[leaf];
+    const MixCoef cf = coefs[lf.type];
+    const long long base = ((long long)b * L + leaf) * 256;
+    long long* tl = tiles + slot * TS;  // row r (-1..16) at tl + (r + 1) * RS
+    // (0) loads: column t of u and this lane's ghost value on every side
+    double uc[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) uc[i] = act ? u64[base + i * 16 + t] : 0.0;
+    double gv[4];
+#pragma unroll
+    for (int side = 0; side < 4; ++side) gv[side] = act ? lf.g64[(long long)(side * 16 + t) * B + b] : 0.0;
+    // (1) largest biased exponent of u and the ghosts (Eu), at least 1
+    int eu = 1;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) eu = max(eu, fx_bexp(uc[i]));
+#pragma unroll
+    for (int side = 0; side < 4; ++side) eu = max(eu, fx_bexp(gv[side]));
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) eu = max(eu, __shfl_xor_sync(0xffffffffu, eu, o));
+    const int Eu = eu;
+    // (2) fixed point: the column into the tile, the W/E ghost rows, this lane's S/N ghosts
+    long long gx[4];
+#pragma unroll
+    for (int side = 0; side < 4; ++side) gx[side] = fx_from(gv[side], Eu);
+    long long top_c, bot_c;  // the column's first and last cells (W and E edge fluxes)
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const long long m = fx_from(uc[i], Eu);
+        tl[(i + 1) * RS + t] = m;
+        if (i == 0) top_c = m;
+        if (i == 15) bot_c = m;
+    }
+    tl[t] = 2 * gx[0] - top_c;
+    tl[17 * RS + t] = 2 * gx[1] - bot_c;
+    // row t of f (16-byte vectors), in flight while the second differences are formed
+    double2 fr[8];
+    const double2* f2 = reinterpret_cast<const double2*>(f + base + t * 16);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) fr[m] = act ? f2[m] : make_double2(0.0, 0.0);
+    __syncwarp();
+    // (3) row t: second differences (iso: sx = Sx + Sy) from the rows above and below and the
+    // row's own cells, the S/N ghost cells at its ends
+    const bool lam = FORM != 0 && cf.lmm != 0, iso = FORM == 0 || cf.iso != 0;
+    const long long* rw = tl + (t + 1) * RS;
+    if (act) {
+        // edge fluxes of the state, h = +-(2/d)(u_edge - g): W/E at column t, S/N at row t; the
+        // difference of the fixed-point values is exact, then one rounding to FP64
+        double* h = lf.h64 + b;
+        h[(long long)(0 * 16 + t) * B] = cf.dtn_x * fx_to_double(top_c - gx[0], Eu - 1081);
+        h[(long long)(1 * 16 + t) * B] = -cf.dtn_x * fx_to_double(bot_c - gx[1], Eu - 1081);
+        h[(long long)(2 * 16 + t) * B] = cf.dtn_y * fx_to_double(rw[0] - gx[2], Eu - 1081);
+        h[(long long)(3 * 16 + t) * B] = -cf.dtn_y * fx_to_double(rw[15] - gx[3], Eu - 1081);
+    }
+    auto row_diffs = [&](int m, long long (&c)[2], long long (&sx)[2], long long (&sy)[2]) {
+        const longlong2 cc = reinterpret_cast<const longlong2*>(rw)[m];
+        const longlong2 up = reinterpret_cast<const longlong2*>(rw - RS)[m];
+        const longlong2 dn = reinterpret_cast<const longlong2*>(rw + RS)[m];
+        const long long left = m > 0 ? rw[2 * m - 1] : 2 * gx[2] - cc.x;
+        const long long right = m < 7 ? rw[2 * m + 2] : 2 * gx[3] - cc.y;
+        c[0] = cc.x;
+        c[1] = cc.y;
+        sx[0] = up.x + dn.x - 2 * cc.x;
+        sx[1] = up.y + dn.y - 2 * cc.y;
+        sy[0] = left + cc.y - 2 * cc.x;
+        sy[1] = cc.x + right - 2 * cc.y;
+        if (iso) {
+            sx[0] += sy[0];
+            sx[1] += sy[1];
+        }
+    };
+    constexpr bool KEEP = FORM == 0;
+    long long ks[KEEP ? 16 : 1];
+    unsigned long long ox = 0ull, oy = 0ull;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        long long c[2], sx[2], sy[2];
+        row_diffs(m, c, sx, sy);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (KEEP) ks[(2 * m + k) % (KEEP ? 16 : 1)] = sx[k];
+            ox |= (unsigned long long)(sx[k] ^ (sx[k] >> 63));
+            if (!iso) oy |= (unsigned long long)(sy[k] ^ (sy[k] >> 63));
+        }
+    }
+    int bx = ox ? 65 - __clzll((long long)ox) : 1, by = oy ? 65 - __clzll((long long)oy) : 1;
+    // largest biased exponent of f (Ef), at least 1
+    int ef = 1;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) ef = max(ef, max(fx_bexp(fr[m].x), fx_bexp(fr[m].y)));
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+        bx = max(bx, __shfl_xor_sync(0xffffffffu, bx, o));
+        if (!iso) by = max(by, __shfl_xor_sync(0xffffffffu, by, o));
+        ef = max(ef, __shfl_xor_sync(0xffffffffu, ef, o));
+    }
+    const int Ef = ef;
+    // (4) the common scale and the products, as in k_mx_leaf_residual
+    const bool bad = Eu == 0x7ff || Ef == 0x7ff;
+    int top = bx + Eu - 1081 + cf.ecx;
+    if (!iso) top = max(top, by + Eu - 1081 + cf.ecy);
+    if (lam) top = max(top, 59 + Eu - 1081 + cf.elm);
+    const int sc = max(Ef - 1083, top - 61);
+    const int dx = sc - (Eu - 1144 + cf.ecx), dy = sc - (Eu - 1144 + cf.ecy), dl = sc - (Eu - 1144 + cf.elm);
+    const int sa = max(-126, min(127, sc)), sb = max(-126, min(127, sc - sa));
+    const float pa = __uint_as_float(unsigned(127 + sa) << 23), pb = __uint_as_float(unsigned(127 + sb) << 23);
+    float mx = 0.f;
+    float4* q4 = reinterpret_cast<float4*>(q + base + t * 16);
+    // r of cells 2m, 2m+1 of the row
+    auto finish = [&](const long long (&c)[2], const long long (&sx)[2], const long long (&sy)[2], double2 fv,
+                      float& r0, float& r1) {
+        float rr[2];
+        const double fk[2] = {fv.x, fv.y};
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            long long R = fx_scaled(fk[k], sc) - fx_term(sx[k], cf.cxm, dx);
+            if (!iso) R -= fx_term(sy[k], cf.cym, dy);
+            if (lam) R -= fx_term(c[k], cf.lmm, dl);
+            rr[k] = bad ? __int_as_float(0x7fffffff) : __fmul_rn(__fmul_rn(__ll2float_rn(R), pa), pb);
+            mx = fmaxf(mx, fabsf(rr[k]));
+        }
+        r0 = rr[0];
+        r1 = rr[1];
+    };
+    if constexpr (KEEP) {
+#pragma unroll
+        for (int m2 = 0; m2 < 4; ++m2) {
+            float4 r4;
+            const long long c0[2] = {0, 0}, sx0[2] = {ks[4 * m2], ks[4 * m2 + 1]};
+            const long long sx1[2] = {ks[4 * m2 + 2], ks[4 * m2 + 3]};
+            finish(c0, sx0, c0, fr[2 * m2], r4.x, r4.y);
+            finish(c0, sx1, c0, fr[2 * m2 + 1], r4.z, r4.w);
+            if (act) q4[m2] = r4;
+        }
+    } else {
+        // the second differences again from the tile, f again from memory (cached): the fully
+        // unrolled sweep would hold too many registers with three products per cell
+        const double2* f2 = reinterpret_cast<const double2*>(f + base + t * 16);
+#pragma unroll 1
+        for (int m2 = 0; m2 < 4; ++m2) {
+            float4 r4;
+            long long c[2], sx[2], sy[2];
+            const double2 fa = act ? f2[2 * m2] : make_double2(0.0, 0.0);
+            const double2 fb = act ? f2[2 * m2 + 1] : make_double2(0.0, 0.0);
+            row_diffs(2 * m2, c, sx, sy);
+            finish(c, sx, sy, fa, r4.x, r4.y);
+            row_diffs(2 * m2 + 1, c, sx, sy);
+            finish(c, sx, sy, fb, r4.z, r4.w);
+            if (act) q4[m2] = r4;
+        }
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (rleaf && act && t == 0) rleaf[(long long)b * L + leaf] = mx;
+}
+
 template <int FORM>
 void mx_residual_launch(cudaStream_t st, unsigned grid, unsigned threads, size_t smem, const MixCoef* coefs,
                         const MixLeaf* leaves, int L, int B, int n, int ipc, const double* f, const double* u64,
@@ -1713,8 +1897,15 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
         if (rmax) mx_rmax(st, rleaf, L, B, rmax);
         return;
     }
-    if (form == 0) mx_residual_launch<0>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
-    else mx_residual_launch<1>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    if (n == 16 && !g_general_residual.load()) {
+        const unsigned grid16 = unsigned((items + 15) / 16);
+        if (form == 0) k_mx_resid16<0><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl);
+        else k_mx_resid16<1><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl);
+    } else if (form == 0) {
+        mx_residual_launch<0>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    } else {
+        mx_residual_launch<1>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
+    }
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }

@@ -234,6 +234,52 @@ def test_device_resident_lane_matches_lane0(ef):
     assert np.array_equal(out.cpu().numpy().reshape(3, n), u0)
 
 
+def _set_general_residual(hps, on):
+    from ellipticforest_gb300._lib import check, load
+    check(load().ef_hps_set_option(hps.handle, b"general-leaf-residual", int(on)))
+
+
+@pytest.mark.parametrize("kind,dom,lam,zero_f,B", [
+    (("uniform", 4), (-1.0, 1.0, -1.0, 1.0), 0.0, False, 5),     # form 0: cx = cy, lambda = 0
+    (("uniform", 3), (0.0, 2.0, 0.0, 1.0), 0.0, False, 3),       # form 1: rectangular cells
+    (("uniform", 3), (-1.0, 1.0, -1.0, 1.0), -2.5, False, 3),    # form 1: Helmholtz lambda
+    (("uniform", 3), (-1.0, 1.0, -1.0, 1.0), 0.0, True, 2),      # f = 0: every product above f
+    (("adaptive", lambda x, y: (x - 0.7) ** 2 + (y - 0.7) ** 2 < 0.04, 0, 4), (0.0, 1.0, 0.0, 1.0), 0.0,
+     False, 3),                                                   # ragged last block
+])
+def test_residual_kernel_16_bit_identical_to_general_kernel(ef, kind, dom, lam, zero_f, B):
+    """16 x 16 leaves take the exact residual through their own kernel (column, then row ownership
+    of the item's fixed-point tile); the general leaf-size kernel computes the same integers, so
+    the two give bit-identical solutions and residual histories."""
+    n = 16
+    root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, dom[0], dom[1], n, dom[2], dom[3]))
+    if kind[0] == "uniform":
+        mesh = ef.Mesh().uniform(kind[1], root)
+    else:
+        mesh = ef.Mesh().refineByFunction(kind[1], 0.0, kind[2], kind[3], root)
+    hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90,
+                                                      lambda_function=lambda x, y: lam + 0.0 * x))
+    hps.buildStage()
+    F, A, R = requests(hps, mesh, B, 57)
+    if zero_f:
+        F[:] = 0.0
+    F[0] *= 1.0e6   # requests of very different size share no scale
+    got = []
+    try:
+        for general in (0, 1):
+            _set_general_residual(hps, general)
+            hps.mixed_init(B)
+            u = hps.mixed_solve(F, A, R, sweeps=2)
+            got.append((u, hps.mixed_residuals(3)[:, :B]))
+    finally:
+        _set_general_residual(hps, 0)
+    assert np.array_equal(got[0][0], got[1][0])
+    assert np.array_equal(got[0][1], got[1][1])
+    ref = fp64_solutions(hps, F, A, R)
+    for k in range(B):
+        assert np.abs(got[0][0][k] - ref[k]).max() <= TOL * np.abs(ref[k]).max(), k
+
+
 def _set_tc(hps, on):
     from ellipticforest_gb300._lib import check, load
     check(load().ef_hps_set_option(hps.handle, b"tensor-cores", int(on)))
