@@ -334,6 +334,8 @@ int ef_hps_set_option(ef_hps* h, const char* key, int value) {
     } else if (k == "tensor-cores") {
         if (value < 0 || value > 2) return fail(EF_ERR_INVALID, "tensor-cores: 0 off, 1 tuned, 2 forced");
         h->hps->set_tensor_cores(value);  // block solvers created from now on
+    } else if (k == "per-level-interface") {
+        efgb::g_level_interface.store(value != 0);  // process-wide, block solvers created from now on
     } else if (k == "general-leaf-residual") {
         efgb::g_general_residual.store(value != 0);  // process-wide
     } else if (k == "cooperative-lu") {

@@ -495,6 +495,13 @@ private:
     float* rleaf_ = nullptr;
     MixCoef* d_coef_ = nullptr;
     int res_form_ = 0;  // residual kernel form: 0 when all leaf types have dx = dy and lambda = 0
+    // interface rows traced to the leaves (trees without coarsening steps)
+    bool direct_ = false;
+    MxRow* d_gsrc_ = nullptr;     // [L][4n] Dirichlet rows of the leaves
+    MxMis* d_mis_ = nullptr;      // interface mismatch rows of every node
+    long long nmis_ = 0;
+    MxRow* d_rootsrc_ = nullptr;  // the root's boundary-flux rows (Robin root data)
+    int nroot_ = 0;
     MixFp* d_fps_ = nullptr;  // FivePointStencil leaves only
     float* fp_band32_ = nullptr;
     float* fp_bcoef32_ = nullptr;

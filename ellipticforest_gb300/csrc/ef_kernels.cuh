@@ -34,6 +34,9 @@ extern std::atomic<bool> g_cooperative_lu;
 // 16 x 16 leaves take the exact residual through the general leaf-size kernel (default off; the
 // kernel for 16 x 16 leaves gives bit-identical results)
 extern std::atomic<bool> g_general_residual;
+// mixed block solvers created while set run the residual's interface rows level by level on every
+// tree (default off: trees without coarsening steps read and difference the rows in place)
+extern std::atomic<bool> g_level_interface;
 
 // ------------------------------------------------------------------------------------------------
 // Batched FP64 dense linear algebra (pointer arrays, uniform shapes and offsets per launch)
@@ -141,13 +144,51 @@ struct LeafType32 {
     const float* Dinv;
 };
 
+// A [B]-row of a mixed solver's arena: its buffer (byte offset / 256 from the arena's base) and row;
+// the address depends on the block's request count B, the row stride of every buffer
+struct MxRow {
+    unsigned buf, row;
+};
+template <class T>
+__host__ __device__ inline T* mx_row(const char* arena, MxRow r, int B) {
+    return reinterpret_cast<T*>(const_cast<char*>(arena) + size_t(r.buf) * 256) + size_t(r.row) * size_t(B);
+}
+
 struct MixLeaf {
     int type;
     float* g32;   // [4n][B] Dirichlet data of the FP32 pass
     float* h32;   // [4n][B] particular flux of the FP32 pass
     double* g64;  // [4n][B] exact Dirichlet data of the state
     double* h64;  // [4n][B] edge flux of the state
+    // the 4n rows of the exact Dirichlet data where they live: rows of g64, or, on a tree without
+    // coarsening steps, rows of the root data and of the ancestors' interface states
+    const MxRow* gsrc;
+    const char* arena;  // base of the rows
 };
+
+// Merge index maps of a 4-to-1 node (the mixed kernels and the host tables that trace them).
+// Interface I (0..3) of a node with child interfaces of s points: its lower and upper children and
+// their rows; exterior row p of the node (8s rows, 2s per side): child c and its row q.
+__host__ __device__ inline int mx_lower_child(int I) { return (I == 1) ? 1 : (I == 3 ? 2 : 0); }
+__host__ __device__ inline int mx_upper_child(int I) { return (I == 0) ? 2 : (I == 2 ? 1 : 3); }
+__host__ __device__ inline int mx_q_lower(int I, int o, int s) { return (I < 2 ? 3 * s : s) + o; }
+__host__ __device__ inline int mx_q_upper(int I, int o, int s) { return (I < 2 ? 2 * s : 0) + o; }
+__host__ __device__ inline void mx_ext_map(int p, int s, int& c, int& q) {
+    const int side = p / (2 * s);
+    const int r = p - side * 2 * s;
+    const int hlf = r >= s ? 1 : 0;
+    c = side < 2 ? side + 2 * hlf : (side == 2 ? 0 : 2) + hlf;
+    q = side * s + (r - hlf * s);
+}
+
+// one interface row of the residual's flux mismatch: out[b] = FP32(lo[b] - up[b]), lo and up the
+// edge-flux rows of the leaves on the interface's two sides
+struct MxMis {
+    MxRow out, lo, up;
+};
+void mx_mismatch(cudaStream_t st, const char* arena, const MxMis* rows, long long nrows, int B);
+// dst row e ([B], rows contiguous) = row src[e]
+void mx_gather_rows64(cudaStream_t st, const char* arena, const MxRow* src, double* dst, int nrows, int B);
 
 struct MixItem {
     const float* S;       // 4s x 8s

@@ -30,6 +30,7 @@ namespace cg = cooperative_groups;
 namespace efgb {
 
 std::atomic<bool> g_general_residual{false};
+std::atomic<bool> g_level_interface{false};
 
 namespace {
 
@@ -514,6 +515,47 @@ __global__ void k_mx_flux_up4(const MixItem* __restrict__ items, int s, int B) {
                 make_float4(d2f_rn_bits(l0.x - u0.x), d2f_rn_bits(l0.y - u0.y), d2f_rn_bits(l1.x - u1.x),
                             d2f_rn_bits(l1.y - u1.y));
         }
+    }
+}
+
+// The same two steps on a tree without coarsening steps, where every row is copied unchanged from
+// level to level: the leaves' residual kernels read their Dirichlet rows where they live (the
+// root data and the ancestors' interface states, through MixLeaf::gsrc), and every interface row
+// of every node takes its flux mismatch straight from the edge fluxes of the two leaves that meet
+// there -- one launch instead of a scatter and a flux step per level.
+__global__ void k_mx_mismatch(const char* __restrict__ arena, const MxMis* __restrict__ rows, long long nrows, int B) {
+    if ((B & 3) == 0) {
+        const int B4 = B >> 2;
+        for (long long e4 = blockIdx.x * (long long)blockDim.x + threadIdx.x; e4 < nrows * B4;
+             e4 += (long long)gridDim.x * blockDim.x) {
+            const long long r = e4 / B4;
+            const int b = int(e4 - r * B4) * 4;
+            const MxMis m = rows[r];
+            const double* lo = mx_row<const double>(arena, m.lo, B) + b;
+            const double* up = mx_row<const double>(arena, m.up, B) + b;
+            const double2 l0 = *reinterpret_cast<const double2*>(lo), l1 = *reinterpret_cast<const double2*>(lo + 2);
+            const double2 u0 = *reinterpret_cast<const double2*>(up), u1 = *reinterpret_cast<const double2*>(up + 2);
+            *reinterpret_cast<float4*>(mx_row<float>(arena, m.out, B) + b) = make_float4(d2f_rn_bits(l0.x - u0.x), d2f_rn_bits(l0.y - u0.y),
+                                                                d2f_rn_bits(l1.x - u1.x), d2f_rn_bits(l1.y - u1.y));
+        }
+    } else {
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nrows * B;
+             e += (long long)gridDim.x * blockDim.x) {
+            const long long r = e / B;
+            const int b = int(e - r * B);
+            const MxMis m = rows[r];
+            mx_row<float>(arena, m.out, B)[b] = d2f_rn_bits(mx_row<const double>(arena, m.lo, B)[b] -
+                                                            mx_row<const double>(arena, m.up, B)[b]);
+        }
+    }
+}
+
+__global__ void k_mx_gather_rows64(const char* __restrict__ arena, const MxRow* __restrict__ src,
+                                   double* __restrict__ dst, int nrows, int B) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)nrows * B;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int r = int(e / B), b = int(e - (long long)r * B);
+        dst[e] = mx_row<const double>(arena, src[r], B)[b];
     }
 }
 
@@ -1030,7 +1072,8 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     extern __shared__ long long fx_tile[];
     __shared__ unsigned smax[64];
     __shared__ int seu[64], sef[64], sbx[64], sby[64];
-    __shared__ const double* sg[64];
+    __shared__ const MxRow* sg[64];  // the item's Dirichlet data rows
+    __shared__ int sgb[64];                   // and its request
     __shared__ double* sh[64];
     const int n = NT ? NT : n_arg;
     const int nn = n * n, tpi = nn / 4, n4 = 4 * n;
@@ -1048,7 +1091,8 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
         const int it = item0 + int(threadIdx.x);
         if ((long long)it < items) {
             const int lf = it / B, bb = it - lf * B;
-            sg[threadIdx.x] = leaves[lf].g64 + bb;
+            sg[threadIdx.x] = leaves[lf].gsrc;
+            sgb[threadIdx.x] = bb;
             sh[threadIdx.x] = leaves[lf].h64 + bb;
         }
     }
@@ -1078,7 +1122,8 @@ __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(con
     for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
         const int k = idx / IPC, s = idx - k * IPC;
         if (s < nact)
-            reinterpret_cast<double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k] = sg[s][(long long)k * B];
+            reinterpret_cast<double*>(fx_tile + (long long)s * (nn + 2 * n4) + nn + n4)[k] =
+                mx_row<const double>(leaves[0].arena, sg[s][k], B)[sgb[s]];
     }
     __syncthreads();
     // (1) scales: largest biased exponents of u and the ghosts (Eu), and of f (Ef)
@@ -1262,7 +1307,8 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
                                                            float* __restrict__ q, float* __restrict__ rleaf) {
     extern __shared__ double r0_gd[];  // per item: 4n ghost values, later the fluxes; then 4n floats
     __shared__ unsigned smax[64];
-    __shared__ const double* sg[64];
+    __shared__ const MxRow* sg[64];  // the item's Dirichlet data rows
+    __shared__ int sgb[64];                   // and its request
     __shared__ double* sh[64];
     const int n = NT ? NT : n_arg;
     const int nn = n * n, tpi = nn / 4, n4 = 4 * n;
@@ -1276,7 +1322,8 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
         const int it = item0 + int(threadIdx.x);
         if ((long long)it < items) {
             const int lf = it / B, bb = it - lf * B;
-            sg[threadIdx.x] = leaves[lf].g64 + bb;
+            sg[threadIdx.x] = leaves[lf].gsrc;
+            sgb[threadIdx.x] = bb;
             sh[threadIdx.x] = leaves[lf].h64 + bb;
         }
     }
@@ -1297,7 +1344,7 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0(const MixCoef* __rest
     for (int idx = threadIdx.x; idx < n4 * IPC; idx += blockDim.x) {
         const int k = idx / IPC, s = idx - k * IPC;
         if (s < nact) {
-            const double g = sg[s][(long long)k * B];
+            const double g = mx_row<const double>(leaves[0].arena, sg[s][k], B)[sgb[s]];
             r0_gd[s * n4 + k] = g;
             const MixCoef& c = coefs[leaves[(item0 + s) / B].type];
             gt[s * n4 + k] = -2.0f * (k < 2 * n ? c.cx32 : c.cy32) * d2f_rn_bits(g);
@@ -1549,6 +1596,19 @@ void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B)
     ++g_kernel_launches;
 }
 
+void mx_mismatch(cudaStream_t st, const char* arena, const MxMis* rows, long long nrows, int B) {
+    if (nrows <= 0) return;
+    const long long work = (B % 4 == 0) ? nrows * (B / 4) : nrows * B;
+    k_mx_mismatch<<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
+    ++g_kernel_launches;
+}
+
+void mx_gather_rows64(cudaStream_t st, const char* arena, const MxRow* src, double* dst, int nrows, int B) {
+    if (nrows <= 0) return;
+    k_mx_gather_rows64<<<mx_grid((long long)nrows * B), 256, 0, st>>>(arena, src, dst, nrows, B);
+    ++g_kernel_launches;
+}
+
 void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B) {
     dim3 g(mx_grid(2LL * nf * B), count);
     if (fp64) k_mx_coarsen<double><<<g, 256, 0, st>>>((const double* const*)in, (double* const*)out, nf, B);
@@ -1643,7 +1703,7 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __r
     for (int m = 0; m < 8; ++m) fv[m] = act ? f2[t + 16 * m] : make_double2(0.0, 0.0);
     double gv[4];
 #pragma unroll
-    for (int side = 0; side < 4; ++side) gv[side] = act ? lf.g64[(long long)(side * 16 + t) * B + b] : 0.0;
+    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
     float* gt = gts + slot * 64;
 #pragma unroll
     for (int side = 0; side < 4; ++side)
@@ -1717,7 +1777,7 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     for (int i = 0; i < 16; ++i) uc[i] = act ? u64[base + i * 16 + t] : 0.0;
     double gv[4];
 #pragma unroll
-    for (int side = 0; side < 4; ++side) gv[side] = act ? lf.g64[(long long)(side * 16 + t) * B + b] : 0.0;
+    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
     // (1) largest biased exponent of u and the ghosts (Eu), at least 1
     int eu = 1;
 #pragma unroll

@@ -9,17 +9,6 @@
 namespace efgb {
 namespace {
 
-__device__ __forceinline__ int mx_lower_child(int I) { return (I == 1) ? 1 : (I == 3 ? 2 : 0); }
-__device__ __forceinline__ int mx_upper_child(int I) { return (I == 0) ? 2 : (I == 2 ? 1 : 3); }
-__device__ __forceinline__ int mx_q_lower(int I, int o, int s) { return (I < 2 ? 3 * s : s) + o; }
-__device__ __forceinline__ int mx_q_upper(int I, int o, int s) { return (I < 2 ? 2 * s : 0) + o; }
-__device__ __forceinline__ void mx_ext_map(int p, int s, int& c, int& q) {
-    const int side = p / (2 * s);
-    const int r = p - side * 2 * s;
-    const int hlf = r >= s ? 1 : 0;
-    c = side < 2 ? side + 2 * hlf : (side == 2 ? 0 : 2) + hlf;
-    q = side * s + (r - hlf * s);
-}
 __device__ __forceinline__ void mx_child_ifaces(int c, int& Ia, int& Ib) {
     Ia = (c == 0 || c == 2) ? 0 : 1;
     Ib = (c < 2) ? 2 : 3;

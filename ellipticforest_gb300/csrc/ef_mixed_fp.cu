@@ -272,10 +272,8 @@ __global__ void __launch_bounds__(256) k_mx_fp_residual(const MixFp* __restrict_
     }
     __syncthreads();  // the boundary phase rewrites cells stored by other threads of the block
     if (act) {
-        const double* gW = lf.g64 + b;
-        const double* gE = lf.g64 + (long long)n * B + b;
-        const double* gS = lf.g64 + 2LL * n * B + b;
-        const double* gN = lf.g64 + 3LL * n * B + b;
+        // Dirichlet data row k of the leaf
+        auto gr = [&](int k) { return mx_row<const double>(lf.arena, lf.gsrc[k], B); };
         for (int k = lt; k < 4 * n - 4; k += tpe) {
             int i, j;
             if (k < n) { i = 0; j = k; }
@@ -283,10 +281,10 @@ __global__ void __launch_bounds__(256) k_mx_fp_residual(const MixFp* __restrict_
             else { const int m = k - 2 * n; i = 1 + (m >> 1); j = (m & 1) ? n - 1 : 0; }
             const int c = i * n + j;
             const double uc = zero_state ? 0.0 : uu[c];
-            const double xm = i > 0 ? (zero_state ? 0.0 : uu[c - n]) : fma(2.0, gW[(long long)j * B], -uc);
-            const double xp = i < n - 1 ? (zero_state ? 0.0 : uu[c + n]) : fma(2.0, gE[(long long)j * B], -uc);
-            const double ym = j > 0 ? (zero_state ? 0.0 : uu[c - 1]) : fma(2.0, gS[(long long)i * B], -uc);
-            const double yp = j < n - 1 ? (zero_state ? 0.0 : uu[c + 1]) : fma(2.0, gN[(long long)i * B], -uc);
+            const double xm = i > 0 ? (zero_state ? 0.0 : uu[c - n]) : fma(2.0, gr(j)[b], -uc);
+            const double xp = i < n - 1 ? (zero_state ? 0.0 : uu[c + n]) : fma(2.0, gr(n + j)[b], -uc);
+            const double ym = j > 0 ? (zero_state ? 0.0 : uu[c - 1]) : fma(2.0, gr(2 * n + i)[b], -uc);
+            const double yp = j < n - 1 ? (zero_state ? 0.0 : uu[c + 1]) : fma(2.0, gr(3 * n + i)[b], -uc);
             const double r = fma(-cN[c], yp, fma(-cS[c], ym, fma(-cE[c], xp, fma(-cW[c], xm, fma(-cC[c], uc, ff[c])))));
             const float rf = d2f_bits_fp(r);
             q[base + c] = rf;
@@ -300,7 +298,7 @@ __global__ void __launch_bounds__(256) k_mx_fp_residual(const MixFp* __restrict_
             else if (side == 1) cell = (n - 1) * n + pos;
             else if (side == 2) cell = pos * n;
             else cell = pos * n + n - 1;
-            const double gv = lf.g64[(long long)r * B + b];
+            const double gv = gr(r)[b];
             const double dtn = (side == 0 || side == 2) ? (side < 2 ? mf.dtn_x : mf.dtn_y)
                                                         : -(side < 2 ? mf.dtn_x : mf.dtn_y);
             lf.h64[(long long)r * B + b] = zero_state ? -dtn * gv : dtn * (uu[cell] - gv);

@@ -100,6 +100,14 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     const Mesh& mesh = hps.mesh();
     mn_.assign(N, MNode());
 
+    // a tree without coarsening steps copies rows unchanged from level to level: the residual reads
+    // the leaves' Dirichlet rows where they live and takes every interface mismatch straight from
+    // two leaf edge-flux rows (tables traced below)
+    const bool direct = hps.step_nodes_t_.empty() && hps.step_nodes_g_.empty() && !g_level_interface.load();
+    long long nmis = 0;
+    for (int id = 0; id < N && direct; ++id)
+        if (!mesh.nodes[id].leaf()) nmis += 4LL * hps.nodes_[id].s;
+    const int nroot = direct && N > 1 ? 8 * hps.nodes_[0].s : 0;
     auto layout = [&](MxCarver& cv) {
         // interface states first, contiguous (cleared at every solve)
         const size_t ug0 = cv.off;
@@ -150,6 +158,9 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         d_coef_ = cv.get<MixCoef>(hps.types_.size());
         d_types32_ = cv.get<LeafType32>(hps.types_.size());
         d_leaves_ = cv.get<MixLeaf>(L);
+        d_gsrc_ = cv.get<MxRow>(size_t(L) * 4 * n);
+        d_mis_ = cv.get<MxMis>(size_t(nmis));
+        d_rootsrc_ = cv.get<MxRow>(size_t(nroot));
         if (fp) {
             // FP32 band factors and FP64 stencil tables, shared by the lanes of one tree
             d_fps_ = cv.get<MixFp>(L);
@@ -267,10 +278,90 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         }
         ck(upload_sync(st_, d_coef_, co.data(), co.size() * sizeof(MixCoef)), "mixed coefs");
     }
+    // where each leaf's Dirichlet rows live, and the rows of every interface mismatch: traced
+    // through the index maps of the per-level kernels (exterior rows to the children, the parent's
+    // interface state to both sides; upward, exterior fluxes from the children)
+    direct_ = direct;
+    nmis_ = nmis;
+    nroot_ = nroot;
+    {
+        // rows are named by buffer and row: their addresses depend on the block's request count
+        auto row = [&](const void* buf, size_t r) {
+            const size_t off = size_t(reinterpret_cast<const char*>(buf) - arena_);
+            if (off % 256 != 0 || off / 256 > 0xffffffffull) throw std::logic_error("mixed solver: arena row");
+            return MxRow{unsigned(off / 256), unsigned(r)};
+        };
+        const size_t n4 = 4 * size_t(n);
+        std::vector<MxRow> gtab(size_t(L) * n4);
+        if (direct) {
+            std::vector<int> order{0};  // breadth first: parents before children
+            for (size_t i = 0; i < order.size(); ++i)
+                if (!mesh.nodes[order[i]].leaf())
+                    for (int c = 0; c < 4; ++c) order.push_back(mesh.nodes[order[i]].child[c]);
+            std::vector<std::vector<MxRow>> gt(N), ht(N);
+            gt[0].resize(N > 1 ? 8 * size_t(hps.nodes_[0].s) : n4);
+            for (size_t p = 0; p < gt[0].size(); ++p) gt[0][p] = row(mn_[0].g64, p);
+            for (int id : order) {
+                if (mesh.nodes[id].leaf()) continue;
+                const int s = hps.nodes_[id].s;
+                const int* ch = mesh.nodes[id].child;
+                for (int c = 0; c < 4; ++c) gt[ch[c]].assign(4 * size_t(s), MxRow{0u, 0u});
+                for (int p = 0; p < 8 * s; ++p) {
+                    int c, q;
+                    mx_ext_map(p, s, c, q);
+                    gt[ch[c]][q] = gt[id][p];
+                }
+                for (int r = 0; r < 4 * s; ++r) {
+                    const int I = r / s, o = r - I * s;
+                    const MxRow v = row(mn_[id].uG, size_t(r));
+                    gt[ch[mx_lower_child(I)]][mx_q_lower(I, o, s)] = v;
+                    gt[ch[mx_upper_child(I)]][mx_q_upper(I, o, s)] = v;
+                }
+                std::vector<MxRow>().swap(gt[id]);
+            }
+            std::vector<MxMis> mis;
+            mis.reserve(size_t(nmis));
+            for (auto it = order.rbegin(); it != order.rend(); ++it) {
+                const int id = *it;
+                if (mesh.nodes[id].leaf()) {
+                    ht[id].resize(n4);
+                    for (size_t k = 0; k < n4; ++k) ht[id][k] = row(mn_[id].h64, k);
+                    continue;
+                }
+                const int s = hps.nodes_[id].s;
+                const int* ch = mesh.nodes[id].child;
+                ht[id].resize(8 * size_t(s));
+                for (int e = 0; e < 8 * s; ++e) {
+                    int c, q;
+                    mx_ext_map(e, s, c, q);
+                    ht[id][e] = ht[ch[c]][q];
+                }
+                for (int r = 0; r < 4 * s; ++r) {
+                    const int I = r / s, o = r - I * s;
+                    mis.push_back(MxMis{row(mn_[id].m32, size_t(r)), ht[ch[mx_lower_child(I)]][mx_q_lower(I, o, s)],
+                                        ht[ch[mx_upper_child(I)]][mx_q_upper(I, o, s)]});
+                }
+                for (int c = 0; c < 4; ++c) std::vector<MxRow>().swap(ht[ch[c]]);
+            }
+            for (int k = 0; k < L; ++k) {
+                const auto& g = gt[mesh.leaves[k]];
+                if (g.size() != n4) throw std::logic_error("mixed solver: leaf Dirichlet rows not traced");
+                std::copy(g.begin(), g.end(), gtab.begin() + size_t(k) * n4);
+            }
+            if ((long long)mis.size() != nmis) throw std::logic_error("mixed solver: interface rows not traced");
+            ck(upload_sync(st_, d_mis_, mis.data(), mis.size() * sizeof(MxMis)), "mismatch rows");
+            if (nroot) ck(upload_sync(st_, d_rootsrc_, ht[0].data(), size_t(nroot) * sizeof(MxRow)), "root rows");
+        } else {
+            for (int k = 0; k < L; ++k)
+                for (size_t j = 0; j < n4; ++j) gtab[size_t(k) * n4 + j] = row(mn_[mesh.leaves[k]].g64, j);
+        }
+        ck(upload_sync(st_, d_gsrc_, gtab.data(), gtab.size() * sizeof(MxRow)), "leaf Dirichlet rows");
+    }
     std::vector<MixLeaf> leaves(L);
     for (int k = 0; k < L; ++k) {
         const int id = mesh.leaves[k];
-        leaves[k] = MixLeaf{hps.nodes_[id].leaf_type, mn_[id].g32, mn_[id].h32, mn_[id].g64, mn_[id].h64};
+        leaves[k] = MixLeaf{hps.nodes_[id].leaf_type, mn_[id].g32, mn_[id].h32, mn_[id].g64, mn_[id].h64,
+                            d_gsrc_ + size_t(k) * 4 * n, arena_};
     }
     ck(upload_sync(st_, d_leaves_, leaves.data(), L * sizeof(MixLeaf)), "mix leaves");
     for (size_t gi = 0; gi < groups_.size(); ++gi) {
@@ -532,15 +623,18 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
     cudaStream_t st = st_;
     const int maxL = h.mesh().max_level;
     const double L = h.num_leaves(), nn = double(h.leaf_n()) * h.leaf_n();
-    // exact Dirichlet data of every node from the root data and the interface state
-    h.pb("mx_interface", st);
-    for (int lvl = 0; lvl < maxL; ++lvl) {
-        for (auto& s : gsteps_)
-            if (s.level == lvl) mx_uncoarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
-        for (auto& g : groups_)
-            if (g.level == lvl) mx_scatter64(st, g.d_items, g.cnt, g.s, B);
+    // exact Dirichlet data of every node from the root data and the interface state (read in place
+    // by the leaves on a tree without coarsening steps)
+    if (!direct_) {
+        h.pb("mx_interface", st);
+        for (int lvl = 0; lvl < maxL; ++lvl) {
+            for (auto& s : gsteps_)
+                if (s.level == lvl) mx_uncoarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
+            for (auto& g : groups_)
+                if (g.level == lvl) mx_scatter64(st, g.d_items, g.cnt, g.s, B);
+        }
+        h.pe(0, 0, st);
     }
-    h.pe(0, 0, st);
     h.pb("mx_leaf_residual", st);
     if (d_fps_)
         mx_fp_residual(st, d_fps_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
@@ -550,11 +644,16 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
                          rleaf_, rmax);
     h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
     h.pb("mx_interface", st);
-    for (int lvl = maxL - 1; lvl >= 0; --lvl) {
-        for (auto& s : hsteps_)
-            if (s.level == lvl + 1) mx_coarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
-        for (auto& g : groups_)
-            if (g.level == lvl) mx_flux_up(st, g.d_items, g.cnt, g.s, B);
+    if (direct_) {
+        mx_mismatch(st, arena_, d_mis_, nmis_, B);
+        if (robin_) mx_gather_rows64(st, arena_, d_rootsrc_, mn_[0].h64, nroot_, B);
+    } else {
+        for (int lvl = maxL - 1; lvl >= 0; --lvl) {
+            for (auto& s : hsteps_)
+                if (s.level == lvl + 1) mx_coarsen(st, true, s.in64, s.out64, s.count, s.nf, B);
+            for (auto& g : groups_)
+                if (g.level == lvl) mx_flux_up(st, g.d_items, g.cnt, g.s, B);
+        }
     }
     // residual of the Robin root condition from the state's root data and exact boundary flux
     if (robin_) mx_root_residual(st, 4 * h.root_M(), B, ra64_, rb64_, r_, mn_[0].g64, mn_[0].h64, rho32_);

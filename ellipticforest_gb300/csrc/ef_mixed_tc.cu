@@ -6,17 +6,24 @@
 // a3 = bf16(a - a1 - a2); the three 8-bit significands cover FP32's 24 bits, so the sum is exact),
 // and the request block X the same way as it is staged.  Every product is formed from the six
 // partial products that reach 2^-24 of |a x|:
-//     D_hi += a1 x1                                  (TMEM accumulator 1)
-//     D_lo += a1 x2 + a2 x1 + a1 x3 + a2 x2 + a3 x1   (TMEM accumulator 2)
-// with tcgen05.mma kind::f16 (bf16 inputs, exact products, FP32 accumulation); y = D_hi + D_lo.
-// Keeping the small terms in their own accumulator stops them from being rounded against the large
-// running sum.  The dropped terms a2 x3, a3 x2, a3 x3 are below 2^-24 |a x|.  The tensor core's own
-// FP32 accumulation is not round-to-nearest (a first version that accumulated all of K in TMEM made
-// an FP32 pass 2.1x less accurate than CUDA-core FMA chains), so every 64-wide K chunk goes to a
-// fresh pair of TMEM accumulators (two pairs, alternating) and the epilogue warps add the chunk's
-// sums to FP32 registers with round-to-nearest: the pass is then at least as accurate as the FMA
-// chains, which the one FP64 refinement sweep is sized for (a 3-pass split-TF32 would round each
-// product to ~2^-21).
+//     D_hi   += a1 x1                   (TMEM accumulator 1)
+//     D_lo_a += a1 x2 + a2 x1 + a3 x1    (TMEM accumulator 2)
+//     D_lo_b += a1 x3 + a2 x2            (TMEM accumulator 3)
+// with tcgen05.mma kind::f16 (bf16 inputs, exact products, FP32 accumulation); y = D_hi + D_lo_a +
+// D_lo_b.  The three X planes lie in shared memory as consecutive rows of one K-major operand
+// [x1 | x2 | x3], and the three accumulators as consecutive TMEM columns, so one k-step is three
+// MMAs: a1 [x1 x2 x3] (N = 96), a2 [x1 x2] (N = 64, into the two low accumulators) and a3 x1
+// (N = 32), each A plane read from shared memory once per k-step (six MMAs of N = 32 read a1 three
+// times and a2 twice).  Keeping the small terms in their own accumulators stops them from being
+// rounded against the large running sum.  The dropped terms a2 x3, a3 x2, a3 x3 are below
+// 2^-24 |a x|.  The tensor core's own FP32 accumulation is not round-to-nearest (a first version
+// that accumulated all of K in TMEM made an FP32 pass 2.1x less accurate than CUDA-core FMA
+// chains), so every 64-wide K chunk goes to a fresh set of TMEM accumulators and the epilogue warps
+// add the chunk's sums to FP32 registers with round-to-nearest: the pass is then at least as
+// accurate as the FMA chains, which the one FP64 refinement sweep is sized for (a 3-pass split-TF32
+// would round each product to ~2^-21).  The CTA holds all 512 TMEM columns (its shared memory keeps
+// it alone on the SM): five sets of 96 columns for one request block per tile, two of 192 for two,
+// so the MMAs run that many chunks ahead of the epilogue warps while they store a tile's rows.
 //
 // Layout.  The three planes of a group's operators (one back-to-back row-major matrix per kind, H
 // with each child's two runs of s rows made adjacent) are streamed by TMA in boxes of 128 rows x
@@ -78,13 +85,18 @@ __host__ __device__ inline TcShape tc_shape(int kind, int s) {
 __host__ __device__ constexpr int tc_stages(int nseg) { return nseg <= 1 ? 3 : 2; }
 __host__ __device__ constexpr int tc_stage_bytes(int nseg) { return 3 * kPlaneA + 3 * nseg * kPlaneX; }
 // stages, barriers (256 bytes), then the FP32 staging ring of the request blocks
-inline size_t tc_smem_bytes(int nseg) {
+__host__ __device__ constexpr size_t tc_smem_bytes(int nseg) {
     return 1024 + size_t(tc_stages(nseg)) * tc_stage_bytes(nseg) + 256 + size_t(kXRing) * nseg * kTK * kTB * 4;
 }
 // two chunk buffers x (D_hi, D_lo) x 32 nseg columns
-__host__ __device__ constexpr int tc_tmem_cols(int nseg) {
-    return 4 * kTB * nseg <= 128 ? 128 : (4 * kTB * nseg <= 256 ? 256 : 512);
-}
+// accumulator sets of a chunk: D_hi, D_lo_a, D_lo_b of 32 nseg columns each, as many as fit in 512
+__host__ __device__ constexpr int tc_acc_sets(int nseg) { return 512 / (3 * kTB * nseg); }
+__host__ __device__ constexpr int tc_tmem_cols(int) { return 512; }
+// all of TMEM per CTA needs one CTA per SM: the shared memory of two would exceed the SM's 228 KB
+static_assert(2 * tc_smem_bytes(1) > 228 * 1024 && 2 * tc_smem_bytes(2) > 228 * 1024, "one CTA per SM");
+// the barrier block (256 bytes): 3 per stage, 2 per accumulator set, drain, never, TMEM slot, abort
+static_assert((3 * tc_stages(1) + 2 * tc_acc_sets(1) + 2) * 8 + 8 <= 256, "barrier block");
+static_assert((3 * tc_stages(2) + 2 * tc_acc_sets(2) + 2) * 8 + 8 <= 256, "barrier block");
 
 // compact H row order of the planes: child c's rows [2s c, 2s c + 2s) are its W/E run and then its
 // S/N run; returns the row p of the WESN compact H (the exterior index) of permuted row pr
@@ -136,21 +148,6 @@ __device__ __forceinline__ void tc_mma(unsigned dtmem, uint64_t a, uint64_t b, u
 __device__ __forceinline__ void tc_commit(unsigned long long* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
                  : "memory");
-}
-// 32 consecutive FP32 columns of the calling warp's 32 TMEM lanes (one lane per thread)
-__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
-    unsigned r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 // 16 consecutive FP32 columns of the calling warp's 32 TMEM lanes (one lane per thread)
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
@@ -416,18 +413,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int nsegs_total = KIND == MX_H ? 4 * cnt : cnt;
     constexpr int NS = tc_stages(NSEG), SB = tc_stage_bytes(NSEG);
     constexpr int ncol = kTB * NSEG, tcols = tc_tmem_cols(NSEG);
-    constexpr unsigned idesc = tc_idesc(kTM, ncol);
+    constexpr int NP = tc_acc_sets(NSEG);
+    constexpr unsigned idesc1 = tc_idesc(kTM, ncol), idesc2 = tc_idesc(kTM, 2 * ncol), idesc3 = tc_idesc(kTM, 3 * ncol);
     extern __shared__ unsigned char tc_smem[];
     unsigned char* base = tc_smem + ((1024u - (smem_u32(tc_smem) & 1023u)) & 1023u);
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(base + size_t(NS) * SB);
     unsigned long long* a_full = bars;             // [NS] TMA transaction barriers
     unsigned long long* x_full = bars + NS;        // [NS] 128 staging arrivals
     unsigned long long* empty = bars + 2 * NS;     // [NS] MMA commit
-    unsigned long long* acc_full = bars + 3 * NS;  // [2] MMA commit at the end of a chunk
-    unsigned long long* acc_empty = acc_full + 2;  // [2] 128 epilogue arrivals
-    unsigned long long* drain = acc_full + 4;      // MMA commit before TMEM is freed
-    unsigned long long* never = acc_full + 5;      // nothing arrives on it (failure-path test)
-    unsigned* tmem_slot = reinterpret_cast<unsigned*>(acc_full + 6);
+    unsigned long long* acc_full = bars + 3 * NS;   // [NP] MMA commit at the end of a chunk
+    unsigned long long* acc_empty = acc_full + NP;  // [NP] 128 epilogue arrivals
+    unsigned long long* drain = acc_full + 2 * NP;  // MMA commit before TMEM is freed
+    unsigned long long* never = drain + 1;          // nothing arrives on it (failure-path test)
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(drain + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -458,7 +456,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_init(&x_full[i], kStageThreads);
             mbar_init(&empty[i], 1);
         }
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < NP; ++i) {
             mbar_init(&acc_full[i], 1);
             mbar_init(&acc_empty[i], 128);
         }
@@ -529,30 +527,27 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t a_base = smem_u32(base);
             if (g_mx_inject_timeout && nunits > 0) ok = tc_wait(never, 0u, abort_flag, 1000000LL);
             for (int gch = 0; gch < total && ok; ++gch) {
-                const int c = gch % cpu, bf = gch & 1;
-                // the chunk's accumulator pair was drained two chunks ago
-                if (gch >= 2) ok = tc_wait(&acc_empty[bf], unsigned((gch >> 1) - 1) & 1u, abort_flag);
+                const int c = gch % cpu, bf = gch % NP;
+                // the chunk's accumulator set was drained NP chunks ago
+                if (gch >= NP) ok = tc_wait(&acc_empty[bf], unsigned(gch / NP - 1) & 1u, abort_flag);
                 if (ok) ok = tc_wait(&a_full[st], ph, abort_flag) && tc_wait(&x_full[st], ph, abort_flag);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t sa = a_base + uint32_t(st) * SB;
                 const uint32_t sx = sa + 3u * kPlaneA;
-                const unsigned dhi = tmem + unsigned(bf * 2 * ncol), dlo = dhi + unsigned(ncol);
+                const unsigned dhi = tmem + unsigned(bf * 3 * ncol), dlo = dhi + unsigned(ncol);
                 const int kleft = K - (cbase + c) * kTK;
                 const int nk = kleft >= kTK ? kTK / 16 : (kleft + 15) / 16;
-                constexpr uint32_t xp = uint32_t(NSEG) * kPlaneX;
                 for (int kk = 0; kk < nk; ++kk) {
                     const uint32_t ko = uint32_t(kk) * 32u;
                     const uint64_t a1 = tc_desc(sa + ko), a2 = tc_desc(sa + kPlaneA + ko),
                                    a3 = tc_desc(sa + 2 * kPlaneA + ko);
-                    const uint64_t x1 = tc_desc(sx + ko), x2 = tc_desc(sx + xp + ko), x3 = tc_desc(sx + 2 * xp + ko);
-                    const unsigned acc = kk > 0 ? 1u : 0u;  // a fresh accumulator pair per chunk
-                    tc_mma(dhi, a1, x1, idesc, acc);
-                    tc_mma(dlo, a1, x2, idesc, acc);
-                    tc_mma(dlo, a2, x1, idesc, 1u);
-                    tc_mma(dlo, a1, x3, idesc, 1u);
-                    tc_mma(dlo, a2, x2, idesc, 1u);
-                    tc_mma(dlo, a3, x1, idesc, 1u);
+                    // the three X planes are consecutive rows of one K-major operand: [x1 | x2 | x3]
+                    const uint64_t x123 = tc_desc(sx + ko);
+                    const unsigned acc = kk > 0 ? 1u : 0u;  // a fresh accumulator set per chunk
+                    tc_mma(dhi, a1, x123, idesc3, acc);  // D_hi = a1 x1, D_lo_a = a1 x2, D_lo_b = a1 x3
+                    tc_mma(dlo, a2, x123, idesc2, 1u);   // D_lo_a += a2 x1, D_lo_b += a2 x2
+                    tc_mma(dlo, a3, x123, idesc1, 1u);   // D_lo_a += a3 x1
                 }
                 tc_commit(&empty[st]);
                 tc_commit(&acc_full[bf]);
@@ -665,19 +660,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const int grow = tile_of(u) * kTM + t;
                 if (grow < R) tc_prefetch_row<KIND>(items, s, B, b0, sh.rows_item, grow, pre, vec);
             }
-            const int bf = gch & 1;
-            if (!(ep_ok = tc_wait(&acc_full[bf], unsigned(gch >> 1) & 1u, abort_flag))) break;
+            const int bf = gch % NP;
+            if (!(ep_ok = tc_wait(&acc_full[bf], unsigned(gch / NP) & 1u, abort_flag))) break;
             tc_fence_after();
-            const unsigned col = unsigned(bf * 2 * ncol + jrow * kTB);
+            const unsigned col = unsigned(bf * 3 * ncol + jrow * kTB);
 #pragma unroll
             for (int hf = 0; hf < 2; ++hf) {
-                float hi[16], lo[16];
+                float hi[16], la[16], lb[16];
                 tmem_ld16(tmem + lane_off + col + unsigned(16 * hf), hi);
-                tmem_ld16(tmem + lane_off + col + unsigned(ncol + 16 * hf), lo);
+                tmem_ld16(tmem + lane_off + col + unsigned(ncol + 16 * hf), la);
+                tmem_ld16(tmem + lane_off + col + unsigned(2 * ncol + 16 * hf), lb);
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     v[16 * hf + q] += hi[q];
-                    rlo[16 * hf + q] += lo[q];
+                    rlo[16 * hf + q] += la[q];
+                    rlo[16 * hf + q] += lb[q];
                 }
             }
             tc_fence_before();

@@ -77,7 +77,16 @@ int ef_hps_set_coefficients(ef_hps* hps, const double* alpha, const double* beta
  * (ef_hps_solve_device_async, ef_hps_mixed_solve*) as CUDA graphs after their first two calls.
  * Added key "cooperative-lu" (default 1, process-wide): LU panels of interface matrices with >= 512
  * rows left run on many CTAs (one grid barrier per column); 0 keeps one CTA per panel.  Both give
- * the same factors bit for bit. */
+ * the same factors bit for bit.
+ * Added key "tensor-cores" (default 1) for the mixed block solvers created afterwards: 0 CUDA-core
+ * node GEMMs only, 1 the faster of the CUDA-core and tcgen05 GEMM per node group (timed), 2 the
+ * tcgen05 GEMM wherever it supports the shape.
+ * Verification keys (process-wide, default 0): "general-leaf-residual" 1 runs the exact residual of
+ * 16 x 16 leaves through the general leaf-size kernel; "per-level-interface" 1 makes mixed block
+ * solvers created afterwards move the residual's interface rows level by level even on trees
+ * without coarsening steps (which otherwise read and difference them in place).  Both give the same
+ * results bit for bit; "inject-wait-timeout" 1 makes the tensor-core GEMMs' first wait run out
+ * (failure-path test: the solve returns EF_ERR_CUDA). */
 int ef_hps_set_option(ef_hps* hps, const char* key, int value);
 /* Use an external CUDA stream (cudaStream_t) for all work of this handle; NULL = default stream. */
 int ef_hps_set_stream(ef_hps* hps, void* cuda_stream);

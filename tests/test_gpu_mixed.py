@@ -280,6 +280,29 @@ def test_residual_kernel_16_bit_identical_to_general_kernel(ef, kind, dom, lam, 
         assert np.abs(got[0][0][k] - ref[k]).max() <= TOL * np.abs(ref[k]).max(), k
 
 
+@pytest.mark.parametrize("L,n,B,robin", [(4, 16, 5, False), (3, 8, 8, False), (3, 16, 6, True)])
+def test_interface_rows_in_place_bit_identical_to_per_level(ef, L, n, B, robin):
+    """On a tree without coarsening steps the residual reads each leaf's Dirichlet rows where they
+    live (root data, ancestors' interface states) and takes every interface mismatch straight from
+    two leaf edge-flux rows; moving the rows level by level gives the same bits.  Blocks smaller
+    than the solver's capacity (row stride = the block's request count) and a Robin root included."""
+    from ellipticforest_gb300._lib import check, load
+    mesh, hps = make(ef, ("uniform", L), n, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, B, 71)
+    got = []
+    try:
+        for per_level in (0, 1):
+            check(load().ef_hps_set_option(hps.handle, b"per-level-interface", per_level))
+            hps.mixed_init(B + 3)
+            if robin:
+                hps.mixed_set_root(np.full(4 * hps.M, 1.0), np.full(4 * hps.M, 0.25))
+            got.append([hps.mixed_solve(F[:k], A[:k], R[:k], sweeps=2) for k in (B, B - 2)])
+    finally:
+        check(load().ef_hps_set_option(hps.handle, b"per-level-interface", 0))
+    for u0, u1 in zip(got[0], got[1]):
+        assert np.array_equal(u0, u1)
+
+
 def _set_tc(hps, on):
     from ellipticforest_gb300._lib import check, load
     check(load().ef_hps_set_option(hps.handle, b"tensor-cores", int(on)))
