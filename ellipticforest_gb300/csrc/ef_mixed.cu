@@ -1801,11 +1801,20 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     }
     tl[t] = 2 * gx[0] - top_c;
     tl[17 * RS + t] = 2 * gx[1] - bot_c;
-    // row t of f (16-byte vectors), in flight while the second differences are formed
-    double2 fr[8];
-    const double2* f2 = reinterpret_cast<const double2*>(f + base + t * 16);
+    // f, in flight while the second differences are formed: FORM 0 loads column t (coalesced) and
+    // moves it to the row owners through the tile once the second differences are formed; FORM 1,
+    // which reads the tile again for its products, loads row t (16-byte vectors)
+    constexpr bool KEEP = FORM == 0;
+    double fc[KEEP ? 16 : 1];
+    double2 fr[KEEP ? 1 : 8];
+    if constexpr (KEEP) {
 #pragma unroll
-    for (int m = 0; m < 8; ++m) fr[m] = act ? f2[m] : make_double2(0.0, 0.0);
+        for (int i = 0; i < 16; ++i) fc[i] = act ? f[base + i * 16 + t] : 0.0;
+    } else {
+        const double2* f2 = reinterpret_cast<const double2*>(f + base + t * 16);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) fr[m] = act ? f2[m] : make_double2(0.0, 0.0);
+    }
     __syncwarp();
     // (3) row t: second differences (iso: sx = Sx + Sy) from the rows above and below and the
     // row's own cells, the S/N ghost cells at its ends
@@ -1837,7 +1846,6 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
             sx[1] += sy[1];
         }
     };
-    constexpr bool KEEP = FORM == 0;
     long long ks[KEEP ? 16 : 1];
     unsigned long long ox = 0ull, oy = 0ull;
 #pragma unroll
@@ -1854,8 +1862,13 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     int bx = ox ? 65 - __clzll((long long)ox) : 1, by = oy ? 65 - __clzll((long long)oy) : 1;
     // largest biased exponent of f (Ef), at least 1
     int ef = 1;
+    if constexpr (KEEP) {
 #pragma unroll
-    for (int m = 0; m < 8; ++m) ef = max(ef, max(fx_bexp(fr[m].x), fx_bexp(fr[m].y)));
+        for (int i = 0; i < 16; ++i) ef = max(ef, fx_bexp(fc[i]));
+    } else {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) ef = max(ef, max(fx_bexp(fr[m].x), fx_bexp(fr[m].y)));
+    }
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) {
         bx = max(bx, __shfl_xor_sync(0xffffffffu, bx, o));
@@ -1891,13 +1904,19 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
         r1 = rr[1];
     };
     if constexpr (KEEP) {
+        // f column t into the tile (every lane has read its rows of u), row t back out
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) tl[(i + 1) * RS + t] = __double_as_longlong(fc[i]);
+        __syncwarp();
+        const double2* frow = reinterpret_cast<const double2*>(rw);
 #pragma unroll
         for (int m2 = 0; m2 < 4; ++m2) {
             float4 r4;
             const long long c0[2] = {0, 0}, sx0[2] = {ks[4 * m2], ks[4 * m2 + 1]};
             const long long sx1[2] = {ks[4 * m2 + 2], ks[4 * m2 + 3]};
-            finish(c0, sx0, c0, fr[2 * m2], r4.x, r4.y);
-            finish(c0, sx1, c0, fr[2 * m2 + 1], r4.z, r4.w);
+            finish(c0, sx0, c0, frow[2 * m2], r4.x, r4.y);
+            finish(c0, sx1, c0, frow[2 * m2 + 1], r4.z, r4.w);
             if (act) q4[m2] = r4;
         }
     } else {
