@@ -1029,8 +1029,11 @@ def run_profile_only(args):
     hps = ef.HPSAlgorithm(mesh, ef.FiniteVolumeSolver(solver_type=ef.FISHPACK90))
     hps.set_stream(stream.cuda_stream)
     hps.setupStage()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("build")  # ncu --nvtx --nvtx-include "build/"
     hps.buildStage()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     out = {"profile_only": args.profile_only, "level": args.level, "build_merge_launches": hps.build_info()[0]}
     if args.profile_only == "mixed":
         X, Y = mesh.cell_centres()
@@ -1042,11 +1045,19 @@ def run_profile_only(args):
         R = np.stack([reqs[i % 4][3] for i in range(B)])
         from ellipticforest_gb300._lib import check as _check, load as _load
         _check(_load().ef_hps_set_option(hps.handle, b"tensor-cores", args.tensor_cores))
+        if args.gemm_plan:
+            # a plan timed in an earlier run without the profiler (under ncu the candidates' times
+            # are those of serialised replays)
+            hps.mixed_set_gemm_plan(json.loads(args.gemm_plan))
         hps.mixed_init(B)
         hps.mixed_solve(F, A, R, args.sweeps)
+        torch.cuda.synchronize()
+        # the steady-state blocks alone, for ncu --nvtx --nvtx-include "steady/"
+        torch.cuda.nvtx.range_push("steady")
         for _ in range(args.steps):
             hps.mixed_solve_async(B, args.sweeps)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         out["gemm_plan"] = hps.mixed_gemm_plan()
     print(json.dumps(out), flush=True)
 
@@ -1072,6 +1083,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the 512-RHS level-6 case")
     ap.add_argument("--tensor-cores", type=int, default=1, choices=[0, 1, 2],
                     help="node GEMMs of the mixed form: 0 CUDA cores, 1 the faster per level (tuned), 2 tcgen05 wherever supported")
+    ap.add_argument("--gemm-plan", default=None,
+                    help="--profile-only mixed: JSON node-GEMM plan (rows level, s, W, H, DOWN) instead of timing one")
     ap.add_argument("--profile-only", choices=["build", "mixed"], default=None,
                     help="short run for a profiler's launch list: 'build' = set-up and one FP64 build of the "
                          "tree; 'mixed' = build, block-solver set-up and --steps mixed blocks (no timing line)")

@@ -105,6 +105,7 @@ SIGNATURES = {
                                  _dp, _dp]),
     "ef_hps_build_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "ef_hps_mixed_gemm_plan": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "ef_hps_mixed_set_gemm_plan": (C.c_int, [_vp, C.POINTER(C.c_int), C.c_int]),
     "ef_hps_mixed_set_root": (C.c_int, [_vp, _dp, _dp]),
     "ef_server_set_root": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "ef_mesh_level_count": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),

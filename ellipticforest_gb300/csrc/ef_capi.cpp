@@ -727,6 +727,16 @@ int ef_hps_mixed_gemm_plan(ef_hps* h, int max_groups, int* table, int* ngroups) 
     return EF_OK;
 }
 
+int ef_hps_mixed_set_gemm_plan(ef_hps* h, const int* codes, int ngroups) {
+    if (!h || !codes || ngroups < 0) return fail(EF_ERR_INVALID, "null argument");
+    return guarded([&] {
+        std::vector<std::array<int, 3>> c(static_cast<size_t>(ngroups));
+        for (int i = 0; i < ngroups; ++i) c[i] = {codes[3 * i], codes[3 * i + 1], codes[3 * i + 2]};
+        h->hps->set_mx_plan(c);
+        return EF_OK;
+    });
+}
+
 int ef_hps_mixed_set_root(ef_hps* h, const double* a, const double* b) {
     if (!h || !a || !b) return fail(EF_ERR_INVALID, "null argument");
     if (!h->mixed) return fail(EF_ERR_STATE, "mixed solver not initialised");

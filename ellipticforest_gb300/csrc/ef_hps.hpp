@@ -198,6 +198,10 @@ public:
     // tcgen05 node GEMMs in the mixed solver for block solvers created afterwards: 0 off, 1 (default)
     // wherever the autotuner times them faster than the CUDA-core GEMMs, 2 wherever supported
     void set_tensor_cores(int mode) { tensor_cores_ = mode; }
+    // node-GEMM plan of the mixed block solvers, per node group the W, H, DOWN codes as
+    // MixedSolver::gemm_plan reports them (> 0 CUDA-core K split, 0 its heuristic, < 0 tensor-core
+    // K split): block solvers created afterwards use it instead of timing the candidates
+    void set_mx_plan(const std::vector<std::array<int, 3>>& codes);
     int tensor_cores() const { return tensor_cores_; }
     // FivePointStencil: per-leaf coefficients sampled at the reference's points (host arrays in leaf
     // order: alpha n*n, beta 4*n*n (W, E, S, N face of every cell), lambda n*n per leaf)
@@ -469,8 +473,10 @@ private:
         void** in64 = nullptr;
         void** out64 = nullptr;
     };
-    void residual(int B, double* rmax, bool zero_state);
-    void pass(int B, bool first);
+    // fused: the zero-state residual of 16 x 16 leaves together with the first pass's Neumann step
+    // (mx_leaf16_first); the pass then starts at the upward GEMMs
+    void residual(int B, double* rmax, bool zero_state, bool fused = false);
+    void pass(int B, bool first, bool neumann_done = false);
     // one node GEMM of a group (kind 0 W, 1 H, 2 DOWN): code > 0 the FP32 CUDA-core kernel with K
     // split `code` (0: its heuristic), code < 0 the tensor-core kernel with K split -code
     void node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code);

@@ -287,6 +287,10 @@ void mx_root_update(cudaStream_t st, int m, int B, const float* dg, double* g64)
 void mx_perm_identity(cudaStream_t st, int m, const int* perm, double* Z);
 // rmax[b] = max over leaves of rleaf[b][leaf]
 void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax);
+// 16 x 16 constant-coefficient leaves: the zero-state residual (as mx_leaf_residual with zero_state)
+// fused with the first pass's Neumann step (as mx_leaf32 LEAF_NEUMANN on its output)
+void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves, int L,
+                     int B, const double* f, float* q, float* rleaf, double* rmax);
 
 // Variable-coefficient (FivePointStencil) leaves of the mixed form (ef_mixed_fp.cu), indexed by leaf.
 struct MixFp {

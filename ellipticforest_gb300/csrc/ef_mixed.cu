@@ -862,60 +862,13 @@ __device__ __forceinline__ void mx_dst16_pair(const float (&X)[16], int i, float
 // Two transposes per item pass through a 16 x 17 shared buffer (conflict-free both ways) under
 // __syncwarp only: an item never leaves its half-warp.  NEUMANN writes h32 = DtN(0, q) from the
 // edges of u; SOLVE adds the solution of (g32, q) to the FP64 state u64 (or stores it when
-// accumulate is 0).
+// accumulate is 0).  Steps (2)-(6) on row t of the item's load in x (shared with the fused first
+// residual, k_mx_leaf16_first):
 template <int MODE>
-__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
-                                                   const MixLeaf* __restrict__ leaves, int L, int B,
-                                                   const float* __restrict__ q, double* __restrict__ u64,
-                                                   int accumulate) {
-    __shared__ float buf[16 * 272];
-    __shared__ float Vs[16 * 17];
-    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
-    const long long item = (long long)blockIdx.x * 16 + slot;
-    const bool act = item < (long long)L * B;
-    const int leaf = act ? int(item / B) : 0;
-    const int b = act ? int(item - (long long)leaf * B) : 0;
-    float* bf = buf + slot * 272;
-    if (MODE == LEAF_NEUMANN) {
-        // the full basis, for the edge sums whose basis row depends on the thread
-        const int i = tid >> 4, k = tid & 15;
-        const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
-        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
-        __syncthreads();
-    }
-    const int type = leaves[leaf].type;
-    float x[16], X[16];
-    // (1) row t of the load; the solve adds the Dirichlet terms -2 (cx g_x + cy g_y) of the edge cells
-    if (act) {
-        const float4* qr = reinterpret_cast<const float4*>(q + ((long long)b * L + leaf) * 256 + t * 16);
-#pragma unroll
-        for (int c4 = 0; c4 < 4; ++c4) {
-            const float4 v = qr[c4];
-            x[4 * c4] = v.x; x[4 * c4 + 1] = v.y; x[4 * c4 + 2] = v.z; x[4 * c4 + 3] = v.w;
-        }
-        if (MODE == LEAF_SOLVE) {
-            const float* g = leaves[leaf].g32 + b;
-            const float dx = types[type].dx, dy = types[type].dy;
-            const float cx = 1.0f / (dx * dx), cy = 1.0f / (dy * dy);
-            const float gs = g[(long long)(2 * 16 + t) * B], gn = g[(long long)(3 * 16 + t) * B];
-            if (t == 0 || t == 15) {
-                const long long side = t == 0 ? 0 : 16;
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float acc = cx * g[(side + j) * B];
-                    if (j == 0) acc += cy * gs;
-                    else if (j == 15) acc += cy * gn;
-                    x[j] += -2.0f * acc;
-                }
-            } else {
-                x[0] += -2.0f * (cy * gs);
-                x[15] += -2.0f * (cy * gn);
-            }
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) x[j] = 0.f;
-    }
+__device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const float* Vs, const LeafType32* __restrict__ types,
+                                               int type, const MixLeaf* __restrict__ leaves, int leaf, int b, int L, int B,
+                                               int t, bool act, double* __restrict__ u64, int accumulate) {
+    float X[16];
     // (2) A[t][l] = sum_j F[t][j] V[j][l]; transpose: this thread takes column l = t
     mx_dst16_fwd(x, [&](int l, float v) { bf[t * 17 + l] = v; });
     __syncwarp();
@@ -987,6 +940,143 @@ __global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(c
             h[(long long)(3 * 16 + t) * B] = -dtn_y * (e - o);
         }
     }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
+                                                   const MixLeaf* __restrict__ leaves, int L, int B,
+                                                   const float* __restrict__ q, double* __restrict__ u64,
+                                                   int accumulate) {
+    __shared__ float buf[16 * 272];
+    __shared__ float Vs[16 * 17];
+    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
+    const long long item = (long long)blockIdx.x * 16 + slot;
+    const bool act = item < (long long)L * B;
+    const int leaf = act ? int(item / B) : 0;
+    const int b = act ? int(item - (long long)leaf * B) : 0;
+    float* bf = buf + slot * 272;
+    if (MODE == LEAF_NEUMANN) {
+        // the full basis, for the edge sums whose basis row depends on the thread
+        const int i = tid >> 4, k = tid & 15;
+        const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
+        __syncthreads();
+    }
+    const int type = leaves[leaf].type;
+    float x[16];
+    // (1) row t of the load; the solve adds the Dirichlet terms -2 (cx g_x + cy g_y) of the edge cells
+    if (act) {
+        const float4* qr = reinterpret_cast<const float4*>(q + ((long long)b * L + leaf) * 256 + t * 16);
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4) {
+            const float4 v = qr[c4];
+            x[4 * c4] = v.x; x[4 * c4 + 1] = v.y; x[4 * c4 + 2] = v.z; x[4 * c4 + 3] = v.w;
+        }
+        if (MODE == LEAF_SOLVE) {
+            const float* g = leaves[leaf].g32 + b;
+            const float dx = types[type].dx, dy = types[type].dy;
+            const float cx = 1.0f / (dx * dx), cy = 1.0f / (dy * dy);
+            const float gs = g[(long long)(2 * 16 + t) * B], gn = g[(long long)(3 * 16 + t) * B];
+            if (t == 0 || t == 15) {
+                const long long side = t == 0 ? 0 : 16;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float acc = cx * g[(side + j) * B];
+                    if (j == 0) acc += cy * gs;
+                    else if (j == 15) acc += cy * gn;
+                    x[j] += -2.0f * acc;
+                }
+            } else {
+                x[0] += -2.0f * (cy * gs);
+                x[15] += -2.0f * (cy * gn);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) x[j] = 0.f;
+    }
+    mx_leaf16_body<MODE>(x, bf, Vs, types, type, leaves, leaf, b, L, B, t, act, u64, accumulate);
+}
+
+// The first residual of a block for 16 x 16 leaves fused with the first pass's Neumann step.  The
+// residual of the zero state (r = f - 2 cx g_x - 2 cy g_y at the edge cells, the arithmetic of
+// k_mx_leaf_residual0_16 bit for bit: f read as coalesced 16-byte pairs, FP64 -> FP32 by integer
+// bit operations, the ghost terms through shared memory) is stored as the pass's load q for its
+// solve step and handed to the leaf pass body through the transpose buffer instead of memory; the
+// edge fluxes of the zero state (FP64) and the items' largest |r| are written as by the residual
+// kernel.
+__global__ void __launch_bounds__(256, 3) k_mx_leaf16_first(const LeafType32* __restrict__ types,
+                                                            const MixCoef* __restrict__ coefs,
+                                                            const MixLeaf* __restrict__ leaves, int L, int B,
+                                                            const double* __restrict__ f, float* __restrict__ q,
+                                                            float* __restrict__ rleaf) {
+    __shared__ float buf[16 * 272];
+    __shared__ float Vs[16 * 17];
+    __shared__ float gts[16 * 64];
+    const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
+    const long long item = (long long)blockIdx.x * 16 + slot;
+    const bool act = item < (long long)L * B;
+    const int leaf = act ? int(item / B) : 0;
+    const int b = act ? int(item - (long long)leaf * B) : 0;
+    float* bf = buf + slot * 272;
+    {
+        // the full basis, for the edge sums whose basis row depends on the thread
+        const int i = tid >> 4, k = tid & 15;
+        const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
+        __syncthreads();
+    }
+    const MixLeaf lf = leaves[leaf];
+    const MixCoef cf = coefs[lf.type];
+    const long long base = ((long long)b * L + leaf) * 256;
+    const double2* f2 = reinterpret_cast<const double2*>(f + base);
+    double2 fv[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) fv[m] = act ? f2[t + 16 * m] : make_double2(0.0, 0.0);
+    double gv[4];
+#pragma unroll
+    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
+    float* gt = gts + slot * 64;
+#pragma unroll
+    for (int side = 0; side < 4; ++side)
+        gt[side * 16 + t] = -2.0f * (side < 2 ? cf.cx32 : cf.cy32) * d2f_rn_bits(gv[side]);
+    if (act) {
+        // edge fluxes of the zero state, h = -+(2/d) g
+        double* h = lf.h64 + b;
+        h[(long long)(0 * 16 + t) * B] = -cf.dtn_x * gv[0];
+        h[(long long)(1 * 16 + t) * B] = cf.dtn_x * gv[1];
+        h[(long long)(2 * 16 + t) * B] = -cf.dtn_y * gv[2];
+        h[(long long)(3 * 16 + t) * B] = cf.dtn_y * gv[3];
+    }
+    __syncwarp();
+    float mx = 0.f;
+    float2* q2 = reinterpret_cast<float2*>(q + base);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        const int e2 = t + 16 * m, i = e2 >> 3, j = (e2 & 7) * 2;
+        float r0 = d2f_rn_bits(fv[m].x), r1 = d2f_rn_bits(fv[m].y);
+        if (i == 0) {
+            r0 += gt[j];
+            r1 += gt[j + 1];
+        } else if (i == 15) {
+            r0 += gt[16 + j];
+            r1 += gt[16 + j + 1];
+        }
+        if (j == 0) r0 += gt[32 + i];
+        if (j == 14) r1 += gt[48 + i];
+        mx = fmaxf(mx, fmaxf(fabsf(r0), fabsf(r1)));
+        if (act) q2[e2] = make_float2(r0, r1);
+        bf[i * 17 + j] = act ? r0 : 0.f;
+        bf[i * 17 + j + 1] = act ? r1 : 0.f;
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (rleaf && act && t == 0) rleaf[(long long)b * L + leaf] = mx;
+    __syncwarp();
+    float x[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) x[j] = bf[t * 17 + j];
+    mx_leaf16_body<LEAF_NEUMANN>(x, bf, Vs, types, lf.type, leaves, leaf, b, L, B, t, act, nullptr, 0);
 }
 
 // Leaf residual r = f - (cx (u_W + u_E) + cy (u_S + u_N) + cc u_C) (stored as the next pass's FP32
@@ -1985,6 +2075,15 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
     } else {
         mx_residual_launch<1>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
     }
+    ++g_kernel_launches;
+    if (rmax) mx_rmax(st, rleaf, L, B, rmax);
+}
+
+void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves, int L,
+                     int B, const double* f, float* q, float* rleaf, double* rmax) {
+    const long long items = (long long)L * B;
+    k_mx_leaf16_first<<<unsigned((items + 15) / 16), 256, 0, st>>>(types, coefs, leaves, L, B, f, q,
+                                                                   rmax ? rleaf : nullptr);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }

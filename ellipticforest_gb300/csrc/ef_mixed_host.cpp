@@ -453,6 +453,24 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
     if (hps.mx_split_.size() != groups_.size() || hps.mx_split_tc_ != hps.tensor_cores()) tune();
 }
 
+void Hps::set_mx_plan(const std::vector<std::array<int, 3>>& codes) {
+    if (codes.size() != groups_.size())
+        throw std::invalid_argument("gemm plan: one row per node group (" + std::to_string(groups_.size()) + ")");
+    static const char* kinds[3] = {"W", "H", "DOWN"};
+    for (size_t gi = 0; gi < codes.size(); ++gi)
+        for (int kind = 0; kind < 3; ++kind) {
+            const int c = codes[gi][kind], s = groups_[gi].s;
+            if (c < -8 || c > 8) throw std::invalid_argument("gemm plan: codes lie in [-8, 8]");
+            if (c >= 0) continue;
+            const int k = -c;
+            if (tensor_cores_ == 0 || !mx_tc_supported(kind, s) || (k & (k - 1)) != 0 || k > mx_tc_max_split(kind, s))
+                throw std::invalid_argument(std::string("gemm plan: no tensor-core ") + kinds[kind] + " GEMM with K split " +
+                                            std::to_string(k) + " at s = " + std::to_string(s));
+        }
+    mx_split_ = codes;
+    mx_split_tc_ = tensor_cores_;
+}
+
 void MixedSolver::tune() {
     // per group and kind, the fastest of the CUDA-core GEMM (K split 1, 2, 4, ...: code > 0) and the
     // tensor-core GEMM (code < 0: split -code), timed with CUDA events on a block of min(bmax, 32)
@@ -618,7 +636,7 @@ void MixedSolver::set_root_operator(const double* a, const double* b) {
     robin_ = true;
 }
 
-void MixedSolver::residual(int B, double* rmax, bool zero_state) {
+void MixedSolver::residual(int B, double* rmax, bool zero_state, bool fused) {
     Hps& h = H_;
     cudaStream_t st = st_;
     const int maxL = h.mesh().max_level;
@@ -635,14 +653,22 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
         }
         h.pe(0, 0, st);
     }
-    h.pb("mx_leaf_residual", st);
-    if (d_fps_)
-        mx_fp_residual(st, d_fps_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
-                       rleaf_, rmax);
-    else
-        mx_leaf_residual(st, d_coef_, res_form_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
-                         rleaf_, rmax);
-    h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
+    if (fused) {
+        // f read once for the zero-state residual and the first pass's Neumann step
+        const double items = L * B;
+        h.pb("mx_leaf_first", st);
+        mx_leaf16_first(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, q32_, rleaf_, rmax);
+        h.pe(items * (nn * 12.0 + 4 * 16 * 20.0), items * 2.0 * (3 * nn * 16 + 4 * nn), st);
+    } else {
+        h.pb("mx_leaf_residual", st);
+        if (d_fps_)
+            mx_fp_residual(st, d_fps_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_, u64_, q32_,
+                           rleaf_, rmax);
+        else
+            mx_leaf_residual(st, d_coef_, res_form_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_,
+                             u64_, q32_, rleaf_, rmax);
+        h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
+    }
     h.pb("mx_interface", st);
     if (direct_) {
         mx_mismatch(st, arena_, d_mis_, nmis_, B);
@@ -660,16 +686,18 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state) {
     h.pe(0, 0, st);
 }
 
-void MixedSolver::pass(int B, bool first) {
+void MixedSolver::pass(int B, bool first, bool neumann_done) {
     Hps& h = H_;
     cudaStream_t st = st_;
     const int maxL = h.mesh().max_level;
     const int L = h.num_leaves(), n = h.leaf_n();
     const double items = double(L) * B, nn = double(n) * n;
-    h.pb("mx_leaf_neumann", st);
-    if (d_fps_) mx_fp_leaf32(st, LEAF_NEUMANN, d_fps_, d_leaves_, L, B, n, q32_, nullptr, 0);
-    else mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr, 0);
-    h.pe(items * (nn * 4 + 4 * n * 4), items * 2.0 * (3 * nn * n + 4 * nn), st);
+    if (!neumann_done) {
+        h.pb("mx_leaf_neumann", st);
+        if (d_fps_) mx_fp_leaf32(st, LEAF_NEUMANN, d_fps_, d_leaves_, L, B, n, q32_, nullptr, 0);
+        else mx_leaf32(st, LEAF_NEUMANN, d_types32_, d_leaves_, L, B, n, q32_, nullptr, 0);
+        h.pe(items * (nn * 4 + 4 * n * 4), items * 2.0 * (3 * nn * n + 4 * nn), st);
+    }
     for (int lvl = maxL - 1; lvl >= 0; --lvl) {
         h.pb("mx_interface", st);
         for (auto& s : hsteps_)
@@ -733,9 +761,12 @@ void MixedSolver::solve(int B, int sweeps) {
         ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, s), "clear residuals");
         if (robin_) ck(cudaMemsetAsync(mn_[0].g64, 0, sizeof(double) * 4 * size_t(h.root_M()) * B, s), "root g64");
         else mx_root(s, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
+        // 16 x 16 constant-coefficient leaves fuse the first residual with the first Neumann step
+        // (the general-leaf-residual option keeps them apart: the same bits)
+        const bool fuse = !d_fps_ && h.leaf_n() == 16 && !g_general_residual.load();
         for (int p = 0; p <= sweeps; ++p) {
-            residual(B, rmax_ + size_t(p) * bmax_, p == 0);
-            pass(B, p == 0);
+            residual(B, rmax_ + size_t(p) * bmax_, p == 0, fuse && p == 0);
+            pass(B, p == 0, fuse && p == 0);
         }
     });
 }

@@ -651,6 +651,13 @@ class HPSAlgorithm:
         check(_lib.load().ef_hps_mixed_gemm_plan(self._h, n.value, t, C.byref(n)))
         return [tuple(t[5 * i:5 * i + 5]) for i in range(n.value)]
 
+    def mixed_set_gemm_plan(self, plan):
+        """Use `plan` (rows (level, s, W, H, DOWN) as mixed_gemm_plan returns them, or rows of the
+        three codes) for the block solvers created afterwards instead of timing the candidates."""
+        rows = [tuple(r)[-3:] for r in plan]
+        codes = (C.c_int * (3 * len(rows)))(*[int(c) for r in rows for c in r])
+        check(_lib.load().ef_hps_mixed_set_gemm_plan(self._h, codes, len(rows)))
+
     def mixed_set_root(self, a, b):
         """Fixed root operator a u + b du/dn = r of the block solver (r per request); b = 0 returns
         to per-request Dirichlet data (no reference counterpart: the reference solves one request)."""

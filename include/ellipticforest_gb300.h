@@ -173,6 +173,12 @@ int ef_hps_mixed_init(ef_hps* hps, int bmax);
  * that K split, < 0 = tcgen05 tensor-core kernel with K split -code.  table: 5 * max_groups ints (or
  * NULL to query the count in *ngroups). */
 int ef_hps_mixed_gemm_plan(ef_hps* h, int max_groups, int* table, int* ngroups);
+/* No counterpart in the reference.  Sets the node-GEMM plan instead of timing it: codes[3 * i + k]
+ * for node group i (the row order of ef_hps_mixed_gemm_plan) and kind k (W, H, DOWN), > 0 the
+ * CUDA-core kernel with that K split, 0 its own choice, < 0 the tensor-core kernel with K split
+ * -code (needs "tensor-cores" 1 or 2 and a shape it supports).  Block solvers created afterwards
+ * (ef_hps_mixed_init) use it.  EF_ERR_INVALID for a wrong group count or an unsupported code. */
+int ef_hps_mixed_set_gemm_plan(ef_hps* h, const int* codes, int ngroups);
 
 int ef_hps_mixed_set_root(ef_hps* h, const double* a, const double* b);
 /* Resident buffers: f [B][num_leaves*n*n], a and r [B][4M] (root data, a u = r), u [B][...]. */

@@ -249,8 +249,9 @@ def _set_general_residual(hps, on):
 ])
 def test_residual_kernel_16_bit_identical_to_general_kernel(ef, kind, dom, lam, zero_f, B):
     """16 x 16 leaves take the exact residual through their own kernel (column, then row ownership
-    of the item's fixed-point tile); the general leaf-size kernel computes the same integers, so
-    the two give bit-identical solutions and residual histories."""
+    of the item's fixed-point tile) and the first residual fused with the first Neumann step; the
+    general leaf-size kernels, run apart, compute the same numbers, so the two give bit-identical
+    solutions and residual histories."""
     n = 16
     root = ef.FiniteVolumePatch(ef.FiniteVolumeGrid(n, dom[0], dom[1], n, dom[2], dom[3]))
     if kind[0] == "uniform":
@@ -301,6 +302,31 @@ def test_interface_rows_in_place_bit_identical_to_per_level(ef, L, n, B, robin):
         check(load().ef_hps_set_option(hps.handle, b"per-level-interface", 0))
     for u0, u1 in zip(got[0], got[1]):
         assert np.array_equal(u0, u1)
+
+
+def test_gemm_plan_set_instead_of_timed(ef):
+    """A node-GEMM plan set through the API replaces the timing: the block solver reports it, solves
+    to the FP64 solution with it, and codes the tree cannot run are refused."""
+    from ellipticforest_gb300._lib import EFError
+    mesh, hps = make(ef, ("uniform", 4), 16, (-1.0, 1.0, -1.0, 1.0))
+    F, A, R = requests(hps, mesh, 4, 81)
+    ref = fp64_solutions(hps, F, A, R)
+    hps.mixed_init(4)
+    tuned = hps.mixed_gemm_plan()
+    # every group on the CUDA-core kernel with K split 1, except the tensor-core DOWN at s >= 32
+    plan = [(lv, s, 1, 1, -1 if s >= 32 else 2) for (lv, s, *_rest) in tuned]
+    hps.mixed_set_gemm_plan(plan)
+    hps.mixed_init(4)
+    assert hps.mixed_gemm_plan() == plan
+    u = hps.mixed_solve(F, A, R, sweeps=1)
+    for k in range(4):
+        assert np.abs(u[k] - ref[k]).max() <= TOL * np.abs(ref[k]).max(), k
+    with pytest.raises(EFError):
+        hps.mixed_set_gemm_plan(plan[:-1])                       # one row per group
+    with pytest.raises(EFError):
+        hps.mixed_set_gemm_plan([(lv, s, 1, 1, -16) for (lv, s, *_r) in plan])   # K split too large
+    with pytest.raises(EFError):
+        hps.mixed_set_gemm_plan([(lv, s, -1, -1, -1) for (lv, s, *_r) in plan])  # H at s = 16
 
 
 def _set_tc(hps, on):
