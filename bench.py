@@ -265,12 +265,13 @@ def measure_fp64_peak(torch):
     return 2 * 4096 ** 3 / best / 1e12
 
 
-# DRAM bytes per launch / algorithmic bytes per launch of the solve kernels, from one ncu capture
-# of the same kernels on the uniform L6 tree (the k_gemv_down summary under profiles/); L7 launches
-# stream 4x the bytes of L6 launches with the same access pattern.
-# The mixed step's residual section runs the first residual (12 B per cell-request, DRAM 1.25x) and
-# the exact residual (20 B, DRAM 1.17x) once each per sweep (same L6 capture): 1.20x of its bytes.
-TRAFFIC_RATIO = {"downward": 1.005, "mx_leaf_residual": (1.25 * 12 + 1.17 * 20) / 32}
+# DRAM bytes per launch / algorithmic bytes per launch of the solve kernels, from ncu captures of
+# the same kernels on the uniform L6 tree (launches of 33.5 M cell-requests, far above L2); L7
+# launches stream 4x the bytes of L6 launches with the same access pattern.
+# Below 1 where part of a launch's inputs are still in L2 from the launch before it.
+TRAFFIC_RATIO = {"downward": 1.005, "mx_leaf_residual": 0.934, "mx_leaf_solve": 0.90, "mx_leaf_first": 0.88}
+# sections that launch one kernel (with at most a small reduction): the roofline's candidates
+SINGLE_KERNEL = ("mx_leaf_first", "mx_leaf_residual", "mx_leaf_neumann", "mx_leaf_solve")
 
 
 def load_peaks():
@@ -489,7 +490,9 @@ def run_gb300(args):
     hps.profile_enable(False)
     ksteps = max(2, K // 4)
     tot_ms = sum(v["ms"] for v in prof.values())
-    dom_name = max(prof, key=lambda k: prof[k]["ms"])
+    # the dominant kernel: the node-GEMM sections run several kernels (CUDA-core and tensor-core,
+    # one launch per level); they are reported apart below
+    dom_name = max((k for k in prof if k in SINGLE_KERNEL), key=lambda k: prof[k]["ms"])
     d = prof[dom_name]
     hbm_peak, peak_kind = load_peaks()
     achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
@@ -563,13 +566,18 @@ def run_gb300(args):
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak,
                          "traffic": (TRAFFIC_RATIO[dom_name] * d["bytes"] / max(d["calls"], 1)
-                                     if dom_name in TRAFFIC_RATIO else None),
-                         "traffic_unit": "DRAM bytes per section call (its main kernel and its small "
-                                         "reduction launches), scaled from the L6 ncu capture",
+                                     if TRAFFIC_RATIO.get(dom_name) else None),
+                         "traffic_unit": "DRAM bytes per section call (its kernel launches of one step), "
+                                         "the L6 ncu ratio of DRAM to algorithmic bytes applied to the L7 bytes",
                          "algorithmic_bytes_per_call": d["bytes"] / max(d["calls"], 1),
                          "launches_per_call": d["launches"] / max(d["calls"], 1),
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "share_of_step": d["ms"] / tot_ms},
+            "node_gemm_sections": {k: {"ms_per_step": prof[k]["ms"] / ksteps,
+                                       "achieved_gbs": prof[k]["bytes"] / (prof[k]["ms"] / 1e3) / 1e9,
+                                       "frac_of_hbm": prof[k]["bytes"] / (prof[k]["ms"] / 1e3) / 1e9 / hbm_peak,
+                                       "launches_per_step": prof[k]["launches"] / ksteps}
+                                   for k in ("mx_gemm_w", "mx_gemm_h", "mx_gemm_down") if k in prof},
             "fp64": {"build_tflops": build_flops / build_s / 1e12, "build_flops": build_flops,
                      "dgemm_peak_tflops_measured": fp64_peak,
                      "build_frac_of_dgemm": build_flops / build_s / 1e12 / fp64_peak},

@@ -480,6 +480,7 @@ private:
     // one node GEMM of a group (kind 0 W, 1 H, 2 DOWN): code > 0 the FP32 CUDA-core kernel with K
     // split `code` (0: its heuristic), code < 0 the tensor-core kernel with K split -code
     void node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code);
+    double gemm_bytes(const MGroup& g, int kind, int B, int code) const;
     // times the K-split candidates of every node GEMM (CUDA events, block of min(bmax, 32)) and keeps
     // the fastest per group and kind in the tree
     void tune();

@@ -533,6 +533,19 @@ void MixedSolver::tune() {
     h.mx_split_tc_ = h.tensor_cores();
 }
 
+// Bytes a node GEMM launch moves at the least: the operator (FP32, or the three bf16 planes of the
+// tensor-core form), the right-hand side block and what the epilogue reads and writes per node --
+// W: hd in, w out; H: w in, hc in, h out; DOWN: gf in, w in, both children's interface rows out,
+// the FP64 interface state read and written, the exterior rows copied to the children.
+double MixedSolver::gemm_bytes(const MGroup& g, int kind, int B, int code) const {
+    const double c = g.cnt, s = g.s, eb = (g.tc[kind] && code < 0) ? 6.0 : 4.0;
+    const double op = (kind == 2 ? 32.0 : 16.0) * s * s * eb;
+    // per request: W 4s in + 4s out (FP32); H 8s + 8s in, 8s out; DOWN 8s + 4s in, 2 x 4s out, 4s
+    // FP64 read and written, 8s copied
+    const double vec = kind == 0 ? 32.0 * s : kind == 1 ? 96.0 * s : (32.0 + 16.0 + 32.0 + 64.0 + 64.0) * s;
+    return c * (op + vec * B);
+}
+
 void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code) {
     if (g.tc[kind] && code < 0) {
         const CUtensorMap& tm = kind == 0 ? g.tmXi3 : (kind == 1 ? g.tmH3 : g.tmS3);
@@ -667,7 +680,8 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state, bool fused) {
         else
             mx_leaf_residual(st, d_coef_, res_form_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_,
                              u64_, q32_, rleaf_, rmax);
-        h.pe(L * B * nn * (zero_state ? 12.0 : 20.0), zero_state ? 0.0 : L * B * nn * 6.0, st);
+        // f and the state in, r out; per item the 4n Dirichlet values in, the 4n edge fluxes out (FP64)
+        h.pe(L * B * (nn * (zero_state ? 12.0 : 20.0) + 4.0 * h.leaf_n() * 16), zero_state ? 0.0 : L * B * nn * 6.0, st);
     }
     h.pb("mx_interface", st);
     if (direct_) {
@@ -712,10 +726,10 @@ void MixedSolver::pass(int B, bool first, bool neumann_done) {
             const std::array<int, 3> ks = h.mx_split_.empty() ? std::array<int, 3>{0, 0, 0} : h.mx_split_[gi];
             h.pb("mx_gemm_w", st);
             node_gemm(st, g, 0, B, ks[0]);
-            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
+            h.pe(gemm_bytes(g, 0, B, ks[0]), c * 2.0 * 16 * s2 * B, st);
             h.pb("mx_gemm_h", st);
             node_gemm(st, g, 1, B, ks[1]);
-            h.pe(c * 16 * s2 * 4, c * 2.0 * 16 * s2 * B, st);
+            h.pe(gemm_bytes(g, 1, B, ks[1]), c * 2.0 * 16 * s2 * B, st);
         }
     }
     const int mroot = 4 * h.root_M();
@@ -740,15 +754,17 @@ void MixedSolver::pass(int B, bool first, bool neumann_done) {
             const MGroup& g = groups_[gi];
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
+            const int code = h.mx_split_.empty() ? 0 : h.mx_split_[gi][2];
             h.pb("mx_gemm_down", st);
-            node_gemm(st, g, 2, B, h.mx_split_.empty() ? 0 : h.mx_split_[gi][2]);
-            h.pe(c * 32 * s2 * 4, c * 2.0 * 32 * s2 * B, st);
+            node_gemm(st, g, 2, B, code);
+            h.pe(gemm_bytes(g, 2, B, code), c * 2.0 * 32 * s2 * B, st);
         }
     }
     h.pb("mx_leaf_solve", st);
     if (d_fps_) mx_fp_leaf32(st, LEAF_SOLVE, d_fps_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
     else mx_leaf32(st, LEAF_SOLVE, d_types32_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);
-    h.pe(items * nn * (4 + 16), items * 2.0 * 4 * nn * n, st);
+    // q in, the FP64 state written (and read when accumulating), the Dirichlet rows in
+    h.pe(items * (nn * (first ? 12.0 : 20.0) + 4.0 * n * 4), items * 2.0 * 4 * nn * n, st);
 }
 
 void MixedSolver::solve(int B, int sweeps) {
