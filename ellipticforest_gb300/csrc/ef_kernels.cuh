@@ -291,6 +291,10 @@ void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax);
 // fused with the first pass's Neumann step (as mx_leaf32 LEAF_NEUMANN on its output)
 void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves, int L,
                      int B, const double* f, float* q, float* rleaf, double* rmax);
+// 16 x 16 leaves of residual form 0: the exact residual (as mx_leaf_residual) fused with the next
+// pass's Neumann step
+void mx_leaf16_residual_neumann(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves,
+                                int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
 
 // Variable-coefficient (FivePointStencil) leaves of the mixed form (ef_mixed_fp.cu), indexed by leaf.
 struct MixFp {

@@ -1842,16 +1842,30 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __r
 //    that layout;
 //  - the item's largest exponents and bit lengths reduce over its 16 lanes by shuffles.
 // The tile's rows are 18 words apart (144 B), so the row reads (16-byte vectors) and the column
-// writes (8-byte) are both free of bank conflicts.  f is loaded in the row layout (16-byte vectors).
-// FORM 0 keeps the cells' second differences in registers between the bit-length sweep and the
-// products; FORM 1 (two differences and the lambda term) recomputes them from the tile.
-template <int FORM>
+// writes (8-byte) are both free of bank conflicts.  FORM 0 keeps the cells' second differences in
+// registers between the bit-length sweep and the products and loads f by columns (coalesced),
+// handing it to the row owners through the tile; FORM 1 (two differences and the lambda term)
+// recomputes them from the tile and loads f by rows (16-byte vectors).
+// NEU (FORM 0): the residual then feeds the next pass's Neumann step from registers (the leaf pass
+// body on row t of r, the tile reused as its transpose buffer) -- q is still stored for the pass's
+// solve step.
+template <int FORM, bool NEU>
 __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict__ coefs,
                                                        const MixLeaf* __restrict__ leaves, int L, int B,
                                                        const double* __restrict__ f, const double* __restrict__ u64,
-                                                       float* __restrict__ q, float* __restrict__ rleaf) {
+                                                       float* __restrict__ q, float* __restrict__ rleaf,
+                                                       const LeafType32* __restrict__ types) {
+    static_assert(!NEU || FORM == 0, "the Neumann step is fused with the FORM 0 residual only");
     constexpr int RS = 18, TS = 18 * RS;
     __shared__ __align__(16) long long tiles[16 * TS];
+    __shared__ float Vs[NEU ? 16 * 17 : 1];
+    if constexpr (NEU) {
+        // the full basis, for the Neumann step's edge sums
+        const int i = threadIdx.x >> 4, k = threadIdx.x & 15;
+        const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
+        __syncthreads();
+    }
     const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
     const long long item = (long long)blockIdx.x * 16 + slot;
     const bool act = item < (long long)L * B;
@@ -1977,6 +1991,7 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     const float pa = __uint_as_float(unsigned(127 + sa) << 23), pb = __uint_as_float(unsigned(127 + sb) << 23);
     float mx = 0.f;
     float4* q4 = reinterpret_cast<float4*>(q + base + t * 16);
+    float xr[NEU ? 16 : 1];  // NEU: row t of r
     // r of cells 2m, 2m+1 of the row
     auto finish = [&](const long long (&c)[2], const long long (&sx)[2], const long long (&sy)[2], double2 fv,
                       float& r0, float& r1) {
@@ -2008,6 +2023,12 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
             finish(c0, sx0, c0, frow[2 * m2], r4.x, r4.y);
             finish(c0, sx1, c0, frow[2 * m2 + 1], r4.z, r4.w);
             if (act) q4[m2] = r4;
+            if (NEU) {
+                xr[4 * m2] = r4.x;
+                xr[4 * m2 + 1] = r4.y;
+                xr[4 * m2 + 2] = r4.z;
+                xr[4 * m2 + 3] = r4.w;
+            }
         }
     } else {
         // the second differences again from the tile, f again from memory (cached): the fully
@@ -2029,6 +2050,11 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (rleaf && act && t == 0) rleaf[(long long)b * L + leaf] = mx;
+    if constexpr (NEU) {
+        __syncwarp();  // every lane has read its row of f from the tile
+        mx_leaf16_body<LEAF_NEUMANN>(xr, reinterpret_cast<float*>(tl), Vs, types, lf.type, leaves, leaf, b, L, B, t,
+                                     act, nullptr, 0);
+    }
 }
 
 template <int FORM>
@@ -2068,8 +2094,8 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
     }
     if (n == 16 && !g_general_residual.load()) {
         const unsigned grid16 = unsigned((items + 15) / 16);
-        if (form == 0) k_mx_resid16<0><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl);
-        else k_mx_resid16<1><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl);
+        if (form == 0) k_mx_resid16<0, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr);
+        else k_mx_resid16<1, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr);
     } else if (form == 0) {
         mx_residual_launch<0>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
     } else {
@@ -2084,6 +2110,15 @@ void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* co
     const long long items = (long long)L * B;
     k_mx_leaf16_first<<<unsigned((items + 15) / 16), 256, 0, st>>>(types, coefs, leaves, L, B, f, q,
                                                                    rmax ? rleaf : nullptr);
+    ++g_kernel_launches;
+    if (rmax) mx_rmax(st, rleaf, L, B, rmax);
+}
+
+void mx_leaf16_residual_neumann(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves,
+                                int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax) {
+    const long long items = (long long)L * B;
+    k_mx_resid16<0, true><<<unsigned((items + 15) / 16), 256, 0, st>>>(coefs, leaves, L, B, f, u64, q,
+                                                                       rmax ? rleaf : nullptr, types);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }

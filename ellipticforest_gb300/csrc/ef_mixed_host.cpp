@@ -666,12 +666,18 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state, bool fused) {
         }
         h.pe(0, 0, st);
     }
-    if (fused) {
+    if (fused && zero_state) {
         // f read once for the zero-state residual and the first pass's Neumann step
         const double items = L * B;
         h.pb("mx_leaf_first", st);
         mx_leaf16_first(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, q32_, rleaf_, rmax);
         h.pe(items * (nn * 12.0 + 4 * 16 * 20.0), items * 2.0 * (3 * nn * 16 + 4 * nn), st);
+    } else if (fused) {
+        // the exact residual and the next pass's Neumann step from registers
+        const double items = L * B;
+        h.pb("mx_leaf_residual", st);
+        mx_leaf16_residual_neumann(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, u64_, q32_, rleaf_, rmax);
+        h.pe(items * (nn * 20.0 + 4 * 16 * 20.0), items * (nn * 6.0 + 2.0 * (3 * nn * 16 + 4 * nn)), st);
     } else {
         h.pb("mx_leaf_residual", st);
         if (d_fps_)
@@ -777,12 +783,14 @@ void MixedSolver::solve(int B, int sweeps) {
         ck(cudaMemsetAsync(rmax_, 0, sizeof(double) * size_t(bmax_) * kMaxPasses, s), "clear residuals");
         if (robin_) ck(cudaMemsetAsync(mn_[0].g64, 0, sizeof(double) * 4 * size_t(h.root_M()) * B, s), "root g64");
         else mx_root(s, 4 * h.root_M(), B, a_, r_, mn_[0].g64);
-        // 16 x 16 constant-coefficient leaves fuse the first residual with the first Neumann step
-        // (the general-leaf-residual option keeps them apart: the same bits)
+        // 16 x 16 constant-coefficient leaves fuse each residual with the next Neumann step (the
+        // exact residual in its form 0: square cells, lambda = 0); the general-leaf-residual option
+        // keeps them apart, with the same bits
         const bool fuse = !d_fps_ && h.leaf_n() == 16 && !g_general_residual.load();
         for (int p = 0; p <= sweeps; ++p) {
-            residual(B, rmax_ + size_t(p) * bmax_, p == 0, fuse && p == 0);
-            pass(B, p == 0, fuse && p == 0);
+            const bool f = fuse && (p == 0 || res_form_ == 0);
+            residual(B, rmax_ + size_t(p) * bmax_, p == 0, f);
+            pass(B, p == 0, f);
         }
     });
 }
