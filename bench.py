@@ -1039,7 +1039,10 @@ def run_profile_only(args):
     hps.setupStage()
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("build")  # ncu --nvtx --nvtx-include "build/"
-    hps.buildStage()
+    if args.profile_only == "mbuild":
+        hps.buildStageMixed(3)
+    else:
+        hps.buildStage()
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     out = {"profile_only": args.profile_only, "level": args.level, "build_merge_launches": hps.build_info()[0]}
@@ -1093,9 +1096,10 @@ def main():
                     help="node GEMMs of the mixed form: 0 CUDA cores, 1 the faster per level (tuned), 2 tcgen05 wherever supported")
     ap.add_argument("--gemm-plan", default=None,
                     help="--profile-only mixed: JSON node-GEMM plan (rows level, s, W, H, DOWN) instead of timing one")
-    ap.add_argument("--profile-only", choices=["build", "mixed"], default=None,
+    ap.add_argument("--profile-only", choices=["build", "mbuild", "mixed"], default=None,
                     help="short run for a profiler's launch list: 'build' = set-up and one FP64 build of the "
-                         "tree; 'mixed' = build, block-solver set-up and --steps mixed blocks (no timing line)")
+                         "tree; 'mbuild' = the mixed build (FP64 LU on the top 3 levels); 'mixed' = build, "
+                         "block-solver set-up and --steps mixed blocks (no timing line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
