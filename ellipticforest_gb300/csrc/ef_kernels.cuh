@@ -254,6 +254,8 @@ void mx_tc_set_inject_timeout(int on);
 void mx_gemm_tc(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
                 int* err, int ksplit);
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
+// the pass's exterior rows of every node of a group to its children (gf -> gc)
+void mx_ext32(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 void mx_coarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);
 void mx_uncoarsen(cudaStream_t st, bool fp64, const void* const* in, void* const* out, int count, int nf, int B);

@@ -209,44 +209,6 @@ __global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __g
     auto epilogue = [&](int tile) {
         const MxTile t = mx_tile<KIND>(items, s, B, rt, tpi, tile);
         const MixItem& it = items[t.item];
-        if (KIND == MX_DOWN && blockIdx.y == 0) {
-            // exterior points of the parent go to the children unchanged; each tile copies its share
-            // of the 8s exterior rows, one warp per row (float4 along the batch when B % 4 == 0)
-            const int rows = 8 * s, per = (rows + tpi - 1) / tpi;
-            const int p0 = t.tl * per, p1 = min(rows, p0 + per);
-            if (vecx) {
-                // (row, float4) pairs over all threads, four loads in flight before their stores
-                const int w4 = B >> 2, tot = (p1 - p0) * w4;
-                for (int e0 = tid; e0 < tot; e0 += 4 * nt) {
-                    float4 v[4];
-                    float4* d[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int e = e0 + u * nt;
-                        d[u] = nullptr;
-                        if (e < tot) {
-                            const int p = p0 + e / w4, b4 = e - (e / w4) * w4;
-                            int c, q;
-                            mx_ext_map(p, s, c, q);
-                            v[u] = reinterpret_cast<const float4*>(it.gf + (long long)p * B)[b4];
-                            d[u] = reinterpret_cast<float4*>(it.gc[c] + (long long)q * B) + b4;
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (d[u]) *d[u] = v[u];
-                }
-            } else {
-                const int warp = tid >> 5, lane = tid & 31, nw = (nt + 31) >> 5;
-                for (int p = p0 + warp; p < p1; p += nw) {
-                    int c, q;
-                    mx_ext_map(p, s, c, q);
-                    const float* src = it.gf + (long long)p * B;
-                    float* dst = it.gc[c] + (long long)q * B;
-                    for (int bb = lane; bb < B; bb += 32) dst[bb] = src[bb];
-                }
-            }
-        }
         const int bq = b0 + 4 * tx;
         // the rows' epilogue operands (h_ext for H; w and u_Gamma for DOWN) are all loaded before
         // any store: the compiler cannot move a load above a store to another array of the item
@@ -556,6 +518,39 @@ __global__ void k_mx_gather_rows64(const char* __restrict__ arena, const MxRow* 
          e += (long long)gridDim.x * blockDim.x) {
         const int r = int(e / B), b = int(e - (long long)r * B);
         dst[e] = mx_row<const double>(arena, src[r], B)[b];
+    }
+}
+
+// Exterior points of a parent go to its children unchanged (the pass's FP32 Dirichlet data): rows p
+// of gf, p < 8s, to row q of child c.  Its own launch per level, ahead of the level's DOWN GEMM,
+// whose epilogue writes the children's interface rows.
+__global__ void k_mx_ext32(const MixItem* __restrict__ items, int s, int B) {
+    const MixItem& it = items[blockIdx.y];
+    const int m8 = 8 * s;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m8 * B; e += gridDim.x * blockDim.x) {
+        const int p = e / B, b = e - (e / B) * B;
+        int c, q;
+        mx_ext_map(p, s, c, q);
+        it.gc[c][(long long)q * B + b] = it.gf[e];
+    }
+}
+// the same with four requests per thread (B % 4 == 0), two rows' loads ahead of their stores
+__global__ void k_mx_ext32_4(const MixItem* __restrict__ items, int s, int B) {
+    const MixItem& it = items[blockIdx.y];
+    const int m8 = 8 * s, B4 = B >> 2, tot = m8 * B4;
+    const int stride = gridDim.x * blockDim.x;
+    for (int e4 = blockIdx.x * blockDim.x + threadIdx.x; e4 < tot; e4 += 2 * stride) {
+        const int e4b = e4 + stride;
+        const int r0 = e4 / B4, r1 = e4b / B4;
+        const float4 v0 = reinterpret_cast<const float4*>(it.gf)[e4];
+        const float4 v1 = e4b < tot ? reinterpret_cast<const float4*>(it.gf)[e4b] : v0;
+        int c, q;
+        mx_ext_map(r0, s, c, q);
+        reinterpret_cast<float4*>(it.gc[c] + (long long)q * B)[e4 - r0 * B4] = v0;
+        if (e4b < tot) {
+            mx_ext_map(r1, s, c, q);
+            reinterpret_cast<float4*>(it.gc[c] + (long long)q * B)[e4b - r1 * B4] = v1;
+        }
     }
 }
 
@@ -1671,6 +1666,17 @@ void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int 
     } else {
         dim3 g(mx_grid(12LL * s * B), nitems);
         k_mx_scatter64<<<g, 256, 0, st>>>(items, s, B);
+    }
+    ++g_kernel_launches;
+}
+
+void mx_ext32(cudaStream_t st, const MixItem* items, int nitems, int s, int B) {
+    if (B % 4 == 0) {
+        dim3 g(mx_grid(2LL * s * B), nitems);
+        k_mx_ext32_4<<<g, 256, 0, st>>>(items, s, B);
+    } else {
+        dim3 g(mx_grid(8LL * s * B), nitems);
+        k_mx_ext32<<<g, 256, 0, st>>>(items, s, B);
     }
     ++g_kernel_launches;
 }

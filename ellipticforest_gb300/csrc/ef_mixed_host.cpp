@@ -536,13 +536,13 @@ void MixedSolver::tune() {
 // Bytes a node GEMM launch moves at the least: the operator (FP32, or the three bf16 planes of the
 // tensor-core form), the right-hand side block and what the epilogue reads and writes per node --
 // W: hd in, w out; H: w in, hc in, h out; DOWN: gf in, w in, both children's interface rows out,
-// the FP64 interface state read and written, the exterior rows copied to the children.
+// the FP64 interface state read and written.
 double MixedSolver::gemm_bytes(const MGroup& g, int kind, int B, int code) const {
     const double c = g.cnt, s = g.s, eb = (g.tc[kind] && code < 0) ? 6.0 : 4.0;
     const double op = (kind == 2 ? 32.0 : 16.0) * s * s * eb;
     // per request: W 4s in + 4s out (FP32); H 8s + 8s in, 8s out; DOWN 8s + 4s in, 2 x 4s out, 4s
-    // FP64 read and written, 8s copied
-    const double vec = kind == 0 ? 32.0 * s : kind == 1 ? 96.0 * s : (32.0 + 16.0 + 32.0 + 64.0 + 64.0) * s;
+    // FP64 read and written
+    const double vec = kind == 0 ? 32.0 * s : kind == 1 ? 96.0 * s : (32.0 + 16.0 + 32.0 + 64.0) * s;
     return c * (op + vec * B);
 }
 
@@ -761,6 +761,11 @@ void MixedSolver::pass(int B, bool first, bool neumann_done) {
             if (g.level != lvl) continue;
             const double c = g.cnt, s2 = double(g.s) * g.s;
             const int code = h.mx_split_.empty() ? 0 : h.mx_split_[gi][2];
+            // the exterior rows go to the children unchanged (a streaming launch: in the GEMM's
+            // epilogue the copy's latency sat on the epilogue warps), the GEMM writes the interface rows
+            h.pb("mx_exterior", st);
+            mx_ext32(st, g.d_items, g.cnt, g.s, B);
+            h.pe(c * 8 * g.s * B * 8.0, 0, st);
             h.pb("mx_gemm_down", st);
             node_gemm(st, g, 2, B, code);
             h.pe(gemm_bytes(g, 2, B, code), c * 2.0 * 32 * s2 * B, st);

@@ -36,7 +36,8 @@
 //
 // Roles (256 threads, eight warps: two per SM sub-partition, so up to 255 registers a thread):
 // warps 0-3 add each chunk's accumulators to registers and run the epilogue (warp w reads TMEM lanes
-// 32w..32w+31; the operands a row's epilogue reads are prefetched when its tile starts), warps 4-6
+// 32w..32w+31; the operands a row's epilogue reads are prefetched when its tile starts; the
+// exterior rows of DOWN's children are copied by their own launch, k_mx_ext32), warps 4-6
 // stage X (the next chunk's loads in flight while the current one is split and written), warp 7
 // allocates TMEM, its lane 0 issues the TMA loads and its lane 1 the MMAs.  Stages
 // are handed over through mbarriers; the MMA issuer frees a stage with tcgen05.commit.  Every wait
@@ -354,56 +355,6 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
     }
 }
 
-// exterior points of a parent go to its children unchanged: rows [p0, p1) of one item, all
-// requests, spread over the 128 epilogue threads with eight loads in flight before their stores
-__device__ __forceinline__ void tc_ext_copy(const MixItem& it, int s, int B, int p0, int p1, int t) {
-    if ((B & 3) == 0) {
-        const int w4 = B >> 2, tot = (p1 - p0) * w4;
-        for (int e0 = t; e0 < tot; e0 += 8 * 128) {
-            float4 val[8];
-            float4* dst[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int e = e0 + u * 128;
-                dst[u] = nullptr;
-                if (e < tot) {
-                    const int p = p0 + e / w4, b4 = e - (e / w4) * w4;
-                    int c, q;
-                    mx_ext_map(p, s, c, q);
-                    val[u] = reinterpret_cast<const float4*>(it.gf + (long long)p * B)[b4];
-                    dst[u] = reinterpret_cast<float4*>(it.gc[c] + (long long)q * B) + b4;
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (dst[u]) *dst[u] = val[u];
-        }
-    } else {
-        const int tot = (p1 - p0) * B;
-        for (int e = t; e < tot; e += 128) {
-            const int p = p0 + e / B, bb = e - (e / B) * B;
-            int c, q;
-            mx_ext_map(p, s, c, q);
-            it.gc[c][(long long)q * B + bb] = it.gf[(long long)p * B + bb];
-        }
-    }
-}
-
-// the share of a DOWN tile: the exterior rows of the nodes its rows belong to (a node of >= 128
-// rows splits them over its tiles)
-__device__ __forceinline__ void tc_ext_copy_tile(const MixItem* __restrict__ items, int s, int B, int cnt,
-                                                 int rows_item, int tile, int t) {
-    const int rows = 8 * s;
-    if (rows_item >= kTM) {
-        const int tpi = rows_item / kTM, item = tile / tpi, tl = tile - item * tpi;
-        const int per = (rows + tpi - 1) / tpi;
-        tc_ext_copy(items[item], s, B, tl * per, min(rows, tl * per + per), t);
-    } else {
-        const int ipt = kTM / rows_item;
-        for (int item = tile * ipt; item < min(cnt, tile * ipt + ipt); ++item) tc_ext_copy(items[item], s, B, 0, rows, t);
-    }
-}
-
 template <int KIND, int NSEG>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_mx_umma(const __grid_constant__ CUtensorMap tmA, const MixItem* __restrict__ items, int s, int B, int cnt,
@@ -698,7 +649,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             const int grow = tile * kTM + t;
             if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, pre, vec);
-            if (KIND == MX_DOWN && blockIdx.y == 0) tc_ext_copy_tile(items, s, B, cnt, sh.rows_item, tile, t);
 #pragma unroll
             for (int q = 0; q < 32; ++q) v[q] = 0.f;
         }
@@ -728,7 +678,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const int tile = first_tile;
             const int grow = tile * kTM + t;
             if (grow < R) tc_store_row<KIND>(items, s, B, b0, sh.rows_item, grow, v, pre, vec);
-            if (KIND == MX_DOWN && blockIdx.y == 0) tc_ext_copy_tile(items, s, B, cnt, sh.rows_item, tile, t);
         }
         cluster.sync();
     }
