@@ -506,6 +506,7 @@ private:
     bool direct_ = false;
     MxRow* d_gsrc_ = nullptr;     // [L][4n] Dirichlet rows of the leaves
     MxMis* d_mis_ = nullptr;      // interface mismatch rows of every node
+    MxAdd* d_add_ = nullptr;      // FP64 state update rows of every node
     long long nmis_ = 0;
     MxRow* d_rootsrc_ = nullptr;  // the root's boundary-flux rows (Robin root data)
     int nroot_ = 0;

@@ -187,6 +187,12 @@ struct MxMis {
     MxRow out, lo, up;
 };
 void mx_mismatch(cudaStream_t st, const char* arena, const MxMis* rows, long long nrows, int B);
+// one interface row of the FP64 state update of a pass: ug[b] += FP64(u[b]), u the pass's FP32
+// interface values as the DOWN GEMM wrote them into the lower child's Dirichlet rows
+struct MxAdd {
+    MxRow ug, u;
+};
+void mx_state_add(cudaStream_t st, const char* arena, const MxAdd* rows, long long nrows, int B);
 // dst row e ([B], rows contiguous) = row src[e]
 void mx_gather_rows64(cudaStream_t st, const char* arena, const MxRow* src, double* dst, int nrows, int B);
 

@@ -225,8 +225,10 @@ __global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __g
                     pre4[i] = *reinterpret_cast<const float4*>(it.hc[c] + (long long)q * B + bq);
                 } else {
                     pre4[i] = *reinterpret_cast<const float4*>(it.w + rb);
-                    preu0[i] = reinterpret_cast<const double2*>(it.uG + rb)[0];
-                    preu1[i] = reinterpret_cast<const double2*>(it.uG + rb)[1];
+                    if (it.uG) {
+                        preu0[i] = reinterpret_cast<const double2*>(it.uG + rb)[0];
+                        preu1[i] = reinterpret_cast<const double2*>(it.uG + rb)[1];
+                    }
                 }
             }
         }
@@ -265,8 +267,10 @@ __global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __g
                 }
                 dst0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + bq;
                 dst1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + bq;
-                double* ug = it.uG + rb;
-                if (vecx && bq < B) {
+                // the FP64 state (none: one launch adds the whole pass's values at its end)
+                double* ug = it.uG ? it.uG + rb : nullptr;
+                if (!ug) {
+                } else if (vecx && bq < B) {
                     double2 u0 = preu0[i], u1 = preu1[i];
                     u0.x += f2d_bits(v[0]); u0.y += f2d_bits(v[1]);
                     u1.x += f2d_bits(v[2]); u1.y += f2d_bits(v[3]);
@@ -508,6 +512,38 @@ __global__ void k_mx_mismatch(const char* __restrict__ arena, const MxMis* __res
             const MxMis m = rows[r];
             mx_row<float>(arena, m.out, B)[b] = d2f_rn_bits(mx_row<const double>(arena, m.lo, B)[b] -
                                                             mx_row<const double>(arena, m.up, B)[b]);
+        }
+    }
+}
+
+// The FP64 interface state of every node takes the pass's correction in one launch at the end of the
+// downward pass (trees without coarsening steps), instead of a read-modify-write in every DOWN
+// epilogue, where its latency sat on the epilogue warps.
+__global__ void k_mx_state_add(const char* __restrict__ arena, const MxAdd* __restrict__ rows, long long nrows, int B) {
+    if ((B & 3) == 0) {
+        const int B4 = B >> 2;
+        for (long long e4 = blockIdx.x * (long long)blockDim.x + threadIdx.x; e4 < nrows * B4;
+             e4 += (long long)gridDim.x * blockDim.x) {
+            const long long r = e4 / B4;
+            const int b = int(e4 - r * B4) * 4;
+            const MxAdd a = rows[r];
+            double* ug = mx_row<double>(arena, a.ug, B) + b;
+            const float4 u = *reinterpret_cast<const float4*>(mx_row<const float>(arena, a.u, B) + b);
+            double2 g0 = *reinterpret_cast<const double2*>(ug), g1 = *reinterpret_cast<const double2*>(ug + 2);
+            g0.x += f2d_bits(u.x);
+            g0.y += f2d_bits(u.y);
+            g1.x += f2d_bits(u.z);
+            g1.y += f2d_bits(u.w);
+            *reinterpret_cast<double2*>(ug) = g0;
+            *reinterpret_cast<double2*>(ug + 2) = g1;
+        }
+    } else {
+        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nrows * B;
+             e += (long long)gridDim.x * blockDim.x) {
+            const long long r = e / B;
+            const int b = int(e - r * B);
+            const MxAdd a = rows[r];
+            mx_row<double>(arena, a.ug, B)[b] += f2d_bits(mx_row<const float>(arena, a.u, B)[b]);
         }
     }
 }
@@ -1696,6 +1732,13 @@ void mx_mismatch(cudaStream_t st, const char* arena, const MxMis* rows, long lon
     if (nrows <= 0) return;
     const long long work = (B % 4 == 0) ? nrows * (B / 4) : nrows * B;
     k_mx_mismatch<<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
+    ++g_kernel_launches;
+}
+
+void mx_state_add(cudaStream_t st, const char* arena, const MxAdd* rows, long long nrows, int B) {
+    if (nrows <= 0) return;
+    const long long work = (B % 4 == 0) ? nrows * (B / 4) : nrows * B;
+    k_mx_state_add<<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
     ++g_kernel_launches;
 }
 

@@ -160,6 +160,7 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         d_leaves_ = cv.get<MixLeaf>(L);
         d_gsrc_ = cv.get<MxRow>(size_t(L) * 4 * n);
         d_mis_ = cv.get<MxMis>(size_t(nmis));
+        d_add_ = cv.get<MxAdd>(size_t(nmis));
         d_rootsrc_ = cv.get<MxRow>(size_t(nroot));
         if (fp) {
             // FP32 band factors and FP64 stencil tables, shared by the lanes of one tree
@@ -321,6 +322,21 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             }
             std::vector<MxMis> mis;
             mis.reserve(size_t(nmis));
+            // the FP64 state update of a pass: a node's interface row and the lower child's
+            // Dirichlet row into which DOWN writes the pass's value
+            std::vector<MxAdd> adds;
+            adds.reserve(size_t(nmis));
+            for (int id : order) {
+                if (mesh.nodes[id].leaf()) continue;
+                const int s = hps.nodes_[id].s;
+                const int* ch = mesh.nodes[id].child;
+                for (int r = 0; r < 4 * s; ++r) {
+                    const int I = r / s, o = r - I * s;
+                    adds.push_back(MxAdd{row(mn_[id].uG, size_t(r)), row(mn_[ch[mx_lower_child(I)]].g32, size_t(mx_q_lower(I, o, s)))});
+                }
+            }
+            if ((long long)adds.size() != nmis) throw std::logic_error("mixed solver: state rows not traced");
+            ck(upload_sync(st_, d_add_, adds.data(), adds.size() * sizeof(MxAdd)), "state rows");
             for (auto it = order.rbegin(); it != order.rend(); ++it) {
                 const int id = *it;
                 if (mesh.nodes[id].leaf()) {
@@ -373,7 +389,8 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             const MNode& m = mn_[id];
             MixItem& it = items[i];
             it.S = m.S; it.Xi = m.Xi; it.H = m.H32;
-            it.h = m.h32; it.hd = m.hd32; it.w = m.w32; it.m = m.m32; it.gf = m.gf32; it.uG = m.uG;
+            // uG null: the DOWN epilogues leave the FP64 state to mx_state_add (trees without coarsening)
+            it.h = m.h32; it.hd = m.hd32; it.w = m.w32; it.m = m.m32; it.gf = m.gf32; it.uG = direct_ ? nullptr : m.uG;
             it.gf64 = m.gf64; it.h64 = m.h64; it.mout = m.m32;
             for (int c = 0; c < 4; ++c) {
                 const MNode& ch = mn_[mesh.nodes[id].child[c]];
@@ -542,7 +559,7 @@ double MixedSolver::gemm_bytes(const MGroup& g, int kind, int B, int code) const
     const double op = (kind == 2 ? 32.0 : 16.0) * s * s * eb;
     // per request: W 4s in + 4s out (FP32); H 8s + 8s in, 8s out; DOWN 8s + 4s in, 2 x 4s out, 4s
     // FP64 read and written
-    const double vec = kind == 0 ? 32.0 * s : kind == 1 ? 96.0 * s : (32.0 + 16.0 + 32.0 + 64.0) * s;
+    const double vec = kind == 0 ? 32.0 * s : kind == 1 ? 96.0 * s : (32.0 + 16.0 + 32.0 + (direct_ ? 0.0 : 64.0)) * s;
     return c * (op + vec * B);
 }
 
@@ -770,6 +787,12 @@ void MixedSolver::pass(int B, bool first, bool neumann_done) {
             node_gemm(st, g, 2, B, code);
             h.pe(gemm_bytes(g, 2, B, code), c * 2.0 * 32 * s2 * B, st);
         }
+    }
+    if (direct_) {
+        // the pass's interface values into the FP64 state of every node, in one launch
+        h.pb("mx_interface", st);
+        mx_state_add(st, arena_, d_add_, nmis_, B);
+        h.pe(double(nmis_) * B * 20.0, 0, st);
     }
     h.pb("mx_leaf_solve", st);
     if (d_fps_) mx_fp_leaf32(st, LEAF_SOLVE, d_fps_, d_leaves_, L, B, n, q32_, u64_, first ? 0 : 1);

@@ -315,14 +315,23 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
         const int I = r / s, o = r - (r / s) * s;
         float* d0 = it.gc[mx_lower_child(I)] + (long long)mx_q_lower(I, o, s) * B + cb;
         float* d1 = it.gc[mx_upper_child(I)] + (long long)mx_q_upper(I, o, s) * B + cb;
-        double* ug = it.uG + (long long)r * B + cb;
+        // the FP64 state (none: one launch adds the whole pass's values at its end)
+        double* ug = it.uG ? it.uG + (long long)r * B + cb : nullptr;
 #pragma unroll
         for (int hf = 0; hf < 2; ++hf) {
             const int q0 = 16 * hf;
             float uu[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) uu[i] = v[q0 + i] + pre[q0 + i];
-            if (vec) {
+            if (vec && !ug) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (q0 + 4 * i < nb) {
+                        const float4 o4 = make_float4(uu[4 * i], uu[4 * i + 1], uu[4 * i + 2], uu[4 * i + 3]);
+                        *reinterpret_cast<float4*>(d0 + q0 + 4 * i) = o4;
+                        *reinterpret_cast<float4*>(d1 + q0 + 4 * i) = o4;
+                    }
+            } else if (vec) {
                 double2 u2[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
@@ -342,13 +351,13 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
             } else {
                 double uv[16];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) uv[i] = q0 + i < nb ? ug[q0 + i] : 0.0;
+                for (int i = 0; i < 16; ++i) uv[i] = (ug && q0 + i < nb) ? ug[q0 + i] : 0.0;
 #pragma unroll
                 for (int i = 0; i < 16; ++i)
                     if (q0 + i < nb) {
                         d0[q0 + i] = uu[i];
                         d1[q0 + i] = uu[i];
-                        ug[q0 + i] = uv[i] + f2d_bits(uu[i]);
+                        if (ug) ug[q0 + i] = uv[i] + f2d_bits(uu[i]);
                     }
             }
         }
