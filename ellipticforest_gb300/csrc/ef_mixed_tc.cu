@@ -221,8 +221,15 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16& p0, __nv_bfloat16
     const float r2 = r1 - __bfloat162float(p1);
     p2 = __float2bfloat16_rn(r2);
 }
-__device__ __forceinline__ unsigned pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    return unsigned(__bfloat16_as_ushort(lo)) | (unsigned(__bfloat16_as_ushort(hi)) << 16);
+// the same for a pair (a, b) with packed conversions: planes p0, p1, p2 as (a, b) bf16x2 words
+__device__ __forceinline__ void split3x2(float a, float b, unsigned& p0, unsigned& p1, unsigned& p2) {
+    const __nv_bfloat162 q0 = __floats2bfloat162_rn(a, b);
+    const float ra = a - __low2float(q0), rb = b - __high2float(q0);
+    const __nv_bfloat162 q1 = __floats2bfloat162_rn(ra, rb);
+    const __nv_bfloat162 q2 = __floats2bfloat162_rn(ra - __low2float(q1), rb - __high2float(q1));
+    p0 = *reinterpret_cast<const unsigned*>(&q0);
+    p1 = *reinterpret_cast<const unsigned*>(&q1);
+    p2 = *reinterpret_cast<const unsigned*>(&q2);
 }
 
 // right-hand-side block of segment `gseg` of a group (W, DOWN: one per node; H: one per child)
@@ -588,15 +595,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (int e = t; e < NSEG * 32 * kTB; e += kStageThreads) {
                 const int n = e & 31, kp = (e >> 5) & 31, j = e >> 10;
                 const float x0 = src[(j * kTK + 2 * kp) * kTB + n], x1 = src[(j * kTK + 2 * kp + 1) * kTB + n];
-                __nv_bfloat16 p0a, p1a, p2a, p0b, p1b, p2b;
-                split3(x0, p0a, p1a, p2a);
-                split3(x1, p0b, p1b, p2b);
+                unsigned p0, p1, p2;
+                split3x2(x0, x1, p0, p1, p2);
                 const int kl = 2 * kp;
                 const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
                                      ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
-                *reinterpret_cast<unsigned*>(sx + off) = pack2(p0a, p0b);
-                *reinterpret_cast<unsigned*>(sx + xp + off) = pack2(p1a, p1b);
-                *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = pack2(p2a, p2b);
+                *reinterpret_cast<unsigned*>(sx + off) = p0;
+                *reinterpret_cast<unsigned*>(sx + xp + off) = p1;
+                *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = p2;
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_arrive(&x_full[st]);
