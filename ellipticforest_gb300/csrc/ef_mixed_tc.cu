@@ -591,18 +591,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const float* src = ring + (g % kXRing) * RC;
             unsigned char* sx = base + size_t(st) * SB + 3 * kPlaneA;
             constexpr unsigned xp = unsigned(NSEG) * kPlaneX;
-            // one (k, k + 1) pair of one request per item: NSEG x 32 pairs x 32 requests
-            for (int e = t; e < NSEG * 32 * kTB; e += kStageThreads) {
-                const int n = e & 31, kp = (e >> 5) & 31, j = e >> 10;
-                const float x0 = src[(j * kTK + 2 * kp) * kTB + n], x1 = src[(j * kTK + 2 * kp + 1) * kTB + n];
-                unsigned p0, p1, p2;
-                split3x2(x0, x1, p0, p1, p2);
-                const int kl = 2 * kp;
-                const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u +
-                                     ((unsigned(kl >> 3) ^ unsigned(n & 7)) << 4) + (unsigned(kl & 7) << 1);
-                *reinterpret_cast<unsigned*>(sx + off) = p0;
-                *reinterpret_cast<unsigned*>(sx + xp + off) = p1;
-                *reinterpret_cast<unsigned*>(sx + 2 * xp + off) = p2;
+            // one 16-byte swizzle chunk (8 consecutive k) of one request per item and plane:
+            // NSEG x 8 chunks x 32 requests, the ring read by consecutive requests
+            for (int e = t; e < NSEG * 8 * kTB; e += kStageThreads) {
+                const int n = e & 31, kg = (e >> 5) & 7, j = e >> 8;
+                const float* x = src + (j * kTK + 8 * kg) * kTB + n;
+                uint4 c0, c1, c2;
+                split3x2(x[0], x[kTB], c0.x, c1.x, c2.x);
+                split3x2(x[2 * kTB], x[3 * kTB], c0.y, c1.y, c2.y);
+                split3x2(x[4 * kTB], x[5 * kTB], c0.z, c1.z, c2.z);
+                split3x2(x[6 * kTB], x[7 * kTB], c0.w, c1.w, c2.w);
+                const unsigned off = unsigned(j) * kPlaneX + unsigned(n) * 128u + ((unsigned(kg) ^ unsigned(n & 7)) << 4);
+                *reinterpret_cast<uint4*>(sx + off) = c0;
+                *reinterpret_cast<uint4*>(sx + xp + off) = c1;
+                *reinterpret_cast<uint4*>(sx + 2 * xp + off) = c2;
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_arrive(&x_full[st]);
