@@ -476,7 +476,8 @@ private:
     // fused: the zero-state residual of 16 x 16 leaves together with the first pass's Neumann step
     // (mx_leaf16_first); the pass then starts at the upward GEMMs
     void residual(int B, double* rmax, bool zero_state, bool fused = false);
-    void pass(int B, bool first, bool neumann_done = false);
+    // last: no residual follows, so the interface state need not take the pass's values
+    void pass(int B, bool first, bool neumann_done = false, bool last = false);
     // one node GEMM of a group (kind 0 W, 1 H, 2 DOWN): code > 0 the FP32 CUDA-core kernel with K
     // split `code` (0: its heuristic), code < 0 the tensor-core kernel with K split -code
     void node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code);

@@ -723,7 +723,7 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state, bool fused) {
     h.pe(0, 0, st);
 }
 
-void MixedSolver::pass(int B, bool first, bool neumann_done) {
+void MixedSolver::pass(int B, bool first, bool neumann_done, bool last) {
     Hps& h = H_;
     cudaStream_t st = st_;
     const int maxL = h.mesh().max_level;
@@ -788,8 +788,9 @@ void MixedSolver::pass(int B, bool first, bool neumann_done) {
             h.pe(gemm_bytes(g, 2, B, code), c * 2.0 * 32 * s2 * B, st);
         }
     }
-    if (direct_) {
-        // the pass's interface values into the FP64 state of every node, in one launch
+    if (direct_ && !last) {
+        // the pass's interface values into the FP64 state of every node, in one launch (no residual
+        // reads the state after the last pass)
         h.pb("mx_interface", st);
         mx_state_add(st, arena_, d_add_, nmis_, B);
         h.pe(double(nmis_) * B * 20.0, 0, st);
@@ -818,7 +819,7 @@ void MixedSolver::solve(int B, int sweeps) {
         for (int p = 0; p <= sweeps; ++p) {
             const bool f = fuse && (p == 0 || res_form_ == 0);
             residual(B, rmax_ + size_t(p) * bmax_, p == 0, f);
-            pass(B, p == 0, f);
+            pass(B, p == 0, f, p == sweeps);
         }
     });
 }
