@@ -974,7 +974,7 @@ __device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
+__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 5 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
                                                    const MixLeaf* __restrict__ leaves, int L, int B,
                                                    const float* __restrict__ q, double* __restrict__ u64,
                                                    int accumulate) {
@@ -1036,7 +1036,7 @@ __global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(c
 // solve step and handed to the leaf pass body through the transpose buffer instead of memory; the
 // edge fluxes of the zero state (FP64) and the items' largest |r| are written as by the residual
 // kernel.
-__global__ void __launch_bounds__(256, 3) k_mx_leaf16_first(const LeafType32* __restrict__ types,
+__global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __restrict__ types,
                                                             const MixCoef* __restrict__ coefs,
                                                             const MixLeaf* __restrict__ leaves, int L, int B,
                                                             const double* __restrict__ f, float* __restrict__ q,
