@@ -9,8 +9,9 @@ Fourier modes per side).  The build stage (leaf DtN + all merges, FP64) is timed
             requests solved on the factored tree by FP32 HPS passes (batched node GEMMs, FP32 leaf
             eigen-solves) with --sweeps refinement sweeps (exact fixed-point leaf residual + FP64
             interface flux mismatch), to <= 1e-10 relative of the FP64 HPS solution (rel_err_vs_fp64,
-            measured); inputs resident in HBM; --lanes 2 (default) alternates the steps over two lanes
-            sharing the operators, so two blocks are in flight
+            measured); inputs resident in HBM; one lane by default (--lanes 2 or 3 alternate the
+            steps over lanes sharing the operators, several blocks in flight: slower since the
+            kernels fill the GPU on their own)
   e2e    -- the same form through the C ABI call ef_hps_mixed_solve_blocks on pinned host buffers
             (K blocks in one call, three lanes rotating so two blocks' copies overlap a third's
             solve), the host<->device copies of every block inside the timed region; the one-block
@@ -390,7 +391,7 @@ def run_gb300(args):
     R = np.stack([reqs[i % P][3] for i in range(B)])
     u_mixed = hps.mixed_solve(F, A, R, sweeps)  # also leaves the block's inputs resident in HBM
     rel_err = max(float(np.abs(u_mixed[i] - ref_u[i]).max() / np.abs(ref_u[i]).max()) for i in range(P))
-    # two lanes (the second shares the FP32 operators, own stream) keep two blocks in flight: the
+    # with two lanes (the second shares the FP32 operators, own stream) two blocks are in flight: the
     # residual's integer work overlaps the other block's FP32 GEMM and leaf work.  Both lanes' inputs
     # are made resident by one two-block call, and lane 1 must give the same bits as lane 0.
     lanes = max(1, min(3, args.lanes))
@@ -1085,7 +1086,7 @@ def main():
     ap.add_argument("--sweeps", type=int, default=1,
                     help="refinement sweeps of the mixed form on uniform trees (one keeps the L7 results "
                          "within 1e-10 of the FP64 HPS, and within 3e-11 of a sparse direct solve)")
-    ap.add_argument("--lanes", type=int, default=2,
+    ap.add_argument("--lanes", type=int, default=1,
                     help="device-resident lanes of the headline, 1-3 (2: two blocks in flight on two streams)")
     ap.add_argument("--adaptive-sweeps", type=int, default=2,
                     help="refinement sweeps on the adaptive config-2 tree (one sweep leaves up to 2e-10 there)")
