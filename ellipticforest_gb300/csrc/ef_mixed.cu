@@ -1182,6 +1182,35 @@ __device__ __forceinline__ double fx_to_double(long long D, int sc) {
     return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (m & 0xfffffffffffffull)));
 }
 
+// The same three conversions for the 16 x 16 kernel, written with one variable shift each (the
+// general kernel keeps the forms above, so the test comparing the two kernels checks these against
+// them): for a shift sh = e - E_off <= s_max, m << sh = (m << s_max) >> (s_max - sh) exactly and
+// m >> -sh = (m << s_max) >> (s_max - sh) with truncation, and (m << s_max) < 2^61, so a shift of
+// 63 or more gives 0 as a shift of 64 or more does in fx_shift.
+__device__ __forceinline__ long long fx_from_1(double v, int E) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int e0 = int(bits >> 52) & 0x7ff;
+    const unsigned long long m = (bits & 0xfffffffffffffull) | (e0 ? (1ull << 52) : 0ull);
+    const int k = min(E - max(e0, 1), 63);  // 6 - sh
+    const unsigned long long a = (m << 6) >> k;
+    return (bits >> 63) ? -(long long)a : (long long)a;
+}
+__device__ __forceinline__ long long fx_scaled_1(double v, int sc) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int e0 = int(bits >> 52) & 0x7ff;
+    const unsigned long long m = (bits & 0xfffffffffffffull) | (1ull << 52);
+    const int k = min(1083 + sc - e0, 63);  // 8 - sh, sh = e - 1075 - sc <= 8
+    const unsigned long long a = e0 ? (m << 8) >> k : 0ull;
+    return (bits >> 63) ? -(long long)a : (long long)a;
+}
+// fx_term with the branch on d taken once per item (d is uniform over an item's lanes)
+__device__ __forceinline__ long long fx_term_1(long long S, long long m, int d) {
+    const long long hi = __mul64hi(S, m);
+    if (d >= 64) return d >= 128 ? (hi < 0 ? -1ll : 0ll) : hi >> (d - 64);
+    const unsigned long long lo = (unsigned long long)S * (unsigned long long)m;
+    return (long long)(((unsigned long long)hi << (64 - d)) | (lo >> d));
+}
+
 // FORM 0: every leaf type has cx = cy and lambda = 0 (one product per cell); FORM 1: general
 template <int NT, int FORM>
 __global__ void __launch_bounds__(256, FORM == 0 ? 4 : 2) k_mx_leaf_residual(const MixCoef* __restrict__ coefs,
@@ -1943,11 +1972,11 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     // (2) fixed point: the column into the tile, the W/E ghost rows, this lane's S/N ghosts
     long long gx[4];
 #pragma unroll
-    for (int side = 0; side < 4; ++side) gx[side] = fx_from(gv[side], Eu);
+    for (int side = 0; side < 4; ++side) gx[side] = fx_from_1(gv[side], Eu);
     long long top_c, bot_c;  // the column's first and last cells (W and E edge fluxes)
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        const long long m = fx_from(uc[i], Eu);
+        const long long m = fx_from_1(uc[i], Eu);
         tl[(i + 1) * RS + t] = m;
         if (i == 0) top_c = m;
         if (i == 15) bot_c = m;
@@ -2048,9 +2077,9 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
         const double fk[2] = {fv.x, fv.y};
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            long long R = fx_scaled(fk[k], sc) - fx_term(sx[k], cf.cxm, dx);
-            if (!iso) R -= fx_term(sy[k], cf.cym, dy);
-            if (lam) R -= fx_term(c[k], cf.lmm, dl);
+            long long R = fx_scaled_1(fk[k], sc) - fx_term_1(sx[k], cf.cxm, dx);
+            if (!iso) R -= fx_term_1(sy[k], cf.cym, dy);
+            if (lam) R -= fx_term_1(c[k], cf.lmm, dl);
             rr[k] = bad ? __int_as_float(0x7fffffff) : __fmul_rn(__fmul_rn(__ll2float_rn(R), pa), pb);
             mx = fmaxf(mx, fabsf(rr[k]));
         }
