@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <stdexcept>
 
 #include "ef_kernels.cuh"
@@ -489,12 +490,14 @@ __global__ void k_mx_flux_up4(const MixItem* __restrict__ items, int s, int B) {
 // root data and the ancestors' interface states, through MixLeaf::gsrc), and every interface row
 // of every node takes its flux mismatch straight from the edge fluxes of the two leaves that meet
 // there -- one launch instead of a scatter and a flux step per level.
-__global__ void k_mx_mismatch(const char* __restrict__ arena, const MxMis* __restrict__ rows, long long nrows, int B) {
+// The index type I of these grid-stride kernels is int whenever the element count fits (the launchers
+// choose): a 64-bit integer division runs on GB300's narrow FP64 pipe, a 32-bit one does not.
+template <class I>
+__global__ void k_mx_mismatch(const char* __restrict__ arena, const MxMis* __restrict__ rows, I nrows, int B) {
     if ((B & 3) == 0) {
         const int B4 = B >> 2;
-        for (long long e4 = blockIdx.x * (long long)blockDim.x + threadIdx.x; e4 < nrows * B4;
-             e4 += (long long)gridDim.x * blockDim.x) {
-            const long long r = e4 / B4;
+        for (I e4 = blockIdx.x * (I)blockDim.x + threadIdx.x; e4 < nrows * B4; e4 += (I)gridDim.x * blockDim.x) {
+            const I r = e4 / B4;
             const int b = int(e4 - r * B4) * 4;
             const MxMis m = rows[r];
             const double* lo = mx_row<const double>(arena, m.lo, B) + b;
@@ -505,9 +508,8 @@ __global__ void k_mx_mismatch(const char* __restrict__ arena, const MxMis* __res
                                                                 d2f_rn_bits(l1.x - u1.x), d2f_rn_bits(l1.y - u1.y));
         }
     } else {
-        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nrows * B;
-             e += (long long)gridDim.x * blockDim.x) {
-            const long long r = e / B;
+        for (I e = blockIdx.x * (I)blockDim.x + threadIdx.x; e < nrows * B; e += (I)gridDim.x * blockDim.x) {
+            const I r = e / B;
             const int b = int(e - r * B);
             const MxMis m = rows[r];
             mx_row<float>(arena, m.out, B)[b] = d2f_rn_bits(mx_row<const double>(arena, m.lo, B)[b] -
@@ -519,12 +521,12 @@ __global__ void k_mx_mismatch(const char* __restrict__ arena, const MxMis* __res
 // The FP64 interface state of every node takes the pass's correction in one launch at the end of the
 // downward pass (trees without coarsening steps), instead of a read-modify-write in every DOWN
 // epilogue, where its latency sat on the epilogue warps.
-__global__ void k_mx_state_add(const char* __restrict__ arena, const MxAdd* __restrict__ rows, long long nrows, int B) {
+template <class I>
+__global__ void k_mx_state_add(const char* __restrict__ arena, const MxAdd* __restrict__ rows, I nrows, int B) {
     if ((B & 3) == 0) {
         const int B4 = B >> 2;
-        for (long long e4 = blockIdx.x * (long long)blockDim.x + threadIdx.x; e4 < nrows * B4;
-             e4 += (long long)gridDim.x * blockDim.x) {
-            const long long r = e4 / B4;
+        for (I e4 = blockIdx.x * (I)blockDim.x + threadIdx.x; e4 < nrows * B4; e4 += (I)gridDim.x * blockDim.x) {
+            const I r = e4 / B4;
             const int b = int(e4 - r * B4) * 4;
             const MxAdd a = rows[r];
             double* ug = mx_row<double>(arena, a.ug, B) + b;
@@ -538,9 +540,8 @@ __global__ void k_mx_state_add(const char* __restrict__ arena, const MxAdd* __re
             *reinterpret_cast<double2*>(ug + 2) = g1;
         }
     } else {
-        for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nrows * B;
-             e += (long long)gridDim.x * blockDim.x) {
-            const long long r = e / B;
+        for (I e = blockIdx.x * (I)blockDim.x + threadIdx.x; e < nrows * B; e += (I)gridDim.x * blockDim.x) {
+            const I r = e / B;
             const int b = int(e - r * B);
             const MxAdd a = rows[r];
             mx_row<double>(arena, a.ug, B)[b] += f2d_bits(mx_row<const float>(arena, a.u, B)[b]);
@@ -548,11 +549,11 @@ __global__ void k_mx_state_add(const char* __restrict__ arena, const MxAdd* __re
     }
 }
 
+template <class I>
 __global__ void k_mx_gather_rows64(const char* __restrict__ arena, const MxRow* __restrict__ src,
                                    double* __restrict__ dst, int nrows, int B) {
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)nrows * B;
-         e += (long long)gridDim.x * blockDim.x) {
-        const int r = int(e / B), b = int(e - (long long)r * B);
+    for (I e = blockIdx.x * (I)blockDim.x + threadIdx.x; e < (I)nrows * B; e += (I)gridDim.x * blockDim.x) {
+        const int r = int(e / B), b = int(e - (I)r * B);
         dst[e] = mx_row<const double>(arena, src[r], B)[b];
     }
 }
@@ -949,24 +950,25 @@ __device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const 
             }
         }
     } else {
-        // (5) edge values: S/N at i = t from row t of C, W/E at j = t from rows 0 and 15 of C
-        float e = 0.f, o = 0.f, uw = 0.f, ue = 0.f;
+        // (5) edge values u[i][j] = sum_l C[i][l] V[j][l]: S/N (j = 0, 15) at i = t from row t of C;
+        // W (i = 0) on lanes t < 8 and E (i = 15) on lanes t >= 8, each lane the pair j = t & 7 and
+        // 15 - (t & 7) from one row of C (V[15 - j][l] = (-1)^l V[j][l])
+        float e = 0.f, o = 0.f, ew = 0.f, ow = 0.f;
+        const int jw = t & 7, rc = t < 8 ? 0 : 15;
 #pragma unroll
         for (int l = 0; l < 16; l += 2) {
             e = fmaf(c_mxV16[l], bf[l * 17 + t], e);
             o = fmaf(c_mxV16[l + 1], bf[(l + 1) * 17 + t], o);
-        }
-#pragma unroll
-        for (int l = 0; l < 16; ++l) {
-            const float v = Vs[t * 17 + l];
-            uw = fmaf(bf[l * 17], v, uw);
-            ue = fmaf(bf[l * 17 + 15], v, ue);
+            ew = fmaf(bf[l * 17 + rc], Vs[jw * 17 + l], ew);
+            ow = fmaf(bf[(l + 1) * 17 + rc], Vs[jw * 17 + l + 1], ow);
         }
         if (act) {
             const float dtn_x = 2.0f / types[type].dx, dtn_y = 2.0f / types[type].dy;
             float* h = leaves[leaf].h32 + b;
-            h[(long long)(0 * 16 + t) * B] = dtn_x * uw;
-            h[(long long)(1 * 16 + t) * B] = -dtn_x * ue;
+            const float sw = t < 8 ? dtn_x : -dtn_x;
+            const int side = t < 8 ? 0 : 1;
+            h[(long long)(side * 16 + jw) * B] = sw * (ew + ow);
+            h[(long long)(side * 16 + 15 - jw) * B] = sw * (ew - ow);
             h[(long long)(2 * 16 + t) * B] = dtn_y * (e + o);
             h[(long long)(3 * 16 + t) * B] = -dtn_y * (e - o);
         }
@@ -981,10 +983,10 @@ __global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 5 : 3) k_mx_leaf16(c
     __shared__ float buf[16 * 272];
     __shared__ float Vs[16 * 17];
     const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
-    const long long item = (long long)blockIdx.x * 16 + slot;
-    const bool act = item < (long long)L * B;
-    const int leaf = act ? int(item / B) : 0;
-    const int b = act ? int(item - (long long)leaf * B) : 0;
+    const int item = blockIdx.x * 16 + slot;  // L * B < 2^31 (the launchers check)
+    const bool act = item < L * B;
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
     float* bf = buf + slot * 272;
     if (MODE == LEAF_NEUMANN) {
         // the full basis, for the edge sums whose basis row depends on the thread
@@ -1043,12 +1045,12 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __
                                                             float* __restrict__ rleaf) {
     __shared__ float buf[16 * 272];
     __shared__ float Vs[16 * 17];
-    __shared__ float gts[16 * 64];
+    __shared__ float gts[16 * 80];  // 80 floats per item: the two items of a warp use other banks
     const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
-    const long long item = (long long)blockIdx.x * 16 + slot;
-    const bool act = item < (long long)L * B;
-    const int leaf = act ? int(item / B) : 0;
-    const int b = act ? int(item - (long long)leaf * B) : 0;
+    const int item = blockIdx.x * 16 + slot;  // L * B < 2^31 (the launchers check)
+    const bool act = item < L * B;
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
     float* bf = buf + slot * 272;
     {
         // the full basis, for the edge sums whose basis row depends on the thread
@@ -1067,7 +1069,7 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __
     double gv[4];
 #pragma unroll
     for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
-    float* gt = gts + slot * 64;
+    float* gt = gts + slot * 80;
 #pragma unroll
     for (int side = 0; side < 4; ++side)
         gt[side * 16 + t] = -2.0f * (side < 2 ? cf.cx32 : cf.cy32) * d2f_rn_bits(gv[side]);
@@ -1760,20 +1762,23 @@ void mx_flux_up(cudaStream_t st, const MixItem* items, int nitems, int s, int B)
 void mx_mismatch(cudaStream_t st, const char* arena, const MxMis* rows, long long nrows, int B) {
     if (nrows <= 0) return;
     const long long work = (B % 4 == 0) ? nrows * (B / 4) : nrows * B;
-    k_mx_mismatch<<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
+    if (nrows * B <= INT_MAX / 2) k_mx_mismatch<int><<<mx_grid(work), 256, 0, st>>>(arena, rows, int(nrows), B);
+    else k_mx_mismatch<long long><<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
     ++g_kernel_launches;
 }
 
 void mx_state_add(cudaStream_t st, const char* arena, const MxAdd* rows, long long nrows, int B) {
     if (nrows <= 0) return;
     const long long work = (B % 4 == 0) ? nrows * (B / 4) : nrows * B;
-    k_mx_state_add<<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
+    if (nrows * B <= INT_MAX / 2) k_mx_state_add<int><<<mx_grid(work), 256, 0, st>>>(arena, rows, int(nrows), B);
+    else k_mx_state_add<long long><<<mx_grid(work), 256, 0, st>>>(arena, rows, nrows, B);
     ++g_kernel_launches;
 }
 
 void mx_gather_rows64(cudaStream_t st, const char* arena, const MxRow* src, double* dst, int nrows, int B) {
     if (nrows <= 0) return;
-    k_mx_gather_rows64<<<mx_grid((long long)nrows * B), 256, 0, st>>>(arena, src, dst, nrows, B);
+    if ((long long)nrows * B <= INT_MAX / 2) k_mx_gather_rows64<int><<<mx_grid((long long)nrows * B), 256, 0, st>>>(arena, src, dst, nrows, B);
+    else k_mx_gather_rows64<long long><<<mx_grid((long long)nrows * B), 256, 0, st>>>(arena, src, dst, nrows, B);
     ++g_kernel_launches;
 }
 
@@ -1826,10 +1831,17 @@ void mx_set_basis16(cudaStream_t st, const float* V) {
         throw std::runtime_error("mixed solver: leaf basis upload failed");
 }
 
+// Grid of the 16 x 16 leaf kernels (16 items (leaf, request) per block), whose item index is an int
+inline unsigned mx_grid16(int L, int B) {
+    const long long items = (long long)L * B;
+    if (items > INT_MAX - 16) throw std::invalid_argument("mixed solver: leaves x requests must stay below 2^31");
+    return unsigned((items + 15) / 16);
+}
+
 void mx_leaf32(cudaStream_t st, int mode, const LeafType32* types, const MixLeaf* leaves, int L, int B, int n,
                const float* q, double* u64, int accumulate) {
     if (n == 16) {
-        const unsigned grid16 = unsigned(((long long)L * B + 15) / 16);
+        const unsigned grid16 = mx_grid16(L, B);
         if (mode == LEAF_NEUMANN) k_mx_leaf16<LEAF_NEUMANN><<<grid16, 256, 0, st>>>(types, leaves, L, B, q, u64, 0);
         else k_mx_leaf16<LEAF_SOLVE><<<grid16, 256, 0, st>>>(types, leaves, L, B, q, u64, accumulate);
         ++g_kernel_launches;
@@ -1855,12 +1867,12 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __r
                                                            const MixLeaf* __restrict__ leaves, int L, int B,
                                                            const double* __restrict__ f, float* __restrict__ q,
                                                            float* __restrict__ rleaf) {
-    __shared__ float gts[16 * 64];
+    __shared__ float gts[16 * 80];  // 80 floats per item: the two items of a warp use other banks
     const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
-    const long long item = (long long)blockIdx.x * 16 + slot;
-    const bool act = item < (long long)L * B;
-    const int leaf = act ? int(item / B) : 0;
-    const int b = act ? int(item - (long long)leaf * B) : 0;
+    const int item = blockIdx.x * 16 + slot;  // L * B < 2^31 (the launchers check)
+    const bool act = item < L * B;
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
     const MixLeaf lf = leaves[leaf];
     const MixCoef cf = coefs[lf.type];
     const long long base = ((long long)b * L + leaf) * 256;
@@ -1872,7 +1884,7 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __r
     double gv[4];
 #pragma unroll
     for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
-    float* gt = gts + slot * 64;
+    float* gt = gts + slot * 80;
 #pragma unroll
     for (int side = 0; side < 4; ++side)
         gt[side * 16 + t] = -2.0f * (side < 2 ? cf.cx32 : cf.cy32) * d2f_rn_bits(gv[side]);
@@ -1920,7 +1932,10 @@ __global__ void __launch_bounds__(256) k_mx_leaf_residual0_16(const MixCoef* __r
 //    that layout;
 //  - the item's largest exponents and bit lengths reduce over its 16 lanes by shuffles.
 // The tile's rows are 18 words apart (144 B), so the row reads (16-byte vectors) and the column
-// writes (8-byte) are both free of bank conflicts.  FORM 0 keeps the cells' second differences in
+// writes (8-byte) are both free of bank conflicts; a row's neighbour cells across its 16-byte pairs
+// come from the pairs already read.  The items' tiles are 328 words apart (= 16 banks mod 32), so the
+// two items of a warp also meet no conflict when the Neumann step reuses the tiles as 17-float-row
+// transpose buffers.  FORM 0 keeps the cells' second differences in
 // registers between the bit-length sweep and the products and loads f by columns (coalesced),
 // handing it to the row owners through the tile; FORM 1 (two differences and the lambda term)
 // recomputes them from the tile and loads f by rows (16-byte vectors).
@@ -1934,7 +1949,7 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
                                                        float* __restrict__ q, float* __restrict__ rleaf,
                                                        const LeafType32* __restrict__ types) {
     static_assert(!NEU || FORM == 0, "the Neumann step is fused with the FORM 0 residual only");
-    constexpr int RS = 18, TS = 18 * RS;
+    constexpr int RS = 18, TS = 18 * RS + 4;
     __shared__ __align__(16) long long tiles[16 * TS];
     __shared__ float Vs[NEU ? 16 * 17 : 1];
     if constexpr (NEU) {
@@ -1945,10 +1960,10 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
         __syncthreads();
     }
     const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
-    const long long item = (long long)blockIdx.x * 16 + slot;
-    const bool act = item < (long long)L * B;
-    const int leaf = act ? int(item / B) : 0;
-    const int b = act ? int(item - (long long)leaf * B) : 0;
+    const int item = blockIdx.x * 16 + slot;  // L * B < 2^31 (the launchers check)
+    const bool act = item < L * B;
+    const int leaf = act ? item / B : 0;
+    const int b = act ? item - leaf * B : 0;
     const MixLeaf lf = leaves[leaf];
     const MixCoef cf = coefs[lf.type];
     const long long base = ((long long)b * L + leaf) * 256;
@@ -2028,12 +2043,30 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
             sx[1] += sy[1];
         }
     };
+    // FORM 0: the same differences, the row's pairs read once (a pair's outer neighbours are the
+    // adjacent pairs' inner cells)
+    auto row_diffs_w = [&](int m, longlong2 cc, long long left, long long right, long long (&sx)[2]) {
+        const longlong2 up = reinterpret_cast<const longlong2*>(rw - RS)[m];
+        const longlong2 dn = reinterpret_cast<const longlong2*>(rw + RS)[m];
+        sx[0] = up.x + dn.x - 2 * cc.x + (left + cc.y - 2 * cc.x);
+        sx[1] = up.y + dn.y - 2 * cc.y + (cc.x + right - 2 * cc.y);
+    };
     long long ks[KEEP ? 16 : 1];
     unsigned long long ox = 0ull, oy = 0ull;
+    longlong2 cur = reinterpret_cast<const longlong2*>(rw)[0];
+    long long left = 2 * gx[2] - cur.x;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
         long long c[2], sx[2], sy[2];
-        row_diffs(m, c, sx, sy);
+        if constexpr (KEEP) {
+            const longlong2 nxt = reinterpret_cast<const longlong2*>(rw)[m < 7 ? m + 1 : 7];
+            const long long right = m < 7 ? nxt.x : 2 * gx[3] - cur.y;
+            row_diffs_w(m, cur, left, right, sx);
+            left = cur.y;
+            cur = nxt;
+        } else {
+            row_diffs(m, c, sx, sy);
+        }
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             if (KEEP) ks[(2 * m + k) % (KEEP ? 16 : 1)] = sx[k];
@@ -2161,7 +2194,7 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
     if (zero_state) {
         const size_t smem0 = size_t(ipc) * 4 * size_t(n) * (sizeof(double) + sizeof(float));
         if (n == 16)
-            k_mx_leaf_residual0_16<<<unsigned((items + 15) / 16), 256, 0, st>>>(coefs, leaves, L, B, f, q, rl);
+            k_mx_leaf_residual0_16<<<mx_grid16(L, B), 256, 0, st>>>(coefs, leaves, L, B, f, q, rl);
         else if (n == 8)
             k_mx_leaf_residual0<8><<<grid, unsigned(ipc * tpe), smem0, st>>>(coefs, leaves, L, B, n, ipc, f, q, rl);
         else
@@ -2171,7 +2204,7 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
         return;
     }
     if (n == 16 && !g_general_residual.load()) {
-        const unsigned grid16 = unsigned((items + 15) / 16);
+        const unsigned grid16 = mx_grid16(L, B);
         if (form == 0) k_mx_resid16<0, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr);
         else k_mx_resid16<1, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr);
     } else if (form == 0) {
@@ -2185,18 +2218,15 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
 
 void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves, int L,
                      int B, const double* f, float* q, float* rleaf, double* rmax) {
-    const long long items = (long long)L * B;
-    k_mx_leaf16_first<<<unsigned((items + 15) / 16), 256, 0, st>>>(types, coefs, leaves, L, B, f, q,
-                                                                   rmax ? rleaf : nullptr);
+    k_mx_leaf16_first<<<mx_grid16(L, B), 256, 0, st>>>(types, coefs, leaves, L, B, f, q, rmax ? rleaf : nullptr);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }
 
 void mx_leaf16_residual_neumann(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves,
                                 int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax) {
-    const long long items = (long long)L * B;
-    k_mx_resid16<0, true><<<unsigned((items + 15) / 16), 256, 0, st>>>(coefs, leaves, L, B, f, u64, q,
-                                                                       rmax ? rleaf : nullptr, types);
+    k_mx_resid16<0, true><<<mx_grid16(L, B), 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rmax ? rleaf : nullptr,
+                                                           types);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }
