@@ -847,12 +847,16 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf32(const LeafType32* __restri
 // ---- 16 x 16 leaves: register-resident sine transforms ---------------------------------------------
 // The eigenbasis V[i][k] = c_k sin(pi (k + 1)(i + 1/2) / 16) satisfies V[15 - i][k] = (-1)^k V[i][k],
 // so its rows 0..7 (in constant memory: every FMA takes its coefficient as the constant operand,
-// with no shared-memory traffic) define the whole basis, and each 16-point transform is 128 FMAs on
-// even/odd combinations instead of 256.
+// with no shared-memory traffic) define the whole basis.  The odd modes fold twice more: V[7 - i][k]
+// = +V[i][k] for k = 1, 5, 9, 13 and -V[i][k] for k = 3, 7, 11, 15, and V[3 - i][k] = +V[i][k] for
+// k = 3, 11 and -V[i][k] for k = 7, 15 (sin(n pi - a) = -(-1)^n sin a; the FP32 table keeps these
+// equalities exactly).  A 16-point transform is then 88 FMAs and 28 additions on the folded
+// combinations instead of 256 FMAs (128 after the first fold alone).
 __constant__ float c_mxV16[8 * 16];
 
-// Analysis X[k] = sum_j V[j][k] x[j] over the spatial index: out(k, X[k]) for the even modes (from
-// x[j] + x[15 - j]), then the odd ones (from x[j] - x[15 - j]), so that outputs leave as they are made
+// Analysis X[k] = sum_j V[j][k] x[j] over the spatial index, out(k, X[k]) as the outputs are made:
+// the even modes from P[j] = x[j] + x[15 - j] (8 x 8), the odd ones from M[j] = x[j] - x[15 - j]
+// folded again (4 x 4 and two 2 x 2)
 template <class Out>
 __device__ __forceinline__ void mx_dst16_fwd(const float (&x)[16], Out&& out) {
     float P[8], M[8];
@@ -868,25 +872,50 @@ __device__ __forceinline__ void mx_dst16_fwd(const float (&x)[16], Out&& out) {
         for (int j = 0; j < 8; ++j) a = fmaf(c_mxV16[j * 16 + k], P[j], a);
         out(k, a);
     }
+    float MP[4], MM[4];
 #pragma unroll
-    for (int k = 1; k < 16; k += 2) {
+    for (int j = 0; j < 4; ++j) {
+        MP[j] = M[j] + M[7 - j];
+        MM[j] = M[j] - M[7 - j];
+    }
+#pragma unroll
+    for (int k = 1; k < 16; k += 4) {
         float a = 0.f;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) a = fmaf(c_mxV16[j * 16 + k], M[j], a);
+        for (int j = 0; j < 4; ++j) a = fmaf(c_mxV16[j * 16 + k], MP[j], a);
         out(k, a);
     }
+    const float Q0 = MM[0] + MM[3], Q1 = MM[1] + MM[2], R0 = MM[0] - MM[3], R1 = MM[1] - MM[2];
+    out(3, fmaf(c_mxV16[16 + 3], Q1, c_mxV16[3] * Q0));
+    out(11, fmaf(c_mxV16[16 + 11], Q1, c_mxV16[11] * Q0));
+    out(7, fmaf(c_mxV16[16 + 7], R1, c_mxV16[7] * R0));
+    out(15, fmaf(c_mxV16[16 + 15], R1, c_mxV16[15] * R0));
 }
-// Synthesis of the pair x[i], x[15 - i] (i < 8) from X: x[i] = sum_k V[i][k] X[k] = e + o, x[15 - i]
-// = e - o with e, o the sums over the even and odd modes
-__device__ __forceinline__ void mx_dst16_pair(const float (&X)[16], int i, float& lo, float& hi) {
-    float e = 0.f, o = 0.f;
+// Synthesis x[i] = sum_k V[i][k] X[k], out(i, x[i], x[15 - i]) for i < 8: x[i] = e_i + o_i, x[15 - i]
+// = e_i - o_i with e_i, o_i the sums over the even and odd modes, the o_i from the folded odd modes
+template <class Out>
+__device__ __forceinline__ void mx_dst16_syn(const float (&X)[16], Out&& out) {
+    const float c0 = fmaf(c_mxV16[11], X[11], c_mxV16[3] * X[3]);
+    const float c1 = fmaf(c_mxV16[16 + 11], X[11], c_mxV16[16 + 3] * X[3]);
+    const float d0 = fmaf(c_mxV16[15], X[15], c_mxV16[7] * X[7]);
+    const float d1 = fmaf(c_mxV16[16 + 15], X[15], c_mxV16[16 + 7] * X[7]);
+    const float b[4] = {c0 + d0, c1 + d1, c1 - d1, c0 - d0};
+    float o[8];
 #pragma unroll
-    for (int k = 0; k < 16; k += 2) {
-        e = fmaf(c_mxV16[i * 16 + k], X[k], e);
-        o = fmaf(c_mxV16[i * 16 + k + 1], X[k + 1], o);
+    for (int i = 0; i < 4; ++i) {
+        float a = 0.f;
+#pragma unroll
+        for (int k = 1; k < 16; k += 4) a = fmaf(c_mxV16[i * 16 + k], X[k], a);
+        o[i] = a + b[i];
+        o[7 - i] = a - b[i];
     }
-    lo = e + o;
-    hi = e - o;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        float e = 0.f;
+#pragma unroll
+        for (int k = 0; k < 16; k += 2) e = fmaf(c_mxV16[i * 16 + k], X[k], e);
+        out(i, e + o[i], e - o[i]);
+    }
 }
 
 // FP32 leaf pass for n = 16: a 16-thread group per item (leaf, b), thread t owning row t (x index).
@@ -913,26 +942,20 @@ __device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const 
     }
     // (4) C[i][t] = sum_k V[i][k] G[k][t]; transpose back: buffer row t holds column t of C
     __syncwarp();
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        float lo, hi;
-        mx_dst16_pair(X, i, lo, hi);
+    mx_dst16_syn(X, [&](int i, float lo, float hi) {
         bf[t * 17 + i] = lo;
         bf[t * 17 + 15 - i] = hi;
-    }
+    });
     __syncwarp();
     if (MODE == LEAF_SOLVE) {
         // (5) u[t][j] = sum_l C[t][l] V[j][l], staged in the buffer (row t)
 #pragma unroll
         for (int l = 0; l < 16; ++l) X[l] = bf[l * 17 + t];
         __syncwarp();
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            float lo, hi;
-            mx_dst16_pair(X, i, lo, hi);
+        mx_dst16_syn(X, [&](int i, float lo, float hi) {
             bf[t * 17 + i] = lo;
             bf[t * 17 + 15 - i] = hi;
-        }
+        });
         __syncwarp();
         // (6) the FP64 state, coalesced: thread t takes the value pairs 2 (t + 16 m), m < 8
         if (act) {
