@@ -461,10 +461,9 @@ private:
         MixConv* d_conv = nullptr;
         float *S32 = nullptr, *Xi32 = nullptr, *H32 = nullptr;
         CUtensorMap tmS{}, tmXi{}, tmH{};
-        // tensor-core path: three bf16 planes per operator kind and their tensor maps
+        // tensor-core path: three bf16 planes per operator kind, tiled as the kernel's stage images
         bool tc[3] = {false, false, false};  // per kind (W, H, DOWN)
         void *S3 = nullptr, *Xi3 = nullptr, *H3 = nullptr;
-        CUtensorMap tmS3{}, tmXi3{}, tmH3{};
     };
     struct MStep {
         int level = 0, nf = 0, count = 0;

@@ -248,16 +248,18 @@ void mx_gemm(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* it
 // largest K split worth trying for a GEMM kind at interface size s (every CTA keeps >= 2 chunks)
 int mx_gemm_max_split(int kind, int s);
 // Tensor-core (tcgen05) form of the same node GEMMs (ef_mixed_tc.cu).  The group's operators are
-// three bf16 planes [3][rows][K] whose sum is the FP32 operator (mx_tc_split, compact H rows in the
-// child-major order of the kernel), read through a TMA tensor map of 64 columns x 128 rows per box
-// with the 128-byte swizzle.  Supported for interface sizes s that are powers of two >= 16.
+// three bf16 planes whose sum is the FP32 operator (mx_tc_split, compact H rows in the child-major
+// order of the kernel), stored as 16 KB blocks of 128 rows x 64 columns in the order of their
+// shared-memory image with the 128-byte swizzle (mx_tc_plane_elems elements for the three planes,
+// zeroed before the split).  Supported for interface sizes s that are powers of two >= 16.
 bool mx_tc_supported(int kind, int s);
 int mx_tc_max_split(int kind, int s);
+long long mx_tc_plane_elems(long long rows, int K);
 void mx_tc_split(cudaStream_t st, int kind, const float* src, void* dst, long long rows, int K, int s);
 // failure-path test switch of both GEMM forms (process-wide): every CTA's first wait runs out
 void mx_set_inject_timeout(int on);
 void mx_tc_set_inject_timeout(int on);
-void mx_gemm_tc(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
+void mx_gemm_tc(cudaStream_t st, int kind, const void* planes, const MixItem* items, int nitems, int s, int B,
                 int* err, int ksplit);
 void mx_scatter64(cudaStream_t st, const MixItem* items, int nitems, int s, int B);
 // the pass's exterior rows of every node of a group to its children (gf -> gc)

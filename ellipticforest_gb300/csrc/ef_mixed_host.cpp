@@ -65,21 +65,6 @@ CUtensorMap make_map(float* base, long long rows, int cols, int box_rows) {
     return tm;
 }
 
-// three stacked bf16 planes [3 rows][cols] read in boxes of 64 columns (128 bytes) x 128 rows,
-// 128-byte swizzle: the K-major operand tiles of the tensor-core node GEMMs
-CUtensorMap make_map_bf16(void* base, long long rows3, int cols) {
-    CUtensorMap tm;
-    const cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows3)};
-    const cuuint64_t strides[1] = {cuuint64_t(cols) * 2};
-    const cuuint32_t box[2] = {64u, 128u};
-    const cuuint32_t estr[2] = {1u, 1u};
-    const CUresult r = encode_tiled()(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled (bf16) failed (" + std::to_string(int(r)) + ")");
-    return tm;
-}
-
 }  // namespace
 
 MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
@@ -186,16 +171,19 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             groups_[gi].S32 = S;
             groups_[gi].Xi32 = Xi;
             groups_[gi].H32 = H32;
-            // bf16 planes of the tensor-core path (3 x the FP32 element count, 2 bytes each)
-            // (per kind: W, H, DOWN)
+            // bf16 planes of the tensor-core path (3 x the FP32 element count up to the padding of
+            // the last row tile and K chunk, 2 bytes each) (per kind: W, H, DOWN)
             for (int kind = 0; kind < 3; ++kind)
                 groups_[gi].tc[kind] = hps.tensor_cores() != 0 && mx_tc_supported(kind, g.s);
             if (groups_[gi].tc[2])
-                groups_[gi].S3 = share ? share->groups_[gi].S3 : (void*)cv.get<uint16_t>(3 * cnt * 32 * s * s);
+                groups_[gi].S3 = share ? share->groups_[gi].S3
+                                       : (void*)cv.get<uint16_t>(size_t(mx_tc_plane_elems(cnt * 4 * s, int(8 * s))));
             if (groups_[gi].tc[0])
-                groups_[gi].Xi3 = share ? share->groups_[gi].Xi3 : (void*)cv.get<uint16_t>(3 * cnt * 16 * s * s);
+                groups_[gi].Xi3 = share ? share->groups_[gi].Xi3
+                                        : (void*)cv.get<uint16_t>(size_t(mx_tc_plane_elems(cnt * 4 * s, int(4 * s))));
             if (groups_[gi].tc[1])
-                groups_[gi].H3 = share ? share->groups_[gi].H3 : (void*)cv.get<uint16_t>(3 * cnt * 16 * s * s);
+                groups_[gi].H3 = share ? share->groups_[gi].H3
+                                       : (void*)cv.get<uint16_t>(size_t(mx_tc_plane_elems(cnt * 8 * s, int(2 * s))));
             for (size_t i = 0; i < cnt; ++i) {
                 MNode& m = mn_[g.nodes[i]];
                 m.S = S ? S + i * 32 * s * s : nullptr;
@@ -440,9 +428,6 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
             g.tmS = share->groups_[gi].tmS;
             g.tmXi = share->groups_[gi].tmXi;
             g.tmH = share->groups_[gi].tmH;
-            g.tmS3 = share->groups_[gi].tmS3;
-            g.tmXi3 = share->groups_[gi].tmXi3;
-            g.tmH3 = share->groups_[gi].tmH3;
             continue;
         }
         mx_convert(st, g.d_conv, g.cnt, g.s);
@@ -452,18 +437,10 @@ MixedSolver::MixedSolver(Hps& hps, int bmax, const MixedSolver* share)
         g.tmS = make_map(g.S32, cnt * 4 * s, int(8 * s), mx_tile_rows(0, g.s));
         g.tmXi = make_map(g.Xi32, cnt * 4 * s, int(4 * s), mx_tile_rows(0, g.s));
         g.tmH = make_map(g.H32, cnt * 8 * s, int(2 * s), mx_tile_rows(1, g.s));
-        if (g.tc[2]) {
-            mx_tc_split(st, 2, g.S32, g.S3, cnt * 4 * s, int(8 * s), g.s);
-            g.tmS3 = make_map_bf16(g.S3, 3 * cnt * 4 * s, int(8 * s));
-        }
-        if (g.tc[0]) {
-            mx_tc_split(st, 0, g.Xi32, g.Xi3, cnt * 4 * s, int(4 * s), g.s);
-            g.tmXi3 = make_map_bf16(g.Xi3, 3 * cnt * 4 * s, int(4 * s));
-        }
-        if (g.tc[1]) {
-            mx_tc_split(st, 1, g.H32, g.H3, cnt * 8 * s, int(2 * s), g.s);
-            g.tmH3 = make_map_bf16(g.H3, 3 * cnt * 8 * s, int(2 * s));
-        }
+        // (the arena was zeroed: the planes' padding rows and columns stay zero)
+        if (g.tc[2]) mx_tc_split(st, 2, g.S32, g.S3, cnt * 4 * s, int(8 * s), g.s);
+        if (g.tc[0]) mx_tc_split(st, 0, g.Xi32, g.Xi3, cnt * 4 * s, int(4 * s), g.s);
+        if (g.tc[1]) mx_tc_split(st, 1, g.H32, g.H3, cnt * 8 * s, int(2 * s), g.s);
     }
     ck(cudaGetLastError(), "mixed convert");
     ck(cudaStreamSynchronize(st), "mixed setup");
@@ -565,8 +542,8 @@ double MixedSolver::gemm_bytes(const MGroup& g, int kind, int B, int code) const
 
 void MixedSolver::node_gemm(cudaStream_t st, const MGroup& g, int kind, int B, int code) {
     if (g.tc[kind] && code < 0) {
-        const CUtensorMap& tm = kind == 0 ? g.tmXi3 : (kind == 1 ? g.tmH3 : g.tmS3);
-        mx_gemm_tc(st, kind, tm, g.d_items, g.cnt, g.s, B, d_err_, -code);
+        const void* planes = kind == 0 ? g.Xi3 : (kind == 1 ? g.H3 : g.S3);
+        mx_gemm_tc(st, kind, planes, g.d_items, g.cnt, g.s, B, d_err_, -code);
     } else {
         const int ksplit = code < 0 ? 0 : code;
         const CUtensorMap& tm = kind == 0 ? g.tmXi : (kind == 1 ? g.tmH : g.tmS);

@@ -25,10 +25,11 @@
 // it alone on the SM): five sets of 96 columns for one request block per tile, two of 192 for two,
 // so the MMAs run that many chunks ahead of the epilogue warps while they store a tile's rows.
 //
-// Layout.  The three planes of a group's operators (one back-to-back row-major matrix per kind, H
-// with each child's two runs of s rows made adjacent) are streamed by TMA in boxes of 128 rows x
-// 64 columns (one 128-byte swizzle row of bf16) -- the canonical K-major SWIZZLE_128B operand of
-// the MMA.  X is read as FP32 from the pass buffers ([K][B], requests fastest), split, and written
+// Layout.  The three planes of a group's operators (the rows of one kind's operators back to back,
+// H with each child's two runs of s rows made adjacent) are stored tiled: each 128-row x 64-column
+// block (one 128-byte swizzle row of bf16 per row) is 16 KB of sequential memory already in the
+// canonical K-major SWIZZLE_128B order of the MMA operand, so a stage loads each plane with one
+// bulk copy (cp.async.bulk) of sequential bytes rather than a tensor-map box of 128 rows K apart.  X is read as FP32 from the pass buffers ([K][B], requests fastest), split, and written
 // to shared memory in the same swizzled K-major form by the producer warps.  A tile is 128 rows; a
 // tile whose rows use several right-hand-side blocks (nodes of 4s < 128 rows, or the compact H's
 // four children) puts the blocks side by side in N (32 requests each) and keeps each row's own
@@ -39,7 +40,7 @@
 // 32w..32w+31; the operands a row's epilogue reads are prefetched when its tile starts; the
 // exterior rows of DOWN's children are copied by their own launch, k_mx_ext32), warps 4-6
 // stage X (the next chunk's loads in flight while the current one is split and written), warp 7
-// allocates TMEM, its lane 0 issues the TMA loads and its lane 1 the MMAs.  Stages
+// allocates TMEM, its lane 0 issues the bulk copies and its lane 1 the MMAs.  Stages
 // are handed over through mbarriers; the MMA issuer frees a stage with tcgen05.commit.  Every wait
 // gives up after about one second: the kernel then sets the error word, lets its copies and MMAs in
 // flight finish (bounded waits), frees its TMEM and returns.
@@ -202,12 +203,13 @@ __device__ __forceinline__ bool tc_wait(unsigned long long* bar, unsigned parity
         }
     }
 }
-__device__ __forceinline__ void tma_load_bf16(const CUtensorMap* tm, unsigned long long* bar, void* dst, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
-            "r"(smem_u32(dst)),
-        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
+// one contiguous block of global memory into shared memory (bulk copy engine), completing on `bar`;
+// both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
@@ -373,7 +375,7 @@ __device__ __forceinline__ void tc_store_row(const MixItem* __restrict__ items, 
 
 template <int KIND, int NSEG>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_mx_umma(const __grid_constant__ CUtensorMap tmA, const MixItem* __restrict__ items, int s, int B, int cnt,
+    k_mx_umma(const __nv_bfloat16* __restrict__ A3, const MixItem* __restrict__ items, int s, int B, int cnt,
               int ksplit, int ntiles, int* __restrict__ err) {
     const TcShape sh = tc_shape(KIND, s);  // sh.nseg == NSEG (checked by the launcher)
     const int K = sh.K, R = cnt * sh.rows_item;
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     extern __shared__ unsigned char tc_smem[];
     unsigned char* base = tc_smem + ((1024u - (smem_u32(tc_smem) & 1023u)) & 1023u);
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(base + size_t(NS) * SB);
-    unsigned long long* a_full = bars;             // [NS] TMA transaction barriers
+    unsigned long long* a_full = bars;             // [NS] bulk-copy transaction barriers
     unsigned long long* x_full = bars + NS;        // [NS] 128 staging arrivals
     unsigned long long* empty = bars + 2 * NS;     // [NS] MMA commit
     unsigned long long* acc_full = bars + 3 * NS;   // [NP] MMA commit at the end of a chunk
@@ -453,21 +455,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     bool ep_ok = true;
 
     if (warp == 7) {
-        // ---- lane 0: TMA producer of the three A planes of every stage ----
+        // ---- lane 0: producer of the three A planes of every stage (bulk copies) ----
         if (lane == 0) {
             int st = 0;
             unsigned ph = 0;
             int issued = 0;
             bool ok = true;
+            const long long pstride = (long long)ntiles * nkc * (kTM * kTK);  // elements per plane
             for (int u = 0; u < nunits && ok; ++u) {
-                const int row0 = tile_of(u) * kTM;
+                const long long blk0 = (long long)tile_of(u) * nkc + cbase;
                 for (int c = 0; c < cpu && ok; ++c) {
                     if (issued >= NS) ok = tc_wait(&empty[st], ph ^ 1u, abort_flag);
                     if (!ok) break;
                     unsigned char* sa = base + size_t(st) * SB;
                     mbar_expect_tx(&a_full[st], 3u * kPlaneA);
-                    for (int p = 0; p < 3; ++p)
-                        tma_load_bf16(&tmA, &a_full[st], sa + p * kPlaneA, (cbase + c) * kTK, p * R + row0);
+                    const __nv_bfloat16* src = A3 + (blk0 + c) * (kTM * kTK);
+                    for (int p = 0; p < 3; ++p) bulk_load(sa + p * kPlaneA, src + p * pstride, kPlaneA, &a_full[st]);
                     ++issued;
                     if (++st == NS) { st = 0; ph ^= 1u; }
                 }
@@ -705,11 +708,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp == 7) tmem_dealloc(tmem, unsigned(tcols));
 }
 
-// A planes of one group: dst[p][R][K] (bf16) with src[R][K] = dst[0] + dst[1] + dst[2]; H rows in the
-// child-major order of tc_h_unpermute
+// A planes of one group: three bf16 planes with src[R][K] = plane 0 + plane 1 + plane 2, each stored
+// tiled: the block of row tile t (128 rows) and K chunk c (64 columns) is 16 KB of sequential memory
+// at element ((p * ntiles + t) * nkc + c) * 8192 of the group's planes, in the order of its shared-
+// memory image (row r at 64 r, its 8-element groups g at 8 (g ^ (r & 7)): the 128-byte swizzle that
+// the MMA's shared-memory descriptors read), so that a pipeline stage loads each plane's tile with
+// one bulk copy of sequential bytes instead of 128 row pieces K columns apart.  Rows past R and
+// columns past K of the last tile and chunk stay as the caller zeroed them.  H rows in the
+// child-major order of tc_h_unpermute.
 __global__ void k_tc_split(const float* __restrict__ src, __nv_bfloat16* __restrict__ dst, long long R, int K,
                            int s, int permute_h) {
     const long long tot = R * K;
+    const int nkc = (K + kTK - 1) / kTK;
+    const long long pstride = (R + kTM - 1) / kTM * nkc * (kTM * kTK);
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
          e += (long long)gridDim.x * blockDim.x) {
         const long long row = e / K;
@@ -720,16 +731,19 @@ __global__ void k_tc_split(const float* __restrict__ src, __nv_bfloat16* __restr
             const int pr = int(row - node * 8 * s);
             srow = node * 8 * s + tc_h_unpermute(pr, s);
         }
+        const long long tile = row / kTM;
+        const int r = int(row - tile * kTM), c = k / kTK, kk = k - c * kTK;
+        const long long off = (tile * nkc + c) * (kTM * kTK) + r * kTK + (((kk >> 3) ^ (r & 7)) << 3) + (kk & 7);
         __nv_bfloat16 p0, p1, p2;
         split3(src[srow * K + k], p0, p1, p2);
-        dst[e] = p0;
-        dst[tot + e] = p1;
-        dst[2 * tot + e] = p2;
+        dst[off] = p0;
+        dst[pstride + off] = p1;
+        dst[2 * pstride + off] = p2;
     }
 }
 
 template <int KIND, int NSEG>
-void launch_umma_n(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int cnt, int s, int B, int* err,
+void launch_umma_n(cudaStream_t st, const void* A3, const MixItem* items, int cnt, int s, int B, int* err,
                    int ksplit) {
     const TcShape sh = tc_shape(KIND, s);
     const long long R = (long long)cnt * sh.rows_item;
@@ -755,7 +769,8 @@ void launch_umma_n(cudaStream_t st, const CUtensorMap& tm, const MixItem* items,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = ksplit > 1 ? 1 : 0;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_mx_umma<KIND, NSEG>, tm, items, s, B, cnt, ksplit, ntiles, err);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_mx_umma<KIND, NSEG>, reinterpret_cast<const __nv_bfloat16*>(A3),
+                                             items, s, B, cnt, ksplit, ntiles, err);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         throw std::runtime_error(std::string("tensor-core node GEMM launch (K split ") + std::to_string(ksplit) +
@@ -765,11 +780,11 @@ void launch_umma_n(cudaStream_t st, const CUtensorMap& tm, const MixItem* items,
 }
 
 template <int KIND>
-void launch_umma(cudaStream_t st, const CUtensorMap& tm, const MixItem* items, int cnt, int s, int B, int* err,
+void launch_umma(cudaStream_t st, const void* A3, const MixItem* items, int cnt, int s, int B, int* err,
                  int ksplit) {
     const int nseg = tc_shape(KIND, s).nseg;
-    if (nseg == 1) launch_umma_n<KIND, 1>(st, tm, items, cnt, s, B, err, ksplit);
-    else launch_umma_n<KIND, 2>(st, tm, items, cnt, s, B, err, ksplit);
+    if (nseg == 1) launch_umma_n<KIND, 1>(st, A3, items, cnt, s, B, err, ksplit);
+    else launch_umma_n<KIND, 2>(st, A3, items, cnt, s, B, err, ksplit);
 }
 
 }  // namespace
@@ -791,6 +806,10 @@ int mx_tc_max_split(int kind, int s) {
     return k;
 }
 
+long long mx_tc_plane_elems(long long R, int K) {
+    return 3 * ((R + kTM - 1) / kTM) * ((K + kTK - 1) / kTK) * (kTM * kTK);
+}
+
 void mx_tc_split(cudaStream_t st, int kind, const float* src, void* dst, long long R, int K, int s) {
     const long long tot = R * K;
     const int grid = int(std::min<long long>((tot + 255) / 256, 8192));
@@ -803,13 +822,13 @@ void mx_tc_set_inject_timeout(int on) {
         throw std::runtime_error("tensor-core GEMM: setting the failure-path test switch failed");
 }
 
-void mx_gemm_tc(cudaStream_t st, int kind, const CUtensorMap& tm, const MixItem* items, int nitems, int s, int B,
+void mx_gemm_tc(cudaStream_t st, int kind, const void* planes, const MixItem* items, int nitems, int s, int B,
                 int* err, int ksplit) {
     if (!mx_tc_supported(kind, s)) throw std::invalid_argument("tensor-core node GEMM: unsupported interface size");
     if (ksplit < 1) ksplit = 1;
-    if (kind == MX_W) launch_umma<MX_W>(st, tm, items, nitems, s, B, err, ksplit);
-    else if (kind == MX_H) launch_umma<MX_H>(st, tm, items, nitems, s, B, err, ksplit);
-    else launch_umma<MX_DOWN>(st, tm, items, nitems, s, B, err, ksplit);
+    if (kind == MX_W) launch_umma<MX_W>(st, planes, items, nitems, s, B, err, ksplit);
+    else if (kind == MX_H) launch_umma<MX_H>(st, planes, items, nitems, s, B, err, ksplit);
+    else launch_umma<MX_DOWN>(st, planes, items, nitems, s, B, err, ksplit);
 }
 
 }  // namespace efgb
