@@ -10,37 +10,11 @@
 // cC of FiniteVolumeSolver.cpp:66-100 are tabulated per cell for the residual, which uses the same
 // ghost treatment as the reference's boundary rows (cpp:100-184): a missing neighbour is 2g - u_C.
 #include "ef_kernels.cuh"
+#include "ef_mixed_common.cuh"
 
 namespace efgb {
 
 namespace {
-
-__device__ __forceinline__ double f2d_bits_fp(float x) {
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xffu;
-    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
-    if (e == 0) return __longlong_as_double((long long)sign);
-    const unsigned long long e64 = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
-    return __longlong_as_double((long long)(sign | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
-}
-__device__ __forceinline__ float d2f_bits_fp(double x) {  // rounded to nearest, ties to even
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    const int e = int((b >> 52) & 0x7ffull);
-    unsigned m = (unsigned)((b >> 29) & 0x7fffffull);
-    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
-    int e32 = e - 896;
-    if (e32 <= 0) return __uint_as_float(sign);
-    const unsigned rest = unsigned(b & 0x1fffffffull);
-    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) {
-        if (++m >> 23) {
-            m = 0u;
-            ++e32;
-        }
-    }
-    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);
-    return __uint_as_float(sign | ((unsigned)e32 << 23) | m);
-}
 
 // one CTA per leaf: FP32 boundary coefficients, FP64 stencil table
 __global__ void __launch_bounds__(256) k_mx_fp_convert(const FpLeaf* __restrict__ src, const MixFp* __restrict__ dst) {
@@ -196,7 +170,7 @@ __global__ void __launch_bounds__(256) k_mx_fp_leaf32(const MixFp* __restrict__ 
         for (int e = tid; e < N * nb; e += nt) {
             const int bb = e / N, r = e - bb * N;
             double* dst = u64 + ((long long)(b0 + bb) * L + leaf) * nn + r;
-            const double v = f2d_bits_fp(Y[r * ld + bb]);
+            const double v = f2d_bits(Y[r * ld + bb]);
             *dst = accumulate ? *dst + v : v;
         }
     } else {
@@ -258,7 +232,7 @@ __global__ void __launch_bounds__(256) k_mx_fp_residual(const MixFp* __restrict_
                     if (j > 0) r = fma(-cS[c], uu[c - 1], r);
                     if (j < n - 1) r = fma(-cN[c], uu[c + 1], r);
                 }
-                rr[t] = d2f_bits_fp(r);
+                rr[t] = d2f_rn_bits(r);
             }
             const bool edge_row = i == 0 || i == n - 1;
 #pragma unroll
@@ -286,7 +260,7 @@ __global__ void __launch_bounds__(256) k_mx_fp_residual(const MixFp* __restrict_
             const double ym = j > 0 ? (zero_state ? 0.0 : uu[c - 1]) : fma(2.0, gr(2 * n + i)[b], -uc);
             const double yp = j < n - 1 ? (zero_state ? 0.0 : uu[c + 1]) : fma(2.0, gr(3 * n + i)[b], -uc);
             const double r = fma(-cN[c], yp, fma(-cS[c], ym, fma(-cE[c], xp, fma(-cW[c], xm, fma(-cC[c], uc, ff[c])))));
-            const float rf = d2f_bits_fp(r);
+            const float rf = d2f_rn_bits(r);
             q[base + c] = rf;
             mx = fmaxf(mx, fabsf(rf));
         }
