@@ -999,7 +999,7 @@ __device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 5 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
+__global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(const LeafType32* __restrict__ types,
                                                    const MixLeaf* __restrict__ leaves, int L, int B,
                                                    const float* __restrict__ q, double* __restrict__ u64,
                                                    int accumulate) {
