@@ -957,19 +957,28 @@ __device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const 
             bf[t * 17 + 15 - i] = hi;
         });
         __syncwarp();
-        // (6) the FP64 state, coalesced: thread t takes the value pairs 2 (t + 16 m), m < 8
-        if (act) {
+        // (6) the FP64 state, coalesced: thread t takes the value pairs 2 (t + 16 m), m < 8; a first
+        // pass stores the doubles' words as they are assembled
+        if (act && accumulate) {
             double2* st = reinterpret_cast<double2*>(u64 + ((long long)b * L + leaf) * 256);
 #pragma unroll
             for (int m = 0; m < 8; ++m) {
                 const int e2 = t + 16 * m, i = e2 >> 3, j = (e2 & 7) * 2;
                 double2 v = make_double2(f2d_bits(bf[i * 17 + j]), f2d_bits(bf[i * 17 + j + 1]));
-                if (accumulate) {
-                    const double2 o = st[e2];
-                    v.x += o.x;
-                    v.y += o.y;
-                }
+                const double2 o = st[e2];
+                v.x += o.x;
+                v.y += o.y;
                 st[e2] = v;
+            }
+        } else if (act) {
+            uint4* st = reinterpret_cast<uint4*>(u64 + ((long long)b * L + leaf) * 256);
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+                const int e2 = t + 16 * m, i = e2 >> 3, j = (e2 & 7) * 2;
+                uint4 w;
+                f2d_words(bf[i * 17 + j], w.y, w.x);
+                f2d_words(bf[i * 17 + j + 1], w.w, w.z);
+                st[e2] = w;
             }
         }
     } else {

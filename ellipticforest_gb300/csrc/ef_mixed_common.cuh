@@ -19,15 +19,20 @@ __device__ __forceinline__ void mx_child_ifaces(int c, int& Ia, int& Ib) {
 // below the smallest normal number of the target type become signed zeros; d2f_rn_bits rounds to
 // nearest (ties to even): a one-signed rounding of every residual entry would bias the correction
 // it drives.
-__device__ __forceinline__ double f2d_bits(float x) {
-    // assembled as two 32-bit words (a 64-bit assembly of the same bits measured 7 % slower in the
-    // 16 x 16 leaf solve, whose FP64 state stores take 16 of these per thread)
+// the high and low 32-bit words of the double of x, for stores that need no FP64 register
+__device__ __forceinline__ void f2d_words(float x, unsigned& hi, unsigned& lo) {
     const unsigned b = __float_as_uint(x);
     const unsigned e = (b >> 23) & 0xffu;
     const unsigned sign = b & 0x80000000u;
     const unsigned e11 = e == 0xffu ? 0x7ffu : e + 896u;
-    const unsigned hi = e == 0 ? sign : (sign | (e11 << 20) | ((b & 0x7fffffu) >> 3));
-    const unsigned lo = e == 0 ? 0u : (b << 29);
+    hi = e == 0 ? sign : (sign | (e11 << 20) | ((b & 0x7fffffu) >> 3));
+    lo = e == 0 ? 0u : (b << 29);
+}
+__device__ __forceinline__ double f2d_bits(float x) {
+    // assembled as two 32-bit words (a 64-bit assembly of the same bits measured 7 % slower in the
+    // 16 x 16 leaf solve, whose FP64 state stores take 16 of these per thread)
+    unsigned hi, lo;
+    f2d_words(x, hi, lo);
     return __hiloint2double(int(hi), int(lo));
 }
 __device__ __forceinline__ float d2f_rn_bits(double x) {
