@@ -1028,6 +1028,12 @@ __global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(c
         __syncthreads();
     }
     const int type = leaves[leaf].type;
+    if (MODE == LEAF_SOLVE && accumulate && act) {
+        // the item's FP64 state (2 KB, read back at the end) on its way to L2 while the pass runs:
+        // 128 bytes a thread
+        const double* sp = u64 + ((long long)b * L + leaf) * 256 + t * 16;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(sp));
+    }
     float x[16];
     // (1) row t of the load; the solve adds the Dirichlet terms -2 (cx g_x + cy g_y) of the edge cells
     if (act) {
