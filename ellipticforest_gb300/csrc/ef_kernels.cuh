@@ -284,8 +284,10 @@ struct MixCoef {
 // integer products (more accurate than an FP64 stencil); form 0 when every leaf type has cx = cy and lambda = 0, else 1;
 // zero_state when u is identically zero; rleaf [B][L]
 // scratch for the per-request maximum rmax (may be null)
+// (gsrc, arena: the leaves' Dirichlet row tables, MixLeaf::gsrc of leaf k = gsrc + 4 n k, and their arena)
 void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const MixLeaf* leaves, int L, int B, int n,
-                      int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
+                      int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax,
+                      const MxRow* gsrc, const char* arena);
 void mx_root(cudaStream_t st, int m, int B, const double* a, const double* r, double* g);
 // Robin root data in the mixed form (fixed a, b per block solver; r per request, [B][m]):
 // rho = r - a g64 - b h64 (FP64 -> FP32); rhs = rho - b h32; g64 += dg
@@ -300,11 +302,13 @@ void mx_rmax(cudaStream_t st, const float* rleaf, int L, int B, double* rmax);
 // 16 x 16 constant-coefficient leaves: the zero-state residual (as mx_leaf_residual with zero_state)
 // fused with the first pass's Neumann step (as mx_leaf32 LEAF_NEUMANN on its output)
 void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves, int L,
-                     int B, const double* f, float* q, float* rleaf, double* rmax);
+                     int B, const double* f, float* q, float* rleaf, double* rmax, const MxRow* gsrc,
+                     const char* arena);
 // 16 x 16 leaves of residual form 0: the exact residual (as mx_leaf_residual) fused with the next
 // pass's Neumann step
 void mx_leaf16_residual_neumann(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves,
-                                int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax);
+                                int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax,
+                                const MxRow* gsrc, const char* arena);
 
 // Variable-coefficient (FivePointStencil) leaves of the mixed form (ef_mixed_fp.cu), indexed by leaf.
 struct MixFp {

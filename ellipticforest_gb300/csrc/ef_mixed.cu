@@ -1080,7 +1080,8 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __
                                                             const MixCoef* __restrict__ coefs,
                                                             const MixLeaf* __restrict__ leaves, int L, int B,
                                                             const double* __restrict__ f, float* __restrict__ q,
-                                                            float* __restrict__ rleaf) {
+                                                            float* __restrict__ rleaf, const MxRow* __restrict__ gsrc,
+                                                            const char* __restrict__ arena) {
     __shared__ float buf[16 * 272];
     __shared__ float Vs[16 * 17];
     __shared__ float gts[16 * 80];  // 80 floats per item: the two items of a warp use other banks
@@ -1097,6 +1098,11 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __
         Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
         __syncthreads();
     }
+    // the item's Dirichlet rows (MixLeaf::gsrc of every leaf is gsrc + 64 leaf in one arena): their
+    // table entries are loaded first, independent of the leaf record
+    MxRow gr[4];
+#pragma unroll
+    for (int side = 0; side < 4; ++side) gr[side] = act ? gsrc[leaf * 64 + side * 16 + t] : MxRow{0u, 0u};
     const MixLeaf lf = leaves[leaf];
     const MixCoef cf = coefs[lf.type];
     const long long base = ((long long)b * L + leaf) * 256;
@@ -1106,7 +1112,7 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __
     for (int m = 0; m < 8; ++m) fv[m] = act ? f2[t + 16 * m] : make_double2(0.0, 0.0);
     double gv[4];
 #pragma unroll
-    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
+    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(arena, gr[side], B)[b] : 0.0;
     float* gt = gts + slot * 80;
 #pragma unroll
     for (int side = 0; side < 4; ++side)
@@ -1985,7 +1991,8 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
                                                        const MixLeaf* __restrict__ leaves, int L, int B,
                                                        const double* __restrict__ f, const double* __restrict__ u64,
                                                        float* __restrict__ q, float* __restrict__ rleaf,
-                                                       const LeafType32* __restrict__ types) {
+                                                       const LeafType32* __restrict__ types,
+                                                       const MxRow* __restrict__ gsrc, const char* __restrict__ arena) {
     static_assert(!NEU || FORM == 0, "the Neumann step is fused with the FORM 0 residual only");
     constexpr int RS = 18, TS = 18 * RS + 4;
     __shared__ __align__(16) long long tiles[16 * TS];
@@ -2002,6 +2009,11 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     const bool act = item < L * B;
     const int leaf = act ? item / B : 0;
     const int b = act ? item - leaf * B : 0;
+    // the item's Dirichlet rows (MixLeaf::gsrc of every leaf is gsrc + 64 leaf in one arena): their
+    // table entries are loaded first, independent of the leaf record
+    MxRow gr[4];
+#pragma unroll
+    for (int side = 0; side < 4; ++side) gr[side] = act ? gsrc[leaf * 64 + side * 16 + t] : MxRow{0u, 0u};
     const MixLeaf lf = leaves[leaf];
     const MixCoef cf = coefs[lf.type];
     const long long base = ((long long)b * L + leaf) * 256;
@@ -2012,7 +2024,7 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
     for (int i = 0; i < 16; ++i) uc[i] = act ? u64[base + i * 16 + t] : 0.0;
     double gv[4];
 #pragma unroll
-    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(lf.arena, lf.gsrc[side * 16 + t], B)[b] : 0.0;
+    for (int side = 0; side < 4; ++side) gv[side] = act ? mx_row<const double>(arena, gr[side], B)[b] : 0.0;
     // (1) largest biased exponent of u and the ghosts (Eu), at least 1
     int eu = 1;
 #pragma unroll
@@ -2221,7 +2233,8 @@ void mx_residual_launch(cudaStream_t st, unsigned grid, unsigned threads, size_t
 }
 
 void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const MixLeaf* leaves, int L, int B, int n,
-                      int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax) {
+                      int zero_state, const double* f, const double* u64, float* q, float* rleaf, double* rmax,
+                      const MxRow* gsrc, const char* arena) {
     const int tpi = n * n / 4, tpe = tpi < 256 ? tpi : 256, ipc = 256 / tpe;
     const long long items = (long long)L * B;
     const unsigned grid = unsigned((items + ipc - 1) / ipc);
@@ -2243,8 +2256,8 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
     }
     if (n == 16 && !g_general_residual.load()) {
         const unsigned grid16 = mx_grid16(L, B);
-        if (form == 0) k_mx_resid16<0, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr);
-        else k_mx_resid16<1, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr);
+        if (form == 0) k_mx_resid16<0, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr, gsrc, arena);
+        else k_mx_resid16<1, false><<<grid16, 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rl, nullptr, gsrc, arena);
     } else if (form == 0) {
         mx_residual_launch<0>(st, grid, unsigned(ipc * tpe), smem, coefs, leaves, L, B, n, ipc, f, u64, q, rl);
     } else {
@@ -2255,16 +2268,19 @@ void mx_leaf_residual(cudaStream_t st, const MixCoef* coefs, int form, const Mix
 }
 
 void mx_leaf16_first(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves, int L,
-                     int B, const double* f, float* q, float* rleaf, double* rmax) {
-    k_mx_leaf16_first<<<mx_grid16(L, B), 256, 0, st>>>(types, coefs, leaves, L, B, f, q, rmax ? rleaf : nullptr);
+                     int B, const double* f, float* q, float* rleaf, double* rmax, const MxRow* gsrc,
+                     const char* arena) {
+    k_mx_leaf16_first<<<mx_grid16(L, B), 256, 0, st>>>(types, coefs, leaves, L, B, f, q, rmax ? rleaf : nullptr, gsrc,
+                                                       arena);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }
 
 void mx_leaf16_residual_neumann(cudaStream_t st, const LeafType32* types, const MixCoef* coefs, const MixLeaf* leaves,
-                                int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax) {
+                                int L, int B, const double* f, const double* u64, float* q, float* rleaf, double* rmax,
+                                const MxRow* gsrc, const char* arena) {
     k_mx_resid16<0, true><<<mx_grid16(L, B), 256, 0, st>>>(coefs, leaves, L, B, f, u64, q, rmax ? rleaf : nullptr,
-                                                           types);
+                                                           types, gsrc, arena);
     ++g_kernel_launches;
     if (rmax) mx_rmax(st, rleaf, L, B, rmax);
 }

@@ -664,13 +664,14 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state, bool fused) {
         // f read once for the zero-state residual and the first pass's Neumann step
         const double items = L * B;
         h.pb("mx_leaf_first", st);
-        mx_leaf16_first(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, q32_, rleaf_, rmax);
+        mx_leaf16_first(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, q32_, rleaf_, rmax, d_gsrc_, arena_);
         h.pe(items * (nn * 12.0 + 4 * 16 * 20.0), items * 2.0 * (3 * nn * 16 + 4 * nn), st);
     } else if (fused) {
         // the exact residual and the next pass's Neumann step from registers
         const double items = L * B;
         h.pb("mx_leaf_residual", st);
-        mx_leaf16_residual_neumann(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, u64_, q32_, rleaf_, rmax);
+        mx_leaf16_residual_neumann(st, d_types32_, d_coef_, d_leaves_, h.num_leaves(), B, f_, u64_, q32_, rleaf_, rmax,
+                                   d_gsrc_, arena_);
         h.pe(items * (nn * 20.0 + 4 * 16 * 20.0), items * (nn * 6.0 + 2.0 * (3 * nn * 16 + 4 * nn)), st);
     } else {
         h.pb("mx_leaf_residual", st);
@@ -679,7 +680,7 @@ void MixedSolver::residual(int B, double* rmax, bool zero_state, bool fused) {
                            rleaf_, rmax);
         else
             mx_leaf_residual(st, d_coef_, res_form_, d_leaves_, h.num_leaves(), B, h.leaf_n(), zero_state ? 1 : 0, f_,
-                             u64_, q32_, rleaf_, rmax);
+                             u64_, q32_, rleaf_, rmax, d_gsrc_, arena_);
         // f and the state in, r out; per item the 4n Dirichlet values in, the 4n edge fluxes out (FP64)
         h.pe(L * B * (nn * (zero_state ? 12.0 : 20.0) + 4.0 * h.leaf_n() * 16), zero_state ? 0.0 : L * B * nn * 6.0, st);
     }
