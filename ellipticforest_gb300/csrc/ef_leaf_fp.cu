@@ -184,11 +184,8 @@ void launch_fp_solve(cudaStream_t st, const FpLeaf* leaves, const LeafItem* item
     if (warps_per_cta > 8) warps_per_cta = 8;
     if (warps_per_cta < 1) warps_per_cta = 1;
     const size_t smem = size_t(warps_per_cta) * per_warp;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_fp_solve<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        configured = true;
-    }
+    // set on every launch: the attribute is per device and per context, and the call is cheap
+    cudaFuncSetAttribute(k_fp_solve<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     const unsigned blocks = unsigned((nitems + warps_per_cta - 1) / warps_per_cta);
     k_fp_solve<MODE><<<blocks, 32 * warps_per_cta, smem, st>>>(leaves, items, nitems);
     ++g_kernel_launches;
@@ -199,11 +196,7 @@ void launch_fp_solve(cudaStream_t st, const FpLeaf* leaves, const LeafItem* item
 void fp_factor(cudaStream_t st, const FpLeaf* leaves, int nleaves, int nmax) {
     if (nleaves <= 0) return;
     const size_t smem = size_t((nmax + 1) * (2 * nmax + 1) + nmax) * sizeof(double);
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_fp_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        configured = true;
-    }
+    cudaFuncSetAttribute(k_fp_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     k_fp_factor<<<nleaves, 256, smem, st>>>(leaves);
     ++g_kernel_launches;
 }
