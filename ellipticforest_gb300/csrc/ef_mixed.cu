@@ -987,6 +987,7 @@ __device__ __forceinline__ void mx_leaf16_body(float (&x)[16], float* bf, const 
         // 15 - (t & 7) from one row of C (V[15 - j][l] = (-1)^l V[j][l])
         float e = 0.f, o = 0.f, ew = 0.f, ow = 0.f;
         const int jw = t & 7, rc = t < 8 ? 0 : 15;
+        __syncthreads();  // the block's basis copy Vs (written at kernel start by every thread) is complete
 #pragma unroll
         for (int l = 0; l < 16; l += 2) {
             e = fmaf(c_mxV16[l], bf[l * 17 + t], e);
@@ -1024,8 +1025,7 @@ __global__ void __launch_bounds__(256, MODE == LEAF_SOLVE ? 4 : 3) k_mx_leaf16(c
         // the full basis, for the edge sums whose basis row depends on the thread
         const int i = tid >> 4, k = tid & 15;
         const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
-        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
-        __syncthreads();
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;  // read after the body's block barrier
     }
     const int type = leaves[leaf].type;
     if (MODE == LEAF_SOLVE && accumulate && act) {
@@ -1095,8 +1095,7 @@ __global__ void __launch_bounds__(256, 4) k_mx_leaf16_first(const LeafType32* __
         // the full basis, for the edge sums whose basis row depends on the thread
         const int i = tid >> 4, k = tid & 15;
         const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
-        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
-        __syncthreads();
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;  // read after the body's block barrier
     }
     // the item's Dirichlet rows (MixLeaf::gsrc of every leaf is gsrc + 64 leaf in one arena): their
     // table entries are loaded first, independent of the leaf record
@@ -2001,8 +2000,7 @@ __global__ void __launch_bounds__(256, 2) k_mx_resid16(const MixCoef* __restrict
         // the full basis, for the Neumann step's edge sums
         const int i = threadIdx.x >> 4, k = threadIdx.x & 15;
         const float v = c_mxV16[(i < 8 ? i : 15 - i) * 16 + k];
-        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;
-        __syncthreads();
+        Vs[i * 17 + k] = (i >= 8 && (k & 1)) ? -v : v;  // read after the body's block barrier
     }
     const int tid = threadIdx.x, slot = tid >> 4, t = tid & 15;
     const int item = blockIdx.x * 16 + slot;  // L * B < 2^31 (the launchers check)
