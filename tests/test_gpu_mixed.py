@@ -334,12 +334,16 @@ def _set_tc(hps, on):
     check(load().ef_hps_set_option(hps.handle, b"tensor-cores", int(on)))
 
 
-@pytest.mark.parametrize("kind,n,B", [(("uniform", 4), 16, 5), (("uniform", 5), 16, 40), (("uniform", 3), 32, 8)])
+@pytest.mark.parametrize("kind,n,B", [(("uniform", 4), 16, 5), (("uniform", 5), 16, 40), (("uniform", 3), 32, 8),
+                                     (("adaptive", lambda x, y: (x - 0.2) ** 2 + (y + 0.3) ** 2 < 0.1, 0, 5), 16, 6),
+                                     (("uniform", 1), 16, 3)])
 def test_tensor_core_gemms_match_cuda_core_gemms(ef, kind, n, B):
     """The tcgen05 node GEMMs (three-way bf16 split of the FP32 operators and requests, six tensor
     products, FP32 accumulation in TMEM) give an FP32 pass as accurate as the CUDA-core FP32 GEMMs, and
     one FP64 sweep reaches the FP64 HPS solution to 1e-10; ragged request counts (B = 5, not a
-    multiple of 4; B = 40, two request blocks of 32) included."""
+    multiple of 4; B = 40, two request blocks of 32) included, and node groups whose operator rows
+    end inside a 128-row tile of the tiled bf16 planes (odd node counts on the adaptive tree; the
+    single 64-row W and DOWN operators of a level-1 tree)."""
     mesh, hps = make(ef, kind, n, (-1.0, 1.0, -1.0, 1.0))
     F, A, R = requests(hps, mesh, B, 41)
     ref = fp64_solutions(hps, F, A, R)
