@@ -205,11 +205,20 @@ __device__ __forceinline__ bool tc_wait(unsigned long long* bar, unsigned parity
 }
 // one contiguous block of global memory into shared memory (bulk copy engine), completing on `bar`;
 // both addresses 16-byte aligned, bytes a multiple of 16
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar,
+                                          unsigned long long policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+// L2 policy of the operator planes: each byte is read once per pass, so its lines go first and the
+// right-hand sides that the tiles of a node share stay in L2
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
 }
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
@@ -462,6 +471,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             int issued = 0;
             bool ok = true;
             const long long pstride = (long long)ntiles * nkc * (kTM * kTK);  // elements per plane
+            const unsigned long long pol = l2_evict_first();
             for (int u = 0; u < nunits && ok; ++u) {
                 const long long blk0 = (long long)tile_of(u) * nkc + cbase;
                 for (int c = 0; c < cpu && ok; ++c) {
@@ -470,7 +480,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     unsigned char* sa = base + size_t(st) * SB;
                     mbar_expect_tx(&a_full[st], 3u * kPlaneA);
                     const __nv_bfloat16* src = A3 + (blk0 + c) * (kTM * kTK);
-                    for (int p = 0; p < 3; ++p) bulk_load(sa + p * kPlaneA, src + p * pstride, kPlaneA, &a_full[st]);
+                    for (int p = 0; p < 3; ++p)
+                        bulk_load(sa + p * kPlaneA, src + p * pstride, kPlaneA, &a_full[st], pol);
                     ++issued;
                     if (++st == NS) { st = 0; ph ^= 1u; }
                 }
