@@ -180,7 +180,8 @@ __global__ void __launch_bounds__(128, KIND == MX_W ? 5 : 4) k_mx_gemm(const __g
         const int c = cbase + iss_ch;
         ++iss_ch;
         if (tid == 0)
-            tma_load_tile(&tmA, &full[st], As0 + st * astage, c * kKC, t.item * rows_item + t.row0, tile_bytes);
+            tma_load_tile(&tmA, &full[st], As0 + st * astage, c * kKC, t.item * rows_item + t.row0, tile_bytes,
+                          l2_evict_first());
         const int k0 = c * kKC;
         if (vecx) {
             for (int e = tid; e < kKC * TXN; e += nt) {

@@ -100,15 +100,23 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 // error word set).  Off in normal operation.
 static __device__ int g_mx_inject_timeout = 0;
 
-// one TMA tile (32 columns x rows) of A into shared memory, completing on `bar`
+// L2 policy for operator streams: each operator byte is read once per pass, so its lines go first
+// and the right-hand sides that several tiles of a node share stay in L2
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
+}
+
+// one TMA tile (32 columns x rows) of A into shared memory, completing on `bar`, with L2 policy `pol`
 __device__ __forceinline__ void tma_load_tile(const CUtensorMap* tm, unsigned long long* bar, float* dst, int x,
-                                              int y, unsigned bytes) {
+                                              int y, unsigned bytes, unsigned long long pol) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
-            "r"(smem_u32(dst)),
-        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3}], "
+        "[%4], %5;\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(pol)
         : "memory");
 }
 

@@ -213,13 +213,7 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
         "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
         : "memory");
 }
-// L2 policy of the operator planes: each byte is read once per pass, so its lines go first and the
-// right-hand sides that the tiles of a node share stay in L2
-__device__ __forceinline__ unsigned long long l2_evict_first() {
-    unsigned long long p;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
-    return p;
-}
+
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
